@@ -1,0 +1,150 @@
+"""ctypes binding of ``libfftso3_gb300.so`` (the C ABI in include/fftso3_gb300.h).
+
+The shared library is the only compute path: if it is missing this module
+raises instead of falling back to anything else.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfftso3_gb300.so")
+
+# constants mirrored from include/fftso3_gb300.h
+SUCCESS = 0
+ERR_INVALID_ARG = 1
+ERR_CUDA = 2
+ERR_OOM = 3
+ERR_UNSUPPORTED = 4
+ERR_NO_DEVICE = 5
+
+SO3_COMPLEX = 0
+SO3_REAL = 1
+S2_COMPLEX = 2
+S2_REAL = 3
+
+PREC_FP64 = 0
+PREC_TC_BF16X3 = 1
+
+RECURSION_REFERENCE = 0
+RECURSION_STABLE = 1
+
+FLAG_REFINE = 0x1
+
+PRECISIONS = {"fp64": PREC_FP64, "tc_bf16x3": PREC_TC_BF16X3}
+RECURSIONS = {"reference": RECURSION_REFERENCE, "stable": RECURSION_STABLE}
+
+# every symbol the header declares: name -> (restype, argtypes)
+_vp = ctypes.c_void_p
+_i = ctypes.c_int
+_ll = ctypes.c_longlong
+_d = ctypes.c_double
+_dp = ctypes.POINTER(ctypes.c_double)
+SIGNATURES = {
+    "fftso3_last_error_string": (ctypes.c_char_p, []),
+    "fftso3_version": (_i, []),
+    "fftso3_grid_elems": (_ll, [_i, _i]),
+    "fftso3_coeff_elems": (_ll, [_i, _i]),
+    "fftso3_weights": (_i, [_i, _i, _dp]),
+    "fftso3_plan_create": (_i, [ctypes.POINTER(_vp), _i, _i, _i, _i, _i, ctypes.c_uint]),
+    "fftso3_plan_destroy": (_i, [_vp]),
+    "fftso3_plan_device_bytes": (_ll, [_vp]),
+    "fftso3_forward": (_i, [_vp, _vp, _vp, _vp]),
+    "fftso3_inverse": (_i, [_vp, _vp, _vp, _vp]),
+    "fftso3_forward_host": (_i, [_vp, _vp, _vp, _vp]),
+    "fftso3_inverse_host": (_i, [_vp, _vp, _vp, _vp]),
+    "fftso3_inverse_points": (_i, [_vp, _vp, _i, _dp, _i, _vp, _vp]),
+    "fftso3_wigner_d": (_i, [_d, _i, _i, _dp]),
+}
+
+_lib = None
+
+
+class FFTSO3Error(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"fftso3 error {code}: {msg}")
+        self.code = code
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: build the CUDA library first "
+                "(python -m fftso3_gb300.build, or __graft_entry__.build())"
+            )
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(rc: int) -> None:
+    if rc != SUCCESS:
+        msg = lib().fftso3_last_error_string().decode(errors="replace")
+        raise FFTSO3Error(rc, msg)
+
+
+class Plan:
+    """Owns one ``fftso3_plan`` (tables and workspace on the current device)."""
+
+    def __init__(self, kind: int, l_max: int, batch: int = 1, precision: str | int = "fp64",
+                 recursion: str | int = "reference", flags: int = 0):
+        self.kind = kind
+        self.l_max = int(l_max)
+        self.batch = int(batch)
+        self.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        self.recursion = RECURSIONS[recursion] if isinstance(recursion, str) else int(recursion)
+        self.flags = int(flags)
+        h = _vp()
+        check(lib().fftso3_plan_create(ctypes.byref(h), kind, self.l_max, self.batch, self.precision,
+                                       self.recursion, ctypes.c_uint(self.flags)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def grid_elems(self) -> int:
+        return int(lib().fftso3_grid_elems(self.kind, self.l_max))
+
+    @property
+    def coeff_elems(self) -> int:
+        return int(lib().fftso3_coeff_elems(self.kind, self.l_max))
+
+    @property
+    def device_bytes(self) -> int:
+        return int(lib().fftso3_plan_device_bytes(self._h))
+
+    def forward(self, grid_ptr: int, coeff_ptr: int, stream: int = 0) -> None:
+        check(lib().fftso3_forward(self._h, _vp(grid_ptr), _vp(coeff_ptr), _vp(stream)))
+
+    def inverse(self, coeff_ptr: int, grid_ptr: int, stream: int = 0) -> None:
+        check(lib().fftso3_inverse(self._h, _vp(coeff_ptr), _vp(grid_ptr), _vp(stream)))
+
+    def forward_host(self, grid_ptr: int, coeff_ptr: int, stream: int = 0) -> None:
+        check(lib().fftso3_forward_host(self._h, _vp(grid_ptr), _vp(coeff_ptr), _vp(stream)))
+
+    def inverse_host(self, coeff_ptr: int, grid_ptr: int, stream: int = 0) -> None:
+        check(lib().fftso3_inverse_host(self._h, _vp(coeff_ptr), _vp(grid_ptr), _vp(stream)))
+
+    def inverse_points(self, coeff_ptr: int, index: int, pts, n: int, out_ptr: int, stream: int = 0) -> None:
+        check(lib().fftso3_inverse_points(self._h, _vp(coeff_ptr), int(index), pts, int(n), _vp(out_ptr),
+                                          _vp(stream)))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and _lib is not None:
+            _lib.fftso3_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

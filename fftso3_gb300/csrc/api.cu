@@ -1,0 +1,583 @@
+// C ABI of the GB300 SO(3) / S^2 transform library (declared in include/fftso3_gb300.h).
+//
+// Host side of the plan: argument checks, the FP64 host precompute that the
+// reference does inline (quadrature weights fdcl_FFTSO3.cpp:236-256 /
+// fdcl_FFTS2.cpp:102-123, grid angles :578-591, recursion seeds :135-147),
+// device tables, workspace, and the launch sequence of each transform.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/fftso3_gb300.h"
+#include "common.cuh"
+#include "contract.cuh"
+#include "fft.cuh"
+#include "tables.cuh"
+#include "tc.cuh"
+
+using namespace fftso3;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg)
+{
+    g_err = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what)
+{
+    g_err = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? FFTSO3_ERR_OOM : FFTSO3_ERR_CUDA;
+}
+
+#define CK(call)                                                   \
+    do {                                                           \
+        cudaError_t _e = (call);                                   \
+        if (_e != cudaSuccess) return cuda_fail(_e, #call);        \
+    } while (0)
+
+bool valid_kind(int k) { return k >= FFTSO3_SO3_COMPLEX && k <= FFTSO3_S2_REAL; }
+bool is_so3(int k) { return k == FFTSO3_SO3_COMPLEX || k == FFTSO3_SO3_REAL; }
+bool is_real_kind(int k) { return k == FFTSO3_SO3_REAL || k == FFTSO3_S2_REAL; }
+
+// fdcl_FFTSO3.cpp:578-591 (beta_k, identical expression for theta_k in fdcl_FFTS2.cpp:292-296)
+double beta_k(int B, int k) { return ((double)(2 * k + 1)) * M_PI / 4. / ((double)B); }
+
+void host_weights(int kind, int l_max, double* weight)
+{
+    int B = l_max + 1;
+    double factor = M_PI / ((double)(4 * B));
+    for (int j = 0; j < 2 * B; j++) {
+        double sum = 0.0;
+        for (int k = 0; k < B; k++)
+            sum += 1. / ((double)(2 * k + 1)) * sin((double)((2 * j + 1) * (2 * k + 1)) * factor);
+        if (is_so3(kind))
+            sum *= 1. / ((double)4 * B * B * B) * sin((double)(2 * j + 1) * factor);
+        else
+            sum *= 2. * M_PI / ((double)B * B) * sin((double)(2 * j + 1) * factor);
+        weight[j] = sum;
+    }
+}
+
+WignerSeeds make_seeds(double beta)
+{
+    WignerSeeds s;
+    s.cb = cos(beta);
+    s.sb = sin(beta);
+    double sb2 = sin(beta / 2.), cb2 = cos(beta / 2.);
+    s.tb2 = tan(beta / 2.);
+    s.d111 = pow(cb2, 2.);
+    s.d11m1 = pow(sb2, 2.);
+    s.d110 = -1. / sqrt(2.) * s.sb;
+    s.lc2 = log(fabs(cb2));
+    s.ls2 = log(fabs(sb2));
+    s.c2 = cb2;
+    s.s2 = sb2;
+    return s;
+}
+
+std::vector<double> log_factorials(int n)
+{
+    std::vector<double> f(n + 1);
+    for (int i = 0; i <= n; ++i) f[i] = lgamma((double)i + 1.0);
+    return f;
+}
+
+}  // namespace
+
+struct fftso3_plan {
+    int kind = 0, L = 0, B = 0, N = 0, batch = 0, precision = 0, recursion = 0;
+    unsigned flags = 0;
+    int device = 0;
+    bool so3 = true, real = false, fp64 = true;
+    long long grid_elems = 0, coeff_elems = 0;  // per function
+    FFTFactors fac;
+    std::vector<double> weights;
+    double* d_tw = nullptr;        // N double2
+    double* d_w = nullptr;         // N
+    long long* d_goff = nullptr;   // group offsets into the table
+    double* d_table = nullptr;
+    long long table_elems = 0;
+    double* d_lfact = nullptr;
+    void* d_work = nullptr;        // FFT workspace: batch * grid_elems complex
+    void* d_fc = nullptr;          // complex coefficients of the real kinds
+    void* d_io_grid = nullptr;     // staging for the *_host calls
+    void* d_io_coeff = nullptr;
+    long long bytes = 0;
+    TCState* tc = nullptr;         // tensor-core contraction state
+};
+
+namespace {
+
+int plan_alloc(fftso3_plan* p, void** ptr, size_t bytes)
+{
+    cudaError_t e = cudaMalloc(ptr, bytes);
+    if (e != cudaSuccess) {
+        *ptr = nullptr;
+        return cuda_fail(e, "cudaMalloc");
+    }
+    p->bytes += (long long)bytes;
+    return FFTSO3_SUCCESS;
+}
+
+void plan_free(fftso3_plan* p)
+{
+    void* ptrs[] = {p->d_tw, p->d_w, p->d_goff, p->d_table, p->d_lfact, p->d_work, p->d_fc, p->d_io_grid,
+                    p->d_io_coeff};
+    for (void* q : ptrs)
+        if (q) cudaFree(q);
+    if (p->tc) tc_destroy(p->tc);
+}
+
+size_t cbytes(const fftso3_plan* p) { return p->fp64 ? 16 : 8; }  // complex element bytes
+size_t rbytes(const fftso3_plan* p) { return p->fp64 ? 8 : 4; }   // real element bytes
+
+FFTLaunch fft_rows(const fftso3_plan* p, const void* in, void* out, long long nlines, bool real_in, bool real_out)
+{
+    FFTLaunch L;
+    L.in = in;
+    L.out = out;
+    L.fac = p->fac;
+    L.nlines = nlines;
+    int N = p->N;
+    int lpb = 1;
+    size_t budget = 200 * 1024;
+    while (lpb < 4 && fft_smem_bytes(N, lpb * 2, p->fp64) <= budget) lpb *= 2;
+    L.lpb = lpb;
+    L.inner = 1;
+    L.ostride = N;
+    L.istride = 0;
+    L.es = 1;
+    L.tw = p->d_tw;
+    L.fp64 = p->fp64;
+    L.real_in = real_in;
+    L.real_out = real_out;
+    L.lines_fastest = false;
+    return L;
+}
+
+// FFT along j1 of [outer][N][N] (lines (outer, j2), element stride N)
+FFTLaunch fft_cols(const fftso3_plan* p, const void* in, void* out, long long nouter, bool real_out)
+{
+    FFTLaunch L;
+    L.in = in;
+    L.out = out;
+    L.fac = p->fac;
+    int N = p->N;
+    L.nlines = nouter * N;
+    int lpb = 16;
+    while (lpb > 1 && fft_smem_bytes(N, lpb, p->fp64) > 200 * 1024) lpb /= 2;
+    L.lpb = lpb;
+    L.inner = N;
+    L.ostride = (long long)N * N;
+    L.istride = 1;
+    L.es = N;
+    L.tw = p->d_tw;
+    L.fp64 = p->fp64;
+    L.real_in = false;
+    L.real_out = real_out;
+    L.lines_fastest = true;
+    return L;
+}
+
+int run_forward(fftso3_plan* p, const void* grid, void* coeffs, cudaStream_t st)
+{
+    const int N = p->N, L = p->L, b = p->batch;
+    if (p->precision == FFTSO3_PREC_TC_BF16X3) return tc_forward(p->tc, grid, coeffs, st, g_err);
+    if (p->so3) {
+        CK(launch_fft_lines(fft_rows(p, grid, p->d_work, (long long)b * N * N, p->real, false), st));
+        CK(launch_fft_lines(fft_cols(p, p->d_work, p->d_work, (long long)b * N, false), st));
+        double2* Fout = p->real ? (double2*)p->d_fc : (double2*)coeffs;
+        CK(launch_so3_fwd_fp64(p->d_table, p->d_goff, (const double2*)p->d_work, p->d_w, Fout, L, N, b, st));
+        if (p->real) CK(launch_so3_c2r(p->d_fc, coeffs, true, L, b, st));
+    } else {
+        CK(launch_fft_lines(fft_rows(p, grid, p->d_work, (long long)b * N, p->real, false), st));
+        double2* Fout = p->real ? (double2*)p->d_fc : (double2*)coeffs;
+        CK(launch_s2_fwd_fp64(p->d_table, p->d_goff, (const double2*)p->d_work, p->d_w, Fout, L, N, b, p->real, st));
+        if (p->real) CK(launch_s2_c2r(p->d_fc, coeffs, true, L, b, st));
+    }
+    return FFTSO3_SUCCESS;
+}
+
+int run_inverse(fftso3_plan* p, const void* coeffs, void* grid, cudaStream_t st)
+{
+    const int N = p->N, L = p->L, b = p->batch;
+    if (p->precision == FFTSO3_PREC_TC_BF16X3) return tc_inverse(p->tc, coeffs, grid, st, g_err);
+    if (p->so3) {
+        const double2* Fin = (const double2*)coeffs;
+        if (p->real) {
+            CK(launch_so3_r2c(coeffs, p->d_fc, true, L, b, st));
+            Fin = (const double2*)p->d_fc;
+        }
+        CK(launch_zero_nyquist_so3(p->d_work, true, N, (long long)b * N, st));
+        CK(launch_so3_inv_fp64(p->d_table, p->d_goff, Fin, (double2*)p->d_work, L, N, b, st));
+        CK(launch_fft_lines(fft_rows(p, p->d_work, p->d_work, (long long)b * N * N, false, false), st));
+        CK(launch_fft_lines(fft_cols(p, p->d_work, grid, (long long)b * N, p->real), st));
+    } else {
+        const double2* Fin = (const double2*)coeffs;
+        if (p->real) {
+            CK(launch_s2_r2c(coeffs, p->d_fc, true, L, b, st));
+            Fin = (const double2*)p->d_fc;
+        }
+        CK(launch_zero_nyquist_s2(p->d_work, true, N, (long long)b * N, st));
+        CK(launch_s2_inv_fp64(p->d_table, p->d_goff, Fin, (double2*)p->d_work, L, N, b, st));
+        CK(launch_fft_lines(fft_rows(p, p->d_work, grid, (long long)b * N, false, p->real), st));
+    }
+    return FFTSO3_SUCCESS;
+}
+
+int check_plan(const fftso3_plan* p)
+{
+    if (!p) return fail(FFTSO3_ERR_INVALID_ARG, "plan is NULL");
+    int dev = -1;
+    cudaGetDevice(&dev);
+    if (dev != p->device) {
+        cudaError_t e = cudaSetDevice(p->device);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    }
+    return FFTSO3_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* fftso3_last_error_string(void) { return g_err.c_str(); }
+
+int fftso3_version(void) { return 100; }
+
+long long fftso3_grid_elems(int kind, int l_max)
+{
+    if (!valid_kind(kind) || l_max < 0) return -1;
+    long long N = 2LL * (l_max + 1);
+    return is_so3(kind) ? N * N * N : N * N;
+}
+
+long long fftso3_coeff_elems(int kind, int l_max)
+{
+    if (!valid_kind(kind) || l_max < 0) return -1;
+    long long B = l_max + 1;
+    return is_so3(kind) ? so3_off((int)B) : B * B;
+}
+
+int fftso3_weights(int kind, int l_max, double* weights_out)
+{
+    if (!valid_kind(kind)) return fail(FFTSO3_ERR_INVALID_ARG, "unknown transform kind");
+    if (l_max < 0) return fail(FFTSO3_ERR_INVALID_ARG, "l_max must be >= 0");
+    if (!weights_out) return fail(FFTSO3_ERR_INVALID_ARG, "weights_out is NULL");
+    host_weights(kind, l_max, weights_out);
+    return FFTSO3_SUCCESS;
+}
+
+int fftso3_plan_create(fftso3_plan** out, int kind, int l_max, int batch, int precision, int recursion,
+                       unsigned flags)
+{
+    if (!out) return fail(FFTSO3_ERR_INVALID_ARG, "plan output pointer is NULL");
+    *out = nullptr;
+    if (!valid_kind(kind)) return fail(FFTSO3_ERR_INVALID_ARG, "unknown transform kind");
+    if (l_max < 0) return fail(FFTSO3_ERR_INVALID_ARG, "l_max must be >= 0");
+    if (batch < 1) return fail(FFTSO3_ERR_INVALID_ARG, "batch must be >= 1");
+    if (precision != FFTSO3_PREC_FP64 && precision != FFTSO3_PREC_TC_BF16X3)
+        return fail(FFTSO3_ERR_INVALID_ARG, "unknown precision");
+    if (recursion != FFTSO3_RECURSION_REFERENCE && recursion != FFTSO3_RECURSION_STABLE)
+        return fail(FFTSO3_ERR_INVALID_ARG, "unknown recursion mode");
+    if ((flags & ~FFTSO3_FLAG_REFINE) != 0) return fail(FFTSO3_ERR_INVALID_ARG, "unknown flag bits");
+    if (is_so3(kind) && l_max > 511) return fail(FFTSO3_ERR_UNSUPPORTED, "SO(3) l_max above 511 is not supported");
+    if (!is_so3(kind) && l_max > 2047) return fail(FFTSO3_ERR_UNSUPPORTED, "S^2 l_max above 2047 is not supported");
+    if (precision == FFTSO3_PREC_TC_BF16X3 && kind != FFTSO3_SO3_COMPLEX)
+        return fail(FFTSO3_ERR_UNSUPPORTED, "tensor-core precision is implemented for FFTSO3_SO3_COMPLEX");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(FFTSO3_ERR_NO_DEVICE, "no CUDA device available");
+
+    fftso3_plan* p = new fftso3_plan();
+    p->kind = kind;
+    p->L = l_max;
+    p->B = l_max + 1;
+    p->N = 2 * p->B;
+    p->batch = batch;
+    p->precision = precision;
+    p->recursion = recursion;
+    p->flags = flags;
+    p->so3 = is_so3(kind);
+    p->real = is_real_kind(kind);
+    p->fp64 = (precision == FFTSO3_PREC_FP64);
+    p->grid_elems = fftso3_grid_elems(kind, l_max);
+    p->coeff_elems = fftso3_coeff_elems(kind, l_max);
+    cudaGetDevice(&p->device);
+    make_fft_factors(p->N, p->fac);
+
+    const int B = p->B, N = p->N, L = p->L;
+    int rc;
+    auto bail = [&](int code) {
+        plan_free(p);
+        delete p;
+        return code;
+    };
+
+    // twiddles and weights
+    std::vector<double> tw(2 * N);
+    for (int i = 0; i < N; ++i) {
+        double a = -2. * M_PI * (double)i / (double)N;
+        tw[2 * i] = cos(a);
+        tw[2 * i + 1] = sin(a);
+    }
+    p->weights.resize(N);
+    host_weights(kind, l_max, p->weights.data());
+    if ((rc = plan_alloc(p, (void**)&p->d_tw, sizeof(double) * 2 * N))) return bail(rc);
+    if ((rc = plan_alloc(p, (void**)&p->d_w, sizeof(double) * N))) return bail(rc);
+    if (cudaMemcpy(p->d_tw, tw.data(), sizeof(double) * 2 * N, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(p->d_w, p->weights.data(), sizeof(double) * N, cudaMemcpyHostToDevice) != cudaSuccess)
+        return bail(cuda_fail(cudaGetLastError(), "upload constants"));
+
+    // tables
+    std::vector<long long> goff;
+    if (p->so3) {
+        int ng = B * B;
+        goff.resize(ng + 1);
+        long long o = 0;
+        for (int g = 0; g < ng; ++g) {
+            int m0, n0;
+            group_mn(g, m0, n0);
+            goff[g] = o;
+            o += (long long)(B - m0) * N;
+        }
+        goff[ng] = o;
+        p->table_elems = o;
+    } else {
+        goff.resize(B + 1);
+        long long o = 0;
+        for (int m = 0; m < B; ++m) {
+            goff[m] = o;
+            o += (long long)(B - m) * N;
+        }
+        goff[B] = o;
+        p->table_elems = o;
+    }
+    if ((rc = plan_alloc(p, (void**)&p->d_goff, sizeof(long long) * goff.size()))) return bail(rc);
+    if ((rc = plan_alloc(p, (void**)&p->d_table, sizeof(double) * p->table_elems))) return bail(rc);
+    if (cudaMemcpy(p->d_goff, goff.data(), sizeof(long long) * goff.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+        return bail(cuda_fail(cudaGetLastError(), "upload offsets"));
+    std::vector<double> lf = log_factorials(2 * L + 2);
+    if ((rc = plan_alloc(p, (void**)&p->d_lfact, sizeof(double) * lf.size()))) return bail(rc);
+    if (cudaMemcpy(p->d_lfact, lf.data(), sizeof(double) * lf.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+        return bail(cuda_fail(cudaGetLastError(), "upload log factorials"));
+    {
+        void* d_tmp = nullptr;
+        cudaError_t e;
+        if (p->so3) {
+            std::vector<WignerSeeds> seeds(N);
+            for (int k = 0; k < N; ++k) seeds[k] = make_seeds(beta_k(B, k));
+            if ((e = cudaMalloc(&d_tmp, sizeof(WignerSeeds) * N)) != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc"));
+            cudaMemcpy(d_tmp, seeds.data(), sizeof(WignerSeeds) * N, cudaMemcpyHostToDevice);
+            e = launch_wigner_table(p->d_table, p->d_goff, (const WignerSeeds*)d_tmp, p->d_lfact, L, N, B * B,
+                                    recursion == FFTSO3_RECURSION_STABLE, 0);
+        } else {
+            std::vector<double> xs(N);
+            for (int k = 0; k < N; ++k) xs[k] = cos(beta_k(B, k));
+            if ((e = cudaMalloc(&d_tmp, sizeof(double) * N)) != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc"));
+            cudaMemcpy(d_tmp, xs.data(), sizeof(double) * N, cudaMemcpyHostToDevice);
+            e = launch_legendre_table(p->d_table, p->d_goff, (const double*)d_tmp, L, N, 0);
+        }
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+        cudaFree(d_tmp);
+        if (e != cudaSuccess) return bail(cuda_fail(e, "table generation"));
+    }
+
+    if (p->fp64) {
+        if ((rc = plan_alloc(p, &p->d_work, cbytes(p) * (size_t)batch * p->grid_elems))) return bail(rc);
+        if (p->real)
+            if ((rc = plan_alloc(p, &p->d_fc, 16 * (size_t)batch * p->coeff_elems))) return bail(rc);
+    } else {
+        std::string err;
+        rc = tc_create(&p->tc, p->L, p->N, batch, p->d_table, goff, p->table_elems, p->d_tw, p->d_w, p->fac,
+                       (flags & FFTSO3_FLAG_REFINE) != 0, err);
+        if (rc) {
+            g_err = err;
+            return bail(rc);
+        }
+        p->bytes += tc_device_bytes(p->tc);
+    }
+    *out = p;
+    return FFTSO3_SUCCESS;
+}
+
+int fftso3_plan_destroy(fftso3_plan* plan)
+{
+    if (!plan) return fail(FFTSO3_ERR_INVALID_ARG, "plan is NULL");
+    int dev = -1;
+    const int pdev = plan->device;
+    cudaGetDevice(&dev);
+    if (dev != pdev) cudaSetDevice(pdev);
+    plan_free(plan);
+    delete plan;
+    if (dev >= 0 && dev != pdev) cudaSetDevice(dev);
+    return FFTSO3_SUCCESS;
+}
+
+long long fftso3_plan_device_bytes(const fftso3_plan* plan) { return plan ? plan->bytes : -1; }
+
+int fftso3_forward(fftso3_plan* plan, const void* grid, void* coeffs, void* stream)
+{
+    int rc = check_plan(plan);
+    if (rc) return rc;
+    if (!grid || !coeffs) return fail(FFTSO3_ERR_INVALID_ARG, "grid/coeffs pointer is NULL");
+    return run_forward(plan, grid, coeffs, (cudaStream_t)stream);
+}
+
+int fftso3_inverse(fftso3_plan* plan, const void* coeffs, void* grid, void* stream)
+{
+    int rc = check_plan(plan);
+    if (rc) return rc;
+    if (!grid || !coeffs) return fail(FFTSO3_ERR_INVALID_ARG, "grid/coeffs pointer is NULL");
+    return run_inverse(plan, coeffs, grid, (cudaStream_t)stream);
+}
+
+static size_t grid_bytes(const fftso3_plan* p)
+{
+    return (size_t)p->batch * p->grid_elems * (p->real ? rbytes(p) : cbytes(p));
+}
+static size_t coeff_bytes(const fftso3_plan* p)
+{
+    return (size_t)p->batch * p->coeff_elems * (p->real ? rbytes(p) : cbytes(p));
+}
+
+static int ensure_io(fftso3_plan* p)
+{
+    int rc;
+    if (!p->d_io_grid && (rc = plan_alloc(p, &p->d_io_grid, grid_bytes(p)))) return rc;
+    if (!p->d_io_coeff && (rc = plan_alloc(p, &p->d_io_coeff, coeff_bytes(p)))) return rc;
+    return FFTSO3_SUCCESS;
+}
+
+int fftso3_forward_host(fftso3_plan* plan, const void* grid_host, void* coeffs_host, void* stream)
+{
+    int rc = check_plan(plan);
+    if (rc) return rc;
+    if (!grid_host || !coeffs_host) return fail(FFTSO3_ERR_INVALID_ARG, "grid/coeffs pointer is NULL");
+    if ((rc = ensure_io(plan))) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    CK(cudaMemcpyAsync(plan->d_io_grid, grid_host, grid_bytes(plan), cudaMemcpyHostToDevice, st));
+    if ((rc = run_forward(plan, plan->d_io_grid, plan->d_io_coeff, st))) return rc;
+    CK(cudaMemcpyAsync(coeffs_host, plan->d_io_coeff, coeff_bytes(plan), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return FFTSO3_SUCCESS;
+}
+
+int fftso3_inverse_host(fftso3_plan* plan, const void* coeffs_host, void* grid_host, void* stream)
+{
+    int rc = check_plan(plan);
+    if (rc) return rc;
+    if (!grid_host || !coeffs_host) return fail(FFTSO3_ERR_INVALID_ARG, "grid/coeffs pointer is NULL");
+    if ((rc = ensure_io(plan))) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    CK(cudaMemcpyAsync(plan->d_io_coeff, coeffs_host, coeff_bytes(plan), cudaMemcpyHostToDevice, st));
+    if ((rc = run_inverse(plan, plan->d_io_coeff, plan->d_io_grid, st))) return rc;
+    CK(cudaMemcpyAsync(grid_host, plan->d_io_grid, grid_bytes(plan), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return FFTSO3_SUCCESS;
+}
+
+int fftso3_inverse_points(fftso3_plan* plan, const void* coeffs, int index, const double* pts, int n, void* out,
+                          void* stream)
+{
+    int rc = check_plan(plan);
+    if (rc) return rc;
+    if (!coeffs || !pts || !out) return fail(FFTSO3_ERR_INVALID_ARG, "NULL pointer argument");
+    if (index < 0 || index >= plan->batch) return fail(FFTSO3_ERR_INVALID_ARG, "index outside the plan's batch");
+    if (n < 0) return fail(FFTSO3_ERR_INVALID_ARG, "n must be >= 0");
+    if (n == 0) return FFTSO3_SUCCESS;
+    if (!plan->fp64) return fail(FFTSO3_ERR_UNSUPPORTED, "point evaluation needs an FFTSO3_PREC_FP64 plan");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int L = plan->L;
+    const long long C = plan->coeff_elems;
+    const int dim = plan->so3 ? 3 : 2;
+    // complex coefficients of the selected function
+    void* d_c = nullptr;
+    void* d_pts = nullptr;
+    void* d_seed = nullptr;
+    void* d_out = nullptr;
+    auto cleanup = [&]() {
+        if (d_c) cudaFree(d_c);
+        if (d_pts) cudaFree(d_pts);
+        if (d_seed) cudaFree(d_seed);
+        if (d_out) cudaFree(d_out);
+    };
+    cudaError_t e;
+    const double2* Fc;
+    if (plan->real) {
+        if ((e = cudaMalloc(&d_c, 16 * C)) != cudaSuccess) { cleanup(); return cuda_fail(e, "cudaMalloc"); }
+        const double* src = (const double*)coeffs + (long long)index * C;
+        e = plan->so3 ? launch_so3_r2c(src, d_c, true, L, 1, st) : launch_s2_r2c(src, d_c, true, L, 1, st);
+        if (e != cudaSuccess) { cleanup(); return cuda_fail(e, "real-to-complex coefficients"); }
+        Fc = (const double2*)d_c;
+    } else {
+        Fc = (const double2*)coeffs + (long long)index * C;
+    }
+    if ((e = cudaMalloc(&d_pts, sizeof(double) * dim * n)) != cudaSuccess) { cleanup(); return cuda_fail(e, "cudaMalloc"); }
+    if ((e = cudaMalloc(&d_out, sizeof(double2) * n)) != cudaSuccess) { cleanup(); return cuda_fail(e, "cudaMalloc"); }
+    cudaMemcpyAsync(d_pts, pts, sizeof(double) * dim * n, cudaMemcpyHostToDevice, st);
+    if (plan->so3) {
+        std::vector<WignerSeeds> seeds(n);
+        for (int i = 0; i < n; ++i) seeds[i] = make_seeds(pts[3 * i + 1]);
+        if ((e = cudaMalloc(&d_seed, sizeof(WignerSeeds) * n)) != cudaSuccess) { cleanup(); return cuda_fail(e, "cudaMalloc"); }
+        cudaMemcpyAsync(d_seed, seeds.data(), sizeof(WignerSeeds) * n, cudaMemcpyHostToDevice, st);
+        e = launch_so3_points(Fc, (const WignerSeeds*)d_seed, (const double*)d_pts, plan->d_lfact, L,
+                              plan->recursion == FFTSO3_RECURSION_STABLE, n, (double2*)d_out, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // seeds vector must outlive the copy
+    } else {
+        std::vector<double> xs(n);
+        for (int i = 0; i < n; ++i) xs[i] = cos(pts[2 * i]);
+        if ((e = cudaMalloc(&d_seed, sizeof(double) * n)) != cudaSuccess) { cleanup(); return cuda_fail(e, "cudaMalloc"); }
+        cudaMemcpyAsync(d_seed, xs.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st);
+        e = launch_s2_points(Fc, (const double*)d_seed, (const double*)d_pts, L, n, (double2*)d_out, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    }
+    if (e != cudaSuccess) { cleanup(); return cuda_fail(e, "point evaluation"); }
+    std::vector<double> tmp(2 * (size_t)n);
+    e = cudaMemcpy(tmp.data(), d_out, sizeof(double2) * n, cudaMemcpyDeviceToHost);
+    cleanup();
+    if (e != cudaSuccess) return cuda_fail(e, "copy points");
+    if (plan->real) {
+        for (int i = 0; i < n; ++i) ((double*)out)[i] = tmp[2 * i];
+    } else {
+        memcpy(out, tmp.data(), sizeof(double2) * n);
+    }
+    return FFTSO3_SUCCESS;
+}
+
+int fftso3_wigner_d(double beta, int l_max, int recursion, double* d_out_host)
+{
+    if (l_max < 0) return fail(FFTSO3_ERR_INVALID_ARG, "l_max must be >= 0");
+    if (!d_out_host) return fail(FFTSO3_ERR_INVALID_ARG, "output pointer is NULL");
+    if (recursion != FFTSO3_RECURSION_REFERENCE && recursion != FFTSO3_RECURSION_STABLE)
+        return fail(FFTSO3_ERR_INVALID_ARG, "unknown recursion mode");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(FFTSO3_ERR_NO_DEVICE, "no CUDA device available");
+    long long C = so3_off(l_max + 1);
+    WignerSeeds s = make_seeds(beta);
+    std::vector<double> lf = log_factorials(2 * l_max + 2);
+    void *d_s = nullptr, *d_lf = nullptr, *d_o = nullptr;
+    cudaError_t e = cudaMalloc(&d_s, sizeof(s));
+    if (e == cudaSuccess) e = cudaMalloc(&d_lf, sizeof(double) * lf.size());
+    if (e == cudaSuccess) e = cudaMalloc(&d_o, sizeof(double) * C);
+    if (e == cudaSuccess) e = cudaMemcpy(d_s, &s, sizeof(s), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_lf, lf.data(), sizeof(double) * lf.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = launch_wigner_full((const WignerSeeds*)d_s, (const double*)d_lf, l_max,
+                               recursion == FFTSO3_RECURSION_STABLE, (double*)d_o, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(d_out_host, d_o, sizeof(double) * C, cudaMemcpyDeviceToHost);
+    if (d_s) cudaFree(d_s);
+    if (d_lf) cudaFree(d_lf);
+    if (d_o) cudaFree(d_o);
+    if (e != cudaSuccess) return cuda_fail(e, "wigner_d");
+    return FFTSO3_SUCCESS;
+}
+
+}  // extern "C"

@@ -1,0 +1,23 @@
+// Beta-sum contraction launchers (see contract_fp64.cu, contract_tc.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace fftso3 {
+
+cudaError_t launch_so3_fwd_fp64(const double* table, const long long* goff, const double2* G, const double* w,
+                                double2* F, int L, int N, int batch, cudaStream_t st);
+cudaError_t launch_so3_inv_fp64(const double* table, const long long* goff, const double2* F, double2* H, int L,
+                                int N, int batch, cudaStream_t st);
+cudaError_t launch_zero_nyquist_so3(void* H, bool fp64, int N, long long nslices, cudaStream_t st);
+cudaError_t launch_so3_c2r(const void* Fc, void* Fr, bool fp64, int L, int batch, cudaStream_t st);
+cudaError_t launch_so3_r2c(const void* Fr, void* Fc, bool fp64, int L, int batch, cudaStream_t st);
+
+cudaError_t launch_s2_fwd_fp64(const double* table, const long long* moff, const double2* G, const double* w,
+                               double2* F, int L, int N, int batch, bool is_real, cudaStream_t st);
+cudaError_t launch_s2_inv_fp64(const double* table, const long long* moff, const double2* F, double2* H, int L,
+                               int N, int batch, cudaStream_t st);
+cudaError_t launch_zero_nyquist_s2(void* H, bool fp64, int N, long long nrows, cudaStream_t st);
+cudaError_t launch_s2_c2r(const void* Fc, void* Fr, bool fp64, int L, int batch, cudaStream_t st);
+cudaError_t launch_s2_r2c(const void* Fr, void* Fc, bool fp64, int L, int batch, cudaStream_t st);
+
+}  // namespace fftso3

@@ -1,0 +1,497 @@
+// FP64 beta-sum contractions (the plain method) and the coefficient-basis
+// conversions of the real transforms.
+//
+// SO(3) forward (fdcl_FFTSO3.cpp:704-740):
+//   F(l,m,n) = sum_k w_k d^l_mn(beta_k) G_k(-m mod N, -n mod N),
+// where G_k is the unscaled 2-D DFT of the beta_k slice.  One CTA per
+// (symmetry group, function): the group's <= 4 (m,n) pairs share one table
+// block d_g[l][k], so X[p][k] = w_k G_k(pair p) is staged in shared memory and
+// each warp walks one row l with its lanes over k (coalesced table reads),
+// finishing with a shuffle reduction.
+//
+// SO(3) inverse (grid form of fdcl_FFTSO3.cpp:498-531):
+//   H_k(m,n) = sum_l (2l+1) F(l,m,n) d^l_mn(beta_k), placed at bin
+//   (m mod N, n mod N) of slice k; a forward 2-D DFT of the slice then gives
+//   f(alpha_j1, beta_k, gamma_j2) = sum_mn H_k(m,n) e^{-i m alpha_j1} e^{-i n gamma_j2}.
+//   Threads over k (coalesced table reads), (2l+1) F staged in shared memory.
+//
+// S^2 is the same pattern with the Legendre table and groups m >= 0 serving
+// the pairs (m, -m) (fdcl_FFTS2.cpp:157-173 forward, :194-230 inverse).
+#include "common.cuh"
+#include "contract.cuh"
+
+namespace fftso3 {
+
+__device__ __forceinline__ int mod_n(int a, int N) { int r = a % N; return r < 0 ? r + N : r; }
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// ------------------------------------------------------------------ SO(3)
+
+template <int NT>
+__global__ void __launch_bounds__(NT) so3_fwd_fp64_kernel(const double* __restrict__ table,
+                                                          const long long* __restrict__ goff,
+                                                          const double2* __restrict__ G, const double* __restrict__ w,
+                                                          double2* __restrict__ F, int L, int N, long long gstride,
+                                                          long long cstride)
+{
+    extern __shared__ double2 X[];  // [4][N]
+    const int g = blockIdx.x, b = blockIdx.y;
+    int m0, n0;
+    group_mn(g, m0, n0);
+    const GroupPairs P = group_pairs(m0, n0);
+    const double2* Gb = G + (long long)b * gstride;
+    const long long NN = (long long)N * N;
+    for (int i = threadIdx.x; i < P.np * N; i += NT) {
+        int p = i / N, k = i - p * N;
+        int pi = mod_n(-P.m[p], N), qi = mod_n(-P.n[p], N);
+        double2 v = Gb[(long long)k * NN + (long long)pi * N + qi];
+        double wk = w[k];
+        X[p * N + k] = make_double2(wk * v.x, wk * v.y);
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const double* tg = table + goff[g];
+    double2* Fb = F + (long long)b * cstride;
+    for (int l = m0 + warp; l <= L; l += NT / 32) {
+        const double* drow = tg + (long long)(l - m0) * N;
+        double ar[4] = {0., 0., 0., 0.}, ai[4] = {0., 0., 0., 0.};
+        for (int k = lane; k < N; k += 32) {
+            double d = drow[k];
+#pragma unroll
+            for (int p = 0; p < 4; ++p)
+                if (p < P.np) {
+                    double2 x = X[p * N + k];
+                    ar[p] += d * x.x;
+                    ai[p] += d * x.y;
+                }
+        }
+#pragma unroll
+        for (int p = 0; p < 4; ++p)
+            if (p < P.np) {
+                double r = warp_sum(ar[p]), im = warp_sum(ai[p]);
+                if (lane == 0) Fb[so3_idx(l, P.m[p], P.n[p])] = make_double2(P.sign[p] * r, P.sign[p] * im);
+            }
+    }
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT) so3_inv_fp64_kernel(const double* __restrict__ table,
+                                                          const long long* __restrict__ goff,
+                                                          const double2* __restrict__ F, double2* __restrict__ H,
+                                                          int L, int N, long long gstride, long long cstride)
+{
+    extern __shared__ double2 Y[];  // [4][B]
+    const int g = blockIdx.x, b = blockIdx.y;
+    const int B = L + 1;
+    int m0, n0;
+    group_mn(g, m0, n0);
+    const GroupPairs P = group_pairs(m0, n0);
+    const int nl = B - m0;
+    const double2* Fb = F + (long long)b * cstride;
+    for (int i = threadIdx.x; i < P.np * nl; i += NT) {
+        int p = i / nl, l = m0 + (i - p * nl);
+        double2 c = Fb[so3_idx(l, P.m[p], P.n[p])];
+        double s = (double)(2 * l + 1) * P.sign[p];
+        Y[p * B + (l - m0)] = make_double2(s * c.x, s * c.y);
+    }
+    __syncthreads();
+    const double* tg = table + goff[g];
+    double2* Hb = H + (long long)b * gstride;
+    const long long NN = (long long)N * N;
+    for (int k = threadIdx.x; k < N; k += NT) {
+        double ar[4] = {0., 0., 0., 0.}, ai[4] = {0., 0., 0., 0.};
+        for (int j = 0; j < nl; ++j) {
+            double d = tg[(long long)j * N + k];
+#pragma unroll
+            for (int p = 0; p < 4; ++p)
+                if (p < P.np) {
+                    double2 y = Y[p * B + j];
+                    ar[p] += d * y.x;
+                    ai[p] += d * y.y;
+                }
+        }
+#pragma unroll
+        for (int p = 0; p < 4; ++p)
+            if (p < P.np) {
+                int pi = mod_n(P.m[p], N), qi = mod_n(P.n[p], N);
+                Hb[(long long)k * NN + (long long)pi * N + qi] = make_double2(ar[p], ai[p]);
+            }
+    }
+}
+
+// Zero the Nyquist row p = B and column q = B of every N x N slice (the bins
+// no (m, n) with |m|, |n| <= L maps to).
+template <typename C>
+__global__ void zero_nyquist_so3_kernel(C* __restrict__ H, int N, long long nslices)
+{
+    long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= nslices * 2 * N) return;
+    long long s = idx / (2 * N);
+    int r = (int)(idx % (2 * N));
+    int B = N / 2;
+    C z;
+    z.x = 0;
+    z.y = 0;
+    C* slice = H + s * N * N;
+    if (r < N)
+        slice[(long long)B * N + r] = z;
+    else
+        slice[(long long)(r - N) * N + B] = z;
+}
+
+// matrix2rsph T(l; a, c) (fdcl_FFTSO3.cpp:1107-1139), row a, column c.
+__device__ __forceinline__ double2 tmat(int a, int c)
+{
+    const double s = 1. / sqrt(2.);
+    if (a < 0) {
+        if (c == a) return make_double2(0., s);
+        if (c == -a) return make_double2(0., -s * ((a & 1) ? -1. : 1.));
+    } else if (a == 0) {
+        if (c == 0) return make_double2(1., 0.);
+    } else {
+        if (c == -a) return make_double2(s, 0.);
+        if (c == a) return make_double2(((a & 1) ? -1. : 1.) * s, 0.);
+    }
+    return make_double2(0., 0.);
+}
+
+__device__ __forceinline__ double2 cmul2(double2 a, double2 b)
+{
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 conj2(double2 a) { return make_double2(a.x, -a.y); }
+
+// F_r = Re(T F_c T^H) per l (fdcl_FFTSO3.cpp:1169-1181): the real-basis
+// coefficients of a real function from its complex coefficients.
+template <typename CIN, typename ROUT>
+__global__ void so3_c2r_kernel(const CIN* __restrict__ Fc, ROUT* __restrict__ Fr, int L, long long cstride)
+{
+    const int l = blockIdx.x, b = blockIdx.y;
+    const int W = 2 * l + 1;
+    const CIN* fc = Fc + (long long)b * cstride;
+    ROUT* fr = Fr + (long long)b * cstride;
+    for (int i = threadIdx.x; i < W * W; i += blockDim.x) {
+        int m = i % W - l, n = i / W - l;
+        int am[2] = {-m, m}, bn[2] = {-n, n};
+        int na = (m == 0) ? 1 : 2, nb = (n == 0) ? 1 : 2;
+        double acc = 0.;
+        for (int ia = 0; ia < na; ++ia)
+            for (int ib = 0; ib < nb; ++ib) {
+                double2 t1 = tmat(m, am[ia]), t2 = conj2(tmat(n, bn[ib]));
+                CIN v = fc[so3_idx(l, am[ia], bn[ib])];
+                double2 c = cmul2(cmul2(t1, make_double2((double)v.x, (double)v.y)), t2);
+                acc += c.x;
+            }
+        fr[so3_idx(l, m, n)] = (ROUT)acc;
+    }
+}
+
+// F_c = T^H F_r T per l: the complex coefficients whose synthesis equals the
+// real-basis synthesis sum (2l+1) F_r U (U = Re(conj(T) D T^T), fdcl_FFTSO3.cpp:1010-1022).
+template <typename RIN, typename COUT>
+__global__ void so3_r2c_kernel(const RIN* __restrict__ Fr, COUT* __restrict__ Fc, int L, long long cstride)
+{
+    const int l = blockIdx.x, b = blockIdx.y;
+    const int W = 2 * l + 1;
+    const RIN* fr = Fr + (long long)b * cstride;
+    COUT* fc = Fc + (long long)b * cstride;
+    for (int i = threadIdx.x; i < W * W; i += blockDim.x) {
+        int m = i % W - l, n = i / W - l;
+        int am[2] = {m, -m}, bn[2] = {n, -n};
+        int na = (m == 0) ? 1 : 2, nb = (n == 0) ? 1 : 2;
+        double2 acc = make_double2(0., 0.);
+        for (int ia = 0; ia < na; ++ia)
+            for (int ib = 0; ib < nb; ++ib) {
+                double2 t1 = conj2(tmat(am[ia], m)), t2 = tmat(bn[ib], n);
+                double v = (double)fr[so3_idx(l, am[ia], bn[ib])];
+                double2 c = cmul2(t1, t2);
+                acc.x += c.x * v;
+                acc.y += c.y * v;
+            }
+        COUT o;
+        o.x = acc.x;
+        o.y = acc.y;
+        fc[so3_idx(l, m, n)] = o;
+    }
+}
+
+// ------------------------------------------------------------------- S^2
+
+template <int NT>
+__global__ void __launch_bounds__(NT) s2_fwd_fp64_kernel(const double* __restrict__ table,
+                                                         const long long* __restrict__ moff,
+                                                         const double2* __restrict__ G, const double* __restrict__ w,
+                                                         double2* __restrict__ F, int L, int N, long long gstride,
+                                                         long long cstride, int is_real)
+{
+    extern __shared__ double2 X[];  // [2][N]
+    const int m = blockIdx.x, b = blockIdx.y;
+    const int np = (m > 0 && !is_real) ? 2 : 1;
+    const double2* Gb = G + (long long)b * gstride;
+    for (int i = threadIdx.x; i < np * N; i += NT) {
+        int p = i / N, k = i - p * N;
+        int bin = (p == 0) ? m : N - m;  // F_k(m) and F_k(2B + (-m)), fdcl_FFTS2.cpp:162,165
+        double2 v = Gb[(long long)k * N + bin];
+        double wk = w[k];
+        X[p * N + k] = make_double2(wk * v.x, wk * v.y);
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const double* tg = table + moff[m];
+    double2* Fb = F + (long long)b * cstride;
+    const double sg = (m & 1) ? -1. : 1.;
+    for (int l = m + warp; l <= L; l += NT / 32) {
+        const double* prow = tg + (long long)(l - m) * N;
+        double ar[2] = {0., 0.}, ai[2] = {0., 0.};
+        for (int k = lane; k < N; k += 32) {
+            double d = prow[k];
+            double2 x0 = X[k];
+            ar[0] += d * x0.x;
+            ai[0] += d * x0.y;
+            if (np == 2) {
+                double2 x1 = X[N + k];
+                ar[1] += d * x1.x;
+                ai[1] += d * x1.y;
+            }
+        }
+        double r0 = warp_sum(ar[0]), i0 = warp_sum(ai[0]);
+        double r1 = 0., i1 = 0.;
+        if (np == 2) {
+            r1 = warp_sum(ar[1]);
+            i1 = warp_sum(ai[1]);
+        }
+        if (lane == 0) {
+            Fb[s2_idx(l, m)] = make_double2(r0, i0);
+            if (m > 0) {
+                if (!is_real)
+                    Fb[s2_idx(l, -m)] = make_double2(sg * r1, sg * i1);
+                else  // Hermitian fill, fdcl_FFTS2.cpp:182-188
+                    Fb[s2_idx(l, -m)] = make_double2(sg * r0, sg * -i0);
+            }
+        }
+    }
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT) s2_inv_fp64_kernel(const double* __restrict__ table,
+                                                         const long long* __restrict__ moff,
+                                                         const double2* __restrict__ F, double2* __restrict__ H,
+                                                         int L, int N, long long gstride, long long cstride)
+{
+    extern __shared__ double2 Y[];  // [2][B]
+    const int m = blockIdx.x, b = blockIdx.y;
+    const int B = L + 1;
+    const int nl = B - m;
+    const int np = (m > 0) ? 2 : 1;
+    const double sg = (m & 1) ? -1. : 1.;
+    const double2* Fb = F + (long long)b * cstride;
+    for (int i = threadIdx.x; i < np * nl; i += NT) {
+        int p = i / nl, l = m + (i - p * nl);
+        double2 c = Fb[s2_idx(l, p == 0 ? m : -m)];
+        double s = (p == 0) ? 1. : sg;
+        Y[p * B + (l - m)] = make_double2(s * c.x, s * c.y);
+    }
+    __syncthreads();
+    const double* tg = table + moff[m];
+    double2* Hb = H + (long long)b * gstride;
+    for (int k = threadIdx.x; k < N; k += NT) {
+        double ar[2] = {0., 0.}, ai[2] = {0., 0.};
+        for (int j = 0; j < nl; ++j) {
+            double d = tg[(long long)j * N + k];
+            double2 y0 = Y[j];
+            ar[0] += d * y0.x;
+            ai[0] += d * y0.y;
+            if (np == 2) {
+                double2 y1 = Y[B + j];
+                ar[1] += d * y1.x;
+                ai[1] += d * y1.y;
+            }
+        }
+        // f = sum_m H(m) e^{+i m phi}: H(m) goes to bin -m mod N of a forward DFT
+        Hb[(long long)k * N + mod_n(-m, N)] = make_double2(ar[0], ai[0]);
+        if (np == 2) Hb[(long long)k * N + mod_n(m, N)] = make_double2(ar[1], ai[1]);
+    }
+}
+
+template <typename C>
+__global__ void zero_nyquist_s2_kernel(C* __restrict__ H, int N, long long nrows)
+{
+    long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrows) return;
+    C z;
+    z.x = 0;
+    z.y = 0;
+    H[r * N + N / 2] = z;
+}
+
+// F_r(l) = Re(conj(T(l)) F_c(l)) (fdcl_FFTS2.cpp:424-436).
+template <typename CIN, typename ROUT>
+__global__ void s2_c2r_kernel(const CIN* __restrict__ Fc, ROUT* __restrict__ Fr, int L, long long cstride)
+{
+    const int b = blockIdx.y;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long C = (long long)(L + 1) * (L + 1);
+    if (i >= C) return;
+    int l = (int)floor(sqrt((double)i));
+    while ((long long)l * l > i) --l;
+    while ((long long)(l + 1) * (l + 1) <= i) ++l;
+    int m = (int)(i - (long long)l * l) - l;
+    const CIN* fc = Fc + (long long)b * cstride;
+    int cs[2] = {-m, m};
+    if (m > 0) { cs[0] = -m; cs[1] = m; } else if (m < 0) { cs[0] = m; cs[1] = -m; }
+    int nc = (m == 0) ? 1 : 2;
+    double acc = 0.;
+    for (int j = 0; j < nc; ++j) {
+        double2 t = conj2(tmat(m, cs[j]));
+        CIN v = fc[s2_idx(l, cs[j])];
+        acc += t.x * (double)v.x - t.y * (double)v.y;
+    }
+    Fr[(long long)b * cstride + i] = (ROUT)acc;
+}
+
+// F_c = T^T F_r: the complex coefficients whose synthesis is the real-basis
+// synthesis sum F_r(l,m) y(l,m), y = T Y (fdcl_FFTS2.cpp:383-422).
+template <typename RIN, typename COUT>
+__global__ void s2_r2c_kernel(const RIN* __restrict__ Fr, COUT* __restrict__ Fc, int L, long long cstride)
+{
+    const int b = blockIdx.y;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long C = (long long)(L + 1) * (L + 1);
+    if (i >= C) return;
+    int l = (int)floor(sqrt((double)i));
+    while ((long long)l * l > i) --l;
+    while ((long long)(l + 1) * (l + 1) <= i) ++l;
+    int c = (int)(i - (long long)l * l) - l;
+    const RIN* fr = Fr + (long long)b * cstride;
+    int as[2] = {c, -c};
+    int na = (c == 0) ? 1 : 2;
+    double2 acc = make_double2(0., 0.);
+    for (int j = 0; j < na; ++j) {
+        double2 t = tmat(as[j], c);
+        double v = (double)fr[s2_idx(l, as[j])];
+        acc.x += t.x * v;
+        acc.y += t.y * v;
+    }
+    COUT o;
+    o.x = acc.x;
+    o.y = acc.y;
+    Fc[(long long)b * cstride + i] = o;
+}
+
+// ---------------------------------------------------------------- launchers
+
+cudaError_t launch_so3_fwd_fp64(const double* table, const long long* goff, const double2* G, const double* w,
+                                double2* F, int L, int N, int batch, cudaStream_t st)
+{
+    const int B = L + 1;
+    size_t smem = sizeof(double2) * 4 * N;
+    auto k = so3_fwd_fp64_kernel<256>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid(B * B, batch);
+    k<<<grid, 256, smem, st>>>(table, goff, G, w, F, L, N, (long long)N * N * N, so3_off(B));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_so3_inv_fp64(const double* table, const long long* goff, const double2* F, double2* H, int L,
+                                int N, int batch, cudaStream_t st)
+{
+    const int B = L + 1;
+    size_t smem = sizeof(double2) * 4 * B;
+    dim3 grid(B * B, batch);
+    so3_inv_fp64_kernel<256><<<grid, 256, smem, st>>>(table, goff, F, H, L, N, (long long)N * N * N, so3_off(B));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_zero_nyquist_so3(void* H, bool fp64, int N, long long nslices, cudaStream_t st)
+{
+    long long tot = nslices * 2 * N;
+    unsigned nb = (unsigned)((tot + 255) / 256);
+    if (fp64)
+        zero_nyquist_so3_kernel<double2><<<nb, 256, 0, st>>>((double2*)H, N, nslices);
+    else
+        zero_nyquist_so3_kernel<float2><<<nb, 256, 0, st>>>((float2*)H, N, nslices);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_so3_c2r(const void* Fc, void* Fr, bool fp64, int L, int batch, cudaStream_t st)
+{
+    dim3 grid(L + 1, batch);
+    long long cs = so3_off(L + 1);
+    if (fp64)
+        so3_c2r_kernel<double2, double><<<grid, 256, 0, st>>>((const double2*)Fc, (double*)Fr, L, cs);
+    else
+        so3_c2r_kernel<float2, float><<<grid, 256, 0, st>>>((const float2*)Fc, (float*)Fr, L, cs);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_so3_r2c(const void* Fr, void* Fc, bool fp64, int L, int batch, cudaStream_t st)
+{
+    dim3 grid(L + 1, batch);
+    long long cs = so3_off(L + 1);
+    if (fp64)
+        so3_r2c_kernel<double, double2><<<grid, 256, 0, st>>>((const double*)Fr, (double2*)Fc, L, cs);
+    else
+        so3_r2c_kernel<float, float2><<<grid, 256, 0, st>>>((const float*)Fr, (float2*)Fc, L, cs);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_s2_fwd_fp64(const double* table, const long long* moff, const double2* G, const double* w,
+                               double2* F, int L, int N, int batch, bool is_real, cudaStream_t st)
+{
+    size_t smem = sizeof(double2) * 2 * N;
+    dim3 grid(L + 1, batch);
+    s2_fwd_fp64_kernel<256><<<grid, 256, smem, st>>>(table, moff, G, w, F, L, N, (long long)N * N,
+                                                     (long long)(L + 1) * (L + 1), is_real ? 1 : 0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_s2_inv_fp64(const double* table, const long long* moff, const double2* F, double2* H, int L,
+                               int N, int batch, cudaStream_t st)
+{
+    size_t smem = sizeof(double2) * 2 * (L + 1);
+    dim3 grid(L + 1, batch);
+    s2_inv_fp64_kernel<256><<<grid, 256, smem, st>>>(table, moff, F, H, L, N, (long long)N * N,
+                                                     (long long)(L + 1) * (L + 1));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_zero_nyquist_s2(void* H, bool fp64, int N, long long nrows, cudaStream_t st)
+{
+    unsigned nb = (unsigned)((nrows + 255) / 256);
+    if (fp64)
+        zero_nyquist_s2_kernel<double2><<<nb, 256, 0, st>>>((double2*)H, N, nrows);
+    else
+        zero_nyquist_s2_kernel<float2><<<nb, 256, 0, st>>>((float2*)H, N, nrows);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_s2_c2r(const void* Fc, void* Fr, bool fp64, int L, int batch, cudaStream_t st)
+{
+    long long C = (long long)(L + 1) * (L + 1);
+    dim3 grid((unsigned)((C + 255) / 256), batch);
+    if (fp64)
+        s2_c2r_kernel<double2, double><<<grid, 256, 0, st>>>((const double2*)Fc, (double*)Fr, L, C);
+    else
+        s2_c2r_kernel<float2, float><<<grid, 256, 0, st>>>((const float2*)Fc, (float*)Fr, L, C);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_s2_r2c(const void* Fr, void* Fc, bool fp64, int L, int batch, cudaStream_t st)
+{
+    long long C = (long long)(L + 1) * (L + 1);
+    dim3 grid((unsigned)((C + 255) / 256), batch);
+    if (fp64)
+        s2_r2c_kernel<double, double2><<<grid, 256, 0, st>>>((const double*)Fr, (double2*)Fc, L, C);
+    else
+        s2_r2c_kernel<float, float2><<<grid, 256, 0, st>>>((const float*)Fr, (float2*)Fc, L, C);
+    return cudaGetLastError();
+}
+
+}  // namespace fftso3

@@ -1,0 +1,31 @@
+// Batched strided 1-D FFT launcher (see fft.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace fftso3 {
+
+struct FFTFactors {
+    int N;
+    int n;
+    int r[24];
+};
+
+struct FFTLaunch {
+    const void* in;       // complex (or real when real_in) input
+    void* out;            // complex (or real part only when real_out) output; may equal in
+    FFTFactors fac;
+    long long nlines;     // number of transforms
+    int lpb;              // lines per CTA
+    long long inner, ostride, istride, es;  // line i base = (i/inner)*ostride + (i%inner)*istride; element stride es
+    const void* tw;       // device double2 table, W[i] = exp(-2 pi i i / N)
+    bool fp64;
+    bool real_in;
+    bool real_out;
+    bool lines_fastest;   // consecutive lines adjacent in memory (column pass)
+};
+
+void make_fft_factors(int N, FFTFactors& f);
+size_t fft_smem_bytes(int N, int lpb, bool fp64);
+cudaError_t launch_fft_lines(const FFTLaunch& L, cudaStream_t st);
+
+}  // namespace fftso3

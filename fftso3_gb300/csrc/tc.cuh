@@ -1,0 +1,21 @@
+// Tensor-core (tcgen05, split-BF16) SO(3) transform state (see contract_tc.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <string>
+#include <vector>
+
+#include "fft.cuh"
+
+namespace fftso3 {
+
+struct TCState;
+
+int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64, const std::vector<long long>& goff,
+              long long table_elems, const double* d_tw, const double* d_w, const FFTFactors& fac, bool refine,
+              std::string& err);
+void tc_destroy(TCState* s);
+long long tc_device_bytes(const TCState* s);
+int tc_forward(TCState* s, const void* grid, void* coeffs, cudaStream_t st, std::string& err);
+int tc_inverse(TCState* s, const void* coeffs, void* grid, cudaStream_t st, std::string& err);
+
+}  // namespace fftso3

@@ -1,0 +1,129 @@
+/*
+ * fftso3_gb300.h -- C ABI of the GB300 (sm_103a) SO(3) / S^2 harmonic-transform library.
+ *
+ * Each entry point replaces one operation of the fdcl-gwu/FFTSO3 C++ API
+ * (cited per declaration as file:line of that project).  The ABI uses plain
+ * pointers, sizes and an opaque plan; every call returns an int status
+ * (FFTSO3_SUCCESS == 0) and fftso3_last_error_string() describes the last
+ * failure on the calling thread.  The reference reports errors with assert()
+ * only (fdcl_FFTSO3_matrix.cpp:23-33); this library rejects the same bad
+ * inputs (l_max < 0, index ranges, sizes) with FFTSO3_ERR_INVALID_ARG instead.
+ *
+ * Data layouts (shared by every call):
+ *   B = l_max + 1, N = 2B.
+ *   SO(3) grid   [batch][k][j1][j2]: f(alpha_j1, beta_k, gamma_j2),
+ *                beta_k = (2k+1) pi / (4B), alpha_j = gamma_j = j pi / B
+ *                (fdcl_FFTSO3.cpp:578-591, loop order :676-685).
+ *   S^2 grid     [batch][k][j]: f(theta_k, phi_j), theta_k = (2k+1) pi / (4B),
+ *                phi_j = j pi / B (fdcl_FFTS2.cpp:292-300).
+ *   SO(3) coefficients [batch][C], C = B(4B^2-1)/3, F(l,m,n) at
+ *                l(4l^2-1)/3 + (m+l) + (n+l)(2l+1): the per-l (2l+1)x(2l+1)
+ *                column-major blocks of FFTSO3_matrix (fdcl_FFTSO3_matrix.cpp:43-47)
+ *                laid end to end, so each M[l].data() is one contiguous copy.
+ *   S^2 coefficients [batch][B^2], F(l,m) at l^2 + m + l (fdcl_FFTS2_matrix.cpp:43-47).
+ *   Complex data is interleaved (re, im): complex128 for FFTSO3_PREC_FP64,
+ *   complex64 for the tensor-core / FP32 precisions; real data float64 / float32.
+ *
+ * Streams: `stream` is a cudaStream_t passed as void*; NULL means the legacy
+ * default stream.  Device-pointer calls are asynchronous on that stream.
+ */
+#ifndef FFTSO3_GB300_H
+#define FFTSO3_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define FFTSO3_SUCCESS 0
+#define FFTSO3_ERR_INVALID_ARG 1
+#define FFTSO3_ERR_CUDA 2
+#define FFTSO3_ERR_OOM 3
+#define FFTSO3_ERR_UNSUPPORTED 4
+#define FFTSO3_ERR_NO_DEVICE 5
+
+/* transform kinds: the four reference classes */
+#define FFTSO3_SO3_COMPLEX 0 /* fdcl::FFTSO3_complex, include/fdcl_FFTSO3.hpp:27-177 */
+#define FFTSO3_SO3_REAL 1    /* fdcl::FFTSO3_real,    include/fdcl_FFTSO3.hpp:184-308 */
+#define FFTSO3_S2_COMPLEX 2  /* fdcl::FFTS2_complex,  include/fdcl_FFTS2.hpp:28-100 */
+#define FFTSO3_S2_REAL 3     /* fdcl::FFTS2_real,     include/fdcl_FFTS2.hpp:107-160 */
+
+/* arithmetic of the beta-sum contraction */
+#define FFTSO3_PREC_FP64 0      /* FP64 end to end (the plain method) */
+#define FFTSO3_PREC_TC_BF16X3 1 /* tcgen05 tensor cores, 3-term split-BF16, FP32 accumulate; complex64/float32 data */
+
+/* Wigner-d recursion */
+#define FFTSO3_RECURSION_REFERENCE 0 /* bit-faithful to fdcl_FFTSO3.cpp:127-194 (underflows near beta=pi, l_max>~90) */
+#define FFTSO3_RECURSION_STABLE 1    /* log-domain seeds + extended-exponent recursion */
+
+/* plan flags */
+#define FFTSO3_FLAG_REFINE 0x1u /* tensor-core forward: one residual step F += forward(f - inverse(F)) */
+
+typedef struct fftso3_plan fftso3_plan;
+
+/* Thread-local description of the last error ("" when none). */
+const char* fftso3_last_error_string(void);
+
+/* Library version (major*10000 + minor*100 + patch). */
+int fftso3_version(void);
+
+/* Element counts of one function's grid and coefficient vector for a kind
+ * (complex or real elements as the kind dictates).  -1 on bad arguments. */
+long long fftso3_grid_elems(int kind, int l_max);
+long long fftso3_coeff_elems(int kind, int l_max);
+
+/* Quadrature weights w_k, k < 2B, computed on the host in FP64.
+ * SO(3): fdcl_FFTSO3.cpp:236-256 (compute_weight); S^2: fdcl_FFTS2.cpp:102-123. */
+int fftso3_weights(int kind, int l_max, double* weights_out);
+
+/* Create a plan for `batch` functions of bandwidth l_max on the current CUDA
+ * device.  Replaces the constructor / init(l_max) of the reference classes
+ * (fdcl_FFTSO3.cpp:3-14, :1000-1008, fdcl_FFTS2.cpp:3-15, :371-381); the plan
+ * owns the Wigner-d (SO(3)) or Legendre (S^2) tables, twiddles and workspace.
+ * precision: FFTSO3_PREC_*; recursion: FFTSO3_RECURSION_* (SO(3) only). */
+int fftso3_plan_create(fftso3_plan** plan, int kind, int l_max, int batch, int precision, int recursion,
+                       unsigned flags);
+int fftso3_plan_destroy(fftso3_plan* plan);
+
+/* Device bytes held by the plan (tables + workspace). */
+long long fftso3_plan_device_bytes(const fftso3_plan* plan);
+
+/* Forward transform of `batch` sampled functions (device pointers).
+ * Replaces forward_transform(func): fdcl_FFTSO3.cpp:654-763 (complex),
+ * :774-850 (real), fdcl_FFTS2.cpp:125-192 (complex), :424-436 (real); the
+ * callback is replaced by its samples on the grid above. */
+int fftso3_forward(fftso3_plan* plan, const void* grid, void* coeffs, void* stream);
+
+/* Inverse transform onto the full grid (device pointers): f at every grid
+ * point, with the semantics of inverse_transform(F, alpha, beta, gamma)
+ * (fdcl_FFTSO3.cpp:498-531, :1141-1156; fdcl_FFTS2.cpp:194-230, :500-512)
+ * evaluated at each (alpha_j1, beta_k, gamma_j2) / (theta_k, phi_j). */
+int fftso3_inverse(fftso3_plan* plan, const void* coeffs, void* grid, void* stream);
+
+/* Host-buffer variants: copy host -> device, transform, copy back, and
+ * synchronise the stream before returning (the reference's by-value call
+ * convention).  Host buffers may be pageable or pinned. */
+int fftso3_forward_host(fftso3_plan* plan, const void* grid_host, void* coeffs_host, void* stream);
+int fftso3_inverse_host(fftso3_plan* plan, const void* coeffs_host, void* grid_host, void* stream);
+
+/* Point evaluation of one coefficient set (batch entry `index`) at n points
+ * (device pointers).  SO(3): pts = n x (alpha, beta, gamma); S^2: n x (theta, phi).
+ * Replaces inverse_transform(F, alpha, beta, gamma) (fdcl_FFTSO3.cpp:498-531,
+ * :1141-1156) and inverse_transform(F, theta, phi) (fdcl_FFTS2.cpp:194-230,
+ * :500-512).  Output complex128 (complex kinds) or float64 (real kinds);
+ * FP64 arithmetic regardless of the plan precision. */
+int fftso3_inverse_points(fftso3_plan* plan, const void* coeffs, int index, const double* pts, int n, void* out,
+                          void* stream);
+
+/* Wigner-d table d^l_mn(beta) for all l <= l_max at one angle, packed like
+ * the SO(3) coefficients, computed on the GPU (host output buffer).
+ * Replaces wigner_d(beta) (fdcl_FFTSO3.cpp:122-194). */
+int fftso3_wigner_d(double beta, int l_max, int recursion, double* d_out_host);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FFTSO3_GB300_H */
