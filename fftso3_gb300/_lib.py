@@ -50,6 +50,7 @@ SIGNATURES = {
     "fftso3_plan_create": (_i, [ctypes.POINTER(_vp), _i, _i, _i, _i, _i, ctypes.c_uint]),
     "fftso3_plan_destroy": (_i, [_vp]),
     "fftso3_plan_device_bytes": (_ll, [_vp]),
+    "fftso3_plan_check": (_i, [_vp]),
     "fftso3_forward": (_i, [_vp, _vp, _vp, _vp]),
     "fftso3_inverse": (_i, [_vp, _vp, _vp, _vp]),
     "fftso3_forward_host": (_i, [_vp, _vp, _vp, _vp]),
@@ -137,6 +138,10 @@ class Plan:
     def inverse_points(self, coeff_ptr: int, index: int, pts, n: int, out_ptr: int, stream: int = 0) -> None:
         check(lib().fftso3_inverse_points(self._h, _vp(coeff_ptr), int(index), pts, int(n), _vp(out_ptr),
                                           _vp(stream)))
+
+    def check(self) -> None:
+        """Synchronise and raise if an earlier asynchronous call failed."""
+        check(lib().fftso3_plan_check(self._h))
 
     def close(self) -> None:
         if getattr(self, "_h", None) is not None and _lib is not None:

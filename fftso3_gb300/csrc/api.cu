@@ -402,6 +402,10 @@ int fftso3_plan_create(fftso3_plan** out, int kind, int l_max, int batch, int pr
             return bail(rc);
         }
         p->bytes += tc_device_bytes(p->tc);
+        // the tensor-core path keeps only its BF16 planes of the table
+        cudaFree(p->d_table);
+        p->d_table = nullptr;
+        p->bytes -= (long long)sizeof(double) * p->table_elems;
     }
     *out = p;
     return FFTSO3_SUCCESS;
@@ -421,6 +425,20 @@ int fftso3_plan_destroy(fftso3_plan* plan)
 }
 
 long long fftso3_plan_device_bytes(const fftso3_plan* plan) { return plan ? plan->bytes : -1; }
+
+int fftso3_plan_check(fftso3_plan* plan)
+{
+    int rc = check_plan(plan);
+    if (rc) return rc;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_fail(e, "device synchronize");
+    if (plan->tc) {
+        int code = tc_status(plan->tc);
+        if (code != 0)
+            return fail(FFTSO3_ERR_CUDA, "a tensor-core kernel gave up a bounded wait (code " + std::to_string(code) + ")");
+    }
+    return FFTSO3_SUCCESS;
+}
 
 int fftso3_forward(fftso3_plan* plan, const void* grid, void* coeffs, void* stream)
 {

@@ -17,5 +17,7 @@ void tc_destroy(TCState* s);
 long long tc_device_bytes(const TCState* s);
 int tc_forward(TCState* s, const void* grid, void* coeffs, cudaStream_t st, std::string& err);
 int tc_inverse(TCState* s, const void* coeffs, void* grid, cudaStream_t st, std::string& err);
+// Device error word of the tensor-core kernels (0 = no bounded wait timed out); synchronising read.
+int tc_status(TCState* s);
 
 }  // namespace fftso3

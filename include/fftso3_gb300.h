@@ -90,6 +90,12 @@ int fftso3_plan_destroy(fftso3_plan* plan);
 /* Device bytes held by the plan (tables + workspace). */
 long long fftso3_plan_device_bytes(const fftso3_plan* plan);
 
+/* Synchronise the plan's device and report failures of earlier asynchronous
+ * calls, including a tensor-core kernel that gave up one of its bounded waits
+ * (its kernels never spin without limit; they record an error code instead).
+ * No reference counterpart: the reference has no asynchronous work. */
+int fftso3_plan_check(fftso3_plan* plan);
+
 /* Forward transform of `batch` sampled functions (device pointers).
  * Replaces forward_transform(func): fdcl_FFTSO3.cpp:654-763 (complex),
  * :774-850 (real), fdcl_FFTS2.cpp:125-192 (complex), :424-436 (real); the
@@ -108,8 +114,10 @@ int fftso3_inverse(fftso3_plan* plan, const void* coeffs, void* grid, void* stre
 int fftso3_forward_host(fftso3_plan* plan, const void* grid_host, void* coeffs_host, void* stream);
 int fftso3_inverse_host(fftso3_plan* plan, const void* coeffs_host, void* grid_host, void* stream);
 
-/* Point evaluation of one coefficient set (batch entry `index`) at n points
- * (device pointers).  SO(3): pts = n x (alpha, beta, gamma); S^2: n x (theta, phi).
+/* Point evaluation of one coefficient set (batch entry `index` of the device
+ * array `coeffs`) at n points given in host memory; the n results are written
+ * to host memory and the call synchronises `stream` before returning.
+ * SO(3): pts = n x (alpha, beta, gamma); S^2: n x (theta, phi).
  * Replaces inverse_transform(F, alpha, beta, gamma) (fdcl_FFTSO3.cpp:498-531,
  * :1141-1156) and inverse_transform(F, theta, phi) (fdcl_FFTS2.cpp:194-230,
  * :500-512).  Output complex128 (complex kinds) or float64 (real kinds);
