@@ -69,7 +69,7 @@ def build(verbose: bool = False, extra: list[str] | None = None) -> str:
                 raise RuntimeError("nvcc failed:\n" + "\n".join(errs))
     objs = [os.path.join(BUILD, f.replace(".cu", ".o")) for f in sources()]
     if jobs or not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
-        cmd = [cc, *ARCH, "-shared", "-o", LIB, *objs, "-lcuda"]
+        cmd = [cc, *ARCH, "-shared", "-o", LIB, *objs]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + r.stderr)
