@@ -1,0 +1,411 @@
+#!/usr/bin/env python
+"""Benchmark: SO(3) forward+inverse transform pairs per second at l_max = 255.
+
+Workload (default): a batch of complex SO(3) functions at l_max = 255 (512^3
+Euler grid each, complex64 samples; synthetic seeded coefficients
+F ~ N(0,1)(l+1)^-1.5), transformed with the tensor-core split-BF16 path
+(FFTSO3_PREC_TC_BF16X3, stable Wigner-d recursion).  One step = inverse of the
+whole batch (coefficients -> grids) + forward of the whole batch
+(grids -> coefficients); value = functions x world / step time.
+
+Also reported: the plain FP64 GPU path on the same l_max (pairs/s), the
+accuracy of the tensor-core path against FP64, the end-to-end rate through the
+host-buffer C-ABI calls, the roofline of the dominant kernel (stage timing
+with CUDA events inside the library), and the CPU baseline: the oracle's
+restatement of the reference algorithm timed on the host cores on a bounded
+sample of beta slices.
+
+--impl reference times only that CPU algorithm (all host threads) on the same
+workload and prints its own JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import re
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "SO(3) fwd+inv transforms/s at l_max=255: TC split-BF16 vs FP64 at rel-err<=1e-6"
+UNIT = "transform pairs/s"
+
+
+def seeded_coeffs(l_max: int, seed: int) -> np.ndarray:
+    rng = np.random.Generator(np.random.PCG64(seed))
+    l = np.concatenate([np.full((2 * x + 1) ** 2, x) for x in range(l_max + 1)])
+    s = (l + 1.0) ** -1.5
+    return rng.standard_normal(l.size) * s + 1j * rng.standard_normal(l.size) * s
+
+
+def per_l_errors(a: np.ndarray, b: np.ndarray, l_max: int) -> tuple[float, float]:
+    """rel_rms = ||a-b|| / ||b||; rel_max = max_l max_mn |a-b| / rms_mn |b| (per-l normalised)."""
+    rms = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    mx = 0.0
+    for l in range(l_max + 1):
+        o0, o1 = l * (4 * l * l - 1) // 3, (l + 1) * (4 * (l + 1) ** 2 - 1) // 3
+        d = np.abs(a[o0:o1] - b[o0:o1]).max()
+        r = np.sqrt(np.mean(np.abs(b[o0:o1]) ** 2))
+        mx = max(mx, float(d / r))
+    return rms, mx
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.device)], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        rows = []
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) >= 9 and f[1].replace(".", "").isdigit():
+                    rows.append(f)
+        except Exception:
+            pass
+        finally:
+            try:
+                os.unlink(self.path)
+            except Exception:
+                pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in rows]
+        mx = float(rows[0][2])
+        under = [s for s in sm if s > 0.5 * mx] or sm
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(under)), "sm_max_mhz": mx, "reasons": reasons, "samples": len(rows),
+                "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit())
+                if any(r[3].replace(".", "").isdigit() for r in rows) else None}
+
+
+def measured_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d["bf16_tflops"],
+                "bf16_tflops_sustained": d.get("bf16_tflops_sustained", d["bf16_tflops"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "source": "fallback"}
+
+
+def profiled_traffic(stage: str, l_max: int, batch: int):
+    """dram bytes per launch of `stage` from the committed ncu summary, scaled
+    to this workload (lines 'traffic <stage> l_max=<L> batch=<b> bytes=<n>')."""
+    path = os.path.join(ROOT, "profiles", "traffic.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        m = re.match(r"\s*traffic\s+(\S+)\s+l_max=(\d+)\s+batch=(\d+)\s+bytes=(\d+)", line)
+        if m and m.group(1) == stage and int(m.group(2)) == l_max:
+            return int(m.group(4)) * batch / int(m.group(3))
+    return None
+
+
+# --------------------------------------------------------------- CPU legs
+
+def cpu_sample(l_max: int, nslices: int | None = None, threads: int | None = None) -> dict:
+    """Oracle (restated reference algorithm, OpenMP) on beta slices 0..S-1 of
+    the forward and of the inverse at l_max; pairs/s extrapolated to all 2B slices."""
+    from oracle import oracle as O
+
+    O.build()
+    nth = threads or os.cpu_count() or 1
+    O.set_num_threads(nth)
+    N = 2 * (l_max + 1)
+    S = min(N, nslices or nth)
+    rng = np.random.default_rng(0)
+    F = seeded_coeffs(l_max, 0)
+    slab = (rng.standard_normal((S, N, N)) + 1j * rng.standard_normal((S, N, N)))
+    t0 = time.perf_counter()
+    O.so3_forward_complex_slices(l_max, slab, 0, S)
+    t1 = time.perf_counter()
+    O.so3_inverse_complex_slices(l_max, F, 0, S)
+    t2 = time.perf_counter()
+    per_pair = ((t1 - t0) + (t2 - t1)) * N / S
+    return {"value": 1.0 / per_pair, "unit": UNIT, "cores": nth, "kind": "port",
+            "sample": f"beta slices 0..{S - 1} of {N} of one l_max={l_max} complex forward and inverse "
+                      f"(oracle restatement of fdcl_FFTSO3.cpp:659-763 / :498-531, OpenMP {nth} threads); "
+                      f"pairs/s extrapolated x{N}/{S}",
+            "seconds": t2 - t0}
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    for _ in range(args.warmup):
+        cpu_sample(args.l_max)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vals.append(cpu_sample(args.l_max))
+    wall = time.perf_counter() - t0
+    v = float(np.mean([x["value"] for x in vals]))
+    line = {
+        "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * wall / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "impl": "reference",
+        "config": {"workload": f"SO(3) complex forward+inverse, l_max={args.l_max}, one function per pair; "
+                               "reference CPU algorithm on a bounded sample of beta slices"},
+        "cpu_baseline": {k: vals[-1][k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------- GPU arm
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--l-max", type=int, default=255)
+    ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+
+    import fftso3_gb300 as fg
+    from fftso3_gb300 import _lib
+    from fftso3_gb300 import build as fbuild
+
+    fbuild.build()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    L, b = args.l_max, args.batch
+    N = 2 * (L + 1)
+    C = fg.so3_ncoeff(L)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- FP64 plain path: reference data for the accuracy check + its own rate
+    F0 = seeded_coeffs(L, 1000 * rank)
+    fp64 = None
+    acc = {}
+    p64 = _lib.Plan(_lib.SO3_COMPLEX, L, 1, "fp64", "stable")
+    c64 = torch.from_numpy(F0).to(dev)
+    g64 = torch.empty(N ** 3, dtype=torch.complex128, device=dev)
+    o64 = torch.empty_like(c64)
+    p64.inverse(c64.data_ptr(), g64.data_ptr(), sp)
+    p64.forward(g64.data_ptr(), o64.data_ptr(), sp)
+    torch.cuda.synchronize()
+    F0_fp64 = o64.cpu().numpy()  # FP64 forward of the FP64 synthesis
+    g0_c64 = g64.to(torch.complex64)
+    g0_ref = g64.cpu().numpy()
+    if not args.no_fp64:
+        reps = 2
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            p64.inverse(c64.data_ptr(), g64.data_ptr(), sp)
+            p64.forward(g64.data_ptr(), o64.data_ptr(), sp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        fp64 = {"value": 1000.0 / ms, "unit": UNIT, "ms_per_pair": ms, "batch": 1,
+                "note": "plain FP64 GPU path (FFTSO3_PREC_FP64, stable recursion), same l_max"}
+    del p64, g64, o64, c64
+    torch.cuda.empty_cache()
+
+    # ---- tensor-core plan
+    plan = _lib.Plan(_lib.SO3_COMPLEX, L, b, "tc_bf16x3", "stable")
+    Fb = np.concatenate([seeded_coeffs(L, 1000 * rank + i) for i in range(b)]).astype(np.complex64)
+    coef = torch.from_numpy(Fb).to(dev)
+    grid = torch.empty(b * N ** 3, dtype=torch.complex64, device=dev)
+    plan.inverse(coef.data_ptr(), grid.data_ptr(), sp)  # synthetic band-limited inputs
+    grid[:N ** 3].copy_(g0_c64)                         # function 0: the FP64 synthesis
+    coef_out = torch.empty_like(coef)
+    grid_out = torch.empty_like(grid)
+    torch.cuda.synchronize()
+    plan.check()
+
+    # accuracy vs FP64 (function 0), before the timed region
+    coef0 = torch.from_numpy(F0.astype(np.complex64)).to(dev)
+    coef_in = coef.clone()
+    coef_in[:C].copy_(coef0)
+    plan.forward(grid.data_ptr(), coef_out.data_ptr(), sp)
+    plan.inverse(coef_in.data_ptr(), grid_out.data_ptr(), sp)
+    torch.cuda.synchronize()
+    plan.check()
+    fr, fm = per_l_errors(coef_out[:C].cpu().numpy().astype(np.complex128), F0_fp64, L)
+    gi = grid_out[:N ** 3].cpu().numpy().astype(np.complex128)
+    ir = float(np.linalg.norm(gi - g0_ref) / np.linalg.norm(g0_ref))
+    im = float(np.abs(gi - g0_ref).max() / np.sqrt(np.mean(np.abs(g0_ref) ** 2)))
+    acc = {"forward_rel_rms": fr, "forward_rel_max_per_l": fm, "inverse_rel_rms": ir, "inverse_rel_max": im,
+           "against": "FP64 GPU path (stable recursion) on the same function"}
+    del coef_in, coef0
+
+    # ---- timed region: inputs resident in HBM (each grid 1 GB >> 129 MB L2)
+    for _ in range(args.warmup):
+        plan.inverse(coef.data_ptr(), grid_out.data_ptr(), sp)
+        plan.forward(grid.data_ptr(), coef_out.data_ptr(), sp)
+    barrier()
+    plan.set_timing(True)
+    plan.stage_times(reset=True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        e0.record(stream)
+        for _ in range(args.steps):
+            plan.inverse(coef.data_ptr(), grid_out.data_ptr(), sp)
+            plan.forward(grid.data_ptr(), coef_out.data_ptr(), sp)
+        e1.record(stream)
+        barrier()
+    ms = e0.elapsed_time(e1) / args.steps
+    stages = plan.stage_times(reset=True)
+    plan.set_timing(False)
+    plan.check()
+    clocks = clk.summary()
+    ms_max = ms
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+    value = b * world * 1000.0 / ms_max
+    launches = int(sum(c for _, c in stages.values()))
+
+    # ---- roofline of the dominant kernel
+    peaks = measured_peaks()
+    B = L + 1
+    top = max(stages.items(), key=lambda kv: kv[1][0])
+    name, (tot_ms, cnt) = top
+    per_launch_s = tot_ms / cnt / 1000.0
+    useful_flops = 8.0 * B * C * b            # complex beta-sum flops per direction for the batch
+    grid_bytes = 8.0 * b * N ** 3             # one complex64 pass over the batch's grids
+    Kp = (N + 63) // 64 * 64
+    KLp = (B + 63) // 64 * 64
+    ncols = (8 * b + 127) // 128 * 128
+    if name.startswith("tc_gemm"):
+        achieved = useful_flops / per_launch_s / 1e12
+        peak = peaks["bf16_tflops_sustained"]
+        roof = {"bound": "tensor", "unit": "TFLOP/s", "algorithmic": "8*B*C*batch useful flops per launch"}
+    else:
+        if name.startswith("fft"):
+            byts = 2 * grid_bytes
+        elif name == "tc_pack_fwd":
+            byts = grid_bytes + 6.0 * B * B * ncols * Kp
+        elif name == "tc_pack_inv":
+            byts = 8.0 * C * b + 6.0 * B * B * ncols * KLp
+        else:
+            byts = grid_bytes
+        achieved = byts / per_launch_s / 1e9
+        peak = peaks["hbm_gbs"]
+        roof = {"bound": "hbm", "unit": "GB/s", "algorithmic": "bytes read + written per launch"}
+    roof.update({"kernel": name, "achieved": achieved, "peak": peak, "frac": achieved / peak,
+                 "peak_source": peaks["source"], "ms_per_launch": per_launch_s * 1000.0,
+                 "traffic": profiled_traffic(name, L, b)})
+    stage_summary = {k: {"ms_per_launch": v / c, "launches": c, "share": v / sum(x for x, _ in stages.values())}
+                     for k, (v, c) in stages.items()}
+
+    # ---- end to end through the host-buffer C ABI (pinned host memory)
+    e2e = None
+    if not args.no_e2e:
+        hg = torch.empty(b * N ** 3, dtype=torch.complex64, pin_memory=True)
+        hg.copy_(grid)
+        hc = torch.empty(b * C, dtype=torch.complex64, pin_memory=True)
+        hc.copy_(coef)
+        hgo = torch.empty_like(hg, pin_memory=True)
+        hco = torch.empty_like(hc, pin_memory=True)
+        plan.inverse_host(hc.data_ptr(), hgo.data_ptr(), sp)
+        plan.forward_host(hg.data_ptr(), hco.data_ptr(), sp)
+        barrier()
+        t0 = time.perf_counter()
+        ksteps = max(1, min(args.steps, 3))
+        for _ in range(ksteps):
+            plan.inverse_host(hc.data_ptr(), hgo.data_ptr(), sp)
+            plan.forward_host(hg.data_ptr(), hco.data_ptr(), sp)
+        barrier()
+        dt = (time.perf_counter() - t0) / ksteps
+        if dist is not None:
+            t = torch.tensor([dt], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            dt = float(t.item())
+        e2e = {"value": b * world / dt, "unit": UNIT, "h2d_bytes_per_step": int(8 * b * C + 8 * b * N ** 3),
+               "d2h_bytes_per_step": int(8 * b * N ** 3 + 8 * b * C), "steps": ksteps}
+        del hg, hc, hgo, hco
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_sample(L)
+        cpu.pop("seconds", None)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16x3 (split) / fp32 accumulate / fp32 FFT", "data": "synthetic",
+            "config": {"workload": f"SO(3) complex forward+inverse, l_max={L}, batch={b} functions per GPU "
+                                   f"(512^3 complex64 grid each), TC split-BF16, stable recursion",
+                       "l_max": L, "batch_per_gpu": b, "precision": "tc_bf16x3",
+                       "l2": "inputs larger than L2 (1 GB grid per function)"},
+            "e2e": e2e, "gpu_launches": launches, "roofline": roof, "stages": stage_summary,
+            "accuracy": acc, "fp64_path": fp64,
+            "speedup_vs_fp64_path": (value / world) / fp64["value"] if fp64 else None,
+            "clocks": clocks, "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

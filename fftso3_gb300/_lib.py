@@ -51,6 +51,10 @@ SIGNATURES = {
     "fftso3_plan_destroy": (_i, [_vp]),
     "fftso3_plan_device_bytes": (_ll, [_vp]),
     "fftso3_plan_check": (_i, [_vp]),
+    "fftso3_plan_set_timing": (_i, [_vp, _i]),
+    "fftso3_stage_count": (_i, []),
+    "fftso3_stage_name": (ctypes.c_char_p, [_i]),
+    "fftso3_plan_stage_times": (_i, [_vp, _dp, ctypes.POINTER(_ll), _i]),
     "fftso3_forward": (_i, [_vp, _vp, _vp, _vp]),
     "fftso3_inverse": (_i, [_vp, _vp, _vp, _vp]),
     "fftso3_forward_host": (_i, [_vp, _vp, _vp, _vp]),
@@ -138,6 +142,17 @@ class Plan:
     def inverse_points(self, coeff_ptr: int, index: int, pts, n: int, out_ptr: int, stream: int = 0) -> None:
         check(lib().fftso3_inverse_points(self._h, _vp(coeff_ptr), int(index), pts, int(n), _vp(out_ptr),
                                           _vp(stream)))
+
+    def set_timing(self, enable: bool = True) -> None:
+        check(lib().fftso3_plan_set_timing(self._h, 1 if enable else 0))
+
+    def stage_times(self, reset: bool = False) -> dict:
+        """{stage name: (total ms, launches)} of the timed launches so far."""
+        n = lib().fftso3_stage_count()
+        ms = (ctypes.c_double * n)()
+        cnt = (_ll * n)()
+        check(lib().fftso3_plan_stage_times(self._h, ms, cnt, 1 if reset else 0))
+        return {lib().fftso3_stage_name(i).decode(): (ms[i], cnt[i]) for i in range(n) if cnt[i]}
 
     def check(self) -> None:
         """Synchronise and raise if an earlier asynchronous call failed."""

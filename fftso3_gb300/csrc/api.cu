@@ -16,6 +16,7 @@
 #include "fft.cuh"
 #include "tables.cuh"
 #include "tc.cuh"
+#include "timing.cuh"
 
 using namespace fftso3;
 
@@ -110,6 +111,7 @@ struct fftso3_plan {
     void* d_io_coeff = nullptr;
     long long bytes = 0;
     TCState* tc = nullptr;         // tensor-core contraction state
+    StageTimer timer;              // optional per-stage CUDA-event timing
 };
 
 namespace {
@@ -188,18 +190,27 @@ FFTLaunch fft_cols(const fftso3_plan* p, const void* in, void* out, long long no
 int run_forward(fftso3_plan* p, const void* grid, void* coeffs, cudaStream_t st)
 {
     const int N = p->N, L = p->L, b = p->batch;
-    if (p->precision == FFTSO3_PREC_TC_BF16X3) return tc_forward(p->tc, grid, coeffs, st, g_err);
+    StageTimer& T = p->timer;
+    if (p->precision == FFTSO3_PREC_TC_BF16X3) return tc_forward(p->tc, grid, coeffs, st, &T, g_err);
+#define STAGE(id, call)      \
+    do {                     \
+        T.begin(id, st);     \
+        CK(call);            \
+        T.end(st);           \
+    } while (0)
     if (p->so3) {
-        CK(launch_fft_lines(fft_rows(p, grid, p->d_work, (long long)b * N * N, p->real, false), st));
-        CK(launch_fft_lines(fft_cols(p, p->d_work, p->d_work, (long long)b * N, false), st));
+        STAGE(ST_FFT_ROWS, launch_fft_lines(fft_rows(p, grid, p->d_work, (long long)b * N * N, p->real, false), st));
+        STAGE(ST_FFT_COLS, launch_fft_lines(fft_cols(p, p->d_work, p->d_work, (long long)b * N, false), st));
         double2* Fout = p->real ? (double2*)p->d_fc : (double2*)coeffs;
-        CK(launch_so3_fwd_fp64(p->d_table, p->d_goff, (const double2*)p->d_work, p->d_w, Fout, L, N, b, st));
-        if (p->real) CK(launch_so3_c2r(p->d_fc, coeffs, true, L, b, st));
+        STAGE(ST_FP64_FWD,
+              launch_so3_fwd_fp64(p->d_table, p->d_goff, (const double2*)p->d_work, p->d_w, Fout, L, N, b, st));
+        if (p->real) STAGE(ST_BASIS, launch_so3_c2r(p->d_fc, coeffs, true, L, b, st));
     } else {
-        CK(launch_fft_lines(fft_rows(p, grid, p->d_work, (long long)b * N, p->real, false), st));
+        STAGE(ST_FFT_ROWS, launch_fft_lines(fft_rows(p, grid, p->d_work, (long long)b * N, p->real, false), st));
         double2* Fout = p->real ? (double2*)p->d_fc : (double2*)coeffs;
-        CK(launch_s2_fwd_fp64(p->d_table, p->d_goff, (const double2*)p->d_work, p->d_w, Fout, L, N, b, p->real, st));
-        if (p->real) CK(launch_s2_c2r(p->d_fc, coeffs, true, L, b, st));
+        STAGE(ST_FP64_FWD, launch_s2_fwd_fp64(p->d_table, p->d_goff, (const double2*)p->d_work, p->d_w, Fout, L, N,
+                                              b, p->real, st));
+        if (p->real) STAGE(ST_BASIS, launch_s2_c2r(p->d_fc, coeffs, true, L, b, st));
     }
     return FFTSO3_SUCCESS;
 }
@@ -207,27 +218,29 @@ int run_forward(fftso3_plan* p, const void* grid, void* coeffs, cudaStream_t st)
 int run_inverse(fftso3_plan* p, const void* coeffs, void* grid, cudaStream_t st)
 {
     const int N = p->N, L = p->L, b = p->batch;
-    if (p->precision == FFTSO3_PREC_TC_BF16X3) return tc_inverse(p->tc, coeffs, grid, st, g_err);
+    StageTimer& T = p->timer;
+    if (p->precision == FFTSO3_PREC_TC_BF16X3) return tc_inverse(p->tc, coeffs, grid, st, &T, g_err);
     if (p->so3) {
         const double2* Fin = (const double2*)coeffs;
         if (p->real) {
-            CK(launch_so3_r2c(coeffs, p->d_fc, true, L, b, st));
+            STAGE(ST_BASIS, launch_so3_r2c(coeffs, p->d_fc, true, L, b, st));
             Fin = (const double2*)p->d_fc;
         }
-        CK(launch_zero_nyquist_so3(p->d_work, true, N, (long long)b * N, st));
-        CK(launch_so3_inv_fp64(p->d_table, p->d_goff, Fin, (double2*)p->d_work, L, N, b, st));
-        CK(launch_fft_lines(fft_rows(p, p->d_work, p->d_work, (long long)b * N * N, false, false), st));
-        CK(launch_fft_lines(fft_cols(p, p->d_work, grid, (long long)b * N, p->real), st));
+        STAGE(ST_NYQUIST, launch_zero_nyquist_so3(p->d_work, true, N, (long long)b * N, st));
+        STAGE(ST_FP64_INV, launch_so3_inv_fp64(p->d_table, p->d_goff, Fin, (double2*)p->d_work, L, N, b, st));
+        STAGE(ST_FFT_ROWS, launch_fft_lines(fft_rows(p, p->d_work, p->d_work, (long long)b * N * N, false, false), st));
+        STAGE(ST_FFT_COLS, launch_fft_lines(fft_cols(p, p->d_work, grid, (long long)b * N, p->real), st));
     } else {
         const double2* Fin = (const double2*)coeffs;
         if (p->real) {
-            CK(launch_s2_r2c(coeffs, p->d_fc, true, L, b, st));
+            STAGE(ST_BASIS, launch_s2_r2c(coeffs, p->d_fc, true, L, b, st));
             Fin = (const double2*)p->d_fc;
         }
-        CK(launch_zero_nyquist_s2(p->d_work, true, N, (long long)b * N, st));
-        CK(launch_s2_inv_fp64(p->d_table, p->d_goff, Fin, (double2*)p->d_work, L, N, b, st));
-        CK(launch_fft_lines(fft_rows(p, p->d_work, grid, (long long)b * N, false, p->real), st));
+        STAGE(ST_NYQUIST, launch_zero_nyquist_s2(p->d_work, true, N, (long long)b * N, st));
+        STAGE(ST_FP64_INV, launch_s2_inv_fp64(p->d_table, p->d_goff, Fin, (double2*)p->d_work, L, N, b, st));
+        STAGE(ST_FFT_ROWS, launch_fft_lines(fft_rows(p, p->d_work, grid, (long long)b * N, false, p->real), st));
     }
+#undef STAGE
     return FFTSO3_SUCCESS;
 }
 
@@ -425,6 +438,31 @@ int fftso3_plan_destroy(fftso3_plan* plan)
 }
 
 long long fftso3_plan_device_bytes(const fftso3_plan* plan) { return plan ? plan->bytes : -1; }
+
+int fftso3_plan_set_timing(fftso3_plan* plan, int enable)
+{
+    int rc = check_plan(plan);
+    if (rc) return rc;
+    plan->timer.enabled = (enable != 0);
+    return FFTSO3_SUCCESS;
+}
+
+int fftso3_stage_count(void) { return ST_COUNT; }
+
+const char* fftso3_stage_name(int stage) { return stage_name(stage); }
+
+int fftso3_plan_stage_times(fftso3_plan* plan, double* ms_total, long long* launches, int reset)
+{
+    int rc = check_plan(plan);
+    if (rc) return rc;
+    plan->timer.collect();
+    for (int i = 0; i < ST_COUNT; ++i) {
+        if (ms_total) ms_total[i] = plan->timer.total_ms[i];
+        if (launches) launches[i] = plan->timer.launches[i];
+    }
+    if (reset) plan->timer.reset();
+    return FFTSO3_SUCCESS;
+}
 
 int fftso3_plan_check(fftso3_plan* plan)
 {

@@ -46,6 +46,12 @@ constexpr int PLANE_BYTES = 128 * 128;        // 128 rows x 128 bytes
 constexpr int STAGE_BYTES = 6 * PLANE_BYTES;  // 3 A planes + 3 B planes
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*barriers*/ + 1024 /*alignment*/;
 constexpr int THREADS = 192;
+// TMEM accumulators: k-steps go round-robin to NKC chunk accumulators, and in
+// each chunk the leading product (x0 * y0) and the five smaller products
+// accumulate separately, so the small terms are never rounded against the
+// large running sum.  NACC * BN <= 512 TMEM columns.
+constexpr int NKC = 2;
+constexpr int NACC = 2 * NKC;
 constexpr long long WAIT_CYCLES = 2000000000LL;  // ~1 s at 2 GHz
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -199,7 +205,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"(BN));
+                     "r"(NACC * BN));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -260,7 +266,9 @@ __global__ void __launch_bounds__(THREADS, 1)
                         ad = smem_desc(abase + kk * UK * 128, PLANE_BYTES / 2, 1024);
                     }
                     bd = smem_desc(bbase + kk * UK * 2, 16, 1024);
-                    mma_bf16(tmem, ad, bd, idesc, (i > 0 || kk > 0 || q > 0) ? 1u : 0u);
+                    const int acc = (i % NKC) * 2 + (q == 0 ? 0 : 1);
+                    const bool first = (i < NKC) && kk == 0 && (q <= 1);
+                    mma_bf16(tmem + (uint32_t)(acc * BN), ad, bd, idesc, first ? 0u : 1u);
                 }
             }
             mma_commit(&empty[s]);
@@ -275,9 +283,21 @@ __global__ void __launch_bounds__(THREADS, 1)
         if (ok) {
             const GroupPairs P = group_pairs(m0, n0);
             const int N = args.N;
+            const int nacc = 2 * (nk < NKC ? nk : NKC);
             for (int chunk = 0; chunk < BN / 32; ++chunk) {
-                float v[32];
-                tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + chunk * 32, v);
+                double v[32];
+                {
+                    float u[32];
+                    tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + chunk * 32, u);
+#pragma unroll
+                    for (int t = 0; t < 32; ++t) v[t] = (double)u[t];
+                }
+                for (int j = 1; j < nacc; ++j) {
+                    float u[32];
+                    tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + j * BN + chunk * 32, u);
+#pragma unroll
+                    for (int t = 0; t < 32; ++t) v[t] += (double)u[t];
+                }
 #pragma unroll
                 for (int fl = 0; fl < 4; ++fl) {
                     const int f = (nt * BN + chunk * 32) / 8 + fl;
@@ -287,8 +307,9 @@ __global__ void __launch_bounds__(THREADS, 1)
                         if (r + mt * BM >= nl) continue;
                         float2* Fo = args.F + (long long)f * args.cstride;
                         for (int p = 0; p < P.np; ++p) {
-                            float sg = (float)P.sign[p];
-                            Fo[so3_idx(l, P.m[p], P.n[p])] = make_float2(sg * v[fl * 8 + 2 * p], sg * v[fl * 8 + 2 * p + 1]);
+                            const double sg = P.sign[p];
+                            Fo[so3_idx(l, P.m[p], P.n[p])] =
+                                make_float2((float)(sg * v[fl * 8 + 2 * p]), (float)(sg * v[fl * 8 + 2 * p + 1]));
                         }
                     } else {
                         const int k = mt * BM + r;
@@ -297,7 +318,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                         for (int p = 0; p < P.np; ++p) {
                             int pi = P.m[p] % N; if (pi < 0) pi += N;
                             int qi = P.n[p] % N; if (qi < 0) qi += N;
-                            Ho[(long long)pi * N + qi] = make_float2(v[fl * 8 + 2 * p], v[fl * 8 + 2 * p + 1]);
+                            Ho[(long long)pi * N + qi] = make_float2((float)v[fl * 8 + 2 * p], (float)v[fl * 8 + 2 * p + 1]);
                         }
                     }
                 }
@@ -308,7 +329,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     __syncthreads();
     if (warp == 1) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(NACC * BN));
     }
 }
 
@@ -626,17 +647,24 @@ static FFTLaunch fft_launch(const TCState* s, const void* in, void* out, bool co
         }                                                                  \
     } while (0)
 
-static int tc_forward_once(TCState* s, const float2* grid, float2* F, cudaStream_t st, std::string& err)
+static int tc_forward_once(TCState* s, const float2* grid, float2* F, cudaStream_t st, StageTimer* T,
+                           std::string& err)
 {
     const int N = s->N;
+    T->begin(ST_FFT_ROWS, st);
     TCK(launch_fft_lines(fft_launch(s, grid, s->d_work, false), st));
+    T->end(st);
+    T->begin(ST_FFT_COLS, st);
     TCK(launch_fft_lines(fft_launch(s, s->d_work, s->d_work, true), st));
+    T->end(st);
     {
+        T->begin(ST_PACK_FWD, st);
         long long tot = (long long)s->ngroups * s->ncols * s->Kp;
         pack_fwd_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(s->d_work, s->d_w, s->d_x[0], s->d_x[1],
                                                                         s->d_x[2], s->L, N, s->Kp, s->ncols, s->batch,
                                                                         s->ngroups);
         TCK(cudaGetLastError());
+        T->end(st);
     }
     GemmArgs a;
     a.items = s->d_items_fwd;
@@ -651,23 +679,30 @@ static int tc_forward_once(TCState* s, const float2* grid, float2* F, cudaStream
     a.H = nullptr;
     a.err = s->d_err;
     dim3 lg(s->n_items_fwd, s->ncols / BN);
+    T->begin(ST_GEMM_FWD, st);
     so3_tc_gemm_kernel<true><<<lg, THREADS, SMEM_BYTES, st>>>(s->tmA_fwd[0], s->tmA_fwd[1], s->tmA_fwd[2], s->tmX[0],
                                                                 s->tmX[1], s->tmX[2], a);
     TCK(cudaGetLastError());
+    T->end(st);
     return FFTSO3_SUCCESS;
 }
 
-static int tc_inverse_once(TCState* s, const float2* F, float2* grid, cudaStream_t st, std::string& err)
+static int tc_inverse_once(TCState* s, const float2* F, float2* grid, cudaStream_t st, StageTimer* T,
+                           std::string& err)
 {
     const int N = s->N;
     {
+        T->begin(ST_PACK_INV, st);
         long long tot = (long long)s->ngroups * s->ncols * s->KLp;
         pack_inv_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(F, s->d_y[0], s->d_y[1], s->d_y[2], s->L,
                                                                         s->KLp, s->ncols, s->batch, s->ngroups,
                                                                         so3_off(s->B));
         TCK(cudaGetLastError());
+        T->end(st);
     }
+    T->begin(ST_NYQUIST, st);
     TCK(launch_zero_nyquist_so3(s->d_work, false, N, (long long)s->batch * N, st));
+    T->end(st);
     GemmArgs a;
     a.items = s->d_items_inv;
     a.grow0 = s->d_grow0;
@@ -681,11 +716,17 @@ static int tc_inverse_once(TCState* s, const float2* F, float2* grid, cudaStream
     a.H = s->d_work;
     a.err = s->d_err;
     dim3 lg(s->n_items_inv, s->ncols / BN);
+    T->begin(ST_GEMM_INV, st);
     so3_tc_gemm_kernel<false><<<lg, THREADS, SMEM_BYTES, st>>>(s->tmA_inv[0], s->tmA_inv[1], s->tmA_inv[2],
                                                                  s->tmY[0], s->tmY[1], s->tmY[2], a);
     TCK(cudaGetLastError());
+    T->end(st);
+    T->begin(ST_FFT_ROWS, st);
     TCK(launch_fft_lines(fft_launch(s, s->d_work, s->d_work, false), st));
+    T->end(st);
+    T->begin(ST_FFT_COLS, st);
     TCK(launch_fft_lines(fft_launch(s, s->d_work, grid, true), st));
+    T->end(st);
     return FFTSO3_SUCCESS;
 }
 
@@ -705,25 +746,29 @@ __global__ void add_kernel(float2* __restrict__ F, const float2* __restrict__ d,
     F[i] = make_float2(a.x + b.x, a.y + b.y);
 }
 
-int tc_forward(TCState* s, const void* grid, void* coeffs, cudaStream_t st, std::string& err)
+int tc_forward(TCState* s, const void* grid, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err)
 {
-    int rc = tc_forward_once(s, (const float2*)grid, (float2*)coeffs, st, err);
+    int rc = tc_forward_once(s, (const float2*)grid, (float2*)coeffs, st, T, err);
     if (rc || !s->refine) return rc;
     // one residual step: F += forward(f - inverse(F))
     const long long ng = (long long)s->batch * s->N * s->N * s->N;
     const long long nc = (long long)s->batch * so3_off(s->B);
-    if ((rc = tc_inverse_once(s, (const float2*)coeffs, s->d_resid, st, err))) return rc;
+    if ((rc = tc_inverse_once(s, (const float2*)coeffs, s->d_resid, st, T, err))) return rc;
+    T->begin(ST_REFINE, st);
     resid_kernel<<<(unsigned)((ng + 255) / 256), 256, 0, st>>>((const float2*)grid, s->d_resid, ng);
     TCK(cudaGetLastError());
-    if ((rc = tc_forward_once(s, s->d_resid, s->d_coef2, st, err))) return rc;
+    T->end(st);
+    if ((rc = tc_forward_once(s, s->d_resid, s->d_coef2, st, T, err))) return rc;
+    T->begin(ST_REFINE, st);
     add_kernel<<<(unsigned)((nc + 255) / 256), 256, 0, st>>>((float2*)coeffs, s->d_coef2, nc);
     TCK(cudaGetLastError());
+    T->end(st);
     return FFTSO3_SUCCESS;
 }
 
-int tc_inverse(TCState* s, const void* coeffs, void* grid, cudaStream_t st, std::string& err)
+int tc_inverse(TCState* s, const void* coeffs, void* grid, cudaStream_t st, StageTimer* T, std::string& err)
 {
-    return tc_inverse_once(s, (const float2*)coeffs, (float2*)grid, st, err);
+    return tc_inverse_once(s, (const float2*)coeffs, (float2*)grid, st, T, err);
 }
 
 int tc_status(TCState* s)

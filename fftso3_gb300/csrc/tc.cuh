@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "fft.cuh"
+#include "timing.cuh"
 
 namespace fftso3 {
 
@@ -15,8 +16,8 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
               std::string& err);
 void tc_destroy(TCState* s);
 long long tc_device_bytes(const TCState* s);
-int tc_forward(TCState* s, const void* grid, void* coeffs, cudaStream_t st, std::string& err);
-int tc_inverse(TCState* s, const void* coeffs, void* grid, cudaStream_t st, std::string& err);
+int tc_forward(TCState* s, const void* grid, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err);
+int tc_inverse(TCState* s, const void* coeffs, void* grid, cudaStream_t st, StageTimer* T, std::string& err);
 // Device error word of the tensor-core kernels (0 = no bounded wait timed out); synchronising read.
 int tc_status(TCState* s);
 

@@ -90,6 +90,18 @@ int fftso3_plan_destroy(fftso3_plan* plan);
 /* Device bytes held by the plan (tables + workspace). */
 long long fftso3_plan_device_bytes(const fftso3_plan* plan);
 
+/* Per-stage timing (tracing).  With timing enabled every internal kernel
+ * launch of the plan is bracketed by CUDA events on the caller's stream;
+ * fftso3_plan_stage_times() waits for them and returns, per stage, the summed
+ * milliseconds and the number of launches (arrays of fftso3_stage_count()
+ * entries), optionally resetting the totals.  Stage i is named
+ * fftso3_stage_name(i).  No reference counterpart (the reference times whole
+ * calls with fdcl::tictoc, src/fdcl_tictoc.cpp:4-22). */
+int fftso3_plan_set_timing(fftso3_plan* plan, int enable);
+int fftso3_stage_count(void);
+const char* fftso3_stage_name(int stage);
+int fftso3_plan_stage_times(fftso3_plan* plan, double* ms_total, long long* launches, int reset);
+
 /* Synchronise the plan's device and report failures of earlier asynchronous
  * calls, including a tensor-core kernel that gave up one of its bounded waits
  * (its kernels never spin without limit; they record an error code instead).

@@ -335,7 +335,21 @@ static void dft2_slice(int N, double *s, const double *tw)
  * replaced by the sampled grid f[k][j1][j2] (complex); the OpenMP structure is
  * the reference's: per-k local coefficients zeroed, accumulated, then merged
  * into F under a critical section. */
+static void so3_forward_complex_range(int l_max, const double *grid, int is_real, double *F, int k0, int k1);
+
 void orc_so3_forward_complex(int l_max, const double *grid, int is_real, double *F)
+{
+    so3_forward_complex_range(l_max, grid, is_real, F, 0, 2 * (l_max + 1));
+}
+
+/* The slices k in [k0, k1) of the forward sum (bounded CPU timing samples);
+ * grid holds only those slices, grid[(k - k0)][j1][j2]. */
+void orc_so3_forward_complex_slices(int l_max, const double *grid, double *F, int k0, int k1)
+{
+    so3_forward_complex_range(l_max, grid - 2L * k0 * (2 * (l_max + 1)) * (2 * (l_max + 1)), 0, F, k0, k1);
+}
+
+static void so3_forward_complex_range(int l_max, const double *grid, int is_real, double *F, int k0, int k1)
 {
     int B = l_max + 1, N = 2 * B;
     long C = so3_off(l_max + 1);
@@ -351,7 +365,7 @@ void orc_so3_forward_complex(int l_max, const double *grid, int is_real, double 
         double *F_k = (double *)malloc(sizeof(double) * 2L * N * N);
         int k;
 #pragma omp for schedule(static)
-        for (k = 0; k < N; k++) {
+        for (k = k0; k < k1; k++) {
             double beta = orc_beta_k(B, k);
             memcpy(F_k, grid + 2L * k * N * N, sizeof(double) * 2L * N * N);
             dft2_slice(N, F_k, tw);
@@ -614,7 +628,20 @@ double orc_so3_inverse_real_point(int l_max, const double *F, double alpha, doub
  * every grid point, done separably per beta_k: Fmn(m,n) as the reference
  * forms it, then the alpha and gamma sums with the reference's exponentials
  * exp(-i m alpha_j1), exp(-i n gamma_j2).  O(B^4) instead of O(B^6). */
+static void so3_inverse_complex_range(int l_max, const double *F, double *grid, int k0, int k1);
+
 void orc_so3_inverse_complex_grid(int l_max, const double *F, double *grid)
+{
+    so3_inverse_complex_range(l_max, F, grid, 0, 2 * (l_max + 1));
+}
+
+/* The slices k in [k0, k1) of the grid synthesis, written to grid[(k - k0)][j1][j2]. */
+void orc_so3_inverse_complex_slices(int l_max, const double *F, double *grid, int k0, int k1)
+{
+    so3_inverse_complex_range(l_max, F, grid - 2L * k0 * (2 * (l_max + 1)) * (2 * (l_max + 1)), k0, k1);
+}
+
+static void so3_inverse_complex_range(int l_max, const double *F, double *grid, int k0, int k1)
 {
     int B = l_max + 1, N = 2 * B, W = 2 * l_max + 1;
     double *ex = (double *)malloc(sizeof(double) * 2L * N * W);
@@ -632,7 +659,7 @@ void orc_so3_inverse_complex_grid(int l_max, const double *F, double *grid)
         double *T = (double *)malloc(sizeof(double) * 2L * N * W);
         int k;
 #pragma omp for schedule(static)
-        for (k = 0; k < N; k++) {
+        for (k = k0; k < k1; k++) {
             orc_wigner_d(orc_beta_k(B, k), l_max, d);
             for (int m = -l_max; m <= l_max; m++)
                 for (int n = -l_max; n <= l_max; n++) {

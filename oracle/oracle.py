@@ -59,6 +59,8 @@ def lib():
             "orc_so3_inverse_real_point": (d, [i, _dp, d, d, d]),
             "orc_so3_real_harmonics": (None, [i, d, d, d, _dp]),
             "orc_so3_inverse_complex_grid": (None, [i, _dp, _dp]),
+            "orc_so3_forward_complex_slices": (None, [i, _dp, _dp, i, i]),
+            "orc_so3_inverse_complex_slices": (None, [i, _dp, _dp, i, i]),
             "orc_so3_inverse_real_grid": (None, [i, _dp, _dp]),
             "orc_so3_real_to_complex": (None, [i, _dp, _dp]),
             "orc_s2_forward_complex": (None, [i, _dp, i, _dp]),
@@ -195,6 +197,26 @@ def so3_inverse_complex_grid(l_max: int, F: np.ndarray) -> np.ndarray:
     F = np.ascontiguousarray(F, dtype=np.complex128)
     g = np.zeros((N, N, N), dtype=np.complex128)
     lib().orc_so3_inverse_complex_grid(l_max, _p(F.view(np.float64)), _p(g.view(np.float64)))
+    return g
+
+
+def so3_forward_complex_slices(l_max: int, slab: np.ndarray, k0: int, k1: int) -> np.ndarray:
+    """Contribution of the beta slices k0..k1-1 to the complex forward sum
+    (slab: (k1-k0, N, N) complex); used for bounded CPU timing samples."""
+    N = 2 * (l_max + 1)
+    g = np.ascontiguousarray(slab, dtype=np.complex128)
+    assert g.shape == (k1 - k0, N, N)
+    F = np.zeros(so3_ncoeff(l_max), dtype=np.complex128)
+    lib().orc_so3_forward_complex_slices(l_max, _p(g.view(np.float64)), _p(F.view(np.float64)), k0, k1)
+    return F
+
+
+def so3_inverse_complex_slices(l_max: int, F: np.ndarray, k0: int, k1: int) -> np.ndarray:
+    """Grid synthesis of the beta slices k0..k1-1 only: (k1-k0, N, N) complex."""
+    N = 2 * (l_max + 1)
+    F = np.ascontiguousarray(F, dtype=np.complex128)
+    g = np.zeros((k1 - k0, N, N), dtype=np.complex128)
+    lib().orc_so3_inverse_complex_slices(l_max, _p(F.view(np.float64)), _p(g.view(np.float64)), k0, k1)
     return g
 
 
