@@ -204,6 +204,7 @@ def main() -> None:
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64 reference (profiling runs)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -241,12 +242,15 @@ def main() -> None:
     F0 = seeded_coeffs(L, 1000 * rank)
     fp64 = None
     acc = {}
-    p64 = _lib.Plan(_lib.SO3_COMPLEX, L, 1, "fp64", "stable")
+    if args.no_accuracy:
+        args.no_fp64 = True
+    p64 = None if args.no_accuracy else _lib.Plan(_lib.SO3_COMPLEX, L, 1, "fp64", "stable")
     c64 = torch.from_numpy(F0).to(dev)
     g64 = torch.empty(N ** 3, dtype=torch.complex128, device=dev)
     o64 = torch.empty_like(c64)
-    p64.inverse(c64.data_ptr(), g64.data_ptr(), sp)
-    p64.forward(g64.data_ptr(), o64.data_ptr(), sp)
+    if p64 is not None:
+        p64.inverse(c64.data_ptr(), g64.data_ptr(), sp)
+        p64.forward(g64.data_ptr(), o64.data_ptr(), sp)
     torch.cuda.synchronize()
     F0_fp64 = o64.cpu().numpy()  # FP64 forward of the FP64 synthesis
     g0_c64 = g64.to(torch.complex64)
@@ -272,7 +276,8 @@ def main() -> None:
     coef = torch.from_numpy(Fb).to(dev)
     grid = torch.empty(b * N ** 3, dtype=torch.complex64, device=dev)
     plan.inverse(coef.data_ptr(), grid.data_ptr(), sp)  # synthetic band-limited inputs
-    grid[:N ** 3].copy_(g0_c64)                         # function 0: the FP64 synthesis
+    if not args.no_accuracy:
+        grid[:N ** 3].copy_(g0_c64)                     # function 0: the FP64 synthesis
     coef_out = torch.empty_like(coef)
     grid_out = torch.empty_like(grid)
     torch.cuda.synchronize()
@@ -282,16 +287,17 @@ def main() -> None:
     coef0 = torch.from_numpy(F0.astype(np.complex64)).to(dev)
     coef_in = coef.clone()
     coef_in[:C].copy_(coef0)
-    plan.forward(grid.data_ptr(), coef_out.data_ptr(), sp)
-    plan.inverse(coef_in.data_ptr(), grid_out.data_ptr(), sp)
-    torch.cuda.synchronize()
-    plan.check()
-    fr, fm = per_l_errors(coef_out[:C].cpu().numpy().astype(np.complex128), F0_fp64, L)
-    gi = grid_out[:N ** 3].cpu().numpy().astype(np.complex128)
-    ir = float(np.linalg.norm(gi - g0_ref) / np.linalg.norm(g0_ref))
-    im = float(np.abs(gi - g0_ref).max() / np.sqrt(np.mean(np.abs(g0_ref) ** 2)))
-    acc = {"forward_rel_rms": fr, "forward_rel_max_per_l": fm, "inverse_rel_rms": ir, "inverse_rel_max": im,
-           "against": "FP64 GPU path (stable recursion) on the same function"}
+    if not args.no_accuracy:
+        plan.forward(grid.data_ptr(), coef_out.data_ptr(), sp)
+        plan.inverse(coef_in.data_ptr(), grid_out.data_ptr(), sp)
+        torch.cuda.synchronize()
+        plan.check()
+        fr, fm = per_l_errors(coef_out[:C].cpu().numpy().astype(np.complex128), F0_fp64, L)
+        gi = grid_out[:N ** 3].cpu().numpy().astype(np.complex128)
+        ir = float(np.linalg.norm(gi - g0_ref) / np.linalg.norm(g0_ref))
+        im = float(np.abs(gi - g0_ref).max() / np.sqrt(np.mean(np.abs(g0_ref) ** 2)))
+        acc = {"forward_rel_rms": fr, "forward_rel_max_per_l": fm, "inverse_rel_rms": ir,
+               "inverse_rel_max": im, "against": "FP64 GPU path (stable recursion) on the same function"}
     del coef_in, coef0
 
     # ---- timed region: inputs resident in HBM (each grid 1 GB >> 129 MB L2)
