@@ -400,7 +400,7 @@ def main() -> None:
             "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "bf16x3 (split) / fp32 accumulate / fp32 FFT", "data": "synthetic",
             "config": {"workload": f"SO(3) complex forward+inverse, l_max={L}, batch={b} functions per GPU "
-                                   f"(512^3 complex64 grid each), TC split-BF16, stable recursion",
+                                   f"({N}^3 complex64 grid each), TC split-BF16, stable recursion",
                        "l_max": L, "batch_per_gpu": b, "precision": "tc_bf16x3",
                        "l2": "inputs larger than L2 (1 GB grid per function)"},
             "e2e": e2e, "gpu_launches": launches, "roofline": roof, "stages": stage_summary,

@@ -12,20 +12,29 @@
 // 24 significant bits) and the six products with i + j <= 2 are accumulated
 // by tcgen05.mma (kind::f16, BF16 inputs, FP32 accumulator in TMEM).
 //
-// Kernel structure (one CTA per (group, 128-row tile, 128-column tile)):
-//   warp 0: TMA producer (cp.async.bulk.tensor, 128B swizzle) into a 2-stage ring
-//   warp 1: TMEM allocator and single-thread tcgen05.mma issuer; tcgen05.commit
-//           releases ring slots and finally signals the accumulator
-//   warps 2-5: epilogue, tcgen05.ld 32x32b from their TMEM lane quarter, scatter
-//           to the coefficient vector (forward) or the grid work buffer (inverse)
+// Data path.  The 2-D FFT output is transposed to k-contiguous pencils
+// G'[fn][p][q][k], so each (function, pair) column of X_g is one contiguous
+// run.  The GEMM is persistent (one CTA per SM walking a work list of
+// (group, row tile, column tile) items) and warp-specialised:
+//   warp 0     TMA producer of the table tiles (cp.async.bulk.tensor, 128-byte
+//              swizzle; the three BF16 planes of the table are precomputed);
+//   warp 1     TMEM owner and single-thread tcgen05.mma issuer;
+//   warps 2-5  B-operand producers: gather X (pencils) or Y (coefficients)
+//              in FP32, split each value into three BF16 terms and store them
+//              straight into the swizzled shared-memory tile;
+//   warps 6-9  epilogue: tcgen05.ld from a double-buffered TMEM accumulator,
+//              then the forward scatters coefficients and the inverse writes
+//              k-contiguous pencils H'[fn][p][q][k] (coalesced).
 // The forward reads the table K-major (k contiguous); the inverse reads the
 // same table as an MN-major operand (M = k), so one table serves both.
-// Every mbarrier wait is bounded (about one second of clock64 time); on
-// timeout the kernel records an error code and unwinds, freeing its TMEM.
+// All arithmetic in these kernels is FP32/BF16 (the FP64 pipe is slow on this
+// part).  Every mbarrier wait is bounded (about one second of clock64 time);
+// on timeout the kernel records an error code and unwinds, freeing its TMEM.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "../../include/fftso3_gb300.h"
@@ -38,20 +47,24 @@ namespace fftso3 {
 namespace tc {
 
 constexpr int BM = 128;          // MMA M (rows of the accumulator = TMEM lanes)
-constexpr int BN = 128;          // MMA N (accumulator columns)
+constexpr int BN = 128;          // MMA N (accumulator columns = 16 functions x 4 pairs x re/im)
+constexpr int FPT = BN / 8;      // functions per column tile
 constexpr int BK = 64;           // k-step per ring slot (one 128-byte swizzle row of BF16)
 constexpr int UK = 16;           // K per tcgen05.mma (kind::f16)
 constexpr int STAGES = 2;
 constexpr int PLANE_BYTES = 128 * 128;        // 128 rows x 128 bytes
-constexpr int STAGE_BYTES = 6 * PLANE_BYTES;  // 3 A planes + 3 B planes
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*barriers*/ + 1024 /*alignment*/;
-constexpr int THREADS = 192;
-// TMEM accumulators: k-steps go round-robin to NKC chunk accumulators, and in
-// each chunk the leading product (x0 * y0) and the five smaller products
-// accumulate separately, so the small terms are never rounded against the
-// large running sum.  NACC * BN <= 512 TMEM columns.
-constexpr int NKC = 2;
-constexpr int NACC = 2 * NKC;
+constexpr int STAGE_A = 3 * PLANE_BYTES;      // three BF16 planes of the table tile (TMA)
+constexpr int STAGE_BYTES = 6 * PLANE_BYTES;  // + three planes of the B tile (producer warps)
+constexpr int NPROD = 4;                      // B-producer warps
+constexpr int NEPI = 4;                       // epilogue warps
+constexpr int THREADS = 32 * (2 + NPROD + NEPI);
+constexpr int MAXN = 1024;                    // weights staged in shared memory
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 256 /*barriers*/ + 4 * MAXN /*weights*/ + 1024 /*alignment*/;
+// TMEM: two accumulator buffers (double-buffered across work items); in each
+// the leading product (x0 * y0) and the five smaller products accumulate in
+// separate 128-column halves, so the small terms are never rounded against
+// the large running sum.
+constexpr int TMEM_COLS = 512;
 constexpr long long WAIT_CYCLES = 2000000000LL;  // ~1 s at 2 GHz
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -156,56 +169,102 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void split3f(float x, uint16_t& h, uint16_t& m, uint16_t& l)
+{
+    __nv_bfloat16 a = __float2bfloat16_rn(x);
+    float r = x - __bfloat162float(a);
+    __nv_bfloat16 b = __float2bfloat16_rn(r);
+    r -= __bfloat162float(b);
+    __nv_bfloat16 c = __float2bfloat16_rn(r);
+    h = __bfloat16_as_ushort(a);
+    m = __bfloat16_as_ushort(b);
+    l = __bfloat16_as_ushort(c);
+}
+
 struct GemmArgs {
-    const int2* items;         // (group, row tile)
+    const int4* items;         // (group, row tile, column tile, -)
+    int nitems;
     const long long* grow0;    // first table row of each group
-    int L, N, ncols, batch;
-    int nk_fixed;              // forward: k-steps over the beta axis (Kp / BK)
+    int L, N, Kp, batch;
+    long long fstride;         // pencil elements per function (N^3)
     long long cstride;         // coefficients per function
-    float2* F;                 // forward output coefficients [batch][C]
-    float2* H;                 // inverse output work grid [batch][N][N][N]
+    const float2* pin;         // forward: input pencils G'[fn][p][q][k]
+    const float2* cin;         // inverse: input coefficients
+    float2* cout;              // forward: output coefficients
+    float2* pout;              // inverse: output pencils H'[fn][p][q][k]
+    const float* wf;           // forward: quadrature weights (FP32)
     int* err;
 };
 
-// FWD = true: A = table (K-major, rows l), B = X planes; D[l][c].
-// FWD = false: A = table^T (MN-major, rows k), B = Y planes; D[k][c].
+// Store 8 consecutive k values (one 16-byte chunk) of row R of each BF16 plane.
+__device__ __forceinline__ void store_chunk(uint32_t bplanes, int R, int chunk, const float* x8)
+{
+    uint32_t w[3][4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        uint16_t h0, m0, l0, h1, m1, l1;
+        split3f(x8[2 * j], h0, m0, l0);
+        split3f(x8[2 * j + 1], h1, m1, l1);
+        w[0][j] = (uint32_t)h0 | ((uint32_t)h1 << 16);
+        w[1][j] = (uint32_t)m0 | ((uint32_t)m1 << 16);
+        w[2][j] = (uint32_t)l0 | ((uint32_t)l1 << 16);
+    }
+    const uint32_t off = (uint32_t)R * 128u + (uint32_t)((chunk ^ (R & 7)) * 16);
+#pragma unroll
+    for (int pl = 0; pl < 3; ++pl) {
+        asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(bplanes + pl * PLANE_BYTES + off),
+                     "r"(w[pl][0]), "r"(w[pl][1]), "r"(w[pl][2]), "r"(w[pl][3])
+                     : "memory");
+    }
+}
+
+// FWD = true: A = table (K-major, rows l), B = X from pencils; D[l][c].
+// FWD = false: A = table^T (MN-major, rows k), B = Y from coefficients; D[k][c].
 template <bool FWD>
 __global__ void __launch_bounds__(THREADS, 1)
     so3_tc_gemm_kernel(const __grid_constant__ CUtensorMap tA0, const __grid_constant__ CUtensorMap tA1,
-                       const __grid_constant__ CUtensorMap tA2, const __grid_constant__ CUtensorMap tB0,
-                       const __grid_constant__ CUtensorMap tB1, const __grid_constant__ CUtensorMap tB2,
-                       GemmArgs args)
+                       const __grid_constant__ CUtensorMap tA2, GemmArgs args)
 {
     extern __shared__ unsigned char smem_raw[];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
     uint64_t* empty = full + STAGES;
     uint64_t* accf = empty + STAGES;
-    uint32_t* tmem_slot = (uint32_t*)(accf + 1);
+    uint64_t* acce = accf + 2;
+    uint32_t* tmem_slot = (uint32_t*)(acce + 2);
     volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+    float* wsm = (float*)(smem + STAGES * STAGE_BYTES + 256);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int2 item = args.items[blockIdx.x];
-    const int g = item.x, mt = item.y, nt = blockIdx.y;
-    int m0, n0;
-    group_mn(g, m0, n0);
-    const int B = args.L + 1;
-    const int nl = B - m0;
-    const int nk = FWD ? args.nk_fixed : (nl + BK - 1) / BK;
-    const long long row0 = args.grow0[g];
+    const int B = args.L + 1, N = args.N;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
-            mbar_init(&full[s], 1);
+            mbar_init(&full[s], 1 + NPROD);
             mbar_init(&empty[s], 1);
         }
-        mbar_init(accf, 1);
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&accf[b], 1);
+            mbar_init(&acce[b], NEPI);
+        }
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    if (FWD)
+        for (int i = threadIdx.x; i < N; i += THREADS) wsm[i] = args.wf[i];
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"(NACC * BN));
+                     "r"(TMEM_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -213,138 +272,241 @@ __global__ void __launch_bounds__(THREADS, 1)
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
 
-    if (warp == 0 && lane == 0) {
-        // ---------------- TMA producer
-        const CUtensorMap* tA[3] = {&tA0, &tA1, &tA2};
-        const CUtensorMap* tB[3] = {&tB0, &tB1, &tB2};
-        const int brow = g * args.ncols + nt * BN;
-        for (int i = 0; i < nk && !*abort_flag; ++i) {
-            const int s = i % STAGES;
-            if (i >= STAGES && !mbar_wait(&empty[s], ((i / STAGES) - 1) & 1, args.err, 1)) {
+    if (warp == 0) {
+        if (lane == 0) {
+            // ---------------- TMA producer of the table tiles
+            const CUtensorMap* tA[3] = {&tA0, &tA1, &tA2};
+            int kc = 0;
+            for (int it = blockIdx.x; it < args.nitems && !*abort_flag; it += gridDim.x) {
+                const int4 item = args.items[it];
+                int m0, n0;
+                group_mn(item.x, m0, n0);
+                const int nk = FWD ? args.Kp / BK : (B - m0 + BK - 1) / BK;
+                const long long row0 = args.grow0[item.x];
+                for (int i = 0; i < nk; ++i, ++kc) {
+                    const int s = kc % STAGES;
+                    if (kc >= STAGES && !mbar_wait(&empty[s], ((kc / STAGES) - 1) & 1, args.err, 1)) {
+                        *abort_flag = 1;
+                        break;
+                    }
+                    unsigned char* st = smem + s * STAGE_BYTES;
+                    mbar_expect_tx(&full[s], STAGE_A);
+                    for (int p = 0; p < 3; ++p) {
+                        unsigned char* a = st + p * PLANE_BYTES;
+                        if (FWD) {
+                            tma_load_2d(a, tA[p], i * BK, (int)(row0 + (long long)item.y * BM), &full[s]);
+                        } else {
+                            const int y = (int)(row0 + (long long)i * BK);
+                            tma_load_2d(a, tA[p], item.y * BM, y, &full[s]);
+                            tma_load_2d(a + PLANE_BYTES / 2, tA[p], item.y * BM + 64, y, &full[s]);
+                        }
+                    }
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // ---------------- MMA issuer
+            constexpr uint32_t idesc = idesc_bf16(!FWD);
+            const int pa[6] = {0, 0, 1, 0, 1, 2};
+            const int pb[6] = {0, 1, 0, 2, 1, 0};
+            int kc = 0, t = 0;
+            for (int it = blockIdx.x; it < args.nitems && !*abort_flag; it += gridDim.x, ++t) {
+                const int4 item = args.items[it];
+                int m0, n0;
+                group_mn(item.x, m0, n0);
+                const int nk = FWD ? args.Kp / BK : (B - m0 + BK - 1) / BK;
+                const int ab = t & 1;
+                if (t >= 2 && !mbar_wait(&acce[ab], ((t >> 1) - 1) & 1, args.err, 2)) {
+                    *abort_flag = 1;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t dhi = tmem + (uint32_t)(ab * 256), dlo = dhi + 128;
+                bool ok = true;
+                for (int i = 0; i < nk; ++i, ++kc) {
+                    const int s = kc % STAGES;
+                    if (!mbar_wait(&full[s], (kc / STAGES) & 1, args.err, 3)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
+#pragma unroll
+                    for (int kk = 0; kk < BK / UK; ++kk) {
+#pragma unroll
+                        for (int q = 0; q < 6; ++q) {
+                            const uint32_t abase = st + pa[q] * PLANE_BYTES;
+                            const uint32_t bbase = st + STAGE_A + pb[q] * PLANE_BYTES;
+                            const uint64_t ad = FWD ? smem_desc(abase + kk * UK * 2, 16, 1024)
+                                                    : smem_desc(abase + kk * UK * 128, PLANE_BYTES / 2, 1024);
+                            const uint64_t bd = smem_desc(bbase + kk * UK * 2, 16, 1024);
+                            const bool first = (i == 0) && kk == 0 && q <= 1;
+                            mma_bf16(q == 0 ? dhi : dlo, ad, bd, idesc, first ? 0u : 1u);
+                        }
+                    }
+                    mma_commit(&empty[s]);
+                }
+                mma_commit(&accf[ab]);
+                if (!ok) {
+                    *abort_flag = 1;
+                    ++t;
+                    break;
+                }
+            }
+            // the accumulator commits of the last item(s) must land before TMEM is freed
+            for (int u = (t >= 2 ? t - 2 : 0); u < t; ++u) mbar_wait(&accf[u & 1], (u >> 1) & 1, args.err, 6);
+        }
+    } else if (warp < 2 + NPROD) {
+        // ---------------- B-operand producers (128 threads)
+        const int pt = threadIdx.x - 64;
+        const int c = pt >> 1, half = pt & 1;          // column pair (function, pair) and k half
+        const int fl = c >> 2, pp = c & 3;
+        const int Rre = fl * 8 + 2 * pp, Rim = Rre + 1;
+        int kc = 0;
+        for (int it = blockIdx.x; it < args.nitems && !*abort_flag; it += gridDim.x) {
+            const int4 item = args.items[it];
+            int m0, n0;
+            group_mn(item.x, m0, n0);
+            const GroupPairs P = group_pairs(m0, n0);
+            const int nk = FWD ? args.Kp / BK : (B - m0 + BK - 1) / BK;
+            const int f = item.z * FPT + fl;
+            const bool valid = (f < args.batch) && (pp < P.np);
+            int pm = 0, pn = 0;
+            float sg = 1.f;
+            if (pp < P.np) {
+                pm = P.m[pp];
+                pn = P.n[pp];
+                sg = (float)P.sign[pp];
+            }
+            const float2* src = nullptr;
+            if (FWD && valid) {
+                int pi = (-pm) % N; if (pi < 0) pi += N;
+                int qi = (-pn) % N; if (qi < 0) qi += N;
+                src = args.pin + (long long)f * args.fstride + ((long long)pi * N + qi) * N;
+            }
+            const float2* csrc = (!FWD && valid) ? args.cin + (long long)f * args.cstride : nullptr;
+            bool stop = false;
+            for (int i = 0; i < nk; ++i, ++kc) {
+                const int s = kc % STAGES;
+                if (kc >= STAGES && !mbar_wait(&empty[s], ((kc / STAGES) - 1) & 1, args.err, 4)) {
+                    stop = true;
+                    break;
+                }
+                const uint32_t bpl = smem_u32(smem + s * STAGE_BYTES + STAGE_A);
+#pragma unroll 1
+                for (int ch = 0; ch < 4; ++ch) {
+                    const int kl = half * 32 + ch * 8;        // local index of the chunk's first k (or l)
+                    float re[8], im[8];
+                    if (FWD) {
+                        const int k = i * BK + kl;
+                        if (valid && k + 8 <= N) {
+                            const float4* s4 = reinterpret_cast<const float4*>(src + k);
+#pragma unroll
+                            for (int j = 0; j < 4; ++j) {
+                                float4 v = __ldg(s4 + j);
+                                re[2 * j] = v.x * wsm[k + 2 * j];
+                                im[2 * j] = v.y * wsm[k + 2 * j];
+                                re[2 * j + 1] = v.z * wsm[k + 2 * j + 1];
+                                im[2 * j + 1] = v.w * wsm[k + 2 * j + 1];
+                            }
+                        } else {
+#pragma unroll
+                            for (int j = 0; j < 8; ++j) {
+                                float2 v = (valid && k + j < N) ? src[k + j] : make_float2(0.f, 0.f);
+                                float wk = (valid && k + j < N) ? wsm[k + j] : 0.f;
+                                re[j] = v.x * wk;
+                                im[j] = v.y * wk;
+                            }
+                        }
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) {
+                            const int l = m0 + i * BK + kl + j;
+                            float2 v = make_float2(0.f, 0.f);
+                            if (valid && l <= args.L) v = __ldg(csrc + so3_idx(l, pm, pn));
+                            const float sc = (float)(2 * l + 1) * sg;
+                            re[j] = v.x * sc;
+                            im[j] = v.y * sc;
+                        }
+                    }
+                    store_chunk(bpl, Rre, kl >> 3, re);
+                    store_chunk(bpl, Rim, kl >> 3, im);
+                }
+                fence_proxy_async();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&full[s]);
+            }
+            if (stop) {
                 *abort_flag = 1;
                 break;
             }
-            unsigned char* st = smem + s * STAGE_BYTES;
-            mbar_expect_tx(&full[s], STAGE_BYTES);
-            for (int p = 0; p < 3; ++p) {
-                unsigned char* a = st + p * PLANE_BYTES;
-                if (FWD) {
-                    tma_load_2d(a, tA[p], i * BK, (int)(row0 + (long long)mt * BM), &full[s]);
-                } else {
-                    const int y = (int)(row0 + (long long)i * BK);
-                    tma_load_2d(a, tA[p], mt * BM, y, &full[s]);
-                    tma_load_2d(a + PLANE_BYTES / 2, tA[p], mt * BM + 64, y, &full[s]);
-                }
-                tma_load_2d(st + (3 + p) * PLANE_BYTES, tB[p], i * BK, brow, &full[s]);
-            }
         }
-    } else if (warp == 1 && lane == 0) {
-        // ---------------- MMA issuer
-        constexpr uint32_t idesc = idesc_bf16(!FWD);
-        // products (a, b) with a + b <= 2 of the 3-term splits
-        const int pa[6] = {0, 0, 1, 0, 1, 2};
-        const int pb[6] = {0, 1, 0, 2, 1, 0};
-        for (int i = 0; i < nk; ++i) {
-            const int s = i % STAGES;
-            if (!mbar_wait(&full[s], (i / STAGES) & 1, args.err, 2)) {
+    } else {
+        // ---------------- epilogue (4 warps, one TMEM lane quarter each)
+        const int quarter = warp & 3;
+        const int r = quarter * 32 + lane;
+        int t = 0;
+        for (int it = blockIdx.x; it < args.nitems && !*abort_flag; it += gridDim.x, ++t) {
+            const int4 item = args.items[it];
+            int m0, n0;
+            group_mn(item.x, m0, n0);
+            const GroupPairs P = group_pairs(m0, n0);
+            const int ab = t & 1;
+            if (!mbar_wait(&accf[ab], (t >> 1) & 1, args.err, 5)) {
                 *abort_flag = 1;
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
-#pragma unroll
-            for (int kk = 0; kk < BK / UK; ++kk) {
-#pragma unroll
-                for (int q = 0; q < 6; ++q) {
-                    uint64_t ad, bd;
-                    const uint32_t abase = st + pa[q] * PLANE_BYTES;
-                    const uint32_t bbase = st + (3 + pb[q]) * PLANE_BYTES;
-                    if (FWD) {
-                        ad = smem_desc(abase + kk * UK * 2, 16, 1024);
-                    } else {
-                        // MN-major: 64-wide k blocks 8 KB apart (LBO), 8-row l groups 1 KB apart (SBO)
-                        ad = smem_desc(abase + kk * UK * 128, PLANE_BYTES / 2, 1024);
-                    }
-                    bd = smem_desc(bbase + kk * UK * 2, 16, 1024);
-                    const int acc = (i % NKC) * 2 + (q == 0 ? 0 : 1);
-                    const bool first = (i < NKC) && kk == 0 && (q <= 1);
-                    mma_bf16(tmem + (uint32_t)(acc * BN), ad, bd, idesc, first ? 0u : 1u);
-                }
-            }
-            mma_commit(&empty[s]);
-        }
-        mma_commit(accf);
-    } else if (warp >= 2) {
-        // ---------------- epilogue
-        const int quarter = warp & 3;
-        const int r = quarter * 32 + lane;
-        const bool ok = mbar_wait(accf, 0, args.err, 3);
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        if (ok) {
-            const GroupPairs P = group_pairs(m0, n0);
-            const int N = args.N;
-            const int nacc = 2 * (nk < NKC ? nk : NKC);
+            const uint32_t trow = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(ab * 256);
             for (int chunk = 0; chunk < BN / 32; ++chunk) {
-                double v[32];
-                {
-                    float u[32];
-                    tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + chunk * 32, u);
+                float v[32], u[32];
+                tmem_ld32(trow + chunk * 32, v);
+                tmem_ld32(trow + 128 + chunk * 32, u);
 #pragma unroll
-                    for (int t = 0; t < 32; ++t) v[t] = (double)u[t];
-                }
-                for (int j = 1; j < nacc; ++j) {
-                    float u[32];
-                    tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + j * BN + chunk * 32, u);
+                for (int j = 0; j < 32; ++j) v[j] += u[j];
 #pragma unroll
-                    for (int t = 0; t < 32; ++t) v[t] += (double)u[t];
-                }
-#pragma unroll
-                for (int fl = 0; fl < 4; ++fl) {
-                    const int f = (nt * BN + chunk * 32) / 8 + fl;
+                for (int fq = 0; fq < 4; ++fq) {
+                    const int f = item.z * FPT + chunk * 4 + fq;
                     if (f >= args.batch) continue;
                     if (FWD) {
-                        const int l = m0 + mt * BM + r;
-                        if (r + mt * BM >= nl) continue;
-                        float2* Fo = args.F + (long long)f * args.cstride;
+                        const int row = item.y * BM + r;
+                        if (row >= B - m0) continue;
+                        const int l = m0 + row;
+                        float2* Fo = args.cout + (long long)f * args.cstride;
                         for (int p = 0; p < P.np; ++p) {
-                            const double sg = P.sign[p];
-                            Fo[so3_idx(l, P.m[p], P.n[p])] =
-                                make_float2((float)(sg * v[fl * 8 + 2 * p]), (float)(sg * v[fl * 8 + 2 * p + 1]));
+                            const float sg = (float)P.sign[p];
+                            Fo[so3_idx(l, P.m[p], P.n[p])] = make_float2(sg * v[fq * 8 + 2 * p], sg * v[fq * 8 + 2 * p + 1]);
                         }
                     } else {
-                        const int k = mt * BM + r;
+                        const int k = item.y * BM + r;
                         if (k >= N) continue;
-                        float2* Ho = args.H + (long long)f * N * N * N + (long long)k * N * N;
+                        float2* Ho = args.pout + (long long)f * args.fstride + k;
                         for (int p = 0; p < P.np; ++p) {
                             int pi = P.m[p] % N; if (pi < 0) pi += N;
                             int qi = P.n[p] % N; if (qi < 0) qi += N;
-                            Ho[(long long)pi * N + qi] = make_float2((float)v[fl * 8 + 2 * p], (float)v[fl * 8 + 2 * p + 1]);
+                            Ho[((long long)pi * N + qi) * N] = make_float2(v[fq * 8 + 2 * p], v[fq * 8 + 2 * p + 1]);
                         }
                     }
                 }
             }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acce[ab]);
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 1) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(NACC * BN));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
     }
 }
 
-// ------------------------------------------------------------ pack kernels
+// ------------------------------------------------------- helper kernels
 
-__device__ __forceinline__ void split3(double x, __nv_bfloat16& h, __nv_bfloat16& m, __nv_bfloat16& l)
-{
-    h = __double2bfloat16(x);
-    double r = x - (double)__bfloat162float(h);
-    m = __double2bfloat16(r);
-    r -= (double)__bfloat162float(m);
-    l = __double2bfloat16(r);
-}
-
-// FP64 table [rows][N] -> three BF16 planes [rows][Kp] (zero for k >= N).
+// FP64 table [rows][N] -> three BF16 planes [rows][Kp] (zero for k >= N);
+// the value is first rounded to FP32, whose 24 bits the three terms carry.
 __global__ void table_split_kernel(const double* __restrict__ t, __nv_bfloat16* __restrict__ p0,
                                    __nv_bfloat16* __restrict__ p1, __nv_bfloat16* __restrict__ p2, long long rows,
                                    int N, int Kp)
@@ -353,72 +515,60 @@ __global__ void table_split_kernel(const double* __restrict__ t, __nv_bfloat16* 
     if (i >= rows * Kp) return;
     long long r = i / Kp;
     int k = (int)(i % Kp);
-    double x = (k < N) ? t[r * N + k] : 0.0;
-    __nv_bfloat16 a, b, c;
-    split3(x, a, b, c);
-    p0[i] = a;
-    p1[i] = b;
-    p2[i] = c;
+    float x = (k < N) ? (float)t[r * N + k] : 0.f;
+    uint16_t a, b, c;
+    split3f(x, a, b, c);
+    p0[i] = __ushort_as_bfloat16(a);
+    p1[i] = __ushort_as_bfloat16(b);
+    p2[i] = __ushort_as_bfloat16(c);
 }
 
-// X planes [g * ncols + col][Kp]: col = f*8 + p*2 + (re/im); x = w_k G_k(-m_p, -n_p).
-__global__ void pack_fwd_kernel(const float2* __restrict__ G, const double* __restrict__ w,
-                                __nv_bfloat16* __restrict__ x0, __nv_bfloat16* __restrict__ x1,
-                                __nv_bfloat16* __restrict__ x2, int L, int N, int Kp, int ncols, int batch,
-                                int ngroups)
+// Batched 2-D transpose in[nb][R][Cc] -> out[nb][Cc][R] (complex64), 32x32 tiles.
+__global__ void transpose_kernel(const float2* __restrict__ in, float2* __restrict__ out, long long R, long long Cc)
 {
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    long long total = (long long)ngroups * ncols * Kp;
-    if (i >= total) return;
-    int k = (int)(i % Kp);
-    long long rc = i / Kp;
-    int col = (int)(rc % ncols);
-    int g = (int)(rc / ncols);
-    int f = col / 8, p = (col % 8) / 2, ri = col & 1;
-    int m0, n0;
-    group_mn(g, m0, n0);
-    GroupPairs P = group_pairs(m0, n0);
-    double x = 0.0;
-    if (k < N && f < batch && p < P.np) {
-        int pi = (-P.m[p]) % N; if (pi < 0) pi += N;
-        int qi = (-P.n[p]) % N; if (qi < 0) qi += N;
-        float2 v = G[(long long)f * N * N * N + (long long)k * N * N + (long long)pi * N + qi];
-        x = w[k] * (double)(ri ? v.y : v.x);
+    __shared__ float2 tile[32][33];
+    const long long c0 = (long long)blockIdx.x * 32, r0 = (long long)blockIdx.y * 32;
+    const long long boff = (long long)blockIdx.z * R * Cc;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    for (int j = ty; j < 32; j += 8) {
+        long long r = r0 + j, c = c0 + tx;
+        if (r < R && c < Cc) tile[j][tx] = in[boff + r * Cc + c];
     }
-    __nv_bfloat16 a, b, c;
-    split3(x, a, b, c);
-    x0[i] = a;
-    x1[i] = b;
-    x2[i] = c;
+    __syncthreads();
+    for (int j = ty; j < 32; j += 8) {
+        long long c = c0 + j, r = r0 + tx;
+        if (r < R && c < Cc) out[boff + c * R + r] = tile[tx][j];
+    }
 }
 
-// Y planes [g * ncols + col][KLp]: y = (2l+1) sign_p F(l, m_p, n_p) re/im, l = m0 + l'.
-__global__ void pack_inv_kernel(const float2* __restrict__ F, __nv_bfloat16* __restrict__ y0,
-                                __nv_bfloat16* __restrict__ y1, __nv_bfloat16* __restrict__ y2, int L, int KLp,
-                                int ncols, int batch, int ngroups, long long cstride)
+// Zero the Nyquist pencils (p = B or q = B) of H'[fn][p][q][k].
+__global__ void zero_nyquist_pencils_kernel(float2* __restrict__ H, int N, long long nf)
 {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    long long total = (long long)ngroups * ncols * KLp;
-    if (i >= total) return;
-    int lp = (int)(i % KLp);
-    long long rc = i / KLp;
-    int col = (int)(rc % ncols);
-    int g = (int)(rc / ncols);
-    int f = col / 8, p = (col % 8) / 2, ri = col & 1;
-    int m0, n0;
-    group_mn(g, m0, n0);
-    GroupPairs P = group_pairs(m0, n0);
-    int l = m0 + lp;
-    double y = 0.0;
-    if (l <= L && f < batch && p < P.np) {
-        float2 v = F[(long long)f * cstride + so3_idx(l, P.m[p], P.n[p])];
-        y = (double)(2 * l + 1) * P.sign[p] * (double)(ri ? v.y : v.x);
-    }
-    __nv_bfloat16 a, b, c;
-    split3(y, a, b, c);
-    y0[i] = a;
-    y1[i] = b;
-    y2[i] = c;
+    const long long per = 2LL * N * N;  // per function: N pencils of each kind, N values each
+    if (i >= nf * per) return;
+    long long f = i / per, r = i % per;
+    const int B = N / 2;
+    long long which = r / ((long long)N * N), rr = r % ((long long)N * N);
+    long long a = rr / N, k = rr % N;
+    long long off = (which == 0) ? (((long long)B * N + a) * N + k) : ((a * N + B) * N + k);
+    H[f * (long long)N * N * N + off] = make_float2(0.f, 0.f);
+}
+
+__global__ void resid_kernel(const float2* __restrict__ f, float2* __restrict__ r, long long n)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float2 a = f[i], b = r[i];
+    r[i] = make_float2(a.x - b.x, a.y - b.y);
+}
+
+__global__ void add_kernel(float2* __restrict__ F, const float2* __restrict__ d, long long n)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float2 a = F[i], b = d[i];
+    F[i] = make_float2(a.x + b.x, a.y + b.y);
 }
 
 }  // namespace tc
@@ -428,23 +578,23 @@ __global__ void pack_inv_kernel(const float2* __restrict__ F, __nv_bfloat16* __r
 using namespace tc;
 
 struct TCState {
-    int L = 0, B = 0, N = 0, Kp = 0, KLp = 0, batch = 0, ncols = 0, ngroups = 0;
+    int L = 0, B = 0, N = 0, Kp = 0, batch = 0, ntiles = 0, ngroups = 0;
     bool refine = false;
     FFTFactors fac;
     const double* d_tw = nullptr;
-    const double* d_w = nullptr;
+    float* d_wf = nullptr;
     long long total_rows = 0;
     __nv_bfloat16* d_tab[3] = {nullptr, nullptr, nullptr};
-    __nv_bfloat16* d_x[3] = {nullptr, nullptr, nullptr};
-    __nv_bfloat16* d_y[3] = {nullptr, nullptr, nullptr};
-    float2* d_work = nullptr;
-    float2* d_resid = nullptr;   // refinement: residual grid
-    float2* d_coef2 = nullptr;   // refinement: correction coefficients
+    float2* d_work = nullptr;     // FFT work grid [fn][k][p][q]
+    float2* d_pencil = nullptr;   // pencils [fn][p][q][k]
+    float2* d_resid = nullptr;    // refinement: residual grid
+    float2* d_coef2 = nullptr;    // refinement: correction coefficients
     long long* d_grow0 = nullptr;
-    int2* d_items_fwd = nullptr;
-    int2* d_items_inv = nullptr;
+    int4* d_items_fwd = nullptr;
+    int4* d_items_inv = nullptr;
     int n_items_fwd = 0, n_items_inv = 0;
-    CUtensorMap tmA_fwd[3], tmA_inv[3], tmX[3], tmY[3];
+    int nsm = 0;
+    CUtensorMap tmA_fwd[3], tmA_inv[3];
     int* d_err = nullptr;
     long long bytes = 0;
 };
@@ -478,9 +628,9 @@ static bool encode_2d(CUtensorMap* tm, const void* base, unsigned long long inne
     cuuint64_t strides[1] = {inner * 2};
     cuuint32_t box[2] = {box_inner, box_outer};
     cuuint32_t es[2] = {1, 1};
-    CUresult r = enc(tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims,
-                                        strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
-                                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    CUresult r = enc(tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, es,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS;
 }
 
@@ -499,12 +649,10 @@ static int tc_alloc(TCState* s, void** p, size_t bytes, std::string& err)
 void tc_destroy(TCState* s)
 {
     if (!s) return;
-    for (int p = 0; p < 3; ++p) {
+    for (int p = 0; p < 3; ++p)
         if (s->d_tab[p]) cudaFree(s->d_tab[p]);
-        if (s->d_x[p]) cudaFree(s->d_x[p]);
-        if (s->d_y[p]) cudaFree(s->d_y[p]);
-    }
-    void* ptrs[] = {s->d_work, s->d_resid, s->d_coef2, s->d_grow0, s->d_items_fwd, s->d_items_inv, s->d_err};
+    void* ptrs[] = {s->d_wf, s->d_work, s->d_pencil, s->d_resid, s->d_coef2, s->d_grow0, s->d_items_fwd,
+                    s->d_items_inv, s->d_err};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     delete s;
@@ -517,25 +665,39 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
               std::string& err)
 {
     *out = nullptr;
+    if (N > MAXN) {
+        err = "tensor-core path supports 2(l_max+1) <= 1024";
+        return FFTSO3_ERR_UNSUPPORTED;
+    }
     TCState* s = new TCState();
     s->L = L;
     s->B = L + 1;
     s->N = N;
     s->Kp = (N + 63) / 64 * 64;
-    s->KLp = (s->B + 63) / 64 * 64;
     s->batch = batch;
-    s->ncols = (8 * batch + BN - 1) / BN * BN;
+    s->ntiles = (batch + FPT - 1) / FPT;
     s->ngroups = s->B * s->B;
     s->refine = refine;
     s->fac = fac;
     s->d_tw = d_tw;
-    s->d_w = d_w;
     s->total_rows = table_elems / N;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&s->nsm, cudaDevAttrMultiProcessorCount, dev);
     int rc;
     auto bail = [&](int code) {
         tc_destroy(s);
         return code;
     };
+    // FP32 weights
+    {
+        std::vector<double> w(N);
+        cudaMemcpy(w.data(), d_w, sizeof(double) * N, cudaMemcpyDeviceToHost);
+        std::vector<float> wf(N);
+        for (int k = 0; k < N; ++k) wf[k] = (float)w[k];
+        if ((rc = tc_alloc(s, (void**)&s->d_wf, sizeof(float) * N, err))) return bail(rc);
+        cudaMemcpy(s->d_wf, wf.data(), sizeof(float) * N, cudaMemcpyHostToDevice);
+    }
     // table planes
     for (int p = 0; p < 3; ++p)
         if ((rc = tc_alloc(s, (void**)&s->d_tab[p], sizeof(__nv_bfloat16) * s->total_rows * s->Kp, err)))
@@ -550,46 +712,46 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
             return bail(FFTSO3_ERR_CUDA);
         }
     }
-    const size_t xelems = (size_t)s->ngroups * s->ncols * s->Kp;
-    const size_t yelems = (size_t)s->ngroups * s->ncols * s->KLp;
-    for (int p = 0; p < 3; ++p) {
-        if ((rc = tc_alloc(s, (void**)&s->d_x[p], sizeof(__nv_bfloat16) * xelems, err))) return bail(rc);
-        if ((rc = tc_alloc(s, (void**)&s->d_y[p], sizeof(__nv_bfloat16) * yelems, err))) return bail(rc);
-    }
     const size_t gridel = (size_t)batch * N * N * N;
     if ((rc = tc_alloc(s, (void**)&s->d_work, sizeof(float2) * gridel, err))) return bail(rc);
+    if ((rc = tc_alloc(s, (void**)&s->d_pencil, sizeof(float2) * gridel, err))) return bail(rc);
     if (refine) {
         if ((rc = tc_alloc(s, (void**)&s->d_resid, sizeof(float2) * gridel, err))) return bail(rc);
         if ((rc = tc_alloc(s, (void**)&s->d_coef2, sizeof(float2) * (size_t)batch * so3_off(s->B), err)))
             return bail(rc);
     }
-    // group rows and work items
+    // group rows and work items; the inverse list is ordered by decreasing cost
     std::vector<long long> grow0(s->ngroups);
-    std::vector<int2> itf, iti;
+    std::vector<int4> itf, iti;
     for (int g = 0; g < s->ngroups; ++g) {
         int m0, n0;
         group_mn(g, m0, n0);
         grow0[g] = goff[g] / N;
-        int nl = s->B - m0;
-        for (int mt = 0; mt * BM < nl; ++mt) itf.push_back(make_int2(g, mt));
-        for (int mt = 0; mt * BM < N; ++mt) iti.push_back(make_int2(g, mt));
+        const int nl = s->B - m0;
+        for (int nt = 0; nt < s->ntiles; ++nt) {
+            for (int mt = 0; mt * BM < nl; ++mt) itf.push_back(make_int4(g, mt, nt, 0));
+            for (int mt = 0; mt * BM < N; ++mt) iti.push_back(make_int4(g, mt, nt, 0));
+        }
     }
+    std::stable_sort(iti.begin(), iti.end(), [&](const int4& a, const int4& b) {
+        int ma, na, mb, nb;
+        group_mn(a.x, ma, na);
+        group_mn(b.x, mb, nb);
+        return (s->B - ma + BK - 1) / BK > (s->B - mb + BK - 1) / BK;
+    });
     s->n_items_fwd = (int)itf.size();
     s->n_items_inv = (int)iti.size();
     if ((rc = tc_alloc(s, (void**)&s->d_grow0, sizeof(long long) * grow0.size(), err))) return bail(rc);
-    if ((rc = tc_alloc(s, (void**)&s->d_items_fwd, sizeof(int2) * itf.size(), err))) return bail(rc);
-    if ((rc = tc_alloc(s, (void**)&s->d_items_inv, sizeof(int2) * iti.size(), err))) return bail(rc);
+    if ((rc = tc_alloc(s, (void**)&s->d_items_fwd, sizeof(int4) * itf.size(), err))) return bail(rc);
+    if ((rc = tc_alloc(s, (void**)&s->d_items_inv, sizeof(int4) * iti.size(), err))) return bail(rc);
     if ((rc = tc_alloc(s, (void**)&s->d_err, sizeof(int), err))) return bail(rc);
     cudaMemcpy(s->d_grow0, grow0.data(), sizeof(long long) * grow0.size(), cudaMemcpyHostToDevice);
-    cudaMemcpy(s->d_items_fwd, itf.data(), sizeof(int2) * itf.size(), cudaMemcpyHostToDevice);
-    cudaMemcpy(s->d_items_inv, iti.data(), sizeof(int2) * iti.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(s->d_items_fwd, itf.data(), sizeof(int4) * itf.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(s->d_items_inv, iti.data(), sizeof(int4) * iti.size(), cudaMemcpyHostToDevice);
     cudaMemset(s->d_err, 0, sizeof(int));
-    // tensor maps
     for (int p = 0; p < 3; ++p) {
         bool ok = encode_2d(&s->tmA_fwd[p], s->d_tab[p], s->Kp, s->total_rows, 64, BM) &&
-                  encode_2d(&s->tmA_inv[p], s->d_tab[p], s->Kp, s->total_rows, 64, BK) &&
-                  encode_2d(&s->tmX[p], s->d_x[p], s->Kp, (unsigned long long)s->ngroups * s->ncols, 64, BN) &&
-                  encode_2d(&s->tmY[p], s->d_y[p], s->KLp, (unsigned long long)s->ngroups * s->ncols, 64, BN);
+                  encode_2d(&s->tmA_inv[p], s->d_tab[p], s->Kp, s->total_rows, 64, BK);
         if (!ok) {
             err = "cuTensorMapEncodeTiled failed";
             return bail(FFTSO3_ERR_CUDA);
@@ -618,8 +780,8 @@ static FFTLaunch fft_launch(const TCState* s, const void* in, void* out, bool co
     L.fp64 = false;
     L.real_in = false;
     L.real_out = false;
+    L.nlines = (long long)s->batch * N * N;
     if (!cols) {
-        L.nlines = (long long)s->batch * N * N;
         L.lpb = 4;
         L.inner = 1;
         L.ostride = N;
@@ -627,8 +789,8 @@ static FFTLaunch fft_launch(const TCState* s, const void* in, void* out, bool co
         L.es = 1;
         L.lines_fastest = false;
     } else {
-        L.nlines = (long long)s->batch * N * N;
         L.lpb = 16;
+        while (L.lpb > 1 && fft_smem_bytes(N, L.lpb, false) > 100 * 1024) L.lpb /= 2;
         L.inner = N;
         L.ostride = (long long)N * N;
         L.istride = 1;
@@ -647,41 +809,52 @@ static FFTLaunch fft_launch(const TCState* s, const void* in, void* out, bool co
         }                                                                  \
     } while (0)
 
+static GemmArgs gemm_args(const TCState* s)
+{
+    GemmArgs a;
+    a.items = nullptr;
+    a.nitems = 0;
+    a.grow0 = s->d_grow0;
+    a.L = s->L;
+    a.N = s->N;
+    a.Kp = s->Kp;
+    a.batch = s->batch;
+    a.fstride = (long long)s->N * s->N * s->N;
+    a.cstride = so3_off(s->B);
+    a.pin = nullptr;
+    a.cin = nullptr;
+    a.cout = nullptr;
+    a.pout = nullptr;
+    a.wf = s->d_wf;
+    a.err = s->d_err;
+    return a;
+}
+
 static int tc_forward_once(TCState* s, const float2* grid, float2* F, cudaStream_t st, StageTimer* T,
                            std::string& err)
 {
-    const int N = s->N;
+    const long long N = s->N;
     T->begin(ST_FFT_ROWS, st);
     TCK(launch_fft_lines(fft_launch(s, grid, s->d_work, false), st));
     T->end(st);
     T->begin(ST_FFT_COLS, st);
     TCK(launch_fft_lines(fft_launch(s, s->d_work, s->d_work, true), st));
     T->end(st);
+    T->begin(ST_PACK_FWD, st);
     {
-        T->begin(ST_PACK_FWD, st);
-        long long tot = (long long)s->ngroups * s->ncols * s->Kp;
-        pack_fwd_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(s->d_work, s->d_w, s->d_x[0], s->d_x[1],
-                                                                        s->d_x[2], s->L, N, s->Kp, s->ncols, s->batch,
-                                                                        s->ngroups);
+        dim3 tg((unsigned)((N * N + 31) / 32), (unsigned)((N + 31) / 32), (unsigned)s->batch);
+        transpose_kernel<<<tg, dim3(32, 8), 0, st>>>(s->d_work, s->d_pencil, N, N * N);
         TCK(cudaGetLastError());
-        T->end(st);
     }
-    GemmArgs a;
+    T->end(st);
+    GemmArgs a = gemm_args(s);
     a.items = s->d_items_fwd;
-    a.grow0 = s->d_grow0;
-    a.L = s->L;
-    a.N = N;
-    a.ncols = s->ncols;
-    a.batch = s->batch;
-    a.nk_fixed = s->Kp / BK;
-    a.cstride = so3_off(s->B);
-    a.F = F;
-    a.H = nullptr;
-    a.err = s->d_err;
-    dim3 lg(s->n_items_fwd, s->ncols / BN);
+    a.nitems = s->n_items_fwd;
+    a.pin = s->d_pencil;
+    a.cout = F;
+    const int nctas = s->n_items_fwd < s->nsm ? s->n_items_fwd : s->nsm;
     T->begin(ST_GEMM_FWD, st);
-    so3_tc_gemm_kernel<true><<<lg, THREADS, SMEM_BYTES, st>>>(s->tmA_fwd[0], s->tmA_fwd[1], s->tmA_fwd[2], s->tmX[0],
-                                                                s->tmX[1], s->tmX[2], a);
+    so3_tc_gemm_kernel<true><<<nctas, THREADS, SMEM_BYTES, st>>>(s->tmA_fwd[0], s->tmA_fwd[1], s->tmA_fwd[2], a);
     TCK(cudaGetLastError());
     T->end(st);
     return FFTSO3_SUCCESS;
@@ -690,36 +863,30 @@ static int tc_forward_once(TCState* s, const float2* grid, float2* F, cudaStream
 static int tc_inverse_once(TCState* s, const float2* F, float2* grid, cudaStream_t st, StageTimer* T,
                            std::string& err)
 {
-    const int N = s->N;
-    {
-        T->begin(ST_PACK_INV, st);
-        long long tot = (long long)s->ngroups * s->ncols * s->KLp;
-        pack_inv_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(F, s->d_y[0], s->d_y[1], s->d_y[2], s->L,
-                                                                        s->KLp, s->ncols, s->batch, s->ngroups,
-                                                                        so3_off(s->B));
-        TCK(cudaGetLastError());
-        T->end(st);
-    }
+    const long long N = s->N;
     T->begin(ST_NYQUIST, st);
-    TCK(launch_zero_nyquist_so3(s->d_work, false, N, (long long)s->batch * N, st));
+    {
+        long long tot = (long long)s->batch * 2 * N * N;
+        zero_nyquist_pencils_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(s->d_pencil, (int)N, s->batch);
+        TCK(cudaGetLastError());
+    }
     T->end(st);
-    GemmArgs a;
+    GemmArgs a = gemm_args(s);
     a.items = s->d_items_inv;
-    a.grow0 = s->d_grow0;
-    a.L = s->L;
-    a.N = N;
-    a.ncols = s->ncols;
-    a.batch = s->batch;
-    a.nk_fixed = 0;
-    a.cstride = so3_off(s->B);
-    a.F = nullptr;
-    a.H = s->d_work;
-    a.err = s->d_err;
-    dim3 lg(s->n_items_inv, s->ncols / BN);
+    a.nitems = s->n_items_inv;
+    a.cin = F;
+    a.pout = s->d_pencil;
+    const int nctas = s->n_items_inv < s->nsm ? s->n_items_inv : s->nsm;
     T->begin(ST_GEMM_INV, st);
-    so3_tc_gemm_kernel<false><<<lg, THREADS, SMEM_BYTES, st>>>(s->tmA_inv[0], s->tmA_inv[1], s->tmA_inv[2],
-                                                                 s->tmY[0], s->tmY[1], s->tmY[2], a);
+    so3_tc_gemm_kernel<false><<<nctas, THREADS, SMEM_BYTES, st>>>(s->tmA_inv[0], s->tmA_inv[1], s->tmA_inv[2], a);
     TCK(cudaGetLastError());
+    T->end(st);
+    T->begin(ST_PACK_INV, st);
+    {
+        dim3 tg((unsigned)((N + 31) / 32), (unsigned)((N * N + 31) / 32), (unsigned)s->batch);
+        transpose_kernel<<<tg, dim3(32, 8), 0, st>>>(s->d_pencil, s->d_work, N * N, N);
+        TCK(cudaGetLastError());
+    }
     T->end(st);
     T->begin(ST_FFT_ROWS, st);
     TCK(launch_fft_lines(fft_launch(s, s->d_work, s->d_work, false), st));
@@ -728,22 +895,6 @@ static int tc_inverse_once(TCState* s, const float2* F, float2* grid, cudaStream
     TCK(launch_fft_lines(fft_launch(s, s->d_work, grid, true), st));
     T->end(st);
     return FFTSO3_SUCCESS;
-}
-
-__global__ void resid_kernel(const float2* __restrict__ f, float2* __restrict__ r, long long n)
-{
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float2 a = f[i], b = r[i];
-    r[i] = make_float2(a.x - b.x, a.y - b.y);
-}
-
-__global__ void add_kernel(float2* __restrict__ F, const float2* __restrict__ d, long long n)
-{
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float2 a = F[i], b = d[i];
-    F[i] = make_float2(a.x + b.x, a.y + b.y);
 }
 
 int tc_forward(TCState* s, const void* grid, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err)

@@ -142,7 +142,7 @@ __device__ void stockham_generic(const typename V2<T>::t* __restrict__ src, type
 
 template <typename T, typename TIN, bool REAL_IN, bool REAL_OUT>
 __global__ void __launch_bounds__(256) fft_lines_kernel(const TIN* __restrict__ in, void* __restrict__ out, FFTFactors fac,
-                                                        long long nlines, int lpb, long long inner, long long ostride,
+                                                        long long nlines, int lpb_log2, long long inner, long long ostride,
                                                         long long istride, long long es, const void* __restrict__ twg,
                                                         int lines_fastest)
 {
@@ -150,29 +150,40 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(const TIN* __restrict__ 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int N = fac.N;
     const int LS = N + 1;
+    const int lpb = 1 << lpb_log2;
     C* w = reinterpret_cast<C*>(smem_raw);
     C* buf0 = w + N;
     C* buf1 = buf0 + lpb * LS;
+    long long* base = reinterpret_cast<long long*>(buf1 + lpb * LS);
     const double2* tw = reinterpret_cast<const double2*>(twg);
     for (int i = threadIdx.x; i < N; i += blockDim.x) w[i] = V2<T>::mk((T)tw[i].x, (T)tw[i].y);
 
     const long long line0 = (long long)blockIdx.x * lpb;
     const int nl = (int)min((long long)lpb, nlines - line0);
+    if (threadIdx.x < lpb) {
+        long long i = line0 + threadIdx.x;
+        base[threadIdx.x] = (i / inner) * ostride + (i % inner) * istride;
+    }
+    __syncthreads();
     const int tot = lpb * N;
-    // load
-    for (int e = threadIdx.x; e < tot; e += blockDim.x) {
-        int l, j;
-        if (lines_fastest) { l = e % lpb; j = e / lpb; } else { j = e % N; l = e / N; }
-        if (l >= nl) continue;
-        long long i = line0 + l;
-        long long off = (i / inner) * ostride + (i % inner) * istride + (long long)j * es;
-        C v;
-        if constexpr (REAL_IN) {
-            v = V2<T>::mk((T)in[off], (T)0);
-        } else {
-            v = in[off];
+    // load (per-line base offsets precomputed; no per-element 64-bit division)
+    if (lines_fastest) {
+        for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+            const int l = e & (lpb - 1), j = e >> lpb_log2;
+            if (l >= nl) continue;
+            const long long off = base[l] + (long long)j * es;
+            if constexpr (REAL_IN) buf0[l * LS + j] = V2<T>::mk((T)in[off], (T)0);
+            else buf0[l * LS + j] = in[off];
         }
-        buf0[l * LS + j] = v;
+    } else {
+        for (int l = 0; l < nl; ++l) {
+            const long long b0 = base[l];
+            for (int j = threadIdx.x; j < N; j += blockDim.x) {
+                const long long off = b0 + (long long)j * es;
+                if constexpr (REAL_IN) buf0[l * LS + j] = V2<T>::mk((T)in[off], (T)0);
+                else buf0[l * LS + j] = in[off];
+            }
+        }
     }
     __syncthreads();
     C* src = buf0;
@@ -194,17 +205,24 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(const TIN* __restrict__ 
         Ns *= R;
     }
     // store
-    for (int e = threadIdx.x; e < tot; e += blockDim.x) {
-        int l, j;
-        if (lines_fastest) { l = e % lpb; j = e / lpb; } else { j = e % N; l = e / N; }
-        if (l >= nl) continue;
-        long long i = line0 + l;
-        long long off = (i / inner) * ostride + (i % inner) * istride + (long long)j * es;
-        C v = src[l * LS + j];
-        if constexpr (REAL_OUT) {
-            reinterpret_cast<T*>(out)[off] = v.x;
-        } else {
-            reinterpret_cast<C*>(out)[off] = v;
+    if (lines_fastest) {
+        for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+            const int l = e & (lpb - 1), j = e >> lpb_log2;
+            if (l >= nl) continue;
+            const long long off = base[l] + (long long)j * es;
+            const C v = src[l * LS + j];
+            if constexpr (REAL_OUT) reinterpret_cast<T*>(out)[off] = v.x;
+            else reinterpret_cast<C*>(out)[off] = v;
+        }
+    } else {
+        for (int l = 0; l < nl; ++l) {
+            const long long b0 = base[l];
+            for (int j = threadIdx.x; j < N; j += blockDim.x) {
+                const long long off = b0 + (long long)j * es;
+                const C v = src[l * LS + j];
+                if constexpr (REAL_OUT) reinterpret_cast<T*>(out)[off] = v.x;
+                else reinterpret_cast<C*>(out)[off] = v;
+            }
         }
     }
 }
@@ -225,7 +243,7 @@ void make_fft_factors(int N, FFTFactors& f)
 size_t fft_smem_bytes(int N, int lpb, bool fp64)
 {
     size_t c = fp64 ? 16 : 8;
-    return c * ((size_t)N + 2 * (size_t)lpb * (N + 1));
+    return c * ((size_t)N + 2 * (size_t)lpb * (N + 1)) + 8 * (size_t)lpb;
 }
 
 template <typename T, typename TIN, bool RI, bool RO>
@@ -237,8 +255,11 @@ static cudaError_t launch_one(const void* in, void* out, const FFTFactors& fac, 
     auto kern = fft_lines_kernel<T, TIN, RI, RO>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
+    int lg = 0;
+    while ((1 << lg) < lpb) ++lg;
+    if ((1 << lg) != lpb || lpb > 256) return cudaErrorInvalidValue;  // lines per CTA: power of two
     long long nblk = (nlines + lpb - 1) / lpb;
-    kern<<<(unsigned)nblk, 256, smem, st>>>(reinterpret_cast<const TIN*>(in), out, fac, nlines, lpb, inner, ostride,
+    kern<<<(unsigned)nblk, 256, smem, st>>>(reinterpret_cast<const TIN*>(in), out, fac, nlines, lg, inner, ostride,
                                             istride, es, tw, lines_fastest ? 1 : 0);
     return cudaGetLastError();
 }
