@@ -55,7 +55,7 @@ constexpr int STAGES = 2;
 constexpr int PLANE_BYTES = 128 * 128;        // 128 rows x 128 bytes
 constexpr int STAGE_A = 3 * PLANE_BYTES;      // three BF16 planes of the table tile (TMA)
 constexpr int STAGE_BYTES = 6 * PLANE_BYTES;  // + three planes of the B tile (producer warps)
-constexpr int NPROD = 4;                      // B-producer warps
+constexpr int NPROD = 8;                      // B-producer warps
 constexpr int NEPI = 4;                       // epilogue warps
 constexpr int THREADS = 32 * (2 + NPROD + NEPI);
 constexpr int MAXN = 1024;                    // weights staged in shared memory
@@ -198,9 +198,10 @@ struct GemmArgs {
     int L, N, Kp, batch;
     long long fstride;         // pencil elements per function (N^3)
     long long cstride;         // coefficients per function
+    const long long* goff2;    // group-major coefficient offsets: sum over earlier groups of np * nl
     const float2* pin;         // forward: input pencils G'[fn][p][q][k]
-    const float2* cin;         // inverse: input coefficients
-    float2* cout;              // forward: output coefficients
+    const float2* cin;         // inverse: scaled group-major coefficients Y[fn][goff2 + pair * nl + l']
+    float2* cout;              // forward: group-major output coefficients [fn][goff2 + pair * nl + l']
     float2* pout;              // inverse: output pencils H'[fn][p][q][k]
     const float* wf;           // forward: quadrature weights (FP32)
     int* err;
@@ -358,89 +359,103 @@ __global__ void __launch_bounds__(THREADS, 1)
             for (int u = (t >= 2 ? t - 2 : 0); u < t; ++u) mbar_wait(&accf[u & 1], (u >> 1) & 1, args.err, 6);
         }
     } else if (warp < 2 + NPROD) {
-        // ---------------- B-operand producers (128 threads)
+        // ---------------- B-operand producers (256 threads): thread = (column pair, 16-wide k quarter).
+        // Each k-step's loads are issued one step ahead into registers so the
+        // DRAM latency overlaps the split/store of the previous step.
         const int pt = threadIdx.x - 64;
-        const int c = pt >> 1, half = pt & 1;          // column pair (function, pair) and k half
+        const int c = pt >> 2, q4 = pt & 3;
         const int fl = c >> 2, pp = c & 3;
         const int Rre = fl * 8 + 2 * pp, Rim = Rre + 1;
-        int kc = 0;
-        for (int it = blockIdx.x; it < args.nitems && !*abort_flag; it += gridDim.x) {
+        // source of (item it, k-step i) for this thread: 16 consecutive complex values, or none
+        auto source = [&](int it, int i, int& kbase) -> const float2* {
             const int4 item = args.items[it];
             int m0, n0;
             group_mn(item.x, m0, n0);
             const GroupPairs P = group_pairs(m0, n0);
-            const int nk = FWD ? args.Kp / BK : (B - m0 + BK - 1) / BK;
             const int f = item.z * FPT + fl;
-            const bool valid = (f < args.batch) && (pp < P.np);
-            int pm = 0, pn = 0;
-            float sg = 1.f;
-            if (pp < P.np) {
-                pm = P.m[pp];
-                pn = P.n[pp];
-                sg = (float)P.sign[pp];
+            kbase = i * BK + q4 * 16;
+            if (f >= args.batch || pp >= P.np) return nullptr;
+            if (FWD) {
+                int pi = (-P.m[pp]) % N; if (pi < 0) pi += N;
+                int qi = (-P.n[pp]) % N; if (qi < 0) qi += N;
+                return args.pin + (long long)f * args.fstride + ((long long)pi * N + qi) * N;
             }
-            const float2* src = nullptr;
-            if (FWD && valid) {
-                int pi = (-pm) % N; if (pi < 0) pi += N;
-                int qi = (-pn) % N; if (qi < 0) qi += N;
-                src = args.pin + (long long)f * args.fstride + ((long long)pi * N + qi) * N;
-            }
-            const float2* csrc = (!FWD && valid) ? args.cin + (long long)f * args.cstride : nullptr;
-            bool stop = false;
-            for (int i = 0; i < nk; ++i, ++kc) {
-                const int s = kc % STAGES;
-                if (kc >= STAGES && !mbar_wait(&empty[s], ((kc / STAGES) - 1) & 1, args.err, 4)) {
-                    stop = true;
-                    break;
+            const int nl = B - m0;
+            return args.cin + (long long)f * args.cstride + args.goff2[item.x] + (long long)pp * nl;
+        };
+        auto limit = [&](int it) -> int {
+            if (FWD) return N;
+            int m0, n0;
+            group_mn(args.items[it].x, m0, n0);
+            return B - m0;
+        };
+        auto fetch = [&](const float2* src, int kbase, int lim, float2* v) {
+            if (FWD && src && kbase + 16 <= lim) {
+                const float4* s4 = reinterpret_cast<const float4*>(src + kbase);
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    float4 t = __ldg(s4 + j);
+                    v[2 * j] = make_float2(t.x, t.y);
+                    v[2 * j + 1] = make_float2(t.z, t.w);
                 }
-                const uint32_t bpl = smem_u32(smem + s * STAGE_BYTES + STAGE_A);
-#pragma unroll 1
-                for (int ch = 0; ch < 4; ++ch) {
-                    const int kl = half * 32 + ch * 8;        // local index of the chunk's first k (or l)
-                    float re[8], im[8];
-                    if (FWD) {
-                        const int k = i * BK + kl;
-                        if (valid && k + 8 <= N) {
-                            const float4* s4 = reinterpret_cast<const float4*>(src + k);
+            } else {
 #pragma unroll
-                            for (int j = 0; j < 4; ++j) {
-                                float4 v = __ldg(s4 + j);
-                                re[2 * j] = v.x * wsm[k + 2 * j];
-                                im[2 * j] = v.y * wsm[k + 2 * j];
-                                re[2 * j + 1] = v.z * wsm[k + 2 * j + 1];
-                                im[2 * j + 1] = v.w * wsm[k + 2 * j + 1];
-                            }
-                        } else {
-#pragma unroll
-                            for (int j = 0; j < 8; ++j) {
-                                float2 v = (valid && k + j < N) ? src[k + j] : make_float2(0.f, 0.f);
-                                float wk = (valid && k + j < N) ? wsm[k + j] : 0.f;
-                                re[j] = v.x * wk;
-                                im[j] = v.y * wk;
-                            }
-                        }
-                    } else {
-#pragma unroll
-                        for (int j = 0; j < 8; ++j) {
-                            const int l = m0 + i * BK + kl + j;
-                            float2 v = make_float2(0.f, 0.f);
-                            if (valid && l <= args.L) v = __ldg(csrc + so3_idx(l, pm, pn));
-                            const float sc = (float)(2 * l + 1) * sg;
-                            re[j] = v.x * sc;
-                            im[j] = v.y * sc;
-                        }
-                    }
-                    store_chunk(bpl, Rre, kl >> 3, re);
-                    store_chunk(bpl, Rim, kl >> 3, im);
-                }
-                fence_proxy_async();
-                __syncwarp();
-                if (lane == 0) mbar_arrive(&full[s]);
+                for (int j = 0; j < 16; ++j)
+                    v[j] = (src && kbase + j < lim) ? __ldg(src + kbase + j) : make_float2(0.f, 0.f);
             }
-            if (stop) {
+        };
+        int kc = 0;
+        int it = blockIdx.x, i = 0;
+        float2 cur[16];
+        int kb_cur = 0;
+        if (it < args.nitems) {
+            const float2* s0 = source(it, 0, kb_cur);
+            fetch(s0, kb_cur, limit(it), cur);
+        }
+        while (it < args.nitems && !*abort_flag) {
+            int m0, n0;
+            group_mn(args.items[it].x, m0, n0);
+            const int nk = FWD ? args.Kp / BK : (B - m0 + BK - 1) / BK;
+            int it2 = it, i2 = i + 1;
+            if (i2 == nk) {
+                it2 += gridDim.x;
+                i2 = 0;
+            }
+            float2 nxt[16];
+            int kb_nxt = 0;
+            if (it2 < args.nitems) {
+                const float2* s1 = source(it2, i2, kb_nxt);
+                fetch(s1, kb_nxt, limit(it2), nxt);
+            }
+            const int s = kc % STAGES;
+            if (kc >= STAGES && !mbar_wait(&empty[s], ((kc / STAGES) - 1) & 1, args.err, 4)) {
                 *abort_flag = 1;
                 break;
             }
+            const uint32_t bpl = smem_u32(smem + s * STAGE_BYTES + STAGE_A);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                float re[8], im[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    const float2 v = cur[h * 8 + j];
+                    const float wk = FWD ? ((kb_cur + h * 8 + j < N) ? wsm[kb_cur + h * 8 + j] : 0.f) : 1.f;
+                    re[j] = v.x * wk;
+                    im[j] = v.y * wk;
+                }
+                const int chunk = q4 * 2 + h;
+                store_chunk(bpl, Rre, chunk, re);
+                store_chunk(bpl, Rim, chunk, im);
+            }
+            fence_proxy_async();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&full[s]);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) cur[j] = nxt[j];
+            kb_cur = kb_nxt;
+            it = it2;
+            i = i2;
+            ++kc;
         }
     } else {
         // ---------------- epilogue (4 warps, one TMEM lane quarter each)
@@ -471,12 +486,12 @@ __global__ void __launch_bounds__(THREADS, 1)
                     if (f >= args.batch) continue;
                     if (FWD) {
                         const int row = item.y * BM + r;
-                        if (row >= B - m0) continue;
-                        const int l = m0 + row;
-                        float2* Fo = args.cout + (long long)f * args.cstride;
+                        const int nl = B - m0;
+                        if (row >= nl) continue;
+                        float2* Fo = args.cout + (long long)f * args.cstride + args.goff2[item.x] + row;
                         for (int p = 0; p < P.np; ++p) {
                             const float sg = (float)P.sign[p];
-                            Fo[so3_idx(l, P.m[p], P.n[p])] = make_float2(sg * v[fq * 8 + 2 * p], sg * v[fq * 8 + 2 * p + 1]);
+                            Fo[(long long)p * nl] = make_float2(sg * v[fq * 8 + 2 * p], sg * v[fq * 8 + 2 * p + 1]);
                         }
                     } else {
                         const int k = item.y * BM + r;
@@ -555,6 +570,61 @@ __global__ void zero_nyquist_pencils_kernel(float2* __restrict__ H, int N, long 
     H[f * (long long)N * N * N + off] = make_float2(0.f, 0.f);
 }
 
+// (m, n) -> (symmetry group, pair) consistent with group_pairs().
+__device__ __forceinline__ void pair_of(int m, int n, int& g, int& p)
+{
+    int m0, n0;
+    if (abs(m) >= abs(n)) {
+        if (m >= 0) { m0 = m; n0 = n; p = 0; }
+        else { m0 = -m; n0 = -n; p = 1; }
+    } else {
+        if (n > 0) { m0 = n; n0 = m; p = 2; }
+        else { m0 = -n; n0 = -m; p = 3; }
+    }
+    g = m0 * m0 + m0 + n0;
+}
+
+// Group-major forward output -> packed coefficients (one CTA per (l, function)).
+__global__ void group_to_packed_kernel(const float2* __restrict__ Fg, float2* __restrict__ F,
+                                       const long long* __restrict__ goff2, int L, long long cstride)
+{
+    const int l = blockIdx.x, f = blockIdx.y;
+    const int W = 2 * l + 1;
+    const int B = L + 1;
+    const float2* src = Fg + (long long)f * cstride;
+    float2* dst = F + (long long)f * cstride + so3_off(l);
+    for (int i = threadIdx.x; i < W * W; i += blockDim.x) {
+        const int m = i % W - l, n = i / W - l;
+        int g, p;
+        pair_of(m, n, g, p);
+        const int m0 = (int)sqrtf((float)g + 0.5f) - 1;
+        int mm = m0 < 0 ? 0 : m0;
+        while ((mm + 1) * (mm + 1) <= g) ++mm;
+        while (mm * mm > g) --mm;
+        const int nl = B - mm;
+        dst[i] = src[goff2[g] + (long long)p * nl + (l - mm)];
+    }
+}
+
+// Packed coefficients -> scaled group-major Y = (2l+1) sign F(l, pair) (one CTA per (group, function)).
+__global__ void packed_to_group_kernel(const float2* __restrict__ F, float2* __restrict__ Y,
+                                       const long long* __restrict__ goff2, int L, long long cstride)
+{
+    const int g = blockIdx.x, f = blockIdx.y;
+    int m0, n0;
+    group_mn(g, m0, n0);
+    const GroupPairs P = group_pairs(m0, n0);
+    const int nl = L + 1 - m0;
+    const float2* src = F + (long long)f * cstride;
+    float2* dst = Y + (long long)f * cstride + goff2[g];
+    for (int i = threadIdx.x; i < P.np * nl; i += blockDim.x) {
+        const int p = i / nl, lp = i - p * nl, l = m0 + lp;
+        const float2 v = src[so3_idx(l, P.m[p], P.n[p])];
+        const float sc = (float)(2 * l + 1) * (float)P.sign[p];
+        dst[i] = make_float2(sc * v.x, sc * v.y);
+    }
+}
+
 __global__ void resid_kernel(const float2* __restrict__ f, float2* __restrict__ r, long long n)
 {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -590,6 +660,8 @@ struct TCState {
     float2* d_resid = nullptr;    // refinement: residual grid
     float2* d_coef2 = nullptr;    // refinement: correction coefficients
     long long* d_grow0 = nullptr;
+    long long* d_goff2 = nullptr;  // group-major coefficient offsets
+    float2* d_fg = nullptr;        // group-major coefficients [fn][C]
     int4* d_items_fwd = nullptr;
     int4* d_items_inv = nullptr;
     int n_items_fwd = 0, n_items_inv = 0;
@@ -651,8 +723,8 @@ void tc_destroy(TCState* s)
     if (!s) return;
     for (int p = 0; p < 3; ++p)
         if (s->d_tab[p]) cudaFree(s->d_tab[p]);
-    void* ptrs[] = {s->d_wf, s->d_work, s->d_pencil, s->d_resid, s->d_coef2, s->d_grow0, s->d_items_fwd,
-                    s->d_items_inv, s->d_err};
+    void* ptrs[] = {s->d_wf, s->d_work, s->d_pencil, s->d_resid, s->d_coef2, s->d_grow0, s->d_goff2, s->d_fg,
+                    s->d_items_fwd, s->d_items_inv, s->d_err};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     delete s;
@@ -721,13 +793,16 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
             return bail(rc);
     }
     // group rows and work items; the inverse list is ordered by decreasing cost
-    std::vector<long long> grow0(s->ngroups);
+    std::vector<long long> grow0(s->ngroups), goff2(s->ngroups + 1);
     std::vector<int4> itf, iti;
+    long long acc2 = 0;
     for (int g = 0; g < s->ngroups; ++g) {
         int m0, n0;
         group_mn(g, m0, n0);
         grow0[g] = goff[g] / N;
         const int nl = s->B - m0;
+        goff2[g] = acc2;
+        acc2 += (long long)group_pairs(m0, n0).np * nl;
         for (int nt = 0; nt < s->ntiles; ++nt) {
             for (int mt = 0; mt * BM < nl; ++mt) itf.push_back(make_int4(g, mt, nt, 0));
             for (int mt = 0; mt * BM < N; ++mt) iti.push_back(make_int4(g, mt, nt, 0));
@@ -741,7 +816,15 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
     });
     s->n_items_fwd = (int)itf.size();
     s->n_items_inv = (int)iti.size();
+    goff2[s->ngroups] = acc2;
+    if (acc2 != so3_off(s->B)) {
+        err = "internal: group-major layout does not cover the coefficients";
+        return bail(FFTSO3_ERR_CUDA);
+    }
     if ((rc = tc_alloc(s, (void**)&s->d_grow0, sizeof(long long) * grow0.size(), err))) return bail(rc);
+    if ((rc = tc_alloc(s, (void**)&s->d_goff2, sizeof(long long) * goff2.size(), err))) return bail(rc);
+    if ((rc = tc_alloc(s, (void**)&s->d_fg, sizeof(float2) * (size_t)batch * acc2, err))) return bail(rc);
+    cudaMemcpy(s->d_goff2, goff2.data(), sizeof(long long) * goff2.size(), cudaMemcpyHostToDevice);
     if ((rc = tc_alloc(s, (void**)&s->d_items_fwd, sizeof(int4) * itf.size(), err))) return bail(rc);
     if ((rc = tc_alloc(s, (void**)&s->d_items_inv, sizeof(int4) * iti.size(), err))) return bail(rc);
     if ((rc = tc_alloc(s, (void**)&s->d_err, sizeof(int), err))) return bail(rc);
@@ -815,6 +898,7 @@ static GemmArgs gemm_args(const TCState* s)
     a.items = nullptr;
     a.nitems = 0;
     a.grow0 = s->d_grow0;
+    a.goff2 = s->d_goff2;
     a.L = s->L;
     a.N = s->N;
     a.Kp = s->Kp;
@@ -851,10 +935,14 @@ static int tc_forward_once(TCState* s, const float2* grid, float2* F, cudaStream
     a.items = s->d_items_fwd;
     a.nitems = s->n_items_fwd;
     a.pin = s->d_pencil;
-    a.cout = F;
+    a.cout = s->d_fg;
     const int nctas = s->n_items_fwd < s->nsm ? s->n_items_fwd : s->nsm;
     T->begin(ST_GEMM_FWD, st);
     so3_tc_gemm_kernel<true><<<nctas, THREADS, SMEM_BYTES, st>>>(s->tmA_fwd[0], s->tmA_fwd[1], s->tmA_fwd[2], a);
+    TCK(cudaGetLastError());
+    T->end(st);
+    T->begin(ST_BASIS, st);
+    group_to_packed_kernel<<<dim3(s->B, s->batch), 256, 0, st>>>(s->d_fg, F, s->d_goff2, s->L, so3_off(s->B));
     TCK(cudaGetLastError());
     T->end(st);
     return FFTSO3_SUCCESS;
@@ -871,10 +959,15 @@ static int tc_inverse_once(TCState* s, const float2* F, float2* grid, cudaStream
         TCK(cudaGetLastError());
     }
     T->end(st);
+    T->begin(ST_BASIS, st);
+    packed_to_group_kernel<<<dim3(s->ngroups, s->batch), 128, 0, st>>>(F, s->d_fg, s->d_goff2, s->L,
+                                                                      so3_off(s->B));
+    TCK(cudaGetLastError());
+    T->end(st);
     GemmArgs a = gemm_args(s);
     a.items = s->d_items_inv;
     a.nitems = s->n_items_inv;
-    a.cin = F;
+    a.cin = s->d_fg;
     a.pout = s->d_pencil;
     const int nctas = s->n_items_inv < s->nsm ? s->n_items_inv : s->nsm;
     T->begin(ST_GEMM_INV, st);
