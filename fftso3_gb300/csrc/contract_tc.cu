@@ -918,19 +918,27 @@ static int tc_forward_once(TCState* s, const float2* grid, float2* F, cudaStream
                            std::string& err)
 {
     const long long N = s->N;
-    T->begin(ST_FFT_ROWS, st);
-    TCK(launch_fft_lines(fft_launch(s, grid, s->d_work, false), st));
-    T->end(st);
-    T->begin(ST_FFT_COLS, st);
-    TCK(launch_fft_lines(fft_launch(s, s->d_work, s->d_work, true), st));
-    T->end(st);
-    T->begin(ST_PACK_FWD, st);
-    {
+    if (fft_fast_supported(s->N)) {
+        // register-resident FFTs; the alpha pass writes the k-contiguous pencils directly
+        T->begin(ST_FFT_ROWS, st);
+        TCK(launch_fft_rows_fast(grid, s->d_work, (long long)s->batch * N * N, s->N, s->d_tw, st));
+        T->end(st);
+        T->begin(ST_FFT_COLS, st);
+        TCK(launch_fft_pencil(s->d_work, s->d_pencil, s->batch, s->N, true, s->d_tw, st));
+        T->end(st);
+    } else {
+        T->begin(ST_FFT_ROWS, st);
+        TCK(launch_fft_lines(fft_launch(s, grid, s->d_work, false), st));
+        T->end(st);
+        T->begin(ST_FFT_COLS, st);
+        TCK(launch_fft_lines(fft_launch(s, s->d_work, s->d_work, true), st));
+        T->end(st);
+        T->begin(ST_PACK_FWD, st);
         dim3 tg((unsigned)((N * N + 31) / 32), (unsigned)((N + 31) / 32), (unsigned)s->batch);
         transpose_kernel<<<tg, dim3(32, 8), 0, st>>>(s->d_work, s->d_pencil, N, N * N);
         TCK(cudaGetLastError());
+        T->end(st);
     }
-    T->end(st);
     GemmArgs a = gemm_args(s);
     a.items = s->d_items_fwd;
     a.nitems = s->n_items_fwd;
@@ -974,6 +982,15 @@ static int tc_inverse_once(TCState* s, const float2* F, float2* grid, cudaStream
     so3_tc_gemm_kernel<false><<<nctas, THREADS, SMEM_BYTES, st>>>(s->tmA_inv[0], s->tmA_inv[1], s->tmA_inv[2], a);
     TCK(cudaGetLastError());
     T->end(st);
+    if (fft_fast_supported(s->N)) {
+        T->begin(ST_FFT_COLS, st);
+        TCK(launch_fft_pencil(s->d_pencil, s->d_work, s->batch, s->N, false, s->d_tw, st));
+        T->end(st);
+        T->begin(ST_FFT_ROWS, st);
+        TCK(launch_fft_rows_fast(s->d_work, grid, (long long)s->batch * N * N, s->N, s->d_tw, st));
+        T->end(st);
+        return FFTSO3_SUCCESS;
+    }
     T->begin(ST_PACK_INV, st);
     {
         dim3 tg((unsigned)((N + 31) / 32), (unsigned)((N * N + 31) / 32), (unsigned)s->batch);

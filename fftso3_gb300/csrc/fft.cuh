@@ -28,4 +28,13 @@ void make_fft_factors(int N, FFTFactors& f);
 size_t fft_smem_bytes(int N, int lpb, bool fp64);
 cudaError_t launch_fft_lines(const FFTLaunch& L, cudaStream_t st);
 
+// Register-resident FP32 kernels for N = 64..1024, powers of two (fft_fast.cu).
+bool fft_fast_supported(int N);
+// nlines contiguous lines of N complex64: out[line][K] = FFT(in[line])[K] (in may equal out)
+cudaError_t launch_fft_rows_fast(const void* in, void* out, long long nlines, int N, const void* tw, cudaStream_t st);
+// forward: [nf][k][j1][q] -> FFT over j1 -> pencils [nf][p][q][k];
+// inverse: pencils [nf][p][q][k] -> FFT over p -> [nf][k][j1][q]   (in != out)
+cudaError_t launch_fft_pencil(const void* in, void* out, long long nf, int N, bool forward, const void* tw,
+                              cudaStream_t st);
+
 }  // namespace fftso3
