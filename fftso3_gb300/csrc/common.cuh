@@ -21,11 +21,12 @@ __host__ __device__ __forceinline__ long long s2_idx(int l, int m) { return (lon
 struct GroupPairs {
     int np;        // number of distinct (m,n) pairs served by the group (1, 2 or 4)
     int m[4], n[4];
-    double sign[4];
+    int sign[4];   // +1 or -1
 };
 
 __host__ __device__ __forceinline__ void group_mn(int g, int& m0, int& n0) {
-    int m = 0;
+    int m = (int)sqrtf((float)g);
+    while (m * m > g) --m;
     while ((m + 1) * (m + 1) <= g) ++m;
     m0 = m;
     n0 = g - m * m - m;
@@ -33,13 +34,13 @@ __host__ __device__ __forceinline__ void group_mn(int g, int& m0, int& n0) {
 
 __host__ __device__ __forceinline__ GroupPairs group_pairs(int m0, int n0) {
     GroupPairs p;
-    double s = ((m0 + n0) & 1) ? -1.0 : 1.0;
-    p.m[0] = m0;  p.n[0] = n0;  p.sign[0] = 1.0;
+    const int s = ((m0 + n0) & 1) ? -1 : 1;
+    p.m[0] = m0;  p.n[0] = n0;  p.sign[0] = 1;
     if (m0 == 0) { p.np = 1; return p; }
     p.m[1] = -m0; p.n[1] = -n0; p.sign[1] = s;
     if (n0 == m0 || n0 == -m0) { p.np = 2; return p; }
     p.m[2] = n0;  p.n[2] = m0;  p.sign[2] = s;
-    p.m[3] = -n0; p.n[3] = -m0; p.sign[3] = 1.0;
+    p.m[3] = -n0; p.n[3] = -m0; p.sign[3] = 1;
     p.np = 4;
     return p;
 }

@@ -207,6 +207,14 @@ struct GemmArgs {
     int* err;
 };
 
+// Work items carry (group, row tile, column tile, m0 << 16 | (n0 + 32768)).
+__host__ __device__ __forceinline__ int item_w(int m0, int n0) { return (m0 << 16) | (n0 + 32768); }
+__device__ __forceinline__ void item_mn(const int4& it, int& m0, int& n0)
+{
+    m0 = it.w >> 16;
+    n0 = (it.w & 0xFFFF) - 32768;
+}
+
 // Store 8 consecutive k values (one 16-byte chunk) of row R of each BF16 plane.
 __device__ __forceinline__ void store_chunk(uint32_t bplanes, int R, int chunk, const float* x8)
 {
@@ -281,7 +289,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             for (int it = blockIdx.x; it < args.nitems && !*abort_flag; it += gridDim.x) {
                 const int4 item = args.items[it];
                 int m0, n0;
-                group_mn(item.x, m0, n0);
+                item_mn(item, m0, n0);
                 const int nk = FWD ? args.Kp / BK : (B - m0 + BK - 1) / BK;
                 const long long row0 = args.grow0[item.x];
                 for (int i = 0; i < nk; ++i, ++kc) {
@@ -315,7 +323,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             for (int it = blockIdx.x; it < args.nitems && !*abort_flag; it += gridDim.x, ++t) {
                 const int4 item = args.items[it];
                 int m0, n0;
-                group_mn(item.x, m0, n0);
+                item_mn(item, m0, n0);
                 const int nk = FWD ? args.Kp / BK : (B - m0 + BK - 1) / BK;
                 const int ab = t & 1;
                 if (t >= 2 && !mbar_wait(&acce[ab], ((t >> 1) - 1) & 1, args.err, 2)) {
@@ -359,74 +367,84 @@ __global__ void __launch_bounds__(THREADS, 1)
             for (int u = (t >= 2 ? t - 2 : 0); u < t; ++u) mbar_wait(&accf[u & 1], (u >> 1) & 1, args.err, 6);
         }
     } else if (warp < 2 + NPROD) {
-        // ---------------- B-operand producers (256 threads): thread = (column pair, 16-wide k quarter).
-        // Each k-step's loads are issued one step ahead into registers so the
-        // DRAM latency overlaps the split/store of the previous step.
+        // ---------------- B-operand producers (256 threads): thread = (column pair, k quarter q4),
+        // covering the 16-byte chunks q4 and q4 + 4 of each 64-wide k-step (so the
+        // swizzled stores of a warp spread over all eight bank groups).  Each
+        // k-step's loads are issued one step ahead into registers so the DRAM
+        // latency overlaps the split/store of the previous step.
         const int pt = threadIdx.x - 64;
         const int c = pt >> 2, q4 = pt & 3;
         const int fl = c >> 2, pp = c & 3;
         const int Rre = fl * 8 + 2 * pp, Rim = Rre + 1;
-        // source of (item it, k-step i) for this thread: 16 consecutive complex values, or none
-        auto source = [&](int it, int i, int& kbase) -> const float2* {
+        struct Src {
+            const float2* p;  // run start for this (function, pair), or null
+            int lim;          // valid extent of the run (N, or nl)
+        };
+        auto source = [&](int it) -> Src {
             const int4 item = args.items[it];
             int m0, n0;
-            group_mn(item.x, m0, n0);
+            item_mn(item, m0, n0);
             const GroupPairs P = group_pairs(m0, n0);
             const int f = item.z * FPT + fl;
-            kbase = i * BK + q4 * 16;
-            if (f >= args.batch || pp >= P.np) return nullptr;
+            Src r;
+            r.lim = FWD ? N : B - m0;
+            r.p = nullptr;
+            if (f >= args.batch || pp >= P.np) return r;
             if (FWD) {
                 int pi = (-P.m[pp]) % N; if (pi < 0) pi += N;
                 int qi = (-P.n[pp]) % N; if (qi < 0) qi += N;
-                return args.pin + (long long)f * args.fstride + ((long long)pi * N + qi) * N;
-            }
-            const int nl = B - m0;
-            return args.cin + (long long)f * args.cstride + args.goff2[item.x] + (long long)pp * nl;
-        };
-        auto limit = [&](int it) -> int {
-            if (FWD) return N;
-            int m0, n0;
-            group_mn(args.items[it].x, m0, n0);
-            return B - m0;
-        };
-        auto fetch = [&](const float2* src, int kbase, int lim, float2* v) {
-            if (FWD && src && kbase + 16 <= lim) {
-                const float4* s4 = reinterpret_cast<const float4*>(src + kbase);
-#pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    float4 t = __ldg(s4 + j);
-                    v[2 * j] = make_float2(t.x, t.y);
-                    v[2 * j + 1] = make_float2(t.z, t.w);
-                }
+                r.p = args.pin + (long long)f * args.fstride + ((long long)pi * N + qi) * N;
             } else {
+                r.p = args.cin + (long long)f * args.cstride + args.goff2[item.x] + (long long)pp * r.lim;
+            }
+            return r;
+        };
+        auto fetch = [&](const Src& sr, int i, float2* v) {
 #pragma unroll
-                for (int j = 0; j < 16; ++j)
-                    v[j] = (src && kbase + j < lim) ? __ldg(src + kbase + j) : make_float2(0.f, 0.f);
+            for (int h = 0; h < 2; ++h) {
+                const int k = i * BK + (q4 + 4 * h) * 8;
+                if (FWD && sr.p && k + 8 <= sr.lim) {
+                    const float4* s4 = reinterpret_cast<const float4*>(sr.p + k);
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        float4 t = __ldg(s4 + j);
+                        v[8 * h + 2 * j] = make_float2(t.x, t.y);
+                        v[8 * h + 2 * j + 1] = make_float2(t.z, t.w);
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 8; ++j)
+                        v[8 * h + j] = (sr.p && k + j < sr.lim) ? __ldg(sr.p + k + j) : make_float2(0.f, 0.f);
+                }
             }
         };
         int kc = 0;
         int it = blockIdx.x, i = 0;
         float2 cur[16];
-        int kb_cur = 0;
+        Src scur, snxt;
+        int nk_cur = 0;
         if (it < args.nitems) {
-            const float2* s0 = source(it, 0, kb_cur);
-            fetch(s0, kb_cur, limit(it), cur);
+            scur = source(it);
+            int m0, n0;
+            item_mn(args.items[it], m0, n0);
+            nk_cur = FWD ? args.Kp / BK : (B - m0 + BK - 1) / BK;
+            fetch(scur, 0, cur);
         }
         while (it < args.nitems && !*abort_flag) {
-            int m0, n0;
-            group_mn(args.items[it].x, m0, n0);
-            const int nk = FWD ? args.Kp / BK : (B - m0 + BK - 1) / BK;
-            int it2 = it, i2 = i + 1;
-            if (i2 == nk) {
+            int it2 = it, i2 = i + 1, nk2 = nk_cur;
+            snxt = scur;
+            if (i2 == nk_cur) {
                 it2 += gridDim.x;
                 i2 = 0;
+                if (it2 < args.nitems) {
+                    snxt = source(it2);
+                    int m0, n0;
+                    item_mn(args.items[it2], m0, n0);
+                    nk2 = FWD ? args.Kp / BK : (B - m0 + BK - 1) / BK;
+                }
             }
             float2 nxt[16];
-            int kb_nxt = 0;
-            if (it2 < args.nitems) {
-                const float2* s1 = source(it2, i2, kb_nxt);
-                fetch(s1, kb_nxt, limit(it2), nxt);
-            }
+            if (it2 < args.nitems) fetch(snxt, i2, nxt);
             const int s = kc % STAGES;
             if (kc >= STAGES && !mbar_wait(&empty[s], ((kc / STAGES) - 1) & 1, args.err, 4)) {
                 *abort_flag = 1;
@@ -435,15 +453,16 @@ __global__ void __launch_bounds__(THREADS, 1)
             const uint32_t bpl = smem_u32(smem + s * STAGE_BYTES + STAGE_A);
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
+                const int chunk = q4 + 4 * h;
+                const int k = i * BK + chunk * 8;
                 float re[8], im[8];
 #pragma unroll
                 for (int j = 0; j < 8; ++j) {
                     const float2 v = cur[h * 8 + j];
-                    const float wk = FWD ? ((kb_cur + h * 8 + j < N) ? wsm[kb_cur + h * 8 + j] : 0.f) : 1.f;
+                    const float wk = FWD ? ((k + j < N) ? wsm[k + j] : 0.f) : 1.f;
                     re[j] = v.x * wk;
                     im[j] = v.y * wk;
                 }
-                const int chunk = q4 * 2 + h;
                 store_chunk(bpl, Rre, chunk, re);
                 store_chunk(bpl, Rim, chunk, im);
             }
@@ -452,7 +471,8 @@ __global__ void __launch_bounds__(THREADS, 1)
             if (lane == 0) mbar_arrive(&full[s]);
 #pragma unroll
             for (int j = 0; j < 16; ++j) cur[j] = nxt[j];
-            kb_cur = kb_nxt;
+            scur = snxt;
+            nk_cur = nk2;
             it = it2;
             i = i2;
             ++kc;
@@ -465,8 +485,20 @@ __global__ void __launch_bounds__(THREADS, 1)
         for (int it = blockIdx.x; it < args.nitems && !*abort_flag; it += gridDim.x, ++t) {
             const int4 item = args.items[it];
             int m0, n0;
-            group_mn(item.x, m0, n0);
+            item_mn(item, m0, n0);
             const GroupPairs P = group_pairs(m0, n0);
+            const int nl = B - m0;
+            long long poff[4];
+#pragma unroll
+            for (int p = 0; p < 4; ++p) {
+                if (FWD) {
+                    poff[p] = args.goff2[item.x] + (long long)p * nl;
+                } else {
+                    int pi = P.m[p] % N; if (pi < 0) pi += N;
+                    int qi = P.n[p] % N; if (qi < 0) qi += N;
+                    poff[p] = ((long long)pi * N + qi) * N;
+                }
+            }
             const int ab = t & 1;
             if (!mbar_wait(&accf[ab], (t >> 1) & 1, args.err, 5)) {
                 *abort_flag = 1;
@@ -486,21 +518,22 @@ __global__ void __launch_bounds__(THREADS, 1)
                     if (f >= args.batch) continue;
                     if (FWD) {
                         const int row = item.y * BM + r;
-                        const int nl = B - m0;
                         if (row >= nl) continue;
-                        float2* Fo = args.cout + (long long)f * args.cstride + args.goff2[item.x] + row;
-                        for (int p = 0; p < P.np; ++p) {
+                        float2* Fo = args.cout + (long long)f * args.cstride + row;
+#pragma unroll
+                        for (int p = 0; p < 4; ++p) {
+                            if (p >= P.np) break;
                             const float sg = (float)P.sign[p];
-                            Fo[(long long)p * nl] = make_float2(sg * v[fq * 8 + 2 * p], sg * v[fq * 8 + 2 * p + 1]);
+                            Fo[poff[p]] = make_float2(sg * v[fq * 8 + 2 * p], sg * v[fq * 8 + 2 * p + 1]);
                         }
                     } else {
                         const int k = item.y * BM + r;
                         if (k >= N) continue;
                         float2* Ho = args.pout + (long long)f * args.fstride + k;
-                        for (int p = 0; p < P.np; ++p) {
-                            int pi = P.m[p] % N; if (pi < 0) pi += N;
-                            int qi = P.n[p] % N; if (qi < 0) qi += N;
-                            Ho[((long long)pi * N + qi) * N] = make_float2(v[fq * 8 + 2 * p], v[fq * 8 + 2 * p + 1]);
+#pragma unroll
+                        for (int p = 0; p < 4; ++p) {
+                            if (p >= P.np) break;
+                            Ho[poff[p]] = make_float2(v[fq * 8 + 2 * p], v[fq * 8 + 2 * p + 1]);
                         }
                     }
                 }
@@ -804,8 +837,8 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
         goff2[g] = acc2;
         acc2 += (long long)group_pairs(m0, n0).np * nl;
         for (int nt = 0; nt < s->ntiles; ++nt) {
-            for (int mt = 0; mt * BM < nl; ++mt) itf.push_back(make_int4(g, mt, nt, 0));
-            for (int mt = 0; mt * BM < N; ++mt) iti.push_back(make_int4(g, mt, nt, 0));
+            for (int mt = 0; mt * BM < nl; ++mt) itf.push_back(make_int4(g, mt, nt, item_w(m0, n0)));
+            for (int mt = 0; mt * BM < N; ++mt) iti.push_back(make_int4(g, mt, nt, item_w(m0, n0)));
         }
     }
     std::stable_sort(iti.begin(), iti.end(), [&](const int4& a, const int4& b) {
