@@ -954,10 +954,10 @@ static int tc_forward_once(TCState* s, const float2* grid, float2* F, cudaStream
     if (fft_fast_supported(s->N)) {
         // register-resident FFTs; the alpha pass writes the k-contiguous pencils directly
         T->begin(ST_FFT_ROWS, st);
-        TCK(launch_fft_rows_fast(grid, s->d_work, (long long)s->batch * N * N, s->N, s->d_tw, st));
+        TCK(launch_fft_grid_pass(grid, s->d_work, s->batch, s->N, 1, s->d_tw, st));
         T->end(st);
         T->begin(ST_FFT_COLS, st);
-        TCK(launch_fft_pencil(s->d_work, s->d_pencil, s->batch, s->N, true, s->d_tw, st));
+        TCK(launch_fft_grid_pass(s->d_work, s->d_pencil, s->batch, s->N, 2, s->d_tw, st));
         T->end(st);
     } else {
         T->begin(ST_FFT_ROWS, st);
@@ -1017,10 +1017,10 @@ static int tc_inverse_once(TCState* s, const float2* F, float2* grid, cudaStream
     T->end(st);
     if (fft_fast_supported(s->N)) {
         T->begin(ST_FFT_COLS, st);
-        TCK(launch_fft_pencil(s->d_pencil, s->d_work, s->batch, s->N, false, s->d_tw, st));
+        TCK(launch_fft_grid_pass(s->d_pencil, s->d_work, s->batch, s->N, -2, s->d_tw, st));
         T->end(st);
         T->begin(ST_FFT_ROWS, st);
-        TCK(launch_fft_rows_fast(s->d_work, grid, (long long)s->batch * N * N, s->N, s->d_tw, st));
+        TCK(launch_fft_grid_pass(s->d_work, grid, s->batch, s->N, -1, s->d_tw, st));
         T->end(st);
         return FFTSO3_SUCCESS;
     }

@@ -32,9 +32,12 @@ cudaError_t launch_fft_lines(const FFTLaunch& L, cudaStream_t st);
 bool fft_fast_supported(int N);
 // nlines contiguous lines of N complex64: out[line][K] = FFT(in[line])[K] (in may equal out)
 cudaError_t launch_fft_rows_fast(const void* in, void* out, long long nlines, int N, const void* tw, cudaStream_t st);
-// forward: [nf][k][j1][q] -> FFT over j1 -> pencils [nf][p][q][k];
-// inverse: pencils [nf][p][q][k] -> FFT over p -> [nf][k][j1][q]   (in != out)
-cudaError_t launch_fft_pencil(const void* in, void* out, long long nf, int N, bool forward, const void* tw,
-                              cudaStream_t st);
+// Tiled transposing passes over nf grids of N^3 complex64 (in != out):
+//   pass  1: grid [nf][k][j1][j2] -> FFT over j2 -> T1 [nf][k][q][j1]
+//   pass  2: T1 [nf][k][q][j1]    -> FFT over j1 -> pencils [nf][p][q][k]
+//   pass -2: pencils [nf][p][q][k] -> FFT over p -> T1 [nf][k][q][j1]
+//   pass -1: T1 [nf][k][q][j1]     -> FFT over q -> grid [nf][k][j1][j2]
+cudaError_t launch_fft_grid_pass(const void* in, void* out, long long nf, int N, int pass, const void* tw,
+                                 cudaStream_t st);
 
 }  // namespace fftso3

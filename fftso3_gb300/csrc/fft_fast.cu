@@ -11,15 +11,13 @@
 // W[j] = e^{-2 pi i j / N}, staged in shared memory as FP32.
 //
 // Kernels:
-//   fft_rows_reg      lines contiguous (the gamma / q axis), in place or not;
-//   fft_pencil_fwd    the alpha axis of [fn][k][j1][q] with the result written
-//                     as k-contiguous pencils [fn][p][q][k] (column FFT fused
-//                     with the transpose the beta-sum GEMM wants);
-//   fft_pencil_inv    the reverse: pencils [fn][p][q][k] -> FFT over p ->
-//                     [fn][k][j1][q].
-// The pencil kernels stage a tile of KT x QT lines (4 beta indices x 4 columns)
-// in shared memory so that both the line reads and the pencil writes move
-// whole 32-byte sectors.
+//   fft_rows_reg  lines contiguous (one axis of a contiguous array);
+//   fft_tile      a tile of 16 lines staged in shared memory with one side
+//                 contiguous and the other transposed, so a 2-D transform of
+//                 the Euler grid is two passes that both read and write whole
+//                 128-byte runs, the second one producing the k-contiguous
+//                 pencils [fn][p][q][k] the beta-sum GEMM consumes (and the
+//                 reverse for the inverse).
 #include "common.cuh"
 #include "fft.cuh"
 
@@ -133,57 +131,56 @@ __global__ void __launch_bounds__(32 * WPB) fft_rows_reg(const float2* __restric
     }
 }
 
-constexpr int KT = 4, QT = 4;        // tile: 4 beta indices x 4 columns = 16 lines
+constexpr int TL = 16;               // lines per CTA tile
 constexpr int PWARPS = 8;            // 2 lines per warp
 
 // padded position of element j in a staged line (one pad slot every R elements)
 template <int R>
 __device__ __forceinline__ int ppos(int j) { return j + (j >> ilog2(R)); }
 
-// FORWARD = true : in [fn][k][j1][q]  -> FFT over j1 -> out pencils [fn][p][q][k]
-// FORWARD = false: in pencils [fn][p][q][k] -> FFT over p -> out [fn][k][j1][q]
-template <int R, bool FORWARD>
-__global__ void __launch_bounds__(32 * PWARPS) fft_pencil(const float2* __restrict__ in, float2* __restrict__ out,
-                                                          long long nf, const double2* __restrict__ tw)
+// A tile of TL lines with one side contiguous and the other transposed.
+//   contiguous side: line l, element j at  cbase + l * Ls + j
+//   transposed side: line l, element j at  tbase + j * Js + l    (TL consecutive l)
+// cbase = f N^3 + o Oc + bb TL Ls,  tbase = f N^3 + o Ot + bb TL, with the CTA
+// index split into (f, o < N, bb < N / TL).  C2T = true reads the contiguous
+// side and writes the transposed one; C2T = false the reverse.  Both sides
+// move TL * 8 = 128-byte runs.
+template <int R, bool C2T>
+__global__ void __launch_bounds__(32 * PWARPS) fft_tile(const float2* __restrict__ in, float2* __restrict__ out,
+                                                        long long Oc, long long Ls, long long Ot, long long Js,
+                                                        const double2* __restrict__ tw)
 {
     constexpr int N = 32 * R;
     constexpr int LR = ilog2(R);
     constexpr int LP = N + N / R + 1;  // padded staged line
     extern __shared__ float2 smem_f2[];
     float2* Ws = smem_f2;
-    float2* T = smem_f2 + N;  // [KT * QT][LP]
+    float2* T = smem_f2 + N;  // [TL][LP]
     load_twiddles<N>(Ws, tw);
 
-    const long long ntk = N / KT, ntq = N / QT;
+    constexpr int NB = N / TL;
     const long long b = blockIdx.x;
-    const long long f = b / (ntk * ntq);
-    const int k0 = (int)((b / ntq) % ntk) * KT;
-    const int q0 = (int)(b % ntq) * QT;
-    const long long NN = (long long)N * N;
-    const float2* src = in + f * NN * N;
-    float2* dst = out + f * NN * N;
-    constexpr int NL = KT * QT;
-    // load: line = kt * QT + qt
-    for (int e = threadIdx.x; e < NL * N; e += blockDim.x) {
-        int j, kt, qt;
-        long long off;
-        if (FORWARD) {  // q fastest, then j1, then k: runs of QT columns
-            qt = e % QT;
-            j = (e / QT) % N;
-            kt = e / (QT * N);
-            off = (long long)(k0 + kt) * NN + (long long)j * N + (q0 + qt);
-        } else {        // k fastest, then q, then p: runs of KT beta indices
-            kt = e % KT;
-            qt = (e / KT) % QT;
-            j = e / (KT * QT);
-            off = (long long)j * NN + (long long)(q0 + qt) * N + (k0 + kt);
+    const long long f = b / ((long long)N * NB);
+    const long long o = (b / NB) % N;
+    const long long bb = b % NB;
+    const long long N3 = (long long)N * N * N;
+    const long long cbase = f * N3 + o * Oc + bb * TL * Ls;
+    const long long tbase = f * N3 + o * Ot + bb * TL;
+    if (C2T) {
+        for (int e = threadIdx.x; e < TL * N; e += blockDim.x) {
+            const int j = e % N, l = e / N;
+            T[l * LP + ppos<R>(j)] = in[cbase + l * Ls + j];
         }
-        T[(kt * QT + qt) * LP + ppos<R>(j)] = src[off];
+    } else {
+        for (int e = threadIdx.x; e < TL * N; e += blockDim.x) {
+            const int l = e % TL, j = e / TL;
+            T[l * LP + ppos<R>(j)] = in[tbase + (long long)j * Js + l];
+        }
     }
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int t5 = brev(lane, 5);
-    for (int line = warp; line < NL; line += PWARPS) {
+    for (int line = warp; line < TL; line += PWARPS) {
         float2* Tl = T + line * LP;
         float2 v[R];
 #pragma unroll
@@ -194,21 +191,46 @@ __global__ void __launch_bounds__(32 * PWARPS) fft_pencil(const float2* __restri
         for (int k1 = 0; k1 < R; ++k1) Tl[ppos<R>(k1 + R * t5)] = v[brev(k1, LR)];
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < NL * N; e += blockDim.x) {
-        int j, kt, qt;
-        long long off;
-        if (FORWARD) {  // pencils: k fastest, then q, then p
-            kt = e % KT;
-            qt = (e / KT) % QT;
-            j = e / (KT * QT);
-            off = (long long)j * NN + (long long)(q0 + qt) * N + (k0 + kt);
-        } else {        // rows: q fastest, then j1, then k
-            qt = e % QT;
-            j = (e / QT) % N;
-            kt = e / (QT * N);
-            off = (long long)(k0 + kt) * NN + (long long)j * N + (q0 + qt);
+    if (C2T) {
+        for (int e = threadIdx.x; e < TL * N; e += blockDim.x) {
+            const int l = e % TL, j = e / TL;
+            out[tbase + (long long)j * Js + l] = T[l * LP + ppos<R>(j)];
         }
-        dst[off] = T[(kt * QT + qt) * LP + ppos<R>(j)];
+    } else {
+        for (int e = threadIdx.x; e < TL * N; e += blockDim.x) {
+            const int j = e % N, l = e / N;
+            out[cbase + l * Ls + j] = T[l * LP + ppos<R>(j)];
+        }
+    }
+}
+
+template <int R, bool C2T>
+static cudaError_t tile_r(const void* in, void* out, long long nf, long long Oc, long long Ls, long long Ot,
+                          long long Js, const void* tw, cudaStream_t st)
+{
+    constexpr int N = 32 * R;
+    constexpr int LP = N + N / R + 1;
+    const size_t smem = sizeof(float2) * ((size_t)N + (size_t)TL * LP);
+    auto k = fft_tile<R, C2T>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const long long nblk = nf * (long long)N * (N / TL);
+    k<<<(unsigned)nblk, 32 * PWARPS, smem, st>>>((const float2*)in, (float2*)out, Oc, Ls, Ot, Js,
+                                                  (const double2*)tw);
+    return cudaGetLastError();
+}
+
+template <bool C2T>
+static cudaError_t tile_dispatch(const void* in, void* out, long long nf, int N, long long Oc, long long Ls,
+                                 long long Ot, long long Js, const void* tw, cudaStream_t st)
+{
+    switch (N) {
+        case 64: return tile_r<2, C2T>(in, out, nf, Oc, Ls, Ot, Js, tw, st);
+        case 128: return tile_r<4, C2T>(in, out, nf, Oc, Ls, Ot, Js, tw, st);
+        case 256: return tile_r<8, C2T>(in, out, nf, Oc, Ls, Ot, Js, tw, st);
+        case 512: return tile_r<16, C2T>(in, out, nf, Oc, Ls, Ot, Js, tw, st);
+        case 1024: return tile_r<32, C2T>(in, out, nf, Oc, Ls, Ot, Js, tw, st);
+        default: return cudaErrorNotSupported;
     }
 }
 
@@ -219,20 +241,6 @@ static cudaError_t rows_r(const void* in, void* out, long long nlines, const voi
     const long long per = (long long)WPB * LPW;
     fft_rows_reg<R, WPB, LPW><<<(unsigned)((nlines + per - 1) / per), 32 * WPB, 0, st>>>(
         (const float2*)in, (float2*)out, nlines, (const double2*)tw);
-    return cudaGetLastError();
-}
-
-template <int R, bool FWD>
-static cudaError_t pencil_r(const void* in, void* out, long long nf, const void* tw, cudaStream_t st)
-{
-    constexpr int N = 32 * R;
-    constexpr int LP = N + N / R + 1;
-    const size_t smem = sizeof(float2) * ((size_t)N + (size_t)KT * QT * LP);
-    auto k = fft_pencil<R, FWD>;
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    const long long nblk = nf * (N / KT) * (N / QT);
-    k<<<(unsigned)nblk, 32 * PWARPS, smem, st>>>((const float2*)in, (float2*)out, nf, (const double2*)tw);
     return cudaGetLastError();
 }
 
@@ -252,16 +260,22 @@ cudaError_t launch_fft_rows_fast(const void* in, void* out, long long nlines, in
     }
 }
 
-cudaError_t launch_fft_pencil(const void* in, void* out, long long nf, int N, bool forward, const void* tw,
-                              cudaStream_t st)
+// Forward passes of one batch of N^3 grids (see fft.cuh):
+//   pass 1: grid [f][k][j1][j2] -> FFT over j2 -> T1 [f][k][q][j1]
+//   pass 2: T1 [f][k][q][j1]    -> FFT over j1 -> pencils [f][p][q][k]
+// Inverse passes:
+//   pass 2': pencils [f][p][q][k] -> FFT over p  -> T1 [f][k][q][j1]
+//   pass 1': T1 [f][k][q][j1]     -> FFT over q  -> grid [f][k][j1][j2]
+cudaError_t launch_fft_grid_pass(const void* in, void* out, long long nf, int N, int pass, const void* tw,
+                                 cudaStream_t st)
 {
-    switch (N) {
-        case 64: return forward ? ffast::pencil_r<2, true>(in, out, nf, tw, st) : ffast::pencil_r<2, false>(in, out, nf, tw, st);
-        case 128: return forward ? ffast::pencil_r<4, true>(in, out, nf, tw, st) : ffast::pencil_r<4, false>(in, out, nf, tw, st);
-        case 256: return forward ? ffast::pencil_r<8, true>(in, out, nf, tw, st) : ffast::pencil_r<8, false>(in, out, nf, tw, st);
-        case 512: return forward ? ffast::pencil_r<16, true>(in, out, nf, tw, st) : ffast::pencil_r<16, false>(in, out, nf, tw, st);
-        case 1024: return forward ? ffast::pencil_r<32, true>(in, out, nf, tw, st) : ffast::pencil_r<32, false>(in, out, nf, tw, st);
-        default: return cudaErrorNotSupported;
+    const long long N1 = N, N2 = (long long)N * N;
+    switch (pass) {
+        case 1: return ffast::tile_dispatch<true>(in, out, nf, N, N2, N1, N2, N1, tw, st);
+        case 2: return ffast::tile_dispatch<true>(in, out, nf, N, N1, N2, N1, N2, tw, st);
+        case -2: return ffast::tile_dispatch<false>(in, out, nf, N, N1, N2, N1, N2, tw, st);
+        case -1: return ffast::tile_dispatch<false>(in, out, nf, N, N2, N1, N2, N1, tw, st);
+        default: return cudaErrorInvalidValue;
     }
 }
 
