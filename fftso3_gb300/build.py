@@ -19,9 +19,10 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libfftso3_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+          "--expt-relaxed-constexpr",
           "-I", os.path.join(HERE, "..", "include")]
-PER_FILE = {"tables.cu": ["-fmad=false"]}
+PER_FILE = {"tables.cu": ["-fmad=false"], "noalloc.cu": ["-fmad=false"]}
 
 
 def nvcc() -> str:
