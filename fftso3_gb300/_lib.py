@@ -61,6 +61,7 @@ SIGNATURES = {
     "fftso3_inverse_host": (_i, [_vp, _vp, _vp, _vp]),
     "fftso3_inverse_points": (_i, [_vp, _vp, _i, _dp, _i, _vp, _vp]),
     "fftso3_wigner_d": (_i, [_d, _i, _i, _dp]),
+    "fftso3_forward_noalloc": (_i, [_i, _vp, _vp, _vp]),
 }
 
 _lib = None

@@ -91,6 +91,11 @@ std::vector<double> log_factorials(int n)
 
 }  // namespace
 
+namespace fftso3 {
+// Lets other translation units report through fftso3_last_error_string().
+void set_last_error(const std::string& msg) { g_err = msg; }
+}  // namespace fftso3
+
 struct fftso3_plan {
     int kind = 0, L = 0, B = 0, N = 0, batch = 0, precision = 0, recursion = 0;
     unsigned flags = 0;

@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 namespace fftso3 {
 
 // Packed SO(3) coefficient layout (fdcl_FFTSO3_matrix.cpp:43-47 stores
@@ -44,6 +46,9 @@ __host__ __device__ __forceinline__ GroupPairs group_pairs(int m0, int n0) {
     p.np = 4;
     return p;
 }
+
+// Records the message returned by fftso3_last_error_string() on this thread.
+void set_last_error(const std::string& msg);
 
 template <typename T> struct cplx;
 template <> struct cplx<double> { using type = double2; };

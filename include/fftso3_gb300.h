@@ -142,6 +142,26 @@ int fftso3_inverse_points(fftso3_plan* plan, const void* coeffs, int index, cons
  * Replaces wigner_d(beta) (fdcl_FFTSO3.cpp:122-194). */
 int fftso3_wigner_d(double beta, int l_max, int recursion, double* d_out_host);
 
+/* Largest l_max accepted by fftso3_forward_noalloc(). */
+#define FFTSO3_NOALLOC_MAX_LMAX 31
+
+/* Allocation-free forward transform: FFTSO3_SO3_COMPLEX, FP64, the reference
+ * Wigner-d recursion, one function, l_max <= FFTSO3_NOALLOC_MAX_LMAX.  No
+ * counterpart in the reference: it is the forward transform of a batch-1
+ * FP64 plan (fdcl_FFTSO3.cpp:654-763 semantics) for callers that cannot
+ * allocate device memory -- a host that owns all device memory and does not
+ * let libraries call cudaMalloc, or a latency-critical loop where
+ * cudaMalloc/cudaFree would synchronise the device.  It allocates nothing: its
+ * intermediates (tables, seeds, the Wigner-d table and the 64^3 FFT work
+ * grid, about 10 MB) live in one file-scope __device__ array that every GPU
+ * which loads the library holds until the process exits.  grid (complex128,
+ * (2l_max+2)^3) and coeffs (complex128) are device pointers; the call is
+ * asynchronous on `stream`.  The first call on a device looks up that array's
+ * address (cudaGetSymbolAddress, with the device current): make it before any
+ * stream capture.  All calls share the array, so calls that overlap on the GPU
+ * race; serialise them.  l_max above the limit returns FFTSO3_ERR_INVALID_ARG. */
+int fftso3_forward_noalloc(int l_max, const void* grid, void* coeffs, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
