@@ -298,6 +298,21 @@ def main() -> None:
         im = float(np.abs(gi - g0_ref).max() / np.sqrt(np.mean(np.abs(g0_ref) ** 2)))
         acc = {"forward_rel_rms": fr, "forward_rel_max_per_l": fm, "inverse_rel_rms": ir,
                "inverse_rel_max": im, "against": "FP64 GPU path (stable recursion) on the same function"}
+        # one residual refinement step F += forward(f - inverse(F)) (FFTSO3_FLAG_REFINE), same function
+        pr = _lib.Plan(_lib.SO3_COMPLEX, L, 1, "tc_bf16x3", "stable", _lib.FLAG_REFINE)
+        cr = torch.empty(C, dtype=torch.complex64, device=dev)
+        pr.forward(g0_c64.data_ptr(), cr.data_ptr(), sp)
+        e0r, e1r = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0r.record(stream)
+        pr.forward(g0_c64.data_ptr(), cr.data_ptr(), sp)
+        e1r.record(stream)
+        torch.cuda.synchronize()
+        pr.check()
+        rr, rm = per_l_errors(cr.cpu().numpy().astype(np.complex128), F0_fp64, L)
+        acc["refined_forward_rel_rms"] = rr
+        acc["refined_forward_rel_max_per_l"] = rm
+        acc["refined_forward_ms_batch1"] = e0r.elapsed_time(e1r)
+        del pr, cr
     del coef_in, coef0
 
     # ---- timed region: inputs resident in HBM (each grid 1 GB >> 129 MB L2)

@@ -146,7 +146,7 @@ __device__ __forceinline__ int ppos(int j) { return j + (j >> ilog2(R)); }
 // side and writes the transposed one; C2T = false the reverse.  Both sides
 // move TL * 8 = 128-byte runs.
 template <int R, bool C2T>
-__global__ void __launch_bounds__(32 * PWARPS) fft_tile(const float2* __restrict__ in, float2* __restrict__ out,
+__global__ void __launch_bounds__(32 * PWARPS, 3) fft_tile(const float2* __restrict__ in, float2* __restrict__ out,
                                                         long long Oc, long long Ls, long long Ot, long long Js,
                                                         const double2* __restrict__ tw)
 {
@@ -166,15 +166,40 @@ __global__ void __launch_bounds__(32 * PWARPS) fft_tile(const float2* __restrict
     const long long N3 = (long long)N * N * N;
     const long long cbase = f * N3 + o * Oc + bb * TL * Ls;
     const long long tbase = f * N3 + o * Ot + bb * TL;
-    if (C2T) {
-        for (int e = threadIdx.x; e < TL * N; e += blockDim.x) {
-            const int j = e % N, l = e / N;
-            T[l * LP + ppos<R>(j)] = in[cbase + l * Ls + j];
+    // Load: every thread issues all of its 16-byte loads (two complex values
+    // each) before touching shared memory, so many requests are in flight.
+    constexpr int NV = TL * N / 2 / (32 * PWARPS);  // float4 loads per thread
+    static_assert(TL * N / 2 % (32 * PWARPS) == 0, "tile must split evenly over the threads");
+    constexpr int VB = NV < 8 ? NV : 8;  // loads in flight per thread per batch
+    const float4* in4 = reinterpret_cast<const float4*>(in);
+#pragma unroll 1
+    for (int u0 = 0; u0 < NV; u0 += VB) {
+        float4 buf[VB];
+#pragma unroll
+        for (int v = 0; v < VB; ++v) {
+            const int u = u0 + v;
+            const int e2 = threadIdx.x + u * 32 * PWARPS;
+            if (C2T) {  // pair (j, j + 1) of line l
+                const int j = (e2 % (N / 2)) * 2, l = e2 / (N / 2);
+                buf[v] = __ldg(in4 + (cbase + l * Ls + j) / 2);
+            } else {    // pair (l, l + 1) of element j
+                const int l = (e2 % (TL / 2)) * 2, j = e2 / (TL / 2);
+                buf[v] = __ldg(in4 + (tbase + (long long)j * Js + l) / 2);
+            }
         }
-    } else {
-        for (int e = threadIdx.x; e < TL * N; e += blockDim.x) {
-            const int l = e % TL, j = e / TL;
-            T[l * LP + ppos<R>(j)] = in[tbase + (long long)j * Js + l];
+#pragma unroll
+        for (int v = 0; v < VB; ++v) {
+            const int u = u0 + v;
+            const int e2 = threadIdx.x + u * 32 * PWARPS;
+            if (C2T) {
+                const int j = (e2 % (N / 2)) * 2, l = e2 / (N / 2);
+                T[l * LP + ppos<R>(j)] = make_float2(buf[v].x, buf[v].y);
+                T[l * LP + ppos<R>(j + 1)] = make_float2(buf[v].z, buf[v].w);
+            } else {
+                const int l = (e2 % (TL / 2)) * 2, j = e2 / (TL / 2);
+                T[l * LP + ppos<R>(j)] = make_float2(buf[v].x, buf[v].y);
+                T[(l + 1) * LP + ppos<R>(j)] = make_float2(buf[v].z, buf[v].w);
+            }
         }
     }
     __syncthreads();
@@ -191,15 +216,20 @@ __global__ void __launch_bounds__(32 * PWARPS) fft_tile(const float2* __restrict
         for (int k1 = 0; k1 < R; ++k1) Tl[ppos<R>(k1 + R * t5)] = v[brev(k1, LR)];
     }
     __syncthreads();
-    if (C2T) {
-        for (int e = threadIdx.x; e < TL * N; e += blockDim.x) {
-            const int l = e % TL, j = e / TL;
-            out[tbase + (long long)j * Js + l] = T[l * LP + ppos<R>(j)];
-        }
-    } else {
-        for (int e = threadIdx.x; e < TL * N; e += blockDim.x) {
-            const int j = e % N, l = e / N;
-            out[cbase + l * Ls + j] = T[l * LP + ppos<R>(j)];
+    {
+        float4* out4 = reinterpret_cast<float4*>(out);
+#pragma unroll 4
+        for (int u = 0; u < NV; ++u) {
+            const int e2 = threadIdx.x + u * 32 * PWARPS;
+            if (C2T) {  // transposed side: pair (l, l + 1) of element j
+                const int l = (e2 % (TL / 2)) * 2, j = e2 / (TL / 2);
+                const float2 a = T[l * LP + ppos<R>(j)], b = T[(l + 1) * LP + ppos<R>(j)];
+                out4[(tbase + (long long)j * Js + l) / 2] = make_float4(a.x, a.y, b.x, b.y);
+            } else {    // contiguous side: pair (j, j + 1) of line l
+                const int j = (e2 % (N / 2)) * 2, l = e2 / (N / 2);
+                const float2 a = T[l * LP + ppos<R>(j)], b = T[l * LP + ppos<R>(j + 1)];
+                out4[(cbase + l * Ls + j) / 2] = make_float4(a.x, a.y, b.x, b.y);
+            }
         }
     }
 }
