@@ -96,6 +96,72 @@ __device__ __forceinline__ void warp_fft(float2 (&v)[R], const float2* __restric
     }
 }
 
+// Line FFT of a staged line through shared memory (fewer shuffles than warp_fft).
+// Tl holds the line at ppos(j); the result is written back to Tl at ppos(K).
+//   step A: lane t takes x[t + 32 i] (i < R), R-point DFT over i, twiddle
+//           w_N^{t k1}, and stores Y[t][k1] at Tl[k1 * 33 + t];
+//   step B: lane (k1, h) (h < P = 32 / R) takes Y[P s + h][k1] (s < R), R-point
+//           DFT over s (index kappa), twiddle w_32^{h kappa}, then a P-point DFT
+//           across its P lanes (log2 P shuffle stages) giving
+//           Z_k1[kappa + R brP(h)] = X[k1 + R kappa + R^2 brP(h)].
+template <int R>
+__device__ __forceinline__ void line_fft_smem(float2* Tl, const float2* __restrict__ W, int lane)
+{
+    constexpr int N = 32 * R;
+    constexpr int LR = ilog2(R);
+    constexpr int P = 32 / R;
+    constexpr int LP2 = ilog2(P);
+    float2 v[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) v[i] = Tl[(lane + 32 * i) + ((lane + 32 * i) >> LR)];
+    reg_dif<R>(v, W, N);
+    __syncwarp();
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int k1 = brev(r, LR);
+        const float2 y = (r == 0) ? v[r] : cmulf(v[r], W[lane * k1]);
+        Tl[k1 * 33 + lane] = y;
+    }
+    __syncwarp();
+    const int k1 = lane / P, h = lane % P;
+#pragma unroll
+    for (int s2 = 0; s2 < R; ++s2) v[s2] = Tl[k1 * 33 + P * s2 + h];
+    reg_dif<R>(v, W, N);  // R-point DFT over s: register r holds kappa = brR(r)
+    if (P > 1) {
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+            const int kappa = brev(r, LR);
+            if (h != 0) v[r] = cmulf(v[r], W[(h * kappa) * (N / 32)]);
+        }
+#pragma unroll
+        for (int hh = P / 2; hh >= 1; hh >>= 1) {
+            const bool upper = (h & hh) != 0;
+            const int kk = h & (hh - 1);
+            const float2 w = W[kk * (N / (2 * hh))];
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const float ox = __shfl_xor_sync(FULL, v[r].x, hh);
+                const float oy = __shfl_xor_sync(FULL, v[r].y, hh);
+                if (!upper) {
+                    v[r].x += ox;
+                    v[r].y += oy;
+                } else {
+                    v[r] = cmulf(make_float2(ox - v[r].x, oy - v[r].y), w);
+                }
+            }
+        }
+    }
+    __syncwarp();
+    const int c = brev(h, LP2);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int kappa = brev(r, LR);
+        const int K = k1 + R * kappa + R * R * c;
+        Tl[K + (K >> LR)] = v[r];
+    }
+    __syncwarp();
+}
+
 template <int N>
 __device__ __forceinline__ void load_twiddles(float2* Ws, const double2* __restrict__ tw)
 {
@@ -204,17 +270,8 @@ __global__ void __launch_bounds__(32 * PWARPS, 3) fft_tile(const float2* __restr
     }
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int t5 = brev(lane, 5);
-    for (int line = warp; line < TL; line += PWARPS) {
-        float2* Tl = T + line * LP;
-        float2 v[R];
-#pragma unroll
-        for (int i = 0; i < R; ++i) v[i] = Tl[ppos<R>(lane + 32 * i)];
-        warp_fft<R>(v, Ws, lane);
-        __syncwarp();
-#pragma unroll
-        for (int k1 = 0; k1 < R; ++k1) Tl[ppos<R>(k1 + R * t5)] = v[brev(k1, LR)];
-    }
+    
+    for (int line = warp; line < TL; line += PWARPS) line_fft_smem<R>(T + line * LP, Ws, lane);
     __syncthreads();
     {
         float4* out4 = reinterpret_cast<float4*>(out);
