@@ -96,37 +96,40 @@ __device__ __forceinline__ void warp_fft(float2 (&v)[R], const float2* __restric
     }
 }
 
-// Line FFT of a staged line through shared memory (fewer shuffles than warp_fft).
-// Tl holds the line at ppos(j); the result is written back to Tl at ppos(K).
-//   step A: lane t takes x[t + 32 i] (i < R), R-point DFT over i, twiddle
-//           w_N^{t k1}, and stores Y[t][k1] at Tl[k1 * 33 + t];
-//   step B: lane (k1, h) (h < P = 32 / R) takes Y[P s + h][k1] (s < R), R-point
+// Line FFT through shared memory (far fewer shuffles than warp_fft), in two
+// steps on a per-warp scratch line Tl (at least 33 R elements):
+//   step A: lane t holds x[t + 32 i] (i < R); R-point DFT over i, twiddle
+//           w_N^{t k1}, store Y[t][k1] at Tl[k1 * 33 + t];
+//   step B: lane (k1, h) (h < P = 32 / R) loads Y[P s + h][k1] (s < R), R-point
 //           DFT over s (index kappa), twiddle w_32^{h kappa}, then a P-point DFT
-//           across its P lanes (log2 P shuffle stages) giving
-//           Z_k1[kappa + R brP(h)] = X[k1 + R kappa + R^2 brP(h)].
+//           across its P lanes (log2 P shuffle stages).  Register r then holds
+//           X[K(r)], K(r) = k1 + R kappa(r) + R^2 brP(h), kappa(r) = brR(r).
 template <int R>
-__device__ __forceinline__ void line_fft_smem(float2* Tl, const float2* __restrict__ W, int lane)
+__device__ __forceinline__ void line_step_a(float2 (&v)[R], float2* Tl, const float2* __restrict__ W, int lane)
 {
     constexpr int N = 32 * R;
     constexpr int LR = ilog2(R);
-    constexpr int P = 32 / R;
-    constexpr int LP2 = ilog2(P);
-    float2 v[R];
-#pragma unroll
-    for (int i = 0; i < R; ++i) v[i] = Tl[(lane + 32 * i) + ((lane + 32 * i) >> LR)];
     reg_dif<R>(v, W, N);
     __syncwarp();
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         const int k1 = brev(r, LR);
-        const float2 y = (r == 0) ? v[r] : cmulf(v[r], W[lane * k1]);
-        Tl[k1 * 33 + lane] = y;
+        Tl[k1 * 33 + lane] = (r == 0) ? v[r] : cmulf(v[r], W[lane * k1]);
     }
     __syncwarp();
+}
+
+template <int R>
+__device__ __forceinline__ void line_step_b(float2 (&v)[R], const float2* Tl, const float2* __restrict__ W,
+                                            int lane)
+{
+    constexpr int N = 32 * R;
+    constexpr int LR = ilog2(R);
+    constexpr int P = 32 / R;
     const int k1 = lane / P, h = lane % P;
 #pragma unroll
     for (int s2 = 0; s2 < R; ++s2) v[s2] = Tl[k1 * 33 + P * s2 + h];
-    reg_dif<R>(v, W, N);  // R-point DFT over s: register r holds kappa = brR(r)
+    reg_dif<R>(v, W, N);
     if (P > 1) {
 #pragma unroll
         for (int r = 1; r < R; ++r) {
@@ -151,15 +154,15 @@ __device__ __forceinline__ void line_fft_smem(float2* Tl, const float2* __restri
             }
         }
     }
-    __syncwarp();
-    const int c = brev(h, LP2);
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-        const int kappa = brev(r, LR);
-        const int K = k1 + R * kappa + R * R * c;
-        Tl[K + (K >> LR)] = v[r];
-    }
-    __syncwarp();
+}
+
+template <int R>
+__device__ __forceinline__ int line_out_index(int lane, int r)
+{
+    constexpr int LR = ilog2(R);
+    constexpr int P = 32 / R;
+    const int k1 = lane / P, h = lane % P;
+    return k1 + R * brev(r, LR) + R * R * brev(h, ilog2(P));
 }
 
 template <int N>
@@ -232,61 +235,70 @@ __global__ void __launch_bounds__(32 * PWARPS, 3) fft_tile(const float2* __restr
     const long long N3 = (long long)N * N * N;
     const long long cbase = f * N3 + o * Oc + bb * TL * Ls;
     const long long tbase = f * N3 + o * Ot + bb * TL;
-    // Load: every thread issues all of its 16-byte loads (two complex values
-    // each) before touching shared memory, so many requests are in flight.
-    constexpr int NV = TL * N / 2 / (32 * PWARPS);  // float4 loads per thread
-    static_assert(TL * N / 2 % (32 * PWARPS) == 0, "tile must split evenly over the threads");
-    constexpr int VB = NV < 8 ? NV : 8;  // loads in flight per thread per batch
-    const float4* in4 = reinterpret_cast<const float4*>(in);
-#pragma unroll 1
-    for (int u0 = 0; u0 < NV; u0 += VB) {
-        float4 buf[VB];
-#pragma unroll
-        for (int v = 0; v < VB; ++v) {
-            const int u = u0 + v;
-            const int e2 = threadIdx.x + u * 32 * PWARPS;
-            if (C2T) {  // pair (j, j + 1) of line l
-                const int j = (e2 % (N / 2)) * 2, l = e2 / (N / 2);
-                buf[v] = __ldg(in4 + (cbase + l * Ls + j) / 2);
-            } else {    // pair (l, l + 1) of element j
-                const int l = (e2 % (TL / 2)) * 2, j = e2 / (TL / 2);
-                buf[v] = __ldg(in4 + (tbase + (long long)j * Js + l) / 2);
-            }
-        }
-#pragma unroll
-        for (int v = 0; v < VB; ++v) {
-            const int u = u0 + v;
-            const int e2 = threadIdx.x + u * 32 * PWARPS;
-            if (C2T) {
-                const int j = (e2 % (N / 2)) * 2, l = e2 / (N / 2);
-                T[l * LP + ppos<R>(j)] = make_float2(buf[v].x, buf[v].y);
-                T[l * LP + ppos<R>(j + 1)] = make_float2(buf[v].z, buf[v].w);
-            } else {
-                const int l = (e2 % (TL / 2)) * 2, j = e2 / (TL / 2);
-                T[l * LP + ppos<R>(j)] = make_float2(buf[v].x, buf[v].y);
-                T[(l + 1) * LP + ppos<R>(j)] = make_float2(buf[v].z, buf[v].w);
-            }
-        }
-    }
-    __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    
-    for (int line = warp; line < TL; line += PWARPS) line_fft_smem<R>(T + line * LP, Ws, lane);
-    __syncthreads();
-    {
+    constexpr int NV = TL * N / 2 / (32 * PWARPS);  // float4 accesses per thread on the transposed side
+    static_assert(TL * N / 2 % (32 * PWARPS) == 0, "tile must split evenly over the threads");
+    if (C2T) {
+        // contiguous input: each warp loads its lines straight into registers
+        __syncthreads();  // twiddles staged
+        for (int line = warp; line < TL; line += PWARPS) {
+            float2* Tl = T + line * LP;
+            const float2* src = in + cbase + line * Ls;
+            float2 v[R];
+#pragma unroll
+            for (int i = 0; i < R; ++i) v[i] = __ldg(src + lane + 32 * i);
+            line_step_a<R>(v, Tl, Ws, lane);
+            line_step_b<R>(v, Tl, Ws, lane);
+            __syncwarp();
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const int K = line_out_index<R>(lane, r);
+                Tl[ppos<R>(K)] = v[r];
+            }
+        }
+        __syncthreads();
+        // transposed output: pairs (l, l + 1) of element j as 16-byte stores
         float4* out4 = reinterpret_cast<float4*>(out);
 #pragma unroll 4
         for (int u = 0; u < NV; ++u) {
             const int e2 = threadIdx.x + u * 32 * PWARPS;
-            if (C2T) {  // transposed side: pair (l, l + 1) of element j
+            const int l = (e2 % (TL / 2)) * 2, j = e2 / (TL / 2);
+            const float2 a = T[l * LP + ppos<R>(j)], b = T[(l + 1) * LP + ppos<R>(j)];
+            out4[(tbase + (long long)j * Js + l) / 2] = make_float4(a.x, a.y, b.x, b.y);
+        }
+    } else {
+        // transposed input staged through shared memory (16-byte loads, all issued first)
+        constexpr int VB = NV < 8 ? NV : 8;
+        const float4* in4 = reinterpret_cast<const float4*>(in);
+#pragma unroll 1
+        for (int u0 = 0; u0 < NV; u0 += VB) {
+            float4 buf[VB];
+#pragma unroll
+            for (int q = 0; q < VB; ++q) {
+                const int e2 = threadIdx.x + (u0 + q) * 32 * PWARPS;
                 const int l = (e2 % (TL / 2)) * 2, j = e2 / (TL / 2);
-                const float2 a = T[l * LP + ppos<R>(j)], b = T[(l + 1) * LP + ppos<R>(j)];
-                out4[(tbase + (long long)j * Js + l) / 2] = make_float4(a.x, a.y, b.x, b.y);
-            } else {    // contiguous side: pair (j, j + 1) of line l
-                const int j = (e2 % (N / 2)) * 2, l = e2 / (N / 2);
-                const float2 a = T[l * LP + ppos<R>(j)], b = T[l * LP + ppos<R>(j + 1)];
-                out4[(cbase + l * Ls + j) / 2] = make_float4(a.x, a.y, b.x, b.y);
+                buf[q] = __ldg(in4 + (tbase + (long long)j * Js + l) / 2);
             }
+#pragma unroll
+            for (int q = 0; q < VB; ++q) {
+                const int e2 = threadIdx.x + (u0 + q) * 32 * PWARPS;
+                const int l = (e2 % (TL / 2)) * 2, j = e2 / (TL / 2);
+                T[l * LP + ppos<R>(j)] = make_float2(buf[q].x, buf[q].y);
+                T[(l + 1) * LP + ppos<R>(j)] = make_float2(buf[q].z, buf[q].w);
+            }
+        }
+        __syncthreads();
+        // contiguous output straight from registers: runs of R consecutive outputs per lane group
+        for (int line = warp; line < TL; line += PWARPS) {
+            float2* Tl = T + line * LP;
+            float2 v[R];
+#pragma unroll
+            for (int i = 0; i < R; ++i) v[i] = Tl[ppos<R>(lane + 32 * i)];
+            line_step_a<R>(v, Tl, Ws, lane);
+            line_step_b<R>(v, Tl, Ws, lane);
+            float2* dst = out + cbase + line * Ls;
+#pragma unroll
+            for (int r = 0; r < R; ++r) dst[line_out_index<R>(lane, r)] = v[r];
         }
     }
 }
