@@ -145,22 +145,44 @@ __global__ void zero_nyquist_so3_kernel(C* __restrict__ H, int N, long long nsli
         slice[(long long)(r - N) * N + B] = z;
 }
 
-// matrix2rsph T(l; a, c) (fdcl_FFTSO3.cpp:1107-1139), row a, column c.
-__device__ __forceinline__ double2 tmat(int a, int c)
+// matrix2rsph T(l; a, c) (fdcl_FFTSO3.cpp:1107-1139), row a, column c, in the
+// arithmetic type A (double for the FP64 path, float for the tensor-core path).
+template <typename A> struct c2t { A x, y; };
+
+// 1/sqrt(2): the FP64 path forms it as the reference does, 1./sqrt(2.).
+template <typename A> __device__ __forceinline__ A inv_sqrt2();
+template <> __device__ __forceinline__ double inv_sqrt2<double>() { return 1. / sqrt(2.); }
+template <> __device__ __forceinline__ float inv_sqrt2<float>() { return 0.70710678118654752440f; }
+
+template <typename A>
+__device__ __forceinline__ c2t<A> tmat_t(int a, int c)
 {
-    const double s = 1. / sqrt(2.);
+    const A s = inv_sqrt2<A>();
     if (a < 0) {
-        if (c == a) return make_double2(0., s);
-        if (c == -a) return make_double2(0., -s * ((a & 1) ? -1. : 1.));
+        if (c == a) return {(A)0, s};
+        if (c == -a) return {(A)0, -s * ((a & 1) ? (A)-1 : (A)1)};
     } else if (a == 0) {
-        if (c == 0) return make_double2(1., 0.);
+        if (c == 0) return {(A)1, (A)0};
     } else {
-        if (c == -a) return make_double2(s, 0.);
-        if (c == a) return make_double2(((a & 1) ? -1. : 1.) * s, 0.);
+        if (c == -a) return {s, (A)0};
+        if (c == a) return {((a & 1) ? (A)-1 : (A)1) * s, (A)0};
     }
-    return make_double2(0., 0.);
+    return {(A)0, (A)0};
 }
 
+template <typename A>
+__device__ __forceinline__ c2t<A> cmul_t(c2t<A> a, c2t<A> b)
+{
+    return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+template <typename A>
+__device__ __forceinline__ c2t<A> conj_t(c2t<A> a) { return {a.x, -a.y}; }
+
+__device__ __forceinline__ double2 tmat(int a, int c)
+{
+    c2t<double> t = tmat_t<double>(a, c);
+    return make_double2(t.x, t.y);
+}
 __device__ __forceinline__ double2 cmul2(double2 a, double2 b)
 {
     return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
@@ -169,7 +191,7 @@ __device__ __forceinline__ double2 conj2(double2 a) { return make_double2(a.x, -
 
 // F_r = Re(T F_c T^H) per l (fdcl_FFTSO3.cpp:1169-1181): the real-basis
 // coefficients of a real function from its complex coefficients.
-template <typename CIN, typename ROUT>
+template <typename CIN, typename ROUT, typename A>
 __global__ void so3_c2r_kernel(const CIN* __restrict__ Fc, ROUT* __restrict__ Fr, int L, long long cstride)
 {
     const int l = blockIdx.x, b = blockIdx.y;
@@ -180,12 +202,12 @@ __global__ void so3_c2r_kernel(const CIN* __restrict__ Fc, ROUT* __restrict__ Fr
         int m = i % W - l, n = i / W - l;
         int am[2] = {-m, m}, bn[2] = {-n, n};
         int na = (m == 0) ? 1 : 2, nb = (n == 0) ? 1 : 2;
-        double acc = 0.;
+        A acc = 0;
         for (int ia = 0; ia < na; ++ia)
             for (int ib = 0; ib < nb; ++ib) {
-                double2 t1 = tmat(m, am[ia]), t2 = conj2(tmat(n, bn[ib]));
+                c2t<A> t1 = tmat_t<A>(m, am[ia]), t2 = conj_t(tmat_t<A>(n, bn[ib]));
                 CIN v = fc[so3_idx(l, am[ia], bn[ib])];
-                double2 c = cmul2(cmul2(t1, make_double2((double)v.x, (double)v.y)), t2);
+                c2t<A> c = cmul_t(cmul_t(t1, c2t<A>{(A)v.x, (A)v.y}), t2);
                 acc += c.x;
             }
         fr[so3_idx(l, m, n)] = (ROUT)acc;
@@ -194,7 +216,7 @@ __global__ void so3_c2r_kernel(const CIN* __restrict__ Fc, ROUT* __restrict__ Fr
 
 // F_c = T^H F_r T per l: the complex coefficients whose synthesis equals the
 // real-basis synthesis sum (2l+1) F_r U (U = Re(conj(T) D T^T), fdcl_FFTSO3.cpp:1010-1022).
-template <typename RIN, typename COUT>
+template <typename RIN, typename COUT, typename A>
 __global__ void so3_r2c_kernel(const RIN* __restrict__ Fr, COUT* __restrict__ Fc, int L, long long cstride)
 {
     const int l = blockIdx.x, b = blockIdx.y;
@@ -205,12 +227,11 @@ __global__ void so3_r2c_kernel(const RIN* __restrict__ Fr, COUT* __restrict__ Fc
         int m = i % W - l, n = i / W - l;
         int am[2] = {m, -m}, bn[2] = {n, -n};
         int na = (m == 0) ? 1 : 2, nb = (n == 0) ? 1 : 2;
-        double2 acc = make_double2(0., 0.);
+        c2t<A> acc = {(A)0, (A)0};
         for (int ia = 0; ia < na; ++ia)
             for (int ib = 0; ib < nb; ++ib) {
-                double2 t1 = conj2(tmat(am[ia], m)), t2 = tmat(bn[ib], n);
-                double v = (double)fr[so3_idx(l, am[ia], bn[ib])];
-                double2 c = cmul2(t1, t2);
+                c2t<A> c = cmul_t(conj_t(tmat_t<A>(am[ia], m)), tmat_t<A>(bn[ib], n));
+                A v = (A)fr[so3_idx(l, am[ia], bn[ib])];
                 acc.x += c.x * v;
                 acc.y += c.y * v;
             }
@@ -425,9 +446,9 @@ cudaError_t launch_so3_c2r(const void* Fc, void* Fr, bool fp64, int L, int batch
     dim3 grid(L + 1, batch);
     long long cs = so3_off(L + 1);
     if (fp64)
-        so3_c2r_kernel<double2, double><<<grid, 256, 0, st>>>((const double2*)Fc, (double*)Fr, L, cs);
+        so3_c2r_kernel<double2, double, double><<<grid, 256, 0, st>>>((const double2*)Fc, (double*)Fr, L, cs);
     else
-        so3_c2r_kernel<float2, float><<<grid, 256, 0, st>>>((const float2*)Fc, (float*)Fr, L, cs);
+        so3_c2r_kernel<float2, float, float><<<grid, 256, 0, st>>>((const float2*)Fc, (float*)Fr, L, cs);
     return cudaGetLastError();
 }
 
@@ -436,9 +457,9 @@ cudaError_t launch_so3_r2c(const void* Fr, void* Fc, bool fp64, int L, int batch
     dim3 grid(L + 1, batch);
     long long cs = so3_off(L + 1);
     if (fp64)
-        so3_r2c_kernel<double, double2><<<grid, 256, 0, st>>>((const double*)Fr, (double2*)Fc, L, cs);
+        so3_r2c_kernel<double, double2, double><<<grid, 256, 0, st>>>((const double*)Fr, (double2*)Fc, L, cs);
     else
-        so3_r2c_kernel<float, float2><<<grid, 256, 0, st>>>((const float*)Fr, (float2*)Fc, L, cs);
+        so3_r2c_kernel<float, float2, float><<<grid, 256, 0, st>>>((const float*)Fr, (float2*)Fc, L, cs);
     return cudaGetLastError();
 }
 

@@ -666,6 +666,13 @@ __global__ void resid_kernel(const float2* __restrict__ f, float2* __restrict__ 
     r[i] = make_float2(a.x - b.x, a.y - b.y);
 }
 
+__global__ void resid_real_kernel(const float* __restrict__ f, float* __restrict__ r, long long n)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    r[i] = f[i] - r[i];
+}
+
 __global__ void add_kernel(float2* __restrict__ F, const float2* __restrict__ d, long long n)
 {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -683,6 +690,7 @@ using namespace tc;
 struct TCState {
     int L = 0, B = 0, N = 0, Kp = 0, batch = 0, ntiles = 0, ngroups = 0;
     bool refine = false;
+    bool real = false;            // real grids (FFTSO3_SO3_REAL): real samples in, real part out
     FFTFactors fac;
     const double* d_tw = nullptr;
     float* d_wf = nullptr;
@@ -692,6 +700,7 @@ struct TCState {
     float2* d_pencil = nullptr;   // pencils [fn][p][q][k]
     float2* d_resid = nullptr;    // refinement: residual grid
     float2* d_coef2 = nullptr;    // refinement: correction coefficients
+    float2* d_fc = nullptr;       // real kinds: complex coefficients [fn][C]
     long long* d_grow0 = nullptr;
     long long* d_goff2 = nullptr;  // group-major coefficient offsets
     float2* d_fg = nullptr;        // group-major coefficients [fn][C]
@@ -756,7 +765,7 @@ void tc_destroy(TCState* s)
     if (!s) return;
     for (int p = 0; p < 3; ++p)
         if (s->d_tab[p]) cudaFree(s->d_tab[p]);
-    void* ptrs[] = {s->d_wf, s->d_work, s->d_pencil, s->d_resid, s->d_coef2, s->d_grow0, s->d_goff2, s->d_fg,
+    void* ptrs[] = {s->d_wf, s->d_work, s->d_pencil, s->d_resid, s->d_coef2, s->d_fc, s->d_grow0, s->d_goff2, s->d_fg,
                     s->d_items_fwd, s->d_items_inv, s->d_err};
     for (void* q : ptrs)
         if (q) cudaFree(q);
@@ -767,7 +776,7 @@ long long tc_device_bytes(const TCState* s) { return s ? s->bytes : 0; }
 
 int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64, const std::vector<long long>& goff,
               long long table_elems, const double* d_tw, const double* d_w, const FFTFactors& fac, bool refine,
-              std::string& err)
+              bool real, std::string& err)
 {
     *out = nullptr;
     if (N > MAXN) {
@@ -783,6 +792,7 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
     s->ntiles = (batch + FPT - 1) / FPT;
     s->ngroups = s->B * s->B;
     s->refine = refine;
+    s->real = real;
     s->fac = fac;
     s->d_tw = d_tw;
     s->total_rows = table_elems / N;
@@ -820,6 +830,9 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
     const size_t gridel = (size_t)batch * N * N * N;
     if ((rc = tc_alloc(s, (void**)&s->d_work, sizeof(float2) * gridel, err))) return bail(rc);
     if ((rc = tc_alloc(s, (void**)&s->d_pencil, sizeof(float2) * gridel, err))) return bail(rc);
+    if (real)
+        if ((rc = tc_alloc(s, (void**)&s->d_fc, sizeof(float2) * (size_t)batch * so3_off(s->B), err)))
+            return bail(rc);
     if (refine) {
         if ((rc = tc_alloc(s, (void**)&s->d_resid, sizeof(float2) * gridel, err))) return bail(rc);
         if ((rc = tc_alloc(s, (void**)&s->d_coef2, sizeof(float2) * (size_t)batch * so3_off(s->B), err)))
@@ -885,7 +898,8 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
     return FFTSO3_SUCCESS;
 }
 
-static FFTLaunch fft_launch(const TCState* s, const void* in, void* out, bool cols)
+static FFTLaunch fft_launch(const TCState* s, const void* in, void* out, bool cols, bool real_in = false,
+                            bool real_out = false)
 {
     FFTLaunch L;
     const int N = s->N;
@@ -894,8 +908,8 @@ static FFTLaunch fft_launch(const TCState* s, const void* in, void* out, bool co
     L.fac = s->fac;
     L.tw = s->d_tw;
     L.fp64 = false;
-    L.real_in = false;
-    L.real_out = false;
+    L.real_in = real_in;
+    L.real_out = real_out;
     L.nlines = (long long)s->batch * N * N;
     if (!cols) {
         L.lpb = 4;
@@ -947,21 +961,22 @@ static GemmArgs gemm_args(const TCState* s)
     return a;
 }
 
-static int tc_forward_once(TCState* s, const float2* grid, float2* F, cudaStream_t st, StageTimer* T,
+// grid: float2 samples, or float samples when s->real.
+static int tc_forward_once(TCState* s, const void* grid, float2* F, cudaStream_t st, StageTimer* T,
                            std::string& err)
 {
     const long long N = s->N;
     if (fft_fast_supported(s->N)) {
         // register-resident FFTs; the alpha pass writes the k-contiguous pencils directly
         T->begin(ST_FFT_ROWS, st);
-        TCK(launch_fft_grid_pass(grid, s->d_work, s->batch, s->N, 1, s->d_tw, st));
+        TCK(launch_fft_grid_pass(grid, s->d_work, s->batch, s->N, 1, s->d_tw, st, s->real));
         T->end(st);
         T->begin(ST_FFT_COLS, st);
         TCK(launch_fft_grid_pass(s->d_work, s->d_pencil, s->batch, s->N, 2, s->d_tw, st));
         T->end(st);
     } else {
         T->begin(ST_FFT_ROWS, st);
-        TCK(launch_fft_lines(fft_launch(s, grid, s->d_work, false), st));
+        TCK(launch_fft_lines(fft_launch(s, grid, s->d_work, false, s->real, false), st));
         T->end(st);
         T->begin(ST_FFT_COLS, st);
         TCK(launch_fft_lines(fft_launch(s, s->d_work, s->d_work, true), st));
@@ -989,7 +1004,8 @@ static int tc_forward_once(TCState* s, const float2* grid, float2* F, cudaStream
     return FFTSO3_SUCCESS;
 }
 
-static int tc_inverse_once(TCState* s, const float2* F, float2* grid, cudaStream_t st, StageTimer* T,
+// grid: float2 samples, or the real parts (float) when s->real.
+static int tc_inverse_once(TCState* s, const float2* F, void* grid, cudaStream_t st, StageTimer* T,
                            std::string& err)
 {
     const long long N = s->N;
@@ -1020,7 +1036,7 @@ static int tc_inverse_once(TCState* s, const float2* F, float2* grid, cudaStream
         TCK(launch_fft_grid_pass(s->d_pencil, s->d_work, s->batch, s->N, -2, s->d_tw, st));
         T->end(st);
         T->begin(ST_FFT_ROWS, st);
-        TCK(launch_fft_grid_pass(s->d_work, grid, s->batch, s->N, -1, s->d_tw, st));
+        TCK(launch_fft_grid_pass(s->d_work, grid, s->batch, s->N, -1, s->d_tw, st, s->real));
         T->end(st);
         return FFTSO3_SUCCESS;
     }
@@ -1035,34 +1051,54 @@ static int tc_inverse_once(TCState* s, const float2* F, float2* grid, cudaStream
     TCK(launch_fft_lines(fft_launch(s, s->d_work, s->d_work, false), st));
     T->end(st);
     T->begin(ST_FFT_COLS, st);
-    TCK(launch_fft_lines(fft_launch(s, s->d_work, grid, true), st));
+    TCK(launch_fft_lines(fft_launch(s, s->d_work, grid, true, false, s->real), st));
     T->end(st);
     return FFTSO3_SUCCESS;
 }
 
 int tc_forward(TCState* s, const void* grid, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err)
 {
-    int rc = tc_forward_once(s, (const float2*)grid, (float2*)coeffs, st, T, err);
-    if (rc || !s->refine) return rc;
-    // one residual step: F += forward(f - inverse(F))
-    const long long ng = (long long)s->batch * s->N * s->N * s->N;
-    const long long nc = (long long)s->batch * so3_off(s->B);
-    if ((rc = tc_inverse_once(s, (const float2*)coeffs, s->d_resid, st, T, err))) return rc;
-    T->begin(ST_REFINE, st);
-    resid_kernel<<<(unsigned)((ng + 255) / 256), 256, 0, st>>>((const float2*)grid, s->d_resid, ng);
-    TCK(cudaGetLastError());
-    T->end(st);
-    if ((rc = tc_forward_once(s, s->d_resid, s->d_coef2, st, T, err))) return rc;
-    T->begin(ST_REFINE, st);
-    add_kernel<<<(unsigned)((nc + 255) / 256), 256, 0, st>>>((float2*)coeffs, s->d_coef2, nc);
-    TCK(cudaGetLastError());
-    T->end(st);
+    // real kinds: complex coefficients in d_fc, then the real basis (fdcl_FFTSO3.cpp:1169-1181)
+    float2* Fc = s->real ? s->d_fc : (float2*)coeffs;
+    int rc = tc_forward_once(s, grid, Fc, st, T, err);
+    if (rc) return rc;
+    if (s->refine) {
+        // one residual step: F += forward(f - inverse(F))
+        const long long ng = (long long)s->batch * s->N * s->N * s->N;
+        const long long nc = (long long)s->batch * so3_off(s->B);
+        if ((rc = tc_inverse_once(s, Fc, s->d_resid, st, T, err))) return rc;
+        T->begin(ST_REFINE, st);
+        if (s->real)
+            resid_real_kernel<<<(unsigned)((ng + 255) / 256), 256, 0, st>>>((const float*)grid, (float*)s->d_resid,
+                                                                            ng);
+        else
+            resid_kernel<<<(unsigned)((ng + 255) / 256), 256, 0, st>>>((const float2*)grid, s->d_resid, ng);
+        TCK(cudaGetLastError());
+        T->end(st);
+        if ((rc = tc_forward_once(s, s->d_resid, s->d_coef2, st, T, err))) return rc;
+        T->begin(ST_REFINE, st);
+        add_kernel<<<(unsigned)((nc + 255) / 256), 256, 0, st>>>(Fc, s->d_coef2, nc);
+        TCK(cudaGetLastError());
+        T->end(st);
+    }
+    if (s->real) {
+        T->begin(ST_BASIS, st);
+        TCK(launch_so3_c2r(Fc, coeffs, false, s->L, s->batch, st));
+        T->end(st);
+    }
     return FFTSO3_SUCCESS;
 }
 
 int tc_inverse(TCState* s, const void* coeffs, void* grid, cudaStream_t st, StageTimer* T, std::string& err)
 {
-    return tc_inverse_once(s, (const float2*)coeffs, (float2*)grid, st, T, err);
+    const float2* Fc = (const float2*)coeffs;
+    if (s->real) {
+        T->begin(ST_BASIS, st);
+        TCK(launch_so3_r2c(coeffs, s->d_fc, false, s->L, s->batch, st));
+        T->end(st);
+        Fc = s->d_fc;
+    }
+    return tc_inverse_once(s, Fc, grid, st, T, err);
 }
 
 int tc_status(TCState* s)

@@ -37,7 +37,8 @@ cudaError_t launch_fft_rows_fast(const void* in, void* out, long long nlines, in
 //   pass  2: T1 [nf][k][q][j1]    -> FFT over j1 -> pencils [nf][p][q][k]
 //   pass -2: pencils [nf][p][q][k] -> FFT over p -> T1 [nf][k][q][j1]
 //   pass -1: T1 [nf][k][q][j1]     -> FFT over q -> grid [nf][k][j1][j2]
+// real_io: pass 1 reads real samples (float), pass -1 writes the real part only.
 cudaError_t launch_fft_grid_pass(const void* in, void* out, long long nf, int N, int pass, const void* tw,
-                                 cudaStream_t st);
+                                 cudaStream_t st, bool real_io = false);
 
 }  // namespace fftso3

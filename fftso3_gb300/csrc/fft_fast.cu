@@ -214,7 +214,9 @@ __device__ __forceinline__ int ppos(int j) { return j + (j >> ilog2(R)); }
 // index split into (f, o < N, bb < N / TL).  C2T = true reads the contiguous
 // side and writes the transposed one; C2T = false the reverse.  Both sides
 // move TL * 8 = 128-byte runs.
-template <int R, bool C2T>
+// REAL_IO: the contiguous side holds real values (pass 1 reads real samples,
+// pass -1 writes the real part only).
+template <int R, bool C2T, bool REAL_IO>
 __global__ void __launch_bounds__(32 * PWARPS, 3) fft_tile(const float2* __restrict__ in, float2* __restrict__ out,
                                                         long long Oc, long long Ls, long long Ot, long long Js,
                                                         const double2* __restrict__ tw)
@@ -243,10 +245,16 @@ __global__ void __launch_bounds__(32 * PWARPS, 3) fft_tile(const float2* __restr
         __syncthreads();  // twiddles staged
         for (int line = warp; line < TL; line += PWARPS) {
             float2* Tl = T + line * LP;
-            const float2* src = in + cbase + line * Ls;
             float2 v[R];
+            if (REAL_IO) {
+                const float* src = reinterpret_cast<const float*>(in) + cbase + line * Ls;
 #pragma unroll
-            for (int i = 0; i < R; ++i) v[i] = __ldg(src + lane + 32 * i);
+                for (int i = 0; i < R; ++i) v[i] = make_float2(__ldg(src + lane + 32 * i), 0.f);
+            } else {
+                const float2* src = in + cbase + line * Ls;
+#pragma unroll
+                for (int i = 0; i < R; ++i) v[i] = __ldg(src + lane + 32 * i);
+            }
             line_step_a<R>(v, Tl, Ws, lane);
             line_step_b<R>(v, Tl, Ws, lane);
             __syncwarp();
@@ -296,21 +304,27 @@ __global__ void __launch_bounds__(32 * PWARPS, 3) fft_tile(const float2* __restr
             for (int i = 0; i < R; ++i) v[i] = Tl[ppos<R>(lane + 32 * i)];
             line_step_a<R>(v, Tl, Ws, lane);
             line_step_b<R>(v, Tl, Ws, lane);
-            float2* dst = out + cbase + line * Ls;
+            if (REAL_IO) {
+                float* dst = reinterpret_cast<float*>(out) + cbase + line * Ls;
 #pragma unroll
-            for (int r = 0; r < R; ++r) dst[line_out_index<R>(lane, r)] = v[r];
+                for (int r = 0; r < R; ++r) dst[line_out_index<R>(lane, r)] = v[r].x;
+            } else {
+                float2* dst = out + cbase + line * Ls;
+#pragma unroll
+                for (int r = 0; r < R; ++r) dst[line_out_index<R>(lane, r)] = v[r];
+            }
         }
     }
 }
 
-template <int R, bool C2T>
+template <int R, bool C2T, bool REAL_IO>
 static cudaError_t tile_r(const void* in, void* out, long long nf, long long Oc, long long Ls, long long Ot,
                           long long Js, const void* tw, cudaStream_t st)
 {
     constexpr int N = 32 * R;
     constexpr int LP = N + N / R + 1;
     const size_t smem = sizeof(float2) * ((size_t)N + (size_t)TL * LP);
-    auto k = fft_tile<R, C2T>;
+    auto k = fft_tile<R, C2T, REAL_IO>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const long long nblk = nf * (long long)N * (N / TL);
@@ -319,16 +333,16 @@ static cudaError_t tile_r(const void* in, void* out, long long nf, long long Oc,
     return cudaGetLastError();
 }
 
-template <bool C2T>
+template <bool C2T, bool REAL_IO>
 static cudaError_t tile_dispatch(const void* in, void* out, long long nf, int N, long long Oc, long long Ls,
                                  long long Ot, long long Js, const void* tw, cudaStream_t st)
 {
     switch (N) {
-        case 64: return tile_r<2, C2T>(in, out, nf, Oc, Ls, Ot, Js, tw, st);
-        case 128: return tile_r<4, C2T>(in, out, nf, Oc, Ls, Ot, Js, tw, st);
-        case 256: return tile_r<8, C2T>(in, out, nf, Oc, Ls, Ot, Js, tw, st);
-        case 512: return tile_r<16, C2T>(in, out, nf, Oc, Ls, Ot, Js, tw, st);
-        case 1024: return tile_r<32, C2T>(in, out, nf, Oc, Ls, Ot, Js, tw, st);
+        case 64: return tile_r<2, C2T, REAL_IO>(in, out, nf, Oc, Ls, Ot, Js, tw, st);
+        case 128: return tile_r<4, C2T, REAL_IO>(in, out, nf, Oc, Ls, Ot, Js, tw, st);
+        case 256: return tile_r<8, C2T, REAL_IO>(in, out, nf, Oc, Ls, Ot, Js, tw, st);
+        case 512: return tile_r<16, C2T, REAL_IO>(in, out, nf, Oc, Ls, Ot, Js, tw, st);
+        case 1024: return tile_r<32, C2T, REAL_IO>(in, out, nf, Oc, Ls, Ot, Js, tw, st);
         default: return cudaErrorNotSupported;
     }
 }
@@ -366,14 +380,19 @@ cudaError_t launch_fft_rows_fast(const void* in, void* out, long long nlines, in
 //   pass 2': pencils [f][p][q][k] -> FFT over p  -> T1 [f][k][q][j1]
 //   pass 1': T1 [f][k][q][j1]     -> FFT over q  -> grid [f][k][j1][j2]
 cudaError_t launch_fft_grid_pass(const void* in, void* out, long long nf, int N, int pass, const void* tw,
-                                 cudaStream_t st)
+                                 cudaStream_t st, bool real_io)
 {
     const long long N1 = N, N2 = (long long)N * N;
+    if (real_io && pass != 1 && pass != -1) return cudaErrorInvalidValue;
     switch (pass) {
-        case 1: return ffast::tile_dispatch<true>(in, out, nf, N, N2, N1, N2, N1, tw, st);
-        case 2: return ffast::tile_dispatch<true>(in, out, nf, N, N1, N2, N1, N2, tw, st);
-        case -2: return ffast::tile_dispatch<false>(in, out, nf, N, N1, N2, N1, N2, tw, st);
-        case -1: return ffast::tile_dispatch<false>(in, out, nf, N, N2, N1, N2, N1, tw, st);
+        case 1:
+            return real_io ? ffast::tile_dispatch<true, true>(in, out, nf, N, N2, N1, N2, N1, tw, st)
+                           : ffast::tile_dispatch<true, false>(in, out, nf, N, N2, N1, N2, N1, tw, st);
+        case 2: return ffast::tile_dispatch<true, false>(in, out, nf, N, N1, N2, N1, N2, tw, st);
+        case -2: return ffast::tile_dispatch<false, false>(in, out, nf, N, N1, N2, N1, N2, tw, st);
+        case -1:
+            return real_io ? ffast::tile_dispatch<false, true>(in, out, nf, N, N2, N1, N2, N1, tw, st)
+                           : ffast::tile_dispatch<false, false>(in, out, nf, N, N2, N1, N2, N1, tw, st);
         default: return cudaErrorInvalidValue;
     }
 }

@@ -55,3 +55,74 @@ def test_tc_batch_and_columns(gblib, oracle, torch_cuda):
     for i in range(b):
         assert rel_err(g[i], gs[i]) < TOL
         assert rel_err(G[i], Fs[i]) < TOL
+
+
+def _plan_pair(gblib, torch, kind, L, batch, recursion, flags=0):
+    return (gblib.Plan(kind, L, batch, "tc_bf16x3", recursion, flags),
+            gblib.Plan(kind, L, batch, "fp64", recursion, 0))
+
+
+@pytest.mark.parametrize("L", [15, 31, 47])
+def test_tc_real_matches_oracle(gblib, oracle, torch_cuda, L):
+    """FFTSO3_real on the tensor cores: real grids (float32), real-basis coefficients.
+
+    l_max 15 and 47 (N = 32, 96) take the generic FFT, l_max 31 (N = 64) the
+    tile FFT with real samples in and the real part out.
+    """
+    torch = torch_cuda
+    N = 2 * (L + 1)
+    Fr = so3_coeffs(L, seed=100 + L, complex_=False, decay="pow")
+    g_ref = oracle.so3_inverse_real_grid(L, Fr)
+    G_ref = oracle.so3_forward_real(L, g_ref)
+    p = gblib.Plan(gblib.SO3_REAL, L, 1, "tc_bf16x3", "reference", 0)
+    s = torch.cuda.current_stream().cuda_stream
+    c = torch.from_numpy(Fr.astype(np.float32)).cuda()
+    g = torch.from_numpy(np.ascontiguousarray(g_ref.astype(np.float32))).cuda()
+    gout = torch.empty_like(g)
+    cout = torch.empty_like(c)
+    p.inverse(c.data_ptr(), gout.data_ptr(), s)
+    p.forward(g.data_ptr(), cout.data_ptr(), s)
+    p.check()
+    assert rel_err(gout.cpu().numpy().astype(np.float64).reshape(N, N, N), g_ref) < TOL
+    assert rel_err(cout.cpu().numpy().astype(np.float64), G_ref) < TOL
+    assert rel_err(cout.cpu().numpy().astype(np.float64), Fr) < TOL
+
+
+def test_tc_real_refined_batch(gblib, oracle, torch_cuda):
+    """Real kind, batch 3, with the residual refinement step on."""
+    torch = torch_cuda
+    L, b = 31, 3
+    Frs = np.stack([so3_coeffs(L, seed=200 + i, complex_=False, decay="pow") for i in range(b)])
+    gs = np.stack([oracle.so3_inverse_real_grid(L, Frs[i]) for i in range(b)])
+    p = gblib.Plan(gblib.SO3_REAL, L, b, "tc_bf16x3", "reference", gblib.FLAG_REFINE)
+    s = torch.cuda.current_stream().cuda_stream
+    g = torch.from_numpy(np.ascontiguousarray(gs.astype(np.float32))).cuda()
+    cout = torch.empty(Frs.shape, dtype=torch.float32, device="cuda")
+    p.forward(g.data_ptr(), cout.data_ptr(), s)
+    p.check()
+    G = cout.cpu().numpy().astype(np.float64)
+    for i in range(b):
+        assert rel_err(G[i], Frs[i]) < TOL
+
+
+def test_tc_generic_fft_lmax96(gblib, torch_cuda):
+    """l_max = 96 (N = 194, not a power of two: mixed-radix FFT + transposes)
+    against the FP64 plan, stable recursion, batch 2."""
+    torch = torch_cuda
+    L, b = 96, 2
+    C = (L + 1) * (4 * (L + 1) ** 2 - 1) // 3
+    F = np.concatenate([so3_coeffs(L, seed=300 + i, decay="pow") for i in range(b)])
+    ptc, p64 = _plan_pair(gblib, torch, gblib.SO3_COMPLEX, L, b, "stable")
+    s = torch.cuda.current_stream().cuda_stream
+    c64 = torch.from_numpy(F).cuda()
+    g64 = torch.empty(b * (2 * L + 2) ** 3, dtype=torch.complex128, device="cuda")
+    p64.inverse(c64.data_ptr(), g64.data_ptr(), s)
+    c32 = c64.to(torch.complex64)
+    g32 = torch.empty(g64.shape, dtype=torch.complex64, device="cuda")
+    ptc.inverse(c32.data_ptr(), g32.data_ptr(), s)
+    ptc.check()
+    assert rel_err(g32.cpu().numpy().astype(np.complex128), g64.cpu().numpy()) < TOL
+    F32 = torch.empty(b * C, dtype=torch.complex64, device="cuda")
+    ptc.forward(g64.to(torch.complex64).data_ptr(), F32.data_ptr(), s)
+    ptc.check()
+    assert rel_err(F32.cpu().numpy().astype(np.complex128), F) < TOL
