@@ -191,6 +191,163 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+# --------------------------------------------------------------- uneven batch
+
+UNEVEN_METRIC = "SO(3) real fwd+inv transforms/s, 4096 functions, l_max~U{8..64}: TC batch vs FP64 per-function loop"
+
+
+def uneven_lmax(n: int, seed: int = 3) -> np.ndarray:
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return rng.integers(8, 65, size=n)
+
+
+def main_uneven(args) -> None:
+    """The batching workload: n real SO(3) functions with l_max drawn uniformly
+    from {8..64}, FP32 samples, coefficients N(0,1)/(2l+1); one fftso3_batch
+    (tensor-core buckets, CUDA graph).  Compared with a per-function launch loop
+    of the plain FP64 path (one batch-1 FFTSO3_REAL FP64 plan per l_max)."""
+    import torch
+
+    from fftso3_gb300 import _lib
+    from fftso3_gb300 import build as fbuild
+
+    fbuild.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    n = args.functions
+    lmax = uneven_lmax(n)
+    t_create = time.perf_counter()
+    bt = _lib.Batch(_lib.SO3_REAL, lmax, "tc_bf16x3", "reference", _lib.FLAG_GRAPH)
+    t_create = time.perf_counter() - t_create
+    G, Ctot = bt.grid_elems, bt.coeff_elems
+    # seeded coefficients N(0,1)/(2l+1), generated on the device per function
+    Lm = int(lmax.max())
+    deg = torch.from_numpy(np.concatenate([np.full((2 * l + 1) ** 2, l) for l in range(Lm + 1)])).to(dev)
+    scale = 1.0 / (2.0 * deg.double() + 1.0)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(11)
+    coef = torch.empty(Ctot, dtype=torch.float32, device=dev)
+    for i in range(n):
+        o0 = bt.coeff_offset(i)
+        c = _lib.lib().fftso3_coeff_elems(_lib.SO3_REAL, int(lmax[i]))
+        coef[o0:o0 + c] = (torch.randn(c, generator=gen, device=dev, dtype=torch.float64) * scale[:c]).float()
+    grid = torch.empty(G, dtype=torch.float32, device=dev)
+    bt.inverse(coef.data_ptr(), grid.data_ptr(), sp)      # band-limited FP32 samples
+    grid_out = torch.empty_like(grid)
+    coef_out = torch.empty_like(coef)
+    torch.cuda.synchronize()
+    bt.check()
+
+    # accuracy on a sample of functions against the FP64 plain path on the same FP32 samples
+    acc_rms, acc_idx = [], []
+    plans64 = {}
+    bt.forward(grid.data_ptr(), coef_out.data_ptr(), sp)
+    for i in np.linspace(0, n - 1, 8).astype(int):
+        L = int(lmax[i])
+        p = plans64.setdefault(L, _lib.Plan(_lib.SO3_REAL, L, 1, "fp64", "reference"))
+        g0, c0 = bt.grid_offset(i), bt.coeff_offset(i)
+        gi = grid[g0:g0 + p.grid_elems].double()
+        ci = torch.empty(p.coeff_elems, dtype=torch.float64, device=dev)
+        p.forward(gi.data_ptr(), ci.data_ptr(), sp)
+        torch.cuda.synchronize()
+        a = coef_out[c0:c0 + p.coeff_elems].double()
+        acc_rms.append(float(torch.linalg.norm(a - ci) / torch.linalg.norm(ci)))
+        acc_idx.append(int(i))
+    bt.check()
+
+    # ---- timed region (inputs resident; 10+ GB of samples >> L2)
+    for _ in range(args.warmup):
+        bt.inverse(coef.data_ptr(), grid_out.data_ptr(), sp)
+        bt.forward(grid.data_ptr(), coef_out.data_ptr(), sp)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            bt.inverse(coef.data_ptr(), grid_out.data_ptr(), sp)
+            bt.forward(grid.data_ptr(), coef_out.data_ptr(), sp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    bt.check()
+    clocks = clk.summary()
+    value = n * 1000.0 / ms
+    # one more step, eager with per-stage events, for the stage breakdown
+    bt.set_timing(True)
+    bt.stage_times(reset=True)
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s0.record(stream)
+    bt.inverse(coef.data_ptr(), grid_out.data_ptr(), sp)
+    bt.forward(grid.data_ptr(), coef_out.data_ptr(), sp)
+    s1.record(stream)
+    torch.cuda.synchronize()
+    eager_ms = s0.elapsed_time(s1)
+    st_all = bt.stage_times()
+    per_bucket = []
+    for k in range(bt.buckets):
+        L, cnt = bt.bucket_info(k)
+        t = bt.stage_times(bucket=k)
+        per_bucket.append((sum(v for v, _ in t.values()), L, cnt, {a: round(v, 3) for a, (v, _) in t.items()}))
+    bt.stage_times(reset=True)
+    bt.set_timing(False)
+    per_bucket.sort(reverse=True)
+    stage_summary = {k: {"ms": v, "launches": c} for k, (v, c) in st_all.items()}
+    launches = int(sum(c for _, c in st_all.values()))
+    io_bytes = 2.0 * 4.0 * (G + Ctot)  # per pair: grid + coefficients read once and written once
+    peaks = measured_peaks()
+
+    # ---- baseline: per-function launch loop of the FP64 path (one FP64 plan per l_max)
+    fp64 = None
+    if not args.no_fp64:
+        for L in sorted(set(int(x) for x in lmax)):
+            plans64.setdefault(L, _lib.Plan(_lib.SO3_REAL, L, 1, "fp64", "reference"))
+        g64 = grid.double()
+        c64 = coef.double()
+        go64 = torch.empty_like(g64)
+        co64 = torch.empty_like(c64)
+        goff = [bt.grid_offset(i) for i in range(n)]
+        coff = [bt.coeff_offset(i) for i in range(n)]
+        gp, cp, gop, cop = g64.data_ptr(), c64.data_ptr(), go64.data_ptr(), co64.data_ptr()
+
+        def loop():
+            for i in range(n):
+                p = plans64[int(lmax[i])]
+                p.inverse(cp + 8 * coff[i], gop + 8 * goff[i], sp)
+                p.forward(gp + 8 * goff[i], cop + 8 * coff[i], sp)
+
+        loop()
+        torch.cuda.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        loop()
+        f1.record(stream)
+        torch.cuda.synchronize()
+        ms64 = f0.elapsed_time(f1)
+        fp64 = {"value": n * 1000.0 / ms64, "unit": UNIT, "ms_per_step": ms64,
+                "note": "per-function launch loop, FFTSO3_REAL FP64 plans (batch 1, one per l_max), float64 samples"}
+        del g64, c64, go64, co64
+    line = {
+        "metric": UNEVEN_METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16x3 (split) / fp32 accumulate / fp32 FFT; fp32 samples",
+        "data": "synthetic",
+        "config": {"workload": f"{n} real SO(3) functions, l_max uniform in 8..64 (seed 3), coefficients "
+                               "N(0,1)/(2l+1), FP32 samples; fftso3_batch, tensor-core buckets, CUDA graph",
+                   "functions": n, "buckets": bt.buckets, "samples": int(G), "coefficients": int(Ctot),
+                   "l2": "inputs larger than L2"},
+        "io_gbs": io_bytes / (ms / 1000.0) / 1e9, "io_frac_of_hbm": io_bytes / (ms / 1000.0) / 1e9 / peaks["hbm_gbs"],
+        "batch_create_s": t_create, "device_gb": bt.device_bytes / 1e9,
+        "accuracy": {"rel_rms_vs_fp64_max": max(acc_rms), "functions": acc_idx},
+        "fp64_loop": fp64, "speedup_vs_fp64_loop": value / fp64["value"] if fp64 else None,
+        "clocks": clocks, "gpu_launches": launches * args.steps,
+        "stages_eager_sum_ms": stage_summary, "eager_timed_step_ms": eager_ms,
+        "top_buckets": [{"l_max": L, "functions": c, "ms": t, "stages": d} for t, L, c, d in per_bucket[:6]],
+    }
+    print(json.dumps(line), flush=True)
+
+
 # --------------------------------------------------------------- GPU arm
 
 def main() -> None:
@@ -205,9 +362,15 @@ def main() -> None:
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64 reference (profiling runs)")
+    ap.add_argument("--workload", default="lmax255", choices=["lmax255", "uneven"],
+                    help="lmax255: the headline batch at one l_max; uneven: the mixed-bandwidth batch")
+    ap.add_argument("--functions", type=int, default=4096, help="uneven workload: number of functions")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload == "uneven":
+        main_uneven(args)
         return
 
     import torch

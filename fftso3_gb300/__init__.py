@@ -9,11 +9,11 @@ from .matrix import (FFTS2_matrix_complex, FFTS2_matrix_real, FFTSO3_matrix_comp
                      s2_index, s2_ncoeff, so3_index, so3_ncoeff, so3_offset)
 from .rotation import R_to_euler323, euler323_to_R
 from .transforms import FFTS2_complex, FFTS2_real, FFTSO3_complex, FFTSO3_real, alpha_j, beta_k
-from ._lib import FFTSO3Error, Plan
+from ._lib import Batch, FFTSO3Error, Plan
 
 __all__ = [
     "FFTSO3_complex", "FFTSO3_real", "FFTS2_complex", "FFTS2_real",
     "FFTSO3_matrix_complex", "FFTSO3_matrix_real", "FFTS2_matrix_complex", "FFTS2_matrix_real",
     "so3_index", "so3_ncoeff", "so3_offset", "s2_index", "s2_ncoeff",
-    "R_to_euler323", "euler323_to_R", "alpha_j", "beta_k", "FFTSO3Error", "Plan",
+    "R_to_euler323", "euler323_to_R", "alpha_j", "beta_k", "FFTSO3Error", "Plan", "Batch",
 ]

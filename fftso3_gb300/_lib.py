@@ -31,6 +31,7 @@ RECURSION_REFERENCE = 0
 RECURSION_STABLE = 1
 
 FLAG_REFINE = 0x1
+FLAG_GRAPH = 0x2
 
 PRECISIONS = {"fp64": PREC_FP64, "tc_bf16x3": PREC_TC_BF16X3}
 RECURSIONS = {"reference": RECURSION_REFERENCE, "stable": RECURSION_STABLE}
@@ -62,6 +63,18 @@ SIGNATURES = {
     "fftso3_inverse_points": (_i, [_vp, _vp, _i, _dp, _i, _vp, _vp]),
     "fftso3_wigner_d": (_i, [_d, _i, _i, _dp]),
     "fftso3_forward_noalloc": (_i, [_i, _vp, _vp, _vp]),
+    "fftso3_batch_create": (_i, [ctypes.POINTER(_vp), _i, ctypes.POINTER(_i), _i, _i, _i, ctypes.c_uint]),
+    "fftso3_batch_destroy": (_i, [_vp]),
+    "fftso3_batch_grid_offset": (_ll, [_vp, _i]),
+    "fftso3_batch_coeff_offset": (_ll, [_vp, _i]),
+    "fftso3_batch_bucket_count": (_i, [_vp]),
+    "fftso3_batch_device_bytes": (_ll, [_vp]),
+    "fftso3_batch_forward": (_i, [_vp, _vp, _vp, _vp]),
+    "fftso3_batch_inverse": (_i, [_vp, _vp, _vp, _vp]),
+    "fftso3_batch_bucket_info": (_i, [_vp, _i, ctypes.POINTER(_i), ctypes.POINTER(_i)]),
+    "fftso3_batch_set_timing": (_i, [_vp, _i]),
+    "fftso3_batch_stage_times": (_i, [_vp, _i, _dp, ctypes.POINTER(_ll), _i]),
+    "fftso3_batch_check": (_i, [_vp]),
 }
 
 _lib = None
@@ -162,6 +175,87 @@ class Plan:
     def close(self) -> None:
         if getattr(self, "_h", None) is not None and _lib is not None:
             _lib.fftso3_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Owns one ``fftso3_batch``: functions of one kind with per-function l_max.
+
+    The batch chooses where each function lives in the grid and coefficient
+    buffers (``grid_offset(i)`` / ``coeff_offset(i)``, in elements; ``i = n``
+    gives the totals).
+    """
+
+    def __init__(self, kind: int, l_max, precision: str | int = "fp64", recursion: str | int = "reference",
+                 flags: int = 0):
+        self.kind = kind
+        self.l_max = [int(x) for x in l_max]
+        self.n = len(self.l_max)
+        self.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        self.recursion = RECURSIONS[recursion] if isinstance(recursion, str) else int(recursion)
+        self.flags = int(flags)
+        arr = (_i * max(self.n, 1))(*self.l_max)
+        h = _vp()
+        check(lib().fftso3_batch_create(ctypes.byref(h), kind, arr, self.n, self.precision, self.recursion,
+                                        ctypes.c_uint(self.flags)))
+        self._h = h
+
+    def grid_offset(self, i: int) -> int:
+        return int(lib().fftso3_batch_grid_offset(self._h, int(i)))
+
+    def coeff_offset(self, i: int) -> int:
+        return int(lib().fftso3_batch_coeff_offset(self._h, int(i)))
+
+    @property
+    def grid_elems(self) -> int:
+        return self.grid_offset(self.n)
+
+    @property
+    def coeff_elems(self) -> int:
+        return self.coeff_offset(self.n)
+
+    @property
+    def buckets(self) -> int:
+        return int(lib().fftso3_batch_bucket_count(self._h))
+
+    @property
+    def device_bytes(self) -> int:
+        return int(lib().fftso3_batch_device_bytes(self._h))
+
+    def forward(self, grid_ptr: int, coeff_ptr: int, stream: int = 0) -> None:
+        check(lib().fftso3_batch_forward(self._h, _vp(grid_ptr), _vp(coeff_ptr), _vp(stream)))
+
+    def inverse(self, coeff_ptr: int, grid_ptr: int, stream: int = 0) -> None:
+        check(lib().fftso3_batch_inverse(self._h, _vp(coeff_ptr), _vp(grid_ptr), _vp(stream)))
+
+    def bucket_info(self, k: int) -> tuple:
+        L, c = _i(), _i()
+        check(lib().fftso3_batch_bucket_info(self._h, int(k), ctypes.byref(L), ctypes.byref(c)))
+        return L.value, c.value
+
+    def set_timing(self, enable: bool = True) -> None:
+        check(lib().fftso3_batch_set_timing(self._h, 1 if enable else 0))
+
+    def stage_times(self, bucket: int = -1, reset: bool = False) -> dict:
+        """{stage name: (total ms, launches)} summed over buckets (bucket = -1) or for one bucket."""
+        n = lib().fftso3_stage_count()
+        ms = (ctypes.c_double * n)()
+        cnt = (_ll * n)()
+        check(lib().fftso3_batch_stage_times(self._h, int(bucket), ms, cnt, 1 if reset else 0))
+        return {lib().fftso3_stage_name(i).decode(): (ms[i], cnt[i]) for i in range(n) if cnt[i]}
+
+    def check(self) -> None:
+        check(lib().fftso3_batch_check(self._h))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and _lib is not None:
+            _lib.fftso3_batch_destroy(self._h)
             self._h = None
 
     def __del__(self):

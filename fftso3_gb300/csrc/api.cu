@@ -413,7 +413,7 @@ int fftso3_plan_create(fftso3_plan** out, int kind, int l_max, int batch, int pr
             if ((rc = plan_alloc(p, &p->d_fc, 16 * (size_t)batch * p->coeff_elems))) return bail(rc);
     } else {
         std::string err;
-        rc = tc_create(&p->tc, p->L, p->N, batch, p->d_table, goff, p->table_elems, p->d_tw, p->d_w, p->fac,
+        rc = tc_create(&p->tc, p->L, p->N, batch, p->d_table, goff, p->table_elems, p->d_tw, p->d_w,
                        (flags & FFTSO3_FLAG_REFINE) != 0, p->real, err);
         if (rc) {
             g_err = err;

@@ -775,8 +775,8 @@ void tc_destroy(TCState* s)
 long long tc_device_bytes(const TCState* s) { return s ? s->bytes : 0; }
 
 int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64, const std::vector<long long>& goff,
-              long long table_elems, const double* d_tw, const double* d_w, const FFTFactors& fac, bool refine,
-              bool real, std::string& err)
+              long long table_elems, const double* d_tw, const double* d_w, bool refine, bool real,
+              std::string& err)
 {
     *out = nullptr;
     if (N > MAXN) {
@@ -793,7 +793,7 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
     s->ngroups = s->B * s->B;
     s->refine = refine;
     s->real = real;
-    s->fac = fac;
+    make_fft_factors_prime_first(N, s->fac);
     s->d_tw = d_tw;
     s->total_rows = table_elems / N;
     int dev = 0;
@@ -911,15 +911,18 @@ static FFTLaunch fft_launch(const TCState* s, const void* in, void* out, bool co
     L.real_in = real_in;
     L.real_out = real_out;
     L.nlines = (long long)s->batch * N * N;
+    // lines per CTA: about 2048 elements per CTA (small N would otherwise leave most threads idle)
+    int lpb = 1;
+    while (lpb < 256 && (lpb * 2) * N <= 2048 && fft_smem_bytes(N, lpb * 2, false) <= 100 * 1024) lpb *= 2;
     if (!cols) {
-        L.lpb = 4;
+        L.lpb = lpb;
         L.inner = 1;
         L.ostride = N;
         L.istride = 0;
         L.es = 1;
         L.lines_fastest = false;
     } else {
-        L.lpb = 16;
+        L.lpb = lpb < 16 ? 16 : lpb;  // >= 16 adjacent lines: 128-byte segments
         while (L.lpb > 1 && fft_smem_bytes(N, L.lpb, false) > 100 * 1024) L.lpb /= 2;
         L.inner = N;
         L.ostride = (long long)N * N;

@@ -71,20 +71,43 @@ __device__ __forceinline__ void dft_small(typename V2<T>::t* v, const typename V
         v[1] = cadd(b0, b2); v[5] = csub(b0, b2);
         v[3] = cadd(b1, b3); v[7] = csub(b1, b3);
     } else {
-        // odd radix: out[q] = sum_t v[t] w^{tq}, w = e^{-2 pi i / R} = W_N^{N/R}
+        // odd radix R = 3, 5, 7 in the symmetric form (P = (R-1)/2):
+        //   out[q], out[R-q] = v0 + sum_{t<=P} a_t cos(2 pi t q / R) -/+ i b_t sin(2 pi t q / R),
+        //   a_t = v_t + v_{R-t}, b_t = v_t - v_{R-t};  w[((t q) mod R) Nr] = (cos, -sin)
+        constexpr int P = (R - 1) / 2;
+        C a[P + 1], b[P + 1];
+        C o0 = v[0];
+#pragma unroll
+        for (int t = 1; t <= P; ++t) {
+            a[t] = cadd(v[t], v[R - t]);
+            b[t] = csub(v[t], v[R - t]);
+            o0 = cadd(o0, a[t]);
+        }
         C o[R];
+        o[0] = o0;
 #pragma unroll
-        for (int q = 0; q < R; ++q) {
-            C s = v[0];
+        for (int q = 1; q <= P; ++q) {
+            C cs = v[0], sn = V2<T>::mk((T)0, (T)0);
 #pragma unroll
-            for (int t = 1; t < R; ++t) s = cadd(s, cmul(v[t], w[((t * q) % R) * Nr]));
-            o[q] = s;
+            for (int t = 1; t <= P; ++t) {
+                const C wv = w[((t * q) % R) * Nr];
+                cs.x += a[t].x * wv.x;
+                cs.y += a[t].y * wv.x;
+                sn.x -= b[t].x * wv.y;
+                sn.y -= b[t].y * wv.y;
+            }
+            o[q] = V2<T>::mk(cs.x + sn.y, cs.y - sn.x);
+            o[R - q] = V2<T>::mk(cs.x - sn.y, cs.y + sn.x);
         }
 #pragma unroll
         for (int q = 0; q < R; ++q) v[q] = o[q];
     }
 }
 
+// One Stockham pass of radix R over the lpb lines in shared memory.  Thread
+// items b = threadIdx.x + i blockDim.x map to (line l, butterfly j) and the
+// twiddle class k = j mod Ns; they advance by constant steps (Nr is a
+// multiple of Ns, so k survives the wrap of j), so the loop does no division.
 template <typename T, int R>
 __device__ __forceinline__ void stockham_stage(const typename V2<T>::t* __restrict__ src,
                                                typename V2<T>::t* __restrict__ dst,
@@ -95,9 +118,10 @@ __device__ __forceinline__ void stockham_stage(const typename V2<T>::t* __restri
     const int Nr = N / R;
     const int total = lpb * Nr;
     const int tstride = N / (Ns * R);
-    for (int b = threadIdx.x; b < total; b += blockDim.x) {
-        int l = b / Nr, j = b - l * Nr;
-        int k = j % Ns;
+    const int nt = blockDim.x;
+    const int linc = nt / Nr, jinc = nt - linc * Nr, kinc = jinc % Ns;
+    int l = threadIdx.x / Nr, j = threadIdx.x - l * Nr, k = j % Ns;
+    for (int b = threadIdx.x; b < total; b += nt) {
         const C* s = src + l * LS;
         C v[R];
 #pragma unroll
@@ -111,33 +135,135 @@ __device__ __forceinline__ void stockham_stage(const typename V2<T>::t* __restri
         C* d = dst + l * LS + (j - k) * R + k;
 #pragma unroll
         for (int t = 0; t < R; ++t) d[t * Ns] = v[t];
+        l += linc;
+        j += jinc;
+        k += kinc;
+        if (k >= Ns) k -= Ns;
+        if (j >= Nr) {
+            j -= Nr;
+            ++l;
+        }
     }
 }
 
-// Generic radix (any prime R): one output per thread, O(R) work each.
+// Generic radix (any prime R): each thread forms GQ outputs q of one
+// (line, j) group, sharing the R loads; the twiddle exponent of term t,
+// t (k tstride + q Nr) mod N, advances by one add and one conditional
+// subtract per term (no division in the inner loop).  Terms are summed in
+// ascending t, the plain DFT order.
 template <typename T>
 __device__ void stockham_generic(const typename V2<T>::t* __restrict__ src, typename V2<T>::t* __restrict__ dst,
                                  const typename V2<T>::t* __restrict__ w, int N, int Ns, int R, int lpb, int LS)
 {
     using C = typename V2<T>::t;
+    constexpr int GQ = 4;
     const int Nr = N / R;
-    const int total = lpb * N;
+    const int nqb = (R + GQ - 1) / GQ;
+    const int per_line = Nr * nqb;
+    const int total = lpb * per_line;
     const int tstride = N / (Ns * R);
     for (int b = threadIdx.x; b < total; b += blockDim.x) {
-        int l = b / N, o = b - l * N;
-        int k = o % Ns;
-        int q = (o / Ns) % R;
-        int jb = o / (Ns * R);
-        int j = jb * Ns + k;
+        const int l = b / per_line, rem = b - l * per_line;
+        const int qb = rem / Nr, j = rem - qb * Nr;
+        const int k = j % Ns;
         const C* s = src + l * LS;
-        C acc = s[j];
-        for (int t = 1; t < R; ++t) {
-            // twiddle W_N^{t k N/(Ns R)} times DFT factor W_N^{t q N/R}
-            long long e = ((long long)t * k * tstride + (long long)((t * q) % R) * Nr) % N;
-            acc = cadd(acc, cmul(s[j + t * Nr], w[e]));
+        C acc[GQ];
+        int e[GQ], step[GQ];
+        const C x0 = s[j];
+#pragma unroll
+        for (int u = 0; u < GQ; ++u) {
+            acc[u] = x0;
+            int st = k * tstride + (qb * GQ + u) * Nr;
+            st = st >= N ? st - N : st;
+            step[u] = st;
+            e[u] = st;
         }
-        dst[l * LS + o] = acc;
+        for (int t = 1; t < R; ++t) {
+            const C v = s[j + t * Nr];
+#pragma unroll
+            for (int u = 0; u < GQ; ++u) {
+                acc[u] = cadd(acc[u], cmul(v, w[e[u]]));
+                const int ne = e[u] + step[u];
+                e[u] = ne >= N ? ne - N : ne;
+            }
+        }
+        C* d = dst + l * LS + (j - k) * R + k;
+#pragma unroll
+        for (int u = 0; u < GQ; ++u) {
+            const int q = qb * GQ + u;
+            if (q < R) d[q * Ns] = acc[u];
+        }
     }
+}
+
+// First stage (Ns = 1) of a prime radix R > 8: the plain R-point DFTs of the
+// stride-Nr subsequences, X[j R + q] = sum_t x[j + t Nr] e^{-2 pi i t q / R},
+// in the symmetric form (P = (R-1)/2, a_t = x_t + x_{R-t}, b_t = x_t - x_{R-t}):
+//   X[q]     = x_0 + sum_{t<=P} a_t cos(2 pi t q / R) - i b_t sin(2 pi t q / R)
+//   X[R - q] = x_0 + sum_{t<=P} a_t cos(2 pi t q / R) + i b_t sin(2 pi t q / R)
+// which takes about R real FMAs per output instead of 4R.  The (cos, sin)
+// matrix of the R-point DFT, mat[(t-1) P4 + (q-1)], is built per CTA in shared
+// memory.  Each thread forms the outputs q and R - q of GP consecutive q
+// (two 16-byte matrix reads per term); work items run (j, line) fastest, so
+// the lanes of a warp share one block of q and every matrix read is a
+// broadcast.
+template <typename T>
+__device__ void dft_prime_first(const typename V2<T>::t* __restrict__ src, typename V2<T>::t* __restrict__ dst,
+                                const typename V2<T>::t* __restrict__ mat, int N, int R, int lpb, int LS)
+{
+    using C = typename V2<T>::t;
+    constexpr int GP = 4;
+    const int Nr = N / R;
+    const int P = (R - 1) / 2;
+    const int P4 = (P + GP - 1) / GP * GP;
+    const int nblk = P4 / GP;
+    const int per_blk = Nr * lpb;
+    const int total = per_blk * nblk;
+    for (int b = threadIdx.x; b < total; b += blockDim.x) {
+        const int blk = b / per_blk, rem = b - blk * per_blk;
+        const int l = rem / Nr, j = rem - l * Nr;
+        const C* s = src + l * LS + j;
+        const C x0 = s[0];
+        C acc0 = x0;
+        C Cs[GP], Ss[GP];
+#pragma unroll
+        for (int u = 0; u < GP; ++u) {
+            Cs[u] = V2<T>::mk((T)0, (T)0);
+            Ss[u] = V2<T>::mk((T)0, (T)0);
+        }
+        const C* m = mat + blk * GP;
+        for (int t = 1; t <= P; ++t, m += P4) {
+            const C xt = s[t * Nr], xr = s[(R - t) * Nr];
+            const C a = cadd(xt, xr), bb = csub(xt, xr);
+            acc0 = cadd(acc0, a);
+#pragma unroll
+            for (int u = 0; u < GP; ++u) {
+                const C cs = m[u];  // (cos, sin)
+                Cs[u].x += a.x * cs.x;
+                Cs[u].y += a.y * cs.x;
+                Ss[u].x += bb.x * cs.y;
+                Ss[u].y += bb.y * cs.y;
+            }
+        }
+        C* d = dst + l * LS + j * R;
+        if (blk == 0) d[0] = acc0;
+#pragma unroll
+        for (int u = 0; u < GP; ++u) {
+            const int q = 1 + blk * GP + u;
+            if (q <= P) {
+                const C base = cadd(x0, Cs[u]);
+                d[q] = V2<T>::mk(base.x + Ss[u].y, base.y - Ss[u].x);
+                d[R - q] = V2<T>::mk(base.x - Ss[u].y, base.y + Ss[u].x);
+            }
+        }
+    }
+}
+
+// entries of the (cos, sin) matrix used by dft_prime_first for prime radix R
+__host__ __device__ inline int prime_mat_entries(int R)
+{
+    const int P = (R - 1) / 2;
+    return P * ((P + 3) / 4 * 4);
 }
 
 template <typename T, typename TIN, bool REAL_IN, bool REAL_OUT>
@@ -155,8 +281,22 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(const TIN* __restrict__ 
     C* buf0 = w + N;
     C* buf1 = buf0 + lpb * LS;
     long long* base = reinterpret_cast<long long*>(buf1 + lpb * LS);
+    C* mat = reinterpret_cast<C*>(base + lpb);  // prime-first DFT matrix (only when fac.r[0] > 8)
     const double2* tw = reinterpret_cast<const double2*>(twg);
     for (int i = threadIdx.x; i < N; i += blockDim.x) w[i] = V2<T>::mk((T)tw[i].x, (T)tw[i].y);
+    if (fac.r[0] > 8) {
+        const int R = fac.r[0], P = (R - 1) / 2, P4 = (P + 3) / 4 * 4, Nr = N / R;
+        for (int i = threadIdx.x; i < P * P4; i += blockDim.x) {
+            const int t = i / P4 + 1, q = i - (t - 1) * P4 + 1;
+            T c = 0, sn = 0;
+            if (q <= P) {
+                const double2 v = tw[((t * q) % R) * Nr];  // e^{-2 pi i t q / R}
+                c = (T)v.x;
+                sn = (T)(-v.y);
+            }
+            mat[i] = V2<T>::mk(c, sn);
+        }
+    }
 
     const long long line0 = (long long)blockIdx.x * lpb;
     const int nl = (int)min((long long)lpb, nlines - line0);
@@ -176,12 +316,17 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(const TIN* __restrict__ 
             else buf0[l * LS + j] = in[off];
         }
     } else {
-        for (int l = 0; l < nl; ++l) {
-            const long long b0 = base[l];
-            for (int j = threadIdx.x; j < N; j += blockDim.x) {
-                const long long off = b0 + (long long)j * es;
-                if constexpr (REAL_IN) buf0[l * LS + j] = V2<T>::mk((T)in[off], (T)0);
-                else buf0[l * LS + j] = in[off];
+        const int linc = blockDim.x / N, jinc = blockDim.x - linc * N;
+        int l = threadIdx.x / N, j = threadIdx.x - l * N;
+        for (int e = threadIdx.x; e < nl * N; e += blockDim.x) {
+            const long long off = base[l] + (long long)j * es;
+            if constexpr (REAL_IN) buf0[l * LS + j] = V2<T>::mk((T)in[off], (T)0);
+            else buf0[l * LS + j] = in[off];
+            l += linc;
+            j += jinc;
+            if (j >= N) {
+                j -= N;
+                ++l;
             }
         }
     }
@@ -198,7 +343,10 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(const TIN* __restrict__ 
             case 5: stockham_stage<T, 5>(src, dst, w, N, Ns, lpb, LS); break;
             case 7: stockham_stage<T, 7>(src, dst, w, N, Ns, lpb, LS); break;
             case 8: stockham_stage<T, 8>(src, dst, w, N, Ns, lpb, LS); break;
-            default: stockham_generic<T>(src, dst, w, N, Ns, R, lpb, LS); break;
+            default:
+                if (Ns == 1) dft_prime_first<T>(src, dst, mat, N, R, lpb, LS);
+                else stockham_generic<T>(src, dst, w, N, Ns, R, lpb, LS);
+                break;
         }
         __syncthreads();
         C* t = src; src = dst; dst = t;
@@ -215,14 +363,17 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(const TIN* __restrict__ 
             else reinterpret_cast<C*>(out)[off] = v;
         }
     } else {
-        for (int l = 0; l < nl; ++l) {
-            const long long b0 = base[l];
-            for (int j = threadIdx.x; j < N; j += blockDim.x) {
-                const long long off = b0 + (long long)j * es;
-                const C v = src[l * LS + j];
-                if constexpr (REAL_OUT) reinterpret_cast<T*>(out)[off] = v.x;
-                else reinterpret_cast<C*>(out)[off] = v;
+        const int linc = blockDim.x / N, jinc = blockDim.x - linc * N;
+        int l = threadIdx.x / N, j = threadIdx.x - l * N;
+        for (int e = threadIdx.x; e < nl * N; e += blockDim.x, l += linc, j += jinc) {
+            if (j >= N) {
+                j -= N;
+                ++l;
             }
+            const long long off = base[l] + (long long)j * es;
+            const C v = src[l * LS + j];
+            if constexpr (REAL_OUT) reinterpret_cast<T*>(out)[off] = v.x;
+            else reinterpret_cast<C*>(out)[off] = v;
         }
     }
 }
@@ -240,10 +391,31 @@ void make_fft_factors(int N, FFTFactors& f)
     }
 }
 
+void make_fft_factors_prime_first(int N, FFTFactors& f)
+{
+    FFTFactors g;
+    make_fft_factors(N, g);
+    f.N = N;
+    f.n = 0;
+    for (int i = g.n - 1; i >= 0; --i)
+        if (g.r[i] > 8) f.r[f.n++] = g.r[i];
+    for (int i = 0; i < g.n; ++i)
+        if (g.r[i] <= 8) f.r[f.n++] = g.r[i];
+}
+
 size_t fft_smem_bytes(int N, int lpb, bool fp64)
 {
     size_t c = fp64 ? 16 : 8;
-    return c * ((size_t)N + 2 * (size_t)lpb * (N + 1)) + 8 * (size_t)lpb;
+    // the largest prime factor above 8 may head the factor list (prime-first order)
+    int r = N, pmax = 0;
+    for (int p = 2; r > 1; ++p)
+        while (r % p == 0) {
+            r /= p;
+            pmax = p;
+        }
+    // (only FP32 plans order factors prime-first; N = 2B keeps FP64 lists starting with 8, 4 or 2)
+    const size_t mat = (!fp64 && pmax > 8) ? (size_t)prime_mat_entries(pmax) : 0;
+    return c * ((size_t)N + 2 * (size_t)lpb * (N + 1)) + 8 * (size_t)lpb + c * mat;
 }
 
 template <typename T, typename TIN, bool RI, bool RO>

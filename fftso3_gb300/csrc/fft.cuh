@@ -25,6 +25,9 @@ struct FFTLaunch {
 };
 
 void make_fft_factors(int N, FFTFactors& f);
+// Same factors with the prime radices above 8 first (largest first): the
+// first stage is then a plain DFT whose twiddles every lane of a warp shares.
+void make_fft_factors_prime_first(int N, FFTFactors& f);
 size_t fft_smem_bytes(int N, int lpb, bool fp64);
 cudaError_t launch_fft_lines(const FFTLaunch& L, cudaStream_t st);
 

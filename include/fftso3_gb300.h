@@ -60,8 +60,10 @@ extern "C" {
 
 /* plan flags */
 #define FFTSO3_FLAG_REFINE 0x1u /* tensor-core forward: one residual step F += forward(f - inverse(F)) */
+#define FFTSO3_FLAG_GRAPH 0x2u  /* batches: capture each direction into a CUDA graph, replay it */
 
 typedef struct fftso3_plan fftso3_plan;
+typedef struct fftso3_batch fftso3_batch;
 
 /* Thread-local description of the last error ("" when none). */
 const char* fftso3_last_error_string(void);
@@ -141,6 +143,44 @@ int fftso3_inverse_points(fftso3_plan* plan, const void* coeffs, int index, cons
  * the SO(3) coefficients, computed on the GPU (host output buffer).
  * Replaces wigner_d(beta) (fdcl_FFTSO3.cpp:122-194). */
 int fftso3_wigner_d(double beta, int l_max, int recursion, double* d_out_host);
+
+/* ---- batches of uneven bandwidth ----
+ * One object for n_functions functions of one kind whose l_max differs per
+ * function (l_max[i]).  It replaces the reference user's loop of
+ * forward_transform / inverse_transform calls over functions
+ * (fdcl_FFTSO3.cpp:654-763, :774-850, :1141-1167; fdcl_FFTS2.cpp:125-230,
+ * :424-512), re-initialising the object whenever l_max changes (:500).
+ * Functions are bucketed by l_max and every bucket runs as one batched plan;
+ * the buckets run side by side on internal streams forked from and joined
+ * into the caller's stream.
+ * Layout: function i's grid starts fftso3_batch_grid_offset(b, i) elements
+ * into `grids` and its coefficients fftso3_batch_coeff_offset(b, i) elements
+ * into `coeffs` (elements of the kind's and precision's type, as for plans);
+ * i = n_functions gives the totals.  The batch chooses the offsets
+ * (ascending l_max, caller order within one l_max) so that no gather pass is
+ * needed.  flags: FFTSO3_FLAG_REFINE (tensor-core forward refinement),
+ * FFTSO3_FLAG_GRAPH (capture each direction once per (input, output) pair of
+ * pointers into a CUDA graph and replay it; a new pointer pair re-captures).
+ * Calls on one batch object must not overlap (shared workspaces). */
+int fftso3_batch_create(fftso3_batch** batch, int kind, const int* l_max, int n_functions, int precision,
+                        int recursion, unsigned flags);
+int fftso3_batch_destroy(fftso3_batch* batch);
+long long fftso3_batch_grid_offset(const fftso3_batch* batch, int fn);
+long long fftso3_batch_coeff_offset(const fftso3_batch* batch, int fn);
+int fftso3_batch_bucket_count(const fftso3_batch* batch);
+long long fftso3_batch_device_bytes(const fftso3_batch* batch);
+int fftso3_batch_forward(fftso3_batch* batch, const void* grids, void* coeffs, void* stream);
+int fftso3_batch_inverse(fftso3_batch* batch, const void* coeffs, void* grids, void* stream);
+/* Bucket `bucket` (0 <= bucket < fftso3_batch_bucket_count()): its l_max and number of functions. */
+int fftso3_batch_bucket_info(const fftso3_batch* batch, int bucket, int* l_max, int* count);
+/* Per-stage timing of every bucket's plan (as fftso3_plan_set_timing); while
+ * it is on, calls launch eagerly instead of through the CUDA graph, and the
+ * buckets run one after another on the caller's stream.  Stage
+ * times are summed over all buckets (bucket = -1) or given for one bucket. */
+int fftso3_batch_set_timing(fftso3_batch* batch, int enable);
+int fftso3_batch_stage_times(fftso3_batch* batch, int bucket, double* ms_total, long long* launches, int reset);
+/* Synchronise and report asynchronous failures of every bucket (fftso3_plan_check). */
+int fftso3_batch_check(fftso3_batch* batch);
 
 /* Largest l_max accepted by fftso3_forward_noalloc(). */
 #define FFTSO3_NOALLOC_MAX_LMAX 31

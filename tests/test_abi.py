@@ -68,6 +68,23 @@ def test_plan_create_rejects_bad_arguments(gblib, args, msg):
     assert not h.value
 
 
+@pytest.mark.parametrize("lmax,flags,msg", [
+    ([4, -1], 0, "l_max[1]"),
+    ([], 0, "n_functions"),
+    ([4], 0x80, "flag"),
+])
+def test_batch_create_rejects_bad_arguments(gblib, lmax, flags, msg):
+    h = ctypes.c_void_p()
+    arr = (ctypes.c_int * max(len(lmax), 1))(*lmax)
+    rc = gblib.lib().fftso3_batch_create(ctypes.byref(h), gblib.SO3_REAL, arr, len(lmax), 0, 0,
+                                         ctypes.c_uint(flags))
+    assert rc == gblib.ERR_INVALID_ARG
+    assert msg in gblib.lib().fftso3_last_error_string().decode()
+    assert not h.value
+    assert gblib.lib().fftso3_batch_grid_offset(None, 0) == -1
+    assert gblib.lib().fftso3_batch_forward(None, None, None, None) == gblib.ERR_INVALID_ARG
+
+
 def test_null_plan_is_rejected(gblib):
     L = gblib.lib()
     assert L.fftso3_forward(None, None, None, None) == gblib.ERR_INVALID_ARG

@@ -1,0 +1,109 @@
+"""Batches of uneven bandwidth (fftso3_batch_*) against per-function plans and the oracle (GPU).
+
+Tolerances: the FP64 batch equals per-function FP64 plans bit for bit (same
+kernels, same arithmetic per function); tensor-core results are within
+1e-6 relative of the FP64 oracle, as for plans.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_err, so3_coeffs
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-6
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    import torch
+    assert torch.cuda.is_available()
+    return torch
+
+
+def _layout_ok(b, lmax, kind, gblib):
+    """Bucket-major offsets, ascending l_max, caller order within a bucket, no overlap."""
+    lib = gblib.lib()
+    n = len(lmax)
+    order = sorted(range(n), key=lambda i: (lmax[i], i))
+    g = c = 0
+    for i in order:
+        assert b.grid_offset(i) == g and b.coeff_offset(i) == c
+        g += lib.fftso3_grid_elems(kind, lmax[i])
+        c += lib.fftso3_coeff_elems(kind, lmax[i])
+    assert b.grid_elems == g and b.coeff_elems == c
+    assert b.buckets == len(set(lmax))
+    assert b.grid_offset(n + 1) == -1 and b.grid_offset(-1) == -1
+
+
+def test_batch_real_tc_matches_oracle(gblib, oracle, torch_cuda):
+    torch = torch_cuda
+    lmax = [8, 12, 8, 20, 15, 12, 31, 9, 8]
+    kind = gblib.SO3_REAL
+    b = gblib.Batch(kind, lmax, "tc_bf16x3", "reference", gblib.FLAG_GRAPH)
+    _layout_ok(b, lmax, kind, gblib)
+    Fr = [so3_coeffs(L, seed=500 + i, complex_=False) for i, L in enumerate(lmax)]
+    grids = [oracle.so3_inverse_real_grid(L, F) for L, F in zip(lmax, Fr)]
+    gbuf = np.zeros(b.grid_elems, dtype=np.float32)
+    cbuf = np.zeros(b.coeff_elems, dtype=np.float32)
+    for i, L in enumerate(lmax):
+        gbuf[b.grid_offset(i):b.grid_offset(i) + grids[i].size] = grids[i].ravel()
+        cbuf[b.coeff_offset(i):b.coeff_offset(i) + Fr[i].size] = Fr[i]
+    s = torch.cuda.current_stream().cuda_stream
+    g = torch.from_numpy(gbuf).cuda()
+    c = torch.from_numpy(cbuf).cuda()
+    cout = torch.zeros_like(c)
+    gout = torch.zeros_like(g)
+    for _ in range(2):  # capture, then replay
+        b.forward(g.data_ptr(), cout.data_ptr(), s)
+        b.inverse(c.data_ptr(), gout.data_ptr(), s)
+    b.check()
+    co = cout.cpu().numpy().astype(np.float64)
+    go = gout.cpu().numpy().astype(np.float64)
+    for i, L in enumerate(lmax):
+        F_i = co[b.coeff_offset(i):b.coeff_offset(i) + Fr[i].size]
+        g_i = go[b.grid_offset(i):b.grid_offset(i) + grids[i].size]
+        assert rel_err(F_i, Fr[i]) < TOL, (i, L)
+        assert rel_err(g_i, grids[i].ravel()) < TOL, (i, L)
+
+
+def test_batch_fp64_equals_plans(gblib, torch_cuda):
+    """FP64 complex batch (graph and eager) equals one batch-1 plan per function, bit for bit."""
+    torch = torch_cuda
+    lmax = [5, 3, 5, 7, 3, 16]
+    kind = gblib.SO3_COMPLEX
+    s = torch.cuda.current_stream().cuda_stream
+    Fs = [so3_coeffs(L, seed=600 + i) for i, L in enumerate(lmax)]
+    outs = {}
+    for flags in (0, gblib.FLAG_GRAPH):
+        b = gblib.Batch(kind, lmax, "fp64", "reference", flags)
+        _layout_ok(b, lmax, kind, gblib)
+        cbuf = np.zeros(b.coeff_elems, dtype=np.complex128)
+        for i in range(len(lmax)):
+            cbuf[b.coeff_offset(i):b.coeff_offset(i) + Fs[i].size] = Fs[i]
+        c = torch.from_numpy(cbuf).cuda()
+        g = torch.zeros(b.grid_elems, dtype=torch.complex128, device="cuda")
+        c2 = torch.zeros_like(c)
+        b.inverse(c.data_ptr(), g.data_ptr(), s)
+        b.forward(g.data_ptr(), c2.data_ptr(), s)
+        # a second pointer pair forces a new capture in graph mode
+        g2 = torch.zeros_like(g)
+        b.inverse(c.data_ptr(), g2.data_ptr(), s)
+        b.check()
+        assert torch.equal(g, g2)
+        outs[flags] = (b, g.cpu().numpy(), c2.cpu().numpy())
+    b0, g0, c0 = outs[0]
+    b1, g1, c1 = outs[gblib.FLAG_GRAPH]
+    assert np.array_equal(g0, g1) and np.array_equal(c0, c1)
+    for i, L in enumerate(lmax):
+        p = gblib.Plan(kind, L, 1, "fp64", "reference")
+        ci = torch.from_numpy(Fs[i]).cuda()
+        gi = torch.zeros(p.grid_elems, dtype=torch.complex128, device="cuda")
+        fi = torch.zeros_like(ci)
+        p.inverse(ci.data_ptr(), gi.data_ptr(), s)
+        p.forward(gi.data_ptr(), fi.data_ptr(), s)
+        p.check()
+        go, co = b0.grid_offset(i), b0.coeff_offset(i)
+        assert np.array_equal(g0[go:go + p.grid_elems], gi.cpu().numpy())
+        assert np.array_equal(c0[co:co + p.coeff_elems], fi.cpu().numpy())
+        assert rel_err(c0[co:co + p.coeff_elems], Fs[i]) < 1e-12
+
