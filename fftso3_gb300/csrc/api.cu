@@ -307,8 +307,8 @@ int fftso3_plan_create(fftso3_plan** out, int kind, int l_max, int batch, int pr
     if ((flags & ~FFTSO3_FLAG_REFINE) != 0) return fail(FFTSO3_ERR_INVALID_ARG, "unknown flag bits");
     if (is_so3(kind) && l_max > 511) return fail(FFTSO3_ERR_UNSUPPORTED, "SO(3) l_max above 511 is not supported");
     if (!is_so3(kind) && l_max > 2047) return fail(FFTSO3_ERR_UNSUPPORTED, "S^2 l_max above 2047 is not supported");
-    if (precision == FFTSO3_PREC_TC_BF16X3 && !is_so3(kind))
-        return fail(FFTSO3_ERR_UNSUPPORTED, "tensor-core precision is implemented for the SO(3) kinds");
+    if (precision == FFTSO3_PREC_TC_BF16X3 && l_max > 511)
+        return fail(FFTSO3_ERR_UNSUPPORTED, "the tensor-core path supports l_max <= 511 (2(l_max+1) <= 1024)");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
         return fail(FFTSO3_ERR_NO_DEVICE, "no CUDA device available");
@@ -414,7 +414,7 @@ int fftso3_plan_create(fftso3_plan** out, int kind, int l_max, int batch, int pr
     } else {
         std::string err;
         rc = tc_create(&p->tc, p->L, p->N, batch, p->d_table, goff, p->table_elems, p->d_tw, p->d_w,
-                       (flags & FFTSO3_FLAG_REFINE) != 0, p->real, err);
+                       (flags & FFTSO3_FLAG_REFINE) != 0, p->real, !p->so3, err);
         if (rc) {
             g_err = err;
             return bail(rc);

@@ -48,7 +48,8 @@ namespace tc {
 
 constexpr int BM = 128;          // MMA M (rows of the accumulator = TMEM lanes)
 constexpr int BN = 128;          // MMA N (accumulator columns = 16 functions x 4 pairs x re/im)
-constexpr int FPT = BN / 8;      // functions per column tile
+constexpr int FPT = BN / 8;      // SO(3): functions per column tile (4 (m,n) pairs x re/im each)
+constexpr int FPT_S2 = BN / 4;   // S^2: functions per column tile (pairs m, -m x re/im)
 constexpr int BK = 64;           // k-step per ring slot (one 128-byte swizzle row of BF16)
 constexpr int UK = 16;           // K per tcgen05.mma (kind::f16)
 constexpr int STAGES = 2;
@@ -237,9 +238,29 @@ __device__ __forceinline__ void store_chunk(uint32_t bplanes, int R, int chunk, 
     }
 }
 
+// S^2 groups: g = m >= 0, pair 0 = (m, FFT bin m), pair 1 = (-m, bin N - m)
+// with sign (-1)^m (fdcl_FFTS2.cpp:160-166); the inverse writes pair 0 to bin
+// -m mod N and pair 1 to bin m (f = sum_m H(m) e^{+i m phi} by a forward DFT).
+__device__ __forceinline__ GroupPairs s2_pairs(int m)
+{
+    GroupPairs p;
+    p.np = m > 0 ? 2 : 1;
+    p.m[0] = m;
+    p.n[0] = 0;
+    p.sign[0] = 1;
+    p.m[1] = -m;
+    p.n[1] = 0;
+    p.sign[1] = (m & 1) ? -1 : 1;
+    p.m[2] = p.m[3] = p.n[2] = p.n[3] = 0;
+    p.sign[2] = p.sign[3] = 1;
+    return p;
+}
+
 // FWD = true: A = table (K-major, rows l), B = X from pencils; D[l][c].
 // FWD = false: A = table^T (MN-major, rows k), B = Y from coefficients; D[k][c].
-template <bool FWD>
+// S2 = false: SO(3) Wigner-d groups, pencils [fn][p][q][k], 4 pairs per function;
+// S2 = true: S^2 Legendre groups (g = m), pencils [fn][p][k], 2 pairs per function.
+template <bool FWD, bool S2>
 __global__ void __launch_bounds__(THREADS, 1)
     so3_tc_gemm_kernel(const __grid_constant__ CUtensorMap tA0, const __grid_constant__ CUtensorMap tA1,
                        const __grid_constant__ CUtensorMap tA2, GemmArgs args)
@@ -256,6 +277,8 @@ __global__ void __launch_bounds__(THREADS, 1)
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int B = args.L + 1, N = args.N;
+    constexpr int PPF = S2 ? 2 : 4;        // pairs per function
+    constexpr int FPTK = BN / (2 * PPF);   // functions per column tile
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
@@ -374,8 +397,8 @@ __global__ void __launch_bounds__(THREADS, 1)
         // latency overlaps the split/store of the previous step.
         const int pt = threadIdx.x - 64;
         const int c = pt >> 2, q4 = pt & 3;
-        const int fl = c >> 2, pp = c & 3;
-        const int Rre = fl * 8 + 2 * pp, Rim = Rre + 1;
+        const int fl = c / PPF, pp = c % PPF;
+        const int Rre = fl * 2 * PPF + 2 * pp, Rim = Rre + 1;
         struct Src {
             const float2* p;  // run start for this (function, pair), or null
             int lim;          // valid extent of the run (N, or nl)
@@ -384,13 +407,16 @@ __global__ void __launch_bounds__(THREADS, 1)
             const int4 item = args.items[it];
             int m0, n0;
             item_mn(item, m0, n0);
-            const GroupPairs P = group_pairs(m0, n0);
-            const int f = item.z * FPT + fl;
+            const GroupPairs P = S2 ? s2_pairs(m0) : group_pairs(m0, n0);
+            const int f = item.z * FPTK + fl;
             Src r;
             r.lim = FWD ? N : B - m0;
             r.p = nullptr;
             if (f >= args.batch || pp >= P.np) return r;
-            if (FWD) {
+            if (FWD && S2) {
+                const int bin = pp == 0 ? m0 : N - m0;
+                r.p = args.pin + (long long)f * args.fstride + (long long)bin * N;
+            } else if (FWD) {
                 int pi = (-P.m[pp]) % N; if (pi < 0) pi += N;
                 int qi = (-P.n[pp]) % N; if (qi < 0) qi += N;
                 r.p = args.pin + (long long)f * args.fstride + ((long long)pi * N + qi) * N;
@@ -486,13 +512,16 @@ __global__ void __launch_bounds__(THREADS, 1)
             const int4 item = args.items[it];
             int m0, n0;
             item_mn(item, m0, n0);
-            const GroupPairs P = group_pairs(m0, n0);
+            const GroupPairs P = S2 ? s2_pairs(m0) : group_pairs(m0, n0);
             const int nl = B - m0;
             long long poff[4];
 #pragma unroll
             for (int p = 0; p < 4; ++p) {
                 if (FWD) {
                     poff[p] = args.goff2[item.x] + (long long)p * nl;
+                } else if (S2) {
+                    int bin = (p == 0 ? -m0 : m0) % N; if (bin < 0) bin += N;
+                    poff[p] = (long long)bin * N;
                 } else {
                     int pi = P.m[p] % N; if (pi < 0) pi += N;
                     int qi = P.n[p] % N; if (qi < 0) qi += N;
@@ -513,8 +542,8 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
                 for (int j = 0; j < 32; ++j) v[j] += u[j];
 #pragma unroll
-                for (int fq = 0; fq < 4; ++fq) {
-                    const int f = item.z * FPT + chunk * 4 + fq;
+                for (int fq = 0; fq < 32 / (2 * PPF); ++fq) {
+                    const int f = item.z * FPTK + chunk * (32 / (2 * PPF)) + fq;
                     if (f >= args.batch) continue;
                     if (FWD) {
                         const int row = item.y * BM + r;
@@ -524,7 +553,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                         for (int p = 0; p < 4; ++p) {
                             if (p >= P.np) break;
                             const float sg = (float)P.sign[p];
-                            Fo[poff[p]] = make_float2(sg * v[fq * 8 + 2 * p], sg * v[fq * 8 + 2 * p + 1]);
+                            Fo[poff[p]] = make_float2(sg * v[fq * 2 * PPF + 2 * p], sg * v[fq * 2 * PPF + 2 * p + 1]);
                         }
                     } else {
                         const int k = item.y * BM + r;
@@ -533,7 +562,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
                         for (int p = 0; p < 4; ++p) {
                             if (p >= P.np) break;
-                            Ho[poff[p]] = make_float2(v[fq * 8 + 2 * p], v[fq * 8 + 2 * p + 1]);
+                            Ho[poff[p]] = make_float2(v[fq * 2 * PPF + 2 * p], v[fq * 2 * PPF + 2 * p + 1]);
                         }
                     }
                 }
@@ -658,6 +687,46 @@ __global__ void packed_to_group_kernel(const float2* __restrict__ F, float2* __r
     }
 }
 
+// S^2: group-major forward output -> packed F(l, m) at l^2 + m + l (one CTA per (l, function)).
+__global__ void s2_group_to_packed_kernel(const float2* __restrict__ Fg, float2* __restrict__ F,
+                                          const long long* __restrict__ goff2, int L, long long cstride)
+{
+    const int l = blockIdx.x, f = blockIdx.y;
+    const int B = L + 1;
+    const float2* src = Fg + (long long)f * cstride;
+    float2* dst = F + (long long)f * cstride + (long long)l * l;
+    for (int i = threadIdx.x; i < 2 * l + 1; i += blockDim.x) {
+        const int m = i - l, g = m < 0 ? -m : m, p = m < 0 ? 1 : 0;
+        dst[i] = src[goff2[g] + (long long)p * (B - g) + (l - g)];
+    }
+}
+
+// S^2: packed F -> group-major Y (pair 0: F(l, m); pair 1: (-1)^m F(l, -m)), one CTA per (m, function).
+__global__ void s2_packed_to_group_kernel(const float2* __restrict__ F, float2* __restrict__ Y,
+                                          const long long* __restrict__ goff2, int L, long long cstride)
+{
+    const int m = blockIdx.x, f = blockIdx.y;
+    const int nl = L + 1 - m, np = m > 0 ? 2 : 1;
+    const float sg = (m & 1) ? -1.f : 1.f;
+    const float2* src = F + (long long)f * cstride;
+    float2* dst = Y + (long long)f * cstride + goff2[m];
+    for (int i = threadIdx.x; i < np * nl; i += blockDim.x) {
+        const int p = i / nl, l = m + (i - p * nl);
+        const float2 v = src[s2_idx(l, p == 0 ? m : -m)];
+        const float sc = p == 0 ? 1.f : sg;
+        dst[i] = make_float2(sc * v.x, sc * v.y);
+    }
+}
+
+// S^2: zero the Nyquist pencil p = B of H'[fn][p][k].
+__global__ void s2_zero_nyquist_pencils_kernel(float2* __restrict__ H, int N, long long nf)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nf * N) return;
+    const long long f = i / N, k = i % N;
+    H[f * (long long)N * N + (long long)(N / 2) * N + k] = make_float2(0.f, 0.f);
+}
+
 __global__ void resid_kernel(const float2* __restrict__ f, float2* __restrict__ r, long long n)
 {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -690,7 +759,8 @@ using namespace tc;
 struct TCState {
     int L = 0, B = 0, N = 0, Kp = 0, batch = 0, ntiles = 0, ngroups = 0;
     bool refine = false;
-    bool real = false;            // real grids (FFTSO3_SO3_REAL): real samples in, real part out
+    bool real = false;            // real grids (FFTSO3_*_REAL): real samples in, real part out
+    bool s2 = false;              // S^2 (Legendre groups g = m, grids N^2) instead of SO(3)
     FFTFactors fac;
     const double* d_tw = nullptr;
     float* d_wf = nullptr;
@@ -775,7 +845,7 @@ void tc_destroy(TCState* s)
 long long tc_device_bytes(const TCState* s) { return s ? s->bytes : 0; }
 
 int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64, const std::vector<long long>& goff,
-              long long table_elems, const double* d_tw, const double* d_w, bool refine, bool real,
+              long long table_elems, const double* d_tw, const double* d_w, bool refine, bool real, bool s2,
               std::string& err)
 {
     *out = nullptr;
@@ -789,8 +859,9 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
     s->N = N;
     s->Kp = (N + 63) / 64 * 64;
     s->batch = batch;
-    s->ntiles = (batch + FPT - 1) / FPT;
-    s->ngroups = s->B * s->B;
+    s->s2 = s2;
+    s->ntiles = s2 ? (batch + FPT_S2 - 1) / FPT_S2 : (batch + FPT - 1) / FPT;
+    s->ngroups = s2 ? s->B : s->B * s->B;
     s->refine = refine;
     s->real = real;
     make_fft_factors_prime_first(N, s->fac);
@@ -827,43 +898,40 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
             return bail(FFTSO3_ERR_CUDA);
         }
     }
-    const size_t gridel = (size_t)batch * N * N * N;
+    const size_t gridel = (size_t)batch * N * N * (s2 ? 1 : N);
+    const long long C = s2 ? (long long)s->B * s->B : so3_off(s->B);
     if ((rc = tc_alloc(s, (void**)&s->d_work, sizeof(float2) * gridel, err))) return bail(rc);
     if ((rc = tc_alloc(s, (void**)&s->d_pencil, sizeof(float2) * gridel, err))) return bail(rc);
     if (real)
-        if ((rc = tc_alloc(s, (void**)&s->d_fc, sizeof(float2) * (size_t)batch * so3_off(s->B), err)))
-            return bail(rc);
+        if ((rc = tc_alloc(s, (void**)&s->d_fc, sizeof(float2) * (size_t)batch * C, err))) return bail(rc);
     if (refine) {
         if ((rc = tc_alloc(s, (void**)&s->d_resid, sizeof(float2) * gridel, err))) return bail(rc);
-        if ((rc = tc_alloc(s, (void**)&s->d_coef2, sizeof(float2) * (size_t)batch * so3_off(s->B), err)))
-            return bail(rc);
+        if ((rc = tc_alloc(s, (void**)&s->d_coef2, sizeof(float2) * (size_t)batch * C, err))) return bail(rc);
     }
     // group rows and work items; the inverse list is ordered by decreasing cost
     std::vector<long long> grow0(s->ngroups), goff2(s->ngroups + 1);
     std::vector<int4> itf, iti;
     long long acc2 = 0;
     for (int g = 0; g < s->ngroups; ++g) {
-        int m0, n0;
-        group_mn(g, m0, n0);
+        int m0 = g, n0 = 0;
+        if (!s2) group_mn(g, m0, n0);
         grow0[g] = goff[g] / N;
         const int nl = s->B - m0;
         goff2[g] = acc2;
-        acc2 += (long long)group_pairs(m0, n0).np * nl;
+        acc2 += (long long)(s2 ? (m0 > 0 ? 2 : 1) : group_pairs(m0, n0).np) * nl;
         for (int nt = 0; nt < s->ntiles; ++nt) {
             for (int mt = 0; mt * BM < nl; ++mt) itf.push_back(make_int4(g, mt, nt, item_w(m0, n0)));
             for (int mt = 0; mt * BM < N; ++mt) iti.push_back(make_int4(g, mt, nt, item_w(m0, n0)));
         }
     }
     std::stable_sort(iti.begin(), iti.end(), [&](const int4& a, const int4& b) {
-        int ma, na, mb, nb;
-        group_mn(a.x, ma, na);
-        group_mn(b.x, mb, nb);
+        const int ma = a.w >> 16, mb = b.w >> 16;
         return (s->B - ma + BK - 1) / BK > (s->B - mb + BK - 1) / BK;
     });
     s->n_items_fwd = (int)itf.size();
     s->n_items_inv = (int)iti.size();
     goff2[s->ngroups] = acc2;
-    if (acc2 != so3_off(s->B)) {
+    if (acc2 != C) {
         err = "internal: group-major layout does not cover the coefficients";
         return bail(FFTSO3_ERR_CUDA);
     }
@@ -886,10 +954,11 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
             return bail(FFTSO3_ERR_CUDA);
         }
     }
-    cudaError_t e = cudaFuncSetAttribute(so3_tc_gemm_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         SMEM_BYTES);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(so3_tc_gemm_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    cudaError_t e = cudaSuccess;
+    const void* kernels[4] = {(const void*)so3_tc_gemm_kernel<true, false>, (const void*)so3_tc_gemm_kernel<false, false>,
+                              (const void*)so3_tc_gemm_kernel<true, true>, (const void*)so3_tc_gemm_kernel<false, true>};
+    for (int i = 0; i < 4 && e == cudaSuccess; ++i)
+        e = cudaFuncSetAttribute(kernels[i], cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     if (e != cudaSuccess) {
         err = std::string("tensor-core kernel attributes: ") + cudaGetErrorString(e);
         return bail(FFTSO3_ERR_CUDA);
@@ -910,7 +979,7 @@ static FFTLaunch fft_launch(const TCState* s, const void* in, void* out, bool co
     L.fp64 = false;
     L.real_in = real_in;
     L.real_out = real_out;
-    L.nlines = (long long)s->batch * N * N;
+    L.nlines = (long long)s->batch * N * (s->s2 ? 1 : N);
     // lines per CTA: about 2048 elements per CTA (small N would otherwise leave most threads idle)
     int lpb = 1;
     while (lpb < 256 && (lpb * 2) * N <= 2048 && fft_smem_bytes(N, lpb * 2, false) <= 100 * 1024) lpb *= 2;
@@ -953,8 +1022,8 @@ static GemmArgs gemm_args(const TCState* s)
     a.N = s->N;
     a.Kp = s->Kp;
     a.batch = s->batch;
-    a.fstride = (long long)s->N * s->N * s->N;
-    a.cstride = so3_off(s->B);
+    a.fstride = (long long)s->N * s->N * (s->s2 ? 1 : s->N);
+    a.cstride = s->s2 ? (long long)s->B * s->B : so3_off(s->B);
     a.pin = nullptr;
     a.cin = nullptr;
     a.cout = nullptr;
@@ -964,77 +1033,83 @@ static GemmArgs gemm_args(const TCState* s)
     return a;
 }
 
-// grid: float2 samples, or float samples when s->real.
-static int tc_forward_once(TCState* s, const void* grid, float2* F, cudaStream_t st, StageTimer* T,
-                           std::string& err)
+static int launch_gemm(TCState* s, bool fwd, cudaStream_t st, std::string& err)
+{
+    GemmArgs a = gemm_args(s);
+    a.items = fwd ? s->d_items_fwd : s->d_items_inv;
+    a.nitems = fwd ? s->n_items_fwd : s->n_items_inv;
+    if (fwd) {
+        a.pin = s->d_pencil;
+        a.cout = s->d_fg;
+    } else {
+        a.cin = s->d_fg;
+        a.pout = s->d_pencil;
+    }
+    const int nctas = a.nitems < s->nsm ? a.nitems : s->nsm;
+    const CUtensorMap* tm = fwd ? s->tmA_fwd : s->tmA_inv;
+    if (fwd && s->s2)
+        so3_tc_gemm_kernel<true, true><<<nctas, THREADS, SMEM_BYTES, st>>>(tm[0], tm[1], tm[2], a);
+    else if (fwd)
+        so3_tc_gemm_kernel<true, false><<<nctas, THREADS, SMEM_BYTES, st>>>(tm[0], tm[1], tm[2], a);
+    else if (s->s2)
+        so3_tc_gemm_kernel<false, true><<<nctas, THREADS, SMEM_BYTES, st>>>(tm[0], tm[1], tm[2], a);
+    else
+        so3_tc_gemm_kernel<false, false><<<nctas, THREADS, SMEM_BYTES, st>>>(tm[0], tm[1], tm[2], a);
+    TCK(cudaGetLastError());
+    return FFTSO3_SUCCESS;
+}
+
+static long long coeffs_per_fn(const TCState* s) { return s->s2 ? (long long)s->B * s->B : so3_off(s->B); }
+static long long grid_per_fn(const TCState* s) { return (long long)s->N * s->N * (s->s2 ? 1 : s->N); }
+
+// grid -> k-contiguous pencils (SO(3): [fn][p][q][k], S^2: [fn][p][k]); grid is
+// float2, or float when s->real.
+static int fft_forward(TCState* s, const void* grid, cudaStream_t st, StageTimer* T, std::string& err)
 {
     const long long N = s->N;
     if (fft_fast_supported(s->N)) {
-        // register-resident FFTs; the alpha pass writes the k-contiguous pencils directly
+        // register-resident FFTs; the last pass writes the k-contiguous pencils directly
         T->begin(ST_FFT_ROWS, st);
-        TCK(launch_fft_grid_pass(grid, s->d_work, s->batch, s->N, 1, s->d_tw, st, s->real));
+        if (s->s2)
+            TCK(launch_fft_s2_pass(grid, s->d_pencil, s->batch, s->N, 1, s->d_tw, st, s->real));
+        else
+            TCK(launch_fft_grid_pass(grid, s->d_work, s->batch, s->N, 1, s->d_tw, st, s->real));
         T->end(st);
-        T->begin(ST_FFT_COLS, st);
-        TCK(launch_fft_grid_pass(s->d_work, s->d_pencil, s->batch, s->N, 2, s->d_tw, st));
-        T->end(st);
-    } else {
-        T->begin(ST_FFT_ROWS, st);
-        TCK(launch_fft_lines(fft_launch(s, grid, s->d_work, false, s->real, false), st));
-        T->end(st);
+        if (!s->s2) {
+            T->begin(ST_FFT_COLS, st);
+            TCK(launch_fft_grid_pass(s->d_work, s->d_pencil, s->batch, s->N, 2, s->d_tw, st));
+            T->end(st);
+        }
+        return FFTSO3_SUCCESS;
+    }
+    T->begin(ST_FFT_ROWS, st);
+    TCK(launch_fft_lines(fft_launch(s, grid, s->d_work, false, s->real, false), st));
+    T->end(st);
+    if (!s->s2) {
         T->begin(ST_FFT_COLS, st);
         TCK(launch_fft_lines(fft_launch(s, s->d_work, s->d_work, true), st));
         T->end(st);
-        T->begin(ST_PACK_FWD, st);
-        dim3 tg((unsigned)((N * N + 31) / 32), (unsigned)((N + 31) / 32), (unsigned)s->batch);
-        transpose_kernel<<<tg, dim3(32, 8), 0, st>>>(s->d_work, s->d_pencil, N, N * N);
-        TCK(cudaGetLastError());
-        T->end(st);
     }
-    GemmArgs a = gemm_args(s);
-    a.items = s->d_items_fwd;
-    a.nitems = s->n_items_fwd;
-    a.pin = s->d_pencil;
-    a.cout = s->d_fg;
-    const int nctas = s->n_items_fwd < s->nsm ? s->n_items_fwd : s->nsm;
-    T->begin(ST_GEMM_FWD, st);
-    so3_tc_gemm_kernel<true><<<nctas, THREADS, SMEM_BYTES, st>>>(s->tmA_fwd[0], s->tmA_fwd[1], s->tmA_fwd[2], a);
-    TCK(cudaGetLastError());
-    T->end(st);
-    T->begin(ST_BASIS, st);
-    group_to_packed_kernel<<<dim3(s->B, s->batch), 256, 0, st>>>(s->d_fg, F, s->d_goff2, s->L, so3_off(s->B));
+    T->begin(ST_PACK_FWD, st);
+    const long long Cc = s->s2 ? N : N * N;  // [k][rest] -> [rest][k]
+    dim3 tg((unsigned)((Cc + 31) / 32), (unsigned)((N + 31) / 32), (unsigned)s->batch);
+    transpose_kernel<<<tg, dim3(32, 8), 0, st>>>(s->d_work, s->d_pencil, N, Cc);
     TCK(cudaGetLastError());
     T->end(st);
     return FFTSO3_SUCCESS;
 }
 
-// grid: float2 samples, or the real parts (float) when s->real.
-static int tc_inverse_once(TCState* s, const float2* F, void* grid, cudaStream_t st, StageTimer* T,
-                           std::string& err)
+// k-contiguous pencils -> grid (float2, or the real parts when s->real).
+static int fft_inverse(TCState* s, void* grid, cudaStream_t st, StageTimer* T, std::string& err)
 {
     const long long N = s->N;
-    T->begin(ST_NYQUIST, st);
-    {
-        long long tot = (long long)s->batch * 2 * N * N;
-        zero_nyquist_pencils_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(s->d_pencil, (int)N, s->batch);
-        TCK(cudaGetLastError());
-    }
-    T->end(st);
-    T->begin(ST_BASIS, st);
-    packed_to_group_kernel<<<dim3(s->ngroups, s->batch), 128, 0, st>>>(F, s->d_fg, s->d_goff2, s->L,
-                                                                      so3_off(s->B));
-    TCK(cudaGetLastError());
-    T->end(st);
-    GemmArgs a = gemm_args(s);
-    a.items = s->d_items_inv;
-    a.nitems = s->n_items_inv;
-    a.cin = s->d_fg;
-    a.pout = s->d_pencil;
-    const int nctas = s->n_items_inv < s->nsm ? s->n_items_inv : s->nsm;
-    T->begin(ST_GEMM_INV, st);
-    so3_tc_gemm_kernel<false><<<nctas, THREADS, SMEM_BYTES, st>>>(s->tmA_inv[0], s->tmA_inv[1], s->tmA_inv[2], a);
-    TCK(cudaGetLastError());
-    T->end(st);
     if (fft_fast_supported(s->N)) {
+        if (s->s2) {
+            T->begin(ST_FFT_ROWS, st);
+            TCK(launch_fft_s2_pass(s->d_pencil, grid, s->batch, s->N, -1, s->d_tw, st, s->real));
+            T->end(st);
+            return FFTSO3_SUCCESS;
+        }
         T->begin(ST_FFT_COLS, st);
         TCK(launch_fft_grid_pass(s->d_pencil, s->d_work, s->batch, s->N, -2, s->d_tw, st));
         T->end(st);
@@ -1045,11 +1120,18 @@ static int tc_inverse_once(TCState* s, const float2* F, void* grid, cudaStream_t
     }
     T->begin(ST_PACK_INV, st);
     {
-        dim3 tg((unsigned)((N + 31) / 32), (unsigned)((N * N + 31) / 32), (unsigned)s->batch);
-        transpose_kernel<<<tg, dim3(32, 8), 0, st>>>(s->d_pencil, s->d_work, N * N, N);
+        const long long Cc = s->s2 ? N : N * N;
+        dim3 tg((unsigned)((N + 31) / 32), (unsigned)((Cc + 31) / 32), (unsigned)s->batch);
+        transpose_kernel<<<tg, dim3(32, 8), 0, st>>>(s->d_pencil, s->d_work, Cc, N);
         TCK(cudaGetLastError());
     }
     T->end(st);
+    if (s->s2) {
+        T->begin(ST_FFT_ROWS, st);
+        TCK(launch_fft_lines(fft_launch(s, s->d_work, grid, false, false, s->real), st));
+        T->end(st);
+        return FFTSO3_SUCCESS;
+    }
     T->begin(ST_FFT_ROWS, st);
     TCK(launch_fft_lines(fft_launch(s, s->d_work, s->d_work, false), st));
     T->end(st);
@@ -1059,16 +1141,67 @@ static int tc_inverse_once(TCState* s, const float2* F, void* grid, cudaStream_t
     return FFTSO3_SUCCESS;
 }
 
+static int tc_forward_once(TCState* s, const void* grid, float2* F, cudaStream_t st, StageTimer* T,
+                           std::string& err)
+{
+    int rc = fft_forward(s, grid, st, T, err);
+    if (rc) return rc;
+    T->begin(ST_GEMM_FWD, st);
+    if ((rc = launch_gemm(s, true, st, err))) return rc;
+    T->end(st);
+    T->begin(ST_BASIS, st);
+    if (s->s2)
+        s2_group_to_packed_kernel<<<dim3(s->B, s->batch), 256, 0, st>>>(s->d_fg, F, s->d_goff2, s->L,
+                                                                       coeffs_per_fn(s));
+    else
+        group_to_packed_kernel<<<dim3(s->B, s->batch), 256, 0, st>>>(s->d_fg, F, s->d_goff2, s->L,
+                                                                    coeffs_per_fn(s));
+    TCK(cudaGetLastError());
+    T->end(st);
+    return FFTSO3_SUCCESS;
+}
+
+static int tc_inverse_once(TCState* s, const float2* F, void* grid, cudaStream_t st, StageTimer* T,
+                           std::string& err)
+{
+    const long long N = s->N;
+    T->begin(ST_NYQUIST, st);
+    if (s->s2) {
+        const long long tot = (long long)s->batch * N;
+        s2_zero_nyquist_pencils_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(s->d_pencil, (int)N, s->batch);
+    } else {
+        const long long tot = (long long)s->batch * 2 * N * N;
+        zero_nyquist_pencils_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(s->d_pencil, (int)N, s->batch);
+    }
+    TCK(cudaGetLastError());
+    T->end(st);
+    T->begin(ST_BASIS, st);
+    if (s->s2)
+        s2_packed_to_group_kernel<<<dim3(s->ngroups, s->batch), 128, 0, st>>>(F, s->d_fg, s->d_goff2, s->L,
+                                                                             coeffs_per_fn(s));
+    else
+        packed_to_group_kernel<<<dim3(s->ngroups, s->batch), 128, 0, st>>>(F, s->d_fg, s->d_goff2, s->L,
+                                                                          coeffs_per_fn(s));
+    TCK(cudaGetLastError());
+    T->end(st);
+    T->begin(ST_GEMM_INV, st);
+    int rc = launch_gemm(s, false, st, err);
+    if (rc) return rc;
+    T->end(st);
+    return fft_inverse(s, grid, st, T, err);
+}
+
 int tc_forward(TCState* s, const void* grid, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err)
 {
-    // real kinds: complex coefficients in d_fc, then the real basis (fdcl_FFTSO3.cpp:1169-1181)
+    // real kinds: complex coefficients in d_fc, then the real basis
+    // (fdcl_FFTSO3.cpp:1169-1181, fdcl_FFTS2.cpp:424-436)
     float2* Fc = s->real ? s->d_fc : (float2*)coeffs;
     int rc = tc_forward_once(s, grid, Fc, st, T, err);
     if (rc) return rc;
     if (s->refine) {
         // one residual step: F += forward(f - inverse(F))
-        const long long ng = (long long)s->batch * s->N * s->N * s->N;
-        const long long nc = (long long)s->batch * so3_off(s->B);
+        const long long ng = (long long)s->batch * grid_per_fn(s);
+        const long long nc = (long long)s->batch * coeffs_per_fn(s);
         if ((rc = tc_inverse_once(s, Fc, s->d_resid, st, T, err))) return rc;
         T->begin(ST_REFINE, st);
         if (s->real)
@@ -1086,7 +1219,10 @@ int tc_forward(TCState* s, const void* grid, void* coeffs, cudaStream_t st, Stag
     }
     if (s->real) {
         T->begin(ST_BASIS, st);
-        TCK(launch_so3_c2r(Fc, coeffs, false, s->L, s->batch, st));
+        if (s->s2)
+            TCK(launch_s2_c2r(Fc, coeffs, false, s->L, s->batch, st));
+        else
+            TCK(launch_so3_c2r(Fc, coeffs, false, s->L, s->batch, st));
         T->end(st);
     }
     return FFTSO3_SUCCESS;
@@ -1097,7 +1233,10 @@ int tc_inverse(TCState* s, const void* coeffs, void* grid, cudaStream_t st, Stag
     const float2* Fc = (const float2*)coeffs;
     if (s->real) {
         T->begin(ST_BASIS, st);
-        TCK(launch_so3_r2c(coeffs, s->d_fc, false, s->L, s->batch, st));
+        if (s->s2)
+            TCK(launch_s2_r2c(coeffs, s->d_fc, false, s->L, s->batch, st));
+        else
+            TCK(launch_so3_r2c(coeffs, s->d_fc, false, s->L, s->batch, st));
         T->end(st);
         Fc = s->d_fc;
     }

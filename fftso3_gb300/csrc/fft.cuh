@@ -43,5 +43,11 @@ cudaError_t launch_fft_rows_fast(const void* in, void* out, long long nlines, in
 // real_io: pass 1 reads real samples (float), pass -1 writes the real part only.
 cudaError_t launch_fft_grid_pass(const void* in, void* out, long long nf, int N, int pass, const void* tw,
                                  cudaStream_t st, bool real_io = false);
+// Tiled pass over nf S^2 grids of N^2 complex64 (in != out):
+//   dir  1: grid [nf][k][j]     -> FFT over j -> pencils [nf][p][k]
+//   dir -1: pencils [nf][p][k]  -> FFT over p -> grid [nf][k][j]
+// real_io: dir 1 reads real samples, dir -1 writes the real part only.
+cudaError_t launch_fft_s2_pass(const void* in, void* out, long long nf, int N, int dir, const void* tw,
+                               cudaStream_t st, bool real_io = false);
 
 }  // namespace fftso3

@@ -207,19 +207,25 @@ constexpr int PWARPS = 8;            // 2 lines per warp
 template <int R>
 __device__ __forceinline__ int ppos(int j) { return j + (j >> ilog2(R)); }
 
+// Geometry of a tiled pass (element offsets).
+struct TileGeo {
+    long long FS;  // per function (N^3 for SO(3) grids, N^2 for S^2 grids)
+    int NO;        // outer index range (N for SO(3), 1 for S^2)
+    long long Oc, Ls, Ot, Js;
+};
+
 // A tile of TL lines with one side contiguous and the other transposed.
 //   contiguous side: line l, element j at  cbase + l * Ls + j
 //   transposed side: line l, element j at  tbase + j * Js + l    (TL consecutive l)
-// cbase = f N^3 + o Oc + bb TL Ls,  tbase = f N^3 + o Ot + bb TL, with the CTA
-// index split into (f, o < N, bb < N / TL).  C2T = true reads the contiguous
+// cbase = f FS + o Oc + bb TL Ls,  tbase = f FS + o Ot + bb TL, with the CTA
+// index split into (f, o < NO, bb < N / TL).  C2T = true reads the contiguous
 // side and writes the transposed one; C2T = false the reverse.  Both sides
 // move TL * 8 = 128-byte runs.
 // REAL_IO: the contiguous side holds real values (pass 1 reads real samples,
 // pass -1 writes the real part only).
 template <int R, bool C2T, bool REAL_IO>
 __global__ void __launch_bounds__(32 * PWARPS, 3) fft_tile(const float2* __restrict__ in, float2* __restrict__ out,
-                                                        long long Oc, long long Ls, long long Ot, long long Js,
-                                                        const double2* __restrict__ tw)
+                                                        const TileGeo g, const double2* __restrict__ tw)
 {
     constexpr int N = 32 * R;
     constexpr int LR = ilog2(R);
@@ -231,12 +237,12 @@ __global__ void __launch_bounds__(32 * PWARPS, 3) fft_tile(const float2* __restr
 
     constexpr int NB = N / TL;
     const long long b = blockIdx.x;
-    const long long f = b / ((long long)N * NB);
-    const long long o = (b / NB) % N;
+    const long long f = b / ((long long)g.NO * NB);
+    const long long o = (b / NB) % g.NO;
     const long long bb = b % NB;
-    const long long N3 = (long long)N * N * N;
-    const long long cbase = f * N3 + o * Oc + bb * TL * Ls;
-    const long long tbase = f * N3 + o * Ot + bb * TL;
+    const long long Ls = g.Ls, Js = g.Js;
+    const long long cbase = f * g.FS + o * g.Oc + bb * TL * Ls;
+    const long long tbase = f * g.FS + o * g.Ot + bb * TL;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     constexpr int NV = TL * N / 2 / (32 * PWARPS);  // float4 accesses per thread on the transposed side
     static_assert(TL * N / 2 % (32 * PWARPS) == 0, "tile must split evenly over the threads");
@@ -318,8 +324,7 @@ __global__ void __launch_bounds__(32 * PWARPS, 3) fft_tile(const float2* __restr
 }
 
 template <int R, bool C2T, bool REAL_IO>
-static cudaError_t tile_r(const void* in, void* out, long long nf, long long Oc, long long Ls, long long Ot,
-                          long long Js, const void* tw, cudaStream_t st)
+static cudaError_t tile_r(const void* in, void* out, long long nf, const TileGeo& g, const void* tw, cudaStream_t st)
 {
     constexpr int N = 32 * R;
     constexpr int LP = N + N / R + 1;
@@ -327,24 +332,31 @@ static cudaError_t tile_r(const void* in, void* out, long long nf, long long Oc,
     auto k = fft_tile<R, C2T, REAL_IO>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    const long long nblk = nf * (long long)N * (N / TL);
-    k<<<(unsigned)nblk, 32 * PWARPS, smem, st>>>((const float2*)in, (float2*)out, Oc, Ls, Ot, Js,
-                                                  (const double2*)tw);
+    const long long nblk = nf * (long long)g.NO * (N / TL);
+    k<<<(unsigned)nblk, 32 * PWARPS, smem, st>>>((const float2*)in, (float2*)out, g, (const double2*)tw);
     return cudaGetLastError();
 }
 
 template <bool C2T, bool REAL_IO>
-static cudaError_t tile_dispatch(const void* in, void* out, long long nf, int N, long long Oc, long long Ls,
-                                 long long Ot, long long Js, const void* tw, cudaStream_t st)
+static cudaError_t tile_dispatch(const void* in, void* out, long long nf, int N, const TileGeo& g, const void* tw,
+                                 cudaStream_t st)
 {
     switch (N) {
-        case 64: return tile_r<2, C2T, REAL_IO>(in, out, nf, Oc, Ls, Ot, Js, tw, st);
-        case 128: return tile_r<4, C2T, REAL_IO>(in, out, nf, Oc, Ls, Ot, Js, tw, st);
-        case 256: return tile_r<8, C2T, REAL_IO>(in, out, nf, Oc, Ls, Ot, Js, tw, st);
-        case 512: return tile_r<16, C2T, REAL_IO>(in, out, nf, Oc, Ls, Ot, Js, tw, st);
-        case 1024: return tile_r<32, C2T, REAL_IO>(in, out, nf, Oc, Ls, Ot, Js, tw, st);
+        case 64: return tile_r<2, C2T, REAL_IO>(in, out, nf, g, tw, st);
+        case 128: return tile_r<4, C2T, REAL_IO>(in, out, nf, g, tw, st);
+        case 256: return tile_r<8, C2T, REAL_IO>(in, out, nf, g, tw, st);
+        case 512: return tile_r<16, C2T, REAL_IO>(in, out, nf, g, tw, st);
+        case 1024: return tile_r<32, C2T, REAL_IO>(in, out, nf, g, tw, st);
         default: return cudaErrorNotSupported;
     }
+}
+
+template <bool C2T>
+static cudaError_t tile_any(const void* in, void* out, long long nf, int N, const TileGeo& g, const void* tw,
+                            cudaStream_t st, bool real_io)
+{
+    return real_io ? tile_dispatch<C2T, true>(in, out, nf, N, g, tw, st)
+                   : tile_dispatch<C2T, false>(in, out, nf, N, g, tw, st);
 }
 
 template <int R>
@@ -382,19 +394,27 @@ cudaError_t launch_fft_rows_fast(const void* in, void* out, long long nlines, in
 cudaError_t launch_fft_grid_pass(const void* in, void* out, long long nf, int N, int pass, const void* tw,
                                  cudaStream_t st, bool real_io)
 {
-    const long long N1 = N, N2 = (long long)N * N;
+    const long long N1 = N, N2 = (long long)N * N, N3 = N2 * N;
     if (real_io && pass != 1 && pass != -1) return cudaErrorInvalidValue;
+    const ffast::TileGeo g1{N3, N, N2, N1, N2, N1};  // lines along j2 / q, transposed (q, j1)
+    const ffast::TileGeo g2{N3, N, N1, N2, N1, N2};  // lines along j1 / p, transposed (p.., k)
     switch (pass) {
-        case 1:
-            return real_io ? ffast::tile_dispatch<true, true>(in, out, nf, N, N2, N1, N2, N1, tw, st)
-                           : ffast::tile_dispatch<true, false>(in, out, nf, N, N2, N1, N2, N1, tw, st);
-        case 2: return ffast::tile_dispatch<true, false>(in, out, nf, N, N1, N2, N1, N2, tw, st);
-        case -2: return ffast::tile_dispatch<false, false>(in, out, nf, N, N1, N2, N1, N2, tw, st);
-        case -1:
-            return real_io ? ffast::tile_dispatch<false, true>(in, out, nf, N, N2, N1, N2, N1, tw, st)
-                           : ffast::tile_dispatch<false, false>(in, out, nf, N, N2, N1, N2, N1, tw, st);
+        case 1: return ffast::tile_any<true>(in, out, nf, N, g1, tw, st, real_io);
+        case 2: return ffast::tile_any<true>(in, out, nf, N, g2, tw, st, false);
+        case -2: return ffast::tile_any<false>(in, out, nf, N, g2, tw, st, false);
+        case -1: return ffast::tile_any<false>(in, out, nf, N, g1, tw, st, real_io);
         default: return cudaErrorInvalidValue;
     }
+}
+
+cudaError_t launch_fft_s2_pass(const void* in, void* out, long long nf, int N, int dir, const void* tw,
+                               cudaStream_t st, bool real_io)
+{
+    const long long N1 = N, N2 = (long long)N * N;
+    const ffast::TileGeo g{N2, 1, 0, N1, 0, N1};  // lines along j (contiguous), transposed [p][k]
+    if (dir == 1) return ffast::tile_any<true>(in, out, nf, N, g, tw, st, real_io);
+    if (dir == -1) return ffast::tile_any<false>(in, out, nf, N, g, tw, st, real_io);
+    return cudaErrorInvalidValue;
 }
 
 }  // namespace fftso3

@@ -1,4 +1,4 @@
-// Tensor-core (tcgen05, split-BF16) SO(3) transform state (see contract_tc.cu).
+// Tensor-core (tcgen05, split-BF16) SO(3) / S^2 transform state (see contract_tc.cu).
 #pragma once
 #include <cuda_runtime.h>
 #include <string>
@@ -12,7 +12,7 @@ namespace fftso3 {
 struct TCState;
 
 int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64, const std::vector<long long>& goff,
-              long long table_elems, const double* d_tw, const double* d_w, bool refine, bool real,
+              long long table_elems, const double* d_tw, const double* d_w, bool refine, bool real, bool s2,
               std::string& err);
 void tc_destroy(TCState* s);
 long long tc_device_bytes(const TCState* s);

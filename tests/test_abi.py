@@ -58,7 +58,7 @@ def test_sizes(gblib):
     ((0, 5, 1, 7, 0, 0), "precision"),
     ((0, 5, 1, 0, 3, 0), "recursion"),
     ((0, 5, 1, 0, 0, 0x10), "flag"),
-    ((2, 5, 1, 1, 0, 0), "tensor-core"),
+    ((2, 600, 1, 1, 0, 0), "tensor-core"),
 ])
 def test_plan_create_rejects_bad_arguments(gblib, args, msg):
     h = ctypes.c_void_p()
