@@ -126,15 +126,24 @@ def measured_peaks() -> dict:
 
 
 def profiled_traffic(stage: str, l_max: int, batch: int):
-    """dram bytes per launch of `stage` from the committed ncu summary, scaled
-    to this workload (lines 'traffic <stage> l_max=<L> batch=<b> bytes=<n>')."""
+    """DRAM bytes per launch of `stage` from the committed ncu summary
+    (lines 'traffic <stage> l_max=<L> batch=<b> bytes=<n>'), scaled to this
+    workload: by batch at the same l_max, and for the FFT passes (whose
+    traffic is one read and one write of every sample) by batch * N^3 across l_max."""
     path = os.path.join(ROOT, "profiles", "traffic.md")
     if not os.path.exists(path):
         return None
+    found = []
     for line in open(path):
         m = re.match(r"\s*traffic\s+(\S+)\s+l_max=(\d+)\s+batch=(\d+)\s+bytes=(\d+)", line)
-        if m and m.group(1) == stage and int(m.group(2)) == l_max:
-            return int(m.group(4)) * batch / int(m.group(3))
+        if m and m.group(1) == stage:
+            found.append((int(m.group(2)), int(m.group(3)), int(m.group(4))))
+    for L0, b0, byts in found:
+        if L0 == l_max:
+            return byts * batch / b0
+    for L0, b0, byts in found:
+        if stage.startswith("fft"):
+            return byts * batch / b0 * ((l_max + 1) / (L0 + 1)) ** 3
     return None
 
 
@@ -348,6 +357,126 @@ def main_uneven(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+# --------------------------------------------------------------- S^2 batch
+
+S2_METRIC = "S2 real fwd+inv transforms/s, 512 signals at l_max=511: TC split-BF16 vs FP64"
+
+
+def main_s2(args) -> None:
+    """512 real S^2 signals at l_max = 511 (1024 x 1024 grids, FP32 samples,
+    coefficients N(0,1)/(l+1)) through one FFTS2_real tensor-core plan."""
+    import torch
+
+    from fftso3_gb300 import _lib
+    from fftso3_gb300 import build as fbuild
+
+    fbuild.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    L, b = 511, args.functions if args.functions != 4096 else 512
+    B, N = L + 1, 2 * (L + 1)
+    C = B * B
+    plan = _lib.Plan(_lib.S2_REAL, L, b, "tc_bf16x3", "reference")
+    deg = torch.from_numpy(np.concatenate([np.full(2 * l + 1, l) for l in range(B)])).to(dev)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(21)
+    coef = (torch.randn(b, C, generator=gen, device=dev, dtype=torch.float64) / (deg.double() + 1.0)).float()
+    grid = torch.empty(b * N * N, dtype=torch.float32, device=dev)
+    plan.inverse(coef.data_ptr(), grid.data_ptr(), sp)
+    grid_out = torch.empty_like(grid)
+    coef_out = torch.empty_like(coef)
+    torch.cuda.synchronize()
+    plan.check()
+
+    # accuracy of signal 0 against the FP64 plan (same FP32-rounded coefficients and samples)
+    p64 = _lib.Plan(_lib.S2_REAL, L, 1, "fp64", "reference")
+    c0 = coef[0].double().contiguous()
+    g64 = torch.empty(N * N, dtype=torch.float64, device=dev)
+    p64.inverse(c0.data_ptr(), g64.data_ptr(), sp)
+    F64 = torch.empty(C, dtype=torch.float64, device=dev)
+    g0 = grid[:N * N].double().contiguous()
+    p64.forward(g0.data_ptr(), F64.data_ptr(), sp)
+    plan.inverse(coef.data_ptr(), grid_out.data_ptr(), sp)
+    plan.forward(grid.data_ptr(), coef_out.data_ptr(), sp)
+    torch.cuda.synchronize()
+    plan.check()
+    acc = {"forward_rel_rms": float(torch.linalg.norm(coef_out[0].double() - F64) / torch.linalg.norm(F64)),
+           "inverse_rel_rms": float(torch.linalg.norm(grid_out[:N * N].double() - g64) / torch.linalg.norm(g64)),
+           "against": "FP64 plan (FFTS2_real, FP64) on signal 0"}
+
+    # FP64 path rate (batch 16, per signal)
+    b64 = 16
+    p64b = _lib.Plan(_lib.S2_REAL, L, b64, "fp64", "reference")
+    cb = coef[:b64].double().contiguous()
+    gb = torch.empty(b64 * N * N, dtype=torch.float64, device=dev)
+    ob = torch.empty_like(cb)
+    p64b.inverse(cb.data_ptr(), gb.data_ptr(), sp)
+    p64b.forward(gb.data_ptr(), ob.data_ptr(), sp)
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    f0.record(stream)
+    p64b.inverse(cb.data_ptr(), gb.data_ptr(), sp)
+    p64b.forward(gb.data_ptr(), ob.data_ptr(), sp)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    fp64 = {"value": b64 * 1000.0 / f0.elapsed_time(f1), "unit": UNIT, "batch": b64,
+            "note": "plain FP64 GPU path (FFTS2_real, FP64), same l_max"}
+    del p64b, cb, gb, ob
+
+    for _ in range(args.warmup):
+        plan.inverse(coef.data_ptr(), grid_out.data_ptr(), sp)
+        plan.forward(grid.data_ptr(), coef_out.data_ptr(), sp)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            plan.inverse(coef.data_ptr(), grid_out.data_ptr(), sp)
+            plan.forward(grid.data_ptr(), coef_out.data_ptr(), sp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    clocks = clk.summary()
+    plan.set_timing(True)
+    plan.stage_times(reset=True)
+    plan.inverse(coef.data_ptr(), grid_out.data_ptr(), sp)
+    plan.forward(grid.data_ptr(), coef_out.data_ptr(), sp)
+    torch.cuda.synchronize()
+    stages = plan.stage_times(reset=True)
+    plan.set_timing(False)
+    plan.check()
+    peaks = measured_peaks()
+    flops = 4.0 * N * B * B * b  # useful flops per direction (pairs m, -m; re/im)
+    gemm = {}
+    for name in ("tc_gemm_fwd", "tc_gemm_inv"):
+        if name in stages:
+            t = stages[name][0] / stages[name][1] / 1000.0
+            gemm[name] = {"ms": t * 1000.0, "tflops": flops / t / 1e12,
+                          "frac_of_bf16": flops / t / 1e12 / peaks["bf16_tflops_sustained"]}
+    fft_bytes = 4.0 * b * N * N + 8.0 * b * N * N  # real samples + complex pencils, one pass
+    fft = {}
+    for name in ("fft_rows",):
+        if name in stages:
+            t = stages[name][0] / stages[name][1] / 1000.0
+            fft[name] = {"ms": t * 1000.0, "gbs": fft_bytes / t / 1e9, "frac_of_hbm": fft_bytes / t / 1e9 / peaks["hbm_gbs"]}
+    value = b * 1000.0 / ms
+    line = {
+        "metric": S2_METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16x3 (split) / fp32 accumulate / fp32 FFT; fp32 samples", "data": "synthetic",
+        "config": {"workload": f"{b} real S^2 signals, l_max={L} ({N}x{N} grid, FP32 samples), coefficients "
+                               "N(0,1)/(l+1); FFTS2_real tensor-core plan", "signals": b, "l_max": L,
+                   "l2": "inputs larger than L2 (2 GB of samples)"},
+        "accuracy": acc, "fp64_path": fp64, "speedup_vs_fp64_path": value / fp64["value"],
+        "gemm": gemm, "fft": fft,
+        "stages": {k: {"ms": v, "launches": c} for k, (v, c) in stages.items()},
+        "gpu_launches": int(sum(c for _, c in stages.values())) * args.steps, "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
 # --------------------------------------------------------------- GPU arm
 
 def main() -> None:
@@ -362,8 +491,9 @@ def main() -> None:
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64 reference (profiling runs)")
-    ap.add_argument("--workload", default="lmax255", choices=["lmax255", "uneven"],
-                    help="lmax255: the headline batch at one l_max; uneven: the mixed-bandwidth batch")
+    ap.add_argument("--workload", default="lmax255", choices=["lmax255", "uneven", "s2"],
+                    help="lmax255: the headline SO(3) batch at one l_max (--l-max/--batch); uneven: the "
+                         "mixed-bandwidth SO(3) batch; s2: the S^2 batch at l_max=511")
     ap.add_argument("--functions", type=int, default=4096, help="uneven workload: number of functions")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -371,6 +501,9 @@ def main() -> None:
         return
     if args.workload == "uneven":
         main_uneven(args)
+        return
+    if args.workload == "s2":
+        main_s2(args)
         return
 
     import torch
@@ -515,20 +648,13 @@ def main() -> None:
     per_launch_s = tot_ms / cnt / 1000.0
     useful_flops = 8.0 * B * C * b            # complex beta-sum flops per direction for the batch
     grid_bytes = 8.0 * b * N ** 3             # one complex64 pass over the batch's grids
-    Kp = (N + 63) // 64 * 64
-    KLp = (B + 63) // 64 * 64
-    ncols = (8 * b + 127) // 128 * 128
     if name.startswith("tc_gemm"):
         achieved = useful_flops / per_launch_s / 1e12
         peak = peaks["bf16_tflops_sustained"]
         roof = {"bound": "tensor", "unit": "TFLOP/s", "algorithmic": "8*B*C*batch useful flops per launch"}
     else:
-        if name.startswith("fft"):
-            byts = 2 * grid_bytes
-        elif name == "tc_pack_fwd":
-            byts = grid_bytes + 6.0 * B * B * ncols * Kp
-        elif name == "tc_pack_inv":
-            byts = 8.0 * C * b + 6.0 * B * B * ncols * KLp
+        if name.startswith("fft") or name.startswith("tc_pack"):
+            byts = 2 * grid_bytes  # one complex64 read and write of the batch's grids (FFT pass / transpose)
         else:
             byts = grid_bytes
         achieved = byts / per_launch_s / 1e9
@@ -573,8 +699,9 @@ def main() -> None:
         cpu.pop("seconds", None)
 
     if rank == 0:
+        metric = METRIC if L == 255 else METRIC.replace("l_max=255", f"l_max={L}")
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "metric": metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "bf16x3 (split) / fp32 accumulate / fp32 FFT", "data": "synthetic",
             "config": {"workload": f"SO(3) complex forward+inverse, l_max={L}, batch={b} functions per GPU "

@@ -351,51 +351,57 @@ __global__ void zero_nyquist_s2_kernel(C* __restrict__ H, int N, long long nrows
     H[r * N + N / 2] = z;
 }
 
-// F_r(l) = Re(conj(T(l)) F_c(l)) (fdcl_FFTS2.cpp:424-436).
-template <typename CIN, typename ROUT>
+// degree l of packed S^2 index i = l^2 + l + m (integer fix-up of a float square root)
+__device__ __forceinline__ int s2_degree(long long i)
+{
+    int l = (int)sqrtf((float)i);
+    while ((long long)l * l > i) --l;
+    while ((long long)(l + 1) * (l + 1) <= i) ++l;
+    return l;
+}
+
+// F_r(l) = Re(conj(T(l)) F_c(l)) (fdcl_FFTS2.cpp:424-436), arithmetic in A
+// (double for the FP64 path, float for the tensor-core path).
+template <typename CIN, typename ROUT, typename A>
 __global__ void s2_c2r_kernel(const CIN* __restrict__ Fc, ROUT* __restrict__ Fr, int L, long long cstride)
 {
     const int b = blockIdx.y;
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long C = (long long)(L + 1) * (L + 1);
     if (i >= C) return;
-    int l = (int)floor(sqrt((double)i));
-    while ((long long)l * l > i) --l;
-    while ((long long)(l + 1) * (l + 1) <= i) ++l;
-    int m = (int)(i - (long long)l * l) - l;
+    const int l = s2_degree(i);
+    const int m = (int)(i - (long long)l * l) - l;
     const CIN* fc = Fc + (long long)b * cstride;
     int cs[2] = {-m, m};
     if (m > 0) { cs[0] = -m; cs[1] = m; } else if (m < 0) { cs[0] = m; cs[1] = -m; }
-    int nc = (m == 0) ? 1 : 2;
-    double acc = 0.;
+    const int nc = (m == 0) ? 1 : 2;
+    A acc = 0;
     for (int j = 0; j < nc; ++j) {
-        double2 t = conj2(tmat(m, cs[j]));
-        CIN v = fc[s2_idx(l, cs[j])];
-        acc += t.x * (double)v.x - t.y * (double)v.y;
+        const c2t<A> t = conj_t(tmat_t<A>(m, cs[j]));
+        const CIN v = fc[s2_idx(l, cs[j])];
+        acc += t.x * (A)v.x - t.y * (A)v.y;
     }
     Fr[(long long)b * cstride + i] = (ROUT)acc;
 }
 
 // F_c = T^T F_r: the complex coefficients whose synthesis is the real-basis
 // synthesis sum F_r(l,m) y(l,m), y = T Y (fdcl_FFTS2.cpp:383-422).
-template <typename RIN, typename COUT>
+template <typename RIN, typename COUT, typename A>
 __global__ void s2_r2c_kernel(const RIN* __restrict__ Fr, COUT* __restrict__ Fc, int L, long long cstride)
 {
     const int b = blockIdx.y;
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long C = (long long)(L + 1) * (L + 1);
     if (i >= C) return;
-    int l = (int)floor(sqrt((double)i));
-    while ((long long)l * l > i) --l;
-    while ((long long)(l + 1) * (l + 1) <= i) ++l;
-    int c = (int)(i - (long long)l * l) - l;
+    const int l = s2_degree(i);
+    const int c = (int)(i - (long long)l * l) - l;
     const RIN* fr = Fr + (long long)b * cstride;
-    int as[2] = {c, -c};
-    int na = (c == 0) ? 1 : 2;
-    double2 acc = make_double2(0., 0.);
+    const int as[2] = {c, -c};
+    const int na = (c == 0) ? 1 : 2;
+    c2t<A> acc = {(A)0, (A)0};
     for (int j = 0; j < na; ++j) {
-        double2 t = tmat(as[j], c);
-        double v = (double)fr[s2_idx(l, as[j])];
+        const c2t<A> t = tmat_t<A>(as[j], c);
+        const A v = (A)fr[s2_idx(l, as[j])];
         acc.x += t.x * v;
         acc.y += t.y * v;
     }
@@ -498,9 +504,9 @@ cudaError_t launch_s2_c2r(const void* Fc, void* Fr, bool fp64, int L, int batch,
     long long C = (long long)(L + 1) * (L + 1);
     dim3 grid((unsigned)((C + 255) / 256), batch);
     if (fp64)
-        s2_c2r_kernel<double2, double><<<grid, 256, 0, st>>>((const double2*)Fc, (double*)Fr, L, C);
+        s2_c2r_kernel<double2, double, double><<<grid, 256, 0, st>>>((const double2*)Fc, (double*)Fr, L, C);
     else
-        s2_c2r_kernel<float2, float><<<grid, 256, 0, st>>>((const float2*)Fc, (float*)Fr, L, C);
+        s2_c2r_kernel<float2, float, float><<<grid, 256, 0, st>>>((const float2*)Fc, (float*)Fr, L, C);
     return cudaGetLastError();
 }
 
@@ -509,9 +515,9 @@ cudaError_t launch_s2_r2c(const void* Fr, void* Fc, bool fp64, int L, int batch,
     long long C = (long long)(L + 1) * (L + 1);
     dim3 grid((unsigned)((C + 255) / 256), batch);
     if (fp64)
-        s2_r2c_kernel<double, double2><<<grid, 256, 0, st>>>((const double*)Fr, (double2*)Fc, L, C);
+        s2_r2c_kernel<double, double2, double><<<grid, 256, 0, st>>>((const double*)Fr, (double2*)Fc, L, C);
     else
-        s2_r2c_kernel<float, float2><<<grid, 256, 0, st>>>((const float*)Fr, (float2*)Fc, L, C);
+        s2_r2c_kernel<float, float2, float><<<grid, 256, 0, st>>>((const float*)Fr, (float2*)Fc, L, C);
     return cudaGetLastError();
 }
 
