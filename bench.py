@@ -228,7 +228,7 @@ def main_uneven(args) -> None:
     n = args.functions
     lmax = uneven_lmax(n)
     t_create = time.perf_counter()
-    bt = _lib.Batch(_lib.SO3_REAL, lmax, "tc_bf16x3", "reference", _lib.FLAG_GRAPH)
+    bt = _lib.Batch(_lib.SO3_REAL, lmax, "tc_bf16x3", "reference", _lib.FLAG_GRAPH | _lib.FLAG_AUTOTUNE)
     t_create = time.perf_counter() - t_create
     G, Ctot = bt.grid_elems, bt.coeff_elems
     # seeded coefficients N(0,1)/(2l+1), generated on the device per function
@@ -343,8 +343,10 @@ def main_uneven(args) -> None:
         "vs_baseline": None, "dtype": "bf16x3 (split) / fp32 accumulate / fp32 FFT; fp32 samples",
         "data": "synthetic",
         "config": {"workload": f"{n} real SO(3) functions, l_max uniform in 8..64 (seed 3), coefficients "
-                               "N(0,1)/(2l+1), FP32 samples; fftso3_batch, tensor-core buckets, CUDA graph",
-                   "functions": n, "buckets": bt.buckets, "samples": int(G), "coefficients": int(Ctot),
+                               "N(0,1)/(2l+1), FP32 samples; fftso3_batch, tensor-core buckets, CUDA graph, "
+                               "autotuned",
+                   "functions": n, "buckets": bt.buckets, "streams": bt.streams, "samples": int(G),
+                   "coefficients": int(Ctot), "autotune": "FFT launch shapes per N, bucket streams",
                    "l2": "inputs larger than L2"},
         "io_gbs": io_bytes / (ms / 1000.0) / 1e9, "io_frac_of_hbm": io_bytes / (ms / 1000.0) / 1e9 / peaks["hbm_gbs"],
         "batch_create_s": t_create, "device_gb": bt.device_bytes / 1e9,
@@ -567,7 +569,7 @@ def main() -> None:
     torch.cuda.empty_cache()
 
     # ---- tensor-core plan
-    plan = _lib.Plan(_lib.SO3_COMPLEX, L, b, "tc_bf16x3", "stable")
+    plan = _lib.Plan(_lib.SO3_COMPLEX, L, b, "tc_bf16x3", "stable", _lib.FLAG_AUTOTUNE)
     Fb = np.concatenate([seeded_coeffs(L, 1000 * rank + i) for i in range(b)]).astype(np.complex64)
     coef = torch.from_numpy(Fb).to(dev)
     grid = torch.empty(b * N ** 3, dtype=torch.complex64, device=dev)

@@ -32,6 +32,7 @@ RECURSION_STABLE = 1
 
 FLAG_REFINE = 0x1
 FLAG_GRAPH = 0x2
+FLAG_AUTOTUNE = 0x4
 
 PRECISIONS = {"fp64": PREC_FP64, "tc_bf16x3": PREC_TC_BF16X3}
 RECURSIONS = {"reference": RECURSION_REFERENCE, "stable": RECURSION_STABLE}
@@ -68,6 +69,7 @@ SIGNATURES = {
     "fftso3_batch_grid_offset": (_ll, [_vp, _i]),
     "fftso3_batch_coeff_offset": (_ll, [_vp, _i]),
     "fftso3_batch_bucket_count": (_i, [_vp]),
+    "fftso3_batch_stream_count": (_i, [_vp]),
     "fftso3_batch_device_bytes": (_ll, [_vp]),
     "fftso3_batch_forward": (_i, [_vp, _vp, _vp, _vp]),
     "fftso3_batch_inverse": (_i, [_vp, _vp, _vp, _vp]),
@@ -223,6 +225,10 @@ class Batch:
     @property
     def buckets(self) -> int:
         return int(lib().fftso3_batch_bucket_count(self._h))
+
+    @property
+    def streams(self) -> int:
+        return int(lib().fftso3_batch_stream_count(self._h))
 
     @property
     def device_bytes(self) -> int:

@@ -304,7 +304,8 @@ int fftso3_plan_create(fftso3_plan** out, int kind, int l_max, int batch, int pr
         return fail(FFTSO3_ERR_INVALID_ARG, "unknown precision");
     if (recursion != FFTSO3_RECURSION_REFERENCE && recursion != FFTSO3_RECURSION_STABLE)
         return fail(FFTSO3_ERR_INVALID_ARG, "unknown recursion mode");
-    if ((flags & ~FFTSO3_FLAG_REFINE) != 0) return fail(FFTSO3_ERR_INVALID_ARG, "unknown flag bits");
+    if ((flags & ~(FFTSO3_FLAG_REFINE | FFTSO3_FLAG_AUTOTUNE)) != 0)
+        return fail(FFTSO3_ERR_INVALID_ARG, "unknown flag bits");
     if (is_so3(kind) && l_max > 511) return fail(FFTSO3_ERR_UNSUPPORTED, "SO(3) l_max above 511 is not supported");
     if (!is_so3(kind) && l_max > 2047) return fail(FFTSO3_ERR_UNSUPPORTED, "S^2 l_max above 2047 is not supported");
     if (precision == FFTSO3_PREC_TC_BF16X3 && l_max > 511)
@@ -414,7 +415,8 @@ int fftso3_plan_create(fftso3_plan** out, int kind, int l_max, int batch, int pr
     } else {
         std::string err;
         rc = tc_create(&p->tc, p->L, p->N, batch, p->d_table, goff, p->table_elems, p->d_tw, p->d_w,
-                       (flags & FFTSO3_FLAG_REFINE) != 0, p->real, !p->so3, err);
+                       (flags & FFTSO3_FLAG_REFINE) != 0, p->real, !p->so3, (flags & FFTSO3_FLAG_AUTOTUNE) != 0,
+                       err);
         if (rc) {
             g_err = err;
             return bail(rc);

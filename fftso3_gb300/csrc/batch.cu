@@ -73,6 +73,8 @@ struct fftso3_batch {
     } graphs[2];
     long long bytes = 0;
     bool timing = false;                         // per-stage timing (eager launches, no graph)
+    bool tuned = false;                          // stream count chosen (FFTSO3_FLAG_AUTOTUNE)
+    int nstreams_used = 0;
 };
 
 namespace {
@@ -100,6 +102,61 @@ int check_batch(const fftso3_batch* b)
         cudaError_t e = cudaSetDevice(b->device);
         if (e != cudaSuccess) return bcuda(e, "cudaSetDevice");
     }
+    return FFTSO3_SUCCESS;
+}
+
+// buckets to ns streams: longest work first, each to the least-loaded stream
+void assign_streams(fftso3_batch* b, int ns)
+{
+    std::vector<double> load(ns, 0.0);
+    std::vector<int> byc(b->buckets.size());
+    std::iota(byc.begin(), byc.end(), 0);
+    std::stable_sort(byc.begin(), byc.end(),
+                     [&](int a, int c) { return b->buckets[a].cost > b->buckets[c].cost; });
+    for (int i : byc) {
+        const int s = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        b->buckets[i].stream = s;
+        load[s] += b->buckets[i].cost;
+    }
+    b->nstreams_used = ns;
+}
+
+int launch_all(fftso3_batch* b, int dir, const void* in, void* out, cudaStream_t st);
+
+// FFTSO3_FLAG_AUTOTUNE: time 1, 2, 4, 8 bucket streams on this call's own
+// buffers (one warm-up and one timed eager run each; the real call follows and
+// overwrites the output) and keep the fastest.
+int tune_streams(fftso3_batch* b, int dir, const void* in, void* out, cudaStream_t st)
+{
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    int bestn = (int)b->streams.size();
+    for (int ns = 1; ns <= (int)b->streams.size(); ns *= 2) {
+        assign_streams(b, ns);
+        int rc = launch_all(b, dir, in, out, st);
+        if (!rc) {
+            cudaEventRecord(e0, st);
+            rc = launch_all(b, dir, in, out, st);
+            cudaEventRecord(e1, st);
+        }
+        if (rc || cudaEventSynchronize(e1) != cudaSuccess) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return rc ? rc : bcuda(cudaGetLastError(), "autotune");
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) {
+            best = ms;
+            bestn = ns;
+        }
+    }
+    assign_streams(b, bestn);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->tuned = true;
     return FFTSO3_SUCCESS;
 }
 
@@ -133,6 +190,8 @@ int run(fftso3_batch* b, int dir, const void* in, void* out, void* stream)
     if (rc) return rc;
     if (!in || !out) return bfail(FFTSO3_ERR_INVALID_ARG, "input/output pointer is NULL");
     cudaStream_t st = (cudaStream_t)stream;
+    if ((b->flags & FFTSO3_FLAG_AUTOTUNE) && !b->tuned && !b->timing)
+        if ((rc = tune_streams(b, dir, in, out, st))) return rc;
     if (!(b->flags & FFTSO3_FLAG_GRAPH) || b->timing) return launch_all(b, dir, in, out, st);
 
     auto& g = b->graphs[dir];
@@ -177,7 +236,7 @@ int fftso3_batch_create(fftso3_batch** out, int kind, const int* l_max, int n_fu
     *out = nullptr;
     if (!l_max) return bfail(FFTSO3_ERR_INVALID_ARG, "l_max array is NULL");
     if (n_functions < 1) return bfail(FFTSO3_ERR_INVALID_ARG, "n_functions must be >= 1");
-    if ((flags & ~(FFTSO3_FLAG_REFINE | FFTSO3_FLAG_GRAPH)) != 0)
+    if ((flags & ~(FFTSO3_FLAG_REFINE | FFTSO3_FLAG_GRAPH | FFTSO3_FLAG_AUTOTUNE)) != 0)
         return bfail(FFTSO3_ERR_INVALID_ARG, "unknown flag bits");
     if (kind < FFTSO3_SO3_COMPLEX || kind > FFTSO3_S2_REAL)
         return bfail(FFTSO3_ERR_INVALID_ARG, "unknown transform kind");
@@ -230,7 +289,8 @@ int fftso3_batch_create(fftso3_batch** out, int kind, const int* l_max, int n_fu
 
     // one plan per bucket
     for (auto& k : b->buckets) {
-        int rc = fftso3_plan_create(&k.plan, kind, k.L, k.count, precision, recursion, flags & FFTSO3_FLAG_REFINE);
+        int rc = fftso3_plan_create(&k.plan, kind, k.L, k.count, precision, recursion,
+                                    flags & (FFTSO3_FLAG_REFINE | FFTSO3_FLAG_AUTOTUNE));
         if (rc) {
             k.plan = nullptr;
             std::string m = fftso3_last_error_string();
@@ -244,15 +304,7 @@ int fftso3_batch_create(fftso3_batch** out, int kind, const int* l_max, int n_fu
 
     // streams: longest bucket first, each to the least-loaded stream
     const int ns = std::min<int>(MAX_STREAMS, (int)b->buckets.size());
-    std::vector<double> load(ns, 0.0);
-    std::vector<int> byc(b->buckets.size());
-    std::iota(byc.begin(), byc.end(), 0);
-    std::stable_sort(byc.begin(), byc.end(), [&](int a, int c2) { return b->buckets[a].cost > b->buckets[c2].cost; });
-    for (int i : byc) {
-        int s = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-        b->buckets[i].stream = s;
-        load[s] += b->buckets[i].cost;
-    }
+    assign_streams(b, ns);
     cudaError_t e;
     b->streams.assign(ns, nullptr);
     b->joined.assign(ns, nullptr);
@@ -296,6 +348,8 @@ long long fftso3_batch_coeff_offset(const fftso3_batch* b, int fn)
 }
 
 int fftso3_batch_bucket_count(const fftso3_batch* b) { return b ? (int)b->buckets.size() : -1; }
+
+int fftso3_batch_stream_count(const fftso3_batch* b) { return b ? b->nstreams_used : -1; }
 
 long long fftso3_batch_device_bytes(const fftso3_batch* b) { return b ? b->bytes : -1; }
 

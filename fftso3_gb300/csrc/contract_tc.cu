@@ -35,6 +35,9 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "../../include/fftso3_gb300.h"
@@ -761,6 +764,8 @@ struct TCState {
     bool refine = false;
     bool real = false;            // real grids (FFTSO3_*_REAL): real samples in, real part out
     bool s2 = false;              // S^2 (Legendre groups g = m, grids N^2) instead of SO(3)
+    int lpb[2] = {0, 0};          // generic-N FFT lines per CTA (rows, cols); 0 = heuristic
+    int thr[2] = {256, 256};      // generic-N FFT threads per CTA (rows, cols)
     FFTFactors fac;
     const double* d_tw = nullptr;
     float* d_wf = nullptr;
@@ -844,9 +849,11 @@ void tc_destroy(TCState* s)
 
 long long tc_device_bytes(const TCState* s) { return s ? s->bytes : 0; }
 
+static int autotune_fft(TCState* s, std::string& err);
+
 int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64, const std::vector<long long>& goff,
               long long table_elems, const double* d_tw, const double* d_w, bool refine, bool real, bool s2,
-              std::string& err)
+              bool autotune, std::string& err)
 {
     *out = nullptr;
     if (N > MAXN) {
@@ -963,6 +970,8 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
         err = std::string("tensor-core kernel attributes: ") + cudaGetErrorString(e);
         return bail(FFTSO3_ERR_CUDA);
     }
+    if (autotune && !fft_fast_supported(N))
+        if ((rc = autotune_fft(s, err))) return bail(rc);
     *out = s;
     return FFTSO3_SUCCESS;
 }
@@ -983,8 +992,9 @@ static FFTLaunch fft_launch(const TCState* s, const void* in, void* out, bool co
     // lines per CTA: about 2048 elements per CTA (small N would otherwise leave most threads idle)
     int lpb = 1;
     while (lpb < 256 && (lpb * 2) * N <= 2048 && fft_smem_bytes(N, lpb * 2, false) <= 100 * 1024) lpb *= 2;
+    L.threads = s->thr[cols ? 1 : 0];
     if (!cols) {
-        L.lpb = lpb;
+        L.lpb = s->lpb[0] ? s->lpb[0] : lpb;
         L.inner = 1;
         L.ostride = N;
         L.istride = 0;
@@ -993,6 +1003,7 @@ static FFTLaunch fft_launch(const TCState* s, const void* in, void* out, bool co
     } else {
         L.lpb = lpb < 16 ? 16 : lpb;  // >= 16 adjacent lines: 128-byte segments
         while (L.lpb > 1 && fft_smem_bytes(N, L.lpb, false) > 100 * 1024) L.lpb /= 2;
+        if (s->lpb[1]) L.lpb = s->lpb[1];
         L.inner = N;
         L.ostride = (long long)N * N;
         L.istride = 1;
@@ -1000,6 +1011,90 @@ static FFTLaunch fft_launch(const TCState* s, const void* in, void* out, bool co
         L.lines_fastest = true;
     }
     return L;
+}
+
+// ---- autotuner of the generic-N FFT launch shape (lines per CTA, threads per CTA)
+//
+// For N that the register FFT does not cover, the best lines-per-CTA and CTA
+// size depend on N (its factors, the shared memory per line) and on the pass
+// (rows: lines contiguous; columns: lines adjacent).  With FFTSO3_FLAG_AUTOTUNE
+// the plan times every candidate on its own workspace (about 32 M samples,
+// one warm-up and three timed launches each, CUDA events) and keeps the
+// fastest; choices are cached per (N, pass, real input/output) for the process,
+// so the many plans of an uneven batch tune each N once.
+struct TuneKey {
+    int N, cols, real_in, real_out;
+    bool operator<(const TuneKey& o) const
+    {
+        return std::tie(N, cols, real_in, real_out) < std::tie(o.N, o.cols, o.real_in, o.real_out);
+    }
+};
+static std::mutex g_tune_mutex;
+static std::map<TuneKey, std::pair<int, int>> g_tune_cache;
+
+static int autotune_fft(TCState* s, std::string& err)
+{
+    const int N = s->N;
+    cudaStream_t st;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+        err = "autotune: cudaStreamCreate";
+        return FFTSO3_ERR_CUDA;
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const size_t gridel = (size_t)s->batch * N * N * (s->s2 ? 1 : N);
+    cudaMemsetAsync(s->d_work, 0, sizeof(float2) * gridel, st);
+    cudaMemsetAsync(s->d_pencil, 0, sizeof(float2) * gridel, st);
+    const int npass = s->s2 ? 1 : 2;
+    int rc = FFTSO3_SUCCESS;
+    for (int cols = 0; cols < npass && rc == FFTSO3_SUCCESS; ++cols) {
+        const TuneKey key{N, cols, (!cols && s->real) ? 1 : 0, 0};
+        {
+            std::lock_guard<std::mutex> lk(g_tune_mutex);
+            auto it = g_tune_cache.find(key);
+            if (it != g_tune_cache.end()) {
+                s->lpb[cols] = it->second.first;
+                s->thr[cols] = it->second.second;
+                continue;
+            }
+        }
+        float best = 1e30f;
+        int blpb = 0, bthr = 256;
+        for (int thr = 128; thr <= 256; thr *= 2) {
+            for (int lpb = cols ? 4 : 1; lpb <= 256; lpb *= 2) {
+                if ((long long)lpb * N > 8192 || fft_smem_bytes(N, lpb, false) > 100 * 1024) break;
+                s->lpb[cols] = lpb;
+                s->thr[cols] = thr;
+                FFTLaunch L = fft_launch(s, s->d_pencil, s->d_work, cols != 0, key.real_in != 0, false);
+                L.nlines = std::min<long long>(L.nlines, (32LL << 20) / N / lpb * lpb + lpb);
+                if (launch_fft_lines(L, st) != cudaSuccess) continue;
+                cudaEventRecord(e0, st);
+                for (int r = 0; r < 3; ++r) launch_fft_lines(L, st);
+                cudaEventRecord(e1, st);
+                if (cudaEventSynchronize(e1) != cudaSuccess) {
+                    err = std::string("autotune: ") + cudaGetErrorString(cudaGetLastError());
+                    rc = FFTSO3_ERR_CUDA;
+                    break;
+                }
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (ms < best) {
+                    best = ms;
+                    blpb = lpb;
+                    bthr = thr;
+                }
+            }
+        }
+        s->lpb[cols] = blpb;
+        s->thr[cols] = bthr;
+        std::lock_guard<std::mutex> lk(g_tune_mutex);
+        g_tune_cache[key] = {blpb, bthr};
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamDestroy(st);
+    return rc;
 }
 
 #define TCK(call)                                                          \

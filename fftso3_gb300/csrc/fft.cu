@@ -203,13 +203,13 @@ __device__ void stockham_generic(const typename V2<T>::t* __restrict__ src, type
 //   X[R - q] = x_0 + sum_{t<=P} a_t cos(2 pi t q / R) + i b_t sin(2 pi t q / R)
 // which takes about R real FMAs per output instead of 4R.  The (cos, sin)
 // matrix of the R-point DFT, mat[(t-1) P4 + (q-1)], is built per CTA in shared
-// memory.  Each thread forms the outputs q and R - q of GP consecutive q
-// (two 16-byte matrix reads per term); work items run (j, line) fastest, so
-// the lanes of a warp share one block of q and every matrix read is a
-// broadcast.
-template <typename T>
-__device__ void dft_prime_first(const typename V2<T>::t* __restrict__ src, typename V2<T>::t* __restrict__ dst,
-                                const typename V2<T>::t* __restrict__ mat, int N, int R, int lpb, int LS)
+// memory.  Each thread forms the outputs q and R - q of GP consecutive q for
+// LPT lines (l and l + lpb/2 when lpb >= 2), so one matrix read feeds
+// 4 LPT FMAs; work items run (j, line) fastest, so the lanes of a warp share
+// one block of q and every matrix read is a broadcast.
+template <typename T, int LPT>
+__device__ void dft_prime_first_t(const typename V2<T>::t* __restrict__ src, typename V2<T>::t* __restrict__ dst,
+                                  const typename V2<T>::t* __restrict__ mat, int N, int R, int lpb, int LS)
 {
     using C = typename V2<T>::t;
     constexpr int GP = 4;
@@ -217,46 +217,72 @@ __device__ void dft_prime_first(const typename V2<T>::t* __restrict__ src, typen
     const int P = (R - 1) / 2;
     const int P4 = (P + GP - 1) / GP * GP;
     const int nblk = P4 / GP;
-    const int per_blk = Nr * lpb;
+    const int lgroups = lpb / LPT;               // line l and l + lgroups share each matrix read
+    const int per_blk = Nr * lgroups;
     const int total = per_blk * nblk;
     for (int b = threadIdx.x; b < total; b += blockDim.x) {
         const int blk = b / per_blk, rem = b - blk * per_blk;
         const int l = rem / Nr, j = rem - l * Nr;
-        const C* s = src + l * LS + j;
-        const C x0 = s[0];
-        C acc0 = x0;
-        C Cs[GP], Ss[GP];
+        const C* s[LPT];
+        C x0[LPT], acc0[LPT], Cs[LPT][GP], Ss[LPT][GP];
 #pragma unroll
-        for (int u = 0; u < GP; ++u) {
-            Cs[u] = V2<T>::mk((T)0, (T)0);
-            Ss[u] = V2<T>::mk((T)0, (T)0);
+        for (int u = 0; u < LPT; ++u) {
+            s[u] = src + (l + u * lgroups) * LS + j;
+            x0[u] = s[u][0];
+            acc0[u] = x0[u];
+#pragma unroll
+            for (int g = 0; g < GP; ++g) {
+                Cs[u][g] = V2<T>::mk((T)0, (T)0);
+                Ss[u][g] = V2<T>::mk((T)0, (T)0);
+            }
         }
         const C* m = mat + blk * GP;
         for (int t = 1; t <= P; ++t, m += P4) {
-            const C xt = s[t * Nr], xr = s[(R - t) * Nr];
-            const C a = cadd(xt, xr), bb = csub(xt, xr);
-            acc0 = cadd(acc0, a);
+            C a[LPT], bb[LPT];
 #pragma unroll
-            for (int u = 0; u < GP; ++u) {
-                const C cs = m[u];  // (cos, sin)
-                Cs[u].x += a.x * cs.x;
-                Cs[u].y += a.y * cs.x;
-                Ss[u].x += bb.x * cs.y;
-                Ss[u].y += bb.y * cs.y;
+            for (int u = 0; u < LPT; ++u) {
+                const C xt = s[u][t * Nr], xr = s[u][(R - t) * Nr];
+                a[u] = cadd(xt, xr);
+                bb[u] = csub(xt, xr);
+                acc0[u] = cadd(acc0[u], a[u]);
+            }
+#pragma unroll
+            for (int g = 0; g < GP; ++g) {
+                const C cs = m[g];  // (cos, sin)
+#pragma unroll
+                for (int u = 0; u < LPT; ++u) {
+                    Cs[u][g].x += a[u].x * cs.x;
+                    Cs[u][g].y += a[u].y * cs.x;
+                    Ss[u][g].x += bb[u].x * cs.y;
+                    Ss[u][g].y += bb[u].y * cs.y;
+                }
             }
         }
-        C* d = dst + l * LS + j * R;
-        if (blk == 0) d[0] = acc0;
 #pragma unroll
-        for (int u = 0; u < GP; ++u) {
-            const int q = 1 + blk * GP + u;
-            if (q <= P) {
-                const C base = cadd(x0, Cs[u]);
-                d[q] = V2<T>::mk(base.x + Ss[u].y, base.y - Ss[u].x);
-                d[R - q] = V2<T>::mk(base.x - Ss[u].y, base.y + Ss[u].x);
+        for (int u = 0; u < LPT; ++u) {
+            C* d = dst + (l + u * lgroups) * LS + j * R;
+            if (blk == 0) d[0] = acc0[u];
+#pragma unroll
+            for (int g = 0; g < GP; ++g) {
+                const int q = 1 + blk * GP + g;
+                if (q <= P) {
+                    const C base = cadd(x0[u], Cs[u][g]);
+                    d[q] = V2<T>::mk(base.x + Ss[u][g].y, base.y - Ss[u][g].x);
+                    d[R - q] = V2<T>::mk(base.x - Ss[u][g].y, base.y + Ss[u][g].x);
+                }
             }
         }
     }
+}
+
+template <typename T>
+__device__ void dft_prime_first(const typename V2<T>::t* __restrict__ src, typename V2<T>::t* __restrict__ dst,
+                                const typename V2<T>::t* __restrict__ mat, int N, int R, int lpb, int LS)
+{
+    if (lpb >= 2)
+        dft_prime_first_t<T, 2>(src, dst, mat, N, R, lpb, LS);
+    else
+        dft_prime_first_t<T, 1>(src, dst, mat, N, R, lpb, LS);
 }
 
 // entries of the (cos, sin) matrix used by dft_prime_first for prime radix R
@@ -300,9 +326,9 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(const TIN* __restrict__ 
 
     const long long line0 = (long long)blockIdx.x * lpb;
     const int nl = (int)min((long long)lpb, nlines - line0);
-    if (threadIdx.x < lpb) {
-        long long i = line0 + threadIdx.x;
-        base[threadIdx.x] = (i / inner) * ostride + (i % inner) * istride;
+    for (int t = threadIdx.x; t < lpb; t += blockDim.x) {
+        const long long i = line0 + t;
+        base[t] = (i / inner) * ostride + (i % inner) * istride;
     }
     __syncthreads();
     const int tot = lpb * N;
@@ -421,8 +447,9 @@ size_t fft_smem_bytes(int N, int lpb, bool fp64)
 template <typename T, typename TIN, bool RI, bool RO>
 static cudaError_t launch_one(const void* in, void* out, const FFTFactors& fac, long long nlines, int lpb,
                               long long inner, long long ostride, long long istride, long long es,
-                              const void* tw, bool lines_fastest, cudaStream_t st)
+                              const void* tw, bool lines_fastest, int threads, cudaStream_t st)
 {
+    if (threads < 32 || threads > 256 || threads % 32 != 0) return cudaErrorInvalidValue;
     size_t smem = fft_smem_bytes(fac.N, lpb, sizeof(T) == 8);
     auto kern = fft_lines_kernel<T, TIN, RI, RO>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -431,7 +458,7 @@ static cudaError_t launch_one(const void* in, void* out, const FFTFactors& fac, 
     while ((1 << lg) < lpb) ++lg;
     if ((1 << lg) != lpb || lpb > 256) return cudaErrorInvalidValue;  // lines per CTA: power of two
     long long nblk = (nlines + lpb - 1) / lpb;
-    kern<<<(unsigned)nblk, 256, smem, st>>>(reinterpret_cast<const TIN*>(in), out, fac, nlines, lg, inner, ostride,
+    kern<<<(unsigned)nblk, threads, smem, st>>>(reinterpret_cast<const TIN*>(in), out, fac, nlines, lg, inner, ostride,
                                             istride, es, tw, lines_fastest ? 1 : 0);
     return cudaGetLastError();
 }
@@ -442,22 +469,22 @@ cudaError_t launch_fft_lines(const FFTLaunch& L, cudaStream_t st)
         if (L.real_in && L.real_out) return cudaErrorInvalidValue;
         if (L.real_in)
             return launch_one<double, double, true, false>(L.in, L.out, L.fac, L.nlines, L.lpb, L.inner, L.ostride,
-                                                           L.istride, L.es, L.tw, L.lines_fastest, st);
+                                                           L.istride, L.es, L.tw, L.lines_fastest, L.threads, st);
         if (L.real_out)
             return launch_one<double, double2, false, true>(L.in, L.out, L.fac, L.nlines, L.lpb, L.inner, L.ostride,
-                                                            L.istride, L.es, L.tw, L.lines_fastest, st);
+                                                            L.istride, L.es, L.tw, L.lines_fastest, L.threads, st);
         return launch_one<double, double2, false, false>(L.in, L.out, L.fac, L.nlines, L.lpb, L.inner, L.ostride,
-                                                         L.istride, L.es, L.tw, L.lines_fastest, st);
+                                                         L.istride, L.es, L.tw, L.lines_fastest, L.threads, st);
     } else {
         if (L.real_in && L.real_out) return cudaErrorInvalidValue;
         if (L.real_in)
             return launch_one<float, float, true, false>(L.in, L.out, L.fac, L.nlines, L.lpb, L.inner, L.ostride,
-                                                         L.istride, L.es, L.tw, L.lines_fastest, st);
+                                                         L.istride, L.es, L.tw, L.lines_fastest, L.threads, st);
         if (L.real_out)
             return launch_one<float, float2, false, true>(L.in, L.out, L.fac, L.nlines, L.lpb, L.inner, L.ostride,
-                                                          L.istride, L.es, L.tw, L.lines_fastest, st);
+                                                          L.istride, L.es, L.tw, L.lines_fastest, L.threads, st);
         return launch_one<float, float2, false, false>(L.in, L.out, L.fac, L.nlines, L.lpb, L.inner, L.ostride,
-                                                       L.istride, L.es, L.tw, L.lines_fastest, st);
+                                                       L.istride, L.es, L.tw, L.lines_fastest, L.threads, st);
     }
 }
 

@@ -22,6 +22,7 @@ struct FFTLaunch {
     bool real_in;
     bool real_out;
     bool lines_fastest;   // consecutive lines adjacent in memory (column pass)
+    int threads = 256;    // threads per CTA (<= 256)
 };
 
 void make_fft_factors(int N, FFTFactors& f);

@@ -13,7 +13,7 @@ struct TCState;
 
 int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64, const std::vector<long long>& goff,
               long long table_elems, const double* d_tw, const double* d_w, bool refine, bool real, bool s2,
-              std::string& err);
+              bool autotune, std::string& err);
 void tc_destroy(TCState* s);
 long long tc_device_bytes(const TCState* s);
 int tc_forward(TCState* s, const void* grid, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err);

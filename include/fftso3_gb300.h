@@ -62,6 +62,10 @@ extern "C" {
 /* plan flags */
 #define FFTSO3_FLAG_REFINE 0x1u /* tensor-core forward: one residual step F += forward(f - inverse(F)) */
 #define FFTSO3_FLAG_GRAPH 0x2u  /* batches: capture each direction into a CUDA graph, replay it */
+#define FFTSO3_FLAG_AUTOTUNE 0x4u /* tensor-core plans: time the launch shapes of the generic-N FFT passes on
+                                     the plan's workspace at creation and keep the fastest (cached per N for
+                                     the process); batches: also time 1/2/4/8 bucket streams on the first
+                                     call of each direction */
 
 typedef struct fftso3_plan fftso3_plan;
 typedef struct fftso3_batch fftso3_batch;
@@ -161,7 +165,9 @@ int fftso3_wigner_d(double beta, int l_max, int recursion, double* d_out_host);
  * (ascending l_max, caller order within one l_max) so that no gather pass is
  * needed.  flags: FFTSO3_FLAG_REFINE (tensor-core forward refinement),
  * FFTSO3_FLAG_GRAPH (capture each direction once per (input, output) pair of
- * pointers into a CUDA graph and replay it; a new pointer pair re-captures).
+ * pointers into a CUDA graph and replay it; a new pointer pair re-captures),
+ * FFTSO3_FLAG_AUTOTUNE (tune each bucket plan's FFT launch shapes at creation
+ * and the number of bucket streams on the first call).
  * Calls on one batch object must not overlap (shared workspaces). */
 int fftso3_batch_create(fftso3_batch** batch, int kind, const int* l_max, int n_functions, int precision,
                         int recursion, unsigned flags);
@@ -169,6 +175,8 @@ int fftso3_batch_destroy(fftso3_batch* batch);
 long long fftso3_batch_grid_offset(const fftso3_batch* batch, int fn);
 long long fftso3_batch_coeff_offset(const fftso3_batch* batch, int fn);
 int fftso3_batch_bucket_count(const fftso3_batch* batch);
+/* Internal streams the buckets are spread over (chosen by FFTSO3_FLAG_AUTOTUNE on the first call). */
+int fftso3_batch_stream_count(const fftso3_batch* batch);
 long long fftso3_batch_device_bytes(const fftso3_batch* batch);
 int fftso3_batch_forward(fftso3_batch* batch, const void* grids, void* coeffs, void* stream);
 int fftso3_batch_inverse(fftso3_batch* batch, const void* coeffs, void* grids, void* stream);

@@ -107,3 +107,37 @@ def test_batch_fp64_equals_plans(gblib, torch_cuda):
         assert np.array_equal(c0[co:co + p.coeff_elems], fi.cpu().numpy())
         assert rel_err(c0[co:co + p.coeff_elems], Fs[i]) < 1e-12
 
+
+
+def test_autotuned_plan_and_batch(gblib, oracle, torch_cuda):
+    """FFTSO3_FLAG_AUTOTUNE changes only launch shapes: results stay within the tensor-core tolerance of the
+    oracle, for a plan with a large prime factor in N (l_max = 60, N = 122 = 2 * 61) and for a batch."""
+    torch = torch_cuda
+    s = torch.cuda.current_stream().cuda_stream
+    L = 60
+    Fr = so3_coeffs(L, seed=1000, complex_=False)
+    g_ref = oracle.so3_inverse_real_grid(L, Fr)
+    for flags in (0, gblib.FLAG_AUTOTUNE):
+        p = gblib.Plan(gblib.SO3_REAL, L, 2, "tc_bf16x3", "reference", flags)
+        g = torch.from_numpy(np.concatenate([g_ref.ravel(), g_ref.ravel()]).astype(np.float32)).cuda()
+        c = torch.empty(2 * Fr.size, dtype=torch.float32, device="cuda")
+        p.forward(g.data_ptr(), c.data_ptr(), s)
+        p.check()
+        co = c.cpu().numpy().astype(np.float64)
+        assert rel_err(co[:Fr.size], Fr) < TOL and rel_err(co[Fr.size:], Fr) < TOL
+    lmax = [10, 33, 10, 21, 46, 33]
+    b = gblib.Batch(gblib.SO3_REAL, lmax, "tc_bf16x3", "reference", gblib.FLAG_GRAPH | gblib.FLAG_AUTOTUNE)
+    Fs = [so3_coeffs(l, seed=1100 + i, complex_=False) for i, l in enumerate(lmax)]
+    cbuf = np.zeros(b.coeff_elems, dtype=np.float32)
+    for i in range(len(lmax)):
+        cbuf[b.coeff_offset(i):b.coeff_offset(i) + Fs[i].size] = Fs[i]
+    c = torch.from_numpy(cbuf).cuda()
+    g = torch.empty(b.grid_elems, dtype=torch.float32, device="cuda")
+    c2 = torch.empty_like(c)
+    b.inverse(c.data_ptr(), g.data_ptr(), s)
+    b.forward(g.data_ptr(), c2.data_ptr(), s)
+    b.check()
+    assert 1 <= b.streams <= b.buckets
+    co = c2.cpu().numpy().astype(np.float64)
+    for i in range(len(lmax)):
+        assert rel_err(co[b.coeff_offset(i):b.coeff_offset(i) + Fs[i].size], Fs[i]) < TOL
