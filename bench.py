@@ -492,6 +492,7 @@ def main() -> None:
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp32", action="store_true", help="skip the FP32 CUDA-core beta-sum comparison")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64 reference (profiling runs)")
     ap.add_argument("--workload", default="lmax255", choices=["lmax255", "uneven", "s2"],
                     help="lmax255: the headline SO(3) batch at one l_max (--l-max/--batch); uneven: the "
@@ -695,6 +696,38 @@ def main() -> None:
                "d2h_bytes_per_step": int(8 * b * N ** 3 + 8 * b * C), "steps": ksteps}
         del hg, hc, hgo, hco
 
+    # ---- the FP32 form of the beta-sum (CUDA cores, FFTSO3_PREC_FP32) on the same batch
+    fp32 = None
+    if not args.no_fp32:
+        del grid_out
+        torch.cuda.empty_cache()
+        p32 = _lib.Plan(_lib.SO3_COMPLEX, L, b, "fp32", "stable")
+        g32 = torch.empty_like(grid)
+        c32 = torch.empty_like(coef)
+        p32.inverse(coef.data_ptr(), g32.data_ptr(), sp)
+        p32.forward(grid.data_ptr(), c32.data_ptr(), sp)
+        torch.cuda.synchronize()
+        p32.check()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        p32.inverse(coef.data_ptr(), g32.data_ptr(), sp)
+        p32.forward(grid.data_ptr(), c32.data_ptr(), sp)
+        f1.record(stream)
+        torch.cuda.synchronize()
+        ms32 = f0.elapsed_time(f1)
+        fp32 = {"value": b * world * 1000.0 / ms32, "unit": UNIT, "ms_per_step": ms32,
+                "note": "FFTSO3_PREC_FP32: FP32 table and FMA accumulation on the CUDA cores, same batch"}
+        if not args.no_accuracy:
+            pa = _lib.Plan(_lib.SO3_COMPLEX, L, 1, "fp32", "stable")
+            ca = torch.empty(C, dtype=torch.complex64, device=dev)
+            pa.forward(g0_c64.data_ptr(), ca.data_ptr(), sp)
+            torch.cuda.synchronize()
+            fr32, fm32 = per_l_errors(ca.cpu().numpy().astype(np.complex128), F0_fp64, L)
+            fp32.update({"forward_rel_rms": fr32, "forward_rel_max_per_l": fm32})
+            del pa, ca
+        del p32, g32, c32
+        torch.cuda.empty_cache()
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_sample(L)
@@ -711,7 +744,7 @@ def main() -> None:
                        "l_max": L, "batch_per_gpu": b, "precision": "tc_bf16x3",
                        "l2": "inputs larger than L2 (1 GB grid per function)"},
             "e2e": e2e, "gpu_launches": launches, "roofline": roof, "stages": stage_summary,
-            "accuracy": acc, "fp64_path": fp64,
+            "accuracy": acc, "fp64_path": fp64, "fp32_cuda_core_path": fp32,
             "speedup_vs_fp64_path": (value / world) / fp64["value"] if fp64 else None,
             "clocks": clocks, "cpu_baseline": cpu,
         }

@@ -26,6 +26,7 @@ S2_REAL = 3
 
 PREC_FP64 = 0
 PREC_TC_BF16X3 = 1
+PREC_FP32 = 2
 
 RECURSION_REFERENCE = 0
 RECURSION_STABLE = 1
@@ -34,7 +35,7 @@ FLAG_REFINE = 0x1
 FLAG_GRAPH = 0x2
 FLAG_AUTOTUNE = 0x4
 
-PRECISIONS = {"fp64": PREC_FP64, "tc_bf16x3": PREC_TC_BF16X3}
+PRECISIONS = {"fp64": PREC_FP64, "tc_bf16x3": PREC_TC_BF16X3, "fp32": PREC_FP32}
 RECURSIONS = {"reference": RECURSION_REFERENCE, "stable": RECURSION_STABLE}
 
 # every symbol the header declares: name -> (restype, argtypes)

@@ -196,7 +196,7 @@ int run_forward(fftso3_plan* p, const void* grid, void* coeffs, cudaStream_t st)
 {
     const int N = p->N, L = p->L, b = p->batch;
     StageTimer& T = p->timer;
-    if (p->precision == FFTSO3_PREC_TC_BF16X3) return tc_forward(p->tc, grid, coeffs, st, &T, g_err);
+    if (p->tc) return tc_forward(p->tc, grid, coeffs, st, &T, g_err);
 #define STAGE(id, call)      \
     do {                     \
         T.begin(id, st);     \
@@ -224,7 +224,7 @@ int run_inverse(fftso3_plan* p, const void* coeffs, void* grid, cudaStream_t st)
 {
     const int N = p->N, L = p->L, b = p->batch;
     StageTimer& T = p->timer;
-    if (p->precision == FFTSO3_PREC_TC_BF16X3) return tc_inverse(p->tc, coeffs, grid, st, &T, g_err);
+    if (p->tc) return tc_inverse(p->tc, coeffs, grid, st, &T, g_err);
     if (p->so3) {
         const double2* Fin = (const double2*)coeffs;
         if (p->real) {
@@ -300,7 +300,7 @@ int fftso3_plan_create(fftso3_plan** out, int kind, int l_max, int batch, int pr
     if (!valid_kind(kind)) return fail(FFTSO3_ERR_INVALID_ARG, "unknown transform kind");
     if (l_max < 0) return fail(FFTSO3_ERR_INVALID_ARG, "l_max must be >= 0");
     if (batch < 1) return fail(FFTSO3_ERR_INVALID_ARG, "batch must be >= 1");
-    if (precision != FFTSO3_PREC_FP64 && precision != FFTSO3_PREC_TC_BF16X3)
+    if (precision != FFTSO3_PREC_FP64 && precision != FFTSO3_PREC_TC_BF16X3 && precision != FFTSO3_PREC_FP32)
         return fail(FFTSO3_ERR_INVALID_ARG, "unknown precision");
     if (recursion != FFTSO3_RECURSION_REFERENCE && recursion != FFTSO3_RECURSION_STABLE)
         return fail(FFTSO3_ERR_INVALID_ARG, "unknown recursion mode");
@@ -308,8 +308,9 @@ int fftso3_plan_create(fftso3_plan** out, int kind, int l_max, int batch, int pr
         return fail(FFTSO3_ERR_INVALID_ARG, "unknown flag bits");
     if (is_so3(kind) && l_max > 511) return fail(FFTSO3_ERR_UNSUPPORTED, "SO(3) l_max above 511 is not supported");
     if (!is_so3(kind) && l_max > 2047) return fail(FFTSO3_ERR_UNSUPPORTED, "S^2 l_max above 2047 is not supported");
-    if (precision == FFTSO3_PREC_TC_BF16X3 && l_max > 511)
-        return fail(FFTSO3_ERR_UNSUPPORTED, "the tensor-core path supports l_max <= 511 (2(l_max+1) <= 1024)");
+    if (precision != FFTSO3_PREC_FP64 && l_max > 511)
+        return fail(FFTSO3_ERR_UNSUPPORTED,
+                    "the tensor-core and FP32 paths support l_max <= 511 (2(l_max+1) <= 1024)");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
         return fail(FFTSO3_ERR_NO_DEVICE, "no CUDA device available");
@@ -416,13 +417,13 @@ int fftso3_plan_create(fftso3_plan** out, int kind, int l_max, int batch, int pr
         std::string err;
         rc = tc_create(&p->tc, p->L, p->N, batch, p->d_table, goff, p->table_elems, p->d_tw, p->d_w,
                        (flags & FFTSO3_FLAG_REFINE) != 0, p->real, !p->so3, (flags & FFTSO3_FLAG_AUTOTUNE) != 0,
-                       err);
+                       precision == FFTSO3_PREC_FP32, err);
         if (rc) {
             g_err = err;
             return bail(rc);
         }
         p->bytes += tc_device_bytes(p->tc);
-        // the tensor-core path keeps only its BF16 planes of the table
+        // the FP32-data paths keep only their BF16 planes / FP32 copy of the table
         cudaFree(p->d_table);
         p->d_table = nullptr;
         p->bytes -= (long long)sizeof(double) * p->table_elems;

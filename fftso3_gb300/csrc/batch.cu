@@ -240,7 +240,7 @@ int fftso3_batch_create(fftso3_batch** out, int kind, const int* l_max, int n_fu
         return bfail(FFTSO3_ERR_INVALID_ARG, "unknown flag bits");
     if (kind < FFTSO3_SO3_COMPLEX || kind > FFTSO3_S2_REAL)
         return bfail(FFTSO3_ERR_INVALID_ARG, "unknown transform kind");
-    if (precision != FFTSO3_PREC_FP64 && precision != FFTSO3_PREC_TC_BF16X3)
+    if (precision != FFTSO3_PREC_FP64 && precision != FFTSO3_PREC_TC_BF16X3 && precision != FFTSO3_PREC_FP32)
         return bfail(FFTSO3_ERR_INVALID_ARG, "unknown precision");
     for (int i = 0; i < n_functions; ++i)
         if (l_max[i] < 0)

@@ -583,6 +583,140 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
 }
 
+// ------------------------------------------------- FP32 (CUDA-core) form
+//
+// The same products on the FP32 pipes (FFTSO3_PREC_FP32): one CTA of 256
+// threads per work item (group, row tile, column tile) computes the 128 x 128
+// tile D[rows][c] = sum over K of A[rows][K] B[K][c] with FP32 FMAs, 8 x 8
+// outputs per thread, K in steps of 16 staged in shared memory.  A comes from
+// an FP32 copy of the table ([row][Kp], zero for k >= N), read K-major for the
+// forward (rows l, K = k) and transposed for the inverse (rows k, K = l); B is
+// X (pencils x weights) or Y (group-major coefficients), as in the
+// tensor-core kernel, and so are the epilogue's scatters.
+constexpr int SBK = 16;
+
+template <bool FWD, bool S2>
+__global__ void __launch_bounds__(256) so3_fp32_gemm_kernel(const float* __restrict__ tab, GemmArgs args)
+{
+    __shared__ __align__(16) float As[SBK][BM + 4];
+    __shared__ __align__(16) float Bs[SBK][BN + 4];
+    constexpr int PPF = S2 ? 2 : 4;
+    constexpr int FPTK = BN / (2 * PPF);
+    const int B = args.L + 1, N = args.N, Kp = args.Kp;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int4 item = args.items[blockIdx.x];
+    int m0, n0;
+    item_mn(item, m0, n0);
+    const GroupPairs P = S2 ? s2_pairs(m0) : group_pairs(m0, n0);
+    const int nl = B - m0;
+    const long long row0 = args.grow0[item.x];
+    const int K = FWD ? N : nl;
+    const int mbase = item.y * BM;
+    float acc[8][8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+    for (int k0 = 0; k0 < K; k0 += SBK) {
+        // A tile
+        for (int e = threadIdx.x; e < BM * SBK; e += 256) {
+            float v;
+            if (FWD) {
+                const int i = e / SBK, kk = e - i * SBK;
+                const int m = mbase + i, k = k0 + kk;
+                v = (m < nl && k < N) ? __ldg(tab + (row0 + m) * Kp + k) : 0.f;
+                As[kk][i] = v;
+            } else {
+                const int kk = e / BM, i = e - kk * BM;
+                const int l = k0 + kk, k = mbase + i;
+                v = (l < nl && k < N) ? __ldg(tab + (row0 + l) * Kp + k) : 0.f;
+                As[kk][i] = v;
+            }
+        }
+        // B tile: 64 (function, pair) columns x re/im
+        for (int e = threadIdx.x; e < (BN / 2) * SBK; e += 256) {
+            const int cp = e / SBK, kk = e - cp * SBK;
+            const int fl = cp / PPF, pp = cp % PPF;
+            const int f = item.z * FPTK + fl, k = k0 + kk;
+            float2 v = make_float2(0.f, 0.f);
+            if (f < args.batch && pp < P.np && k < K) {
+                if (FWD) {
+                    long long off;
+                    if (S2) {
+                        const int bin = pp == 0 ? m0 : N - m0;
+                        off = (long long)bin * N;
+                    } else {
+                        int pi = (-P.m[pp]) % N; if (pi < 0) pi += N;
+                        int qi = (-P.n[pp]) % N; if (qi < 0) qi += N;
+                        off = ((long long)pi * N + qi) * N;
+                    }
+                    v = __ldg(args.pin + (long long)f * args.fstride + off + k);
+                    const float wk = __ldg(args.wf + k);
+                    v.x *= wk;
+                    v.y *= wk;
+                } else {
+                    v = __ldg(args.cin + (long long)f * args.cstride + args.goff2[item.x] + (long long)pp * nl + k);
+                }
+            }
+            Bs[kk][2 * cp] = v.x;
+            Bs[kk][2 * cp + 1] = v.y;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < SBK; ++kk) {
+            const float4 a0 = *reinterpret_cast<const float4*>(&As[kk][ty * 8]);
+            const float4 a1 = *reinterpret_cast<const float4*>(&As[kk][ty * 8 + 4]);
+            const float4 b0 = *reinterpret_cast<const float4*>(&Bs[kk][tx * 8]);
+            const float4 b1 = *reinterpret_cast<const float4*>(&Bs[kk][tx * 8 + 4]);
+            const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+#pragma unroll
+                for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+    // epilogue: thread columns tx*8 .. tx*8+7 = (function, pair) tx*4 .. tx*4+3, re/im
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj) {
+        const int cp = tx * 4 + jj;
+        const int fl = cp / PPF, pp = cp % PPF;
+        const int f = item.z * FPTK + fl;
+        if (f >= args.batch || pp >= P.np) continue;
+        long long base;
+        if (FWD) {
+            base = (long long)f * args.cstride + args.goff2[item.x] + (long long)pp * nl;
+        } else if (S2) {
+            int bin = (pp == 0 ? -m0 : m0) % N; if (bin < 0) bin += N;
+            base = (long long)f * args.fstride + (long long)bin * N;
+        } else {
+            int pi = P.m[pp] % N; if (pi < 0) pi += N;
+            int qi = P.n[pp] % N; if (qi < 0) qi += N;
+            base = (long long)f * args.fstride + ((long long)pi * N + qi) * N;
+        }
+        const float sg = FWD ? (float)P.sign[pp] : 1.f;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int r = mbase + ty * 8 + i;
+            if (r >= (FWD ? nl : N)) break;
+            const float2 v = make_float2(sg * acc[i][2 * jj], sg * acc[i][2 * jj + 1]);
+            if (FWD) args.cout[base + r] = v;
+            else args.pout[base + r] = v;
+        }
+    }
+}
+
+// FP64 table [rows][N] -> FP32 [rows][Kp] (zero for k >= N).
+__global__ void table_fp32_kernel(const double* __restrict__ t, float* __restrict__ o, long long rows, int N, int Kp)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= rows * Kp) return;
+    const long long r = i / Kp;
+    const int k = (int)(i % Kp);
+    o[i] = (k < N) ? (float)t[r * N + k] : 0.f;
+}
+
 // ------------------------------------------------------- helper kernels
 
 // FP64 table [rows][N] -> three BF16 planes [rows][Kp] (zero for k >= N);
@@ -764,6 +898,8 @@ struct TCState {
     bool refine = false;
     bool real = false;            // real grids (FFTSO3_*_REAL): real samples in, real part out
     bool s2 = false;              // S^2 (Legendre groups g = m, grids N^2) instead of SO(3)
+    bool simt = false;            // FP32 CUDA-core beta-sum (FFTSO3_PREC_FP32) instead of tcgen05
+    float* d_tab32 = nullptr;     // FP32 table [row][Kp] (simt)
     int lpb[2] = {0, 0};          // generic-N FFT lines per CTA (rows, cols); 0 = heuristic
     int thr[2] = {256, 256};      // generic-N FFT threads per CTA (rows, cols)
     FFTFactors fac;
@@ -840,7 +976,7 @@ void tc_destroy(TCState* s)
     if (!s) return;
     for (int p = 0; p < 3; ++p)
         if (s->d_tab[p]) cudaFree(s->d_tab[p]);
-    void* ptrs[] = {s->d_wf, s->d_work, s->d_pencil, s->d_resid, s->d_coef2, s->d_fc, s->d_grow0, s->d_goff2, s->d_fg,
+    void* ptrs[] = {s->d_tab32, s->d_wf, s->d_work, s->d_pencil, s->d_resid, s->d_coef2, s->d_fc, s->d_grow0, s->d_goff2, s->d_fg,
                     s->d_items_fwd, s->d_items_inv, s->d_err};
     for (void* q : ptrs)
         if (q) cudaFree(q);
@@ -853,7 +989,7 @@ static int autotune_fft(TCState* s, std::string& err);
 
 int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64, const std::vector<long long>& goff,
               long long table_elems, const double* d_tw, const double* d_w, bool refine, bool real, bool s2,
-              bool autotune, std::string& err)
+              bool autotune, bool simt, std::string& err)
 {
     *out = nullptr;
     if (N > MAXN) {
@@ -867,6 +1003,7 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
     s->Kp = (N + 63) / 64 * 64;
     s->batch = batch;
     s->s2 = s2;
+    s->simt = simt;
     s->ntiles = s2 ? (batch + FPT_S2 - 1) / FPT_S2 : (batch + FPT - 1) / FPT;
     s->ngroups = s2 ? s->B : s->B * s->B;
     s->refine = refine;
@@ -891,14 +1028,18 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
         if ((rc = tc_alloc(s, (void**)&s->d_wf, sizeof(float) * N, err))) return bail(rc);
         cudaMemcpy(s->d_wf, wf.data(), sizeof(float) * N, cudaMemcpyHostToDevice);
     }
-    // table planes
-    for (int p = 0; p < 3; ++p)
-        if ((rc = tc_alloc(s, (void**)&s->d_tab[p], sizeof(__nv_bfloat16) * s->total_rows * s->Kp, err)))
-            return bail(rc);
-    {
-        long long tot = s->total_rows * s->Kp;
+    // table: three BF16 planes (tensor cores) or one FP32 copy (CUDA cores)
+    const long long tot = s->total_rows * s->Kp;
+    if (simt) {
+        if ((rc = tc_alloc(s, (void**)&s->d_tab32, sizeof(float) * tot, err))) return bail(rc);
+        table_fp32_kernel<<<(unsigned)((tot + 255) / 256), 256>>>(d_table_fp64, s->d_tab32, s->total_rows, N, s->Kp);
+    } else {
+        for (int p = 0; p < 3; ++p)
+            if ((rc = tc_alloc(s, (void**)&s->d_tab[p], sizeof(__nv_bfloat16) * tot, err))) return bail(rc);
         table_split_kernel<<<(unsigned)((tot + 255) / 256), 256>>>(d_table_fp64, s->d_tab[0], s->d_tab[1],
                                                                    s->d_tab[2], s->total_rows, N, s->Kp);
+    }
+    {
         cudaError_t e = cudaDeviceSynchronize();
         if (e != cudaSuccess) {
             err = std::string("table split: ") + cudaGetErrorString(e);
@@ -953,7 +1094,7 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
     cudaMemcpy(s->d_items_fwd, itf.data(), sizeof(int4) * itf.size(), cudaMemcpyHostToDevice);
     cudaMemcpy(s->d_items_inv, iti.data(), sizeof(int4) * iti.size(), cudaMemcpyHostToDevice);
     cudaMemset(s->d_err, 0, sizeof(int));
-    for (int p = 0; p < 3; ++p) {
+    for (int p = 0; p < 3 && !simt; ++p) {
         bool ok = encode_2d(&s->tmA_fwd[p], s->d_tab[p], s->Kp, s->total_rows, 64, BM) &&
                   encode_2d(&s->tmA_inv[p], s->d_tab[p], s->Kp, s->total_rows, 64, BK);
         if (!ok) {
@@ -1139,6 +1280,18 @@ static int launch_gemm(TCState* s, bool fwd, cudaStream_t st, std::string& err)
     } else {
         a.cin = s->d_fg;
         a.pout = s->d_pencil;
+    }
+    if (s->simt) {
+        if (fwd && s->s2)
+            so3_fp32_gemm_kernel<true, true><<<a.nitems, 256, 0, st>>>(s->d_tab32, a);
+        else if (fwd)
+            so3_fp32_gemm_kernel<true, false><<<a.nitems, 256, 0, st>>>(s->d_tab32, a);
+        else if (s->s2)
+            so3_fp32_gemm_kernel<false, true><<<a.nitems, 256, 0, st>>>(s->d_tab32, a);
+        else
+            so3_fp32_gemm_kernel<false, false><<<a.nitems, 256, 0, st>>>(s->d_tab32, a);
+        TCK(cudaGetLastError());
+        return FFTSO3_SUCCESS;
     }
     const int nctas = a.nitems < s->nsm ? a.nitems : s->nsm;
     const CUtensorMap* tm = fwd ? s->tmA_fwd : s->tmA_inv;

@@ -54,6 +54,8 @@ extern "C" {
 #define FFTSO3_PREC_FP64 0      /* FP64 end to end (the plain method) */
 #define FFTSO3_PREC_TC_BF16X3 1 /* tcgen05 tensor cores, 3-term split-BF16, FP32 accumulate; complex64/float32 data;
                                    all four kinds, l_max <= 511 */
+#define FFTSO3_PREC_FP32 2      /* FP32 beta-sum on the CUDA cores (FP32 table, FP32 FMA accumulate), FP32 FFT;
+                                   complex64/float32 data; all four kinds, l_max <= 511 */
 
 /* Wigner-d recursion */
 #define FFTSO3_RECURSION_REFERENCE 0 /* bit-faithful to fdcl_FFTSO3.cpp:127-194 (underflows near beta=pi, l_max>~90) */
