@@ -361,7 +361,7 @@ def main_uneven(args) -> None:
 
 # --------------------------------------------------------------- S^2 batch
 
-S2_METRIC = "S2 real fwd+inv transforms/s, 512 signals at l_max=511: TC split-BF16 vs FP64"
+S2_METRIC = "S2 real fwd+inv transforms/s, {b} signals at l_max={L}: TC split-BF16 vs FP64"
 
 
 def main_s2(args) -> None:
@@ -377,7 +377,7 @@ def main_s2(args) -> None:
     torch.cuda.set_device(dev)
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
-    L, b = 511, args.functions if args.functions != 4096 else 512
+    L, b = args.s2_l_max, args.functions if args.functions != 4096 else 512
     B, N = L + 1, 2 * (L + 1)
     C = B * B
     plan = _lib.Plan(_lib.S2_REAL, L, b, "tc_bf16x3", "reference")
@@ -407,6 +407,16 @@ def main_s2(args) -> None:
     acc = {"forward_rel_rms": float(torch.linalg.norm(coef_out[0].double() - F64) / torch.linalg.norm(F64)),
            "inverse_rel_rms": float(torch.linalg.norm(grid_out[:N * N].double() - g64) / torch.linalg.norm(g64)),
            "against": "FP64 plan (FFTS2_real, FP64) on signal 0"}
+    # the same signal through the FP32 CUDA-core beta-sum (same FP32 FFT): separates GEMM and FFT error
+    p32 = _lib.Plan(_lib.S2_REAL, L, 1, "fp32", "reference")
+    c32 = torch.empty(C, dtype=torch.float32, device=dev)
+    g32 = torch.empty(N * N, dtype=torch.float32, device=dev)
+    p32.forward(grid.data_ptr(), c32.data_ptr(), sp)
+    p32.inverse(coef.data_ptr(), g32.data_ptr(), sp)
+    torch.cuda.synchronize()
+    acc["fp32_cuda_core_forward_rel_rms"] = float(torch.linalg.norm(c32.double() - F64) / torch.linalg.norm(F64))
+    acc["fp32_cuda_core_inverse_rel_rms"] = float(torch.linalg.norm(g32.double() - g64) / torch.linalg.norm(g64))
+    del p32, c32, g32
 
     # FP64 path rate (batch 16, per signal)
     b64 = 16
@@ -465,7 +475,7 @@ def main_s2(args) -> None:
             fft[name] = {"ms": t * 1000.0, "gbs": fft_bytes / t / 1e9, "frac_of_hbm": fft_bytes / t / 1e9 / peaks["hbm_gbs"]}
     value = b * 1000.0 / ms
     line = {
-        "metric": S2_METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "metric": S2_METRIC.format(b=b, L=L), "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "bf16x3 (split) / fp32 accumulate / fp32 FFT; fp32 samples", "data": "synthetic",
         "config": {"workload": f"{b} real S^2 signals, l_max={L} ({N}x{N} grid, FP32 samples), coefficients "
@@ -498,6 +508,7 @@ def main() -> None:
                     help="lmax255: the headline SO(3) batch at one l_max (--l-max/--batch); uneven: the "
                          "mixed-bandwidth SO(3) batch; s2: the S^2 batch at l_max=511")
     ap.add_argument("--functions", type=int, default=4096, help="uneven workload: number of functions")
+    ap.add_argument("--s2-l-max", type=int, default=511, help="s2 workload: l_max")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -96,10 +96,16 @@ __device__ __forceinline__ void warp_fft(float2 (&v)[R], const float2* __restric
     }
 }
 
+// Scratch row stride of the line FFT: 32 + P (P = 32 / R), so that step B's
+// reads (lane = (k1, h), h < P) fall in distinct banks for each half-warp of
+// 8-byte accesses ((32 + P) k1 + h is distinct mod 16).
+template <int R>
+__host__ __device__ constexpr int scratch_stride() { return 32 + 32 / R; }
+
 // Line FFT through shared memory (far fewer shuffles than warp_fft), in two
-// steps on a per-warp scratch line Tl (at least 33 R elements):
+// steps on a per-warp scratch line Tl (at least R * scratch_stride<R>() elements):
 //   step A: lane t holds x[t + 32 i] (i < R); R-point DFT over i, twiddle
-//           w_N^{t k1}, store Y[t][k1] at Tl[k1 * 33 + t];
+//           w_N^{t k1}, store Y[t][k1] at Tl[k1 * S + t], S = scratch_stride<R>();
 //   step B: lane (k1, h) (h < P = 32 / R) loads Y[P s + h][k1] (s < R), R-point
 //           DFT over s (index kappa), twiddle w_32^{h kappa}, then a P-point DFT
 //           across its P lanes (log2 P shuffle stages).  Register r then holds
@@ -114,7 +120,7 @@ __device__ __forceinline__ void line_step_a(float2 (&v)[R], float2* Tl, const fl
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         const int k1 = brev(r, LR);
-        Tl[k1 * 33 + lane] = (r == 0) ? v[r] : cmulf(v[r], W[lane * k1]);
+        Tl[k1 * scratch_stride<R>() + lane] = (r == 0) ? v[r] : cmulf(v[r], W[lane * k1]);
     }
     __syncwarp();
 }
@@ -128,7 +134,7 @@ __device__ __forceinline__ void line_step_b(float2 (&v)[R], const float2* Tl, co
     constexpr int P = 32 / R;
     const int k1 = lane / P, h = lane % P;
 #pragma unroll
-    for (int s2 = 0; s2 < R; ++s2) v[s2] = Tl[k1 * 33 + P * s2 + h];
+    for (int s2 = 0; s2 < R; ++s2) v[s2] = Tl[k1 * scratch_stride<R>() + P * s2 + h];
     reg_dif<R>(v, W, N);
     if (P > 1) {
 #pragma unroll
@@ -203,9 +209,31 @@ __global__ void __launch_bounds__(32 * WPB) fft_rows_reg(const float2* __restric
 constexpr int TL = 16;               // lines per CTA tile
 constexpr int PWARPS = 8;            // 2 lines per warp
 
-// padded position of element j in a staged line (one pad slot every R elements)
+// Padded position of element j in a staged line: one pad slot every R
+// elements, plus SH slots every R^2 elements.  The output element K of lane
+// (k1, h) in register r is K = k1 + R brR(r) + R^2 brP(h); with
+// SH = R/2 - R^2 - R (mod 16) the 16 lanes of a half-warp store to 16
+// distinct banks (8-byte elements) for every r.
 template <int R>
-__device__ __forceinline__ int ppos(int j) { return j + (j >> ilog2(R)); }
+__host__ __device__ constexpr int pad_sh()
+{
+    return R >= 32 ? 0 : (((R / 2 - R * R - R) % 16) + 16) % 16;
+}
+template <int R>
+__device__ __forceinline__ int ppos(int j)
+{
+    return j + (j >> ilog2(R)) + pad_sh<R>() * (j >> (2 * ilog2(R)));
+}
+// Staged line length: holds every padded position and the line-FFT scratch;
+// odd, so the transposed side's pairs of lines (l, l + 1) spread over the banks.
+template <int R>
+__host__ __device__ constexpr int tile_lp()
+{
+    constexpr int N = 32 * R;
+    constexpr int need = (N - 1) + (N - 1) / R + pad_sh<R>() * ((N - 1) / (R * R)) + 1;
+    constexpr int lp = need > R * scratch_stride<R>() ? need : R * scratch_stride<R>();
+    return lp | 1;
+}
 
 // Geometry of a tiled pass (element offsets).
 struct TileGeo {
@@ -229,7 +257,7 @@ __global__ void __launch_bounds__(32 * PWARPS, 3) fft_tile(const float2* __restr
 {
     constexpr int N = 32 * R;
     constexpr int LR = ilog2(R);
-    constexpr int LP = N + N / R + 1;  // padded staged line
+    constexpr int LP = tile_lp<R>();  // padded staged line
     extern __shared__ float2 smem_f2[];
     float2* Ws = smem_f2;
     float2* T = smem_f2 + N;  // [TL][LP]
@@ -327,7 +355,7 @@ template <int R, bool C2T, bool REAL_IO>
 static cudaError_t tile_r(const void* in, void* out, long long nf, const TileGeo& g, const void* tw, cudaStream_t st)
 {
     constexpr int N = 32 * R;
-    constexpr int LP = N + N / R + 1;
+    constexpr int LP = tile_lp<R>();
     const size_t smem = sizeof(float2) * ((size_t)N + (size_t)TL * LP);
     auto k = fft_tile<R, C2T, REAL_IO>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -80,3 +80,29 @@ def test_s2_tc_real_refined(gblib, oracle, torch_cuda):
     g_ref = oracle.s2_inverse_real_grid(L, F)
     _, G = _roundtrip(gblib, torch_cuda, gblib.S2_REAL, L, 1, F, g_ref, flags=gblib.FLAG_REFINE)
     assert rel_err(G, F) < TOL
+
+
+def test_s2_tc_lmax511_against_fp64_plan(gblib, torch_cuda):
+    """N = 1024 (tile FFT with R = 32), real signals, batch 3, against the FP64 plan run on
+    the same FP32-rounded samples and coefficients (the error of the transform itself; at
+    l_max = 511 it is 7e-7 .. 9e-7, of which the FP32 FFT alone gives about 5e-7)."""
+    torch = torch_cuda
+    L, b = 511, 3
+    F = np.concatenate([s2_coeffs(L, seed=1600 + i, complex_=False) for i in range(b)])
+    s = torch.cuda.current_stream().cuda_stream
+    p64 = gblib.Plan(gblib.S2_REAL, L, b, "fp64", "reference")
+    ptc = gblib.Plan(gblib.S2_REAL, L, b, "tc_bf16x3", "reference")
+    c32 = torch.from_numpy(F).cuda().float()
+    c64 = c32.double()
+    g64 = torch.empty(b * (2 * L + 2) ** 2, dtype=torch.float64, device="cuda")
+    p64.inverse(c64.data_ptr(), g64.data_ptr(), s)
+    g32 = torch.empty(g64.shape, dtype=torch.float32, device="cuda")
+    ptc.inverse(c32.data_ptr(), g32.data_ptr(), s)
+    gin = g64.float()
+    F64 = torch.empty(F.shape, dtype=torch.float64, device="cuda")
+    p64.forward(gin.double().data_ptr(), F64.data_ptr(), s)
+    F32 = torch.empty(F.shape, dtype=torch.float32, device="cuda")
+    ptc.forward(gin.data_ptr(), F32.data_ptr(), s)
+    ptc.check()
+    assert rel_err(g32.cpu().numpy().astype(np.float64), g64.cpu().numpy()) < TOL
+    assert rel_err(F32.cpu().numpy().astype(np.float64), F64.cpu().numpy()) < TOL

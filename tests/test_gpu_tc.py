@@ -126,3 +126,23 @@ def test_tc_generic_fft_lmax96(gblib, torch_cuda):
     ptc.forward(g64.to(torch.complex64).data_ptr(), F32.data_ptr(), s)
     ptc.check()
     assert rel_err(F32.cpu().numpy().astype(np.complex128), F) < TOL
+
+
+@pytest.mark.parametrize("L", [63, 127])
+def test_tc_tile_fft_sizes(gblib, torch_cuda, L):
+    """Tile FFT at N = 128 and 256 (R = 4, 8) against the FP64 plan, stable recursion."""
+    torch = torch_cuda
+    C = (L + 1) * (4 * (L + 1) ** 2 - 1) // 3
+    F = so3_coeffs(L, seed=1500 + L, decay="pow")
+    ptc, p64 = _plan_pair(gblib, torch, gblib.SO3_COMPLEX, L, 1, "stable")
+    s = torch.cuda.current_stream().cuda_stream
+    c64 = torch.from_numpy(F).cuda()
+    g64 = torch.empty((2 * L + 2) ** 3, dtype=torch.complex128, device="cuda")
+    p64.inverse(c64.data_ptr(), g64.data_ptr(), s)
+    g32 = torch.empty(g64.shape, dtype=torch.complex64, device="cuda")
+    ptc.inverse(c64.to(torch.complex64).data_ptr(), g32.data_ptr(), s)
+    F32 = torch.empty(C, dtype=torch.complex64, device="cuda")
+    ptc.forward(g64.to(torch.complex64).data_ptr(), F32.data_ptr(), s)
+    ptc.check()
+    assert rel_err(g32.cpu().numpy().astype(np.complex128), g64.cpu().numpy()) < TOL
+    assert rel_err(F32.cpu().numpy().astype(np.complex128), F) < TOL
