@@ -119,6 +119,11 @@ struct fftso3_plan {
     StageTimer timer;              // optional per-stage CUDA-event timing
 };
 
+namespace fftso3 {
+TCState* plan_tc_state(fftso3_plan* p) { return p ? p->tc : nullptr; }
+StageTimer* plan_timer(fftso3_plan* p) { return p ? &p->timer : nullptr; }
+}  // namespace fftso3
+
 namespace {
 
 int plan_alloc(fftso3_plan* p, void** ptr, size_t bytes)

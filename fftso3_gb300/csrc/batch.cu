@@ -15,6 +15,11 @@
 //  * buckets are spread over a few internal streams (longest work first, each
 //    bucket to the least-loaded stream) forked from and joined back into the
 //    caller's stream, so small bandwidths run side by side on the SMs;
+//  * tensor-core batches without refinement run the beta-sum GEMM of all
+//    buckets as ONE persistent launch (tc_fused_gemm: one work list over every
+//    bucket's (group, row tile, column tile) items, longest first): forward =
+//    fork / per-bucket FFTs / join / fused GEMM / fork / per-bucket coefficient
+//    permutations / join, inverse the mirror image;
 //  * with FFTSO3_FLAG_GRAPH the whole fork / bucket launches / join sequence
 //    is captured once per (direction, input, output) into a CUDA graph and
 //    replayed with one cudaGraphLaunch afterwards, which removes the
@@ -27,6 +32,7 @@
 
 #include "../../include/fftso3_gb300.h"
 #include "common.cuh"
+#include "tc.cuh"
 
 using namespace fftso3;
 
@@ -75,12 +81,17 @@ struct fftso3_batch {
     bool timing = false;                         // per-stage timing (eager launches, no graph)
     bool tuned = false;                          // stream count chosen (FFTSO3_FLAG_AUTOTUNE)
     int nstreams_used = 0;
+    TCFused* fused = nullptr;                    // one GEMM launch over all buckets
+    StageTimer timer;                            // the fused GEMM's stage time
 };
 
 namespace {
 
 void batch_free(fftso3_batch* b)
 {
+    if (b->fused) tc_fused_destroy(b->fused);
+    b->timer.enabled = false;
+    b->timer.collect();
     for (auto& g : b->graphs)
         if (g.exec) cudaGraphExecDestroy(g.exec);
     for (auto& k : b->buckets)
@@ -160,28 +171,84 @@ int tune_streams(fftso3_batch* b, int dir, const void* in, void* out, cudaStream
     return FFTSO3_SUCCESS;
 }
 
-// fork from `st`, every bucket on its stream, join back into `st`
-int launch_all(fftso3_batch* b, int dir, const void* in, void* out, cudaStream_t st)
+int fork_from(fftso3_batch* b, cudaStream_t st)
 {
     cudaError_t e;
     if ((e = cudaEventRecord(b->fork, st)) != cudaSuccess) return bcuda(e, "cudaEventRecord");
     for (cudaStream_t s : b->streams)
         if ((e = cudaStreamWaitEvent(s, b->fork, 0)) != cudaSuccess) return bcuda(e, "cudaStreamWaitEvent");
-    const size_t isz = dir == 0 ? b->gbytes : b->cbytes, osz = dir == 0 ? b->cbytes : b->gbytes;
-    for (const auto& k : b->buckets) {
-        const long long i0 = dir == 0 ? k.g0 : k.c0, o0 = dir == 0 ? k.c0 : k.g0;
-        const void* pin = (const char*)in + (size_t)i0 * isz;
-        void* pout = (char*)out + (size_t)o0 * osz;
-        // timing mode runs the buckets one after another on the caller's stream (exact stage times)
-        cudaStream_t s = b->timing ? st : b->streams[k.stream];
-        int rc = dir == 0 ? fftso3_forward(k.plan, pin, pout, s) : fftso3_inverse(k.plan, pin, pout, s);
-        if (rc) return rc;
-    }
+    return FFTSO3_SUCCESS;
+}
+
+int join_into(fftso3_batch* b, cudaStream_t st)
+{
+    cudaError_t e;
     for (size_t i = 0; i < b->streams.size(); ++i) {
         if ((e = cudaEventRecord(b->joined[i], b->streams[i])) != cudaSuccess) return bcuda(e, "cudaEventRecord");
         if ((e = cudaStreamWaitEvent(st, b->joined[i], 0)) != cudaSuccess) return bcuda(e, "cudaStreamWaitEvent");
     }
     return FFTSO3_SUCCESS;
+}
+
+// phase 0 (before the fused GEMM) or 1 (after it) of one bucket
+int bucket_phase(fftso3_batch* b, const fftso3_batch::Bucket& k, int dir, int phase, const void* pin, void* pout,
+                 cudaStream_t s)
+{
+    TCState* tc = plan_tc_state(k.plan);
+    StageTimer* T = plan_timer(k.plan);
+    std::string err;
+    int rc;
+    if (dir == 0)
+        rc = phase == 0 ? tc_forward_fft(tc, pin, s, T, err) : tc_forward_finish(tc, pout, s, T, err);
+    else
+        rc = phase == 0 ? tc_inverse_prepare(tc, pin, s, T, err) : tc_inverse_fft(tc, pout, s, T, err);
+    if (rc) return bfail(rc, err);
+    return FFTSO3_SUCCESS;
+}
+
+// fork from `st`, every bucket on its stream, join back into `st` (with a
+// fused GEMM: twice, around the one GEMM launch on `st`)
+int launch_all(fftso3_batch* b, int dir, const void* in, void* out, cudaStream_t st)
+{
+    int rc;
+    const size_t isz = dir == 0 ? b->gbytes : b->cbytes, osz = dir == 0 ? b->cbytes : b->gbytes;
+    auto ptrs = [&](const fftso3_batch::Bucket& k, const void*& pin, void*& pout) {
+        const long long i0 = dir == 0 ? k.g0 : k.c0, o0 = dir == 0 ? k.c0 : k.g0;
+        pin = (const char*)in + (size_t)i0 * isz;
+        pout = (char*)out + (size_t)o0 * osz;
+    };
+    // timing mode runs the buckets one after another on the caller's stream (exact stage times)
+    auto sof = [&](const fftso3_batch::Bucket& k) { return b->timing ? st : b->streams[k.stream]; };
+    if ((rc = fork_from(b, st))) return rc;
+    if (!b->fused) {
+        for (const auto& k : b->buckets) {
+            const void* pin;
+            void* pout;
+            ptrs(k, pin, pout);
+            rc = dir == 0 ? fftso3_forward(k.plan, pin, pout, sof(k)) : fftso3_inverse(k.plan, pin, pout, sof(k));
+            if (rc) return rc;
+        }
+        return join_into(b, st);
+    }
+    for (const auto& k : b->buckets) {
+        const void* pin;
+        void* pout;
+        ptrs(k, pin, pout);
+        if ((rc = bucket_phase(b, k, dir, 0, pin, pout, sof(k)))) return rc;
+    }
+    if ((rc = join_into(b, st))) return rc;
+    {
+        std::string err;
+        if ((rc = tc_fused_gemm(b->fused, dir == 0, st, &b->timer, err))) return bfail(rc, err);
+    }
+    if ((rc = fork_from(b, st))) return rc;
+    for (const auto& k : b->buckets) {
+        const void* pin;
+        void* pout;
+        ptrs(k, pin, pout);
+        if ((rc = bucket_phase(b, k, dir, 1, pin, pout, sof(k)))) return rc;
+    }
+    return join_into(b, st);
 }
 
 int run(fftso3_batch* b, int dir, const void* in, void* out, void* stream)
@@ -318,6 +385,16 @@ int fftso3_batch_create(fftso3_batch** out, int kind, const int* l_max, int n_fu
         return bail(bcuda(e, "cudaEventCreateWithFlags"));
     if ((e = cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking)) != cudaSuccess)
         return bail(bcuda(e, "cudaStreamCreateWithFlags"));
+    if (precision == FFTSO3_PREC_TC_BF16X3 && !(flags & FFTSO3_FLAG_REFINE)) {
+        std::vector<TCState*> parts;
+        for (auto& k : b->buckets) parts.push_back(plan_tc_state(k.plan));
+        std::string err;
+        int rc = tc_fused_create(&b->fused, parts, err);
+        if (rc) {
+            bail(rc);
+            return bfail(rc, err);
+        }
+    }
     *out = b;
     return FFTSO3_SUCCESS;
 }
@@ -379,6 +456,7 @@ int fftso3_batch_set_timing(fftso3_batch* b, int enable)
     for (auto& k : b->buckets)
         if ((rc = fftso3_plan_set_timing(k.plan, enable))) return rc;
     b->timing = enable != 0;
+    b->timer.enabled = enable != 0;
     return FFTSO3_SUCCESS;
 }
 
@@ -401,6 +479,14 @@ int fftso3_batch_stage_times(fftso3_batch* b, int bucket, double* ms_total, long
             if (launches) launches[s] += cnt[s];
         }
     }
+    if (bucket == -1) {  // the fused GEMM launches belong to no single bucket
+        b->timer.collect();
+        for (int s = 0; s < ns; ++s) {
+            if (ms_total) ms_total[s] += b->timer.total_ms[s];
+            if (launches) launches[s] += b->timer.launches[s];
+        }
+        if (reset) b->timer.reset();
+    }
     return FFTSO3_SUCCESS;
 }
 
@@ -410,6 +496,12 @@ int fftso3_batch_check(fftso3_batch* b)
     if (rc) return rc;
     for (auto& k : b->buckets)
         if ((rc = fftso3_plan_check(k.plan))) return rc;
+    if (b->fused) {
+        const int code = tc_fused_status(b->fused);
+        if (code != 0)
+            return bfail(FFTSO3_ERR_CUDA,
+                         "the fused tensor-core GEMM gave up a bounded wait (code " + std::to_string(code) + ")");
+    }
     return FFTSO3_SUCCESS;
 }
 

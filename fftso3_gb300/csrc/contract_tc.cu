@@ -211,6 +211,14 @@ struct GemmArgs {
     int* err;
 };
 
+// One plan's share of a fused launch over several plans (the l_max buckets of
+// an uneven batch): its table maps and arguments.  Work items of a fused launch
+// carry (segment << 16 | column tile) in .z.
+struct alignas(64) GemmSeg {
+    CUtensorMap tm[3];
+    GemmArgs a;
+};
+
 // Work items carry (group, row tile, column tile, m0 << 16 | (n0 + 32768)).
 __host__ __device__ __forceinline__ int item_w(int m0, int n0) { return (m0 << 16) | (n0 + 32768); }
 __device__ __forceinline__ void item_mn(const int4& it, int& m0, int& n0)
@@ -263,10 +271,14 @@ __device__ __forceinline__ GroupPairs s2_pairs(int m)
 // FWD = false: A = table^T (MN-major, rows k), B = Y from coefficients; D[k][c].
 // S2 = false: SO(3) Wigner-d groups, pencils [fn][p][q][k], 4 pairs per function;
 // S2 = true: S^2 Legendre groups (g = m), pencils [fn][p][k], 2 pairs per function.
-template <bool FWD, bool S2>
+// FUSED = true: the work list spans several plans (segments); each item's
+// table map, sizes and buffers come from segs[item.z >> 16] (args then holds
+// only the merged item list and the error word).
+template <bool FWD, bool S2, bool FUSED>
 __global__ void __launch_bounds__(THREADS, 1)
     so3_tc_gemm_kernel(const __grid_constant__ CUtensorMap tA0, const __grid_constant__ CUtensorMap tA1,
-                       const __grid_constant__ CUtensorMap tA2, GemmArgs args)
+                       const __grid_constant__ CUtensorMap tA2, const __grid_constant__ GemmArgs args,
+                       const GemmSeg* __restrict__ segs)
 {
     extern __shared__ unsigned char smem_raw[];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -279,9 +291,16 @@ __global__ void __launch_bounds__(THREADS, 1)
     float* wsm = (float*)(smem + STAGES * STAGE_BYTES + 256);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int B = args.L + 1, N = args.N;
     constexpr int PPF = S2 ? 2 : 4;        // pairs per function
     constexpr int FPTK = BN / (2 * PPF);   // functions per column tile
+    // per-item arguments and column tile
+    auto argsof = [&](const int4& it) -> const GemmArgs& { return FUSED ? segs[it.z >> 16].a : args; };
+    auto ctile = [&](const int4& it) { return FUSED ? (it.z & 0xFFFF) : it.z; };
+    auto nsteps = [&](const int4& it, const GemmArgs& A) {
+        int m0, n0;
+        item_mn(it, m0, n0);
+        return FWD ? A.Kp / BK : (A.L + 1 - m0 + BK - 1) / BK;
+    };
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
@@ -295,8 +314,8 @@ __global__ void __launch_bounds__(THREADS, 1)
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (FWD)
-        for (int i = threadIdx.x; i < N; i += THREADS) wsm[i] = args.wf[i];
+    if (FWD && !FUSED)
+        for (int i = threadIdx.x; i < args.N; i += THREADS) wsm[i] = args.wf[i];
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                      "r"(TMEM_COLS));
@@ -310,14 +329,15 @@ __global__ void __launch_bounds__(THREADS, 1)
     if (warp == 0) {
         if (lane == 0) {
             // ---------------- TMA producer of the table tiles
-            const CUtensorMap* tA[3] = {&tA0, &tA1, &tA2};
             int kc = 0;
             for (int it = blockIdx.x; it < args.nitems && !*abort_flag; it += gridDim.x) {
                 const int4 item = args.items[it];
-                int m0, n0;
-                item_mn(item, m0, n0);
-                const int nk = FWD ? args.Kp / BK : (B - m0 + BK - 1) / BK;
-                const long long row0 = args.grow0[item.x];
+                const GemmArgs& A = argsof(item);
+                const CUtensorMap* tA[3] = {FUSED ? &segs[item.z >> 16].tm[0] : &tA0,
+                                            FUSED ? &segs[item.z >> 16].tm[1] : &tA1,
+                                            FUSED ? &segs[item.z >> 16].tm[2] : &tA2};
+                const int nk = nsteps(item, A);
+                const long long row0 = A.grow0[item.x];
                 for (int i = 0; i < nk; ++i, ++kc) {
                     const int s = kc % STAGES;
                     if (kc >= STAGES && !mbar_wait(&empty[s], ((kc / STAGES) - 1) & 1, args.err, 1)) {
@@ -348,9 +368,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             int kc = 0, t = 0;
             for (int it = blockIdx.x; it < args.nitems && !*abort_flag; it += gridDim.x, ++t) {
                 const int4 item = args.items[it];
-                int m0, n0;
-                item_mn(item, m0, n0);
-                const int nk = FWD ? args.Kp / BK : (B - m0 + BK - 1) / BK;
+                const int nk = nsteps(item, argsof(item));
                 const int ab = t & 1;
                 if (t >= 2 && !mbar_wait(&acce[ab], ((t >> 1) - 1) & 1, args.err, 2)) {
                     *abort_flag = 1;
@@ -405,26 +423,32 @@ __global__ void __launch_bounds__(THREADS, 1)
         struct Src {
             const float2* p;  // run start for this (function, pair), or null
             int lim;          // valid extent of the run (N, or nl)
+            int N;            // the item's grid size (weights are zero beyond it)
+            const float* wf;  // the item's quadrature weights (fused launches)
         };
         auto source = [&](int it) -> Src {
             const int4 item = args.items[it];
+            const GemmArgs& A = argsof(item);
+            const int N = A.N;
             int m0, n0;
             item_mn(item, m0, n0);
             const GroupPairs P = S2 ? s2_pairs(m0) : group_pairs(m0, n0);
-            const int f = item.z * FPTK + fl;
+            const int f = ctile(item) * FPTK + fl;
             Src r;
-            r.lim = FWD ? N : B - m0;
+            r.lim = FWD ? N : A.L + 1 - m0;
+            r.N = N;
+            r.wf = A.wf;
             r.p = nullptr;
-            if (f >= args.batch || pp >= P.np) return r;
+            if (f >= A.batch || pp >= P.np) return r;
             if (FWD && S2) {
                 const int bin = pp == 0 ? m0 : N - m0;
-                r.p = args.pin + (long long)f * args.fstride + (long long)bin * N;
+                r.p = A.pin + (long long)f * A.fstride + (long long)bin * N;
             } else if (FWD) {
                 int pi = (-P.m[pp]) % N; if (pi < 0) pi += N;
                 int qi = (-P.n[pp]) % N; if (qi < 0) qi += N;
-                r.p = args.pin + (long long)f * args.fstride + ((long long)pi * N + qi) * N;
+                r.p = A.pin + (long long)f * A.fstride + ((long long)pi * N + qi) * N;
             } else {
-                r.p = args.cin + (long long)f * args.cstride + args.goff2[item.x] + (long long)pp * r.lim;
+                r.p = A.cin + (long long)f * A.cstride + A.goff2[item.x] + (long long)pp * r.lim;
             }
             return r;
         };
@@ -454,9 +478,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         int nk_cur = 0;
         if (it < args.nitems) {
             scur = source(it);
-            int m0, n0;
-            item_mn(args.items[it], m0, n0);
-            nk_cur = FWD ? args.Kp / BK : (B - m0 + BK - 1) / BK;
+            nk_cur = nsteps(args.items[it], argsof(args.items[it]));
             fetch(scur, 0, cur);
         }
         while (it < args.nitems && !*abort_flag) {
@@ -467,9 +489,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                 i2 = 0;
                 if (it2 < args.nitems) {
                     snxt = source(it2);
-                    int m0, n0;
-                    item_mn(args.items[it2], m0, n0);
-                    nk2 = FWD ? args.Kp / BK : (B - m0 + BK - 1) / BK;
+                    nk2 = nsteps(args.items[it2], argsof(args.items[it2]));
                 }
             }
             float2 nxt[16];
@@ -488,7 +508,8 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
                 for (int j = 0; j < 8; ++j) {
                     const float2 v = cur[h * 8 + j];
-                    const float wk = FWD ? ((k + j < N) ? wsm[k + j] : 0.f) : 1.f;
+                    const float wk =
+                        FWD ? ((k + j < scur.N) ? (FUSED ? __ldg(scur.wf + k + j) : wsm[k + j]) : 0.f) : 1.f;
                     re[j] = v.x * wk;
                     im[j] = v.y * wk;
                 }
@@ -513,15 +534,17 @@ __global__ void __launch_bounds__(THREADS, 1)
         int t = 0;
         for (int it = blockIdx.x; it < args.nitems && !*abort_flag; it += gridDim.x, ++t) {
             const int4 item = args.items[it];
+            const GemmArgs& A = argsof(item);
+            const int N = A.N;
             int m0, n0;
             item_mn(item, m0, n0);
             const GroupPairs P = S2 ? s2_pairs(m0) : group_pairs(m0, n0);
-            const int nl = B - m0;
+            const int nl = A.L + 1 - m0;
             long long poff[4];
 #pragma unroll
             for (int p = 0; p < 4; ++p) {
                 if (FWD) {
-                    poff[p] = args.goff2[item.x] + (long long)p * nl;
+                    poff[p] = A.goff2[item.x] + (long long)p * nl;
                 } else if (S2) {
                     int bin = (p == 0 ? -m0 : m0) % N; if (bin < 0) bin += N;
                     poff[p] = (long long)bin * N;
@@ -546,12 +569,12 @@ __global__ void __launch_bounds__(THREADS, 1)
                 for (int j = 0; j < 32; ++j) v[j] += u[j];
 #pragma unroll
                 for (int fq = 0; fq < 32 / (2 * PPF); ++fq) {
-                    const int f = item.z * FPTK + chunk * (32 / (2 * PPF)) + fq;
-                    if (f >= args.batch) continue;
+                    const int f = ctile(item) * FPTK + chunk * (32 / (2 * PPF)) + fq;
+                    if (f >= A.batch) continue;
                     if (FWD) {
                         const int row = item.y * BM + r;
                         if (row >= nl) continue;
-                        float2* Fo = args.cout + (long long)f * args.cstride + row;
+                        float2* Fo = A.cout + (long long)f * A.cstride + row;
 #pragma unroll
                         for (int p = 0; p < 4; ++p) {
                             if (p >= P.np) break;
@@ -561,7 +584,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                     } else {
                         const int k = item.y * BM + r;
                         if (k >= N) continue;
-                        float2* Ho = args.pout + (long long)f * args.fstride + k;
+                        float2* Ho = A.pout + (long long)f * A.fstride + k;
 #pragma unroll
                         for (int p = 0; p < 4; ++p) {
                             if (p >= P.np) break;
@@ -918,6 +941,7 @@ struct TCState {
     int4* d_items_fwd = nullptr;
     int4* d_items_inv = nullptr;
     int n_items_fwd = 0, n_items_inv = 0;
+    std::vector<int4> items_h[2];  // host copies (forward, inverse), for fused launches
     int nsm = 0;
     CUtensorMap tmA_fwd[3], tmA_inv[3];
     int* d_err = nullptr;
@@ -1078,6 +1102,8 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
     });
     s->n_items_fwd = (int)itf.size();
     s->n_items_inv = (int)iti.size();
+    s->items_h[0] = itf;
+    s->items_h[1] = iti;
     goff2[s->ngroups] = acc2;
     if (acc2 != C) {
         err = "internal: group-major layout does not cover the coefficients";
@@ -1103,9 +1129,12 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
         }
     }
     cudaError_t e = cudaSuccess;
-    const void* kernels[4] = {(const void*)so3_tc_gemm_kernel<true, false>, (const void*)so3_tc_gemm_kernel<false, false>,
-                              (const void*)so3_tc_gemm_kernel<true, true>, (const void*)so3_tc_gemm_kernel<false, true>};
-    for (int i = 0; i < 4 && e == cudaSuccess; ++i)
+    const void* kernels[8] = {
+        (const void*)so3_tc_gemm_kernel<true, false, false>, (const void*)so3_tc_gemm_kernel<false, false, false>,
+        (const void*)so3_tc_gemm_kernel<true, true, false>,  (const void*)so3_tc_gemm_kernel<false, true, false>,
+        (const void*)so3_tc_gemm_kernel<true, false, true>,  (const void*)so3_tc_gemm_kernel<false, false, true>,
+        (const void*)so3_tc_gemm_kernel<true, true, true>,   (const void*)so3_tc_gemm_kernel<false, true, true>};
+    for (int i = 0; i < 8 && e == cudaSuccess; ++i)
         e = cudaFuncSetAttribute(kernels[i], cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     if (e != cudaSuccess) {
         err = std::string("tensor-core kernel attributes: ") + cudaGetErrorString(e);
@@ -1296,13 +1325,13 @@ static int launch_gemm(TCState* s, bool fwd, cudaStream_t st, std::string& err)
     const int nctas = a.nitems < s->nsm ? a.nitems : s->nsm;
     const CUtensorMap* tm = fwd ? s->tmA_fwd : s->tmA_inv;
     if (fwd && s->s2)
-        so3_tc_gemm_kernel<true, true><<<nctas, THREADS, SMEM_BYTES, st>>>(tm[0], tm[1], tm[2], a);
+        so3_tc_gemm_kernel<true, true, false><<<nctas, THREADS, SMEM_BYTES, st>>>(tm[0], tm[1], tm[2], a, nullptr);
     else if (fwd)
-        so3_tc_gemm_kernel<true, false><<<nctas, THREADS, SMEM_BYTES, st>>>(tm[0], tm[1], tm[2], a);
+        so3_tc_gemm_kernel<true, false, false><<<nctas, THREADS, SMEM_BYTES, st>>>(tm[0], tm[1], tm[2], a, nullptr);
     else if (s->s2)
-        so3_tc_gemm_kernel<false, true><<<nctas, THREADS, SMEM_BYTES, st>>>(tm[0], tm[1], tm[2], a);
+        so3_tc_gemm_kernel<false, true, false><<<nctas, THREADS, SMEM_BYTES, st>>>(tm[0], tm[1], tm[2], a, nullptr);
     else
-        so3_tc_gemm_kernel<false, false><<<nctas, THREADS, SMEM_BYTES, st>>>(tm[0], tm[1], tm[2], a);
+        so3_tc_gemm_kernel<false, false, false><<<nctas, THREADS, SMEM_BYTES, st>>>(tm[0], tm[1], tm[2], a, nullptr);
     TCK(cudaGetLastError());
     return FFTSO3_SUCCESS;
 }
@@ -1489,6 +1518,188 @@ int tc_inverse(TCState* s, const void* coeffs, void* grid, cudaStream_t st, Stag
         Fc = s->d_fc;
     }
     return tc_inverse_once(s, Fc, grid, st, T, err);
+}
+
+// ---- phases of one direction, for launches fused across plans
+
+int tc_forward_fft(TCState* s, const void* grid, cudaStream_t st, StageTimer* T, std::string& err)
+{
+    return fft_forward(s, grid, st, T, err);
+}
+
+int tc_forward_finish(TCState* s, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err)
+{
+    float2* Fc = s->real ? s->d_fc : (float2*)coeffs;
+    T->begin(ST_BASIS, st);
+    if (s->s2)
+        s2_group_to_packed_kernel<<<dim3(s->B, s->batch), 256, 0, st>>>(s->d_fg, Fc, s->d_goff2, s->L,
+                                                                       coeffs_per_fn(s));
+    else
+        group_to_packed_kernel<<<dim3(s->B, s->batch), 256, 0, st>>>(s->d_fg, Fc, s->d_goff2, s->L,
+                                                                    coeffs_per_fn(s));
+    TCK(cudaGetLastError());
+    if (s->real) {
+        if (s->s2)
+            TCK(launch_s2_c2r(Fc, coeffs, false, s->L, s->batch, st));
+        else
+            TCK(launch_so3_c2r(Fc, coeffs, false, s->L, s->batch, st));
+    }
+    T->end(st);
+    return FFTSO3_SUCCESS;
+}
+
+int tc_inverse_prepare(TCState* s, const void* coeffs, cudaStream_t st, StageTimer* T, std::string& err)
+{
+    const float2* Fc = (const float2*)coeffs;
+    const long long N = s->N;
+    T->begin(ST_BASIS, st);
+    if (s->real) {
+        if (s->s2)
+            TCK(launch_s2_r2c(coeffs, s->d_fc, false, s->L, s->batch, st));
+        else
+            TCK(launch_so3_r2c(coeffs, s->d_fc, false, s->L, s->batch, st));
+        Fc = s->d_fc;
+    }
+    if (s->s2) {
+        const long long tot = (long long)s->batch * N;
+        s2_zero_nyquist_pencils_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(s->d_pencil, (int)N, s->batch);
+        s2_packed_to_group_kernel<<<dim3(s->ngroups, s->batch), 128, 0, st>>>(Fc, s->d_fg, s->d_goff2, s->L,
+                                                                             coeffs_per_fn(s));
+    } else {
+        const long long tot = (long long)s->batch * 2 * N * N;
+        zero_nyquist_pencils_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(s->d_pencil, (int)N, s->batch);
+        packed_to_group_kernel<<<dim3(s->ngroups, s->batch), 128, 0, st>>>(Fc, s->d_fg, s->d_goff2, s->L,
+                                                                          coeffs_per_fn(s));
+    }
+    TCK(cudaGetLastError());
+    T->end(st);
+    return FFTSO3_SUCCESS;
+}
+
+int tc_inverse_fft(TCState* s, void* grid, cudaStream_t st, StageTimer* T, std::string& err)
+{
+    return fft_inverse(s, grid, st, T, err);
+}
+
+struct TCFused {
+    std::vector<TCState*> parts;
+    GemmSeg* d_segs[2] = {nullptr, nullptr};  // forward, inverse
+    int4* d_items[2] = {nullptr, nullptr};
+    int nitems[2] = {0, 0};
+    int* d_err = nullptr;
+    int nsm = 0;
+    bool s2 = false;
+};
+
+void tc_fused_destroy(TCFused* f)
+{
+    if (!f) return;
+    for (int d = 0; d < 2; ++d) {
+        if (f->d_segs[d]) cudaFree(f->d_segs[d]);
+        if (f->d_items[d]) cudaFree(f->d_items[d]);
+    }
+    if (f->d_err) cudaFree(f->d_err);
+    delete f;
+}
+
+// One work list over the tensor-core plans `parts` (same kind, at most 32768
+// plans): items of plan i carry segment i; sorted by decreasing k-steps so the
+// longest items start first on the persistent CTAs.
+int tc_fused_create(TCFused** out, const std::vector<TCState*>& parts, std::string& err)
+{
+    *out = nullptr;
+    if (parts.empty() || parts.size() > 32768) {
+        err = "fused launch: 1 to 32768 plans";
+        return FFTSO3_ERR_INVALID_ARG;
+    }
+    for (TCState* p : parts)
+        if (!p || p->simt || p->s2 != parts[0]->s2 || p->ntiles > 0xFFFF) {
+            err = "fused launch: all plans must be tensor-core plans of one family (SO(3) or S^2)";
+            return FFTSO3_ERR_INVALID_ARG;
+        }
+    TCFused* f = new TCFused();
+    f->parts = parts;
+    f->s2 = parts[0]->s2;
+    f->nsm = parts[0]->nsm;
+    auto fail = [&](cudaError_t e, const char* what) {
+        err = std::string(what) + ": " + cudaGetErrorString(e);
+        tc_fused_destroy(f);
+        return FFTSO3_ERR_CUDA;
+    };
+    cudaError_t e;
+    for (int d = 0; d < 2; ++d) {
+        const bool fwd = d == 0;
+        std::vector<GemmSeg> segs(parts.size());
+        std::vector<std::pair<int, int4>> items;
+        for (size_t i = 0; i < parts.size(); ++i) {
+            TCState* p = parts[i];
+            GemmArgs a = gemm_args(p);
+            if (fwd) {
+                a.pin = p->d_pencil;
+                a.cout = p->d_fg;
+            } else {
+                a.cin = p->d_fg;
+                a.pout = p->d_pencil;
+            }
+            segs[i].a = a;
+            for (int q = 0; q < 3; ++q) segs[i].tm[q] = fwd ? p->tmA_fwd[q] : p->tmA_inv[q];
+            for (const int4& it : p->items_h[d]) {
+                const int m0 = it.w >> 16;
+                const int nk = fwd ? p->Kp / BK : (p->B - m0 + BK - 1) / BK;
+                items.push_back({nk, make_int4(it.x, it.y, ((int)i << 16) | it.z, it.w)});
+            }
+        }
+        std::stable_sort(items.begin(), items.end(),
+                         [](const std::pair<int, int4>& a, const std::pair<int, int4>& b) { return a.first > b.first; });
+        std::vector<int4> flat(items.size());
+        for (size_t i = 0; i < items.size(); ++i) flat[i] = items[i].second;
+        f->nitems[d] = (int)flat.size();
+        if ((e = cudaMalloc(&f->d_segs[d], sizeof(GemmSeg) * segs.size())) != cudaSuccess) return fail(e, "cudaMalloc");
+        if ((e = cudaMalloc(&f->d_items[d], sizeof(int4) * std::max<size_t>(flat.size(), 1))) != cudaSuccess)
+            return fail(e, "cudaMalloc");
+        if ((e = cudaMemcpy(f->d_segs[d], segs.data(), sizeof(GemmSeg) * segs.size(), cudaMemcpyHostToDevice)) !=
+            cudaSuccess)
+            return fail(e, "cudaMemcpy");
+        if (!flat.empty() && (e = cudaMemcpy(f->d_items[d], flat.data(), sizeof(int4) * flat.size(),
+                                             cudaMemcpyHostToDevice)) != cudaSuccess)
+            return fail(e, "cudaMemcpy");
+    }
+    if ((e = cudaMalloc(&f->d_err, sizeof(int))) != cudaSuccess) return fail(e, "cudaMalloc");
+    cudaMemset(f->d_err, 0, sizeof(int));
+    *out = f;
+    return FFTSO3_SUCCESS;
+}
+
+// The beta-sum GEMM of every plan of `f` in one persistent launch.
+int tc_fused_gemm(TCFused* f, bool fwd, cudaStream_t st, StageTimer* T, std::string& err)
+{
+    const int d = fwd ? 0 : 1;
+    if (f->nitems[d] == 0) return FFTSO3_SUCCESS;
+    GemmArgs a = gemm_args(f->parts[0]);
+    a.items = f->d_items[d];
+    a.nitems = f->nitems[d];
+    a.err = f->d_err;
+    const int nctas = a.nitems < f->nsm ? a.nitems : f->nsm;
+    const CUtensorMap* tm = fwd ? f->parts[0]->tmA_fwd : f->parts[0]->tmA_inv;  // unused by fused kernels
+    T->begin(fwd ? ST_GEMM_FWD : ST_GEMM_INV, st);
+    if (fwd && f->s2)
+        so3_tc_gemm_kernel<true, true, true><<<nctas, THREADS, SMEM_BYTES, st>>>(tm[0], tm[1], tm[2], a, f->d_segs[d]);
+    else if (fwd)
+        so3_tc_gemm_kernel<true, false, true><<<nctas, THREADS, SMEM_BYTES, st>>>(tm[0], tm[1], tm[2], a, f->d_segs[d]);
+    else if (f->s2)
+        so3_tc_gemm_kernel<false, true, true><<<nctas, THREADS, SMEM_BYTES, st>>>(tm[0], tm[1], tm[2], a, f->d_segs[d]);
+    else
+        so3_tc_gemm_kernel<false, false, true><<<nctas, THREADS, SMEM_BYTES, st>>>(tm[0], tm[1], tm[2], a, f->d_segs[d]);
+    TCK(cudaGetLastError());
+    T->end(st);
+    return FFTSO3_SUCCESS;
+}
+
+int tc_fused_status(TCFused* f)
+{
+    int h = 0;
+    if (cudaMemcpy(&h, f->d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+    return h;
 }
 
 int tc_status(TCState* s)

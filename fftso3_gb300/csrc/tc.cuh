@@ -4,6 +4,7 @@
 #include <string>
 #include <vector>
 
+#include "../../include/fftso3_gb300.h"
 #include "fft.cuh"
 #include "timing.cuh"
 
@@ -20,5 +21,24 @@ int tc_forward(TCState* s, const void* grid, void* coeffs, cudaStream_t st, Stag
 int tc_inverse(TCState* s, const void* coeffs, void* grid, cudaStream_t st, StageTimer* T, std::string& err);
 // Device error word of the tensor-core kernels (0 = no bounded wait timed out); synchronising read.
 int tc_status(TCState* s);
+
+// Phases of one direction, so that several plans can share one GEMM launch:
+//   forward = tc_forward_fft, GEMM, tc_forward_finish (no refinement);
+//   inverse = tc_inverse_prepare, GEMM, tc_inverse_fft.
+int tc_forward_fft(TCState* s, const void* grid, cudaStream_t st, StageTimer* T, std::string& err);
+int tc_forward_finish(TCState* s, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err);
+int tc_inverse_prepare(TCState* s, const void* coeffs, cudaStream_t st, StageTimer* T, std::string& err);
+int tc_inverse_fft(TCState* s, void* grid, cudaStream_t st, StageTimer* T, std::string& err);
+
+// One persistent tensor-core GEMM launch over the work items of several plans.
+struct TCFused;
+int tc_fused_create(TCFused** out, const std::vector<TCState*>& parts, std::string& err);
+void tc_fused_destroy(TCFused* f);
+int tc_fused_gemm(TCFused* f, bool fwd, cudaStream_t st, StageTimer* T, std::string& err);
+int tc_fused_status(TCFused* f);
+
+// A plan's tensor-core state (null for FP64 plans) and stage timer (api.cu).
+TCState* plan_tc_state(fftso3_plan* p);
+StageTimer* plan_timer(fftso3_plan* p);
 
 }  // namespace fftso3

@@ -141,3 +141,35 @@ def test_autotuned_plan_and_batch(gblib, oracle, torch_cuda):
     co = c2.cpu().numpy().astype(np.float64)
     for i in range(len(lmax)):
         assert rel_err(co[b.coeff_offset(i):b.coeff_offset(i) + Fs[i].size], Fs[i]) < TOL
+
+
+def test_fused_gemm_batch_equals_bucket_plans(gblib, torch_cuda):
+    """A tensor-core batch runs one GEMM launch over all buckets; every item is computed exactly as the
+    bucket's own plan computes it, so the results are bit-identical to one plan per l_max (complex SO(3))."""
+    torch = torch_cuda
+    s = torch.cuda.current_stream().cuda_stream
+    lmax = [12, 20, 12, 31, 20, 12]
+    kind = gblib.SO3_COMPLEX
+    b = gblib.Batch(kind, lmax, "tc_bf16x3", "reference", 0)
+    Fs = [so3_coeffs(L, seed=1700 + i, decay="pow").astype(np.complex64) for i, L in enumerate(lmax)]
+    cbuf = np.zeros(b.coeff_elems, dtype=np.complex64)
+    for i in range(len(lmax)):
+        cbuf[b.coeff_offset(i):b.coeff_offset(i) + Fs[i].size] = Fs[i]
+    c = torch.from_numpy(cbuf).cuda()
+    g = torch.empty(b.grid_elems, dtype=torch.complex64, device="cuda")
+    c2 = torch.empty_like(c)
+    b.inverse(c.data_ptr(), g.data_ptr(), s)
+    b.forward(g.data_ptr(), c2.data_ptr(), s)
+    b.check()
+    for L in sorted(set(lmax)):
+        idx = [i for i in range(len(lmax)) if lmax[i] == L]
+        p = gblib.Plan(kind, L, len(idx), "tc_bf16x3", "reference")
+        g0, c0 = b.grid_offset(idx[0]), b.coeff_offset(idx[0])
+        n_g, n_c = len(idx) * p.grid_elems, len(idx) * p.coeff_elems
+        gp = torch.empty(n_g, dtype=torch.complex64, device="cuda")
+        cp = torch.empty(n_c, dtype=torch.complex64, device="cuda")
+        p.inverse(c[c0:c0 + n_c].data_ptr(), gp.data_ptr(), s)
+        p.forward(g[g0:g0 + n_g].data_ptr(), cp.data_ptr(), s)
+        p.check()
+        assert torch.equal(gp, g[g0:g0 + n_g])
+        assert torch.equal(cp, c2[c0:c0 + n_c])
