@@ -65,6 +65,8 @@ SIGNATURES = {
     "fftso3_inverse_points": (_i, [_vp, _vp, _i, _dp, _i, _vp, _vp]),
     "fftso3_wigner_d": (_i, [_d, _i, _i, _dp]),
     "fftso3_forward_noalloc": (_i, [_i, _vp, _vp, _vp]),
+    "fftso3_correlate_s2": (_i, [_vp, _vp, _vp, _vp, _vp]),
+    "fftso3_grid_argmax": (_i, [_vp, _vp, ctypes.POINTER(_ll), _dp, _vp]),
     "fftso3_batch_create": (_i, [ctypes.POINTER(_vp), _i, ctypes.POINTER(_i), _i, _i, _i, ctypes.c_uint]),
     "fftso3_batch_destroy": (_i, [_vp]),
     "fftso3_batch_grid_offset": (_ll, [_vp, _i]),
@@ -159,6 +161,16 @@ class Plan:
     def inverse_points(self, coeff_ptr: int, index: int, pts, n: int, out_ptr: int, stream: int = 0) -> None:
         check(lib().fftso3_inverse_points(self._h, _vp(coeff_ptr), int(index), pts, int(n), _vp(out_ptr),
                                           _vp(stream)))
+
+    def correlate_s2(self, F_ptr: int, G_ptr: int, grid_ptr: int, stream: int = 0) -> None:
+        check(lib().fftso3_correlate_s2(self._h, _vp(F_ptr), _vp(G_ptr), _vp(grid_ptr), _vp(stream)))
+
+    def grid_argmax(self, grid_ptr: int, stream: int = 0) -> tuple:
+        """(flat indices, values) of the maximum of each of the batch's real grids."""
+        idx = (_ll * self.batch)()
+        val = (ctypes.c_double * self.batch)()
+        check(lib().fftso3_grid_argmax(self._h, _vp(grid_ptr), idx, val, _vp(stream)))
+        return list(idx), list(val)
 
     def set_timing(self, enable: bool = True) -> None:
         check(lib().fftso3_plan_set_timing(self._h, 1 if enable else 0))

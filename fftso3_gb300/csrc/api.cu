@@ -114,6 +114,8 @@ struct fftso3_plan {
     void* d_fc = nullptr;          // complex coefficients of the real kinds
     void* d_io_grid = nullptr;     // staging for the *_host calls
     void* d_io_coeff = nullptr;
+    void* d_corr = nullptr;        // correlation coefficients (fftso3_correlate_s2)
+    void* d_amax = nullptr;        // arg-max scratch (fftso3_grid_argmax)
     long long bytes = 0;
     TCState* tc = nullptr;         // tensor-core contraction state
     StageTimer timer;              // optional per-stage CUDA-event timing
@@ -140,7 +142,7 @@ int plan_alloc(fftso3_plan* p, void** ptr, size_t bytes)
 void plan_free(fftso3_plan* p)
 {
     void* ptrs[] = {p->d_tw, p->d_w, p->d_goff, p->d_table, p->d_lfact, p->d_work, p->d_fc, p->d_io_grid,
-                    p->d_io_coeff};
+                    p->d_io_coeff, p->d_corr, p->d_amax};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     if (p->tc) tc_destroy(p->tc);
@@ -548,6 +550,38 @@ int fftso3_inverse_host(fftso3_plan* plan, const void* coeffs_host, void* grid_h
     CK(cudaMemcpyAsync(plan->d_io_coeff, coeffs_host, coeff_bytes(plan), cudaMemcpyHostToDevice, st));
     if ((rc = run_inverse(plan, plan->d_io_coeff, plan->d_io_grid, st))) return rc;
     CK(cudaMemcpyAsync(grid_host, plan->d_io_grid, grid_bytes(plan), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return FFTSO3_SUCCESS;
+}
+
+int fftso3_correlate_s2(fftso3_plan* plan, const void* F_s2, const void* G_s2, void* grid, void* stream)
+{
+    int rc = check_plan(plan);
+    if (rc) return rc;
+    if (plan->kind != FFTSO3_SO3_REAL)
+        return fail(FFTSO3_ERR_INVALID_ARG, "correlation needs an FFTSO3_SO3_REAL plan");
+    if (!F_s2 || !G_s2 || !grid) return fail(FFTSO3_ERR_INVALID_ARG, "NULL pointer argument");
+    if (!plan->d_corr && (rc = plan_alloc(plan, &plan->d_corr, coeff_bytes(plan)))) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    CK(launch_corr_coeffs(F_s2, G_s2, plan->d_corr, plan->fp64, plan->L, plan->batch, st));
+    return run_inverse(plan, plan->d_corr, grid, st);
+}
+
+int fftso3_grid_argmax(fftso3_plan* plan, const void* grid, long long* index_out, double* value_out, void* stream)
+{
+    int rc = check_plan(plan);
+    if (rc) return rc;
+    if (!plan->real) return fail(FFTSO3_ERR_INVALID_ARG, "arg-max needs a real-kind plan");
+    if (!grid || !index_out) return fail(FFTSO3_ERR_INVALID_ARG, "NULL pointer argument");
+    const int chunks = 256, nb = plan->batch;
+    const size_t sb = argmax_scratch_bytes(nb, chunks);
+    if (!plan->d_amax && (rc = plan_alloc(plan, &plan->d_amax, sb))) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    double* ov = (double*)((char*)plan->d_amax + (size_t)nb * chunks * 16);
+    long long* oi = (long long*)(ov + nb);
+    CK(launch_argmax(grid, plan->fp64, plan->grid_elems, nb, chunks, plan->d_amax, ov, oi, st));
+    CK(cudaMemcpyAsync(index_out, oi, sizeof(long long) * nb, cudaMemcpyDeviceToHost, st));
+    if (value_out) CK(cudaMemcpyAsync(value_out, ov, sizeof(double) * nb, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     return FFTSO3_SUCCESS;
 }

@@ -20,4 +20,11 @@ cudaError_t launch_zero_nyquist_s2(void* H, bool fp64, int N, long long nrows, c
 cudaError_t launch_s2_c2r(const void* Fc, void* Fr, bool fp64, int L, int batch, cudaStream_t st);
 cudaError_t launch_s2_r2c(const void* Fr, void* Fc, bool fp64, int L, int batch, cudaStream_t st);
 
+// S^2 -> SO(3) correlation coefficients Fr(l,m,n) = G_l(m) F_l(n) / (2l+1) (correlate.cu)
+cudaError_t launch_corr_coeffs(const void* F, const void* G, void* C, bool fp64, int L, int batch, cudaStream_t st);
+// per-array arg-max (value, flat index) of nb real arrays of n elements; ov, oi device arrays of nb
+size_t argmax_scratch_bytes(int nb, int chunks);
+cudaError_t launch_argmax(const void* x, bool fp64, long long n, int nb, int chunks, void* scratch, double* ov,
+                          long long* oi, cudaStream_t st);
+
 }  // namespace fftso3

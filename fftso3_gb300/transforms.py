@@ -299,3 +299,30 @@ class FFTS2_real(FFTS2_complex):
         F.setRandom(rng)
         G = self.forward_transform(self.inverse_grid(F))
         return (F - G).norm()
+
+
+def correlate_s2(F, G, *, precision: str = "fp64", recursion: str = "reference"):
+    """S^2 -> SO(3) correlation of two real spherical functions (shape matching).
+
+    F, G: FFTS2_matrix_real of one l_max.  Returns (J, (alpha, beta, gamma), R): J the
+    score J(R) = sum_l G[l]^T U^l(R) F[l] on the whole (2B)^3 Euler grid (the cost of
+    the reference's shape-matching example, example/example3_SSM.hpp), and the grid
+    rotation that maximises it, as Euler 3-2-3 angles and as a rotation matrix.
+    """
+    import torch
+
+    if F.l_max != G.l_max:
+        raise ValueError("F and G must have the same l_max")
+    L = F.l_max
+    N = 2 * (L + 1)
+    plan = _lib.Plan(_lib.SO3_REAL, L, 1, precision, recursion)
+    dt = torch.float64 if precision == "fp64" else torch.float32
+    f = torch.from_numpy(np.ascontiguousarray(F.M, dtype=np.float64)).to(device="cuda", dtype=dt)
+    g = torch.from_numpy(np.ascontiguousarray(G.M, dtype=np.float64)).to(device="cuda", dtype=dt)
+    grid = torch.empty(N ** 3, dtype=dt, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    plan.correlate_s2(f.data_ptr(), g.data_ptr(), grid.data_ptr(), s)
+    (idx,), _ = plan.grid_argmax(grid.data_ptr(), s)
+    k, j1, j2 = idx // (N * N), (idx // N) % N, idx % N
+    abg = (float(alpha_j(L, j1)), float(beta_k(L, k)), float(alpha_j(L, j2)))
+    return grid.cpu().numpy().astype(np.float64).reshape(N, N, N), abg, euler323_to_R(*abg)

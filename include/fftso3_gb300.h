@@ -146,6 +146,26 @@ int fftso3_inverse_host(fftso3_plan* plan, const void* coeffs_host, void* grid_h
 int fftso3_inverse_points(fftso3_plan* plan, const void* coeffs, int index, const double* pts, int n, void* out,
                           void* stream);
 
+/* S^2 -> SO(3) correlation (spherical shape matching).  For `batch` pairs of
+ * real S^2 coefficient vectors F, G (device, [batch][B^2], packed like
+ * FFTS2_matrix_real, float64 for FP64 plans, float32 otherwise), writes to the
+ * device grid of a FFTSO3_SO3_REAL plan the score of every grid rotation R,
+ *   J(R) = sum_l G[l]^T U^l(R) F[l]
+ * (U^l the real harmonics of R, fdcl_FFTSO3.cpp:1062-1105) -- the cost the
+ * reference's example evaluates one rotation at a time
+ * (example/example3_SSM.hpp, J(R); example/example3.cpp:28-95).  It forms the
+ * real SO(3) coefficients Fr(l,m,n) = G_l(m) F_l(n) / (2l+1) and runs the
+ * plan's inverse transform.  Asynchronous on `stream`. */
+int fftso3_correlate_s2(fftso3_plan* plan, const void* F_s2, const void* G_s2, void* grid, void* stream);
+
+/* Arg-max of each of the plan's `batch` real grids (device): flat grid index
+ * (k N^2 + j1 N + j2 for SO(3), k N + j for S^2; ties -> smallest index) and
+ * value, written to host arrays of `batch` entries (value_out may be NULL);
+ * synchronises `stream`.  With fftso3_correlate_s2 it gives the best rotation
+ * (alpha_j1, beta_k, gamma_j2) to the grid's resolution.  No reference
+ * counterpart (the reference descends the gradient from an initial guess). */
+int fftso3_grid_argmax(fftso3_plan* plan, const void* grid, long long* index_out, double* value_out, void* stream);
+
 /* Wigner-d table d^l_mn(beta) for all l <= l_max at one angle, packed like
  * the SO(3) coefficients, computed on the GPU (host output buffer).
  * Replaces wigner_d(beta) (fdcl_FFTSO3.cpp:122-194). */
