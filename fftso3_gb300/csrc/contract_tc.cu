@@ -806,45 +806,101 @@ __device__ __forceinline__ void pair_of(int m, int n, int& g, int& p)
     g = m0 * m0 + m0 + n0;
 }
 
-// Group-major forward output -> packed coefficients (one CTA per (l, function)).
-__global__ void group_to_packed_kernel(const float2* __restrict__ Fg, float2* __restrict__ F,
-                                       const long long* __restrict__ goff2, int L, long long cstride)
+
+// Tiled permutations between the group-major layout (contiguous in l for a
+// fixed (m, n)) and the packed layout (contiguous in m for a fixed (l, n)):
+// one CTA per (function, n, 32 l's, 32 m's) stages the tile in shared memory,
+// so both sides move runs of 32 consecutive elements.  The group of (m, n) has
+// m0 = max(|m|, |n|) and rows l = m0..L; the pair index and sign follow
+// group_pairs() (pair_of()).
+constexpr int PT = 32;
+
+// grid: x = n + L (2L + 1), y = l tile (ceil(B / 32)), z = m tile + mtiles * function
+__device__ __forceinline__ bool ptile_coords(int L, int& n, int& l0, int& mb, int& f)
 {
-    const int l = blockIdx.x, f = blockIdx.y;
-    const int W = 2 * l + 1;
-    const int B = L + 1;
+    const int mtiles = (2 * L + 1 + PT - 1) / PT;
+    n = (int)blockIdx.x - L;
+    l0 = (int)blockIdx.y * PT;
+    mb = -L + (int)(blockIdx.z % mtiles) * PT;
+    f = (int)(blockIdx.z / mtiles);
+    const int an = n < 0 ? -n : n;
+    const int amin = (mb <= 0 && mb + PT - 1 >= 0) ? 0 : min(abs(mb), abs(mb + PT - 1));
+    // some (l, m) of the tile must satisfy l >= max(|m|, |n|)
+    return l0 + PT - 1 >= max(an, amin) && l0 <= L;
+}
+
+// group-major pair (g, p) of (m, n) and its group's first degree m0 (consistent with group_pairs)
+__device__ __forceinline__ void pair_m0(int m, int n, int& g, int& p, int& m0, int& sign)
+{
+    pair_of(m, n, g, p);
+    m0 = max(abs(m), abs(n));
+    const int n0 = g - m0 * m0 - m0;
+    sign = ((p == 1 || p == 2) && ((m0 + n0) & 1)) ? -1 : 1;
+}
+
+__global__ void __launch_bounds__(256) group_to_packed_tiled(const float2* __restrict__ Fg, float2* __restrict__ F,
+                                                             const long long* __restrict__ goff2, int L,
+                                                             long long cstride)
+{
+    __shared__ float2 tile[PT][PT + 1];  // [m - mb][l - l0]
+    int n, l0, mb, f;
+    if (!ptile_coords(L, n, l0, mb, f)) return;
+    const int B = L + 1, an = abs(n);
     const float2* src = Fg + (long long)f * cstride;
-    float2* dst = F + (long long)f * cstride + so3_off(l);
-    for (int i = threadIdx.x; i < W * W; i += blockDim.x) {
-        const int m = i % W - l, n = i / W - l;
-        int g, p;
-        pair_of(m, n, g, p);
-        const int m0 = (int)sqrtf((float)g + 0.5f) - 1;
-        int mm = m0 < 0 ? 0 : m0;
-        while ((mm + 1) * (mm + 1) <= g) ++mm;
-        while (mm * mm > g) --mm;
-        const int nl = B - mm;
-        dst[i] = src[goff2[g] + (long long)p * nl + (l - mm)];
+    // gather: lanes run along l (contiguous in the group-major layout)
+    for (int e = threadIdx.x; e < PT * PT; e += blockDim.x) {
+        const int mi = e / PT, li = e % PT;
+        const int m = mb + mi, l = l0 + li;
+        if (m > L || l > L || l < abs(m) || l < an) continue;
+        int g, pp, m0, sg;
+        pair_m0(m, n, g, pp, m0, sg);
+        tile[mi][li] = src[goff2[g] + (long long)pp * (B - m0) + (l - m0)];
+    }
+    __syncthreads();
+    // scatter: lanes run along m (contiguous in the packed layout)
+    float2* dst = F + (long long)f * cstride;
+    for (int e = threadIdx.x; e < PT * PT; e += blockDim.x) {
+        const int li = e / PT, mi = e % PT;
+        const int m = mb + mi, l = l0 + li;
+        if (m > L || l > L || l < abs(m) || l < an) continue;
+        dst[so3_idx(l, m, n)] = tile[mi][li];
     }
 }
 
-// Packed coefficients -> scaled group-major Y = (2l+1) sign F(l, pair) (one CTA per (group, function)).
-__global__ void packed_to_group_kernel(const float2* __restrict__ F, float2* __restrict__ Y,
-                                       const long long* __restrict__ goff2, int L, long long cstride)
+// packed -> scaled group-major Y = (2l+1) sign F(l, pair)
+__global__ void __launch_bounds__(256) packed_to_group_tiled(const float2* __restrict__ F, float2* __restrict__ Y,
+                                                             const long long* __restrict__ goff2, int L,
+                                                             long long cstride)
 {
-    const int g = blockIdx.x, f = blockIdx.y;
-    int m0, n0;
-    group_mn(g, m0, n0);
-    const GroupPairs P = group_pairs(m0, n0);
-    const int nl = L + 1 - m0;
+    __shared__ float2 tile[PT][PT + 1];  // [m - mb][l - l0]
+    int n, l0, mb, f;
+    if (!ptile_coords(L, n, l0, mb, f)) return;
+    const int B = L + 1, an = abs(n);
     const float2* src = F + (long long)f * cstride;
-    float2* dst = Y + (long long)f * cstride + goff2[g];
-    for (int i = threadIdx.x; i < P.np * nl; i += blockDim.x) {
-        const int p = i / nl, lp = i - p * nl, l = m0 + lp;
-        const float2 v = src[so3_idx(l, P.m[p], P.n[p])];
-        const float sc = (float)(2 * l + 1) * (float)P.sign[p];
-        dst[i] = make_float2(sc * v.x, sc * v.y);
+    for (int e = threadIdx.x; e < PT * PT; e += blockDim.x) {
+        const int li = e / PT, mi = e % PT;
+        const int m = mb + mi, l = l0 + li;
+        if (m > L || l > L || l < abs(m) || l < an) continue;
+        tile[mi][li] = src[so3_idx(l, m, n)];
     }
+    __syncthreads();
+    float2* dst = Y + (long long)f * cstride;
+    for (int e = threadIdx.x; e < PT * PT; e += blockDim.x) {
+        const int mi = e / PT, li = e % PT;
+        const int m = mb + mi, l = l0 + li;
+        if (m > L || l > L || l < abs(m) || l < an) continue;
+        int g, pp, m0, sg;
+        pair_m0(m, n, g, pp, m0, sg);
+        const float sc = (float)(2 * l + 1) * (float)sg;
+        const float2 v = tile[mi][li];
+        dst[goff2[g] + (long long)pp * (B - m0) + (l - m0)] = make_float2(sc * v.x, sc * v.y);
+    }
+}
+
+static dim3 ptile_grid(int L, int batch)
+{
+    const int mtiles = (2 * L + 1 + PT - 1) / PT;
+    return dim3((unsigned)(2 * L + 1), (unsigned)((L + 1 + PT - 1) / PT), (unsigned)(mtiles * batch));
 }
 
 // S^2: group-major forward output -> packed F(l, m) at l^2 + m + l (one CTA per (l, function)).
@@ -1028,6 +1084,11 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
     s->batch = batch;
     s->s2 = s2;
     s->simt = simt;
+    if (!s2 && (long long)((2 * L + 1 + 31) / 32) * batch > 65535) {
+        err = "batch too large for this l_max (at most 65535 / ceil((2 l_max + 1) / 32) functions per plan)";
+        delete s;
+        return FFTSO3_ERR_UNSUPPORTED;
+    }
     s->ntiles = s2 ? (batch + FPT_S2 - 1) / FPT_S2 : (batch + FPT - 1) / FPT;
     s->ngroups = s2 ? s->B : s->B * s->B;
     s->refine = refine;
@@ -1431,7 +1492,7 @@ static int tc_forward_once(TCState* s, const void* grid, float2* F, cudaStream_t
         s2_group_to_packed_kernel<<<dim3(s->B, s->batch), 256, 0, st>>>(s->d_fg, F, s->d_goff2, s->L,
                                                                        coeffs_per_fn(s));
     else
-        group_to_packed_kernel<<<dim3(s->B, s->batch), 256, 0, st>>>(s->d_fg, F, s->d_goff2, s->L,
+        group_to_packed_tiled<<<ptile_grid(s->L, s->batch), 256, 0, st>>>(s->d_fg, F, s->d_goff2, s->L,
                                                                     coeffs_per_fn(s));
     TCK(cudaGetLastError());
     T->end(st);
@@ -1457,7 +1518,7 @@ static int tc_inverse_once(TCState* s, const float2* F, void* grid, cudaStream_t
         s2_packed_to_group_kernel<<<dim3(s->ngroups, s->batch), 128, 0, st>>>(F, s->d_fg, s->d_goff2, s->L,
                                                                              coeffs_per_fn(s));
     else
-        packed_to_group_kernel<<<dim3(s->ngroups, s->batch), 128, 0, st>>>(F, s->d_fg, s->d_goff2, s->L,
+        packed_to_group_tiled<<<ptile_grid(s->L, s->batch), 256, 0, st>>>(F, s->d_fg, s->d_goff2, s->L,
                                                                           coeffs_per_fn(s));
     TCK(cudaGetLastError());
     T->end(st);
@@ -1535,7 +1596,7 @@ int tc_forward_finish(TCState* s, void* coeffs, cudaStream_t st, StageTimer* T, 
         s2_group_to_packed_kernel<<<dim3(s->B, s->batch), 256, 0, st>>>(s->d_fg, Fc, s->d_goff2, s->L,
                                                                        coeffs_per_fn(s));
     else
-        group_to_packed_kernel<<<dim3(s->B, s->batch), 256, 0, st>>>(s->d_fg, Fc, s->d_goff2, s->L,
+        group_to_packed_tiled<<<ptile_grid(s->L, s->batch), 256, 0, st>>>(s->d_fg, Fc, s->d_goff2, s->L,
                                                                     coeffs_per_fn(s));
     TCK(cudaGetLastError());
     if (s->real) {
@@ -1568,7 +1629,7 @@ int tc_inverse_prepare(TCState* s, const void* coeffs, cudaStream_t st, StageTim
     } else {
         const long long tot = (long long)s->batch * 2 * N * N;
         zero_nyquist_pencils_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(s->d_pencil, (int)N, s->batch);
-        packed_to_group_kernel<<<dim3(s->ngroups, s->batch), 128, 0, st>>>(Fc, s->d_fg, s->d_goff2, s->L,
+        packed_to_group_tiled<<<ptile_grid(s->L, s->batch), 256, 0, st>>>(Fc, s->d_fg, s->d_goff2, s->L,
                                                                           coeffs_per_fn(s));
     }
     TCK(cudaGetLastError());
