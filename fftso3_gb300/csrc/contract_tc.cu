@@ -815,18 +815,21 @@ __device__ __forceinline__ void pair_of(int m, int n, int& g, int& p)
 // group_pairs() (pair_of()).
 constexpr int PT = 32;
 
-// grid: x = n + L (2L + 1), y = l tile (ceil(B / 32)), z = m tile + mtiles * function
+// grid: x = n + L (2L + 1), y = l tile (ceil(B / 32)), z = m tile + mtiles * function.
+// The m tiles of l tile [l0, l0 + 32) cover only |m| <= min(L, l0 + 31), so
+// small degrees do not run mostly empty tiles.
 __device__ __forceinline__ bool ptile_coords(int L, int& n, int& l0, int& mb, int& f)
 {
     const int mtiles = (2 * L + 1 + PT - 1) / PT;
     n = (int)blockIdx.x - L;
     l0 = (int)blockIdx.y * PT;
-    mb = -L + (int)(blockIdx.z % mtiles) * PT;
     f = (int)(blockIdx.z / mtiles);
+    const int t = (int)(blockIdx.z % mtiles);
+    const int mmax = min(L, l0 + PT - 1);
+    if (t * PT > 2 * mmax) return false;  // beyond this l tile's m range
+    mb = -mmax + t * PT;
     const int an = n < 0 ? -n : n;
-    const int amin = (mb <= 0 && mb + PT - 1 >= 0) ? 0 : min(abs(mb), abs(mb + PT - 1));
-    // some (l, m) of the tile must satisfy l >= max(|m|, |n|)
-    return l0 + PT - 1 >= max(an, amin) && l0 <= L;
+    return l0 + PT - 1 >= an && l0 <= L;
 }
 
 // group-major pair (g, p) of (m, n) and its group's first degree m0 (consistent with group_pairs)
