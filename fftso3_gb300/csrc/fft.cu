@@ -292,6 +292,12 @@ __host__ __device__ inline int prime_mat_entries(int R)
     return P * ((P + 3) / 4 * 4);
 }
 
+// Real data, two lines per transform: with REAL_IN the real lines 2p and 2p+1
+// are transformed together as z = x_{2p} + i x_{2p+1} and separated with
+// X[k] = (Z[k] + conj Z[-k]) / 2, Y[k] = (Z[k] - conj Z[-k]) / 2i; with REAL_OUT
+// (the input spectra are those of real lines) z = X_{2p} + i X_{2p+1} and the
+// real and imaginary parts of its transform are the two lines.  Either way the
+// CTA transforms lpb / 2 complex lines.
 template <typename T, typename TIN, bool REAL_IN, bool REAL_OUT>
 __global__ void __launch_bounds__(256) fft_lines_kernel(const TIN* __restrict__ in, void* __restrict__ out, FFTFactors fac,
                                                         long long nlines, int lpb_log2, long long inner, long long ostride,
@@ -299,14 +305,16 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(const TIN* __restrict__ 
                                                         int lines_fastest)
 {
     using C = typename V2<T>::t;
+    constexpr bool PACK = REAL_IN || REAL_OUT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int N = fac.N;
     const int LS = N + 1;
     const int lpb = 1 << lpb_log2;
+    const int lbuf = PACK ? lpb / 2 : lpb;  // complex lines transformed by the CTA
     C* w = reinterpret_cast<C*>(smem_raw);
     C* buf0 = w + N;
-    C* buf1 = buf0 + lpb * LS;
-    long long* base = reinterpret_cast<long long*>(buf1 + lpb * LS);
+    C* buf1 = buf0 + lbuf * LS;
+    long long* base = reinterpret_cast<long long*>(buf1 + lbuf * LS);
     C* mat = reinterpret_cast<C*>(base + lpb);  // prime-first DFT matrix (only when fac.r[0] > 8)
     const double2* tw = reinterpret_cast<const double2*>(twg);
     for (int i = threadIdx.x; i < N; i += blockDim.x) w[i] = V2<T>::mk((T)tw[i].x, (T)tw[i].y);
@@ -325,29 +333,45 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(const TIN* __restrict__ 
     }
 
     const long long line0 = (long long)blockIdx.x * lpb;
-    const int nl = (int)min((long long)lpb, nlines - line0);
+    const int nl = (int)min((long long)lpb, nlines - line0);  // even when PACK (nlines, lpb even)
     for (int t = threadIdx.x; t < lpb; t += blockDim.x) {
         const long long i = line0 + t;
         base[t] = (i / inner) * ostride + (i % inner) * istride;
     }
     __syncthreads();
-    const int tot = lpb * N;
     // load (per-line base offsets precomputed; no per-element 64-bit division)
-    if (lines_fastest) {
-        for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+    if (REAL_OUT) {
+        // pairs (2p, 2p+1) of complex spectra -> X_{2p} + i X_{2p+1}
+        const int np2 = nl / 2;
+        for (int e = threadIdx.x; e < lbuf * N; e += blockDim.x) {
+            int p2, j;
+            if (lines_fastest) {
+                p2 = e & (lbuf - 1);
+                j = e >> (lpb_log2 - 1);
+            } else {
+                p2 = e / N;
+                j = e - p2 * N;
+            }
+            if (p2 >= np2) continue;
+            const C a = reinterpret_cast<const C*>(in)[base[2 * p2] + (long long)j * es];
+            const C b = reinterpret_cast<const C*>(in)[base[2 * p2 + 1] + (long long)j * es];
+            buf0[p2 * LS + j] = V2<T>::mk(a.x - b.y, a.y + b.x);
+        }
+    } else if (lines_fastest) {
+        for (int e = threadIdx.x; e < lpb * N; e += blockDim.x) {
             const int l = e & (lpb - 1), j = e >> lpb_log2;
             if (l >= nl) continue;
             const long long off = base[l] + (long long)j * es;
-            if constexpr (REAL_IN) buf0[l * LS + j] = V2<T>::mk((T)in[off], (T)0);
-            else buf0[l * LS + j] = in[off];
+            if constexpr (REAL_IN) reinterpret_cast<T*>(buf0)[2 * ((l >> 1) * LS + j) + (l & 1)] = (T)in[off];
+            else buf0[l * LS + j] = reinterpret_cast<const C*>(in)[off];
         }
     } else {
         const int linc = blockDim.x / N, jinc = blockDim.x - linc * N;
         int l = threadIdx.x / N, j = threadIdx.x - l * N;
         for (int e = threadIdx.x; e < nl * N; e += blockDim.x) {
             const long long off = base[l] + (long long)j * es;
-            if constexpr (REAL_IN) buf0[l * LS + j] = V2<T>::mk((T)in[off], (T)0);
-            else buf0[l * LS + j] = in[off];
+            if constexpr (REAL_IN) reinterpret_cast<T*>(buf0)[2 * ((l >> 1) * LS + j) + (l & 1)] = (T)in[off];
+            else buf0[l * LS + j] = reinterpret_cast<const C*>(in)[off];
             l += linc;
             j += jinc;
             if (j >= N) {
@@ -363,15 +387,15 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(const TIN* __restrict__ 
     for (int s = 0; s < fac.n; ++s) {
         const int R = fac.r[s];
         switch (R) {
-            case 2: stockham_stage<T, 2>(src, dst, w, N, Ns, lpb, LS); break;
-            case 3: stockham_stage<T, 3>(src, dst, w, N, Ns, lpb, LS); break;
-            case 4: stockham_stage<T, 4>(src, dst, w, N, Ns, lpb, LS); break;
-            case 5: stockham_stage<T, 5>(src, dst, w, N, Ns, lpb, LS); break;
-            case 7: stockham_stage<T, 7>(src, dst, w, N, Ns, lpb, LS); break;
-            case 8: stockham_stage<T, 8>(src, dst, w, N, Ns, lpb, LS); break;
+            case 2: stockham_stage<T, 2>(src, dst, w, N, Ns, lbuf, LS); break;
+            case 3: stockham_stage<T, 3>(src, dst, w, N, Ns, lbuf, LS); break;
+            case 4: stockham_stage<T, 4>(src, dst, w, N, Ns, lbuf, LS); break;
+            case 5: stockham_stage<T, 5>(src, dst, w, N, Ns, lbuf, LS); break;
+            case 7: stockham_stage<T, 7>(src, dst, w, N, Ns, lbuf, LS); break;
+            case 8: stockham_stage<T, 8>(src, dst, w, N, Ns, lbuf, LS); break;
             default:
-                if (Ns == 1) dft_prime_first<T>(src, dst, mat, N, R, lpb, LS);
-                else stockham_generic<T>(src, dst, w, N, Ns, R, lpb, LS);
+                if (Ns == 1) dft_prime_first<T>(src, dst, mat, N, R, lbuf, LS);
+                else stockham_generic<T>(src, dst, w, N, Ns, R, lbuf, LS);
                 break;
         }
         __syncthreads();
@@ -379,12 +403,24 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(const TIN* __restrict__ 
         Ns *= R;
     }
     // store
+    auto value = [&](int l, int j) -> C {
+        if constexpr (REAL_IN) {
+            const C z = src[(l >> 1) * LS + j], zm = src[(l >> 1) * LS + (j == 0 ? 0 : N - j)];
+            return (l & 1) ? V2<T>::mk((T)0.5 * (z.y + zm.y), (T)-0.5 * (z.x - zm.x))
+                           : V2<T>::mk((T)0.5 * (z.x + zm.x), (T)0.5 * (z.y - zm.y));
+        } else if constexpr (REAL_OUT) {
+            const C z = src[(l >> 1) * LS + j];
+            return V2<T>::mk((l & 1) ? z.y : z.x, (T)0);
+        } else {
+            return src[l * LS + j];
+        }
+    };
     if (lines_fastest) {
-        for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+        for (int e = threadIdx.x; e < lpb * N; e += blockDim.x) {
             const int l = e & (lpb - 1), j = e >> lpb_log2;
             if (l >= nl) continue;
             const long long off = base[l] + (long long)j * es;
-            const C v = src[l * LS + j];
+            const C v = value(l, j);
             if constexpr (REAL_OUT) reinterpret_cast<T*>(out)[off] = v.x;
             else reinterpret_cast<C*>(out)[off] = v;
         }
@@ -397,7 +433,7 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(const TIN* __restrict__ 
                 ++l;
             }
             const long long off = base[l] + (long long)j * es;
-            const C v = src[l * LS + j];
+            const C v = value(l, j);
             if constexpr (REAL_OUT) reinterpret_cast<T*>(out)[off] = v.x;
             else reinterpret_cast<C*>(out)[off] = v;
         }
@@ -450,7 +486,10 @@ static cudaError_t launch_one(const void* in, void* out, const FFTFactors& fac, 
                               const void* tw, bool lines_fastest, int threads, cudaStream_t st)
 {
     if (threads < 32 || threads > 256 || threads % 32 != 0) return cudaErrorInvalidValue;
-    size_t smem = fft_smem_bytes(fac.N, lpb, sizeof(T) == 8);
+    if ((RI || RO) && lpb < 2) lpb = 2;  // real data: lines transformed in pairs
+    if ((RI || RO) && nlines % 2) return cudaErrorInvalidValue;
+    const int lbuf = (RI || RO) ? lpb / 2 : lpb;
+    size_t smem = fft_smem_bytes(fac.N, lbuf, sizeof(T) == 8) + 8 * (size_t)(lpb - lbuf);
     auto kern = fft_lines_kernel<T, TIN, RI, RO>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

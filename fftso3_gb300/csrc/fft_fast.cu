@@ -274,18 +274,23 @@ __global__ void __launch_bounds__(32 * PWARPS, 3) fft_tile(const float2* __restr
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     constexpr int NV = TL * N / 2 / (32 * PWARPS);  // float4 accesses per thread on the transposed side
     static_assert(TL * N / 2 % (32 * PWARPS) == 0, "tile must split evenly over the threads");
+    // REAL_IO: real lines 2p and 2p+1 share one complex transform (staged row p):
+    // forward z = x_{2p} + i x_{2p+1}, X = (Z[k] + conj Z[-k]) / 2, Y = (Z[k] - conj Z[-k]) / 2i;
+    // inverse z = X_{2p} + i X_{2p+1} (spectra of real lines), lines = Re, Im of its transform.
+    constexpr int TLI = REAL_IO ? TL / 2 : TL;  // transforms (staged rows) per tile
     if (C2T) {
-        // contiguous input: each warp loads its lines straight into registers
+        // contiguous input: each warp loads its line(s) straight into registers
         __syncthreads();  // twiddles staged
-        for (int line = warp; line < TL; line += PWARPS) {
-            float2* Tl = T + line * LP;
+        for (int row = warp; row < TLI; row += PWARPS) {
+            float2* Tl = T + row * LP;
             float2 v[R];
             if (REAL_IO) {
-                const float* src = reinterpret_cast<const float*>(in) + cbase + line * Ls;
+                const float* s0 = reinterpret_cast<const float*>(in) + cbase + (2 * row) * Ls;
+                const float* s1 = s0 + Ls;
 #pragma unroll
-                for (int i = 0; i < R; ++i) v[i] = make_float2(__ldg(src + lane + 32 * i), 0.f);
+                for (int i = 0; i < R; ++i) v[i] = make_float2(__ldg(s0 + lane + 32 * i), __ldg(s1 + lane + 32 * i));
             } else {
-                const float2* src = in + cbase + line * Ls;
+                const float2* src = in + cbase + row * Ls;
 #pragma unroll
                 for (int i = 0; i < R; ++i) v[i] = __ldg(src + lane + 32 * i);
             }
@@ -305,7 +310,16 @@ __global__ void __launch_bounds__(32 * PWARPS, 3) fft_tile(const float2* __restr
         for (int u = 0; u < NV; ++u) {
             const int e2 = threadIdx.x + u * 32 * PWARPS;
             const int l = (e2 % (TL / 2)) * 2, j = e2 / (TL / 2);
-            const float2 a = T[l * LP + ppos<R>(j)], b = T[(l + 1) * LP + ppos<R>(j)];
+            float2 a, b;
+            if (REAL_IO) {
+                const float2 z = T[(l / 2) * LP + ppos<R>(j)];
+                const float2 zm = T[(l / 2) * LP + ppos<R>((N - j) & (N - 1))];
+                a = make_float2(0.5f * (z.x + zm.x), 0.5f * (z.y - zm.y));
+                b = make_float2(0.5f * (z.y + zm.y), -0.5f * (z.x - zm.x));
+            } else {
+                a = T[l * LP + ppos<R>(j)];
+                b = T[(l + 1) * LP + ppos<R>(j)];
+            }
             out4[(tbase + (long long)j * Js + l) / 2] = make_float4(a.x, a.y, b.x, b.y);
         }
     } else {
@@ -325,25 +339,34 @@ __global__ void __launch_bounds__(32 * PWARPS, 3) fft_tile(const float2* __restr
             for (int q = 0; q < VB; ++q) {
                 const int e2 = threadIdx.x + (u0 + q) * 32 * PWARPS;
                 const int l = (e2 % (TL / 2)) * 2, j = e2 / (TL / 2);
-                T[l * LP + ppos<R>(j)] = make_float2(buf[q].x, buf[q].y);
-                T[(l + 1) * LP + ppos<R>(j)] = make_float2(buf[q].z, buf[q].w);
+                if (REAL_IO) {
+                    T[(l / 2) * LP + ppos<R>(j)] = make_float2(buf[q].x - buf[q].w, buf[q].y + buf[q].z);
+                } else {
+                    T[l * LP + ppos<R>(j)] = make_float2(buf[q].x, buf[q].y);
+                    T[(l + 1) * LP + ppos<R>(j)] = make_float2(buf[q].z, buf[q].w);
+                }
             }
         }
         __syncthreads();
         // contiguous output straight from registers: runs of R consecutive outputs per lane group
-        for (int line = warp; line < TL; line += PWARPS) {
-            float2* Tl = T + line * LP;
+        for (int row = warp; row < TLI; row += PWARPS) {
+            float2* Tl = T + row * LP;
             float2 v[R];
 #pragma unroll
             for (int i = 0; i < R; ++i) v[i] = Tl[ppos<R>(lane + 32 * i)];
             line_step_a<R>(v, Tl, Ws, lane);
             line_step_b<R>(v, Tl, Ws, lane);
             if (REAL_IO) {
-                float* dst = reinterpret_cast<float*>(out) + cbase + line * Ls;
+                float* d0 = reinterpret_cast<float*>(out) + cbase + (2 * row) * Ls;
+                float* d1 = d0 + Ls;
 #pragma unroll
-                for (int r = 0; r < R; ++r) dst[line_out_index<R>(lane, r)] = v[r].x;
+                for (int r = 0; r < R; ++r) {
+                    const int K = line_out_index<R>(lane, r);
+                    d0[K] = v[r].x;
+                    d1[K] = v[r].y;
+                }
             } else {
-                float2* dst = out + cbase + line * Ls;
+                float2* dst = out + cbase + row * Ls;
 #pragma unroll
                 for (int r = 0; r < R; ++r) dst[line_out_index<R>(lane, r)] = v[r];
             }
@@ -356,7 +379,8 @@ static cudaError_t tile_r(const void* in, void* out, long long nf, const TileGeo
 {
     constexpr int N = 32 * R;
     constexpr int LP = tile_lp<R>();
-    const size_t smem = sizeof(float2) * ((size_t)N + (size_t)TL * LP);
+    constexpr int TLI = REAL_IO ? TL / 2 : TL;  // staged rows (real lines go in pairs)
+    const size_t smem = sizeof(float2) * ((size_t)N + (size_t)TLI * LP);
     auto k = fft_tile<R, C2T, REAL_IO>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
