@@ -498,7 +498,7 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--l-max", type=int, default=255)
-    ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--batch", type=int, default=32)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -687,15 +687,15 @@ def main() -> None:
         hg.copy_(grid)
         hc = torch.empty(b * C, dtype=torch.complex64, pin_memory=True)
         hc.copy_(coef)
-        hgo = torch.empty_like(hg, pin_memory=True)
         hco = torch.empty_like(hc, pin_memory=True)
-        plan.inverse_host(hc.data_ptr(), hgo.data_ptr(), sp)
+        # the inverse writes the grid the forward then reads (one pinned grid buffer)
+        plan.inverse_host(hc.data_ptr(), hg.data_ptr(), sp)
         plan.forward_host(hg.data_ptr(), hco.data_ptr(), sp)
         barrier()
         t0 = time.perf_counter()
         ksteps = max(1, min(args.steps, 3))
         for _ in range(ksteps):
-            plan.inverse_host(hc.data_ptr(), hgo.data_ptr(), sp)
+            plan.inverse_host(hc.data_ptr(), hg.data_ptr(), sp)
             plan.forward_host(hg.data_ptr(), hco.data_ptr(), sp)
         barrier()
         dt = (time.perf_counter() - t0) / ksteps
@@ -705,13 +705,14 @@ def main() -> None:
             dt = float(t.item())
         e2e = {"value": b * world / dt, "unit": UNIT, "h2d_bytes_per_step": int(8 * b * C + 8 * b * N ** 3),
                "d2h_bytes_per_step": int(8 * b * N ** 3 + 8 * b * C), "steps": ksteps}
-        del hg, hc, hgo, hco
+        del hg, hc, hco
 
     # ---- the FP32 form of the beta-sum (CUDA cores, FFTSO3_PREC_FP32) on the same batch
     fp32 = None
+    plan.close()  # the tensor-core plan's tables and workspace make room for the FP32 plan
+    del plan, grid_out, coef_out
+    torch.cuda.empty_cache()
     if not args.no_fp32:
-        del grid_out
-        torch.cuda.empty_cache()
         p32 = _lib.Plan(_lib.SO3_COMPLEX, L, b, "fp32", "stable")
         g32 = torch.empty_like(grid)
         c32 = torch.empty_like(coef)
