@@ -37,3 +37,19 @@ def R_to_euler323(R) -> tuple[float, float, float]:
         a = float(np.arccos(np.clip(R[0, 0], -1.0, 1.0)) / 2.0)
         g = a
     return a, b, g
+
+
+def hat(v) -> np.ndarray:
+    """hat map R^3 -> so(3) (misc_matrix_func.cpp:7-17)."""
+    x, y, z = (float(t) for t in v)
+    return np.array([[0.0, -z, y], [z, 0.0, -x], [-y, x, 0.0]])
+
+
+def expm_SO3(r) -> np.ndarray:
+    """exp(hat r) by the Rodrigues formula (the rotation misc_matrix_func.cpp:49-60 computes)."""
+    r = np.asarray(r, float)
+    th = float(np.linalg.norm(r))
+    K = hat(r)
+    if th < 1e-12:
+        return np.eye(3) + K
+    return np.eye(3) + np.sin(th) / th * K + (1.0 - np.cos(th)) / th ** 2 * (K @ K)

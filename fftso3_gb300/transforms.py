@@ -29,7 +29,7 @@ import numpy as np
 from . import _lib
 from .matrix import (FFTS2_matrix_complex, FFTS2_matrix_real, FFTSO3_matrix_complex, FFTSO3_matrix_real,
                      so3_ncoeff, s2_ncoeff)
-from .rotation import R_to_euler323, euler323_to_R
+from .rotation import R_to_euler323, euler323_to_R, expm_SO3
 
 
 def beta_k(l_max: int, k) -> np.ndarray:
@@ -41,6 +41,33 @@ def beta_k(l_max: int, k) -> np.ndarray:
 def alpha_j(l_max: int, j) -> np.ndarray:
     """alpha_j = gamma_j = j pi / B (fdcl_FFTSO3.cpp:583-591)."""
     return np.asarray(j, float) * np.pi / (l_max + 1)
+
+
+def _rsph(l: int) -> np.ndarray:
+    """matrix2rsph T(l) (fdcl_FFTSO3.cpp:1107-1139): row a, column c, indices shifted by l."""
+    W = 2 * l + 1
+    T = np.zeros((W, W), complex)
+    s = 1.0 / np.sqrt(2.0)
+    for a in range(-l, l + 1):
+        sg = -1.0 if (a & 1) else 1.0
+        if a < 0:
+            T[a + l, a + l] = 1j * s
+            T[a + l, -a + l] = -1j * s * sg
+        elif a == 0:
+            T[l, l] = 1.0
+        else:
+            T[a + l, -a + l] = s
+            T[a + l, a + l] = sg * s
+    return T
+
+
+def real_from_wigner_D(D) -> FFTSO3_matrix_real:
+    """Real harmonics U^l = Re(conj(T) D^l T^T) of a Wigner-D container (fdcl_FFTSO3.cpp:1062-1105)."""
+    U = FFTSO3_matrix_real(D.l_max)
+    for l in range(D.l_max + 1):
+        T = _rsph(l)
+        U[l] = np.real(np.conj(T) @ D[l] @ T.T)
+    return U
 
 
 def _n_params(func) -> int:
@@ -228,6 +255,41 @@ class FFTSO3_complex(_Transform):
             D[l] = d[l] * np.exp(-1j * m * a)[:, None] * np.exp(-1j * m * g)[None, :]
         return D
 
+    def deriv_wigner_D(self) -> list:
+        """[None, u1, u2, u3]: d/dt D(exp(t e_i)) at t = 0 for each l (fdcl_FFTSO3.cpp:417-453),
+        so that d/dt D(R exp(t e_i)) = D(R) u_i."""
+        u = [None] + [FFTSO3_matrix_complex(self.l_max) for _ in range(3)]
+        for l in range(self.l_max + 1):
+            m = np.arange(-l, l + 1)
+            W = 2 * l + 1
+            u3 = np.zeros((W, W), complex)
+            u3[m + l, m + l] = -1j * m
+            u1 = np.zeros((W, W), complex)
+            u2 = np.zeros((W, W), complex)
+            up = m[:-1]                      # n = m + 1
+            c = np.sqrt((l + up + 1.0) * (l - up))
+            u2[up + l, up + 1 + l] = 0.5 * c
+            u1[up + l, up + 1 + l] = -0.5j * c
+            dn = m[1:]                       # n = m - 1
+            c = np.sqrt((l - dn + 1.0) * (l + dn))
+            u2[dn + l, dn - 1 + l] = -0.5 * c
+            u1[dn + l, dn - 1 + l] = -0.5j * c
+            u[1][l], u[2][l], u[3][l] = u1, u2, u3
+        return u
+
+    def check_deriv_wigner_D(self, eps: float = 1e-6) -> float:
+        """fdcl_FFTSO3.cpp:455-492: the derivatives against (D(exp(eps e_i)) - D(I)) / eps."""
+        u = self.deriv_wigner_D()
+        D0 = self.wigner_D(0.0, 0.0, 0.0)
+        err = np.zeros(self.l_max)
+        for i in range(1, 4):
+            e = np.zeros(3)
+            e[i - 1] = eps
+            D1 = self.wigner_D(expm_SO3(e))
+            for l in range(1, self.l_max + 1):
+                err[l - 1] += np.linalg.norm((D1[l] - D0[l]) / eps - u[i][l]) / np.linalg.norm(u[i][l])
+        return float(err.max() * 1e-9)
+
     def check_transform(self, rng=None) -> float:
         """fdcl_FFTSO3.cpp:598-610: ||F - forward(inverse(F))|| for random F."""
         F = FFTSO3_matrix_complex(self.l_max)
@@ -250,6 +312,55 @@ class FFTSO3_real(FFTSO3_complex):
         else:
             a, b, g = args
         return float(self._points(F, np.array([[a, b, g]]))[0])
+
+    def real_harmonics(self, *args) -> FFTSO3_matrix_real:
+        """U^l = Re(conj(T) D^l T^T), T = matrix2rsph (fdcl_FFTSO3.cpp:1062-1139)."""
+        return real_from_wigner_D(self.wigner_D(*args))
+
+    def deriv_real_harmonics(self) -> list:
+        """[None, u1, u2, u3]: d/dt U(exp(t e_i)) at t = 0 (fdcl_FFTSO3.cpp:1577-1645), so that
+        d/dt U(R exp(t e_i)) = U(R) u_i."""
+        u = [None] + [FFTSO3_matrix_real(self.l_max) for _ in range(3)]
+        for l in range(self.l_max + 1):
+            W = 2 * l + 1
+            M = [np.zeros((W, W)) for _ in range(3)]
+            ix = lambda m: m + l  # noqa: E731
+            for p in range(1, l + 1):
+                M[2][ix(p), ix(-p)] = -p          # u3(l, m, -m) = -m
+                M[2][ix(-p), ix(p)] = p
+            for p in range(2, l + 1):
+                t = 0.5 * np.sqrt((l + p) * (l - p + 1.0))
+                M[1][ix(p), ix(p - 1)] = t
+                M[1][ix(-p), ix(-p + 1)] = t
+                M[0][ix(p), ix(-p + 1)] = (p + (-p + 1)) * t
+                M[0][ix(-p), ix(p - 1)] = (-p + (p - 1)) * t
+                q = p - 1
+                t = 0.5 * np.sqrt((l - q) * (l + q + 1.0))
+                M[1][ix(q), ix(q + 1)] = -t
+                M[1][ix(-q), ix(-q - 1)] = -t
+                M[0][ix(q), ix(-q - 1)] = -(q + (-q - 1)) * t
+                M[0][ix(-q), ix(q + 1)] = -(-q + (q + 1)) * t
+            if l >= 1:
+                t = np.sqrt(l * (l + 1.0) / 2.0)
+                M[1][ix(1), ix(0)] = t
+                M[1][ix(0), ix(1)] = -t
+                M[0][ix(-1), ix(0)] = -t
+                M[0][ix(0), ix(-1)] = t
+            u[1][l], u[2][l], u[3][l] = M
+        return u
+
+    def check_deriv_real_harmonics(self, eps: float = 1e-6) -> float:
+        """fdcl_FFTSO3.cpp:1648-1681: the derivatives against (U(exp(eps e_i)) - U(I)) / eps."""
+        u = self.deriv_real_harmonics()
+        U0 = self.real_harmonics(0.0, 0.0, 0.0)
+        err = 0.0
+        for i in range(1, 4):
+            e = np.zeros(3)
+            e[i - 1] = eps
+            U1 = self.real_harmonics(expm_SO3(e))
+            for l in range(1, self.l_max + 1):
+                err += np.linalg.norm((U1[l] - U0[l]) / eps - u[i][l]) / np.linalg.norm(u[i][l])
+        return float(err * 1e-9)
 
     def check_transform(self, rng=None) -> float:
         """fdcl_FFTSO3.cpp:1785-1797."""
@@ -301,13 +412,16 @@ class FFTS2_real(FFTS2_complex):
         return (F - G).norm()
 
 
-def correlate_s2(F, G, *, precision: str = "fp64", recursion: str = "reference"):
+def correlate_s2(F, G, *, precision: str = "fp64", recursion: str = "reference", gradient: bool = False):
     """S^2 -> SO(3) correlation of two real spherical functions (shape matching).
 
     F, G: FFTS2_matrix_real of one l_max.  Returns (J, (alpha, beta, gamma), R): J the
     score J(R) = sum_l G[l]^T U^l(R) F[l] on the whole (2B)^3 Euler grid (the cost of
     the reference's shape-matching example, example/example3_SSM.hpp), and the grid
     rotation that maximises it, as Euler 3-2-3 angles and as a rotation matrix.
+    With gradient=True also dJ (3, N, N, N): dJ_i(R) = d/dt J(R exp(t e_i)) at t = 0
+    = sum_l G[l]^T U^l(R) u_i^l F[l] (the reference's gradient(R), example3_SSM.hpp),
+    i.e. the same correlation with F[l] replaced by u_i^l F[l].
     """
     import torch
 
@@ -325,4 +439,14 @@ def correlate_s2(F, G, *, precision: str = "fp64", recursion: str = "reference")
     (idx,), _ = plan.grid_argmax(grid.data_ptr(), s)
     k, j1, j2 = idx // (N * N), (idx // N) % N, idx % N
     abg = (float(alpha_j(L, j1)), float(beta_k(L, k)), float(alpha_j(L, j2)))
-    return grid.cpu().numpy().astype(np.float64).reshape(N, N, N), abg, euler323_to_R(*abg)
+    J = grid.cpu().numpy().astype(np.float64).reshape(N, N, N)
+    if not gradient:
+        return J, abg, euler323_to_R(*abg)
+    u = FFTSO3_real(L).deriv_real_harmonics()
+    dJ = np.empty((3, N, N, N))
+    for i in range(1, 4):
+        Fi = np.concatenate([u[i][l] @ F[l] for l in range(L + 1)])
+        fi = torch.from_numpy(Fi).to(device="cuda", dtype=dt)
+        plan.correlate_s2(fi.data_ptr(), g.data_ptr(), grid.data_ptr(), s)
+        dJ[i - 1] = grid.cpu().numpy().astype(np.float64).reshape(N, N, N)
+    return J, abg, euler323_to_R(*abg), dJ

@@ -76,3 +76,28 @@ def test_shape_matching_recovers_grid_rotation(gblib, oracle, torch_cuda):
     assert np.unravel_index(np.argmax(J), J.shape) == (k, j1, j2)
     assert np.allclose(abg, (a, b, g))
     assert np.allclose(R, fg.euler323_to_R(a, b, g))
+
+
+def test_correlation_gradient_grid(gblib, oracle, torch_cuda):
+    """dJ_i on the grid (correlate_s2(gradient=True)) against central differences of the
+    oracle's J at R exp(+-h e_i), at sampled grid rotations."""
+    import fftso3_gb300 as fg
+    L = 6
+    N = 2 * (L + 1)
+    F = s2_coeffs(L, seed=2000, complex_=False)
+    G = s2_coeffs(L, seed=2001, complex_=False)
+    Fm, Gm = fg.FFTS2_matrix_real(L), fg.FFTS2_matrix_real(L)
+    Fm.M[:] = F
+    Gm.M[:] = G
+    J, _, _, dJ = fg.correlate_s2(Fm, Gm, gradient=True)
+    h = 1e-5
+    rng = np.random.default_rng(9)
+    for k, j1, j2 in rng.integers(0, N, size=(6, 3)):
+        R = fg.euler323_to_R(oracle.alpha_j(L, j1), oracle.beta_k(L, k), oracle.alpha_j(L, j2))
+        for i in range(3):
+            e = np.zeros(3)
+            e[i] = h
+            Jp = _J_oracle(oracle, L, F, G, *fg.R_to_euler323(R @ fg.expm_SO3(e)))
+            Jm = _J_oracle(oracle, L, F, G, *fg.R_to_euler323(R @ fg.expm_SO3(-e)))
+            num = (Jp - Jm) / (2 * h)
+            assert abs(dJ[i, k, j1, j2] - num) <= 1e-6 * max(1.0, abs(num)), (i, k, j1, j2)
