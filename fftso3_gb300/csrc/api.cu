@@ -518,12 +518,27 @@ static size_t coeff_bytes(const fftso3_plan* p)
     return (size_t)p->batch * p->coeff_elems * (p->real ? rbytes(p) : cbytes(p));
 }
 
-static int ensure_io(fftso3_plan* p)
+static int ensure_io_grid(fftso3_plan* p)
 {
-    int rc;
-    if (!p->d_io_grid && (rc = plan_alloc(p, &p->d_io_grid, grid_bytes(p)))) return rc;
-    if (!p->d_io_coeff && (rc = plan_alloc(p, &p->d_io_coeff, coeff_bytes(p)))) return rc;
-    return FFTSO3_SUCCESS;
+    return p->d_io_grid ? FFTSO3_SUCCESS : plan_alloc(p, &p->d_io_grid, grid_bytes(p));
+}
+static int ensure_io_coeff(fftso3_plan* p)
+{
+    return p->d_io_coeff ? FFTSO3_SUCCESS : plan_alloc(p, &p->d_io_coeff, coeff_bytes(p));
+}
+
+// Device address of a pinned (page-locked) host buffer, or null for pageable memory.
+// With unified addressing the GPU reads and writes pinned host memory directly
+// (over the C2C link on Grace-Blackwell), so a transform can stream its input
+// from, and its output to, host memory instead of staging whole copies.
+static void* host_device_ptr(const void* p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
 
 int fftso3_forward_host(fftso3_plan* plan, const void* grid_host, void* coeffs_host, void* stream)
@@ -531,11 +546,17 @@ int fftso3_forward_host(fftso3_plan* plan, const void* grid_host, void* coeffs_h
     int rc = check_plan(plan);
     if (rc) return rc;
     if (!grid_host || !coeffs_host) return fail(FFTSO3_ERR_INVALID_ARG, "grid/coeffs pointer is NULL");
-    if ((rc = ensure_io(plan))) return rc;
     cudaStream_t st = (cudaStream_t)stream;
-    CK(cudaMemcpyAsync(plan->d_io_grid, grid_host, grid_bytes(plan), cudaMemcpyHostToDevice, st));
-    if ((rc = run_forward(plan, plan->d_io_grid, plan->d_io_coeff, st))) return rc;
-    CK(cudaMemcpyAsync(coeffs_host, plan->d_io_coeff, coeff_bytes(plan), cudaMemcpyDeviceToHost, st));
+    // pinned buffers: read the samples / write the coefficients in place
+    const void* gin = host_device_ptr(grid_host);
+    void* cout = host_device_ptr(coeffs_host);
+    if ((!gin && (rc = ensure_io_grid(plan))) || (!cout && (rc = ensure_io_coeff(plan)))) return rc;
+    if (!gin) {
+        CK(cudaMemcpyAsync(plan->d_io_grid, grid_host, grid_bytes(plan), cudaMemcpyHostToDevice, st));
+        gin = plan->d_io_grid;
+    }
+    if ((rc = run_forward(plan, gin, cout ? cout : plan->d_io_coeff, st))) return rc;
+    if (!cout) CK(cudaMemcpyAsync(coeffs_host, plan->d_io_coeff, coeff_bytes(plan), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     return FFTSO3_SUCCESS;
 }
@@ -545,11 +566,16 @@ int fftso3_inverse_host(fftso3_plan* plan, const void* coeffs_host, void* grid_h
     int rc = check_plan(plan);
     if (rc) return rc;
     if (!grid_host || !coeffs_host) return fail(FFTSO3_ERR_INVALID_ARG, "grid/coeffs pointer is NULL");
-    if ((rc = ensure_io(plan))) return rc;
     cudaStream_t st = (cudaStream_t)stream;
-    CK(cudaMemcpyAsync(plan->d_io_coeff, coeffs_host, coeff_bytes(plan), cudaMemcpyHostToDevice, st));
-    if ((rc = run_inverse(plan, plan->d_io_coeff, plan->d_io_grid, st))) return rc;
-    CK(cudaMemcpyAsync(grid_host, plan->d_io_grid, grid_bytes(plan), cudaMemcpyDeviceToHost, st));
+    const void* cin = host_device_ptr(coeffs_host);
+    void* gout = host_device_ptr(grid_host);
+    if ((!cin && (rc = ensure_io_coeff(plan))) || (!gout && (rc = ensure_io_grid(plan)))) return rc;
+    if (!cin) {
+        CK(cudaMemcpyAsync(plan->d_io_coeff, coeffs_host, coeff_bytes(plan), cudaMemcpyHostToDevice, st));
+        cin = plan->d_io_coeff;
+    }
+    if ((rc = run_inverse(plan, cin, gout ? gout : plan->d_io_grid, st))) return rc;
+    if (!gout) CK(cudaMemcpyAsync(grid_host, plan->d_io_grid, grid_bytes(plan), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     return FFTSO3_SUCCESS;
 }

@@ -129,9 +129,11 @@ int fftso3_forward(fftso3_plan* plan, const void* grid, void* coeffs, void* stre
  * evaluated at each (alpha_j1, beta_k, gamma_j2) / (theta_k, phi_j). */
 int fftso3_inverse(fftso3_plan* plan, const void* coeffs, void* grid, void* stream);
 
-/* Host-buffer variants: copy host -> device, transform, copy back, and
- * synchronise the stream before returning (the reference's by-value call
- * convention).  Host buffers may be pageable or pinned. */
+/* Host-buffer variants: transform host data and synchronise the stream
+ * before returning (the reference's by-value call convention).  Host buffers
+ * may be pageable or pinned: pageable buffers are staged through device
+ * copies, pinned (page-locked) ones are read and written in place by the
+ * kernels over the host link, without staging. */
 int fftso3_forward_host(fftso3_plan* plan, const void* grid_host, void* coeffs_host, void* stream);
 int fftso3_inverse_host(fftso3_plan* plan, const void* coeffs_host, void* grid_host, void* stream);
 

@@ -146,3 +146,26 @@ def test_tc_tile_fft_sizes(gblib, torch_cuda, L):
     ptc.check()
     assert rel_err(g32.cpu().numpy().astype(np.complex128), g64.cpu().numpy()) < TOL
     assert rel_err(F32.cpu().numpy().astype(np.complex128), F) < TOL
+
+
+def test_host_calls_pinned_equal_pageable(gblib, torch_cuda):
+    """The host-buffer calls read/write pinned buffers in place and stage pageable ones;
+    both give bit-identical results (tensor-core plan, batch 2)."""
+    torch = torch_cuda
+    L, b = 16, 2
+    N = 2 * (L + 1)
+    C = (L + 1) * (4 * (L + 1) ** 2 - 1) // 3
+    p = gblib.Plan(gblib.SO3_COMPLEX, L, b, "tc_bf16x3", "reference")
+    F = np.concatenate([so3_coeffs(L, seed=2100 + i) for i in range(b)]).astype(np.complex64)
+    g_pageable = np.empty(b * N ** 3, dtype=np.complex64)
+    p.inverse_host(F.ctypes.data, g_pageable.ctypes.data)
+    c_pageable = np.empty_like(F)
+    p.forward_host(g_pageable.ctypes.data, c_pageable.ctypes.data)
+    Fp = torch.from_numpy(F).pin_memory()
+    gp = torch.empty(b * N ** 3, dtype=torch.complex64).pin_memory()
+    cp = torch.empty(b * C, dtype=torch.complex64).pin_memory()
+    p.inverse_host(Fp.data_ptr(), gp.data_ptr())
+    p.forward_host(gp.data_ptr(), cp.data_ptr())
+    assert np.array_equal(gp.numpy(), g_pageable)
+    assert np.array_equal(cp.numpy(), c_pageable)
+    assert rel_err(cp.numpy().astype(np.complex128), F.astype(np.complex128)) < TOL
