@@ -362,6 +362,23 @@ class FFTSO3_real(FFTSO3_complex):
                 err += np.linalg.norm((U1[l] - U0[l]) / eps - u[i][l]) / np.linalg.norm(u[i][l])
         return float(err * 1e-9)
 
+    def check_Clebsch_Gordon(self, l1: int = 3, l2: int = 5, rng=None) -> float:
+        """fdcl_FFTSO3.cpp:1683+: ||U^{l1} (x) U^{l2} - c ((+)_l U^l) c^H|| at a random rotation."""
+        from .clebsch_gordan import Clebsch_Gordon_real
+
+        rng = np.random.default_rng(rng)
+        a, b, g = rng.uniform(0, 2 * np.pi), rng.uniform(0, np.pi), rng.uniform(0, 2 * np.pi)
+        U = FFTSO3_real(l1 + l2, recursion=self.recursion).real_harmonics(a, b, g)
+        cg = Clebsch_Gordon_real()
+        cg.compute(l1, l2)
+        n = cg.c.shape[0]
+        B = np.zeros((n, n))
+        i = 0
+        for l in range(abs(l1 - l2), l1 + l2 + 1):
+            B[i:i + 2 * l + 1, i:i + 2 * l + 1] = U[l]
+            i += 2 * l + 1
+        return float(np.linalg.norm(np.kron(U[l1], U[l2]) - cg.c @ B @ cg.c.conj().T))
+
     def check_transform(self, rng=None) -> float:
         """fdcl_FFTSO3.cpp:1785-1797."""
         F = FFTSO3_matrix_real(self.l_max)

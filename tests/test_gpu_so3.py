@@ -226,3 +226,11 @@ def test_bad_calls_raise(gblib):
     pts = np.zeros(3)
     with pytest.raises(gblib.FFTSO3Error):
         p.inverse_points(1, 5, pts.ctypes.data_as(gblib._dp), 1, pts.ctypes.data)
+
+
+def test_check_clebsch_gordon_and_derivatives(gblib):
+    """The reference's check members on the GPU-computed real harmonics / Wigner D."""
+    import fftso3_gb300 as fg
+    assert fg.FFTSO3_real(8).check_Clebsch_Gordon(rng=1) < 1e-10
+    assert fg.FFTSO3_real(6).check_deriv_real_harmonics() < 1e-9
+    assert fg.FFTSO3_complex(6).check_deriv_wigner_D() < 1e-9
