@@ -359,6 +359,93 @@ def main_uneven(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+# --------------------------------------------------------------- FP64 plain path
+
+FP64_METRIC = "SO(3) FP64 fwd+inv transforms/s at l_max={L}: plain FP64 GPU path (complex and real)"
+
+
+def main_fp64(args) -> None:
+    """The plain FP64 GPU path (FFTSO3_PREC_FP64, reference recursion) on one function at
+    l_max = 127 (256^3 grid), complex and real: transform pairs/s, HBM GB/s of the FFT passes
+    and of the table generation (plan creation), FP64 rate of the beta-sum."""
+    import torch
+
+    from fftso3_gb300 import _lib
+    from fftso3_gb300 import build as fbuild
+
+    fbuild.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    L = args.fp64_l_max
+    B, N = L + 1, 2 * (L + 1)
+    C = B * (4 * B * B - 1) // 3
+    out = {}
+    for kind, name in ((_lib.SO3_COMPLEX, "complex"), (_lib.SO3_REAL, "real")):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        p = _lib.Plan(kind, L, 1, "fp64", "reference")
+        torch.cuda.synchronize()
+        t_plan = time.perf_counter() - t0
+        cplx = kind == _lib.SO3_COMPLEX
+        dt = torch.complex128 if cplx else torch.float64
+        rng = np.random.Generator(np.random.PCG64(5))
+        l = np.concatenate([np.full((2 * x + 1) ** 2, x) for x in range(B)])
+        F = rng.standard_normal(C) / (2 * l + 1)
+        if cplx:
+            F = F + 1j * rng.standard_normal(C) / (2 * l + 1)
+        c = torch.from_numpy(F).to(dev)
+        g = torch.empty(N ** 3, dtype=dt, device=dev)
+        c2 = torch.empty_like(c)
+        for _ in range(args.warmup):
+            p.inverse(c.data_ptr(), g.data_ptr(), sp)
+            p.forward(g.data_ptr(), c2.data_ptr(), sp)
+        torch.cuda.synchronize()
+        p.set_timing(True)
+        p.stage_times(reset=True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            p.inverse(c.data_ptr(), g.data_ptr(), sp)
+            p.forward(g.data_ptr(), c2.data_ptr(), sp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        st = p.stage_times(reset=True)
+        p.set_timing(False)
+        p.check()
+        rel = float(torch.linalg.norm(c2 - c) / torch.linalg.norm(c))
+        esz = 16 if cplx else 8
+        grid_b = 16.0 * N ** 3  # complex128 work grid
+        fft = {}
+        for k in ("fft_rows", "fft_cols"):
+            if k in st:
+                t = st[k][0] / st[k][1] / 1000.0
+                fft[k] = {"ms_per_launch": t * 1000.0, "gbs": 2 * grid_b / t / 1e9}
+        table_bytes = 8.0 * sum((2 * m + 1) * (B - m) for m in range(B)) * N
+        flops = 8.0 * B * C  # beta-sum per direction
+        contr = {}
+        for k in ("fp64_fwd_contract", "fp64_inv_contract"):
+            if k in st:
+                t = st[k][0] / st[k][1] / 1000.0
+                contr[k] = {"ms_per_launch": t * 1000.0, "fp64_tflops": flops / t / 1e12}
+        out[name] = {"pairs_per_s": 1000.0 / ms, "ms_per_pair": ms, "round_trip_rel_err": rel,
+                     "fft": fft, "contraction": contr,
+                     "table": {"plan_create_s": t_plan, "table_gb": table_bytes / 1e9,
+                               "table_gbs_incl_setup": table_bytes / t_plan / 1e9},
+                     "stages_ms": {k: v for k, (v, _) in st.items()}, "grid_elem_bytes": esz}
+        del p, c, g, c2
+        torch.cuda.empty_cache()
+    line = {"metric": FP64_METRIC.format(L=L), "value": out["complex"]["pairs_per_s"], "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["complex"]["ms_per_pair"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"one SO(3) function, l_max={L} ({N}^3 grid), FP64, reference recursion; "
+                                   "coefficients N(0,1)/(2l+1)"},
+            "complex": out["complex"], "real": out["real"]}
+    print(json.dumps(line), flush=True)
+
+
 # --------------------------------------------------------------- S^2 batch
 
 S2_METRIC = "S2 real fwd+inv transforms/s, {b} signals at l_max={L}: TC split-BF16 vs FP64"
@@ -504,11 +591,12 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp32", action="store_true", help="skip the FP32 CUDA-core beta-sum comparison")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64 reference (profiling runs)")
-    ap.add_argument("--workload", default="lmax255", choices=["lmax255", "uneven", "s2"],
+    ap.add_argument("--workload", default="lmax255", choices=["lmax255", "uneven", "s2", "fp64"],
                     help="lmax255: the headline SO(3) batch at one l_max (--l-max/--batch); uneven: the "
                          "mixed-bandwidth SO(3) batch; s2: the S^2 batch at l_max=511")
     ap.add_argument("--functions", type=int, default=4096, help="uneven workload: number of functions")
     ap.add_argument("--s2-l-max", type=int, default=511, help="s2 workload: l_max")
+    ap.add_argument("--fp64-l-max", type=int, default=127, help="fp64 workload: l_max")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -518,6 +606,9 @@ def main() -> None:
         return
     if args.workload == "s2":
         main_s2(args)
+        return
+    if args.workload == "fp64":
+        main_fp64(args)
         return
 
     import torch

@@ -841,32 +841,64 @@ __device__ __forceinline__ void pair_m0(int m, int n, int& g, int& p, int& m0, i
     sign = ((p == 1 || p == 2) && ((m0 + n0) & 1)) ? -1 : 1;
 }
 
+// Per-tile index tables (shared memory): for each m of the tile the
+// group-major base (index = base + l), the first degree m0 = max(|m|, |n|)
+// (valid l are m0..L) and the pair sign; for each l the packed base
+// (index = base + m).  The element loops then do one compare and one address
+// add per element.
+struct PTileIdx {
+    long long gbase[PT];
+    int gm0[PT];
+    float gsign[PT];
+    long long pbase[PT];
+};
+
+__device__ __forceinline__ void ptile_index(PTileIdx& t, int L, int n, int l0, int mb, const long long* goff2)
+{
+    const int B = L + 1;
+    if (threadIdx.x < PT) {
+        const int m = mb + (int)threadIdx.x;
+        if (m < -L || m > L) {
+            t.gm0[threadIdx.x] = 0x7fffffff;
+            t.gbase[threadIdx.x] = 0;
+            t.gsign[threadIdx.x] = 0.f;
+        } else {
+            int g, pp, m0, sg;
+            pair_m0(m, n, g, pp, m0, sg);
+            t.gm0[threadIdx.x] = m0;
+            t.gbase[threadIdx.x] = goff2[g] + (long long)pp * (B - m0) - m0;
+            t.gsign[threadIdx.x] = (float)sg;
+        }
+    } else if (threadIdx.x < 2 * PT) {
+        const int l = l0 + (int)threadIdx.x - PT;
+        t.pbase[threadIdx.x - PT] = so3_off(l) + l + (long long)(n + l) * (2 * l + 1);
+    }
+    __syncthreads();
+}
+
 __global__ void __launch_bounds__(256) group_to_packed_tiled(const float2* __restrict__ Fg, float2* __restrict__ F,
                                                              const long long* __restrict__ goff2, int L,
                                                              long long cstride)
 {
     __shared__ float2 tile[PT][PT + 1];  // [m - mb][l - l0]
+    __shared__ PTileIdx ix;
     int n, l0, mb, f;
     if (!ptile_coords(L, n, l0, mb, f)) return;
-    const int B = L + 1, an = abs(n);
+    ptile_index(ix, L, n, l0, mb, goff2);
     const float2* src = Fg + (long long)f * cstride;
     // gather: lanes run along l (contiguous in the group-major layout)
     for (int e = threadIdx.x; e < PT * PT; e += blockDim.x) {
-        const int mi = e / PT, li = e % PT;
-        const int m = mb + mi, l = l0 + li;
-        if (m > L || l > L || l < abs(m) || l < an) continue;
-        int g, pp, m0, sg;
-        pair_m0(m, n, g, pp, m0, sg);
-        tile[mi][li] = src[goff2[g] + (long long)pp * (B - m0) + (l - m0)];
+        const int mi = e / PT, li = e % PT, l = l0 + li;
+        if (l < ix.gm0[mi] || l > L) continue;
+        tile[mi][li] = src[ix.gbase[mi] + l];
     }
     __syncthreads();
     // scatter: lanes run along m (contiguous in the packed layout)
     float2* dst = F + (long long)f * cstride;
     for (int e = threadIdx.x; e < PT * PT; e += blockDim.x) {
-        const int li = e / PT, mi = e % PT;
-        const int m = mb + mi, l = l0 + li;
-        if (m > L || l > L || l < abs(m) || l < an) continue;
-        dst[so3_idx(l, m, n)] = tile[mi][li];
+        const int li = e / PT, mi = e % PT, l = l0 + li;
+        if (l < ix.gm0[mi] || l > L) continue;
+        dst[ix.pbase[li] + mb + mi] = tile[mi][li];
     }
 }
 
@@ -876,27 +908,24 @@ __global__ void __launch_bounds__(256) packed_to_group_tiled(const float2* __res
                                                              long long cstride)
 {
     __shared__ float2 tile[PT][PT + 1];  // [m - mb][l - l0]
+    __shared__ PTileIdx ix;
     int n, l0, mb, f;
     if (!ptile_coords(L, n, l0, mb, f)) return;
-    const int B = L + 1, an = abs(n);
+    ptile_index(ix, L, n, l0, mb, goff2);
     const float2* src = F + (long long)f * cstride;
     for (int e = threadIdx.x; e < PT * PT; e += blockDim.x) {
-        const int li = e / PT, mi = e % PT;
-        const int m = mb + mi, l = l0 + li;
-        if (m > L || l > L || l < abs(m) || l < an) continue;
-        tile[mi][li] = src[so3_idx(l, m, n)];
+        const int li = e / PT, mi = e % PT, l = l0 + li;
+        if (l < ix.gm0[mi] || l > L) continue;
+        tile[mi][li] = src[ix.pbase[li] + mb + mi];
     }
     __syncthreads();
     float2* dst = Y + (long long)f * cstride;
     for (int e = threadIdx.x; e < PT * PT; e += blockDim.x) {
-        const int mi = e / PT, li = e % PT;
-        const int m = mb + mi, l = l0 + li;
-        if (m > L || l > L || l < abs(m) || l < an) continue;
-        int g, pp, m0, sg;
-        pair_m0(m, n, g, pp, m0, sg);
-        const float sc = (float)(2 * l + 1) * (float)sg;
+        const int mi = e / PT, li = e % PT, l = l0 + li;
+        if (l < ix.gm0[mi] || l > L) continue;
+        const float sc = (float)(2 * l + 1) * ix.gsign[mi];
         const float2 v = tile[mi][li];
-        dst[goff2[g] + (long long)pp * (B - m0) + (l - m0)] = make_float2(sc * v.x, sc * v.y);
+        dst[ix.gbase[mi] + l] = make_float2(sc * v.x, sc * v.y);
     }
 }
 
