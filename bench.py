@@ -192,8 +192,11 @@ def run_reference(args) -> None:
         "warmup": args.warmup, "ms_per_step": 1000.0 * wall / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "impl": "reference",
-        "config": {"workload": f"SO(3) complex forward+inverse, l_max={args.l_max}, one function per pair; "
-                               "reference CPU algorithm on a bounded sample of beta slices"},
+        "config": {"workload": f"SO(3) complex forward+inverse, l_max={args.l_max}, batch={args.batch} functions per "
+                               f"GPU ({2 * (args.l_max + 1)}^3 grid each); the reference's CPU algorithm (oracle port, "
+                               "all host threads) timed on a bounded sample of beta slices of one function, pairs/s "
+                               "extrapolated per function",
+                   "l_max": args.l_max, "batch_per_gpu": args.batch, "precision": "f64 (CPU)"},
         "cpu_baseline": {k: vals[-1][k] for k in ("value", "unit", "cores", "kind", "sample")},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
