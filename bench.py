@@ -617,7 +617,7 @@ def main() -> None:
     import torch
 
     import fftso3_gb300 as fg
-    from fftso3_gb300 import _lib
+    from fftso3_gb300 import _lib, shard
     from fftso3_gb300 import build as fbuild
 
     fbuild.build()
@@ -740,11 +740,7 @@ def main() -> None:
     plan.set_timing(False)
     plan.check()
     clocks = clk.summary()
-    ms_max = ms
-    if dist is not None:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_max = float(t.item())
+    ms_max = shard.max_over_ranks(ms)  # whole-job time: the slowest rank
     value = b * world * 1000.0 / ms_max
     launches = int(sum(c for _, c in stages.values()))
 
@@ -792,11 +788,7 @@ def main() -> None:
             plan.inverse_host(hc.data_ptr(), hg.data_ptr(), sp)
             plan.forward_host(hg.data_ptr(), hco.data_ptr(), sp)
         barrier()
-        dt = (time.perf_counter() - t0) / ksteps
-        if dist is not None:
-            t = torch.tensor([dt], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            dt = float(t.item())
+        dt = shard.max_over_ranks((time.perf_counter() - t0) / ksteps)
         e2e = {"value": b * world / dt, "unit": UNIT, "h2d_bytes_per_step": int(8 * b * C + 8 * b * N ** 3),
                "d2h_bytes_per_step": int(8 * b * N ** 3 + 8 * b * C), "steps": ksteps}
         del hg, hc, hco
