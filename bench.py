@@ -449,6 +449,69 @@ def main_fp64(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+# --------------------------------------------------------------- grid FFT stage
+
+FFT_METRIC = "SO(3) grid FFT stage GB/s (grids <-> pencils, one launch per direction), N={N}, {nf} grids"
+
+
+def main_fft(args) -> None:
+    """The grid FFT stage alone (fftso3_grid_fft) on nf complex64 grids of N^3 samples:
+    one step = the grids -> pencils launch and the pencils -> grids launch.  GB/s counts
+    the algorithmic bytes (each sample read once and written once per launch)."""
+    import torch
+
+    from fftso3_gb300 import _lib
+    from fftso3_gb300 import build as fbuild
+
+    fbuild.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    N, nf = args.fft_n, args.batch
+    gen = torch.Generator(device=dev).manual_seed(3)
+    g = torch.randn((nf, N, N, N), dtype=torch.complex64, device=dev, generator=gen)
+    pen = torch.empty_like(g)
+    back = torch.empty_like(g)
+    nws = _lib.grid_fft_workspace_bytes(N, nf)
+    wbuf = torch.zeros(nws + 256, dtype=torch.uint8, device=dev)
+    ws = wbuf.data_ptr() + (-wbuf.data_ptr()) % 256
+
+    def step():
+        _lib.grid_fft(N, nf, 1, False, g.data_ptr(), pen.data_ptr(), ws, sp)
+        _lib.grid_fft(N, nf, -1, False, pen.data_ptr(), back.data_ptr(), ws, sp)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    _lib.grid_fft_check(ws, sp)
+    ms = e0.elapsed_time(e1) / args.steps
+    idx = (-torch.arange(N, device=dev)) % N
+    rel = float(torch.linalg.vector_norm(back[0] - g[0][:, idx][:, :, idx] * (N * N)) /
+                torch.linalg.vector_norm(g[0] * (N * N)))
+    byts = 2 * 2 * 8.0 * nf * N ** 3  # two launches, each reads and writes every complex64 sample
+    peaks = measured_peaks()
+    gbs = byts / (ms / 1000.0) / 1e9
+    line = {"metric": FFT_METRIC.format(N=N, nf=nf), "value": gbs, "unit": "GB/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (complex64)", "data": "synthetic",
+            "config": {"workload": f"{nf} complex64 grids of {N}^3 samples (N(0,1)), forward then inverse direction",
+                       "l2": f"inputs larger than L2 ({8.0 * nf * N ** 3 / 1e9:.1f} GB per array)"},
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                         "frac": gbs / peaks["hbm_gbs"], "peak_source": peaks["source"],
+                         "algorithmic": "one read + one write of every sample per launch"},
+            "double_transform_rel_err": rel, "gpu_launches": 2 * args.steps,
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 # --------------------------------------------------------------- S^2 batch
 
 S2_METRIC = "S2 real fwd+inv transforms/s, {b} signals at l_max={L}: TC split-BF16 vs FP64"
@@ -594,12 +657,13 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp32", action="store_true", help="skip the FP32 CUDA-core beta-sum comparison")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64 reference (profiling runs)")
-    ap.add_argument("--workload", default="lmax255", choices=["lmax255", "uneven", "s2", "fp64"],
+    ap.add_argument("--workload", default="lmax255", choices=["lmax255", "uneven", "s2", "fp64", "fft"],
                     help="lmax255: the headline SO(3) batch at one l_max (--l-max/--batch); uneven: the "
                          "mixed-bandwidth SO(3) batch; s2: the S^2 batch at l_max=511")
     ap.add_argument("--functions", type=int, default=4096, help="uneven workload: number of functions")
     ap.add_argument("--s2-l-max", type=int, default=511, help="s2 workload: l_max")
     ap.add_argument("--fp64-l-max", type=int, default=127, help="fp64 workload: l_max")
+    ap.add_argument("--fft-n", type=int, default=512, help="fft workload: grid size N (64..512), --batch grids")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -612,6 +676,9 @@ def main() -> None:
         return
     if args.workload == "fp64":
         main_fp64(args)
+        return
+    if args.workload == "fft":
+        main_fft(args)
         return
 
     import torch

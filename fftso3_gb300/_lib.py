@@ -80,6 +80,10 @@ SIGNATURES = {
     "fftso3_batch_set_timing": (_i, [_vp, _i]),
     "fftso3_batch_stage_times": (_i, [_vp, _i, _dp, ctypes.POINTER(_ll), _i]),
     "fftso3_batch_check": (_i, [_vp]),
+    "fftso3_grid_fft_workspace_bytes": (ctypes.c_size_t, [_i, _ll]),
+    "fftso3_grid_fft": (_i, [_i, _ll, _i, _i, _vp, _vp, _vp, _vp]),
+    "fftso3_grid_fft_check": (_i, [_vp, _vp]),
+    "fftso3_grid_fft_reset": (_i, [_vp, _vp]),
 }
 
 _lib = None
@@ -112,6 +116,21 @@ def check(rc: int) -> None:
     if rc != SUCCESS:
         msg = lib().fftso3_last_error_string().decode(errors="replace")
         raise FFTSO3Error(rc, msg)
+
+
+def grid_fft_workspace_bytes(N: int, nf: int) -> int:
+    """Device workspace (bytes) of grid_fft for nf grids of N^3 samples (0: unsupported N)."""
+    return int(lib().fftso3_grid_fft_workspace_bytes(int(N), int(nf)))
+
+
+def grid_fft(N: int, nf: int, direction: int, real: bool, src: int, dst: int, workspace: int, stream: int = 0) -> None:
+    """The grid FFT stage alone (fftso3_grid_fft): direction 1 grids -> pencils, -1 pencils -> grids;
+    device pointers, asynchronous on `stream`; workspace zeroed before its first use."""
+    check(lib().fftso3_grid_fft(int(N), int(nf), int(direction), 1 if real else 0, src, dst, workspace, stream))
+
+
+def grid_fft_check(workspace: int, stream: int = 0) -> None:
+    check(lib().fftso3_grid_fft_check(workspace, stream))
 
 
 class Plan:

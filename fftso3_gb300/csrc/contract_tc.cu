@@ -35,6 +35,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -368,7 +369,13 @@ __global__ void __launch_bounds__(THREADS, 1)
             int kc = 0, t = 0;
             for (int it = blockIdx.x; it < args.nitems && !*abort_flag; it += gridDim.x, ++t) {
                 const int4 item = args.items[it];
-                const int nk = nsteps(item, argsof(item));
+                const GemmArgs& A = argsof(item);
+                const int nk = nsteps(item, A);
+                int m0, n0;
+                item_mn(item, m0, n0);
+                // valid K (zero-padded beyond): the forward sums over N samples, the inverse over nl degrees;
+                // the last k-step issues only the 16-wide MMAs that hold valid K
+                const int kvalid = FWD ? A.N : A.L + 1 - m0;
                 const int ab = t & 1;
                 if (t >= 2 && !mbar_wait(&acce[ab], ((t >> 1) - 1) & 1, args.err, 2)) {
                     *abort_flag = 1;
@@ -385,8 +392,11 @@ __global__ void __launch_bounds__(THREADS, 1)
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                     const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
+                    const int krem = kvalid - i * BK;
+                    const int nkk = krem >= BK ? BK / UK : (krem + UK - 1) / UK;
 #pragma unroll
                     for (int kk = 0; kk < BK / UK; ++kk) {
+                        if (kk >= nkk) break;
 #pragma unroll
                         for (int q = 0; q < 6; ++q) {
                             const uint32_t abase = st + pa[q] * PLANE_BYTES;
@@ -1018,7 +1028,11 @@ struct TCState {
     float* d_wf = nullptr;
     long long total_rows = 0;
     __nv_bfloat16* d_tab[3] = {nullptr, nullptr, nullptr};
-    float2* d_work = nullptr;     // FFT work grid [fn][k][p][q]
+    float2* d_work = nullptr;     // FFT work grid [fn][k][p][q] (two-pass and generic-N FFTs)
+    bool fused_fft = false;       // SO(3), N = 64..512: both FFT passes in one launch through an L2 ring
+    float2* d_ring = nullptr;     // fused FFT: ring of beta-slice chunks
+    size_t ring_elems = 0;
+    int* d_fctl = nullptr;        // fused FFT: tile counter and per-chunk completion counts
     float2* d_pencil = nullptr;   // pencils [fn][p][q][k]
     float2* d_resid = nullptr;    // refinement: residual grid
     float2* d_coef2 = nullptr;    // refinement: correction coefficients
@@ -1088,7 +1102,7 @@ void tc_destroy(TCState* s)
     if (!s) return;
     for (int p = 0; p < 3; ++p)
         if (s->d_tab[p]) cudaFree(s->d_tab[p]);
-    void* ptrs[] = {s->d_tab32, s->d_wf, s->d_work, s->d_pencil, s->d_resid, s->d_coef2, s->d_fc, s->d_grow0, s->d_goff2, s->d_fg,
+    void* ptrs[] = {s->d_tab32, s->d_wf, s->d_work, s->d_ring, s->d_fctl, s->d_pencil, s->d_resid, s->d_coef2, s->d_fc, s->d_grow0, s->d_goff2, s->d_fg,
                     s->d_items_fwd, s->d_items_inv, s->d_err};
     for (void* q : ptrs)
         if (q) cudaFree(q);
@@ -1165,7 +1179,20 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
     }
     const size_t gridel = (size_t)batch * N * N * (s2 ? 1 : N);
     const long long C = s2 ? (long long)s->B * s->B : so3_off(s->B);
-    if ((rc = tc_alloc(s, (void**)&s->d_work, sizeof(float2) * gridel, err))) return bail(rc);
+    // FFT scratch: the fused two-pass FFT needs only a ring of beta-slice chunks
+    // (FFTSO3_TWO_PASS_FFT=1 in the environment selects the two-launch form, for comparison)
+    {
+        const char* ev = getenv("FFTSO3_TWO_PASS_FFT");
+        s->fused_fft = !s2 && fft_grid_fused_supported(N) && !(ev && ev[0] == '1');
+    }
+    if (s->fused_fft) {
+        s->ring_elems = fft_grid_fused_ring_elems(N);
+        if ((rc = tc_alloc(s, (void**)&s->d_ring, sizeof(float2) * s->ring_elems, err))) return bail(rc);
+        if ((rc = tc_alloc(s, (void**)&s->d_fctl, sizeof(int) * fft_grid_fused_ctl_ints(batch, N), err)))
+            return bail(rc);
+    } else if (!(s2 && fft_fast_supported(N))) {
+        if ((rc = tc_alloc(s, (void**)&s->d_work, sizeof(float2) * gridel, err))) return bail(rc);
+    }
     if ((rc = tc_alloc(s, (void**)&s->d_pencil, sizeof(float2) * gridel, err))) return bail(rc);
     if (real)
         if ((rc = tc_alloc(s, (void**)&s->d_fc, sizeof(float2) * (size_t)batch * C, err))) return bail(rc);
@@ -1439,6 +1466,13 @@ static int fft_forward(TCState* s, const void* grid, cudaStream_t st, StageTimer
     const long long N = s->N;
     if (fft_fast_supported(s->N)) {
         // register-resident FFTs; the last pass writes the k-contiguous pencils directly
+        if (s->fused_fft) {
+            T->begin(ST_FFT_2D, st);
+            TCK(launch_fft_grid_fused(grid, s->d_pencil, s->d_ring, s->ring_elems, s->d_fctl, s->d_err, s->batch, s->N, 1, s->d_tw,
+                                      st, s->real));
+            T->end(st);
+            return FFTSO3_SUCCESS;
+        }
         T->begin(ST_FFT_ROWS, st);
         if (s->s2)
             TCK(launch_fft_s2_pass(grid, s->d_pencil, s->batch, s->N, 1, s->d_tw, st, s->real));
@@ -1477,6 +1511,13 @@ static int fft_inverse(TCState* s, void* grid, cudaStream_t st, StageTimer* T, s
         if (s->s2) {
             T->begin(ST_FFT_ROWS, st);
             TCK(launch_fft_s2_pass(s->d_pencil, grid, s->batch, s->N, -1, s->d_tw, st, s->real));
+            T->end(st);
+            return FFTSO3_SUCCESS;
+        }
+        if (s->fused_fft) {
+            T->begin(ST_FFT_2D, st);
+            TCK(launch_fft_grid_fused(s->d_pencil, grid, s->d_ring, s->ring_elems, s->d_fctl, s->d_err, s->batch, s->N, -1, s->d_tw,
+                                      st, s->real));
             T->end(st);
             return FFTSO3_SUCCESS;
         }

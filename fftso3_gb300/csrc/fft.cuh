@@ -44,6 +44,19 @@ cudaError_t launch_fft_rows_fast(const void* in, void* out, long long nlines, in
 // real_io: pass 1 reads real samples (float), pass -1 writes the real part only.
 cudaError_t launch_fft_grid_pass(const void* in, void* out, long long nf, int N, int pass, const void* tw,
                                  cudaStream_t st, bool real_io = false);
+// Both passes of one direction in one persistent launch (N = 64..512): dir 1
+// grid -> pencils (passes 1, 2), dir -1 pencils -> grid (passes -2, -1), the
+// intermediate held in a ring of ring_elems >= fft_grid_fused_ring_elems(N)
+// complex64 (sized for the current device) that stays in L2, instead of a
+// full-size work grid.  ctl: fft_grid_fused_ctl_ints device ints (zeroed by
+// the launch, on st); err: device error word (9 when a wait on another tile
+// timed out).  Same arithmetic as the two-pass form: bit-identical results.
+bool fft_grid_fused_supported(int N);
+size_t fft_grid_fused_ring_elems(int N);
+size_t fft_grid_fused_ctl_ints(long long nf, int N);
+cudaError_t launch_fft_grid_fused(const void* in, void* out, void* ring, size_t ring_elems, int* ctl, int* err,
+                                  long long nf, int N, int dir, const void* tw, cudaStream_t st,
+                                  bool real_io = false);
 // Tiled pass over nf S^2 grids of N^2 complex64 (in != out):
 //   dir  1: grid [nf][k][j]     -> FFT over j -> pencils [nf][p][k]
 //   dir -1: pencils [nf][p][k]  -> FFT over p -> grid [nf][k][j]

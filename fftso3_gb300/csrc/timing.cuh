@@ -17,6 +17,7 @@ enum Stage {
     ST_PACK_INV,
     ST_GEMM_INV,
     ST_REFINE,
+    ST_FFT_2D,
     ST_COUNT
 };
 
@@ -24,7 +25,7 @@ inline const char* stage_name(int s)
 {
     static const char* names[ST_COUNT] = {"fft_rows", "fft_cols", "zero_nyquist", "fp64_fwd_contract",
                                           "fp64_inv_contract", "basis_convert", "tc_pack_fwd", "tc_gemm_fwd",
-                                          "tc_pack_inv", "tc_gemm_inv", "tc_refine_elementwise"};
+                                          "tc_pack_inv", "tc_gemm_inv", "tc_refine_elementwise", "fft_2d"};
     return (s >= 0 && s < ST_COUNT) ? names[s] : "";
 }
 

@@ -235,6 +235,30 @@ int fftso3_batch_check(fftso3_batch* batch);
  * race; serialise them.  l_max above the limit returns FFTSO3_ERR_INVALID_ARG. */
 int fftso3_forward_noalloc(int l_max, const void* grid, void* coeffs, void* stream);
 
+/* The two-dimensional grid FFT stage of the tensor-core SO(3) transforms on
+ * its own (the alpha/gamma FFTs that the reference runs inside its forward
+ * transforms, fdcl_FFTSO3.cpp:689-699 and :805-815).  N = 2(l_max+1) in {64, 128, 256,
+ * 512}; nf grids; in != out, device buffers, asynchronous on `stream`.
+ *   dir = 1:  grids g[f][k][j1][j2] (complex64, or float32 when real != 0) ->
+ *             pencils P[f][p][q][k] = sum_{j1,j2} g[f][k][j1][j2] e^{-2 pi i (p j1 + q j2) / N}
+ *   dir = -1: pencils P[f][p][q][k] -> grids g[f][k][j1][j2] = sum_{p,q} P[f][p][q][k] e^{-2 pi i (p j1 + q j2) / N}
+ *             (complex64; with real != 0 the pencils must be Hermitian, P[f][-p][-q][k] =
+ *             conj P[f][p][q][k] indices mod N, as those of a real grid are, and g is written as float32)
+ * Both directions use the kernel e^{-2 pi i / N} without normalisation (the
+ * inverse SO(3) transform feeds it bin-reversed pencils).  One launch: the
+ * intermediate goes through a small ring in L2, not through device memory.
+ * workspace: fftso3_grid_fft_workspace_bytes(N, nf) bytes of device memory,
+ * 256-byte aligned, zeroed once before first use (its first int is the error
+ * word); calls that share a workspace must not overlap on the GPU.  No
+ * allocation, so the call may be captured into a CUDA graph.
+ * fftso3_grid_fft_check() synchronises `stream` and reports a bounded wait that
+ * gave up (FFTSO3_ERR_CUDA); fftso3_grid_fft_reset() clears the error word. */
+size_t fftso3_grid_fft_workspace_bytes(int N, long long nf);
+int fftso3_grid_fft(int N, long long nf, int dir, int real, const void* in, void* out, void* workspace,
+                    void* stream);
+int fftso3_grid_fft_check(const void* workspace, void* stream);
+int fftso3_grid_fft_reset(void* workspace, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -99,3 +99,19 @@ def test_no_device_is_reported(gblib):
     assert rc == gblib.ERR_NO_DEVICE
     with pytest.raises(gblib.FFTSO3Error):
         gblib.Plan(gblib.SO3_COMPLEX, 5)
+
+
+def test_grid_fft_rejects_bad_arguments_without_device_work(gblib):
+    """Argument checks of the stand-alone grid FFT come before any CUDA call."""
+    L = gblib.lib()
+    assert L.fftso3_grid_fft_workspace_bytes(100, 1) == 0
+    assert L.fftso3_grid_fft_workspace_bytes(64, 0) == 0
+    ws = ctypes.c_void_p(256)  # never dereferenced: every call below fails its checks first
+    a, b = ctypes.c_void_p(4096), ctypes.c_void_p(8192)
+    cases = [(100, 1, 1, a, b, ws, "N must be"), (64, 0, 1, a, b, ws, "number of grids"),
+             (64, 1, 0, a, b, ws, "dir must be"), (64, 1, 1, a, a, ws, "in == out"),
+             (64, 1, 1, a, b, ctypes.c_void_p(264), "256-byte aligned")]
+    for N, nf, d, i, o, w, msg in cases:
+        assert L.fftso3_grid_fft(N, nf, d, 0, i, o, w, None) == gblib.ERR_INVALID_ARG
+        assert msg in L.fftso3_last_error_string().decode()
+    assert L.fftso3_grid_fft_check(None, None) == gblib.ERR_INVALID_ARG

@@ -169,3 +169,34 @@ def test_host_calls_pinned_equal_pageable(gblib, torch_cuda):
     assert np.array_equal(gp.numpy(), g_pageable)
     assert np.array_equal(cp.numpy(), c_pageable)
     assert rel_err(cp.numpy().astype(np.complex128), F.astype(np.complex128)) < TOL
+
+
+@pytest.mark.parametrize("kind,L,b", [("complex", 31, 3), ("real", 31, 2), ("complex", 63, 2),
+                                      ("real", 127, 1), ("complex", 255, 1), ("real", 255, 1)])
+def test_fused_fft_bitwise_equals_two_pass(gblib, torch_cuda, monkeypatch, kind, L, b):
+    """The one-launch FFT (both passes through the L2 ring of beta-slice chunks) gives
+    bit-identical grids and coefficients to the two-launch FFT through a full work grid
+    (FFTSO3_TWO_PASS_FFT=1), for complex and real grids, N = 64 .. 512."""
+    torch = torch_cuda
+    N = 2 * (L + 1)
+    k = gblib.SO3_COMPLEX if kind == "complex" else gblib.SO3_REAL
+    C = (L + 1) * (4 * (L + 1) ** 2 - 1) // 3
+    dt = torch.complex64 if kind == "complex" else torch.float32
+    gen = torch.Generator(device="cuda").manual_seed(L + b)
+    grid = torch.randn(b * N ** 3, dtype=dt, device="cuda", generator=gen)
+    coef = torch.randn(b * C, dtype=dt, device="cuda", generator=gen)
+    s = torch.cuda.current_stream().cuda_stream
+    out = []
+    for two_pass in ("0", "1"):
+        monkeypatch.setenv("FFTSO3_TWO_PASS_FFT", two_pass)
+        p = gblib.Plan(k, L, b, "tc_bf16x3", "stable")
+        g = torch.empty_like(grid)
+        c = torch.empty_like(coef)
+        p.inverse(coef.data_ptr(), g.data_ptr(), s)
+        p.forward(grid.data_ptr(), c.data_ptr(), s)
+        p.check()
+        out.append((g.cpu(), c.cpu()))
+        del p
+    assert torch.equal(out[0][0], out[1][0])
+    assert torch.equal(out[0][1], out[1][1])
+    assert torch.isfinite(out[0][1]).all()
