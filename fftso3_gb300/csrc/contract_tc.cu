@@ -121,6 +121,18 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, in
         : "memory");
 }
 
+// k-steps of table tiles the forward GEMM prefetches into L2 ahead of its TMA ring.
+#ifndef FFTSO3_GEMM_PF
+#define FFTSO3_GEMM_PF 3
+#endif
+
+// L2 prefetch of the same box (no shared memory, no completion to wait for).
+__device__ __forceinline__ void tma_prefetch_2d(const CUtensorMap* tm, int x, int y)
+{
+    asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global.tile [%0, {%1, %2}];" ::"l"((uint64_t)tm), "r"(x), "r"(y)
+                 : "memory");
+}
+
 // UMMA shared-memory descriptor, 128-byte swizzle (SM100 layout code 2, version 1).
 __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
 {
@@ -330,6 +342,35 @@ __global__ void __launch_bounds__(THREADS, 1)
     if (warp == 0) {
         if (lane == 0) {
             // ---------------- TMA producer of the table tiles
+            // The ring holds only STAGES k-steps, so each step's tiles are also
+            // prefetched into L2 PF steps ahead (across item boundaries): the
+            // table streams from HBM with more bytes in flight than the ring.
+            constexpr int PF = FWD ? FFTSO3_GEMM_PF : 0;  // the inverse re-reads each table tile from L2 (4 row tiles)
+            auto prefetch = [&](int it, int i) {
+                if (PF == 0) return;
+                while (it < args.nitems) {
+                    const int4 item = args.items[it];
+                    const GemmArgs& A = argsof(item);
+                    const int nk = nsteps(item, A);
+                    if (i < nk) {
+                        const long long row0 = A.grow0[item.x];
+                        for (int p = 0; p < 3; ++p) {
+                            const CUtensorMap* tm = FUSED ? &segs[item.z >> 16].tm[p] : (p == 0 ? &tA0 : p == 1 ? &tA1 : &tA2);
+                            if (FWD) {
+                                tma_prefetch_2d(tm, i * BK, (int)(row0 + (long long)item.y * BM));
+                            } else {
+                                const int y = (int)(row0 + (long long)i * BK);
+                                tma_prefetch_2d(tm, item.y * BM, y);
+                                tma_prefetch_2d(tm, item.y * BM + 64, y);
+                            }
+                        }
+                        return;
+                    }
+                    i -= nk;
+                    it += gridDim.x;
+                }
+            };
+            for (int i = 0; i < PF; ++i) prefetch(blockIdx.x, i);
             int kc = 0;
             for (int it = blockIdx.x; it < args.nitems && !*abort_flag; it += gridDim.x) {
                 const int4 item = args.items[it];
@@ -340,6 +381,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                 const int nk = nsteps(item, A);
                 const long long row0 = A.grow0[item.x];
                 for (int i = 0; i < nk; ++i, ++kc) {
+                    prefetch(it, i + PF);
                     const int s = kc % STAGES;
                     if (kc >= STAGES && !mbar_wait(&empty[s], ((kc / STAGES) - 1) & 1, args.err, 1)) {
                         *abort_flag = 1;
@@ -504,6 +546,14 @@ __global__ void __launch_bounds__(THREADS, 1)
             }
             float2 nxt[16];
             if (it2 < args.nitems) fetch(snxt, i2, nxt);
+            if (FWD && it2 < args.nitems && snxt.p) {
+                // pencil runs two k-steps further into L2 (the register prefetch covers one)
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int k = (i2 + 2) * BK + (q4 + 4 * h) * 8;
+                    if (k < snxt.lim) asm volatile("prefetch.global.L2 [%0];" ::"l"(snxt.p + k) : "memory");
+                }
+            }
             const int s = kc % STAGES;
             if (kc >= STAGES && !mbar_wait(&empty[s], ((kc / STAGES) - 1) & 1, args.err, 4)) {
                 *abort_flag = 1;
@@ -825,7 +875,7 @@ __device__ __forceinline__ void pair_of(int m, int n, int& g, int& p)
 // group_pairs() (pair_of()).
 constexpr int PT = 32;
 
-// grid: x = n + L (2L + 1), y = l tile (ceil(B / 32)), z = m tile + mtiles * function.
+// grid: x = n + L (2L + 1), y = l tile (ceil(B / 32)), z = m tile + mtiles * (function / PFPC).
 // The m tiles of l tile [l0, l0 + 32) cover only |m| <= min(L, l0 + 31), so
 // small degrees do not run mostly empty tiles.
 __device__ __forceinline__ bool ptile_coords(int L, int& n, int& l0, int& mb, int& f)
@@ -886,63 +936,93 @@ __device__ __forceinline__ void ptile_index(PTileIdx& t, int L, int n, int l0, i
     __syncthreads();
 }
 
+// Functions per CTA of the tiled permutations: the index tables are built once
+// and reused, and two functions' tiles are in flight per iteration.
+constexpr int PFPC = 8;
+
 __global__ void __launch_bounds__(256) group_to_packed_tiled(const float2* __restrict__ Fg, float2* __restrict__ F,
                                                              const long long* __restrict__ goff2, int L,
-                                                             long long cstride)
+                                                             long long cstride, int batch)
 {
-    __shared__ float2 tile[PT][PT + 1];  // [m - mb][l - l0]
+    __shared__ float2 tile[2][PT][PT + 1];  // [function & 1][m - mb][l - l0]
     __shared__ PTileIdx ix;
-    int n, l0, mb, f;
-    if (!ptile_coords(L, n, l0, mb, f)) return;
+    int n, l0, mb, fg;
+    if (!ptile_coords(L, n, l0, mb, fg)) return;
     ptile_index(ix, L, n, l0, mb, goff2);
-    const float2* src = Fg + (long long)f * cstride;
-    // gather: lanes run along l (contiguous in the group-major layout)
-    for (int e = threadIdx.x; e < PT * PT; e += blockDim.x) {
-        const int mi = e / PT, li = e % PT, l = l0 + li;
-        if (l < ix.gm0[mi] || l > L) continue;
-        tile[mi][li] = src[ix.gbase[mi] + l];
-    }
-    __syncthreads();
-    // scatter: lanes run along m (contiguous in the packed layout)
-    float2* dst = F + (long long)f * cstride;
-    for (int e = threadIdx.x; e < PT * PT; e += blockDim.x) {
-        const int li = e / PT, mi = e % PT, l = l0 + li;
-        if (l < ix.gm0[mi] || l > L) continue;
-        dst[ix.pbase[li] + mb + mi] = tile[mi][li];
+    const int fend = min(batch, (fg + 1) * PFPC);
+    for (int f = fg * PFPC; f < fend; f += 2) {
+        const int nfn = f + 1 < fend ? 2 : 1;
+        // gather: lanes run along l (contiguous in the group-major layout)
+#pragma unroll
+        for (int u = 0; u < PT * PT / 256; ++u) {
+            const int e = threadIdx.x + u * 256;
+            const int mi = e / PT, li = e % PT, l = l0 + li;
+            if (l < ix.gm0[mi] || l > L) continue;
+            const long long o = ix.gbase[mi] + l;
+            tile[0][mi][li] = Fg[(long long)f * cstride + o];
+            if (nfn == 2) tile[1][mi][li] = Fg[(long long)(f + 1) * cstride + o];
+        }
+        __syncthreads();
+        // scatter: lanes run along m (contiguous in the packed layout)
+#pragma unroll
+        for (int u = 0; u < PT * PT / 256; ++u) {
+            const int e = threadIdx.x + u * 256;
+            const int li = e / PT, mi = e % PT, l = l0 + li;
+            if (l < ix.gm0[mi] || l > L) continue;
+            const long long o = ix.pbase[li] + mb + mi;
+            F[(long long)f * cstride + o] = tile[0][mi][li];
+            if (nfn == 2) F[(long long)(f + 1) * cstride + o] = tile[1][mi][li];
+        }
+        __syncthreads();
     }
 }
 
 // packed -> scaled group-major Y = (2l+1) sign F(l, pair)
 __global__ void __launch_bounds__(256) packed_to_group_tiled(const float2* __restrict__ F, float2* __restrict__ Y,
                                                              const long long* __restrict__ goff2, int L,
-                                                             long long cstride)
+                                                             long long cstride, int batch)
 {
-    __shared__ float2 tile[PT][PT + 1];  // [m - mb][l - l0]
+    __shared__ float2 tile[2][PT][PT + 1];  // [function & 1][m - mb][l - l0]
     __shared__ PTileIdx ix;
-    int n, l0, mb, f;
-    if (!ptile_coords(L, n, l0, mb, f)) return;
+    int n, l0, mb, fg;
+    if (!ptile_coords(L, n, l0, mb, fg)) return;
     ptile_index(ix, L, n, l0, mb, goff2);
-    const float2* src = F + (long long)f * cstride;
-    for (int e = threadIdx.x; e < PT * PT; e += blockDim.x) {
-        const int li = e / PT, mi = e % PT, l = l0 + li;
-        if (l < ix.gm0[mi] || l > L) continue;
-        tile[mi][li] = src[ix.pbase[li] + mb + mi];
-    }
-    __syncthreads();
-    float2* dst = Y + (long long)f * cstride;
-    for (int e = threadIdx.x; e < PT * PT; e += blockDim.x) {
-        const int mi = e / PT, li = e % PT, l = l0 + li;
-        if (l < ix.gm0[mi] || l > L) continue;
-        const float sc = (float)(2 * l + 1) * ix.gsign[mi];
-        const float2 v = tile[mi][li];
-        dst[ix.gbase[mi] + l] = make_float2(sc * v.x, sc * v.y);
+    const int fend = min(batch, (fg + 1) * PFPC);
+    for (int f = fg * PFPC; f < fend; f += 2) {
+        const int nfn = f + 1 < fend ? 2 : 1;
+#pragma unroll
+        for (int u = 0; u < PT * PT / 256; ++u) {
+            const int e = threadIdx.x + u * 256;
+            const int li = e / PT, mi = e % PT, l = l0 + li;
+            if (l < ix.gm0[mi] || l > L) continue;
+            const long long o = ix.pbase[li] + mb + mi;
+            tile[0][mi][li] = F[(long long)f * cstride + o];
+            if (nfn == 2) tile[1][mi][li] = F[(long long)(f + 1) * cstride + o];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < PT * PT / 256; ++u) {
+            const int e = threadIdx.x + u * 256;
+            const int mi = e / PT, li = e % PT, l = l0 + li;
+            if (l < ix.gm0[mi] || l > L) continue;
+            const float sc = (float)(2 * l + 1) * ix.gsign[mi];
+            const long long o = ix.gbase[mi] + l;
+            const float2 v0 = tile[0][mi][li];
+            Y[(long long)f * cstride + o] = make_float2(sc * v0.x, sc * v0.y);
+            if (nfn == 2) {
+                const float2 v1 = tile[1][mi][li];
+                Y[(long long)(f + 1) * cstride + o] = make_float2(sc * v1.x, sc * v1.y);
+            }
+        }
+        __syncthreads();
     }
 }
 
 static dim3 ptile_grid(int L, int batch)
 {
     const int mtiles = (2 * L + 1 + PT - 1) / PT;
-    return dim3((unsigned)(2 * L + 1), (unsigned)((L + 1 + PT - 1) / PT), (unsigned)(mtiles * batch));
+    const int fgroups = (batch + PFPC - 1) / PFPC;
+    return dim3((unsigned)(2 * L + 1), (unsigned)((L + 1 + PT - 1) / PT), (unsigned)(mtiles * fgroups));
 }
 
 // S^2: group-major forward output -> packed F(l, m) at l^2 + m + l (one CTA per (l, function)).
@@ -1566,7 +1646,7 @@ static int tc_forward_once(TCState* s, const void* grid, float2* F, cudaStream_t
                                                                        coeffs_per_fn(s));
     else
         group_to_packed_tiled<<<ptile_grid(s->L, s->batch), 256, 0, st>>>(s->d_fg, F, s->d_goff2, s->L,
-                                                                    coeffs_per_fn(s));
+                                                                    coeffs_per_fn(s), s->batch);
     TCK(cudaGetLastError());
     T->end(st);
     return FFTSO3_SUCCESS;
@@ -1592,7 +1672,7 @@ static int tc_inverse_once(TCState* s, const float2* F, void* grid, cudaStream_t
                                                                              coeffs_per_fn(s));
     else
         packed_to_group_tiled<<<ptile_grid(s->L, s->batch), 256, 0, st>>>(F, s->d_fg, s->d_goff2, s->L,
-                                                                          coeffs_per_fn(s));
+                                                                          coeffs_per_fn(s), s->batch);
     TCK(cudaGetLastError());
     T->end(st);
     T->begin(ST_GEMM_INV, st);
@@ -1670,7 +1750,7 @@ int tc_forward_finish(TCState* s, void* coeffs, cudaStream_t st, StageTimer* T, 
                                                                        coeffs_per_fn(s));
     else
         group_to_packed_tiled<<<ptile_grid(s->L, s->batch), 256, 0, st>>>(s->d_fg, Fc, s->d_goff2, s->L,
-                                                                    coeffs_per_fn(s));
+                                                                    coeffs_per_fn(s), s->batch);
     TCK(cudaGetLastError());
     if (s->real) {
         if (s->s2)
@@ -1703,7 +1783,7 @@ int tc_inverse_prepare(TCState* s, const void* coeffs, cudaStream_t st, StageTim
         const long long tot = (long long)s->batch * 2 * N * N;
         zero_nyquist_pencils_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(s->d_pencil, (int)N, s->batch);
         packed_to_group_tiled<<<ptile_grid(s->L, s->batch), 256, 0, st>>>(Fc, s->d_fg, s->d_goff2, s->L,
-                                                                          coeffs_per_fn(s));
+                                                                          coeffs_per_fn(s), s->batch);
     }
     TCK(cudaGetLastError());
     T->end(st);
