@@ -208,6 +208,22 @@ __device__ __forceinline__ void split3f(float x, uint16_t& h, uint16_t& m, uint1
     l = __bfloat16_as_ushort(c);
 }
 
+// split3f of two values at once, packed as BF16 pairs (x0 in the low half):
+// one cvt.rn.bf16x2.f32 per term, the BF16 -> FP32 widening by shifts.  The
+// same roundings as split3f, so the same bits.
+__device__ __forceinline__ void split3f_pair(float x0, float x1, uint32_t& h, uint32_t& m, uint32_t& l)
+{
+    auto pack = [](float a, float b) {
+        const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);  // .x = a (low half), .y = b
+        return *reinterpret_cast<const uint32_t*>(&v);
+    };
+    h = pack(x0, x1);
+    const float r0 = x0 - __uint_as_float(h << 16), r1 = x1 - __uint_as_float(h & 0xffff0000u);
+    m = pack(r0, r1);
+    const float s0 = r0 - __uint_as_float(m << 16), s1 = r1 - __uint_as_float(m & 0xffff0000u);
+    l = pack(s0, s1);
+}
+
 struct GemmArgs {
     const int4* items;         // (group, row tile, column tile, -)
     int nitems;
@@ -245,14 +261,7 @@ __device__ __forceinline__ void store_chunk(uint32_t bplanes, int R, int chunk, 
 {
     uint32_t w[3][4];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        uint16_t h0, m0, l0, h1, m1, l1;
-        split3f(x8[2 * j], h0, m0, l0);
-        split3f(x8[2 * j + 1], h1, m1, l1);
-        w[0][j] = (uint32_t)h0 | ((uint32_t)h1 << 16);
-        w[1][j] = (uint32_t)m0 | ((uint32_t)m1 << 16);
-        w[2][j] = (uint32_t)l0 | ((uint32_t)l1 << 16);
-    }
+    for (int j = 0; j < 4; ++j) split3f_pair(x8[2 * j], x8[2 * j + 1], w[0][j], w[1][j], w[2][j]);
     const uint32_t off = (uint32_t)R * 128u + (uint32_t)((chunk ^ (R & 7)) * 16);
 #pragma unroll
     for (int pl = 0; pl < 3; ++pl) {
