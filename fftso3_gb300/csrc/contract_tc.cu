@@ -226,6 +226,7 @@ __device__ __forceinline__ void split3f_pair(float x0, float x1, uint32_t& h, ui
 
 struct GemmArgs {
     const int4* items;         // (group, row tile, column tile, -)
+    const int2* iaux;          // per item: (group-major offset goff2[g], first table row grow0[g])
     int nitems;
     const long long* grow0;    // first table row of each group
     int L, N, Kp, batch;
@@ -362,7 +363,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                     const GemmArgs& A = argsof(item);
                     const int nk = nsteps(item, A);
                     if (i < nk) {
-                        const long long row0 = A.grow0[item.x];
+                        const long long row0 = args.iaux[it].y;
                         for (int p = 0; p < 3; ++p) {
                             const CUtensorMap* tm = FUSED ? &segs[item.z >> 16].tm[p] : (p == 0 ? &tA0 : p == 1 ? &tA1 : &tA2);
                             if (FWD) {
@@ -388,7 +389,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                                             FUSED ? &segs[item.z >> 16].tm[1] : &tA1,
                                             FUSED ? &segs[item.z >> 16].tm[2] : &tA2};
                 const int nk = nsteps(item, A);
-                const long long row0 = A.grow0[item.x];
+                const long long row0 = args.iaux[it].y;
                 for (int i = 0; i < nk; ++i, ++kc) {
                     prefetch(it, i + PF);
                     const int s = kc % STAGES;
@@ -487,8 +488,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             int N;            // the item's grid size (weights are zero beyond it)
             const float* wf;  // the item's quadrature weights (fused launches)
         };
-        auto source = [&](int it) -> Src {
-            const int4 item = args.items[it];
+        auto source = [&](const int4& item, const int2& aux) -> Src {
             const GemmArgs& A = argsof(item);
             const int N = A.N;
             int m0, n0;
@@ -509,7 +509,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                 int qi = (-P.n[pp]) % N; if (qi < 0) qi += N;
                 r.p = A.pin + (long long)f * A.fstride + ((long long)pi * N + qi) * N;
             } else {
-                r.p = A.cin + (long long)f * A.cstride + A.goff2[item.x] + (long long)pp * r.lim;
+                r.p = A.cin + (long long)f * A.cstride + aux.x + (long long)pp * r.lim;
             }
             return r;
         };
@@ -537,10 +537,18 @@ __global__ void __launch_bounds__(THREADS, 1)
         float2 cur[16];
         Src scur, snxt;
         int nk_cur = 0;
+        // the next item's metadata is loaded one item ahead (no dependent load at a transition)
+        int4 pitem = make_int4(0, 0, 0, 0);
+        int2 paux = make_int2(0, 0);
         if (it < args.nitems) {
-            scur = source(it);
-            nk_cur = nsteps(args.items[it], argsof(args.items[it]));
+            const int4 item0 = args.items[it];
+            scur = source(item0, args.iaux[it]);
+            nk_cur = nsteps(item0, argsof(item0));
             fetch(scur, 0, cur);
+            if (it + (int)gridDim.x < args.nitems) {
+                pitem = args.items[it + gridDim.x];
+                paux = args.iaux[it + gridDim.x];
+            }
         }
         while (it < args.nitems && !*abort_flag) {
             int it2 = it, i2 = i + 1, nk2 = nk_cur;
@@ -549,8 +557,12 @@ __global__ void __launch_bounds__(THREADS, 1)
                 it2 += gridDim.x;
                 i2 = 0;
                 if (it2 < args.nitems) {
-                    snxt = source(it2);
-                    nk2 = nsteps(args.items[it2], argsof(args.items[it2]));
+                    snxt = source(pitem, paux);
+                    nk2 = nsteps(pitem, argsof(pitem));
+                    if (it2 + (int)gridDim.x < args.nitems) {
+                        pitem = args.items[it2 + gridDim.x];
+                        paux = args.iaux[it2 + gridDim.x];
+                    }
                 }
             }
             float2 nxt[16];
@@ -601,8 +613,19 @@ __global__ void __launch_bounds__(THREADS, 1)
         const int quarter = warp & 3;
         const int r = quarter * 32 + lane;
         int t = 0;
+        int4 nitem = make_int4(0, 0, 0, 0);
+        int2 naux = make_int2(0, 0);
+        if (blockIdx.x < args.nitems) {
+            nitem = args.items[blockIdx.x];
+            naux = args.iaux[blockIdx.x];
+        }
         for (int it = blockIdx.x; it < args.nitems && !*abort_flag; it += gridDim.x, ++t) {
-            const int4 item = args.items[it];
+            const int4 item = nitem;
+            const int2 aux = naux;
+            if (it + (int)gridDim.x < args.nitems) {  // one item ahead
+                nitem = args.items[it + gridDim.x];
+                naux = args.iaux[it + gridDim.x];
+            }
             const GemmArgs& A = argsof(item);
             const int N = A.N;
             int m0, n0;
@@ -613,7 +636,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
             for (int p = 0; p < 4; ++p) {
                 if (FWD) {
-                    poff[p] = A.goff2[item.x] + (long long)p * nl;
+                    poff[p] = aux.x + (long long)p * nl;
                 } else if (S2) {
                     int bin = (p == 0 ? -m0 : m0) % N; if (bin < 0) bin += N;
                     poff[p] = (long long)bin * N;
@@ -1133,6 +1156,9 @@ struct TCState {
     int4* d_items_inv = nullptr;
     int n_items_fwd = 0, n_items_inv = 0;
     std::vector<int4> items_h[2];  // host copies (forward, inverse), for fused launches
+    std::vector<int2> iaux_h[2];   // per item (goff2[g], grow0[g]), same order
+    int2* d_iaux_fwd = nullptr;
+    int2* d_iaux_inv = nullptr;
     int nsm = 0;
     CUtensorMap tmA_fwd[3], tmA_inv[3];
     int* d_err = nullptr;
@@ -1192,7 +1218,7 @@ void tc_destroy(TCState* s)
     for (int p = 0; p < 3; ++p)
         if (s->d_tab[p]) cudaFree(s->d_tab[p]);
     void* ptrs[] = {s->d_tab32, s->d_wf, s->d_work, s->d_ring, s->d_fctl, s->d_pencil, s->d_resid, s->d_coef2, s->d_fc, s->d_grow0, s->d_goff2, s->d_fg,
-                    s->d_items_fwd, s->d_items_inv, s->d_err};
+                    s->d_items_fwd, s->d_items_inv, s->d_iaux_fwd, s->d_iaux_inv, s->d_err};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     delete s;
@@ -1318,12 +1344,27 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
         err = "internal: group-major layout does not cover the coefficients";
         return bail(FFTSO3_ERR_CUDA);
     }
+    if (acc2 > 0x7fffffffLL || s->total_rows > 0x7fffffffLL) {
+        err = "internal: per-item offsets exceed 32 bits";
+        return bail(FFTSO3_ERR_UNSUPPORTED);
+    }
+    for (int d = 0; d < 2; ++d) {
+        s->iaux_h[d].resize(s->items_h[d].size());
+        for (size_t i = 0; i < s->items_h[d].size(); ++i) {
+            const int g = s->items_h[d][i].x;
+            s->iaux_h[d][i] = make_int2((int)goff2[g], (int)grow0[g]);
+        }
+    }
     if ((rc = tc_alloc(s, (void**)&s->d_grow0, sizeof(long long) * grow0.size(), err))) return bail(rc);
     if ((rc = tc_alloc(s, (void**)&s->d_goff2, sizeof(long long) * goff2.size(), err))) return bail(rc);
     if ((rc = tc_alloc(s, (void**)&s->d_fg, sizeof(float2) * (size_t)batch * acc2, err))) return bail(rc);
     cudaMemcpy(s->d_goff2, goff2.data(), sizeof(long long) * goff2.size(), cudaMemcpyHostToDevice);
     if ((rc = tc_alloc(s, (void**)&s->d_items_fwd, sizeof(int4) * itf.size(), err))) return bail(rc);
     if ((rc = tc_alloc(s, (void**)&s->d_items_inv, sizeof(int4) * iti.size(), err))) return bail(rc);
+    if ((rc = tc_alloc(s, (void**)&s->d_iaux_fwd, sizeof(int2) * itf.size(), err))) return bail(rc);
+    if ((rc = tc_alloc(s, (void**)&s->d_iaux_inv, sizeof(int2) * iti.size(), err))) return bail(rc);
+    cudaMemcpy(s->d_iaux_fwd, s->iaux_h[0].data(), sizeof(int2) * itf.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(s->d_iaux_inv, s->iaux_h[1].data(), sizeof(int2) * iti.size(), cudaMemcpyHostToDevice);
     if ((rc = tc_alloc(s, (void**)&s->d_err, sizeof(int), err))) return bail(rc);
     cudaMemcpy(s->d_grow0, grow0.data(), sizeof(long long) * grow0.size(), cudaMemcpyHostToDevice);
     cudaMemcpy(s->d_items_fwd, itf.data(), sizeof(int4) * itf.size(), cudaMemcpyHostToDevice);
@@ -1489,6 +1530,7 @@ static GemmArgs gemm_args(const TCState* s)
 {
     GemmArgs a;
     a.items = nullptr;
+    a.iaux = nullptr;
     a.nitems = 0;
     a.grow0 = s->d_grow0;
     a.goff2 = s->d_goff2;
@@ -1511,6 +1553,7 @@ static int launch_gemm(TCState* s, bool fwd, cudaStream_t st, std::string& err)
 {
     GemmArgs a = gemm_args(s);
     a.items = fwd ? s->d_items_fwd : s->d_items_inv;
+    a.iaux = fwd ? s->d_iaux_fwd : s->d_iaux_inv;
     a.nitems = fwd ? s->n_items_fwd : s->n_items_inv;
     if (fwd) {
         a.pin = s->d_pencil;
@@ -1808,6 +1851,7 @@ struct TCFused {
     std::vector<TCState*> parts;
     GemmSeg* d_segs[2] = {nullptr, nullptr};  // forward, inverse
     int4* d_items[2] = {nullptr, nullptr};
+    int2* d_iaux[2] = {nullptr, nullptr};
     int nitems[2] = {0, 0};
     int* d_err = nullptr;
     int nsm = 0;
@@ -1820,6 +1864,7 @@ void tc_fused_destroy(TCFused* f)
     for (int d = 0; d < 2; ++d) {
         if (f->d_segs[d]) cudaFree(f->d_segs[d]);
         if (f->d_items[d]) cudaFree(f->d_items[d]);
+        if (f->d_iaux[d]) cudaFree(f->d_iaux[d]);
     }
     if (f->d_err) cudaFree(f->d_err);
     delete f;
@@ -1853,7 +1898,12 @@ int tc_fused_create(TCFused** out, const std::vector<TCState*>& parts, std::stri
     for (int d = 0; d < 2; ++d) {
         const bool fwd = d == 0;
         std::vector<GemmSeg> segs(parts.size());
-        std::vector<std::pair<int, int4>> items;
+        struct FItem {
+            int nk;
+            int4 it;
+            int2 aux;
+        };
+        std::vector<FItem> items;
         for (size_t i = 0; i < parts.size(); ++i) {
             TCState* p = parts[i];
             GemmArgs a = gemm_args(p);
@@ -1866,16 +1916,20 @@ int tc_fused_create(TCFused** out, const std::vector<TCState*>& parts, std::stri
             }
             segs[i].a = a;
             for (int q = 0; q < 3; ++q) segs[i].tm[q] = fwd ? p->tmA_fwd[q] : p->tmA_inv[q];
-            for (const int4& it : p->items_h[d]) {
+            for (size_t j = 0; j < p->items_h[d].size(); ++j) {
+                const int4& it = p->items_h[d][j];
                 const int m0 = it.w >> 16;
                 const int nk = fwd ? p->Kp / BK : (p->B - m0 + BK - 1) / BK;
-                items.push_back({nk, make_int4(it.x, it.y, ((int)i << 16) | it.z, it.w)});
+                items.push_back({nk, make_int4(it.x, it.y, ((int)i << 16) | it.z, it.w), p->iaux_h[d][j]});
             }
         }
-        std::stable_sort(items.begin(), items.end(),
-                         [](const std::pair<int, int4>& a, const std::pair<int, int4>& b) { return a.first > b.first; });
+        std::stable_sort(items.begin(), items.end(), [](const FItem& a, const FItem& b) { return a.nk > b.nk; });
         std::vector<int4> flat(items.size());
-        for (size_t i = 0; i < items.size(); ++i) flat[i] = items[i].second;
+        std::vector<int2> faux(items.size());
+        for (size_t i = 0; i < items.size(); ++i) {
+            flat[i] = items[i].it;
+            faux[i] = items[i].aux;
+        }
         f->nitems[d] = (int)flat.size();
         if ((e = cudaMalloc(&f->d_segs[d], sizeof(GemmSeg) * segs.size())) != cudaSuccess) return fail(e, "cudaMalloc");
         if ((e = cudaMalloc(&f->d_items[d], sizeof(int4) * std::max<size_t>(flat.size(), 1))) != cudaSuccess)
@@ -1884,6 +1938,11 @@ int tc_fused_create(TCFused** out, const std::vector<TCState*>& parts, std::stri
             cudaSuccess)
             return fail(e, "cudaMemcpy");
         if (!flat.empty() && (e = cudaMemcpy(f->d_items[d], flat.data(), sizeof(int4) * flat.size(),
+                                             cudaMemcpyHostToDevice)) != cudaSuccess)
+            return fail(e, "cudaMemcpy");
+        if ((e = cudaMalloc(&f->d_iaux[d], sizeof(int2) * std::max<size_t>(faux.size(), 1))) != cudaSuccess)
+            return fail(e, "cudaMalloc");
+        if (!faux.empty() && (e = cudaMemcpy(f->d_iaux[d], faux.data(), sizeof(int2) * faux.size(),
                                              cudaMemcpyHostToDevice)) != cudaSuccess)
             return fail(e, "cudaMemcpy");
     }
@@ -1900,6 +1959,7 @@ int tc_fused_gemm(TCFused* f, bool fwd, cudaStream_t st, StageTimer* T, std::str
     if (f->nitems[d] == 0) return FFTSO3_SUCCESS;
     GemmArgs a = gemm_args(f->parts[0]);
     a.items = f->d_items[d];
+    a.iaux = f->d_iaux[d];
     a.nitems = f->nitems[d];
     a.err = f->d_err;
     const int nctas = a.nitems < f->nsm ? a.nitems : f->nsm;
