@@ -126,6 +126,32 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, in
 #define FFTSO3_GEMM_PF 3
 #endif
 
+// The same box delivered to the same shared-memory offset of every CTA of the
+// cluster in ctaMask, each CTA's barrier at that offset receiving the bytes.
+__device__ __forceinline__ void tma_load_2d_mc(void* dst, const CUtensorMap* tm, int x, int y, uint64_t* bar,
+                                               uint16_t mask)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster"
+        " [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(smem_u32(dst)),
+        "l"((uint64_t)tm), "r"(x), "r"(y), "r"(smem_u32(bar)), "h"(mask)
+        : "memory");
+}
+
+__device__ __forceinline__ uint32_t cluster_rank()
+{
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+// All threads of every CTA of the cluster.
+__device__ __forceinline__ void cluster_sync()
+{
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
 // L2 prefetch of the same box (no shared memory, no completion to wait for).
 __device__ __forceinline__ void tma_prefetch_2d(const CUtensorMap* tm, int x, int y)
 {
@@ -169,9 +195,19 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar)
                  : "memory");
 }
 
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
+// Completion of this CTA's MMAs arrives on the barrier at the same offset in every CTA of ctaMask.
+__device__ __forceinline__ void mma_commit_mc(uint64_t* bar, uint16_t mask)
 {
-    uint32_t r[32];
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+            smem_u32(bar)),
+        "h"(mask)
+        : "memory");
+}
+
+// 32 consecutive columns of this thread's TMEM lane (no wait).
+__device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, uint32_t (&r)[32])
+{
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
         "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
@@ -181,9 +217,17 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
           "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
           "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
         : "r"(taddr));
+}
+
+// hi + lo accumulator columns [c, c + 32): both loads in flight, one wait.
+__device__ __forceinline__ void tmem_ld32_sum(uint32_t thi, uint32_t tlo, float* v)
+{
+    uint32_t a[32], b[32];
+    tmem_ld32_nowait(thi, a);
+    tmem_ld32_nowait(tlo, b);
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(a[i]) + __uint_as_float(b[i]);
 }
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar)
@@ -228,6 +272,7 @@ struct GemmArgs {
     const int4* items;         // (group, row tile, column tile, -)
     const int2* iaux;          // per item: (group-major offset goff2[g], first table row grow0[g])
     int nitems;
+    int csize;                 // CTAs per cluster sharing each table tile (items in blocks of csize)
     const long long* grow0;    // first table row of each group
     int L, N, Kp, batch;
     long long fstride;         // pencil elements per function (N^3)
@@ -297,6 +342,12 @@ __device__ __forceinline__ GroupPairs s2_pairs(int m)
 // FUSED = true: the work list spans several plans (segments); each item's
 // table map, sizes and buffers come from segs[item.z >> 16] (args then holds
 // only the merged item list and the error word).
+// args.csize = C > 1: the launch is in clusters of C CTAs and the work list in
+// blocks of C items with the same (group, row tile) and consecutive column
+// tiles; the C CTAs of a cluster take one block together, each table tile is
+// read once for all of them (each CTA issues its share of the tile's TMA boxes
+// with cluster multicast) and a stage is released when all C CTAs' MMAs are
+// done with it (multicast commits; empty barriers count C).
 template <bool FWD, bool S2, bool FUSED>
 __global__ void __launch_bounds__(THREADS, 1)
     so3_tc_gemm_kernel(const __grid_constant__ CUtensorMap tA0, const __grid_constant__ CUtensorMap tA1,
@@ -325,10 +376,13 @@ __global__ void __launch_bounds__(THREADS, 1)
         return FWD ? A.Kp / BK : (A.L + 1 - m0 + BK - 1) / BK;
     };
 
+    const int CL = FUSED ? 1 : args.csize;
+    const uint32_t crank = CL > 1 ? cluster_rank() : 0;
+    const uint16_t cmask = (uint16_t)((1u << CL) - 1u);
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
             mbar_init(&full[s], 1 + NPROD);
-            mbar_init(&empty[s], 1);
+            mbar_init(&empty[s], CL);
         }
         for (int b = 0; b < 2; ++b) {
             mbar_init(&accf[b], 1);
@@ -346,6 +400,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
+    if (CL > 1) cluster_sync();  // every CTA's barriers initialised before any multicast reaches them
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
 
@@ -367,11 +422,11 @@ __global__ void __launch_bounds__(THREADS, 1)
                         for (int p = 0; p < 3; ++p) {
                             const CUtensorMap* tm = FUSED ? &segs[item.z >> 16].tm[p] : (p == 0 ? &tA0 : p == 1 ? &tA1 : &tA2);
                             if (FWD) {
-                                tma_prefetch_2d(tm, i * BK, (int)(row0 + (long long)item.y * BM));
+                                if (p % CL == (int)crank) tma_prefetch_2d(tm, i * BK, (int)(row0 + (long long)item.y * BM));
                             } else {
                                 const int y = (int)(row0 + (long long)i * BK);
-                                tma_prefetch_2d(tm, item.y * BM, y);
-                                tma_prefetch_2d(tm, item.y * BM + 64, y);
+                                if ((2 * p) % CL == (int)crank) tma_prefetch_2d(tm, item.y * BM, y);
+                                if ((2 * p + 1) % CL == (int)crank) tma_prefetch_2d(tm, item.y * BM + 64, y);
                             }
                         }
                         return;
@@ -398,19 +453,36 @@ __global__ void __launch_bounds__(THREADS, 1)
                         break;
                     }
                     unsigned char* st = smem + s * STAGE_BYTES;
-                    mbar_expect_tx(&full[s], STAGE_A);
+                    mbar_expect_tx(&full[s], STAGE_A);  // the whole tile lands in every CTA of the cluster
+                    // the tile's boxes: plane p (forward), or plane p half h (inverse) = box j = 2 p + h;
+                    // box j is issued by cluster rank j mod C
                     for (int p = 0; p < 3; ++p) {
                         unsigned char* a = st + p * PLANE_BYTES;
                         if (FWD) {
-                            tma_load_2d(a, tA[p], i * BK, (int)(row0 + (long long)item.y * BM), &full[s]);
+                            if (p % CL != (int)crank) continue;
+                            if (CL > 1)
+                                tma_load_2d_mc(a, tA[p], i * BK, (int)(row0 + (long long)item.y * BM), &full[s], cmask);
+                            else
+                                tma_load_2d(a, tA[p], i * BK, (int)(row0 + (long long)item.y * BM), &full[s]);
                         } else {
                             const int y = (int)(row0 + (long long)i * BK);
-                            tma_load_2d(a, tA[p], item.y * BM, y, &full[s]);
-                            tma_load_2d(a + PLANE_BYTES / 2, tA[p], item.y * BM + 64, y, &full[s]);
+                            for (int h = 0; h < 2; ++h) {
+                                if ((2 * p + h) % CL != (int)crank) continue;
+                                if (CL > 1)
+                                    tma_load_2d_mc(a + h * (PLANE_BYTES / 2), tA[p], item.y * BM + 64 * h, y, &full[s],
+                                                   cmask);
+                                else
+                                    tma_load_2d(a + h * (PLANE_BYTES / 2), tA[p], item.y * BM + 64 * h, y, &full[s]);
+                            }
                         }
                     }
                 }
             }
+            // cluster: the last stages' tiles (this CTA's boxes and the other CTAs' multicasts) have
+            // landed in this CTA before the cluster's final barrier lets any CTA exit
+            if (CL > 1)
+                for (int k = (kc > STAGES ? kc - STAGES : 0); k < kc; ++k)
+                    mbar_wait(&full[k % STAGES], (k / STAGES) & 1, args.err, 7);
         }
     } else if (warp == 1) {
         if (lane == 0) {
@@ -460,7 +532,10 @@ __global__ void __launch_bounds__(THREADS, 1)
                             mma_bf16(q == 0 ? dhi : dlo, ad, bd, idesc, first ? 0u : 1u);
                         }
                     }
-                    mma_commit(&empty[s]);
+                    if (CL > 1)
+                        mma_commit_mc(&empty[s], cmask);  // the stage's table tile is shared by the cluster
+                    else
+                        mma_commit(&empty[s]);
                 }
                 mma_commit(&accf[ab]);
                 if (!ok) {
@@ -654,11 +729,8 @@ __global__ void __launch_bounds__(THREADS, 1)
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t trow = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(ab * 256);
             for (int chunk = 0; chunk < BN / 32; ++chunk) {
-                float v[32], u[32];
-                tmem_ld32(trow + chunk * 32, v);
-                tmem_ld32(trow + 128 + chunk * 32, u);
-#pragma unroll
-                for (int j = 0; j < 32; ++j) v[j] += u[j];
+                float v[32];
+                tmem_ld32_sum(trow + chunk * 32, trow + 128 + chunk * 32, v);
 #pragma unroll
                 for (int fq = 0; fq < 32 / (2 * PPF); ++fq) {
                     const int f = ctile(item) * FPTK + chunk * (32 / (2 * PPF)) + fq;
@@ -692,6 +764,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
+    if (CL > 1) cluster_sync();  // no CTA exits while another may still multicast into it or arrive on its barriers
     if (warp == 1) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
@@ -1128,6 +1201,7 @@ using namespace tc;
 
 struct TCState {
     int L = 0, B = 0, N = 0, Kp = 0, batch = 0, ntiles = 0, ngroups = 0;
+    int csize = 1;                 // CTAs per cluster of the tensor-core GEMM launches (shared table tiles)
     bool refine = false;
     bool real = false;            // real grids (FFTSO3_*_REAL): real samples in, real part out
     bool s2 = false;              // S^2 (Legendre groups g = m, grids N^2) instead of SO(3)
@@ -1335,10 +1409,47 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
         const int ma = a.w >> 16, mb = b.w >> 16;
         return (s->B - ma + BK - 1) / BK > (s->B - mb + BK - 1) / BK;
     });
+    s->items_h[0] = itf;  // one-CTA order, for fused launches over several plans
+    s->items_h[1] = iti;
+    // Launch lists.  With column tiles to share, clusters of C CTAs (C a power of two <= column tiles, at
+    // most FFTSO3_GEMM_CLUSTER, default 2) take blocks of C items (same group and row tile, consecutive
+    // column tiles; tiles past the batch are empty) and read each table tile once for the block.
+    {
+        const char* ev = getenv("FFTSO3_GEMM_CLUSTER");
+        int cmax = ev ? atoi(ev) : 2;
+        cmax = cmax >= 4 ? 4 : cmax >= 2 ? 2 : 1;
+        int cl = 1;
+        if (!simt)
+            while (cl * 2 <= cmax && cl * 2 <= s->ntiles) cl *= 2;
+        s->csize = cl;
+    }
+    if (s->csize > 1) {
+        const int CLs = s->csize, ntb = (s->ntiles + CLs - 1) / CLs;
+        std::vector<std::vector<int4>> blocks;
+        itf.clear();
+        for (int g = 0; g < s->ngroups; ++g) {
+            int m0 = g, n0 = 0;
+            if (!s2) group_mn(g, m0, n0);
+            const int nl = s->B - m0;
+            for (int mt = 0; mt * BM < nl; ++mt)
+                for (int b = 0; b < ntb; ++b)
+                    for (int r = 0; r < CLs; ++r) itf.push_back(make_int4(g, mt, b * CLs + r, item_w(m0, n0)));
+            for (int mt = 0; mt * BM < N; ++mt)
+                for (int b = 0; b < ntb; ++b) {
+                    std::vector<int4> blk;
+                    for (int r = 0; r < CLs; ++r) blk.push_back(make_int4(g, mt, b * CLs + r, item_w(m0, n0)));
+                    blocks.push_back(blk);
+                }
+        }
+        std::stable_sort(blocks.begin(), blocks.end(), [&](const std::vector<int4>& a, const std::vector<int4>& b) {
+            const int ma = a[0].w >> 16, mb = b[0].w >> 16;
+            return (s->B - ma + BK - 1) / BK > (s->B - mb + BK - 1) / BK;
+        });
+        iti.clear();
+        for (const auto& blk : blocks) iti.insert(iti.end(), blk.begin(), blk.end());
+    }
     s->n_items_fwd = (int)itf.size();
     s->n_items_inv = (int)iti.size();
-    s->items_h[0] = itf;
-    s->items_h[1] = iti;
     goff2[s->ngroups] = acc2;
     if (acc2 != C) {
         err = "internal: group-major layout does not cover the coefficients";
@@ -1355,6 +1466,9 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
             s->iaux_h[d][i] = make_int2((int)goff2[g], (int)grow0[g]);
         }
     }
+    std::vector<int2> auxf(itf.size()), auxi(iti.size());
+    for (size_t i = 0; i < itf.size(); ++i) auxf[i] = make_int2((int)goff2[itf[i].x], (int)grow0[itf[i].x]);
+    for (size_t i = 0; i < iti.size(); ++i) auxi[i] = make_int2((int)goff2[iti[i].x], (int)grow0[iti[i].x]);
     if ((rc = tc_alloc(s, (void**)&s->d_grow0, sizeof(long long) * grow0.size(), err))) return bail(rc);
     if ((rc = tc_alloc(s, (void**)&s->d_goff2, sizeof(long long) * goff2.size(), err))) return bail(rc);
     if ((rc = tc_alloc(s, (void**)&s->d_fg, sizeof(float2) * (size_t)batch * acc2, err))) return bail(rc);
@@ -1363,8 +1477,8 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
     if ((rc = tc_alloc(s, (void**)&s->d_items_inv, sizeof(int4) * iti.size(), err))) return bail(rc);
     if ((rc = tc_alloc(s, (void**)&s->d_iaux_fwd, sizeof(int2) * itf.size(), err))) return bail(rc);
     if ((rc = tc_alloc(s, (void**)&s->d_iaux_inv, sizeof(int2) * iti.size(), err))) return bail(rc);
-    cudaMemcpy(s->d_iaux_fwd, s->iaux_h[0].data(), sizeof(int2) * itf.size(), cudaMemcpyHostToDevice);
-    cudaMemcpy(s->d_iaux_inv, s->iaux_h[1].data(), sizeof(int2) * iti.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(s->d_iaux_fwd, auxf.data(), sizeof(int2) * itf.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(s->d_iaux_inv, auxi.data(), sizeof(int2) * iti.size(), cudaMemcpyHostToDevice);
     if ((rc = tc_alloc(s, (void**)&s->d_err, sizeof(int), err))) return bail(rc);
     cudaMemcpy(s->d_grow0, grow0.data(), sizeof(long long) * grow0.size(), cudaMemcpyHostToDevice);
     cudaMemcpy(s->d_items_fwd, itf.data(), sizeof(int4) * itf.size(), cudaMemcpyHostToDevice);
@@ -1532,6 +1646,7 @@ static GemmArgs gemm_args(const TCState* s)
     a.items = nullptr;
     a.iaux = nullptr;
     a.nitems = 0;
+    a.csize = 1;
     a.grow0 = s->d_grow0;
     a.goff2 = s->d_goff2;
     a.L = s->L;
@@ -1574,17 +1689,39 @@ static int launch_gemm(TCState* s, bool fwd, cudaStream_t st, std::string& err)
         TCK(cudaGetLastError());
         return FFTSO3_SUCCESS;
     }
-    const int nctas = a.nitems < s->nsm ? a.nitems : s->nsm;
     const CUtensorMap* tm = fwd ? s->tmA_fwd : s->tmA_inv;
-    if (fwd && s->s2)
-        so3_tc_gemm_kernel<true, true, false><<<nctas, THREADS, SMEM_BYTES, st>>>(tm[0], tm[1], tm[2], a, nullptr);
-    else if (fwd)
-        so3_tc_gemm_kernel<true, false, false><<<nctas, THREADS, SMEM_BYTES, st>>>(tm[0], tm[1], tm[2], a, nullptr);
-    else if (s->s2)
-        so3_tc_gemm_kernel<false, true, false><<<nctas, THREADS, SMEM_BYTES, st>>>(tm[0], tm[1], tm[2], a, nullptr);
-    else
-        so3_tc_gemm_kernel<false, false, false><<<nctas, THREADS, SMEM_BYTES, st>>>(tm[0], tm[1], tm[2], a, nullptr);
-    TCK(cudaGetLastError());
+    auto kern = fwd ? (s->s2 ? so3_tc_gemm_kernel<true, true, false> : so3_tc_gemm_kernel<true, false, false>)
+                    : (s->s2 ? so3_tc_gemm_kernel<false, true, false> : so3_tc_gemm_kernel<false, false, false>);
+    if (s->csize == 1) {
+        const int nctas = a.nitems < s->nsm ? a.nitems : s->nsm;
+        kern<<<nctas, THREADS, SMEM_BYTES, st>>>(tm[0], tm[1], tm[2], a, nullptr);
+        TCK(cudaGetLastError());
+        return FFTSO3_SUCCESS;
+    }
+    // clusters of csize CTAs (the item list is in blocks of csize): as many clusters as fit at once
+    a.csize = s->csize;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)s->csize;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(THREADS);
+    cfg.dynamicSmemBytes = SMEM_BYTES;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cfg.gridDim = dim3((unsigned)s->csize);
+    int nclusters = 0;
+    TCK(cudaOccupancyMaxActiveClusters(&nclusters, kern, &cfg));
+    if (nclusters < 1) {
+        err = "tensor-core GEMM: no cluster of " + std::to_string(s->csize) + " CTAs fits on this device";
+        return FFTSO3_ERR_UNSUPPORTED;
+    }
+    long long nctas = (long long)nclusters * s->csize;
+    if (nctas > a.nitems) nctas = a.nitems;  // a.nitems is a multiple of csize
+    cfg.gridDim = dim3((unsigned)nctas);
+    TCK(cudaLaunchKernelEx(&cfg, kern, tm[0], tm[1], tm[2], a, (const GemmSeg*)nullptr));
     return FFTSO3_SUCCESS;
 }
 

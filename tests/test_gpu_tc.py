@@ -200,3 +200,34 @@ def test_fused_fft_bitwise_equals_two_pass(gblib, torch_cuda, monkeypatch, kind,
     assert torch.equal(out[0][0], out[1][0])
     assert torch.equal(out[0][1], out[1][1])
     assert torch.isfinite(out[0][1]).all()
+
+
+@pytest.mark.parametrize("kind,L,b,cl", [("so3", 31, 40, "2"), ("so3", 63, 64, "4"), ("s2", 127, 100, "2"),
+                                         ("s2", 255, 130, "4")])
+def test_gemm_clusters_bitwise_equal_single_cta(gblib, torch_cuda, monkeypatch, kind, L, b, cl):
+    """Clusters of 2 or 4 CTAs sharing each table tile by TMA multicast (FFTSO3_GEMM_CLUSTER) give
+    bit-identical results to one CTA per item (=1): the same products in the same order.  Batches
+    whose column tiles do not fill the last cluster block (40 SO(3) functions = 3 tiles in blocks of 2,
+    130 S^2 signals = 5 tiles in blocks of 4) run empty tiles."""
+    torch = torch_cuda
+    k = gblib.SO3_COMPLEX if kind == "so3" else gblib.S2_COMPLEX
+    N = 2 * (L + 1)
+    G = b * (N ** 3 if kind == "so3" else N ** 2)
+    C = b * ((L + 1) * (4 * (L + 1) ** 2 - 1) // 3 if kind == "so3" else (L + 1) ** 2)
+    gen = torch.Generator(device="cuda").manual_seed(L + b)
+    grid = torch.randn(G, dtype=torch.complex64, device="cuda", generator=gen)
+    coef = torch.randn(C, dtype=torch.complex64, device="cuda", generator=gen)
+    s = torch.cuda.current_stream().cuda_stream
+    out = []
+    for c in ("1", cl):
+        monkeypatch.setenv("FFTSO3_GEMM_CLUSTER", c)
+        p = gblib.Plan(k, L, b, "tc_bf16x3", "stable")
+        g = torch.empty_like(grid)
+        co = torch.empty_like(coef)
+        p.inverse(coef.data_ptr(), g.data_ptr(), s)
+        p.forward(grid.data_ptr(), co.data_ptr(), s)
+        p.check()
+        out.append((g.cpu(), co.cpu()))
+        del p
+    assert torch.equal(out[0][0], out[1][0])
+    assert torch.equal(out[0][1], out[1][1])
