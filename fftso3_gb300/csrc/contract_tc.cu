@@ -171,12 +171,19 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
     return d;
 }
 
-// Instruction descriptor, kind::f16: D = F32, A = B = BF16, M = 128, N = 128.
-__host__ __device__ constexpr uint32_t idesc_bf16(bool a_mn_major)
+// Instruction descriptor, kind::f16: D = F32, A = B = BF16, M = 128, N = n (128 or 256).
+__host__ __device__ constexpr uint32_t idesc_bf16(bool a_mn_major, int n = BN)
 {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((a_mn_major ? 1u : 0u) << 15) | ((uint32_t)(BN >> 3) << 17) |
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((a_mn_major ? 1u : 0u) << 15) | ((uint32_t)(n >> 3) << 17) |
            ((uint32_t)(BM >> 4) << 24);
 }
+
+// 1: the products A_hi B_hi (-> hi accumulator) and A_hi B_mid (-> lo accumulator)
+// are one N = 256 MMA over the adjacent B_hi and B_mid planes into the
+// adjacent hi and lo accumulators (5 MMA instructions per 16-wide k instead of 6).
+#ifndef FFTSO3_MMA_N256
+#define FFTSO3_MMA_N256 1
+#endif
 
 __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                          uint32_t accumulate)
@@ -437,14 +444,24 @@ __global__ void __launch_bounds__(THREADS, 1)
             };
             for (int i = 0; i < PF; ++i) prefetch(blockIdx.x, i);
             int kc = 0;
+            int4 nitem = make_int4(0, 0, 0, 0);
+            int nrow0 = 0;
+            if (blockIdx.x < args.nitems) {
+                nitem = args.items[blockIdx.x];
+                nrow0 = args.iaux[blockIdx.x].y;
+            }
             for (int it = blockIdx.x; it < args.nitems && !*abort_flag; it += gridDim.x) {
-                const int4 item = args.items[it];
+                const int4 item = nitem;
+                const long long row0 = nrow0;
+                if (it + (int)gridDim.x < args.nitems) {  // one item ahead
+                    nitem = args.items[it + gridDim.x];
+                    nrow0 = args.iaux[it + gridDim.x].y;
+                }
                 const GemmArgs& A = argsof(item);
                 const CUtensorMap* tA[3] = {FUSED ? &segs[item.z >> 16].tm[0] : &tA0,
                                             FUSED ? &segs[item.z >> 16].tm[1] : &tA1,
                                             FUSED ? &segs[item.z >> 16].tm[2] : &tA2};
                 const int nk = nsteps(item, A);
-                const long long row0 = args.iaux[it].y;
                 for (int i = 0; i < nk; ++i, ++kc) {
                     prefetch(it, i + PF);
                     const int s = kc % STAGES;
@@ -488,11 +505,14 @@ __global__ void __launch_bounds__(THREADS, 1)
         if (lane == 0) {
             // ---------------- MMA issuer
             constexpr uint32_t idesc = idesc_bf16(!FWD);
+            constexpr uint32_t idesc256 = idesc_bf16(!FWD, 2 * BN);
             const int pa[6] = {0, 0, 1, 0, 1, 2};
             const int pb[6] = {0, 1, 0, 2, 1, 0};
             int kc = 0, t = 0;
+            int4 nitem = blockIdx.x < args.nitems ? args.items[blockIdx.x] : make_int4(0, 0, 0, 0);
             for (int it = blockIdx.x; it < args.nitems && !*abort_flag; it += gridDim.x, ++t) {
-                const int4 item = args.items[it];
+                const int4 item = nitem;
+                if (it + (int)gridDim.x < args.nitems) nitem = args.items[it + gridDim.x];  // one item ahead
                 const GemmArgs& A = argsof(item);
                 const int nk = nsteps(item, A);
                 int m0, n0;
@@ -523,13 +543,15 @@ __global__ void __launch_bounds__(THREADS, 1)
                         if (kk >= nkk) break;
 #pragma unroll
                         for (int q = 0; q < 6; ++q) {
+                            if (FFTSO3_MMA_N256 && q == 1) continue;  // issued with q = 0
                             const uint32_t abase = st + pa[q] * PLANE_BYTES;
                             const uint32_t bbase = st + STAGE_A + pb[q] * PLANE_BYTES;
                             const uint64_t ad = FWD ? smem_desc(abase + kk * UK * 2, 16, 1024)
                                                     : smem_desc(abase + kk * UK * 128, PLANE_BYTES / 2, 1024);
                             const uint64_t bd = smem_desc(bbase + kk * UK * 2, 16, 1024);
                             const bool first = (i == 0) && kk == 0 && q <= 1;
-                            mma_bf16(q == 0 ? dhi : dlo, ad, bd, idesc, first ? 0u : 1u);
+                            mma_bf16(q == 0 ? dhi : dlo, ad, bd, (FFTSO3_MMA_N256 && q == 0) ? idesc256 : idesc,
+                                     first ? 0u : 1u);
                         }
                     }
                     if (CL > 1)
