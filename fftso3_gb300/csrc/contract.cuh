@@ -19,6 +19,12 @@ cudaError_t launch_s2_inv_fp64(const double* table, const long long* moff, const
 cudaError_t launch_zero_nyquist_s2(void* H, bool fp64, int N, long long nrows, cudaStream_t st);
 cudaError_t launch_s2_c2r(const void* Fc, void* Fr, bool fp64, int L, int batch, cudaStream_t st);
 cudaError_t launch_s2_r2c(const void* Fr, void* Fc, bool fp64, int L, int batch, cudaStream_t st);
+// tensor-core S^2 real kinds: group-major GEMM output -> real coefficients, and real coefficients ->
+// scaled group-major GEMM input, each in one pass (FP32; goff2 the group-major offsets, cstride (L+1)^2)
+cudaError_t launch_s2_group_to_real(const void* Fg, void* Fr, const long long* goff2, int L, int batch,
+                                   cudaStream_t st);
+cudaError_t launch_s2_real_to_group(const void* Fr, void* Y, const long long* goff2, int L, int batch,
+                                   cudaStream_t st);
 
 // S^2 -> SO(3) correlation coefficients Fr(l,m,n) = G_l(m) F_l(n) / (2l+1) (correlate.cu)
 cudaError_t launch_corr_coeffs(const void* F, const void* G, void* C, bool fp64, int L, int batch, cudaStream_t st);

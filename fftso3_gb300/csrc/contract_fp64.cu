@@ -411,6 +411,95 @@ __global__ void s2_r2c_kernel(const RIN* __restrict__ Fr, COUT* __restrict__ Fc,
     Fc[(long long)b * cstride + i] = o;
 }
 
+// S^2 real coefficients straight from the tensor-core group-major layout
+// (Fg[f][goff2[g] + p (B - g) + (l - g)] = F_c(l, m) for g = |m|, p = (m < 0)):
+// the gather to the packed complex layout and s2_c2r_kernel in one pass, with
+// the same arithmetic.  A CTA stages a 32 (l) x 32 (m) tile of F_c(l, +-m) in
+// shared memory, so the group-major side is read along l and the packed real
+// side written along m, both in runs of 32.
+constexpr int S2T = 32;
+
+__global__ void __launch_bounds__(256) s2_group_to_real_kernel(const float2* __restrict__ Fg, float* __restrict__ Fr,
+                                                              const long long* __restrict__ goff2, int L,
+                                                              long long cstride)
+{
+    __shared__ float2 tp[S2T][S2T + 1];  // F_c(l0 + li, +(mb + mi)) as [mi][li]
+    __shared__ float2 tn[S2T][S2T + 1];  // F_c(l0 + li, -(mb + mi))
+    const int B = L + 1;
+    const int l0 = blockIdx.x * S2T, mb = (int)blockIdx.y * S2T, b = blockIdx.z;  // |m| tile [mb, mb + 32)
+    if (mb > l0 + S2T - 1 || mb > L) return;  // every |m| of the tile exceeds every l
+    const float2* fg = Fg + (long long)b * cstride;
+    for (int e = threadIdx.x; e < S2T * S2T; e += 256) {
+        const int mi = e / S2T, li = e % S2T, g = mb + mi, l = l0 + li;
+        if (g > L || l > L || l < g) continue;
+        const long long o = goff2[g] + (l - g);
+        tp[mi][li] = fg[o];
+        tn[mi][li] = g > 0 ? fg[o + (B - g)] : fg[o];
+    }
+    __syncthreads();
+    float* fr = Fr + (long long)b * cstride;
+    // outputs (l, m) for |m| in the tile, m = +g and m = -g: runs along m (packed l^2 + l + m)
+    for (int e = threadIdx.x; e < 2 * S2T * S2T; e += 256) {
+        const int li = e / (2 * S2T), r = e % (2 * S2T), neg = r < S2T, mi = neg ? S2T - 1 - r : r - S2T;
+        const int g = mb + mi, l = l0 + li;
+        if (g > L || l > L || l < g || (neg && g == 0)) continue;
+        const int m = neg ? -g : g;
+        int cs[2] = {-m, m};
+        if (m > 0) { cs[0] = -m; cs[1] = m; } else if (m < 0) { cs[0] = m; cs[1] = -m; }
+        const int nc = (m == 0) ? 1 : 2;
+        float acc = 0.f;
+        for (int j = 0; j < nc; ++j) {
+            const c2t<float> t = conj_t(tmat_t<float>(m, cs[j]));
+            const float2 v = cs[j] < 0 ? tn[mi][li] : tp[mi][li];
+            acc += t.x * v.x - t.y * v.y;
+        }
+        fr[(long long)l * l + l + m] = acc;
+    }
+}
+
+// S^2 real coefficients straight into the scaled group-major layout of the
+// inverse GEMM (pair 0: F_c(l, m), pair 1: (-1)^m F_c(l, -m), m >= 0):
+// s2_r2c_kernel and the packed -> group-major permutation in one pass, with
+// the same arithmetic.  A CTA stages F_r(l, +-m) for a 32 (l) x 32 (m) tile,
+// read along m (packed) and written along l (group-major).
+__global__ void __launch_bounds__(256) s2_real_to_group_kernel(const float* __restrict__ Fr, float2* __restrict__ Y,
+                                                              const long long* __restrict__ goff2, int L,
+                                                              long long cstride)
+{
+    __shared__ float tp[S2T][S2T + 1];  // F_r(l0 + li, +(mb + mi)) as [li][mi]
+    __shared__ float tn[S2T][S2T + 1];  // F_r(l0 + li, -(mb + mi))
+    const int B = L + 1;
+    const int l0 = blockIdx.x * S2T, mb = (int)blockIdx.y * S2T, b = blockIdx.z;
+    if (mb > l0 + S2T - 1 || mb > L) return;
+    const float* fr = Fr + (long long)b * cstride;
+    for (int e = threadIdx.x; e < 2 * S2T * S2T; e += 256) {
+        const int li = e / (2 * S2T), r = e % (2 * S2T), neg = r < S2T, mi = neg ? S2T - 1 - r : r - S2T;
+        const int g = mb + mi, l = l0 + li;
+        if (g > L || l > L || l < g) continue;
+        const float v = fr[(long long)l * l + l + (neg ? -g : g)];
+        if (neg) tn[li][mi] = v; else tp[li][mi] = v;
+    }
+    __syncthreads();
+    float2* y = Y + (long long)b * cstride;
+    for (int e = threadIdx.x; e < 2 * S2T * S2T; e += 256) {
+        const int p = e / (S2T * S2T), r = e % (S2T * S2T), mi = r / S2T, li = r % S2T;
+        const int m = mb + mi, l = l0 + li;
+        if (m > L || l > L || l < m || (p == 1 && m == 0)) continue;
+        const int c = p == 0 ? m : -m;
+        const int as[2] = {c, -c};
+        const int na = (c == 0) ? 1 : 2;
+        c2t<float> acc = {0.f, 0.f};
+        for (int j = 0; j < na; ++j) {
+            const c2t<float> t = tmat_t<float>(as[j], c);
+            const float v = as[j] < 0 ? tn[li][mi] : tp[li][mi];
+            acc.x += t.x * v;
+            acc.y += t.y * v;
+        }
+        const float sc = (p == 0 || !(m & 1)) ? 1.f : -1.f;
+        y[goff2[m] + (long long)p * (B - m) + (l - m)] = make_float2(sc * acc.x, sc * acc.y);
+    }
+}
+
 // ---------------------------------------------------------------- launchers
 
 cudaError_t launch_so3_fwd_fp64(const double* table, const long long* goff, const double2* G, const double* w,
@@ -507,6 +596,24 @@ cudaError_t launch_s2_c2r(const void* Fc, void* Fr, bool fp64, int L, int batch,
         s2_c2r_kernel<double2, double, double><<<grid, 256, 0, st>>>((const double2*)Fc, (double*)Fr, L, C);
     else
         s2_c2r_kernel<float2, float, float><<<grid, 256, 0, st>>>((const float2*)Fc, (float*)Fr, L, C);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_s2_group_to_real(const void* Fg, void* Fr, const long long* goff2, int L, int batch,
+                                   cudaStream_t st)
+{
+    const long long C = (long long)(L + 1) * (L + 1);
+    const unsigned nt = (unsigned)((L + 1 + S2T - 1) / S2T);
+    s2_group_to_real_kernel<<<dim3(nt, nt, batch), 256, 0, st>>>((const float2*)Fg, (float*)Fr, goff2, L, C);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_s2_real_to_group(const void* Fr, void* Y, const long long* goff2, int L, int batch,
+                                   cudaStream_t st)
+{
+    const long long C = (long long)(L + 1) * (L + 1);
+    const unsigned nt = (unsigned)((L + 1 + S2T - 1) / S2T);
+    s2_real_to_group_kernel<<<dim3(nt, nt, batch), 256, 0, st>>>((const float*)Fr, (float2*)Y, goff2, L, C);
     return cudaGetLastError();
 }
 

@@ -1843,8 +1843,9 @@ static int fft_inverse(TCState* s, void* grid, cudaStream_t st, StageTimer* T, s
     return FFTSO3_SUCCESS;
 }
 
+// real_out (S^2 real kinds): write the real coefficients straight from the GEMM output instead of F.
 static int tc_forward_once(TCState* s, const void* grid, float2* F, cudaStream_t st, StageTimer* T,
-                           std::string& err)
+                           std::string& err, void* real_out = nullptr)
 {
     int rc = fft_forward(s, grid, st, T, err);
     if (rc) return rc;
@@ -1852,7 +1853,9 @@ static int tc_forward_once(TCState* s, const void* grid, float2* F, cudaStream_t
     if ((rc = launch_gemm(s, true, st, err))) return rc;
     T->end(st);
     T->begin(ST_BASIS, st);
-    if (s->s2)
+    if (real_out)
+        TCK(launch_s2_group_to_real(s->d_fg, real_out, s->d_goff2, s->L, s->batch, st));
+    else if (s->s2)
         s2_group_to_packed_kernel<<<dim3(s->B, s->batch), 256, 0, st>>>(s->d_fg, F, s->d_goff2, s->L,
                                                                        coeffs_per_fn(s));
     else
@@ -1863,8 +1866,9 @@ static int tc_forward_once(TCState* s, const void* grid, float2* F, cudaStream_t
     return FFTSO3_SUCCESS;
 }
 
+// real_in (S^2 real kinds): read the real coefficients straight into the GEMM input instead of F.
 static int tc_inverse_once(TCState* s, const float2* F, void* grid, cudaStream_t st, StageTimer* T,
-                           std::string& err)
+                           std::string& err, const void* real_in = nullptr)
 {
     const long long N = s->N;
     T->begin(ST_NYQUIST, st);
@@ -1878,7 +1882,9 @@ static int tc_inverse_once(TCState* s, const float2* F, void* grid, cudaStream_t
     TCK(cudaGetLastError());
     T->end(st);
     T->begin(ST_BASIS, st);
-    if (s->s2)
+    if (real_in)
+        TCK(launch_s2_real_to_group(real_in, s->d_fg, s->d_goff2, s->L, s->batch, st));
+    else if (s->s2)
         s2_packed_to_group_kernel<<<dim3(s->ngroups, s->batch), 128, 0, st>>>(F, s->d_fg, s->d_goff2, s->L,
                                                                              coeffs_per_fn(s));
     else
@@ -1897,6 +1903,7 @@ int tc_forward(TCState* s, const void* grid, void* coeffs, cudaStream_t st, Stag
 {
     // real kinds: complex coefficients in d_fc, then the real basis
     // (fdcl_FFTSO3.cpp:1169-1181, fdcl_FFTS2.cpp:424-436)
+    if (s->real && s->s2 && !s->refine) return tc_forward_once(s, grid, nullptr, st, T, err, coeffs);
     float2* Fc = s->real ? s->d_fc : (float2*)coeffs;
     int rc = tc_forward_once(s, grid, Fc, st, T, err);
     if (rc) return rc;
@@ -1932,6 +1939,7 @@ int tc_forward(TCState* s, const void* grid, void* coeffs, cudaStream_t st, Stag
 
 int tc_inverse(TCState* s, const void* coeffs, void* grid, cudaStream_t st, StageTimer* T, std::string& err)
 {
+    if (s->real && s->s2) return tc_inverse_once(s, nullptr, grid, st, T, err, coeffs);
     const float2* Fc = (const float2*)coeffs;
     if (s->real) {
         T->begin(ST_BASIS, st);
@@ -1956,6 +1964,11 @@ int tc_forward_finish(TCState* s, void* coeffs, cudaStream_t st, StageTimer* T, 
 {
     float2* Fc = s->real ? s->d_fc : (float2*)coeffs;
     T->begin(ST_BASIS, st);
+    if (s->real && s->s2) {
+        TCK(launch_s2_group_to_real(s->d_fg, coeffs, s->d_goff2, s->L, s->batch, st));
+        T->end(st);
+        return FFTSO3_SUCCESS;
+    }
     if (s->s2)
         s2_group_to_packed_kernel<<<dim3(s->B, s->batch), 256, 0, st>>>(s->d_fg, Fc, s->d_goff2, s->L,
                                                                        coeffs_per_fn(s));
@@ -1978,6 +1991,14 @@ int tc_inverse_prepare(TCState* s, const void* coeffs, cudaStream_t st, StageTim
     const float2* Fc = (const float2*)coeffs;
     const long long N = s->N;
     T->begin(ST_BASIS, st);
+    if (s->real && s->s2) {
+        const long long tot = (long long)s->batch * N;
+        s2_zero_nyquist_pencils_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(s->d_pencil, (int)N, s->batch);
+        TCK(cudaGetLastError());
+        TCK(launch_s2_real_to_group(coeffs, s->d_fg, s->d_goff2, s->L, s->batch, st));
+        T->end(st);
+        return FFTSO3_SUCCESS;
+    }
     if (s->real) {
         if (s->s2)
             TCK(launch_s2_r2c(coeffs, s->d_fc, false, s->L, s->batch, st));

@@ -19,6 +19,7 @@
 //                 pencils [fn][p][q][k] the beta-sum GEMM consumes (and the
 //                 reverse for the inverse).
 #include <algorithm>
+#include <cstdlib>
 
 #include "common.cuh"
 #include "fft.cuh"
@@ -772,6 +773,10 @@ static void fused_geometry(int N, int nsm, int& D, int& S)
 {
     const int W = 12 * nsm;
     D = N >= 512 ? 1 : std::max(1, (W - N + 2 * N - 1) / (2 * N));
+    if (const char* ev = getenv("FFTSO3_FFT_LOOKAHEAD")) {  // tuning override of D (1..16)
+        const int d = atoi(ev);
+        if (d >= 1 && d <= 16) D = d;
+    }
     S = D + std::max(2, (W + N + 2 * N - 1) / (2 * N));
 }
 
