@@ -577,6 +577,9 @@ __global__ void __launch_bounds__(THREADS, 1)
         // latency overlaps the split/store of the previous step.
         const int pt = threadIdx.x - 64;
         const int c = pt >> 2, q4 = pt & 3;
+        // odd columns store their two chunks in the opposite order, so the 8 threads of a quarter-warp
+        // (2 columns x 4 chunks) cover all 8 16-byte bank groups of the swizzled rows
+        const int hs = c & 1;
         const int fl = c / PPF, pp = c % PPF;
         const int Rre = fl * 2 * PPF + 2 * pp, Rim = Rre + 1;
         struct Src {
@@ -613,7 +616,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         auto fetch = [&](const Src& sr, int i, float2* v) {
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
-                const int k = i * BK + (q4 + 4 * h) * 8;
+                const int k = i * BK + (q4 + 4 * (h ^ hs)) * 8;
                 if (FWD && sr.p && k + 8 <= sr.lim) {
                     const float4* s4 = reinterpret_cast<const float4*>(sr.p + k);
 #pragma unroll
@@ -680,7 +683,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             const uint32_t bpl = smem_u32(smem + s * STAGE_BYTES + STAGE_A);
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
-                const int chunk = q4 + 4 * h;
+                const int chunk = q4 + 4 * (h ^ hs);
                 const int k = i * BK + chunk * 8;
                 float re[8], im[8];
 #pragma unroll

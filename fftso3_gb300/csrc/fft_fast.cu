@@ -701,17 +701,23 @@ __global__ void __launch_bounds__(32 * PWARPS, 3) fft_grid2d(const Grid2DArgs a,
         }
         __syncthreads();  // every thread's stores (and discards) of tile t issued; shared memory free
         if (s_slow) {
-            // slow path: the next tile's dependency was incomplete; publish t first (it may be one of them)
+            // the next tile's dependency was incomplete at the middle barrier.  Usually it has completed
+            // since: re-read it and, if so, one fence (acquire) suffices and t stays unpublished until the
+            // next tile's middle barrier.  Otherwise publish t first (it may be one of them) and wait.
             if (threadIdx.x == 0) {
-                fence_gpu();
-                signal(t);
-                const bool ok = spin(dptr);
+                bool published = false, ok = true;
+                if (ld_relaxed(dptr) < N) {
+                    fence_gpu();
+                    signal(t);
+                    published = true;
+                    ok = spin(dptr);
+                }
                 fence_gpu();
                 s_cur[(it + 1) & 1] = ok ? nxt : -1;
                 if (!ok) pend = -1;
+                prev = published ? -1 : t;
             }
             __syncthreads();
-            if (threadIdx.x == 0) prev = -1;
         } else if (threadIdx.x == 0) {
             prev = t;
         }

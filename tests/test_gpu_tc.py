@@ -231,3 +231,32 @@ def test_gemm_clusters_bitwise_equal_single_cta(gblib, torch_cuda, monkeypatch, 
         del p
     assert torch.equal(out[0][0], out[1][0])
     assert torch.equal(out[0][1], out[1][1])
+
+
+@pytest.mark.parametrize("kind", ["complex", "real"])
+def test_tc_round_trip_lmax255(gblib, torch_cuda, kind):
+    """The headline size, l_max = 255 (512^3 grid, one-launch FFT at N = 512, clusters off at batch 1):
+    forward(inverse(F)) returns F within the split-BF16 bound, relative L2 <= 1e-6, and per degree l the
+    relative error stays <= 1e-5 (size-independent properties at full size; the FP64 comparison at this
+    size is bench.py's accuracy line)."""
+    torch = torch_cuda
+    L = 255
+    cplx = kind == "complex"
+    F = so3_coeffs(L, seed=2551, complex_=cplx, decay="pow")
+    k = gblib.SO3_COMPLEX if cplx else gblib.SO3_REAL
+    p = gblib.Plan(k, L, 1, "tc_bf16x3", "stable")
+    s = torch.cuda.current_stream().cuda_stream
+    c = torch.from_numpy(F.astype(np.complex64 if cplx else np.float32)).cuda()
+    g = torch.empty(512 ** 3, dtype=torch.complex64 if cplx else torch.float32, device="cuda")
+    c2 = torch.empty_like(c)
+    p.inverse(c.data_ptr(), g.data_ptr(), s)
+    p.forward(g.data_ptr(), c2.data_ptr(), s)
+    p.check()
+    out = c2.cpu().numpy().astype(np.complex128 if cplx else np.float64)
+    ref = F.astype(np.complex64 if cplx else np.float32).astype(np.complex128 if cplx else np.float64)
+    assert rel_err(out, ref) < TOL
+    from conftest import degrees_so3
+    deg = degrees_so3(L)
+    for l in (0, 1, 64, 128, 200, 255):
+        sel = deg == l
+        assert rel_err(out[sel], ref[sel]) < 1e-5
