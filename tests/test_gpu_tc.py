@@ -260,3 +260,35 @@ def test_tc_round_trip_lmax255(gblib, torch_cuda, kind):
     for l in (0, 1, 64, 128, 200, 255):
         sel = deg == l
         assert rel_err(out[sel], ref[sel]) < 1e-5
+
+
+@pytest.mark.parametrize("L,kind", [(10, "complex"), (12, "real"), (28, "complex"), (36, "real"), (60, "complex"),
+                                    (22, "complex")])
+def test_tc_prime_factor_fft(gblib, torch_cuda, L, kind):
+    """Generic-N grids N = 2(l_max + 1) whose largest factor is a prime p > 8 (p = 11, 13, 23, 29,
+    37, 61): the first FFT stage is the symmetric prime DFT.  TC vs the FP64 plan on the same
+    coefficients, relative L2 <= 1e-6 for the grids and the coefficients, batch 2."""
+    torch = torch_cuda
+    cplx = kind == "complex"
+    k = gblib.SO3_COMPLEX if cplx else gblib.SO3_REAL
+    N = 2 * (L + 1)
+    F = so3_coeffs(L, seed=3000 + L, complex_=cplx, decay="pow")
+    ptc = gblib.Plan(k, L, 2, "tc_bf16x3", "stable")
+    p64 = gblib.Plan(k, L, 1, "fp64", "stable")
+    s = torch.cuda.current_stream().cuda_stream
+    F2 = np.concatenate([F, F])
+    c64 = torch.from_numpy(F).cuda()
+    g64 = torch.empty(N ** 3, dtype=torch.complex128 if cplx else torch.float64, device="cuda")
+    p64.inverse(c64.data_ptr(), g64.data_ptr(), s)
+    c32 = torch.from_numpy(F2.astype(np.complex64 if cplx else np.float32)).cuda()
+    g32 = torch.empty(2 * N ** 3, dtype=torch.complex64 if cplx else torch.float32, device="cuda")
+    ptc.inverse(c32.data_ptr(), g32.data_ptr(), s)
+    gin = torch.cat([g64, g64]).to(torch.complex64 if cplx else torch.float32)
+    F32 = torch.empty_like(c32)
+    ptc.forward(gin.data_ptr(), F32.data_ptr(), s)
+    ptc.check()
+    gref = g64.cpu().numpy()
+    gg = g32.cpu().numpy().astype(np.complex128 if cplx else np.float64)
+    assert rel_err(gg[:N ** 3], gref) < TOL and rel_err(gg[N ** 3:], gref) < TOL
+    FF = F32.cpu().numpy().astype(np.complex128 if cplx else np.float64)
+    assert rel_err(FF[:F.size], F) < TOL and rel_err(FF[F.size:], F) < TOL
