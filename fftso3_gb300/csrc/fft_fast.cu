@@ -534,20 +534,25 @@ __global__ void __launch_bounds__(32 * PWARPS, 3) fft_tile(const float2* __restr
 //   A(0), ..., A(D-1), A(D), B(0), A(D+1), B(1), ..., B(C-1)
 // so a phase-B tile's producers were claimed at least D + 1 blocks earlier
 // and a slot is reused 2 (S - D) - 1 blocks after its last reader was claimed;
-// D and S are chosen from the number of resident CTAs so that in steady state
-// every dependency is complete when its tile is claimed, while only about
-// D + 1 slots hold live data (the rest were dropped from L2 as they were read).
-// Every tile waits only on tiles claimed before it, by CTAs that are running
-// or done, so the launch cannot deadlock and needs no co-residency; waits are
-// bounded, and on timeout the launch records an error and stops claiming.
+// D and S are chosen from the number of resident CTAs (about 12 tiles per SM
+// are claimed but not yet published at any time) so that dependencies are
+// normally complete when checked, while only about D + 1 slots hold live data
+// (the rest were dropped from L2 as they were read).  At N = 512 D stays 1 so
+// that the live 32 MB slots fit in L2; about a third of the tiles then find
+// their dependency incomplete at the first check (a larger D was measured
+// slower).  Every tile waits only on tiles claimed before it, by CTAs that are
+// running or done, so the launch cannot deadlock and needs no co-residency;
+// waits are bounded, and on timeout the launch records an error and every CTA
+// stops at its next wait.
 //
-// Control (thread 0 of each CTA), kept off the critical path: the claim of
-// the tile after next is issued when a tile starts and the next tile's
-// dependency counter is read then too; at the tile's middle barrier (its input
-// consumed, nothing outstanding) one fence both publishes the previous tile
-// (release) and validates that counter read (acquire), so a tile costs two
-// barriers and no exposed round trip.  Only a dependency still incomplete at
-// that point takes the slow path: publish the current tile, then wait.
+// Control (thread 0 of each CTA), kept off the critical path where it can be:
+// the claim of the tile after next is issued when a tile starts and the next
+// tile's dependency counter is read then too; at the tile's middle barrier
+// (its input consumed) one fence both publishes the previous tile (release)
+// and validates that counter read (acquire), so a tile costs two barriers and
+// one fence.  A dependency still incomplete at that point is read again at the
+// end of the tile (one more fence if it has completed); only if it is still
+// incomplete is the current tile published first, then waited for.
 constexpr long long WAIT_LIMIT = 4000000000LL;  // clock64 cycles (~2 s)
 
 struct Grid2DArgs {
