@@ -1344,8 +1344,11 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
     s->batch = batch;
     s->s2 = s2;
     s->simt = simt;
-    if (!s2 && (long long)((2 * L + 1 + 31) / 32) * batch > 65535) {
-        err = "batch too large for this l_max (at most 65535 / ceil((2 l_max + 1) / 32) functions per plan)";
+    // grid limits: the coefficient permutations run ceil((2L+1)/32) m tiles x ceil(batch / 8) function groups in
+    // gridDim.z, the per-function conversions take the batch in gridDim.y
+    if (batch > 65535 || (!s2 && (long long)((2 * L + 1 + 31) / 32) * ((batch + PFPC - 1) / PFPC) > 65535)) {
+        err = "batch too large for this l_max (at most 65535 functions, and 65535 / ceil((2 l_max + 1) / 32) "
+              "groups of 8 functions for SO(3))";
         delete s;
         return FFTSO3_ERR_UNSUPPORTED;
     }
