@@ -171,12 +171,20 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
     return d;
 }
 
-// Instruction descriptor, kind::f16: D = F32, A = B = BF16, M = 128, N = n (128 or 256).
-__host__ __device__ constexpr uint32_t idesc_bf16(bool a_mn_major, int n = BN)
+// Instruction descriptor, kind::f16: D = F32, A = B = BF16, M = m (128 or 64), N = n (128 or 256).
+__host__ __device__ constexpr uint32_t idesc_bf16(bool a_mn_major, int n = BN, int m = BM)
 {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((a_mn_major ? 1u : 0u) << 15) | ((uint32_t)(n >> 3) << 17) |
-           ((uint32_t)(BM >> 4) << 24);
+           ((uint32_t)(m >> 4) << 24);
 }
+
+// 1: a forward row tile with at most 64 valid rows (degrees) issues M = 64 MMAs
+// (half the tensor work of the padded 128-row tile).  Their accumulator rows
+// r < 64 sit in TMEM lanes 32 (r / 16) + r % 16 (16 lanes of each 32-lane
+// quarter), which the epilogue reads accordingly.
+#ifndef FFTSO3_MMA_M64
+#define FFTSO3_MMA_M64 1
+#endif
 
 // 1: the products A_hi B_hi (-> hi accumulator) and A_hi B_mid (-> lo accumulator)
 // are one N = 256 MMA over the adjacent B_hi and B_mid planes into the
@@ -506,6 +514,8 @@ __global__ void __launch_bounds__(THREADS, 1)
             // ---------------- MMA issuer
             constexpr uint32_t idesc = idesc_bf16(!FWD);
             constexpr uint32_t idesc256 = idesc_bf16(!FWD, 2 * BN);
+            constexpr uint32_t idesc_h = idesc_bf16(!FWD, BN, BM / 2);
+            constexpr uint32_t idesc256_h = idesc_bf16(!FWD, 2 * BN, BM / 2);
             const int pa[6] = {0, 0, 1, 0, 1, 2};
             const int pb[6] = {0, 1, 0, 2, 1, 0};
             int kc = 0, t = 0;
@@ -520,6 +530,8 @@ __global__ void __launch_bounds__(THREADS, 1)
                 // valid K (zero-padded beyond): the forward sums over N samples, the inverse over nl degrees;
                 // the last k-step issues only the 16-wide MMAs that hold valid K
                 const int kvalid = FWD ? A.N : A.L + 1 - m0;
+                const bool half = FWD && FFTSO3_MMA_M64 && (A.L + 1 - m0 - item.y * BM) <= BM / 2;
+                const uint32_t id1 = half ? idesc_h : idesc, id2 = half ? idesc256_h : idesc256;
                 const int ab = t & 1;
                 if (t >= 2 && !mbar_wait(&acce[ab], ((t >> 1) - 1) & 1, args.err, 2)) {
                     *abort_flag = 1;
@@ -550,7 +562,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                                                     : smem_desc(abase + kk * UK * 128, PLANE_BYTES / 2, 1024);
                             const uint64_t bd = smem_desc(bbase + kk * UK * 2, 16, 1024);
                             const bool first = (i == 0) && kk == 0 && q <= 1;
-                            mma_bf16(q == 0 ? dhi : dlo, ad, bd, (FFTSO3_MMA_N256 && q == 0) ? idesc256 : idesc,
+                            mma_bf16(q == 0 ? dhi : dlo, ad, bd, (FFTSO3_MMA_N256 && q == 0) ? id2 : id1,
                                      first ? 0u : 1u);
                         }
                     }
@@ -732,6 +744,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             item_mn(item, m0, n0);
             const GroupPairs P = S2 ? s2_pairs(m0) : group_pairs(m0, n0);
             const int nl = A.L + 1 - m0;
+            const bool half = FWD && FFTSO3_MMA_M64 && (nl - item.y * BM) <= BM / 2;  // M = 64 item (see MMA)
             long long poff[4];
 #pragma unroll
             for (int p = 0; p < 4; ++p) {
@@ -761,8 +774,9 @@ __global__ void __launch_bounds__(THREADS, 1)
                     const int f = ctile(item) * FPTK + chunk * (32 / (2 * PPF)) + fq;
                     if (f >= A.batch) continue;
                     if (FWD) {
-                        const int row = item.y * BM + r;
-                        if (row >= nl) continue;
+                        // M = 64 tiles: rows 16 quarter + lane (lanes 0..15 of each quarter)
+                        const int row = half ? item.y * BM + quarter * 16 + lane : item.y * BM + r;
+                        if ((half && lane >= 16) || row >= nl) continue;
                         float2* Fo = A.cout + (long long)f * A.cstride + row;
 #pragma unroll
                         for (int p = 0; p < 4; ++p) {
