@@ -304,7 +304,7 @@ struct GemmArgs {
 // One plan's share of a fused launch over several plans (the l_max buckets of
 // an uneven batch): its table maps and arguments.  Work items of a fused launch
 // carry (segment << 16 | column tile) in .z.
-struct alignas(64) GemmSeg {
+struct GemmSeg {  // aligned as CUtensorMap (128 bytes), as TMA needs for maps in global memory
     CUtensorMap tm[3];
     GemmArgs a;
 };
@@ -427,8 +427,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             // table streams from HBM with more bytes in flight than the ring.
             constexpr int PF = FWD ? FFTSO3_GEMM_PF : 0;  // the inverse re-reads each table tile from L2 (4 row tiles)
             auto prefetch = [&](int it, int i) {
-                if (PF == 0) return;
-                while (it < args.nitems) {
+                while (PF > 0 && it < args.nitems) {
                     const int4 item = args.items[it];
                     const GemmArgs& A = argsof(item);
                     const int nk = nsteps(item, A);
