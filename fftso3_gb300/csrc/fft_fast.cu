@@ -373,8 +373,8 @@ __device__ __forceinline__ void l2_discard(const void* p)
 // side read and the side written; an IO_SCRATCH input is dropped from L2
 // once the tile holds it (every line of the ring is read by exactly one tile).
 // T: staged tile [TL][LP] in shared memory; Ws: twiddles (staged, synchronised).
-// mid(): run by thread 0 right after the barrier between the two halves of the
-// tile (the input is consumed, no output written yet).
+// mid(): run by every thread right after the barrier between the two halves of
+// the tile (the input is consumed, no output written yet).
 template <int R, bool C2T, bool REAL_IO, int IN, int OUT, typename MID>
 __device__ __forceinline__ void tile_body(const float2* __restrict__ in, float2* __restrict__ out, long long cbase,
                                           long long tbase, long long Ls, long long Js, float2* T,
@@ -416,7 +416,7 @@ __device__ __forceinline__ void tile_body(const float2* __restrict__ in, float2*
             }
         }
         __syncthreads();
-        if (threadIdx.x == 0) mid();
+        mid();
         if (IN == IO_SCRATCH)
             for (int i = threadIdx.x; i < TL * (N / 16); i += 32 * PWARPS)
                 l2_discard(in + cbase + (long long)(i / (N / 16)) * Ls + (i % (N / 16)) * 16);
@@ -464,7 +464,7 @@ __device__ __forceinline__ void tile_body(const float2* __restrict__ in, float2*
             }
         }
         __syncthreads();
-        if (threadIdx.x == 0) mid();
+        mid();
         if (IN == IO_SCRATCH)
             for (int j = threadIdx.x; j < N; j += 32 * PWARPS) l2_discard(in + tbase + (long long)j * Js);
         // contiguous output straight from registers: runs of R consecutive outputs per lane group
@@ -564,6 +564,7 @@ struct Grid2DArgs {
     int nchunks;     // C = nf * N / TL
     int look;        // D
     int nslots;      // S
+    int prefetch;    // 1: prefetch the next claimed phase-A tile's input into L2 at each middle barrier
 };
 
 __device__ __forceinline__ int ld_relaxed(const int* p)
@@ -577,6 +578,7 @@ __device__ __forceinline__ void red_add(int* p, int v)
 {
     asm volatile("red.relaxed.gpu.global.add.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
 // Claim order -> (phase, chunk, tile within the phase).
 __device__ __forceinline__ void decode_task(int t, int N, int C, int D, bool& phaseA, int& c, int& u)
@@ -608,7 +610,7 @@ __global__ void __launch_bounds__(32 * PWARPS, 3) fft_grid2d(const Grid2DArgs a,
     extern __shared__ float2 smem_f2[];
     float2* Ws = smem_f2;
     float2* T = smem_f2 + tile_tw_elems<R>();
-    __shared__ int s_cur[2], s_slow;
+    __shared__ int s_cur[2], s_slow, s_next;
     load_tile_twiddles<R>(Ws, tw);
     const uint64_t pol_stream = l2_policy_first(), pol_keep = l2_policy_last();
     const int C = a.nchunks, D = a.look, S = a.nslots;
@@ -669,8 +671,33 @@ __global__ void __launch_bounds__(32 * PWARPS, 3) fft_grid2d(const Grid2DArgs a,
         if (threadIdx.x == 0) {
             pend = nxt >= 0 ? claim() : -1;  // the tile after next
             dv = dptr ? ld_relaxed(dptr) : N;
+            s_next = nxt;                    // read by every thread after the middle barrier
         }
         auto mid = [&] {
+            // The next tile's input, if it comes from HBM (phase A), is requested into L2 now, a
+            // half tile ahead: its loads then wait on L2 instead of HBM.  Phase-B inputs (the
+            // ring) are in L2 already.
+            const int tn = a.prefetch ? s_next : -1;
+            if (tn >= 0) {
+                bool pa;
+                int cn, un;
+                decode_task(tn, N, C, D, pa, cn, un);
+                if (pa) {
+                    const long long fb = (long long)(cn / NB) * N3, kbn = cn % NB;
+                    if (FWD) {
+                        // TL contiguous grid rows of slice kbn TL + un / NB (as tile_body reads them)
+                        constexpr int ES = REAL_IO ? 4 : 8, NL = TL * N * ES / 128;
+                        const char* base = reinterpret_cast<const char*>(a.in) +
+                                           (fb + (kbn * TL + un / NB) * N2 + (long long)(un % NB) * TL * N) * ES;
+                        for (int i = threadIdx.x; i < NL; i += 32 * PWARPS) prefetch_l2(base + 128LL * i);
+                    } else {
+                        // N runs of TL pencil entries (128 bytes each), one per p
+                        const float2* base = a.in + fb + (long long)un * N + kbn * TL;
+                        for (int j = threadIdx.x; j < N; j += 32 * PWARPS) prefetch_l2(base + (long long)j * N2);
+                    }
+                }
+            }
+            if (threadIdx.x != 0) return;
             fence_gpu();  // release of the previous tile, acquire of the counter read above
             if (prev >= 0) signal(prev);
             prev = -1;
@@ -899,7 +926,9 @@ cudaError_t launch_fft_grid_fused(const void* in, void* out, void* ring, size_t 
     int D, S;
     ffast::fused_geometry(N, ffast::device_sms(), D, S);
     if ((size_t)S * ffast::TL * N * N > ring_elems) return cudaErrorInvalidValue;  // ring sized for another device
-    ffast::Grid2DArgs a{(const float2*)in, (float2*)out, (float2*)ring, ctl, err, (int)C, D, S};
+    const char* pf = getenv("FFTSO3_FFT_PREFETCH");  // 0 turns the next-tile L2 prefetch off (tuning)
+    ffast::Grid2DArgs a{(const float2*)in, (float2*)out, (float2*)ring, ctl, err, (int)C, D, S,
+                        pf && atoi(pf) == 0 ? 0 : 1};
     const long long tiles = 2 * C * N;
     if (dir == 1)
         return real_io ? ffast::grid2d_dispatch<true, true>(a, tiles, N, tw, st)
