@@ -674,9 +674,18 @@ __global__ void __launch_bounds__(32 * PWARPS, 3) fft_grid2d(const Grid2DArgs a,
             s_next = nxt;                    // read by every thread after the middle barrier
         }
         auto mid = [&] {
+            if (threadIdx.x == 0) {
+                fence_gpu();  // release of the previous tile, acquire of the counter read above
+                if (prev >= 0) signal(prev);
+                prev = -1;
+                ready = nxt < 0 || dv >= N;
+                s_cur[(it + 1) & 1] = nxt;
+                s_slow = !ready;
+            }
             // The next tile's input, if it comes from HBM (phase A), is requested into L2 now, a
             // half tile ahead: its loads then wait on L2 instead of HBM.  Phase-B inputs (the
-            // ring) are in L2 already.
+            // ring) are in L2 already.  Thread 0 prefetches after its fence (measured faster than
+            // before it: the fence would also wait for its prefetches).
             const int tn = a.prefetch ? s_next : -1;
             if (tn >= 0) {
                 bool pa;
@@ -697,13 +706,6 @@ __global__ void __launch_bounds__(32 * PWARPS, 3) fft_grid2d(const Grid2DArgs a,
                     }
                 }
             }
-            if (threadIdx.x != 0) return;
-            fence_gpu();  // release of the previous tile, acquire of the counter read above
-            if (prev >= 0) signal(prev);
-            prev = -1;
-            ready = nxt < 0 || dv >= N;
-            s_cur[(it + 1) & 1] = nxt;
-            s_slow = !ready;
         };
         bool phaseA;
         int c, u;
