@@ -610,7 +610,8 @@ __global__ void __launch_bounds__(32 * PWARPS, 3) fft_grid2d(const Grid2DArgs a,
     extern __shared__ float2 smem_f2[];
     float2* Ws = smem_f2;
     float2* T = smem_f2 + tile_tw_elems<R>();
-    __shared__ int s_cur[2], s_slow, s_next;
+    __shared__ int s_cur[2], s_slow;
+    __shared__ const char* s_pf;  // input of the next tile to prefetch into L2 (null: none)
     load_tile_twiddles<R>(Ws, tw);
     const uint64_t pol_stream = l2_policy_first(), pol_keep = l2_policy_last();
     const int C = a.nchunks, D = a.look, S = a.nslots;
@@ -671,7 +672,22 @@ __global__ void __launch_bounds__(32 * PWARPS, 3) fft_grid2d(const Grid2DArgs a,
         if (threadIdx.x == 0) {
             pend = nxt >= 0 ? claim() : -1;  // the tile after next
             dv = dptr ? ld_relaxed(dptr) : N;
-            s_next = nxt;                    // read by every thread after the middle barrier
+            // The next tile's input, if it comes from HBM (phase A), is prefetched into L2 by every
+            // thread after the middle barrier, a half tile ahead: its loads then wait on L2 instead of
+            // HBM.  Phase-B inputs (the ring) are in L2 already.
+            const char* pf = nullptr;
+            if (a.prefetch && nxt >= 0) {
+                bool pa;
+                int cn, un;
+                decode_task(nxt, N, C, D, pa, cn, un);
+                const long long fb = (long long)(cn / NB) * N3, kbn = cn % NB;
+                if (pa && FWD)  // TL contiguous grid rows of slice kbn TL + un / NB (as tile_body reads them)
+                    pf = reinterpret_cast<const char*>(a.in) +
+                         (fb + (kbn * TL + un / NB) * N2 + (long long)(un % NB) * TL * N) * (REAL_IO ? 4 : 8);
+                else if (pa)    // N runs of TL pencil entries (128 bytes each, N^2 apart), one per p
+                    pf = reinterpret_cast<const char*>(a.in + fb + (long long)un * N + kbn * TL);
+            }
+            s_pf = pf;
         }
         auto mid = [&] {
             if (threadIdx.x == 0) {
@@ -682,29 +698,13 @@ __global__ void __launch_bounds__(32 * PWARPS, 3) fft_grid2d(const Grid2DArgs a,
                 s_cur[(it + 1) & 1] = nxt;
                 s_slow = !ready;
             }
-            // The next tile's input, if it comes from HBM (phase A), is requested into L2 now, a
-            // half tile ahead: its loads then wait on L2 instead of HBM.  Phase-B inputs (the
-            // ring) are in L2 already.  Thread 0 prefetches after its fence (measured faster than
-            // before it: the fence would also wait for its prefetches).
-            const int tn = a.prefetch ? s_next : -1;
-            if (tn >= 0) {
-                bool pa;
-                int cn, un;
-                decode_task(tn, N, C, D, pa, cn, un);
-                if (pa) {
-                    const long long fb = (long long)(cn / NB) * N3, kbn = cn % NB;
-                    if (FWD) {
-                        // TL contiguous grid rows of slice kbn TL + un / NB (as tile_body reads them)
-                        constexpr int ES = REAL_IO ? 4 : 8, NL = TL * N * ES / 128;
-                        const char* base = reinterpret_cast<const char*>(a.in) +
-                                           (fb + (kbn * TL + un / NB) * N2 + (long long)(un % NB) * TL * N) * ES;
-                        for (int i = threadIdx.x; i < NL; i += 32 * PWARPS) prefetch_l2(base + 128LL * i);
-                    } else {
-                        // N runs of TL pencil entries (128 bytes each), one per p
-                        const float2* base = a.in + fb + (long long)un * N + kbn * TL;
-                        for (int j = threadIdx.x; j < N; j += 32 * PWARPS) prefetch_l2(base + (long long)j * N2);
-                    }
-                }
+            // next-tile prefetch (thread 0 after its fence: measured faster than before it, the fence
+            // would also wait for its prefetches)
+            if (const char* pf = s_pf) {
+                constexpr int NL = FWD ? TL * N * (REAL_IO ? 4 : 8) / 128 : N;
+                constexpr long long STEP = FWD ? 128 : 8 * N2;
+#pragma unroll
+                for (int i = threadIdx.x; i < NL; i += 32 * PWARPS) prefetch_l2(pf + STEP * i);
             }
         };
         bool phaseA;
