@@ -449,6 +449,95 @@ def main_fp64(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+# --------------------------------------------------------------- point evaluation
+
+POINTS_METRIC = "SO(3) point evaluations/s at l_max={L}: inverse_transform(F, alpha, beta, gamma) at {n} rotations, FP64"
+FP64_NOMINAL_TFLOPS = 1.25  # GB300 FP64 (no FP64 figure among the measured peaks)
+
+
+def main_points(args) -> None:
+    """Batched point evaluation (fftso3_inverse_points, the reference's inverse_transform(F, alpha,
+    beta, gamma) of fdcl_FFTSO3.cpp:498-531 at many rotations) of one complex function at l_max = 127
+    (the size of the reference's own per-point timing), n seeded random rotations per call, FP64 with
+    the reference recursion.  CPU baseline: the oracle's restatement of the same function, one point per
+    host thread; the first points are also compared against the GPU values."""
+    import torch
+    from concurrent.futures import ThreadPoolExecutor
+
+    from fftso3_gb300 import _lib
+    from fftso3_gb300 import build as fbuild
+
+    fbuild.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    L, n = args.points_l_max, args.points
+    B = L + 1
+    C = B * (4 * B * B - 1) // 3
+    F = seeded_coeffs(L, 0)
+    plan = _lib.Plan(_lib.SO3_COMPLEX, L, 1, "fp64", "reference")
+    c = torch.from_numpy(F).to(dev)
+    rng = np.random.Generator(np.random.PCG64(11))
+    pts = np.ascontiguousarray(np.column_stack([rng.uniform(-np.pi, np.pi, n), rng.uniform(0.0, np.pi, n),
+                                                rng.uniform(-np.pi, np.pi, n)]))
+    out = np.empty(n, dtype=np.complex128)
+
+    def call():
+        plan.inverse_points(c.data_ptr(), 0, pts.ctypes.data_as(_lib._dp), n, out.ctypes.data, sp)
+
+    for _ in range(args.warmup):
+        call()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e0.record(stream)
+        for _ in range(args.steps):
+            call()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        wall = (time.perf_counter() - t0) / args.steps
+    ms = e0.elapsed_time(e1) / args.steps
+    clocks = clk.summary()
+    plan.check()
+    value = n * 1000.0 / ms
+    # algorithmic work: the (2l+1) F d products of every coefficient, 6 FP64 flops each, per point
+    achieved = 6.0 * C * n / (ms / 1000.0) / 1e12
+    roof = {"bound": "fp64", "unit": "TFLOP/s", "kernel": "so3_points_kernel", "achieved": achieved,
+            "peak": FP64_NOMINAL_TFLOPS, "frac": achieved / FP64_NOMINAL_TFLOPS, "peak_source": "nominal",
+            "algorithmic": "6 flops per coefficient per point (the recursion's flops not counted)",
+            "traffic": None}
+    cpu = None
+    parity = None
+    if not args.no_cpu:
+        from oracle import oracle as O
+
+        O.build()
+        nth = os.cpu_count() or 1
+        ns = min(n, 10 * nth)
+        t0 = time.perf_counter()
+        with ThreadPoolExecutor(max_workers=nth) as ex:
+            ref = list(ex.map(lambda i: O.so3_inverse_complex_point(L, F, *pts[i]), range(ns)))
+        dt = time.perf_counter() - t0
+        ref = np.array(ref)
+        parity = {"points": ns, "rel_err": float(np.linalg.norm(out[:ns] - ref) / np.linalg.norm(ref)),
+                  "max_abs_err": float(np.abs(out[:ns] - ref).max())}
+        cpu = {"value": ns / dt, "unit": "points/s", "cores": nth, "kind": "port",
+               "sample": f"the first {ns} of the {n} rotations, one point per host thread (oracle restatement of "
+                         "fdcl_FFTSO3.cpp:498-531 with its Wigner-d recursion :127-194)", "seconds": dt}
+    line = {"metric": POINTS_METRIC.format(L=L, n=n), "value": value, "unit": "points/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"one complex SO(3) function, l_max={L} (C={C} coefficients, N(0,1)(l+1)^-1.5), "
+                                   f"{n} seeded random rotations per call, FP64, reference recursion",
+                       "l2": "coefficients (one 16-byte read per coefficient per point) stay in L2"},
+            "e2e": {"value": n / wall, "unit": "points/s", "h2d_bytes_per_step": 24 * n,
+                    "d2h_bytes_per_step": 16 * n},
+            "gpu_launches": args.steps, "roofline": roof, "clocks": clocks, "cpu_baseline": cpu, "parity": parity}
+    print(json.dumps(line), flush=True)
+
+
 # --------------------------------------------------------------- grid FFT stage
 
 FFT_METRIC = "SO(3) grid FFT stage GB/s (grids <-> pencils, one launch per direction), N={N}, {nf} grids"
@@ -657,13 +746,15 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp32", action="store_true", help="skip the FP32 CUDA-core beta-sum comparison")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64 reference (profiling runs)")
-    ap.add_argument("--workload", default="lmax255", choices=["lmax255", "uneven", "s2", "fp64", "fft"],
+    ap.add_argument("--workload", default="lmax255", choices=["lmax255", "uneven", "s2", "fp64", "fft", "points"],
                     help="lmax255: the headline SO(3) batch at one l_max (--l-max/--batch); uneven: the "
                          "mixed-bandwidth SO(3) batch; s2: the S^2 batch at l_max=511")
     ap.add_argument("--functions", type=int, default=4096, help="uneven workload: number of functions")
     ap.add_argument("--s2-l-max", type=int, default=511, help="s2 workload: l_max")
     ap.add_argument("--fp64-l-max", type=int, default=127, help="fp64 workload: l_max")
     ap.add_argument("--fft-n", type=int, default=512, help="fft workload: grid size N (64..512), --batch grids")
+    ap.add_argument("--points", type=int, default=4096, help="points workload: rotations per call")
+    ap.add_argument("--points-l-max", type=int, default=127, help="points workload: l_max")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -679,6 +770,9 @@ def main() -> None:
         return
     if args.workload == "fft":
         main_fft(args)
+        return
+    if args.workload == "points":
+        main_points(args)
         return
 
     import torch

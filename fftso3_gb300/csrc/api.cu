@@ -116,6 +116,8 @@ struct fftso3_plan {
     void* d_io_coeff = nullptr;
     void* d_corr = nullptr;        // correlation coefficients (fftso3_correlate_s2)
     void* d_amax = nullptr;        // arg-max scratch (fftso3_grid_argmax)
+    void* d_prec = nullptr;        // point evaluation: beta-independent recursion factors (built on first use)
+    double* d_psq = nullptr;       //   and the seed factors (inside the same allocation)
     long long bytes = 0;
     TCState* tc = nullptr;         // tensor-core contraction state
     StageTimer timer;              // optional per-stage CUDA-event timing
@@ -142,7 +144,7 @@ int plan_alloc(fftso3_plan* p, void** ptr, size_t bytes)
 void plan_free(fftso3_plan* p)
 {
     void* ptrs[] = {p->d_tw, p->d_w, p->d_goff, p->d_table, p->d_lfact, p->d_work, p->d_fc, p->d_io_grid,
-                    p->d_io_coeff, p->d_corr, p->d_amax};
+                    p->d_io_coeff, p->d_corr, p->d_amax, p->d_prec};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     if (p->tc) tc_destroy(p->tc);
@@ -652,12 +654,34 @@ int fftso3_inverse_points(fftso3_plan* plan, const void* coeffs, int index, cons
     if ((e = cudaMalloc(&d_out, sizeof(double2) * n)) != cudaSuccess) { cleanup(); return cuda_fail(e, "cudaMalloc"); }
     cudaMemcpyAsync(d_pts, pts, sizeof(double) * dim * n, cudaMemcpyHostToDevice, st);
     if (plan->so3) {
+        if (!plan->d_prec) {  // the plan's recursion factors, once
+            const size_t nrec = wigner_rec_elems(L), nsq = wigner_sq_elems(L);
+            if ((rc = plan_alloc(plan, &plan->d_prec, sizeof(double4) * nrec + sizeof(double) * nsq))) {
+                cleanup();
+                return rc;
+            }
+            plan->d_psq = (double*)((double4*)plan->d_prec + nrec);
+            if ((e = launch_wigner_rec_factors((double4*)plan->d_prec, plan->d_psq, L, st)) != cudaSuccess) {
+                cleanup();
+                return cuda_fail(e, "recursion factors");
+            }
+        }
+        int dev = 0, nsm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        int m0b[MAX_POINT_PARTS + 1];
+        const int S = so3_points_parts(L, n, nsm, m0b);
         std::vector<WignerSeeds> seeds(n);
         for (int i = 0; i < n; ++i) seeds[i] = make_seeds(pts[3 * i + 1]);
-        if ((e = cudaMalloc(&d_seed, sizeof(WignerSeeds) * n)) != cudaSuccess) { cleanup(); return cuda_fail(e, "cudaMalloc"); }
+        if ((e = cudaMalloc(&d_seed, sizeof(WignerSeeds) * n + sizeof(double2) * (size_t)S * n)) != cudaSuccess) {
+            cleanup();
+            return cuda_fail(e, "cudaMalloc");
+        }
+        double2* d_part = (double2*)((char*)d_seed + sizeof(WignerSeeds) * n);
         cudaMemcpyAsync(d_seed, seeds.data(), sizeof(WignerSeeds) * n, cudaMemcpyHostToDevice, st);
-        e = launch_so3_points(Fc, (const WignerSeeds*)d_seed, (const double*)d_pts, plan->d_lfact, L,
-                              plan->recursion == FFTSO3_RECURSION_STABLE, n, (double2*)d_out, st);
+        e = launch_so3_points(Fc, (const WignerSeeds*)d_seed, (const double*)d_pts, (const double4*)plan->d_prec,
+                              plan->d_psq, plan->d_lfact, L, plan->recursion == FFTSO3_RECURSION_STABLE, n, m0b, S,
+                              d_part, (double2*)d_out, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // seeds vector must outlive the copy
     } else {
         std::vector<double> xs(n);

@@ -23,8 +23,17 @@ cudaError_t launch_wigner_table(double* table, const long long* goff, const Wign
                                 int L, int N, int ngroups, bool stable, cudaStream_t st);
 cudaError_t launch_legendre_table(double* table, const long long* moff, const double* xs, int L, int N,
                                   cudaStream_t st);
-cudaError_t launch_so3_points(const double2* F, const WignerSeeds* pseeds, const double* pts, const double* lfact,
-                              int L, bool stable, int n, double2* out, cudaStream_t st);
+// SO(3) point evaluation (see tables.cu): the beta-independent recursion factors (built once per
+// plan: wigner_rec_elems(L) double4 and wigner_sq_elems(L) doubles), the split of the degrees into
+// parts (m0b: MAX_POINT_PARTS + 1 ints), and the launch (part: S x n double2 scratch).
+constexpr int MAX_POINT_PARTS = 32;
+size_t wigner_rec_elems(int L);
+size_t wigner_sq_elems(int L);
+cudaError_t launch_wigner_rec_factors(double4* rec, double* sq, int L, cudaStream_t st);
+int so3_points_parts(int L, int n, int nsm, int* m0b);
+cudaError_t launch_so3_points(const double2* F, const WignerSeeds* pseeds, const double* pts, const double4* rec,
+                              const double* sq, const double* lfact, int L, bool stable, int n, const int* m0b,
+                              int S, double2* part, double2* out, cudaStream_t st);
 cudaError_t launch_wigner_full(const WignerSeeds* seed, const double* lfact, int L, bool stable, double* out,
                                cudaStream_t st);
 cudaError_t launch_s2_points(const double2* F, const double* xs, const double* pts, int L, int n, double2* out,
