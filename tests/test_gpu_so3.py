@@ -192,6 +192,27 @@ def test_point_evaluation_matches_reference(gblib, oracle, kind):
     assert rel_err(got, want) < 1e-12
 
 
+@pytest.mark.parametrize("recursion", ["reference", "stable"])
+def test_point_evaluation_partial_warp_many_parts(gblib, oracle, recursion):
+    """Point evaluation with a partial last warp of points and the degrees split into many parts
+    (45 points at l_max = 37: two batches of 32 points, 32 degree parts), points near both poles,
+    and a one-point call; both recursions against the oracle (no underflow at this l_max, so the
+    stable recursion agrees with the reference's to rounding)."""
+    import fftso3_gb300 as fg
+    L = 37
+    rng = np.random.default_rng(21)
+    T = fg.FFTSO3_complex(L, recursion=recursion)
+    F = fg.FFTSO3_matrix_complex(L, data=so3_coeffs(L, 13))
+    pts = np.column_stack([rng.uniform(-np.pi, np.pi, 45), rng.uniform(0.0, np.pi, 45),
+                           rng.uniform(-np.pi, np.pi, 45)])
+    pts[0, 1], pts[1, 1] = 1e-3, np.pi - 1e-3
+    got = T.inverse_points(F, pts)
+    want = np.array([oracle.so3_inverse_complex_point(L, F.M, *p) for p in pts])
+    assert rel_err(got, want) < TOL
+    one = T.inverse_points(F, pts[5:6])
+    assert abs(one[0] - want[5]) < TOL * abs(want[5])
+
+
 def test_python_api_example0(gblib):
     """README example0 through the drop-in API on the GPU: tr R -> F^1 = I/3, f(I) = 3."""
     import fftso3_gb300 as fg
