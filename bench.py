@@ -452,6 +452,7 @@ def main_fp64(args) -> None:
 # --------------------------------------------------------------- point evaluation
 
 POINTS_METRIC = "SO(3) point evaluations/s at l_max={L}: inverse_transform(F, alpha, beta, gamma) at {n} rotations, FP64"
+S2_POINTS_METRIC = "S^2 point evaluations/s at l_max={L}: inverse_transform(F, theta, phi) at {n} points, FP64"
 FP64_NOMINAL_TFLOPS = 1.25  # GB300 FP64 (no FP64 figure among the measured peaks)
 
 
@@ -472,15 +473,23 @@ def main_points(args) -> None:
     torch.cuda.set_device(dev)
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
-    L, n = args.points_l_max, args.points
+    s2 = args.points_kind == "s2"
+    L, n = (args.s2_l_max if s2 else args.points_l_max), args.points
     B = L + 1
-    C = B * (4 * B * B - 1) // 3
-    F = seeded_coeffs(L, 0)
-    plan = _lib.Plan(_lib.SO3_COMPLEX, L, 1, "fp64", "reference")
-    c = torch.from_numpy(F).to(dev)
     rng = np.random.Generator(np.random.PCG64(11))
-    pts = np.ascontiguousarray(np.column_stack([rng.uniform(-np.pi, np.pi, n), rng.uniform(0.0, np.pi, n),
-                                                rng.uniform(-np.pi, np.pi, n)]))
+    if s2:
+        C = B * B
+        l = np.concatenate([np.full(2 * x + 1, x) for x in range(B)])
+        F = (rng.standard_normal(C) + 1j * rng.standard_normal(C)) / (l + 1.0)
+        plan = _lib.Plan(_lib.S2_COMPLEX, L, 1, "fp64", "reference")
+        pts = np.ascontiguousarray(np.column_stack([rng.uniform(0.0, np.pi, n), rng.uniform(0.0, 2 * np.pi, n)]))
+    else:
+        C = B * (4 * B * B - 1) // 3
+        F = seeded_coeffs(L, 0)
+        plan = _lib.Plan(_lib.SO3_COMPLEX, L, 1, "fp64", "reference")
+        pts = np.ascontiguousarray(np.column_stack([rng.uniform(-np.pi, np.pi, n), rng.uniform(0.0, np.pi, n),
+                                                    rng.uniform(-np.pi, np.pi, n)]))
+    c = torch.from_numpy(F).to(dev)
     out = np.empty(n, dtype=np.complex128)
 
     def call():
@@ -502,11 +511,14 @@ def main_points(args) -> None:
     clocks = clk.summary()
     plan.check()
     value = n * 1000.0 / ms
-    # algorithmic work: the (2l+1) F d products of every coefficient, 6 FP64 flops each, per point
-    achieved = 6.0 * C * n / (ms / 1000.0) / 1e12
-    roof = {"bound": "fp64", "unit": "TFLOP/s", "kernel": "so3_points_kernel", "achieved": achieved,
-            "peak": FP64_NOMINAL_TFLOPS, "frac": achieved / FP64_NOMINAL_TFLOPS, "peak_source": "nominal",
-            "algorithmic": "6 flops per coefficient per point (the recursion's flops not counted)",
+    # algorithmic work per point: SO(3) the (2l+1) F d products, 6 FP64 flops per coefficient; S^2 the
+    # F nP products, 4 flops per coefficient
+    fpc = 4.0 if s2 else 6.0
+    achieved = fpc * C * n / (ms / 1000.0) / 1e12
+    roof = {"bound": "fp64", "unit": "TFLOP/s", "kernel": "s2_points_kernel" if s2 else "so3_points_kernel",
+            "achieved": achieved, "peak": FP64_NOMINAL_TFLOPS, "frac": achieved / FP64_NOMINAL_TFLOPS,
+            "peak_source": "nominal",
+            "algorithmic": f"{int(fpc)} flops per coefficient per point (the recursion's flops not counted)",
             "traffic": None}
     cpu = None
     parity = None
@@ -517,22 +529,32 @@ def main_points(args) -> None:
         nth = os.cpu_count() or 1
         ns = min(n, 10 * nth)
         t0 = time.perf_counter()
+        one = (lambda i: O.s2_inverse_complex_point(L, F, *pts[i])) if s2 else \
+            (lambda i: O.so3_inverse_complex_point(L, F, *pts[i]))
+        if s2:
+            ns = min(n, 200 * nth)
         with ThreadPoolExecutor(max_workers=nth) as ex:
-            ref = list(ex.map(lambda i: O.so3_inverse_complex_point(L, F, *pts[i]), range(ns)))
+            ref = list(ex.map(one, range(ns)))
         dt = time.perf_counter() - t0
         ref = np.array(ref)
         parity = {"points": ns, "rel_err": float(np.linalg.norm(out[:ns] - ref) / np.linalg.norm(ref)),
                   "max_abs_err": float(np.abs(out[:ns] - ref).max())}
+        src = ("fdcl_FFTS2.cpp:194-230 with its Legendre recursion :48-100" if s2 else
+               "fdcl_FFTSO3.cpp:498-531 with its Wigner-d recursion :127-194")
         cpu = {"value": ns / dt, "unit": "points/s", "cores": nth, "kind": "port",
-               "sample": f"the first {ns} of the {n} rotations, one point per host thread (oracle restatement of "
-                         "fdcl_FFTSO3.cpp:498-531 with its Wigner-d recursion :127-194)", "seconds": dt}
-    line = {"metric": POINTS_METRIC.format(L=L, n=n), "value": value, "unit": "points/s", "n_gpus": 1,
+               "sample": f"the first {ns} of the {n} points, one point per host thread (oracle restatement of "
+                         f"{src})", "seconds": dt}
+    what = (f"one complex S^2 function, l_max={L} (C={C} coefficients, N(0,1)/(l+1)), {n} seeded random points "
+            "per call, FP64, the reference's Legendre recursion" if s2 else
+            f"one complex SO(3) function, l_max={L} (C={C} coefficients, N(0,1)(l+1)^-1.5), "
+            f"{n} seeded random rotations per call, FP64, reference recursion")
+    line = {"metric": (S2_POINTS_METRIC if s2 else POINTS_METRIC).format(L=L, n=n), "value": value,
+            "unit": "points/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"one complex SO(3) function, l_max={L} (C={C} coefficients, N(0,1)(l+1)^-1.5), "
-                                   f"{n} seeded random rotations per call, FP64, reference recursion",
+            "config": {"workload": what,
                        "l2": "coefficients (one 16-byte read per coefficient per point) stay in L2"},
-            "e2e": {"value": n / wall, "unit": "points/s", "h2d_bytes_per_step": 24 * n,
+            "e2e": {"value": n / wall, "unit": "points/s", "h2d_bytes_per_step": (16 if s2 else 24) * n,
                     "d2h_bytes_per_step": 16 * n},
             "gpu_launches": args.steps, "roofline": roof, "clocks": clocks, "cpu_baseline": cpu, "parity": parity}
     print(json.dumps(line), flush=True)
@@ -754,7 +776,9 @@ def main() -> None:
     ap.add_argument("--fp64-l-max", type=int, default=127, help="fp64 workload: l_max")
     ap.add_argument("--fft-n", type=int, default=512, help="fft workload: grid size N (64..512), --batch grids")
     ap.add_argument("--points", type=int, default=4096, help="points workload: rotations per call")
-    ap.add_argument("--points-l-max", type=int, default=127, help="points workload: l_max")
+    ap.add_argument("--points-l-max", type=int, default=127, help="points workload: l_max (SO(3))")
+    ap.add_argument("--points-kind", default="so3", choices=["so3", "s2"],
+                    help="points workload: SO(3) rotations (--points-l-max) or S^2 points (--s2-l-max)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -116,8 +116,8 @@ struct fftso3_plan {
     void* d_io_coeff = nullptr;
     void* d_corr = nullptr;        // correlation coefficients (fftso3_correlate_s2)
     void* d_amax = nullptr;        // arg-max scratch (fftso3_grid_argmax)
-    void* d_prec = nullptr;        // point evaluation: beta-independent recursion factors (built on first use)
-    double* d_psq = nullptr;       //   and the seed factors (inside the same allocation)
+    void* d_prec = nullptr;        // point evaluation: beta-independent recursion factors (built on first use:
+    double* d_psq = nullptr;       //   SO(3) Wigner factors + seed factors here, or S^2 Legendre factors)
     long long bytes = 0;
     TCState* tc = nullptr;         // tensor-core contraction state
     StageTimer timer;              // optional per-stage CUDA-event timing
@@ -653,6 +653,9 @@ int fftso3_inverse_points(fftso3_plan* plan, const void* coeffs, int index, cons
     if ((e = cudaMalloc(&d_pts, sizeof(double) * dim * n)) != cudaSuccess) { cleanup(); return cuda_fail(e, "cudaMalloc"); }
     if ((e = cudaMalloc(&d_out, sizeof(double2) * n)) != cudaSuccess) { cleanup(); return cuda_fail(e, "cudaMalloc"); }
     cudaMemcpyAsync(d_pts, pts, sizeof(double) * dim * n, cudaMemcpyHostToDevice, st);
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     if (plan->so3) {
         if (!plan->d_prec) {  // the plan's recursion factors, once
             const size_t nrec = wigner_rec_elems(L), nsq = wigner_sq_elems(L);
@@ -666,11 +669,8 @@ int fftso3_inverse_points(fftso3_plan* plan, const void* coeffs, int index, cons
                 return cuda_fail(e, "recursion factors");
             }
         }
-        int dev = 0, nsm = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
         int m0b[MAX_POINT_PARTS + 1];
-        const int S = so3_points_parts(L, n, nsm, m0b);
+        const int S = points_parts(true, L, n, nsm, m0b);
         std::vector<WignerSeeds> seeds(n);
         for (int i = 0; i < n; ++i) seeds[i] = make_seeds(pts[3 * i + 1]);
         if ((e = cudaMalloc(&d_seed, sizeof(WignerSeeds) * n + sizeof(double2) * (size_t)S * n)) != cudaSuccess) {
@@ -684,11 +684,28 @@ int fftso3_inverse_points(fftso3_plan* plan, const void* coeffs, int index, cons
                               d_part, (double2*)d_out, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // seeds vector must outlive the copy
     } else {
+        if (!plan->d_prec) {  // the plan's Legendre factors, once
+            if ((rc = plan_alloc(plan, &plan->d_prec, sizeof(double2) * legendre_rec_elems(L)))) {
+                cleanup();
+                return rc;
+            }
+            if ((e = launch_legendre_rec_factors((double2*)plan->d_prec, L, st)) != cudaSuccess) {
+                cleanup();
+                return cuda_fail(e, "recursion factors");
+            }
+        }
+        int m0b[MAX_POINT_PARTS + 1];
+        const int S = points_parts(false, L, n, nsm, m0b);
         std::vector<double> xs(n);
         for (int i = 0; i < n; ++i) xs[i] = cos(pts[2 * i]);
-        if ((e = cudaMalloc(&d_seed, sizeof(double) * n)) != cudaSuccess) { cleanup(); return cuda_fail(e, "cudaMalloc"); }
+        if ((e = cudaMalloc(&d_seed, sizeof(double) * n + sizeof(double2) * (size_t)S * n + 16)) != cudaSuccess) {
+            cleanup();
+            return cuda_fail(e, "cudaMalloc");
+        }
+        double2* d_part = (double2*)(((uintptr_t)d_seed + sizeof(double) * n + 15) & ~(uintptr_t)15);
         cudaMemcpyAsync(d_seed, xs.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st);
-        e = launch_s2_points(Fc, (const double*)d_seed, (const double*)d_pts, L, n, (double2*)d_out, st);
+        e = launch_s2_points(Fc, (const double*)d_seed, (const double*)d_pts, (const double2*)plan->d_prec, L, n, m0b,
+                             S, d_part, (double2*)d_out, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     }
     if (e != cudaSuccess) { cleanup(); return cuda_fail(e, "point evaluation"); }

@@ -347,20 +347,21 @@ __global__ void sum_parts_kernel(const double2* __restrict__ part, int S, int n,
     out[i] = a;
 }
 
-// Degree parts of about equal work ((2 m0 + 1)(L - m0 + 2) per m0), enough of them that the
-// launch has about 8 warps per SM; returns their number S, bounds in m0b[0..S].
-int so3_points_parts(int L, int n, int nsm, int* m0b)
+// Degree parts of about equal work ((2 m0 + 1)(L - m0 + 2) per m0 for SO(3), L - m + 2 per order m for
+// S^2), enough of them that the launch has about 8 warps per SM; returns their number S, bounds in m0b[0..S].
+int points_parts(bool so3, int L, int n, int nsm, int* m0b)
 {
     const long long nb = ((long long)n + 31) / 32;
     long long S = (8LL * std::max(nsm, 1) + nb - 1) / nb;
     S = std::max(1LL, std::min<long long>({S, (long long)MAX_POINT_PARTS, (long long)L + 1}));
+    auto work = [&](int m) { return (so3 ? 2.0 * m + 1.0 : 1.0) * (L - m + 2); };
     double total = 0.;
-    for (int m = 0; m <= L; ++m) total += (2.0 * m + 1.0) * (L - m + 2);
+    for (int m = 0; m <= L; ++m) total += work(m);
     int k = 0;
     m0b[0] = 0;
     double cum = 0.;
     for (int m = 0; m <= L && k + 1 < S; ++m) {
-        cum += (2.0 * m + 1.0) * (L - m + 2);
+        cum += work(m);
         if (cum >= total * (double)(k + 1) / (double)S && m + 1 <= L) m0b[++k] = m + 1;
     }
     m0b[++k] = L + 1;
@@ -387,47 +388,123 @@ cudaError_t launch_so3_points(const double2* F, const WignerSeeds* pseeds, const
     return cudaGetLastError();
 }
 
-// y(theta,phi) = sum_{l,m} F(l,m) nP(l,m)(cos theta) e^{i m phi} (fdcl_FFTS2.cpp:17-46, :194-230).
-template <int NT>
-__global__ void __launch_bounds__(NT) s2_points_kernel(const double2* __restrict__ F, const double* __restrict__ xs,
-                                                       const double* __restrict__ pts, int L, double2* __restrict__ out)
+// ------------------------------------------------- S^2 point evaluation
+//
+// y(theta,phi) = sum_{l,m} F(l,m) nP(l,m)(cos theta) e^{i m phi} (fdcl_FFTS2.cpp:17-46, :194-230), in the
+// layout of the SO(3) point kernel: one warp per 32 points, the orders m split into parts of equal work.
+// The Legendre recursion of fdcl_FFTS2.cpp:48-100 runs with its beta-independent factors from a per-plan
+// table: step l uses fact(l, m) = sqrt((4l^2 - 1)/(l^2 - m^2)) and 1/fact(l - 1, m) (the reference
+// divides by fact(l - 1, m), so values agree with it to rounding, not bit for bit); the seed pmm(m) keeps
+// the reference's operations, chained over m.  Table: per m, rows l = m + 2..L of {fact, 1/previous
+// fact}, starting at s2_row0(m) (the first previous fact is sqrt(2m + 3)).
+__host__ __device__ inline long long s2_row0(int m, int L)
 {
-    const int pt = blockIdx.x;
-    const double phi = pts[2 * pt + 1];
-    double2 acc = make_double2(0., 0.);
-    for (int m = threadIdx.x; m <= L; m += NT) {
-        double pr = 0., pi = 0., qr = 0., qi = 0.;
-        auto emit = [&](int l, double v) {
-            double2 a = F[s2_idx(l, m)];
-            pr += a.x * v;
-            pi += a.y * v;
-            if (m > 0) {
-                double2 b = F[s2_idx(l, -m)];
-                qr += b.x * v;
-                qi += b.y * v;
-            }
-        };
-        legendre_column_faithful(m, L, xs[pt], emit);
-        double sp, cp;
-        sincos((double)m * phi, &sp, &cp);
-        acc.x += pr * cp - pi * sp;
-        acc.y += pr * sp + pi * cp;
-        if (m > 0) {
-            double sg = (m & 1) ? -1.0 : 1.0;  // nP(l,-m) = (-1)^m nP(l,m), e^{-i m phi}
-            qr *= sg;
-            qi *= sg;
-            acc.x += qr * cp + qi * sp;
-            acc.y += qi * cp - qr * sp;
-        }
+    long long o = 0;
+    for (int k = 0; k < m; ++k) o += (L - k - 1 > 0) ? L - k - 1 : 0;
+    return o;
+}
+size_t legendre_rec_elems(int L) { return (size_t)std::max<long long>(s2_row0(L + 1, L), 1); }
+
+__global__ void legendre_rec_factors_kernel(double2* __restrict__ rec, int L)
+{
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m > L) return;
+    double2* row = rec + s2_row0(m, L);
+    double oldfact = sqrt(2.0 * (double)m + 3.0);
+    for (int l = m + 2; l <= L; ++l) {
+        const double fact = sqrt((4.0 * (double)l * (double)l - 1.0) / (double)(l * l - m * m));
+        row[l - m - 2] = make_double2(fact, 1.0 / oldfact);
+        oldfact = fact;
     }
-    double2 t = block_sum<NT>(acc);
-    if (threadIdx.x == 0) out[pt] = t;
 }
 
-cudaError_t launch_s2_points(const double2* F, const double* xs, const double* pts, int L, int n, double2* out,
-                             cudaStream_t st)
+cudaError_t launch_legendre_rec_factors(double2* rec, int L, cudaStream_t st)
 {
-    s2_points_kernel<128><<<n, 128, 0, st>>>(F, xs, pts, L, out);
+    legendre_rec_factors_kernel<<<(L + 1 + 127) / 128, 128, 0, st>>>(rec, L);
+    return cudaGetLastError();
+}
+
+__global__ void __launch_bounds__(32 * PW) s2_points_kernel(const double2* __restrict__ F, const double* __restrict__ xs,
+                                                            const double* __restrict__ pts,
+                                                            const double2* __restrict__ rec, int L, int n,
+                                                            const PointParts parts, double2* __restrict__ part)
+{
+    const double fourpi = 4.0 * 3.14159265358979323846;
+    const int lane = threadIdx.x & 31;
+    const int b = blockIdx.x * PW + (threadIdx.x >> 5);
+    if (b * 32 >= n) return;
+    const int pt = b * 32 + lane;
+    const int pq = pt < n ? pt : n - 1;  // lanes past n evaluate a copy of the last point, not written
+    const double x = xs[pq], phi = pts[2 * pq + 1];
+    const double omx2 = (1.0 - x) * (1.0 + x);
+    const int mb = parts.m0[blockIdx.y], me = parts.m0[blockIdx.y + 1];
+    // pmm before its sqrt: prod_{i <= m} omx2 (2i - 1) / (2i), the reference's loop chained over m
+    double praw = 1.0;
+    for (int i = 1; i < mb; ++i) {
+        const double fact = (double)(2 * i - 1);
+        praw *= omx2 * fact / (fact + 1.0);
+    }
+    long long row = s2_row0(mb, L);
+    double2 acc = make_double2(0., 0.);
+    for (int m = mb; m < me; ++m) {
+        double pmm;
+        if (m == 0) {
+            pmm = sqrt(1. / fourpi);
+        } else {
+            const double fact = (double)(2 * m - 1);
+            praw *= omx2 * fact / (fact + 1.0);
+            pmm = sqrt((double)(2 * m + 1) * praw / fourpi);
+            if (m & 1) pmm = -pmm;
+        }
+        double2 Dp = make_double2(0., 0.), Dn = Dp;
+        auto emit = [&](int l, double v) {
+            const double2 a = __ldg(&F[s2_idx(l, m)]);
+            Dp.x = __fma_rn(a.x, v, Dp.x);
+            Dp.y = __fma_rn(a.y, v, Dp.y);
+            if (m > 0) {
+                const double2 c = __ldg(&F[s2_idx(l, -m)]);
+                Dn.x = __fma_rn(c.x, v, Dn.x);
+                Dn.y = __fma_rn(c.y, v, Dn.y);
+            }
+        };
+        emit(m, pmm);
+        if (m + 1 <= L) {
+            double p1 = x * sqrt(2.0 * (double)m + 3.0) * pmm, p0 = pmm;
+            emit(m + 1, p1);
+            for (int l = m + 2; l <= L; ++l) {
+                const double2 f = __ldg(&rec[row + (l - m - 2)]);
+                const double v = (x * p1 - p0 * f.y) * f.x;
+                emit(l, v);
+                p0 = p1;
+                p1 = v;
+            }
+        }
+        row += (L - m - 1 > 0) ? L - m - 1 : 0;
+        double sp, cp;
+        sincos((double)m * phi, &sp, &cp);
+        acc.x += Dp.x * cp - Dp.y * sp;  // F(l, m) nP e^{i m phi}
+        acc.y += Dp.x * sp + Dp.y * cp;
+        if (m > 0) {
+            const double sg = (m & 1) ? -1.0 : 1.0;  // nP(l,-m) = (-1)^m nP(l,m), e^{-i m phi}
+            acc.x += sg * (Dn.x * cp + Dn.y * sp);
+            acc.y += sg * (Dn.y * cp - Dn.x * sp);
+        }
+    }
+    if (pt < n) part[(long long)blockIdx.y * n + pt] = acc;
+}
+
+cudaError_t launch_s2_points(const double2* F, const double* xs, const double* pts, const double2* rec, int L, int n,
+                             const int* m0b, int S, double2* part, double2* out, cudaStream_t st)
+{
+    if (S < 1 || S > MAX_POINT_PARTS) return cudaErrorInvalidValue;
+    PointParts P;
+    for (int s = 0; s <= S; ++s) P.m0[s] = m0b[s];
+    const long long nb = ((long long)n + 31) / 32;
+    const dim3 grid((unsigned)((nb + PW - 1) / PW), (unsigned)S);
+    s2_points_kernel<<<grid, 32 * PW, 0, st>>>(F, xs, pts, rec, L, n, P, part);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    sum_parts_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(part, S, n, out);
     return cudaGetLastError();
 }
 

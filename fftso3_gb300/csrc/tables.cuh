@@ -30,13 +30,16 @@ constexpr int MAX_POINT_PARTS = 32;
 size_t wigner_rec_elems(int L);
 size_t wigner_sq_elems(int L);
 cudaError_t launch_wigner_rec_factors(double4* rec, double* sq, int L, cudaStream_t st);
-int so3_points_parts(int L, int n, int nsm, int* m0b);
+int points_parts(bool so3, int L, int n, int nsm, int* m0b);
 cudaError_t launch_so3_points(const double2* F, const WignerSeeds* pseeds, const double* pts, const double4* rec,
                               const double* sq, const double* lfact, int L, bool stable, int n, const int* m0b,
                               int S, double2* part, double2* out, cudaStream_t st);
 cudaError_t launch_wigner_full(const WignerSeeds* seed, const double* lfact, int L, bool stable, double* out,
                                cudaStream_t st);
-cudaError_t launch_s2_points(const double2* F, const double* xs, const double* pts, int L, int n, double2* out,
-                             cudaStream_t st);
+// S^2 point evaluation: the per-plan Legendre factors (legendre_rec_elems(L) double2) and the launch
+size_t legendre_rec_elems(int L);
+cudaError_t launch_legendre_rec_factors(double2* rec, int L, cudaStream_t st);
+cudaError_t launch_s2_points(const double2* F, const double* xs, const double* pts, const double2* rec, int L, int n,
+                             const int* m0b, int S, double2* part, double2* out, cudaStream_t st);
 
 }  // namespace fftso3

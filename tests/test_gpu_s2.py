@@ -86,6 +86,24 @@ def test_s2_point_evaluation(gblib, oracle):
     assert rel_err(got, want) < 1e-12
 
 
+def test_s2_point_evaluation_partial_warp_many_parts(gblib, oracle):
+    """S^2 point evaluation at l_max = 511 (the S^2 batching size) with a partial last warp (70
+    points: three batches of 32) and the orders split into many parts, points near both poles
+    (where the reference's seed underflows at high m), and a one-point call."""
+    import fftso3_gb300 as fg
+    L = 511
+    rng = np.random.default_rng(5)
+    pts = np.column_stack([rng.uniform(0.0, np.pi, 70), rng.uniform(0, 2 * np.pi, 70)])
+    pts[0, 0], pts[1, 0] = 1e-3, np.pi - 1e-3
+    T = fg.FFTS2_complex(L)
+    F = fg.FFTS2_matrix_complex(L, data=s2_coeffs(L, 6))
+    got = T.inverse_points(F, pts)
+    want = np.array([oracle.s2_inverse_complex_point(L, F.M, *p) for p in pts])
+    assert rel_err(got, want) < 1e-12
+    one = T.inverse_points(F, pts[7:8])
+    assert abs(one[0] - want[7]) < 1e-12 * abs(want[7])
+
+
 def test_s2_python_api_roundtrip(gblib):
     import fftso3_gb300 as fg
     assert fg.FFTS2_complex(5).check_transform(np.random.default_rng(0)) < 1e-10
