@@ -118,6 +118,8 @@ struct fftso3_plan {
     void* d_amax = nullptr;        // arg-max scratch (fftso3_grid_argmax)
     void* d_prec = nullptr;        // point evaluation: beta-independent recursion factors (built on first use:
     double* d_psq = nullptr;       //   SO(3) Wigner factors + seed factors here, or S^2 Legendre factors)
+    void* d_pscratch = nullptr;    // point evaluation scratch (grows with n)
+    size_t pscratch_bytes = 0;
     long long bytes = 0;
     TCState* tc = nullptr;         // tensor-core contraction state
     StageTimer timer;              // optional per-stage CUDA-event timing
@@ -144,7 +146,7 @@ int plan_alloc(fftso3_plan* p, void** ptr, size_t bytes)
 void plan_free(fftso3_plan* p)
 {
     void* ptrs[] = {p->d_tw, p->d_w, p->d_goff, p->d_table, p->d_lfact, p->d_work, p->d_fc, p->d_io_grid,
-                    p->d_io_coeff, p->d_corr, p->d_amax, p->d_prec};
+                    p->d_io_coeff, p->d_corr, p->d_amax, p->d_prec, p->d_pscratch};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     if (p->tc) tc_destroy(p->tc);
@@ -628,95 +630,86 @@ int fftso3_inverse_points(fftso3_plan* plan, const void* coeffs, int index, cons
     const int L = plan->L;
     const long long C = plan->coeff_elems;
     const int dim = plan->so3 ? 3 : 2;
-    // complex coefficients of the selected function
-    void* d_c = nullptr;
-    void* d_pts = nullptr;
-    void* d_seed = nullptr;
-    void* d_out = nullptr;
-    auto cleanup = [&]() {
-        if (d_c) cudaFree(d_c);
-        if (d_pts) cudaFree(d_pts);
-        if (d_seed) cudaFree(d_seed);
-        if (d_out) cudaFree(d_out);
-    };
     cudaError_t e;
+    // the plan's recursion factors, once
+    if (!plan->d_prec) {
+        if (plan->so3) {
+            const size_t nrec = wigner_rec_elems(L), nsq = wigner_sq_elems(L);
+            if ((rc = plan_alloc(plan, &plan->d_prec, sizeof(double4) * nrec + sizeof(double) * nsq))) return rc;
+            plan->d_psq = (double*)((double4*)plan->d_prec + nrec);
+            e = launch_wigner_rec_factors((double4*)plan->d_prec, plan->d_psq, L, st);
+        } else {
+            if ((rc = plan_alloc(plan, &plan->d_prec, sizeof(double2) * legendre_rec_elems(L)))) return rc;
+            e = launch_legendre_rec_factors((double2*)plan->d_prec, L, st);
+        }
+        if (e != cudaSuccess) return cuda_fail(e, "recursion factors");
+    }
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    int m0b[MAX_POINT_PARTS + 1];
+    const int S = points_parts(plan->so3, L, n, nsm, m0b);
+    // plan-owned scratch (grows, never shrinks; the call synchronises before returning):
+    // [points][values][seeds][parts][complex coefficients of a real kind], 256-byte aligned pieces
+    auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t b_pts = up(sizeof(double) * dim * n), b_out = up(sizeof(double2) * n);
+    const size_t b_seed = up(plan->so3 ? sizeof(WignerSeeds) * n : sizeof(double) * n);
+    const size_t b_part = up(sizeof(double2) * (size_t)S * n), b_c = plan->real ? up(16 * (size_t)C) : 0;
+    const size_t need = b_pts + b_out + b_seed + b_part + b_c;
+    if (need > plan->pscratch_bytes) {
+        if (plan->d_pscratch) {
+            cudaFree(plan->d_pscratch);
+            plan->bytes -= (long long)plan->pscratch_bytes;
+            plan->d_pscratch = nullptr;
+            plan->pscratch_bytes = 0;
+        }
+        if ((rc = plan_alloc(plan, &plan->d_pscratch, need))) return rc;
+        plan->pscratch_bytes = need;
+    }
+    char* base = (char*)plan->d_pscratch;
+    double* d_pts = (double*)base;
+    double2* d_out = (double2*)(base + b_pts);
+    void* d_seed = base + b_pts + b_out;
+    double2* d_part = (double2*)(base + b_pts + b_out + b_seed);
+    void* d_c = base + b_pts + b_out + b_seed + b_part;
+    // complex coefficients of the selected function
     const double2* Fc;
     if (plan->real) {
-        if ((e = cudaMalloc(&d_c, 16 * C)) != cudaSuccess) { cleanup(); return cuda_fail(e, "cudaMalloc"); }
         const double* src = (const double*)coeffs + (long long)index * C;
         e = plan->so3 ? launch_so3_r2c(src, d_c, true, L, 1, st) : launch_s2_r2c(src, d_c, true, L, 1, st);
-        if (e != cudaSuccess) { cleanup(); return cuda_fail(e, "real-to-complex coefficients"); }
+        if (e != cudaSuccess) return cuda_fail(e, "real-to-complex coefficients");
         Fc = (const double2*)d_c;
     } else {
         Fc = (const double2*)coeffs + (long long)index * C;
     }
-    if ((e = cudaMalloc(&d_pts, sizeof(double) * dim * n)) != cudaSuccess) { cleanup(); return cuda_fail(e, "cudaMalloc"); }
-    if ((e = cudaMalloc(&d_out, sizeof(double2) * n)) != cudaSuccess) { cleanup(); return cuda_fail(e, "cudaMalloc"); }
-    cudaMemcpyAsync(d_pts, pts, sizeof(double) * dim * n, cudaMemcpyHostToDevice, st);
-    int dev = 0, nsm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if ((e = cudaMemcpyAsync(d_pts, pts, sizeof(double) * dim * n, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return cuda_fail(e, "copy points");
     if (plan->so3) {
-        if (!plan->d_prec) {  // the plan's recursion factors, once
-            const size_t nrec = wigner_rec_elems(L), nsq = wigner_sq_elems(L);
-            if ((rc = plan_alloc(plan, &plan->d_prec, sizeof(double4) * nrec + sizeof(double) * nsq))) {
-                cleanup();
-                return rc;
-            }
-            plan->d_psq = (double*)((double4*)plan->d_prec + nrec);
-            if ((e = launch_wigner_rec_factors((double4*)plan->d_prec, plan->d_psq, L, st)) != cudaSuccess) {
-                cleanup();
-                return cuda_fail(e, "recursion factors");
-            }
-        }
-        int m0b[MAX_POINT_PARTS + 1];
-        const int S = points_parts(true, L, n, nsm, m0b);
         std::vector<WignerSeeds> seeds(n);
         for (int i = 0; i < n; ++i) seeds[i] = make_seeds(pts[3 * i + 1]);
-        if ((e = cudaMalloc(&d_seed, sizeof(WignerSeeds) * n + sizeof(double2) * (size_t)S * n)) != cudaSuccess) {
-            cleanup();
-            return cuda_fail(e, "cudaMalloc");
-        }
-        double2* d_part = (double2*)((char*)d_seed + sizeof(WignerSeeds) * n);
-        cudaMemcpyAsync(d_seed, seeds.data(), sizeof(WignerSeeds) * n, cudaMemcpyHostToDevice, st);
-        e = launch_so3_points(Fc, (const WignerSeeds*)d_seed, (const double*)d_pts, (const double4*)plan->d_prec,
-                              plan->d_psq, plan->d_lfact, L, plan->recursion == FFTSO3_RECURSION_STABLE, n, m0b, S,
-                              d_part, (double2*)d_out, st);
+        e = cudaMemcpyAsync(d_seed, seeds.data(), sizeof(WignerSeeds) * n, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess)
+            e = launch_so3_points(Fc, (const WignerSeeds*)d_seed, d_pts, (const double4*)plan->d_prec, plan->d_psq,
+                                  plan->d_lfact, L, plan->recursion == FFTSO3_RECURSION_STABLE, n, m0b, S, d_part,
+                                  d_out, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // seeds vector must outlive the copy
     } else {
-        if (!plan->d_prec) {  // the plan's Legendre factors, once
-            if ((rc = plan_alloc(plan, &plan->d_prec, sizeof(double2) * legendre_rec_elems(L)))) {
-                cleanup();
-                return rc;
-            }
-            if ((e = launch_legendre_rec_factors((double2*)plan->d_prec, L, st)) != cudaSuccess) {
-                cleanup();
-                return cuda_fail(e, "recursion factors");
-            }
-        }
-        int m0b[MAX_POINT_PARTS + 1];
-        const int S = points_parts(false, L, n, nsm, m0b);
         std::vector<double> xs(n);
         for (int i = 0; i < n; ++i) xs[i] = cos(pts[2 * i]);
-        if ((e = cudaMalloc(&d_seed, sizeof(double) * n + sizeof(double2) * (size_t)S * n + 16)) != cudaSuccess) {
-            cleanup();
-            return cuda_fail(e, "cudaMalloc");
-        }
-        double2* d_part = (double2*)(((uintptr_t)d_seed + sizeof(double) * n + 15) & ~(uintptr_t)15);
-        cudaMemcpyAsync(d_seed, xs.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st);
-        e = launch_s2_points(Fc, (const double*)d_seed, (const double*)d_pts, (const double2*)plan->d_prec, L, n, m0b,
-                             S, d_part, (double2*)d_out, st);
+        e = cudaMemcpyAsync(d_seed, xs.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess)
+            e = launch_s2_points(Fc, (const double*)d_seed, d_pts, (const double2*)plan->d_prec, L, n, m0b, S, d_part,
+                                 d_out, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     }
-    if (e != cudaSuccess) { cleanup(); return cuda_fail(e, "point evaluation"); }
-    std::vector<double> tmp(2 * (size_t)n);
-    e = cudaMemcpy(tmp.data(), d_out, sizeof(double2) * n, cudaMemcpyDeviceToHost);
-    cleanup();
-    if (e != cudaSuccess) return cuda_fail(e, "copy points");
+    if (e != cudaSuccess) return cuda_fail(e, "point evaluation");
     if (plan->real) {
+        std::vector<double> tmp(2 * (size_t)n);
+        if ((e = cudaMemcpy(tmp.data(), d_out, sizeof(double2) * n, cudaMemcpyDeviceToHost)) != cudaSuccess)
+            return cuda_fail(e, "copy points");
         for (int i = 0; i < n; ++i) ((double*)out)[i] = tmp[2 * i];
-    } else {
-        memcpy(out, tmp.data(), sizeof(double2) * n);
+    } else if ((e = cudaMemcpy(out, d_out, sizeof(double2) * n, cudaMemcpyDeviceToHost)) != cudaSuccess) {
+        return cuda_fail(e, "copy points");
     }
     return FFTSO3_SUCCESS;
 }

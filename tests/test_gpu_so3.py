@@ -211,6 +211,8 @@ def test_point_evaluation_partial_warp_many_parts(gblib, oracle, recursion):
     assert rel_err(got, want) < TOL
     one = T.inverse_points(F, pts[5:6])
     assert abs(one[0] - want[5]) < TOL * abs(want[5])
+    more = T.inverse_points(F, np.concatenate([pts, pts[::-1]]))  # a larger call reuses the plan's scratch
+    assert rel_err(more, np.concatenate([want, want[::-1]])) < TOL
 
 
 def test_python_api_example0(gblib):
