@@ -348,11 +348,11 @@ __global__ void sum_parts_kernel(const double2* __restrict__ part, int S, int n,
 }
 
 // Degree parts of about equal work ((2 m0 + 1)(L - m0 + 2) per m0 for SO(3), L - m + 2 per order m for
-// S^2), enough of them that the launch has about 8 warps per SM; returns their number S, bounds in m0b[0..S].
+// S^2), enough of them that the launch has about 16 warps per SM; returns their number S, bounds in m0b[0..S].
 int points_parts(bool so3, int L, int n, int nsm, int* m0b)
 {
     const long long nb = ((long long)n + 31) / 32;
-    long long S = (8LL * std::max(nsm, 1) + nb - 1) / nb;
+    long long S = (16LL * std::max(nsm, 1) + nb - 1) / nb;
     S = std::max(1LL, std::min<long long>({S, (long long)MAX_POINT_PARTS, (long long)L + 1}));
     auto work = [&](int m) { return (so3 ? 2.0 * m + 1.0 : 1.0) * (L - m + 2); };
     double total = 0.;
