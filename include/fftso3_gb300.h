@@ -144,7 +144,9 @@ int fftso3_inverse_host(fftso3_plan* plan, const void* coeffs_host, void* grid_h
  * Replaces inverse_transform(F, alpha, beta, gamma) (fdcl_FFTSO3.cpp:498-531,
  * :1141-1156) and inverse_transform(F, theta, phi) (fdcl_FFTS2.cpp:194-230,
  * :500-512).  Output complex128 (complex kinds) or float64 (real kinds);
- * FP64 arithmetic regardless of the plan precision. */
+ * FP64 arithmetic; needs an FFTSO3_PREC_FP64 plan (FFTSO3_ERR_UNSUPPORTED
+ * otherwise).  The first call allocates the plan's beta-independent
+ * recursion factors and a scratch buffer that later calls reuse. */
 int fftso3_inverse_points(fftso3_plan* plan, const void* coeffs, int index, const double* pts, int n, void* out,
                           void* stream);
 
