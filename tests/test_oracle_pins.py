@@ -45,6 +45,31 @@ def test_so3_weight_identities(oracle):
     assert err < 1e-10
 
 
+def test_s2_weight_identities(oracle):
+    """FFTS2_complex::check_weight (fdcl_FFTS2.cpp:232-283): sum_k w_k Y_l^0(theta_k, 0) B / sqrt(pi)
+    = delta_l0 and sum_{j,k} w_k Y_l^m(theta_k, phi_j) / (2 sqrt(pi)) = delta_l0 delta_m0, for l < 2B."""
+    L = 5
+    B, N = L + 1, 2 * (L + 1)
+    Lc = 2 * B - 1
+    w = oracle.s2_weights(L)
+    theta = [oracle.beta_k(L, k) for k in range(N)]  # theta_k = (2k+1) pi / (4B), the SO(3) beta_k
+    phi = np.array([oracle.alpha_j(L, j) for j in range(N)])  # phi_j = j pi / B
+    s = np.zeros(Lc + 1)
+    delta = np.zeros(oracle.s2_ncoeff(Lc), complex)
+    for k in range(N):
+        nP = oracle.nor_assoc_legendre(np.cos(theta[k]), Lc)
+        for l in range(Lc + 1):
+            s[l] += nP[oracle.s2_index(l, 0)] * w[k]
+            for m in range(-l, l + 1):
+                # Y(l, m) = nP(l, m) e^{i m phi}, nP(l, -m) = (-1)^m nP(l, m) (fdcl_FFTS2.cpp:17-46, :95-97)
+                p = nP[oracle.s2_index(l, abs(m))] * ((-1.0) ** m if m < 0 else 1.0)
+                delta[oracle.s2_index(l, m)] += w[k] * p * np.exp(1j * m * phi).sum()
+    err = abs(s[0] * B / np.sqrt(np.pi) - 1) + np.abs(s[1:] * B / np.sqrt(np.pi)).sum()
+    err += abs(delta[0] / (2 * np.sqrt(np.pi)) - 1) + sum(
+        np.linalg.norm(delta[l * l:(l + 1) ** 2]) / (2 * np.sqrt(np.pi)) for l in range(1, Lc + 1))
+    assert err < 1e-10
+
+
 def test_wigner_d_explicit_and_orthogonal(oracle):
     """check_wigner_d (fdcl_FFTSO3.cpp:315-402): explicit l <= 3 forms, d^T d = I."""
     for beta in [0.0, 0.3, 1.2, 2.9, np.pi, -0.7, -2.2]:
