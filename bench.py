@@ -954,6 +954,24 @@ def main() -> None:
                  "traffic": profiled_traffic(name, L, b)})
     stage_summary = {k: {"ms_per_launch": v / c, "launches": c, "share": v / sum(x for x, _ in stages.values())}
                      for k, (v, c) in stages.items()}
+    # ---- roofline of the whole step: the larger of its HBM floor (algorithmic bytes of every stage) and its
+    # tensor floor (the issued split-BF16 MMA flops), against the measured step time
+    Kp = (N + 63) // 64 * 64
+    table_rows = sum((2 * m + 1) * (B - m) for m in range(B))  # rows l of all symmetry groups
+    table_b = 3 * 2.0 * Kp * table_rows                        # three BF16 planes, read once per GEMM launch
+    coef_b = 8.0 * b * C                                        # complex64 coefficients of the batch
+    step_bytes = (2 * 2 * grid_bytes                            # FFT: two launches, one read + one write each
+                  + 2 * (grid_bytes + table_b + coef_b)         # GEMMs: pencils + table + coefficients
+                  + 2 * 2 * coef_b)                             # coefficient permutations
+    hbm_floor_ms = step_bytes / (peaks["hbm_gbs"] * 1e9) * 1e3
+    tensor_floor_ms = 2 * 6 * useful_flops / (peaks["bf16_tflops_sustained"] * 1e12) * 1e3
+    floor_ms = max(hbm_floor_ms, tensor_floor_ms)
+    step_roof = {"bound": "hbm" if hbm_floor_ms >= tensor_floor_ms else "tensor", "algorithmic_bytes": step_bytes,
+                 "hbm_floor_ms": hbm_floor_ms, "tensor_floor_ms": tensor_floor_ms, "ms_per_step": ms_max,
+                 "frac": floor_ms / ms_max, "peak_source": peaks["source"],
+                 "note": "FFT 4 x grid bytes, GEMMs 2 x (pencils + BF16 table planes + coefficients), permutations "
+                         "4 x coefficients; tensor floor = 6 issued BF16 products of the 8BC useful flops, both "
+                         "directions"}
 
     # ---- end to end through the host-buffer C ABI (pinned host memory)
     e2e = None
@@ -1026,7 +1044,8 @@ def main() -> None:
                                    f"({N}^3 complex64 grid each), TC split-BF16, stable recursion",
                        "l_max": L, "batch_per_gpu": b, "precision": "tc_bf16x3",
                        "l2": "inputs larger than L2 (1 GB grid per function)"},
-            "e2e": e2e, "gpu_launches": launches, "roofline": roof, "stages": stage_summary,
+            "e2e": e2e, "gpu_launches": launches, "roofline": roof, "step_roofline": step_roof,
+            "stages": stage_summary,
             "accuracy": acc, "fp64_path": fp64, "fp32_cuda_core_path": fp32,
             "speedup_vs_fp64_path": (value / world) / fp64["value"] if fp64 else None,
             "clocks": clocks, "cpu_baseline": cpu,
