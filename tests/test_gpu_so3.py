@@ -215,6 +215,24 @@ def test_point_evaluation_partial_warp_many_parts(gblib, oracle, recursion):
     assert rel_err(more, np.concatenate([want, want[::-1]])) < TOL
 
 
+@pytest.mark.parametrize("L", [0, 1, 2])
+def test_point_evaluation_smallest_degrees(gblib, oracle, L):
+    """Point evaluation at l_max = 0, 1, 2 (the special seeds of m0 = 0, 1 and an empty or one-row
+    recursion table), SO(3) and S^2, against the oracle."""
+    import fftso3_gb300 as fg
+    rng = np.random.default_rng(40 + L)
+    pts = np.column_stack([rng.uniform(-np.pi, np.pi, 7), rng.uniform(0.0, np.pi, 7), rng.uniform(-np.pi, np.pi, 7)])
+    F = fg.FFTSO3_matrix_complex(L, data=so3_coeffs(L, 50 + L))
+    got = fg.FFTSO3_complex(L).inverse_points(F, pts)
+    want = np.array([oracle.so3_inverse_complex_point(L, F.M, *p) for p in pts])
+    assert rel_err(got, want) < TOL
+    C2 = (L + 1) ** 2
+    G = fg.FFTS2_matrix_complex(L, data=rng.standard_normal(C2) + 1j * rng.standard_normal(C2))
+    got = fg.FFTS2_complex(L).inverse_points(G, pts[:, 1:])
+    want = np.array([oracle.s2_inverse_complex_point(L, G.M, *p) for p in pts[:, 1:]])
+    assert rel_err(got, want) < TOL
+
+
 def test_python_api_example0(gblib):
     """README example0 through the drop-in API on the GPU: tr R -> F^1 = I/3, f(I) = 3."""
     import fftso3_gb300 as fg
