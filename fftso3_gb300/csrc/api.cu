@@ -642,7 +642,14 @@ int fftso3_inverse_points(fftso3_plan* plan, const void* coeffs, int index, cons
             if ((rc = plan_alloc(plan, &plan->d_prec, sizeof(double2) * legendre_rec_elems(L)))) return rc;
             e = launch_legendre_rec_factors((double2*)plan->d_prec, L, st);
         }
-        if (e != cudaSuccess) return cuda_fail(e, "recursion factors");
+        if (e != cudaSuccess) {  // not built: release it, so a later call builds it again
+            cudaFree(plan->d_prec);
+            plan->bytes -= (long long)(plan->so3 ? sizeof(double4) * wigner_rec_elems(L) + sizeof(double) * wigner_sq_elems(L)
+                                                 : sizeof(double2) * legendre_rec_elems(L));
+            plan->d_prec = nullptr;
+            plan->d_psq = nullptr;
+            return cuda_fail(e, "recursion factors");
+        }
     }
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
