@@ -6,7 +6,9 @@ Euler grid each, complex64 samples; synthetic seeded coefficients
 F ~ N(0,1)(l+1)^-1.5), transformed with the tensor-core split-BF16 path
 (FFTSO3_PREC_TC_BF16X3, stable Wigner-d recursion).  One step = inverse of the
 whole batch (coefficients -> grids) + forward of the whole batch
-(grids -> coefficients); value = functions x world / step time.
+(grids -> coefficients); value = functions / step time.  The library runs
+on one GPU (no sharding, no collectives): launched with more than one rank,
+rank 0 prints a line saying so and no GPU work is done.
 
 Also reported: the plain FP64 GPU path on the same l_max (pairs/s), the
 accuracy of the tensor-core path against FP64, the end-to-end rate through the
@@ -126,18 +128,15 @@ def measured_peaks() -> dict:
 
 
 def profiled_traffic(stage: str, l_max: int, batch: int):
-    """DRAM bytes per launch of `stage` from the committed ncu summary
-    (lines 'traffic <stage> l_max=<L> batch=<b> bytes=<n>'), scaled to this
-    workload: by batch at the same l_max, and for the FFT passes (whose
+    """DRAM bytes per launch of `stage` from the committed ncu capture figures
+    (profiles/traffic.json: stage, l_max, batch, bytes per launch), scaled to
+    this workload: by batch at the same l_max, and for the FFT stages (whose
     traffic is one read and one write of every sample) by batch * N^3 across l_max."""
-    path = os.path.join(ROOT, "profiles", "traffic.md")
+    path = os.path.join(ROOT, "profiles", "traffic.json")
     if not os.path.exists(path):
         return None
-    found = []
-    for line in open(path):
-        m = re.match(r"\s*traffic\s+(\S+)\s+l_max=(\d+)\s+batch=(\d+)\s+bytes=(\d+)", line)
-        if m and m.group(1) == stage:
-            found.append((int(m.group(2)), int(m.group(3)), int(m.group(4))))
+    found = [(r["l_max"], r["batch"], r["bytes_per_launch"]) for r in json.load(open(path))["captures"]
+             if r["stage"] == stage]
     for L0, b0, byts in found:
         if L0 == l_max:
             return byts * batch / b0
@@ -780,8 +779,17 @@ def main() -> None:
     ap.add_argument("--points-kind", default="so3", choices=["so3", "s2"],
                     help="points workload: SO(3) rotations (--points-l-max) or S^2 points (--s2-l-max)")
     args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":
         run_reference(args)
+        return
+    if world > 1 or args.gpus > 1:
+        # one GPU by design: no rank touches a GPU, rank 0 says why
+        if int(os.environ.get("RANK", "0")) == 0:
+            print(json.dumps({"metric": METRIC, "n_gpus": max(world, args.gpus), "impl": "gb300",
+                              "unavailable": "single-GPU library: each transform runs on one GPU with no sharding "
+                                             "or collectives; the headline is measured with --gpus 1"}),
+                  flush=True)
         return
     if args.workload == "uneven":
         main_uneven(args)
@@ -802,18 +810,12 @@ def main() -> None:
     import torch
 
     import fftso3_gb300 as fg
-    from fftso3_gb300 import _lib, shard
+    from fftso3_gb300 import _lib
     from fftso3_gb300 import build as fbuild
 
     fbuild.build()
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl")
+    rank = 0
+    local = 0
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream()
@@ -823,8 +825,6 @@ def main() -> None:
     C = fg.so3_ncoeff(L)
 
     def barrier():
-        if dist is not None:
-            dist.barrier()
         torch.cuda.synchronize()
 
     # ---- FP64 plain path: reference data for the accuracy check + its own rate
@@ -925,8 +925,8 @@ def main() -> None:
     plan.set_timing(False)
     plan.check()
     clocks = clk.summary()
-    ms_max = shard.max_over_ranks(ms)  # whole-job time: the slowest rank
-    value = b * world * 1000.0 / ms_max
+    ms_max = ms
+    value = b * 1000.0 / ms_max
     launches = int(sum(c for _, c in stages.values()))
 
     # ---- roofline of the dominant kernel
@@ -986,13 +986,13 @@ def main() -> None:
         plan.forward_host(hg.data_ptr(), hco.data_ptr(), sp)
         barrier()
         t0 = time.perf_counter()
-        ksteps = max(1, min(args.steps, 3))
+        ksteps = args.steps  # the same step count as the device-timed region
         for _ in range(ksteps):
             plan.inverse_host(hc.data_ptr(), hg.data_ptr(), sp)
             plan.forward_host(hg.data_ptr(), hco.data_ptr(), sp)
         barrier()
-        dt = shard.max_over_ranks((time.perf_counter() - t0) / ksteps)
-        e2e = {"value": b * world / dt, "unit": UNIT, "h2d_bytes_per_step": int(8 * b * C + 8 * b * N ** 3),
+        dt = (time.perf_counter() - t0) / ksteps
+        e2e = {"value": b / dt, "unit": UNIT, "h2d_bytes_per_step": int(8 * b * C + 8 * b * N ** 3),
                "d2h_bytes_per_step": int(8 * b * N ** 3 + 8 * b * C), "steps": ksteps}
         del hg, hc, hco
 
@@ -1016,7 +1016,7 @@ def main() -> None:
         f1.record(stream)
         torch.cuda.synchronize()
         ms32 = f0.elapsed_time(f1)
-        fp32 = {"value": b * world * 1000.0 / ms32, "unit": UNIT, "ms_per_step": ms32,
+        fp32 = {"value": b * 1000.0 / ms32, "unit": UNIT, "ms_per_step": ms32,
                 "note": "FFTSO3_PREC_FP32: FP32 table and FMA accumulation on the CUDA cores, same batch"}
         if not args.no_accuracy:
             pa = _lib.Plan(_lib.SO3_COMPLEX, L, 1, "fp32", "stable")
@@ -1029,15 +1029,46 @@ def main() -> None:
         del p32, g32, c32
         torch.cuda.empty_cache()
 
+    # ---- the refined forward (FFTSO3_FLAG_REFINE: F += forward(f - inverse(F)), inverse and difference in FP64):
+    # inverse + refined forward of a few functions of the batch, pairs/s per function
+    refined = None
+    if not args.no_accuracy:
+        rb = min(b, 4)
+        pr = _lib.Plan(_lib.SO3_COMPLEX, L, rb, "tc_bf16x3", "stable", _lib.FLAG_REFINE)
+        gr = torch.empty(rb * N ** 3, dtype=torch.complex64, device=dev)
+        cr = torch.empty(rb * C, dtype=torch.complex64, device=dev)
+        pr.inverse(coef[:rb * C].data_ptr(), gr.data_ptr(), sp)
+        pr.forward(grid[:rb * N ** 3].data_ptr(), cr.data_ptr(), sp)
+        torch.cuda.synchronize()
+        pr.set_timing(True)
+        pr.stage_times(reset=True)
+        r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        r0.record(stream)
+        pr.inverse(coef[:rb * C].data_ptr(), gr.data_ptr(), sp)
+        pr.forward(grid[:rb * N ** 3].data_ptr(), cr.data_ptr(), sp)
+        r1.record(stream)
+        torch.cuda.synchronize()
+        pr.check()
+        rst = pr.stage_times(reset=True)
+        rms_ = r0.elapsed_time(r1)
+        refined = {"value": rb * 1000.0 / rms_, "unit": UNIT, "batch": rb, "ms_per_step": rms_,
+                   "forward_rel_rms": acc.get("refined_forward_rel_rms"),
+                   "forward_rel_max_per_l": acc.get("refined_forward_rel_max_per_l"),
+                   "stages_ms": {k: v for k, (v, _) in rst.items()},
+                   "note": "tensor-core inverse + refined forward (FFTSO3_FLAG_REFINE: the inverse of the first "
+                           "result and f - inverse(F) in FP64, then the tensor-core forward of the residual)"}
+        del pr, gr, cr
+        torch.cuda.empty_cache()
+
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
+    if not args.no_cpu:
         cpu = cpu_sample(L)
         cpu.pop("seconds", None)
 
     if rank == 0:
         metric = METRIC if L == 255 else METRIC.replace("l_max=255", f"l_max={L}")
         line = {
-            "metric": metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "metric": metric, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "bf16x3 (split) / fp32 accumulate / fp32 FFT", "data": "synthetic",
             "config": {"workload": f"SO(3) complex forward+inverse, l_max={L}, batch={b} functions per GPU "
@@ -1046,13 +1077,11 @@ def main() -> None:
                        "l2": "inputs larger than L2 (1 GB grid per function)"},
             "e2e": e2e, "gpu_launches": launches, "roofline": roof, "step_roofline": step_roof,
             "stages": stage_summary,
-            "accuracy": acc, "fp64_path": fp64, "fp32_cuda_core_path": fp32,
-            "speedup_vs_fp64_path": (value / world) / fp64["value"] if fp64 else None,
+            "accuracy": acc, "refined_path": refined, "fp64_path": fp64, "fp32_cuda_core_path": fp32,
+            "speedup_vs_fp64_path": value / fp64["value"] if fp64 else None,
             "clocks": clocks, "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)
-    if dist is not None:
-        dist.destroy_process_group()
 
 
 if __name__ == "__main__":

@@ -120,6 +120,13 @@ struct fftso3_plan {
     double* d_psq = nullptr;       //   SO(3) Wigner factors + seed factors here, or S^2 Legendre factors)
     void* d_pscratch = nullptr;    // point evaluation scratch (grows with n)
     size_t pscratch_bytes = 0;
+    // residual refinement of FP32-data plans (FFTSO3_FLAG_REFINE): the FP64 table stays, and the FP64 inverse of
+    // the first result runs over chunks of rchunk functions
+    void* d_rw = nullptr;          // FP64 work grid of one chunk (complex128)
+    void* d_rg = nullptr;          // FP64 real grid of one chunk (real kinds)
+    void* d_rc = nullptr;          // FP64 copy of one chunk's coefficients
+    void* d_rfc = nullptr;         // complex FP64 coefficients of one chunk (real kinds)
+    int rchunk = 0;
     long long bytes = 0;
     TCState* tc = nullptr;         // tensor-core contraction state
     StageTimer timer;              // optional per-stage CUDA-event timing
@@ -146,7 +153,8 @@ int plan_alloc(fftso3_plan* p, void** ptr, size_t bytes)
 void plan_free(fftso3_plan* p)
 {
     void* ptrs[] = {p->d_tw, p->d_w, p->d_goff, p->d_table, p->d_lfact, p->d_work, p->d_fc, p->d_io_grid,
-                    p->d_io_coeff, p->d_corr, p->d_amax, p->d_prec, p->d_pscratch};
+                    p->d_io_coeff, p->d_corr, p->d_amax, p->d_prec, p->d_pscratch, p->d_rw, p->d_rg, p->d_rc,
+                    p->d_rfc};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     if (p->tc) tc_destroy(p->tc);
@@ -155,7 +163,8 @@ void plan_free(fftso3_plan* p)
 size_t cbytes(const fftso3_plan* p) { return p->fp64 ? 16 : 8; }  // complex element bytes
 size_t rbytes(const fftso3_plan* p) { return p->fp64 ? 8 : 4; }   // real element bytes
 
-FFTLaunch fft_rows(const fftso3_plan* p, const void* in, void* out, long long nlines, bool real_in, bool real_out)
+FFTLaunch fft_rows(const fftso3_plan* p, const void* in, void* out, long long nlines, bool real_in, bool real_out,
+                   bool fp64)
 {
     FFTLaunch L;
     L.in = in;
@@ -165,14 +174,14 @@ FFTLaunch fft_rows(const fftso3_plan* p, const void* in, void* out, long long nl
     int N = p->N;
     int lpb = 1;
     size_t budget = 200 * 1024;
-    while (lpb < 4 && fft_smem_bytes(N, lpb * 2, p->fp64) <= budget) lpb *= 2;
+    while (lpb < 4 && fft_smem_bytes(N, lpb * 2, fp64) <= budget) lpb *= 2;
     L.lpb = lpb;
     L.inner = 1;
     L.ostride = N;
     L.istride = 0;
     L.es = 1;
     L.tw = p->d_tw;
-    L.fp64 = p->fp64;
+    L.fp64 = fp64;
     L.real_in = real_in;
     L.real_out = real_out;
     L.lines_fastest = false;
@@ -180,7 +189,7 @@ FFTLaunch fft_rows(const fftso3_plan* p, const void* in, void* out, long long nl
 }
 
 // FFT along j1 of [outer][N][N] (lines (outer, j2), element stride N)
-FFTLaunch fft_cols(const fftso3_plan* p, const void* in, void* out, long long nouter, bool real_out)
+FFTLaunch fft_cols(const fftso3_plan* p, const void* in, void* out, long long nouter, bool real_out, bool fp64)
 {
     FFTLaunch L;
     L.in = in;
@@ -189,40 +198,102 @@ FFTLaunch fft_cols(const fftso3_plan* p, const void* in, void* out, long long no
     int N = p->N;
     L.nlines = nouter * N;
     int lpb = 16;
-    while (lpb > 1 && fft_smem_bytes(N, lpb, p->fp64) > 200 * 1024) lpb /= 2;
+    while (lpb > 1 && fft_smem_bytes(N, lpb, fp64) > 200 * 1024) lpb /= 2;
     L.lpb = lpb;
     L.inner = N;
     L.ostride = (long long)N * N;
     L.istride = 1;
     L.es = N;
     L.tw = p->d_tw;
-    L.fp64 = p->fp64;
+    L.fp64 = fp64;
     L.real_in = false;
     L.real_out = real_out;
     L.lines_fastest = true;
     return L;
 }
 
-int run_forward(fftso3_plan* p, const void* grid, void* coeffs, cudaStream_t st)
-{
-    const int N = p->N, L = p->L, b = p->batch;
-    StageTimer& T = p->timer;
-    if (p->tc) return tc_forward(p->tc, grid, coeffs, st, &T, g_err);
 #define STAGE(id, call)      \
     do {                     \
         T.begin(id, st);     \
         CK(call);            \
         T.end(st);           \
     } while (0)
+
+// FP64 inverse of nb functions of the plan's kind: coefficients Fin (complex128, or float64 for the real kinds)
+// -> grid gout (complex128 / float64; may be `work` itself for the complex kinds).  work: nb complex128 grids;
+// fc: nb complex128 coefficient vectors (real kinds).  refine: the launches belong to a refinement step (its
+// stage names) of an FP32-data plan.
+int fp64_inverse(fftso3_plan* p, const void* Fin_, void* gout, int nb, void* work, void* fc, bool refine,
+                 cudaStream_t st)
+{
+    const int N = p->N, L = p->L;
+    StageTimer& T = p->timer;
+    const int s_con = refine ? ST_REF_CONTRACT : ST_FP64_INV;
+    const int s_rows = refine ? ST_REF_FFT : ST_FFT_ROWS, s_cols = refine ? ST_REF_FFT : ST_FFT_COLS;
+    const double2* Fin = (const double2*)Fin_;
     if (p->so3) {
-        STAGE(ST_FFT_ROWS, launch_fft_lines(fft_rows(p, grid, p->d_work, (long long)b * N * N, p->real, false), st));
-        STAGE(ST_FFT_COLS, launch_fft_lines(fft_cols(p, p->d_work, p->d_work, (long long)b * N, false), st));
+        if (p->real) {
+            STAGE(ST_BASIS, launch_so3_r2c(Fin_, fc, true, L, nb, st));
+            Fin = (const double2*)fc;
+        }
+        STAGE(ST_NYQUIST, launch_zero_nyquist_so3(work, true, N, (long long)nb * N, st));
+        STAGE(s_con, launch_so3_inv_fp64(p->d_table, p->d_goff, Fin, (double2*)work, L, N, nb, st));
+        STAGE(s_rows, launch_fft_lines(fft_rows(p, work, work, (long long)nb * N * N, false, false, true), st));
+        STAGE(s_cols, launch_fft_lines(fft_cols(p, work, gout, (long long)nb * N, p->real, true), st));
+    } else {
+        if (p->real) {
+            STAGE(ST_BASIS, launch_s2_r2c(Fin_, fc, true, L, nb, st));
+            Fin = (const double2*)fc;
+        }
+        STAGE(ST_NYQUIST, launch_zero_nyquist_s2(work, true, N, (long long)nb * N, st));
+        STAGE(s_con, launch_s2_inv_fp64(p->d_table, p->d_goff, Fin, (double2*)work, L, N, nb, st));
+        STAGE(s_rows, launch_fft_lines(fft_rows(p, work, gout, (long long)nb * N, false, p->real, true), st));
+    }
+    return FFTSO3_SUCCESS;
+}
+
+// One residual step of an FP32-data plan (FFTSO3_FLAG_REFINE) after its forward wrote F to coeffs:
+//   F += forward(f - inverse(F)),
+// the inverse in FP64 (chunks of rchunk functions) and the difference f - inverse(F) formed in FP64, so the
+// correction carries the errors of the first forward, not those of an FP32 inverse.
+int refine_forward(fftso3_plan* p, const void* grid, void* coeffs, cudaStream_t st)
+{
+    StageTimer& T = p->timer;
+    const long long C = p->coeff_elems, G = p->grid_elems;
+    const int rc_per = p->real ? 1 : 2;  // reals per element
+    float* resid = (float*)tc_resid_buffer(p->tc);
+    for (int f0 = 0; f0 < p->batch; f0 += p->rchunk) {
+        const int nb = p->batch - f0 < p->rchunk ? p->batch - f0 : p->rchunk;
+        STAGE(ST_REFINE, launch_widen((const float*)coeffs + (long long)f0 * C * rc_per, (double*)p->d_rc,
+                                      (long long)nb * C * rc_per, st));
+        void* g64 = p->real ? p->d_rg : p->d_rw;
+        int rc = fp64_inverse(p, p->d_rc, g64, nb, p->d_rw, p->d_rfc, true, st);
+        if (rc) return rc;
+        const long long off = (long long)f0 * G * rc_per;
+        STAGE(ST_REFINE, launch_resid_fp64((const float*)grid + off, (const double*)g64, resid + off,
+                                           (long long)nb * G * rc_per, st));
+    }
+    return tc_refine_add(p->tc, resid, coeffs, st, &T, g_err);
+}
+
+int run_forward(fftso3_plan* p, const void* grid, void* coeffs, cudaStream_t st)
+{
+    const int N = p->N, L = p->L, b = p->batch;
+    StageTimer& T = p->timer;
+    if (p->tc) {
+        int rc = tc_forward(p->tc, grid, coeffs, st, &T, g_err);
+        if (rc || !(p->flags & FFTSO3_FLAG_REFINE)) return rc;
+        return refine_forward(p, grid, coeffs, st);
+    }
+    if (p->so3) {
+        STAGE(ST_FFT_ROWS, launch_fft_lines(fft_rows(p, grid, p->d_work, (long long)b * N * N, p->real, false, true), st));
+        STAGE(ST_FFT_COLS, launch_fft_lines(fft_cols(p, p->d_work, p->d_work, (long long)b * N, false, true), st));
         double2* Fout = p->real ? (double2*)p->d_fc : (double2*)coeffs;
         STAGE(ST_FP64_FWD,
               launch_so3_fwd_fp64(p->d_table, p->d_goff, (const double2*)p->d_work, p->d_w, Fout, L, N, b, st));
         if (p->real) STAGE(ST_BASIS, launch_so3_c2r(p->d_fc, coeffs, true, L, b, st));
     } else {
-        STAGE(ST_FFT_ROWS, launch_fft_lines(fft_rows(p, grid, p->d_work, (long long)b * N, p->real, false), st));
+        STAGE(ST_FFT_ROWS, launch_fft_lines(fft_rows(p, grid, p->d_work, (long long)b * N, p->real, false, true), st));
         double2* Fout = p->real ? (double2*)p->d_fc : (double2*)coeffs;
         STAGE(ST_FP64_FWD, launch_s2_fwd_fp64(p->d_table, p->d_goff, (const double2*)p->d_work, p->d_w, Fout, L, N,
                                               b, p->real, st));
@@ -233,32 +304,10 @@ int run_forward(fftso3_plan* p, const void* grid, void* coeffs, cudaStream_t st)
 
 int run_inverse(fftso3_plan* p, const void* coeffs, void* grid, cudaStream_t st)
 {
-    const int N = p->N, L = p->L, b = p->batch;
-    StageTimer& T = p->timer;
-    if (p->tc) return tc_inverse(p->tc, coeffs, grid, st, &T, g_err);
-    if (p->so3) {
-        const double2* Fin = (const double2*)coeffs;
-        if (p->real) {
-            STAGE(ST_BASIS, launch_so3_r2c(coeffs, p->d_fc, true, L, b, st));
-            Fin = (const double2*)p->d_fc;
-        }
-        STAGE(ST_NYQUIST, launch_zero_nyquist_so3(p->d_work, true, N, (long long)b * N, st));
-        STAGE(ST_FP64_INV, launch_so3_inv_fp64(p->d_table, p->d_goff, Fin, (double2*)p->d_work, L, N, b, st));
-        STAGE(ST_FFT_ROWS, launch_fft_lines(fft_rows(p, p->d_work, p->d_work, (long long)b * N * N, false, false), st));
-        STAGE(ST_FFT_COLS, launch_fft_lines(fft_cols(p, p->d_work, grid, (long long)b * N, p->real), st));
-    } else {
-        const double2* Fin = (const double2*)coeffs;
-        if (p->real) {
-            STAGE(ST_BASIS, launch_s2_r2c(coeffs, p->d_fc, true, L, b, st));
-            Fin = (const double2*)p->d_fc;
-        }
-        STAGE(ST_NYQUIST, launch_zero_nyquist_s2(p->d_work, true, N, (long long)b * N, st));
-        STAGE(ST_FP64_INV, launch_s2_inv_fp64(p->d_table, p->d_goff, Fin, (double2*)p->d_work, L, N, b, st));
-        STAGE(ST_FFT_ROWS, launch_fft_lines(fft_rows(p, p->d_work, grid, (long long)b * N, false, p->real), st));
-    }
-#undef STAGE
-    return FFTSO3_SUCCESS;
+    if (p->tc) return tc_inverse(p->tc, coeffs, grid, st, &p->timer, g_err);
+    return fp64_inverse(p, coeffs, grid, p->batch, p->d_work, p->d_fc, false, st);
 }
+#undef STAGE
 
 int check_plan(const fftso3_plan* p)
 {
@@ -434,10 +483,26 @@ int fftso3_plan_create(fftso3_plan** out, int kind, int l_max, int batch, int pr
             return bail(rc);
         }
         p->bytes += tc_device_bytes(p->tc);
-        // the FP32-data paths keep only their BF16 planes / FP32 copy of the table
-        cudaFree(p->d_table);
-        p->d_table = nullptr;
-        p->bytes -= (long long)sizeof(double) * p->table_elems;
+        if (flags & FFTSO3_FLAG_REFINE) {
+            // the refinement's FP64 inverse keeps the FP64 table; its buffers hold one chunk of functions, the
+            // chunk sized to about 4 GB of FP64 work grid
+            const size_t g16 = 16 * (size_t)p->grid_elems;
+            size_t nch = (size_t)4 << 30;
+            nch = nch / g16 < 1 ? 1 : nch / g16;
+            p->rchunk = (int)(nch < (size_t)batch ? nch : (size_t)batch);
+            const size_t nb = (size_t)p->rchunk;
+            if ((rc = plan_alloc(p, &p->d_rw, g16 * nb))) return bail(rc);
+            if ((rc = plan_alloc(p, &p->d_rc, (p->real ? 8 : 16) * (size_t)p->coeff_elems * nb))) return bail(rc);
+            if (p->real) {
+                if ((rc = plan_alloc(p, &p->d_rg, 8 * (size_t)p->grid_elems * nb))) return bail(rc);
+                if ((rc = plan_alloc(p, &p->d_rfc, 16 * (size_t)p->coeff_elems * nb))) return bail(rc);
+            }
+        } else {
+            // the FP32-data paths keep only their BF16 planes / FP32 copy of the table
+            cudaFree(p->d_table);
+            p->d_table = nullptr;
+            p->bytes -= (long long)sizeof(double) * p->table_elems;
+        }
     }
     *out = p;
     return FFTSO3_SUCCESS;

@@ -33,4 +33,10 @@ size_t argmax_scratch_bytes(int nb, int chunks);
 cudaError_t launch_argmax(const void* x, bool fp64, long long n, int nb, int chunks, void* scratch, double* ov,
                           long long* oi, cudaStream_t st);
 
+// residual refinement of the FP32-data plans: FP32 -> FP64 copy; r = f - g (FP64 difference rounded to FP32);
+// F += d.  n counts real elements (twice the complex count for interleaved complex data).
+cudaError_t launch_widen(const float* in, double* out, long long n, cudaStream_t st);
+cudaError_t launch_resid_fp64(const float* f, const double* g, float* r, long long n, cudaStream_t st);
+cudaError_t launch_add_real(float* F, const float* d, long long n, cudaStream_t st);
+
 }  // namespace fftso3

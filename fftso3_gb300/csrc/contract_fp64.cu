@@ -657,4 +657,49 @@ cudaError_t launch_s2_r2c(const void* Fr, void* Fc, bool fp64, int L, int batch,
     return cudaGetLastError();
 }
 
+// ---- residual refinement of the FP32-data plans (F += forward(f - inverse(F)), the inverse in FP64)
+
+__global__ void widen_kernel(const float* __restrict__ in, double* __restrict__ out, long long n)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (double)in[i];
+}
+
+// r = f - g with f the FP32 samples the forward transformed and g the FP64
+// synthesis of its first result: the subtraction is done in FP64 (f is exact
+// there), only the small difference is rounded to FP32.
+__global__ void resid_fp64_kernel(const float* __restrict__ f, const double* __restrict__ g, float* __restrict__ r,
+                                  long long n)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) r[i] = (float)((double)f[i] - g[i]);
+}
+
+__global__ void add_real_kernel(float* __restrict__ F, const float* __restrict__ d, long long n)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) F[i] += d[i];
+}
+
+cudaError_t launch_widen(const float* in, double* out, long long n, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    widen_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, out, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_resid_fp64(const float* f, const double* g, float* r, long long n, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    resid_fp64_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(f, g, r, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_add_real(float* F, const float* d, long long n, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    add_real_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(F, d, n);
+    return cudaGetLastError();
+}
+
 }  // namespace fftso3

@@ -1208,29 +1208,6 @@ __global__ void s2_zero_nyquist_pencils_kernel(float2* __restrict__ H, int N, lo
     H[f * (long long)N * N + (long long)(N / 2) * N + k] = make_float2(0.f, 0.f);
 }
 
-__global__ void resid_kernel(const float2* __restrict__ f, float2* __restrict__ r, long long n)
-{
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float2 a = f[i], b = r[i];
-    r[i] = make_float2(a.x - b.x, a.y - b.y);
-}
-
-__global__ void resid_real_kernel(const float* __restrict__ f, float* __restrict__ r, long long n)
-{
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    r[i] = f[i] - r[i];
-}
-
-__global__ void add_kernel(float2* __restrict__ F, const float2* __restrict__ d, long long n)
-{
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float2 a = F[i], b = d[i];
-    F[i] = make_float2(a.x + b.x, a.y + b.y);
-}
-
 }  // namespace tc
 
 // --------------------------------------------------------------- host side
@@ -1921,30 +1898,12 @@ static int tc_inverse_once(TCState* s, const float2* F, void* grid, cudaStream_t
 int tc_forward(TCState* s, const void* grid, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err)
 {
     // real kinds: complex coefficients in d_fc, then the real basis
-    // (fdcl_FFTSO3.cpp:1169-1181, fdcl_FFTS2.cpp:424-436)
-    if (s->real && s->s2 && !s->refine) return tc_forward_once(s, grid, nullptr, st, T, err, coeffs);
+    // (fdcl_FFTSO3.cpp:1169-1181, fdcl_FFTS2.cpp:424-436); the S^2 real kinds
+    // write the real coefficients straight from the GEMM output
+    if (s->real && s->s2) return tc_forward_once(s, grid, nullptr, st, T, err, coeffs);
     float2* Fc = s->real ? s->d_fc : (float2*)coeffs;
     int rc = tc_forward_once(s, grid, Fc, st, T, err);
     if (rc) return rc;
-    if (s->refine) {
-        // one residual step: F += forward(f - inverse(F))
-        const long long ng = (long long)s->batch * grid_per_fn(s);
-        const long long nc = (long long)s->batch * coeffs_per_fn(s);
-        if ((rc = tc_inverse_once(s, Fc, s->d_resid, st, T, err))) return rc;
-        T->begin(ST_REFINE, st);
-        if (s->real)
-            resid_real_kernel<<<(unsigned)((ng + 255) / 256), 256, 0, st>>>((const float*)grid, (float*)s->d_resid,
-                                                                            ng);
-        else
-            resid_kernel<<<(unsigned)((ng + 255) / 256), 256, 0, st>>>((const float2*)grid, s->d_resid, ng);
-        TCK(cudaGetLastError());
-        T->end(st);
-        if ((rc = tc_forward_once(s, s->d_resid, s->d_coef2, st, T, err))) return rc;
-        T->begin(ST_REFINE, st);
-        add_kernel<<<(unsigned)((nc + 255) / 256), 256, 0, st>>>(Fc, s->d_coef2, nc);
-        TCK(cudaGetLastError());
-        T->end(st);
-    }
     if (s->real) {
         T->begin(ST_BASIS, st);
         if (s->s2)
@@ -1953,6 +1912,41 @@ int tc_forward(TCState* s, const void* grid, void* coeffs, cudaStream_t st, Stag
             TCK(launch_so3_c2r(Fc, coeffs, false, s->L, s->batch, st));
         T->end(st);
     }
+    return FFTSO3_SUCCESS;
+}
+
+void* tc_resid_buffer(TCState* s) { return s ? (void*)s->d_resid : nullptr; }
+
+int tc_refine_add(TCState* s, const void* resid, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err)
+{
+    if (!s->refine || !s->d_coef2) {
+        err = "internal: refinement buffers were not allocated";
+        return FFTSO3_ERR_CUDA;
+    }
+    const long long nc = (long long)s->batch * coeffs_per_fn(s);
+    int rc;
+    float* corr;  // the correction in the coefficients' own element type
+    if (s->real && s->s2) {
+        rc = tc_forward_once(s, resid, nullptr, st, T, err, s->d_coef2);
+        corr = (float*)s->d_coef2;
+    } else {
+        rc = tc_forward_once(s, resid, s->d_coef2, st, T, err);
+        corr = (float*)s->d_coef2;
+        if (!rc && s->real) {
+            // real basis of the correction, into the (complex-sized) scratch d_fc
+            T->begin(ST_BASIS, st);
+            if (s->s2)
+                TCK(launch_s2_c2r(s->d_coef2, s->d_fc, false, s->L, s->batch, st));
+            else
+                TCK(launch_so3_c2r(s->d_coef2, s->d_fc, false, s->L, s->batch, st));
+            T->end(st);
+            corr = (float*)s->d_fc;
+        }
+    }
+    if (rc) return rc;
+    T->begin(ST_REFINE, st);
+    TCK(launch_add_real((float*)coeffs, corr, s->real ? nc : 2 * nc, st));
+    T->end(st);
     return FFTSO3_SUCCESS;
 }
 

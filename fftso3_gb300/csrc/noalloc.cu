@@ -14,8 +14,17 @@
 // would synchronise the device or take the allocator's lock.
 //
 // Set-up: the first call on a device looks up the array's device address with
-// cudaGetSymbolAddress (with that device current) and caches it; make that
-// first call before any stream capture.  Every call shares the one array and
+// cudaGetSymbolAddress (with that device current) and caches it for the life of
+// the process, for device ordinals 0..255 (a higher ordinal is rejected); make
+// that first call before any stream capture.  cudaDeviceReset() on a device
+// destroys its copy of the array, so the cached address is then stale: do not
+// call this entry point on a device after resetting it.
+//
+// The host-computed constants (twiddles, weights, group offsets, recursion
+// seeds: about 15 KB) reach the GPU as one __grid_constant__ kernel parameter,
+// which needs the large kernel parameters of CUDA 12.1 and later (up to 32,764
+// bytes; checked at compile time below) -- no host-to-device copy, so nothing
+// to allocate or pin.  Every call shares the one array and
 // each call rewrites all of it before reading it (nothing has to start at
 // zero), so two calls that overlap on the GPU -- on different streams, or from
 // different host threads -- race and corrupt each other's result: serialise
@@ -72,6 +81,7 @@ struct NAParams {
     long long goff[NA_B * NA_B + 1];
     WignerSeeds seeds[NA_N];
 };
+static_assert(sizeof(NAParams) <= 32764, "NAParams must fit CUDA's 32,764-byte kernel parameter limit");
 
 __global__ void na_setup_kernel(const __grid_constant__ NAParams P, unsigned char* __restrict__ scratch, int L)
 {

@@ -19,11 +19,15 @@ void tc_destroy(TCState* s);
 long long tc_device_bytes(const TCState* s);
 int tc_forward(TCState* s, const void* grid, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err);
 int tc_inverse(TCState* s, const void* coeffs, void* grid, cudaStream_t st, StageTimer* T, std::string& err);
+// Residual refinement (plans created with refine = true): the plan's residual grid buffer (batch grids of the
+// plan's sample type), and coeffs += forward(resid) in the coefficients' element type.
+void* tc_resid_buffer(TCState* s);
+int tc_refine_add(TCState* s, const void* resid, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err);
 // Device error word of the tensor-core kernels (0 = no bounded wait timed out); synchronising read.
 int tc_status(TCState* s);
 
 // Phases of one direction, so that several plans can share one GEMM launch:
-//   forward = tc_forward_fft, GEMM, tc_forward_finish (no refinement);
+//   forward = tc_forward_fft, GEMM, tc_forward_finish;
 //   inverse = tc_inverse_prepare, GEMM, tc_inverse_fft.
 int tc_forward_fft(TCState* s, const void* grid, cudaStream_t st, StageTimer* T, std::string& err);
 int tc_forward_finish(TCState* s, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err);

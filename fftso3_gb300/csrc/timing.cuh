@@ -18,6 +18,8 @@ enum Stage {
     ST_GEMM_INV,
     ST_REFINE,
     ST_FFT_2D,
+    ST_REF_CONTRACT,
+    ST_REF_FFT,
     ST_COUNT
 };
 
@@ -25,7 +27,8 @@ inline const char* stage_name(int s)
 {
     static const char* names[ST_COUNT] = {"fft_rows", "fft_cols", "zero_nyquist", "fp64_fwd_contract",
                                           "fp64_inv_contract", "basis_convert", "tc_pack_fwd", "tc_gemm_fwd",
-                                          "tc_pack_inv", "tc_gemm_inv", "tc_refine_elementwise", "fft_2d"};
+                                          "tc_pack_inv", "tc_gemm_inv", "tc_refine_elementwise", "fft_2d",
+                                          "refine_inverse_contract", "refine_inverse_fft"};
     return (s >= 0 && s < ST_COUNT) ? names[s] : "";
 }
 

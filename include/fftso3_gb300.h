@@ -62,7 +62,9 @@ extern "C" {
 #define FFTSO3_RECURSION_STABLE 1    /* log-domain seeds + extended-exponent recursion */
 
 /* plan flags */
-#define FFTSO3_FLAG_REFINE 0x1u /* tensor-core forward: one residual step F += forward(f - inverse(F)) */
+#define FFTSO3_FLAG_REFINE 0x1u /* FP32-data forward: one residual step F += forward(f - inverse(F)); the
+                                   inverse of F and the difference f - inverse(F) are formed in FP64, so the
+                                   correction removes the first forward's FP32 FFT and contraction errors */
 #define FFTSO3_FLAG_GRAPH 0x2u  /* batches: capture each direction into a CUDA graph, replay it */
 #define FFTSO3_FLAG_AUTOTUNE 0x4u /* tensor-core plans: time the launch shapes of the generic-N FFT passes on
                                      the plan's workspace at creation and keep the fastest (cached per N for
@@ -91,7 +93,15 @@ int fftso3_weights(int kind, int l_max, double* weights_out);
  * device.  Replaces the constructor / init(l_max) of the reference classes
  * (fdcl_FFTSO3.cpp:3-14, :1000-1008, fdcl_FFTS2.cpp:3-15, :371-381); the plan
  * owns the Wigner-d (SO(3)) or Legendre (S^2) tables, twiddles and workspace.
- * precision: FFTSO3_PREC_*; recursion: FFTSO3_RECURSION_* (SO(3) only). */
+ * precision: FFTSO3_PREC_*; recursion: FFTSO3_RECURSION_* (SO(3) only).
+ * Threads: a plan is not re-entrant (nor are the reference objects, whose
+ * init() and weights mutate members).  Calls on one plan share its workspace,
+ * and fftso3_inverse_points may free and regrow the plan's point scratch, so
+ * two host threads must not use one plan at the same time: give each thread
+ * its own plan, or serialise the calls.  Different plans are independent.
+ * With FFTSO3_FLAG_REFINE (FP32-data precisions) the plan also keeps the FP64
+ * table and FP64 work buffers for one chunk of functions (about 4 GB of work
+ * grid) for the refinement's FP64 inverse. */
 int fftso3_plan_create(fftso3_plan** plan, int kind, int l_max, int batch, int precision, int recursion,
                        unsigned flags);
 int fftso3_plan_destroy(fftso3_plan* plan);

@@ -1,0 +1,106 @@
+"""Wigner-d ground truth at l_max = 255: mpmath values d^l_mn(beta_k) (tests/golden/
+wigner_mpmath_lmax255.json, made by make_wigner_mpmath.py) against the oracle (CPU) and
+against the library's stable recursion (GPU).
+
+The fixture holds 240 samples on the l_max = 255 grid, 134 of them within 8 grid steps
+of beta = pi and most with l > 128: the region where the reference recursion
+(fdcl_FFTSO3.cpp:127-194) underflows and the stable recursion must still be right.
+Tolerance for the stable recursion: |d_gpu - d| <= 1e-12 for every sample (|d| <= 1)
+and |d_gpu - d| <= 1e-11 |d| wherever |d| >= 1e-6.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+FIXTURE = os.path.join(HERE, "golden", "wigner_mpmath_lmax255.json")
+L = 255
+N = 2 * (L + 1)
+
+
+def _samples():
+    with open(FIXTURE) as fh:
+        return json.load(fh)["samples"]
+
+
+def test_fixture_covers_the_underflow_region():
+    s = _samples()
+    assert len(s) >= 200
+    near_pi_high_l = [r for r in s if r["k"] >= N - 8 and r["l"] > 128]
+    assert len(near_pi_high_l) >= 120
+    assert sum(1 for r in near_pi_high_l if abs(r["value"]) > 1e-2) >= 30  # O(1) values, not only tiny ones
+    assert all(abs(r["m"]) <= r["l"] and abs(r["n"]) <= r["l"] and 0 <= r["k"] < N for r in s)
+
+
+def test_oracle_reference_recursion_agrees_where_it_is_accurate(oracle):
+    """Away from beta = pi (and at every beta for l <= 64) the reference recursion is accurate, and
+    there it equals the fixture to 1e-12: this pins the fixture's sign convention and values to the
+    reference's own d^l_mn."""
+    cache = {}
+    n_checked = 0
+    for r in _samples():
+        if r["k"] >= N - 8 and r["l"] > 64:
+            continue
+        k = r["k"]
+        if k not in cache:
+            cache[k] = oracle.wigner_d(oracle.beta_k(L, k), L)
+        got = cache[k][oracle.so3_index(r["l"], r["m"], r["n"])]
+        assert abs(got - r["value"]) <= 1e-12, r
+        n_checked += 1
+    assert n_checked >= 100
+
+
+def test_oracle_reference_recursion_underflows_near_pi(oracle):
+    """The documented failure the stable recursion exists for: near beta = pi and l > 128 the
+    reference returns 0 for values of order 0.1."""
+    bad = 0
+    cache = {}
+    for r in _samples():
+        if r["k"] < N - 8 or r["l"] <= 128 or abs(r["value"]) < 1e-2:
+            continue
+        k = r["k"]
+        if k not in cache:
+            cache[k] = oracle.wigner_d(oracle.beta_k(L, k), L)
+        got = cache[k][oracle.so3_index(r["l"], r["m"], r["n"])]
+        bad += abs(got - r["value"]) > 1e-3
+    assert bad >= 20
+
+
+def test_fixture_values_recompute_with_mpmath():
+    mp = pytest.importorskip("mpmath")
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("mkw", os.path.join(HERE, "golden", "make_wigner_mpmath.py"))
+    mkw = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mkw)
+    s = _samples()
+    for r in s[::30]:
+        v = mkw.wigner_d_exact(r["l"], r["m"], r["n"], r["k"], 240)
+        assert float(v) == pytest.approx(r["value"], rel=1e-14, abs=1e-300)
+        with mp.workdps(40):
+            assert abs(v - mp.mpf(r["digits"])) <= abs(v) * mp.mpf(10) ** -28
+
+
+@pytest.mark.gpu
+def test_stable_recursion_matches_mpmath(gblib):
+    """fftso3_wigner_d(beta_k, l, FFTSO3_RECURSION_STABLE) at every fixture sample."""
+    by_k = {}
+    for r in _samples():
+        by_k.setdefault(r["k"], []).append(r)
+    worst_abs = worst_rel = 0.0
+    for k, rows in by_k.items():
+        beta = (2 * k + 1) * np.pi / (4 * (L + 1))
+        lm = max(r["l"] for r in rows)
+        d = np.zeros((lm + 1) * (4 * (lm + 1) ** 2 - 1) // 3)
+        gblib.check(gblib.lib().fftso3_wigner_d(float(beta), lm, gblib.RECURSION_STABLE, d.ctypes.data_as(gblib._dp)))
+        for r in rows:
+            l, m, n = r["l"], r["m"], r["n"]
+            got = d[l * (4 * l * l - 1) // 3 + (m + l) + (n + l) * (2 * l + 1)]
+            err = abs(got - r["value"])
+            worst_abs = max(worst_abs, err)
+            assert err <= 1e-12, (r, got)
+            if abs(r["value"]) >= 1e-6:
+                worst_rel = max(worst_rel, err / abs(r["value"]))
+                assert err <= 1e-11 * abs(r["value"]), (r, got)
+    print(f"stable recursion vs mpmath: max abs err {worst_abs:.3e}, max rel err (|d| >= 1e-6) {worst_rel:.3e}")

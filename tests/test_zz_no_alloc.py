@@ -57,6 +57,28 @@ def test_noalloc_forward_matches_plan_forward_twice(gblib, torch_cuda, L):
         assert rel_err(got, want) < TOL
 
 
+@pytest.mark.parametrize("L", [5, 31])
+def test_noalloc_forward_matches_oracle_twice(gblib, oracle, torch_cuda, L):
+    """Independent data and an independent check: the grid is the oracle's FP64 synthesis of seeded
+    coefficients and the expected coefficients are the oracle's forward of that grid (the reference
+    algorithm restated on the CPU), not the plan path's."""
+    torch = torch_cuda
+    F = so3_coeffs(L, seed=700 + L)
+    g_ref = oracle.so3_inverse_complex_grid(L, F)
+    want = oracle.so3_forward_complex(L, g_ref)
+    s = torch.cuda.current_stream().cuda_stream
+    grid = torch.from_numpy(np.ascontiguousarray(g_ref).ravel()).cuda()
+    lib = gblib.lib()
+    for _ in range(2):
+        out = torch.full((want.size,), float("nan"), dtype=torch.complex128, device="cuda")
+        gblib.check(lib.fftso3_forward_noalloc(L, ctypes.c_void_p(grid.data_ptr()),
+                                               ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(s)))
+        torch.cuda.synchronize()
+        got = out.cpu().numpy()
+        assert np.isfinite(got).all()
+        assert rel_err(got, want) < TOL
+
+
 def test_noalloc_rejects_sizes_above_its_limit(gblib, torch_cuda):
     lib = gblib.lib()
     rc = lib.fftso3_forward_noalloc(32, ctypes.c_void_p(16), ctypes.c_void_p(16), None)
