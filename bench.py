@@ -1033,7 +1033,7 @@ def main() -> None:
     # inverse + refined forward of a few functions of the batch, pairs/s per function
     refined = None
     if not args.no_accuracy:
-        rb = min(b, 4)
+        rb = min(b, 8)
         pr = _lib.Plan(_lib.SO3_COMPLEX, L, rb, "tc_bf16x3", "stable", _lib.FLAG_REFINE)
         gr = torch.empty(rb * N ** 3, dtype=torch.complex64, device=dev)
         cr = torch.empty(rb * C, dtype=torch.complex64, device=dev)
@@ -1056,7 +1056,8 @@ def main() -> None:
                    "forward_rel_max_per_l": acc.get("refined_forward_rel_max_per_l"),
                    "stages_ms": {k: v for k, (v, _) in rst.items()},
                    "note": "tensor-core inverse + refined forward (FFTSO3_FLAG_REFINE: the inverse of the first "
-                           "result and f - inverse(F) in FP64, then the tensor-core forward of the residual)"}
+                           "result exactly on the tensor cores (BF16 digit products summed without rounding) and "
+                           "f - inverse(F) in double-float, then the tensor-core forward of the residual)"}
         del pr, gr, cr
         torch.cuda.empty_cache()
 

@@ -14,6 +14,7 @@
 #include "common.cuh"
 #include "contract.cuh"
 #include "fft.cuh"
+#include "refine_oz.cuh"
 #include "tables.cuh"
 #include "tc.cuh"
 #include "timing.cuh"
@@ -127,6 +128,7 @@ struct fftso3_plan {
     void* d_rc = nullptr;          // FP64 copy of one chunk's coefficients
     void* d_rfc = nullptr;         // complex FP64 coefficients of one chunk (real kinds)
     int rchunk = 0;
+    OZState* oz = nullptr;         // SO(3), l_max <= 255: the refinement's inverse on the tensor cores, exactly
     long long bytes = 0;
     TCState* tc = nullptr;         // tensor-core contraction state
     StageTimer timer;              // optional per-stage CUDA-event timing
@@ -158,6 +160,7 @@ void plan_free(fftso3_plan* p)
     for (void* q : ptrs)
         if (q) cudaFree(q);
     if (p->tc) tc_destroy(p->tc);
+    if (p->oz) oz_destroy(p->oz);
 }
 
 size_t cbytes(const fftso3_plan* p) { return p->fp64 ? 16 : 8; }  // complex element bytes
@@ -262,6 +265,24 @@ int refine_forward(fftso3_plan* p, const void* grid, void* coeffs, cudaStream_t 
     const long long C = p->coeff_elems, G = p->grid_elems;
     const int rc_per = p->real ? 1 : 2;  // reals per element
     float* resid = (float*)tc_resid_buffer(p->tc);
+    if (p->oz) {
+        // SO(3): the inverse on the tensor cores with exact digit sums, double-float FFT and residual
+        for (int f0 = 0; f0 < p->batch; f0 += p->rchunk) {
+            const int nb = p->batch - f0 < p->rchunk ? p->batch - f0 : p->rchunk;
+            const void* Fc = (const float2*)coeffs + (long long)f0 * C;
+            if (p->real) {
+                STAGE(ST_REFINE, launch_widen((const float*)coeffs + (long long)f0 * C, (double*)p->d_rc,
+                                              (long long)nb * C, st));
+                STAGE(ST_BASIS, launch_so3_r2c(p->d_rc, p->d_rfc, true, p->L, nb, st));
+                Fc = p->d_rfc;
+            }
+            const long long off = (long long)f0 * G * rc_per;
+            int rc = oz_inverse_resid(p->oz, Fc, p->real, nb, (const float*)grid + off, p->real, resid + off, st, &T,
+                                      g_err);
+            if (rc) return rc;
+        }
+        return tc_refine_add(p->tc, resid, coeffs, st, &T, g_err);
+    }
     for (int f0 = 0; f0 < p->batch; f0 += p->rchunk) {
         const int nb = p->batch - f0 < p->rchunk ? p->batch - f0 : p->rchunk;
         STAGE(ST_REFINE, launch_widen((const float*)coeffs + (long long)f0 * C * rc_per, (double*)p->d_rc,
@@ -483,7 +504,30 @@ int fftso3_plan_create(fftso3_plan** out, int kind, int l_max, int batch, int pr
             return bail(rc);
         }
         p->bytes += tc_device_bytes(p->tc);
-        if (flags & FFTSO3_FLAG_REFINE) {
+        const char* ev_ref = getenv("FFTSO3_REFINE_FP64");
+        const bool use_oz = (flags & FFTSO3_FLAG_REFINE) && p->so3 && oz_supported(L, N) && !(ev_ref && ev_ref[0] == '1');
+        if (use_oz) {
+            // SO(3) refinement on the tensor cores: digit planes of the FP64 table, then the table is freed;
+            // chunks of up to 8 functions (one column tile), bounded to ~20 GB of double-float pencils
+            const size_t g16 = 16 * (size_t)p->grid_elems;
+            size_t nch = ((size_t)20 << 30) / g16;
+            nch = nch < 1 ? 1 : (nch > 8 ? 8 : nch);
+            p->rchunk = (int)(nch < (size_t)batch ? nch : (size_t)batch);
+            std::string err;
+            if ((rc = oz_create(&p->oz, p->d_table, goff, L, N, p->rchunk, p->d_tw, err))) {
+                g_err = err;
+                return bail(rc);
+            }
+            p->bytes += oz_device_bytes(p->oz);
+            if (p->real) {
+                const size_t nb = (size_t)p->rchunk;
+                if ((rc = plan_alloc(p, &p->d_rc, 8 * (size_t)p->coeff_elems * nb))) return bail(rc);
+                if ((rc = plan_alloc(p, &p->d_rfc, 16 * (size_t)p->coeff_elems * nb))) return bail(rc);
+            }
+            cudaFree(p->d_table);
+            p->d_table = nullptr;
+            p->bytes -= (long long)sizeof(double) * p->table_elems;
+        } else if (flags & FFTSO3_FLAG_REFINE) {
             // the refinement's FP64 inverse keeps the FP64 table; its buffers hold one chunk of functions, the
             // chunk sized to about 4 GB of FP64 work grid
             const size_t g16 = 16 * (size_t)p->grid_elems;
@@ -556,6 +600,7 @@ int fftso3_plan_check(fftso3_plan* plan)
     if (e != cudaSuccess) return cuda_fail(e, "device synchronize");
     if (plan->tc) {
         int code = tc_status(plan->tc);
+        if (code == 0 && plan->oz) code = oz_status(plan->oz);
         if (code != 0)
             return fail(FFTSO3_ERR_CUDA, "a tensor-core kernel gave up a bounded wait (code " + std::to_string(code) + ")");
     }

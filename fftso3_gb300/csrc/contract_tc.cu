@@ -45,10 +45,13 @@
 #include "common.cuh"
 #include "contract.cuh"
 #include "tc.cuh"
+#include "tc_ptx.cuh"
 
 namespace fftso3 {
 
 namespace tc {
+
+using namespace ptx;
 
 constexpr int BM = 128;          // MMA M (rows of the accumulator = TMEM lanes)
 constexpr int BN = 128;          // MMA N (accumulator columns = 16 functions x 4 pairs x re/im)
@@ -70,112 +73,16 @@ constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 256 /*barriers*/ + 4 * MAXN /*
 // separate 128-column halves, so the small terms are never rounded against
 // the large running sum.
 constexpr int TMEM_COLS = 512;
-constexpr long long WAIT_CYCLES = 2000000000LL;  // ~1 s at 2 GHz
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
-{
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// Bounded wait: false (and an error code in *err) after ~1 s.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code)
-{
-    if (mbar_try_wait(bar, parity)) return true;
-    long long t0 = clock64();
-    while (!mbar_try_wait(bar, parity)) {
-        if (clock64() - t0 > WAIT_CYCLES) {
-            atomicCAS(err, 0, code);
-            return false;
-        }
-    }
-    return true;
-}
-
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int x, int y, uint64_t* bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-            smem_u32(dst)),
-        "l"((uint64_t)tm), "r"(x), "r"(y), "r"(smem_u32(bar))
-        : "memory");
-}
 
 // k-steps of table tiles the forward GEMM prefetches into L2 ahead of its TMA ring.
 #ifndef FFTSO3_GEMM_PF
 #define FFTSO3_GEMM_PF 3
 #endif
 
-// The same box delivered to the same shared-memory offset of every CTA of the
-// cluster in ctaMask, each CTA's barrier at that offset receiving the bytes.
-__device__ __forceinline__ void tma_load_2d_mc(void* dst, const CUtensorMap* tm, int x, int y, uint64_t* bar,
-                                               uint16_t mask)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster"
-        " [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(smem_u32(dst)),
-        "l"((uint64_t)tm), "r"(x), "r"(y), "r"(smem_u32(bar)), "h"(mask)
-        : "memory");
-}
-
-__device__ __forceinline__ uint32_t cluster_rank()
-{
-    uint32_t r;
-    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-    return r;
-}
-
-// All threads of every CTA of the cluster.
-__device__ __forceinline__ void cluster_sync()
-{
-    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
-    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
-
-// L2 prefetch of the same box (no shared memory, no completion to wait for).
-__device__ __forceinline__ void tma_prefetch_2d(const CUtensorMap* tm, int x, int y)
-{
-    asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global.tile [%0, {%1, %2}];" ::"l"((uint64_t)tm), "r"(x), "r"(y)
-                 : "memory");
-}
-
-// UMMA shared-memory descriptor, 128-byte swizzle (SM100 layout code 2, version 1).
-__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
-{
-    uint64_t d = 0;
-    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
-    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
-    d |= (uint64_t)1 << 46;
-    d |= (uint64_t)2 << 61;
-    return d;
-}
-
-// Instruction descriptor, kind::f16: D = F32, A = B = BF16, M = m (128 or 64), N = n (128 or 256).
+// Instruction descriptor of this kernel's tiles (M = m, N = n; defaults BM x BN).
 __host__ __device__ constexpr uint32_t idesc_bf16(bool a_mn_major, int n = BN, int m = BM)
 {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((a_mn_major ? 1u : 0u) << 15) | ((uint32_t)(n >> 3) << 17) |
-           ((uint32_t)(m >> 4) << 24);
+    return idesc_bf16_mn(a_mn_major, n, m);
 }
 
 // 1: a forward row tile with at most 64 valid rows (degrees) issues M = 64 MMAs
@@ -192,48 +99,6 @@ __host__ __device__ constexpr uint32_t idesc_bf16(bool a_mn_major, int n = BN, i
 #ifndef FFTSO3_MMA_N256
 #define FFTSO3_MMA_N256 1
 #endif
-
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                         uint32_t accumulate)
-{
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
-        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-        : "memory");
-}
-
-__device__ __forceinline__ void mma_commit(uint64_t* bar)
-{
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-                 : "memory");
-}
-
-// Completion of this CTA's MMAs arrives on the barrier at the same offset in every CTA of ctaMask.
-__device__ __forceinline__ void mma_commit_mc(uint64_t* bar, uint16_t mask)
-{
-    asm volatile(
-        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
-            smem_u32(bar)),
-        "h"(mask)
-        : "memory");
-}
-
-// 32 consecutive columns of this thread's TMEM lane (no wait).
-__device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, uint32_t (&r)[32])
-{
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr));
-}
-
 // hi + lo accumulator columns [c, c + 32): both loads in flight, one wait.
 __device__ __forceinline__ void tmem_ld32_sum(uint32_t thi, uint32_t tlo, float* v)
 {
@@ -243,16 +108,6 @@ __device__ __forceinline__ void tmem_ld32_sum(uint32_t thi, uint32_t tlo, float*
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(a[i]) + __uint_as_float(b[i]);
-}
-
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
-{
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-
-__device__ __forceinline__ void fence_proxy_async()
-{
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
 __device__ __forceinline__ void split3f(float x, uint16_t& h, uint16_t& m, uint16_t& l)
@@ -1274,8 +1129,8 @@ static EncodeTiledFn encode_fn()
     return fn;
 }
 
-static bool encode_2d(CUtensorMap* tm, const void* base, unsigned long long inner, unsigned long long outer,
-                      unsigned box_inner, unsigned box_outer)
+bool tc_encode_bf16_2d(CUtensorMap* tm, const void* base, unsigned long long inner, unsigned long long outer,
+                       unsigned box_inner, unsigned box_outer)
 {
     EncodeTiledFn enc = encode_fn();
     if (!enc) return false;
@@ -1503,8 +1358,8 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
     cudaMemcpy(s->d_items_inv, iti.data(), sizeof(int4) * iti.size(), cudaMemcpyHostToDevice);
     cudaMemset(s->d_err, 0, sizeof(int));
     for (int p = 0; p < 3 && !simt; ++p) {
-        bool ok = encode_2d(&s->tmA_fwd[p], s->d_tab[p], s->Kp, s->total_rows, 64, BM) &&
-                  encode_2d(&s->tmA_inv[p], s->d_tab[p], s->Kp, s->total_rows, 64, BK);
+        bool ok = tc_encode_bf16_2d(&s->tmA_fwd[p], s->d_tab[p], s->Kp, s->total_rows, 64, BM) &&
+                  tc_encode_bf16_2d(&s->tmA_inv[p], s->d_tab[p], s->Kp, s->total_rows, 64, BK);
         if (!ok) {
             err = "cuTensorMapEncodeTiled failed";
             return bail(FFTSO3_ERR_CUDA);

@@ -14,11 +14,16 @@
 // touches contiguous segments.  Twiddles come from an FP64 host table
 // W[i] = e^{-2 pi i i / N} staged in shared memory.
 #include "common.cuh"
+#include "df32.cuh"
 #include "fft.cuh"
 
 namespace fftso3 {
 
 template <typename T> struct V2;
+template <> struct V2<df32> {
+    using t = dfc32;
+    __device__ static inline dfc32 mk(df32 a, df32 b) { return dfc32{a, b}; }
+};
 template <> struct V2<double> {
     using t = double2;
     __device__ static inline double2 mk(double a, double b) { return make_double2(a, b); }
@@ -504,6 +509,11 @@ static cudaError_t launch_one(const void* in, void* out, const FFTFactors& fac, 
 
 cudaError_t launch_fft_lines(const FFTLaunch& L, cudaStream_t st)
 {
+    if (L.df32) {  // double-float complex lines (16 bytes per element), complex in and out only
+        if (L.real_in || L.real_out) return cudaErrorInvalidValue;
+        return launch_one<df32, dfc32, false, false>(L.in, L.out, L.fac, L.nlines, L.lpb, L.inner, L.ostride,
+                                                     L.istride, L.es, L.tw, L.lines_fastest, L.threads, st);
+    }
     if (L.fp64) {
         if (L.real_in && L.real_out) return cudaErrorInvalidValue;
         if (L.real_in)

@@ -19,6 +19,7 @@ struct FFTLaunch {
     long long inner, ostride, istride, es;  // line i base = (i/inner)*ostride + (i%inner)*istride; element stride es
     const void* tw;       // device double2 table, W[i] = exp(-2 pi i i / N)
     bool fp64;
+    bool df32 = false;    // double-float complex data (dfc32, 16 bytes: re.h, re.l, im.h, im.l); complex only
     bool real_in;
     bool real_out;
     bool lines_fastest;   // consecutive lines adjacent in memory (column pass)

@@ -1,0 +1,848 @@
+// Exact tensor-core inverse for the residual refinement of the SO(3) FP32-data
+// transforms (FFTSO3_FLAG_REFINE), sm_103a.
+//
+// The refinement F += forward(f - inverse(F)) removes the first forward's error
+// only if inverse(F) is formed far more accurately than the FP32 path's ~3e-7
+// (the residual is ~5e-7 of f).  Its contraction
+//   H_k(m, n) = sum_l (2l+1) F(l, m, n) d^l_mn(beta_k)        (fdcl_FFTSO3.cpp:498-531, on the grid)
+// costs 8BC flops per function, which the FP64 units of this part run at ~1.2
+// TFLOP/s.  This file runs it on the BF16 tensor cores with exact accumulation
+// (the Ozaki splitting of a product into digit products):
+//
+//  * both operands are written as 2^E sum_{i<4} s_i 2^{-7-8i} with integer
+//    digits |s_i| <= 128 (exact in BF16): the table T_g[l][k] = d^l(beta_k) with
+//    one exponent per (group, k), the coefficients Y_g[l][c] = (2l+1) sign F(l, pair)
+//    (formed exactly, as a double-float product) with one per (function, group,
+//    pair) -- along the contracted degree l every digit of a column shares one
+//    unit.  The factor (2l+1) sits on the coefficient side because the table's
+//    values then keep a small range along l: a digit split is accurate to 2^-31 of
+//    a column's largest value, and (2l+1) d ranges over ~9 more bits than d does;
+//  * the digit products s_i t_j with i + j = v accumulate in FP32 TMEM
+//    accumulator v (v = 0..3).  Every partial sum is an integer multiple of that
+//    accumulator's unit below 2^24 (|s_i t_j| <= 2^14, at most 256 degrees -- the
+//    reason for l_max <= 255 -- and at most 4 products per level), so the tensor
+//    cores add them without rounding;
+//  * the epilogue combines the four levels in double-float and scales by 2^E,
+//    giving H to about 2^-30 of its largest term (the dropped products
+//    i + j >= 4 and the digits below 2^-31), as double-float pencils.
+// A double-float FFT over (p, q) then gives the grid g, and the residual
+// r = f - g is formed against the FP32 samples in the same arithmetic (f is
+// exact there) and rounded to FP32 only as the small difference.
+//
+// Kernel layout (one CTA per SM, persistent over (group, 128 k, 8 functions) items):
+//   warp 0     TMA of the four table digit planes (MN-major operand, 128-byte swizzle);
+//   warp 1     TMEM owner (512 columns: 2 buffers x 4 levels x 64) and MMA issuer:
+//              A_j x [B_0 .. B_{3-j}] as one MMA of N = (4 - j) 64 into levels j..3,
+//              so the 10 digit products take 4 instructions per 16 degrees;
+//   warps 2-9  coefficient producers: double-float Y -> four digit planes in shared memory;
+//   warps 10-13 epilogue: TMEM -> double-float H -> pencils [fn][p][q][k].
+// Every mbarrier wait is bounded (~1 s); on timeout the kernel records an error
+// code in the state's error word and unwinds, freeing its TMEM.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "../../include/fftso3_gb300.h"
+#include "common.cuh"
+#include "df32.cuh"
+#include "fft.cuh"
+#include "refine_oz.cuh"
+#include "tc.cuh"
+#include "tc_ptx.cuh"
+
+namespace fftso3 {
+
+namespace oz {
+
+using namespace ptx;
+
+constexpr int BM = 128;                 // k rows per tile (TMEM lanes)
+constexpr int BN = 64;                  // columns: 8 functions x 4 pairs x re/im
+constexpr int FPT = BN / 8;             // functions per column tile
+constexpr int BK = 64;                  // degrees per stage (one 128-byte swizzle row of BF16)
+constexpr int UK = 16;                  // K per tcgen05.mma (kind::f16)
+constexpr int NS = 4;                   // digits per operand = accumulation levels
+constexpr int STAGES = 2;
+constexpr int APLANE = BM * BK * 2;     // 16 KB: 128 k x 64 l (two 64 x 64 boxes)
+constexpr int BPLANE = BN * BK * 2;     // 8 KB: 64 columns x 64 l
+constexpr int STAGE_A = NS * APLANE;
+constexpr int STAGE_BYTES = STAGE_A + NS * BPLANE;
+constexpr int NPROD = 8;
+constexpr int NEPI = 4;
+constexpr int THREADS = 32 * (2 + NPROD + NEPI);
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 256 /*barriers*/ + 1024 /*alignment*/;
+constexpr int ACC = NS * BN;            // TMEM columns of one accumulator buffer (levels 0..3)
+constexpr int TMEM_COLS = 2 * ACC;
+constexpr int EXP_MIN = -120, EXP_MAX = 120;
+static_assert(SMEM_BYTES <= 227 * 1024, "shared memory");
+static_assert(TMEM_COLS == 512, "TMEM");
+
+struct Args {
+    const int4* items;      // (group, row tile, column tile, m0 << 16 | (n0 + 32768))
+    const int2* iaux;       // per item: (group-major offset goff2[g], first table row grow0[g])
+    int nitems;
+    int L, N, batch, ngroups;
+    long long fstride;      // pencil elements per function (N^3)
+    long long ystride;      // coefficients per function (C)
+    const float4* Y;        // double-float group-major coefficients [fn][goff2 + pair nl + l'] (re.h, re.l, im.h, im.l)
+    const signed char* ey;  // exponents [fn][group][pair]
+    const signed char* et;  // exponents [group][k]
+    float4* pout;           // double-float pencils [fn][p][q][k]
+    int* err;
+};
+
+__device__ __forceinline__ void item_mn(const int4& it, int& m0, int& n0)
+{
+    m0 = it.w >> 16;
+    n0 = (it.w & 0xFFFF) - 32768;
+}
+
+// 2^e as a float for e in [-126, 127] (exact)
+__device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + e) << 23); }
+
+// Digits of x = (h + l) sc (|x| <= 1): x 2^7 = s0 + s1 2^-8 + s2 2^-16 + s3 2^-24 + rest,
+// each |s_i| <= 128 an integer (exact in BF16); every step but the first is exact in FP32.
+__device__ __forceinline__ void digits4(float h, float l, float sc, float (&s)[NS])
+{
+    const float t = (h * sc) * 128.f;
+    s[0] = rintf(t);
+    float r = (t - s[0]) + (l * sc) * 128.f;
+#pragma unroll
+    for (int i = 1; i < NS; ++i) {
+        r *= 256.f;
+        s[i] = rintf(r);
+        r -= s[i];
+    }
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b)
+{
+    const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);  // .x = a (low half)
+    return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+// level sums a_v (integers in units 2^-8v of level 0) -> double-float a_0 + 2^-8 a_1 + 2^-16 a_2 + 2^-24 a_3
+__device__ __forceinline__ df32 combine_levels(float a0, float a1, float a2, float a3)
+{
+    const df32 s = df_two_sum(a0, a1 * 0.00390625f);
+    return df_quick_two_sum(s.h, s.l + (a2 * 1.52587890625e-05f + a3 * 5.9604644775390625e-08f));
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
+    oz_inv_kernel(const __grid_constant__ CUtensorMap t0, const __grid_constant__ CUtensorMap t1,
+                  const __grid_constant__ CUtensorMap t2, const __grid_constant__ CUtensorMap t3,
+                  const __grid_constant__ Args a)
+{
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
+    uint64_t* empty = full + STAGES;
+    uint64_t* accf = empty + STAGES;
+    uint64_t* acce = accf + 2;
+    uint32_t* tmem_slot = (uint32_t*)(acce + 2);
+    volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    auto nsteps = [&](const int4& it) {
+        int m0, n0;
+        item_mn(it, m0, n0);
+        return (a.L + 1 - m0 + BK - 1) / BK;
+    };
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(&full[s], 1 + NPROD);
+            mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&accf[b], 1);
+            mbar_init(&acce[b], NEPI);
+        }
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            // ---------------- TMA producer of the table digit planes
+            const CUtensorMap* tm[NS] = {&t0, &t1, &t2, &t3};
+            int kc = 0;
+            for (int it = blockIdx.x; it < a.nitems && !*abort_flag; it += gridDim.x) {
+                const int4 item = a.items[it];
+                const int row0 = a.iaux[it].y;
+                const int nk = nsteps(item);
+                for (int i = 0; i < nk; ++i, ++kc) {
+                    const int s = kc % STAGES;
+                    if (kc >= STAGES && !mbar_wait(&empty[s], ((kc / STAGES) - 1) & 1, a.err, 21)) {
+                        *abort_flag = 1;
+                        break;
+                    }
+                    unsigned char* st = smem + s * STAGE_BYTES;
+                    mbar_expect_tx(&full[s], STAGE_A);
+                    const int y = row0 + i * BK;
+#pragma unroll
+                    for (int p = 0; p < NS; ++p)
+#pragma unroll
+                        for (int h = 0; h < 2; ++h)
+                            tma_load_2d(st + p * APLANE + h * (APLANE / 2), tm[p], item.y * BM + 64 * h, y, &full[s]);
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // ---------------- MMA issuer: A_j x [B_0 .. B_{3-j}] -> levels j..3
+            uint32_t idesc[NS];
+#pragma unroll
+            for (int j = 0; j < NS; ++j) idesc[j] = idesc_bf16_mn(true, (NS - j) * BN, BM);
+            int kc = 0, t = 0;
+            for (int it = blockIdx.x; it < a.nitems && !*abort_flag; it += gridDim.x, ++t) {
+                const int4 item = a.items[it];
+                const int nk = nsteps(item);
+                int m0, n0;
+                item_mn(item, m0, n0);
+                const int kvalid = a.L + 1 - m0;  // degrees; the producers zero the rest
+                const int ab = t & 1;
+                if (t >= 2 && !mbar_wait(&acce[ab], ((t >> 1) - 1) & 1, a.err, 22)) {
+                    *abort_flag = 1;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t dbase = tmem + (uint32_t)(ab * ACC);
+                bool ok = true;
+                for (int i = 0; i < nk; ++i, ++kc) {
+                    const int s = kc % STAGES;
+                    if (!mbar_wait(&full[s], (kc / STAGES) & 1, a.err, 23)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
+                    const int krem = kvalid - i * BK;
+                    const int nkk = krem >= BK ? BK / UK : (krem + UK - 1) / UK;
+#pragma unroll
+                    for (int kk = 0; kk < BK / UK; ++kk) {
+                        if (kk >= nkk) break;
+                        const uint64_t bd = smem_desc(st + STAGE_A + kk * UK * 2, 16, 1024);
+#pragma unroll
+                        for (int j = 0; j < NS; ++j) {
+                            const uint64_t ad = smem_desc(st + j * APLANE + kk * UK * 128, APLANE / 2, 1024);
+                            const bool first = (i == 0) && kk == 0 && j == 0;  // initialises all four levels
+                            mma_bf16(dbase + (uint32_t)(j * BN), ad, bd, idesc[j], first ? 0u : 1u);
+                        }
+                    }
+                    mma_commit(&empty[s]);
+                }
+                mma_commit(&accf[ab]);
+                if (!ok) {
+                    *abort_flag = 1;
+                    ++t;
+                    break;
+                }
+            }
+            for (int u = (t >= 2 ? t - 2 : 0); u < t; ++u) mbar_wait(&accf[u & 1], (u >> 1) & 1, a.err, 26);
+        }
+    } else if (warp < 2 + NPROD) {
+        // ---------------- coefficient producers (256 threads): thread = (column pair c, 16-byte chunk q8)
+        const int pt = threadIdx.x - 64;
+        const int c = pt >> 3, q8 = pt & 7;
+        const int fl = c >> 2, pp = c & 3;
+        const int Rre = 2 * c, Rim = Rre + 1;  // columns fl 8 + 2 pp (re), + 1 (im)
+        struct Src {
+            const float4* p;
+            int lim;
+            float sc;  // 2^-E of the column
+        };
+        auto source = [&](const int4& item, const int2& aux) -> Src {
+            int m0, n0;
+            item_mn(item, m0, n0);
+            const GroupPairs P = group_pairs(m0, n0);
+            const int f = item.z * FPT + fl;
+            Src r;
+            r.lim = a.L + 1 - m0;
+            r.p = nullptr;
+            r.sc = 0.f;
+            if (f >= a.batch || pp >= P.np) return r;
+            r.p = a.Y + (long long)f * a.ystride + aux.x + (long long)pp * r.lim;
+            r.sc = pow2f(-(int)a.ey[((long long)f * a.ngroups + item.x) * 4 + pp]);
+            return r;
+        };
+        auto fetch = [&](const Src& sr, int i, float4* v) {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int l = i * BK + q8 * 8 + j;
+                v[j] = (sr.p && l < sr.lim) ? __ldg(sr.p + l) : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+        };
+        int kc = 0, it = blockIdx.x, i = 0, nk_cur = 0;
+        float4 cur[8];
+        Src scur, snxt;
+        if (it < a.nitems) {
+            const int4 item0 = a.items[it];
+            scur = source(item0, a.iaux[it]);
+            nk_cur = nsteps(item0);
+            fetch(scur, 0, cur);
+        }
+        while (it < a.nitems && !*abort_flag) {
+            int it2 = it, i2 = i + 1, nk2 = nk_cur;
+            snxt = scur;
+            if (i2 == nk_cur) {
+                it2 += gridDim.x;
+                i2 = 0;
+                if (it2 < a.nitems) {
+                    const int4 item2 = a.items[it2];
+                    snxt = source(item2, a.iaux[it2]);
+                    nk2 = nsteps(item2);
+                }
+            }
+            float4 nxt[8];
+            if (it2 < a.nitems) fetch(snxt, i2, nxt);
+            const int s = kc % STAGES;
+            if (kc >= STAGES && !mbar_wait(&empty[s], ((kc / STAGES) - 1) & 1, a.err, 24)) {
+                *abort_flag = 1;
+                break;
+            }
+            const uint32_t bpl = smem_u32(smem + s * STAGE_BYTES + STAGE_A);
+            uint32_t wre[NS][4], wim[NS][4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                float dr0[NS], dr1[NS], di0[NS], di1[NS];
+                const float4 v0 = cur[2 * j], v1 = cur[2 * j + 1];
+                digits4(v0.x, v0.y, scur.sc, dr0);
+                digits4(v1.x, v1.y, scur.sc, dr1);
+                digits4(v0.z, v0.w, scur.sc, di0);
+                digits4(v1.z, v1.w, scur.sc, di1);
+#pragma unroll
+                for (int p = 0; p < NS; ++p) {
+                    wre[p][j] = pack_bf16(dr0[p], dr1[p]);
+                    wim[p][j] = pack_bf16(di0[p], di1[p]);
+                }
+            }
+            const uint32_t ore = (uint32_t)Rre * 128u + (uint32_t)((q8 ^ (Rre & 7)) * 16);
+            const uint32_t oim = (uint32_t)Rim * 128u + (uint32_t)((q8 ^ (Rim & 7)) * 16);
+#pragma unroll
+            for (int p = 0; p < NS; ++p) {
+                asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(bpl + p * BPLANE + ore), "r"(wre[p][0]),
+                             "r"(wre[p][1]), "r"(wre[p][2]), "r"(wre[p][3])
+                             : "memory");
+                asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(bpl + p * BPLANE + oim), "r"(wim[p][0]),
+                             "r"(wim[p][1]), "r"(wim[p][2]), "r"(wim[p][3])
+                             : "memory");
+            }
+            fence_proxy_async();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&full[s]);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) cur[j] = nxt[j];
+            scur = snxt;
+            nk_cur = nk2;
+            it = it2;
+            i = i2;
+            ++kc;
+        }
+    } else {
+        // ---------------- epilogue (4 warps, one TMEM lane quarter each; thread = one k row)
+        const int quarter = warp & 3;
+        const int r = quarter * 32 + lane;
+        const int N = a.N;
+        int t = 0;
+        for (int it = blockIdx.x; it < a.nitems && !*abort_flag; it += gridDim.x, ++t) {
+            const int4 item = a.items[it];
+            int m0, n0;
+            item_mn(item, m0, n0);
+            const GroupPairs P = group_pairs(m0, n0);
+            const int k = item.y * BM + r;
+            long long poff[4];
+#pragma unroll
+            for (int p = 0; p < 4; ++p) {
+                int pi = P.m[p] % N; if (pi < 0) pi += N;
+                int qi = P.n[p] % N; if (qi < 0) qi += N;
+                poff[p] = ((long long)pi * N + qi) * N;
+            }
+            const int et = k < N ? (int)a.et[(long long)item.x * N + k] : 0;
+            const int ab = t & 1;
+            if (!mbar_wait(&accf[ab], (t >> 1) & 1, a.err, 25)) {
+                *abort_flag = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t trow = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(ab * ACC);
+#pragma unroll 1
+            for (int cc = 0; cc < BN / 16; ++cc) {  // 16 columns = 2 functions x 4 pairs x re/im
+                uint32_t v[NS][16];
+#pragma unroll
+                for (int j = 0; j < NS; ++j) tmem_ld16_nowait(trow + (uint32_t)(j * BN + cc * 16), v[j]);
+                tmem_wait_ld();
+#pragma unroll
+                for (int fq = 0; fq < 2; ++fq) {
+                    const int f = item.z * FPT + cc * 2 + fq;
+                    if (f >= a.batch || k >= N) continue;
+                    float4* Ho = a.pout + (long long)f * a.fstride + k;
+                    const signed char* eyf = a.ey + ((long long)f * a.ngroups + item.x) * 4;
+#pragma unroll
+                    for (int p = 0; p < 4; ++p) {
+                        if (p >= P.np) break;
+                        const int E = et + (int)eyf[p] - 14;  // units: 2^(E_T - 7) 2^(E_Y - 7)
+                        const int cr = fq * 8 + 2 * p;
+                        const df32 re = combine_levels(__uint_as_float(v[0][cr]), __uint_as_float(v[1][cr]),
+                                                       __uint_as_float(v[2][cr]), __uint_as_float(v[3][cr]));
+                        const df32 im = combine_levels(__uint_as_float(v[0][cr + 1]), __uint_as_float(v[1][cr + 1]),
+                                                       __uint_as_float(v[2][cr + 1]), __uint_as_float(v[3][cr + 1]));
+                        Ho[poff[p]] = make_float4(ldexpf(re.h, E), ldexpf(re.l, E), ldexpf(im.h, E), ldexpf(im.l, E));
+                    }
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acce[ab]);
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 1) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+    }
+}
+
+// ---- plan-time table digits (FP64 arithmetic, once per plan)
+
+__device__ __forceinline__ int exp_above(double mx)
+{
+    if (!(mx > 0.0)) return EXP_MIN;
+    int e;
+    frexp(mx, &e);  // mx = m 2^e, m in [0.5, 1): mx < 2^e
+    return e < EXP_MIN ? EXP_MIN : (e > EXP_MAX ? EXP_MAX : e);
+}
+
+// E_T[g][k]: max over the group's degrees of |d^l(beta_k)| < 2^E_T
+__global__ void table_exp_kernel(const double* __restrict__ table, const long long* __restrict__ goff, int L, int N,
+                                 int ngroups, signed char* __restrict__ et)
+{
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)ngroups * N) return;
+    const int g = (int)(idx / N), k = (int)(idx % N);
+    int m0, n0;
+    group_mn(g, m0, n0);
+    const double* tg = table + goff[g] + k;
+    double mx = 0.0;
+    for (int j = 0; j <= L - m0; ++j) mx = fmax(mx, fabs(tg[(long long)j * N]));
+    et[idx] = (signed char)exp_above(mx);
+}
+
+// digit planes [row][Kp] of d 2^-E_T: one block per group, rows grow0[g] + j
+__global__ void table_digits_kernel(const double* __restrict__ table, const long long* __restrict__ goff, int L, int N,
+                                    int Kp, const signed char* __restrict__ et, __nv_bfloat16* __restrict__ p0,
+                                    __nv_bfloat16* __restrict__ p1, __nv_bfloat16* __restrict__ p2,
+                                    __nv_bfloat16* __restrict__ p3)
+{
+    const int g = blockIdx.x;
+    int m0, n0;
+    group_mn(g, m0, n0);
+    const int nl = L + 1 - m0;
+    const long long row0 = goff[g] / N;
+    const double* tg = table + goff[g];
+    for (long long e = threadIdx.x; e < (long long)nl * Kp; e += blockDim.x) {
+        const int j = (int)(e / Kp), k = (int)(e % Kp);
+        double s[NS] = {0.0, 0.0, 0.0, 0.0};
+        if (k < N) {
+            const double x = ldexp(tg[(long long)j * N + k], -(int)et[(long long)g * N + k]);
+            double rr = x * 128.0;
+            s[0] = rint(rr);
+            rr -= s[0];
+            for (int i = 1; i < NS; ++i) {
+                rr *= 256.0;
+                s[i] = rint(rr);
+                rr -= s[i];
+            }
+        }
+        const long long o = (row0 + j) * Kp + k;
+        p0[o] = __double2bfloat16(s[0]);
+        p1[o] = __double2bfloat16(s[1]);
+        p2[o] = __double2bfloat16(s[2]);
+        p3[o] = __double2bfloat16(s[3]);
+    }
+}
+
+// ---- per-call kernels
+
+// One warp per (function, group): the group's coefficient runs (2l+1) sign F(l, pair), l = m0..L, as
+// double-float (group-major, as the tensor-core path's layout; for FP32 input the product is exact:
+// h = fl(c v), l = fma(c, v, -h)) and one exponent per pair with max |value| < 2^E.
+template <typename CIN>
+__global__ void gather_kernel(const CIN* __restrict__ F, long long cstride, float4* __restrict__ Y,
+                              signed char* __restrict__ ey, const long long* __restrict__ goff2, int L, int ngroups,
+                              int nb)
+{
+    const long long w = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (w >= (long long)nb * ngroups) return;
+    const int lane = threadIdx.x & 31;
+    const int f = (int)(w / ngroups), g = (int)(w % ngroups);
+    int m0, n0;
+    group_mn(g, m0, n0);
+    const GroupPairs P = group_pairs(m0, n0);
+    const int nl = L + 1 - m0;
+    const CIN* Fb = F + (long long)f * cstride;
+    float4* Yb = Y + (long long)f * cstride + goff2[g];
+    for (int p = 0; p < 4; ++p) {
+        float mx = 0.f;
+        if (p < P.np) {
+            for (int li = lane; li < nl; li += 32) {
+                const int l = m0 + li;
+                const CIN v = Fb[so3_idx(l, P.m[p], P.n[p])];
+                df32 re, im;
+                if constexpr (sizeof(v.x) == 8) {
+                    re = df32((double)(2 * l + 1) * (double)v.x);
+                    im = df32((double)(2 * l + 1) * (double)v.y);
+                } else {
+                    const float c = (float)(2 * l + 1);
+                    const float rh = c * (float)v.x, ih = c * (float)v.y;
+                    re = df32(rh, fmaf(c, (float)v.x, -rh));
+                    im = df32(ih, fmaf(c, (float)v.y, -ih));
+                }
+                if (P.sign[p] < 0) {
+                    re = -re;
+                    im = -im;
+                }
+                Yb[(long long)p * nl + li] = make_float4(re.h, re.l, im.h, im.l);
+                mx = fmaxf(mx, fmaxf(fabsf(re.h), fabsf(im.h)));
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (lane == 0) {
+            int e = EXP_MIN;
+            if (mx > 0.f) {
+                frexpf(mx, &e);  // mx < 2^e; the low word adds at most half an ulp of mx
+                e = e < EXP_MIN ? EXP_MIN : (e > EXP_MAX ? EXP_MAX : e);
+            }
+            ey[((long long)f * ngroups + g) * 4 + p] = (signed char)e;
+        }
+    }
+}
+
+// the Nyquist pencils (p = B or q = B), which no (m, n) with |m|, |n| <= L maps to
+__global__ void zero_nyquist_kernel(float4* __restrict__ H, int N, long long nb)
+{
+    const long long NN = (long long)N * N;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= nb * 2 * NN) return;
+    const long long f = idx / (2 * NN), r = idx % (2 * NN);
+    const int B = N / 2;
+    long long o;
+    if (r < NN)
+        o = (long long)B * NN + r;                            // p = B: [q][k]
+    else
+        o = ((r - NN) / N) * NN + (long long)B * N + (r - NN) % N;  // q = B: [p][k]
+    H[f * NN * N + o] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// r[fn][k][j1][j2] = f - g with g[fn][j1][j2][k] the double-float grid: (f - g.h) - g.l in FP32 (f - g.h is
+// exact where g is close to f).  32 x 32 tiles of (k, j2) through shared memory; REAL: real samples and the real
+// part of g.
+template <bool REAL>
+__global__ void __launch_bounds__(256) resid_kernel(const float4* __restrict__ g, const void* __restrict__ fin,
+                                                    float* __restrict__ r, int N)
+{
+    __shared__ float4 tile[32][33];
+    const int k0 = blockIdx.x * 32, q0 = blockIdx.y * 32;
+    const long long fj = blockIdx.z;  // fn N + j1
+    const long long f = fj / N, j1 = fj % N;
+    const long long NN = (long long)N * N;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int y = ty; y < 32; y += 8) {
+        const int q = q0 + y, k = k0 + tx;
+        if (q < N && k < N) tile[y][tx] = g[f * NN * N + (j1 * N + q) * N + k];
+    }
+    __syncthreads();
+    for (int y = ty; y < 32; y += 8) {
+        const int k = k0 + y, q = q0 + tx;
+        if (q >= N || k >= N) continue;
+        const float4 v = tile[tx][y];
+        const long long o = f * NN * N + (long long)k * NN + j1 * N + q;
+        if (REAL) {
+            r[o] = (((const float*)fin)[o] - v.x) - v.y;
+        } else {
+            const float2 s = ((const float2*)fin)[o];
+            r[2 * o] = (s.x - v.x) - v.y;
+            r[2 * o + 1] = (s.y - v.z) - v.w;
+        }
+    }
+}
+
+}  // namespace oz
+
+// --------------------------------------------------------------- host side
+
+using namespace oz;
+
+struct OZState {
+    int L = 0, N = 0, B = 0, ngroups = 0, chunk = 0, ntiles = 0, nsm = 0, Kp = 0;
+    long long total_rows = 0, C = 0;
+    __nv_bfloat16* planes[NS] = {nullptr, nullptr, nullptr, nullptr};
+    CUtensorMap tm[NS];
+    signed char* et = nullptr;  // [group][k]
+    signed char* ey = nullptr;  // [chunk][group][pair]
+    float4* Y = nullptr;        // [chunk][C] double-float group-major coefficients
+    float4* pen = nullptr;      // [chunk][N^3] double-float pencils / grid
+    long long* goff2 = nullptr;
+    int4* items = nullptr;
+    int2* iaux = nullptr;
+    int nitems = 0;
+    FFTFactors fac;
+    const double* d_tw = nullptr;
+    int* err = nullptr;
+    long long bytes = 0;
+};
+
+bool oz_supported(int L, int N) { return L >= 0 && L <= 255 && N == 2 * (L + 1); }
+
+static int oz_alloc(OZState* o, void** p, size_t bytes, std::string& err)
+{
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        err = std::string("cudaMalloc (refinement state): ") + cudaGetErrorString(e);
+        return e == cudaErrorMemoryAllocation ? FFTSO3_ERR_OOM : FFTSO3_ERR_CUDA;
+    }
+    o->bytes += (long long)bytes;
+    return FFTSO3_SUCCESS;
+}
+
+void oz_destroy(OZState* o)
+{
+    if (!o) return;
+    for (int p = 0; p < NS; ++p)
+        if (o->planes[p]) cudaFree(o->planes[p]);
+    void* ptrs[] = {o->et, o->ey, o->Y, o->pen, o->goff2, o->items, o->iaux, o->err};
+    for (void* q : ptrs)
+        if (q) cudaFree(q);
+    delete o;
+}
+
+long long oz_device_bytes(const OZState* o) { return o ? o->bytes : 0; }
+
+int oz_create(OZState** out, const double* d_table, const std::vector<long long>& goff, int L, int N, int chunk,
+              const double* d_tw, std::string& err)
+{
+    *out = nullptr;
+    if (!oz_supported(L, N) || chunk < 1) {
+        err = "internal: exact refinement inverse needs SO(3) l_max <= 255";
+        return FFTSO3_ERR_UNSUPPORTED;
+    }
+    OZState* o = new OZState();
+    o->L = L;
+    o->B = L + 1;
+    o->N = N;
+    o->ngroups = o->B * o->B;
+    o->chunk = chunk;
+    o->ntiles = (chunk + FPT - 1) / FPT;
+    o->Kp = (N + 63) / 64 * 64;
+    o->C = so3_off(o->B);
+    o->total_rows = goff[o->ngroups] / N;
+    o->d_tw = d_tw;
+    make_fft_factors(N, o->fac);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&o->nsm, cudaDevAttrMultiProcessorCount, dev);
+    int rc;
+    auto bail = [&](int code) {
+        oz_destroy(o);
+        return code;
+    };
+    // exponents and digit planes of the table, from the FP64 table
+    long long* d_goff = nullptr;
+    if ((rc = oz_alloc(o, (void**)&d_goff, sizeof(long long) * goff.size(), err))) return bail(rc);
+    cudaMemcpy(d_goff, goff.data(), sizeof(long long) * goff.size(), cudaMemcpyHostToDevice);
+    const size_t plane = sizeof(__nv_bfloat16) * (size_t)o->total_rows * o->Kp;
+    for (int p = 0; p < NS; ++p)
+        if ((rc = oz_alloc(o, (void**)&o->planes[p], plane, err))) {
+            cudaFree(d_goff);
+            return bail(rc);
+        }
+    if ((rc = oz_alloc(o, (void**)&o->et, (size_t)o->ngroups * N, err))) {
+        cudaFree(d_goff);
+        return bail(rc);
+    }
+    {
+        const long long tot = (long long)o->ngroups * N;
+        table_exp_kernel<<<(unsigned)((tot + 255) / 256), 256>>>(d_table, d_goff, L, N, o->ngroups, o->et);
+        table_digits_kernel<<<o->ngroups, 256>>>(d_table, d_goff, L, N, o->Kp, o->et, o->planes[0], o->planes[1],
+                                                 o->planes[2], o->planes[3]);
+        cudaError_t e = cudaDeviceSynchronize();
+        cudaFree(d_goff);
+        o->bytes -= (long long)(sizeof(long long) * goff.size());
+        if (e != cudaSuccess) {
+            err = std::string("refinement table digits: ") + cudaGetErrorString(e);
+            return bail(FFTSO3_ERR_CUDA);
+        }
+    }
+    for (int p = 0; p < NS; ++p)
+        if (!tc_encode_bf16_2d(&o->tm[p], o->planes[p], o->Kp, o->total_rows, 64, BK)) {
+            err = "cuTensorMapEncodeTiled failed (refinement table)";
+            return bail(FFTSO3_ERR_CUDA);
+        }
+    // group-major offsets, work items (ordered by decreasing length), per-item (goff2, first row)
+    std::vector<long long> goff2(o->ngroups + 1);
+    std::vector<int4> items;
+    std::vector<int2> aux;
+    long long acc2 = 0;
+    for (int g = 0; g < o->ngroups; ++g) {
+        int m0, n0;
+        group_mn(g, m0, n0);
+        goff2[g] = acc2;
+        acc2 += (long long)group_pairs(m0, n0).np * (o->B - m0);
+        for (int nt = 0; nt < o->ntiles; ++nt)
+            for (int mt = 0; mt * BM < N; ++mt)
+                items.push_back(make_int4(g, mt, nt, (m0 << 16) | (n0 + 32768)));
+    }
+    goff2[o->ngroups] = acc2;
+    if (acc2 != o->C) {
+        err = "internal: group-major layout does not cover the coefficients";
+        return bail(FFTSO3_ERR_CUDA);
+    }
+    std::stable_sort(items.begin(), items.end(), [&](const int4& x, const int4& y) { return (x.w >> 16) < (y.w >> 16); });
+    aux.resize(items.size());
+    for (size_t i = 0; i < items.size(); ++i)
+        aux[i] = make_int2((int)goff2[items[i].x], (int)(goff[items[i].x] / N));
+    o->nitems = (int)items.size();
+    if ((rc = oz_alloc(o, (void**)&o->goff2, sizeof(long long) * goff2.size(), err))) return bail(rc);
+    if ((rc = oz_alloc(o, (void**)&o->items, sizeof(int4) * items.size(), err))) return bail(rc);
+    if ((rc = oz_alloc(o, (void**)&o->iaux, sizeof(int2) * aux.size(), err))) return bail(rc);
+    cudaMemcpy(o->goff2, goff2.data(), sizeof(long long) * goff2.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(o->items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(o->iaux, aux.data(), sizeof(int2) * aux.size(), cudaMemcpyHostToDevice);
+    // per-chunk buffers
+    const size_t grid = (size_t)N * N * N;
+    if ((rc = oz_alloc(o, (void**)&o->Y, sizeof(float4) * (size_t)chunk * o->C, err))) return bail(rc);
+    if ((rc = oz_alloc(o, (void**)&o->ey, (size_t)chunk * o->ngroups * 4, err))) return bail(rc);
+    if ((rc = oz_alloc(o, (void**)&o->pen, sizeof(float4) * (size_t)chunk * grid, err))) return bail(rc);
+    if ((rc = oz_alloc(o, (void**)&o->err, sizeof(int), err))) return bail(rc);
+    cudaMemset(o->err, 0, sizeof(int));
+    cudaError_t e = cudaFuncSetAttribute(oz_inv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        err = std::string("refinement state: ") + cudaGetErrorString(e);
+        return bail(FFTSO3_ERR_CUDA);
+    }
+    *out = o;
+    return FFTSO3_SUCCESS;
+}
+
+int oz_status(OZState* o)
+{
+    int v = 0;
+    if (o && o->err) cudaMemcpy(&v, o->err, sizeof(int), cudaMemcpyDeviceToHost);
+    return v;
+}
+
+#define OZK(call)                                                              \
+    do {                                                                       \
+        cudaError_t _e = (call);                                               \
+        if (_e != cudaSuccess) {                                               \
+            err = std::string(#call) + ": " + cudaGetErrorString(_e);          \
+            return FFTSO3_ERR_CUDA;                                            \
+        }                                                                      \
+    } while (0)
+
+int oz_inverse_resid(OZState* o, const void* F, bool f64, int nb, const void* fgrid, bool real, float* resid,
+                     cudaStream_t st, StageTimer* T, std::string& err)
+{
+    if (nb < 1 || nb > o->chunk) {
+        err = "internal: refinement chunk larger than its buffers";
+        return FFTSO3_ERR_CUDA;
+    }
+    const int N = o->N, L = o->L;
+    const long long NN = (long long)N * N;
+    // coefficients -> double-float group-major runs and their exponents
+    T->begin(ST_REFINE, st);
+    {
+        const long long warps = (long long)nb * o->ngroups;
+        const unsigned blocks = (unsigned)((warps + 7) / 8);
+        if (f64)
+            gather_kernel<double2><<<blocks, 256, 0, st>>>((const double2*)F, o->C, o->Y, o->ey, o->goff2, L,
+                                                           o->ngroups, nb);
+        else
+            gather_kernel<float2><<<blocks, 256, 0, st>>>((const float2*)F, o->C, o->Y, o->ey, o->goff2, L, o->ngroups,
+                                                          nb);
+        OZK(cudaGetLastError());
+        const long long tot = (long long)nb * 2 * NN;
+        zero_nyquist_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(o->pen, N, nb);
+        OZK(cudaGetLastError());
+    }
+    T->end(st);
+    // the exact contraction
+    T->begin(ST_REF_CONTRACT, st);
+    {
+        Args a;
+        a.items = o->items;
+        a.iaux = o->iaux;
+        a.nitems = o->nitems;
+        a.L = L;
+        a.N = N;
+        a.batch = nb;
+        a.ngroups = o->ngroups;
+        a.fstride = NN * N;
+        a.ystride = o->C;
+        a.Y = o->Y;
+        a.ey = o->ey;
+        a.et = o->et;
+        a.pout = o->pen;
+        a.err = o->err;
+        const int nctas = o->nitems < o->nsm ? o->nitems : o->nsm;
+        oz_inv_kernel<<<nctas, THREADS, SMEM_BYTES, st>>>(o->tm[0], o->tm[1], o->tm[2], o->tm[3], a);
+        OZK(cudaGetLastError());
+    }
+    T->end(st);
+    // double-float FFT over q (lines (fn, p, k)), then over p (lines (fn, q, k)), in place
+    T->begin(ST_REF_FFT, st);
+    {
+        FFTLaunch Lq;
+        Lq.in = o->pen;
+        Lq.out = o->pen;
+        Lq.fac = o->fac;
+        Lq.nlines = (long long)nb * NN;
+        Lq.lpb = 8;
+        Lq.inner = N;
+        Lq.ostride = NN;
+        Lq.istride = 1;
+        Lq.es = N;
+        Lq.tw = o->d_tw;
+        Lq.fp64 = false;
+        Lq.df32 = true;
+        Lq.real_in = false;
+        Lq.real_out = false;
+        Lq.lines_fastest = true;
+        OZK(launch_fft_lines(Lq, st));
+        FFTLaunch Lp = Lq;
+        Lp.inner = NN;
+        Lp.ostride = NN * N;
+        Lp.es = NN;
+        OZK(launch_fft_lines(Lp, st));
+    }
+    T->end(st);
+    // residual against the FP32 samples, transposed back to [fn][k][j1][j2]
+    T->begin(ST_REFINE, st);
+    {
+        dim3 grid((unsigned)((N + 31) / 32), (unsigned)((N + 31) / 32), (unsigned)((long long)nb * N));
+        if (real)
+            resid_kernel<true><<<grid, 256, 0, st>>>(o->pen, fgrid, resid, N);
+        else
+            resid_kernel<false><<<grid, 256, 0, st>>>(o->pen, fgrid, resid, N);
+        OZK(cudaGetLastError());
+    }
+    T->end(st);
+    return FFTSO3_SUCCESS;
+}
+
+}  // namespace fftso3

@@ -1,0 +1,29 @@
+// Exact tensor-core inverse of the residual refinement (see refine_oz.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "timing.cuh"
+
+namespace fftso3 {
+
+struct OZState;
+
+// SO(3) with l_max <= 255 (at most 256 degrees per contraction keep the digit sums exact).
+bool oz_supported(int L, int N);
+// Builds the table's digit planes and exponents from the plan's FP64 Wigner-d table (goff: group offsets into
+// it) and buffers for `chunk` functions per call.
+int oz_create(OZState** out, const double* d_table, const std::vector<long long>& goff, int L, int N, int chunk,
+              const double* d_tw, std::string& err);
+void oz_destroy(OZState* o);
+long long oz_device_bytes(const OZState* o);
+// Error word of the exact contraction kernel (a bounded wait that gave up); synchronising read.
+int oz_status(OZState* o);
+// For nb <= chunk functions: r = f - inverse(F), F complex coefficients (complex128 when f64, else complex64),
+// f the FP32 samples (complex64, or float32 when real), r written like f.
+int oz_inverse_resid(OZState* o, const void* F, bool f64, int nb, const void* fgrid, bool real, float* resid,
+                     cudaStream_t st, StageTimer* T, std::string& err);
+
+}  // namespace fftso3

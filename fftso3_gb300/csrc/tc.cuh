@@ -1,5 +1,6 @@
 // FP32-data transform state (see contract_tc.cu): tcgen05 split-BF16 or FP32 CUDA-core beta-sum, SO(3) or S^2.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <string>
 #include <vector>
@@ -40,6 +41,11 @@ int tc_fused_create(TCFused** out, const std::vector<TCState*>& parts, std::stri
 void tc_fused_destroy(TCFused* f);
 int tc_fused_gemm(TCFused* f, bool fwd, cudaStream_t st, StageTimer* T, std::string& err);
 int tc_fused_status(TCFused* f);
+
+// Row-major 2-D BF16 tensor map (inner elements per row, outer rows; 128-byte swizzle, boxes of
+// box_inner x box_outer), resolved through the runtime's driver entry point.
+bool tc_encode_bf16_2d(CUtensorMap* tm, const void* base, unsigned long long inner, unsigned long long outer,
+                       unsigned box_inner, unsigned box_outer);
 
 // A plan's tensor-core state (null for FP64 plans) and stage timer (api.cu).
 TCState* plan_tc_state(fftso3_plan* p);

@@ -1,0 +1,98 @@
+"""The residual refinement (FFTSO3_FLAG_REFINE) of the tensor-core SO(3) forward (GPU).
+
+F += forward(f - inverse(F)): for SO(3) with l_max <= 255 the inverse runs on the
+tensor cores with exact digit sums (BF16 digit planes, FP32 TMEM accumulators that
+never round), then a double-float FFT and the residual against the FP32 samples;
+FFTSO3_REFINE_FP64=1 at plan creation selects the FP64 inverse instead.  Either
+way the refined coefficients are the FP64 forward of the FP32 samples up to the
+complex64 rounding of the output.
+
+Error metric: rel_rms = ||a - b|| / ||b||; rel_max = max_l max_mn |a - b| / rms_mn |b|.
+Bounds: rel_rms <= 1e-7 and rel_max <= 1e-6 against the oracle's forward of the same
+FP32 samples (measured ~3e-8 / ~2e-7 at l_max = 255).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import so3_coeffs
+
+pytestmark = pytest.mark.gpu
+
+
+def per_l_errors(a, b, l_max):
+    rms = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    mx = 0.0
+    for l in range(l_max + 1):
+        o0, o1 = l * (4 * l * l - 1) // 3, (l + 1) * (4 * (l + 1) ** 2 - 1) // 3
+        d = np.abs(a[o0:o1] - b[o0:o1]).max()
+        r = np.sqrt(np.mean(np.abs(b[o0:o1]) ** 2))
+        mx = max(mx, float(d / r))
+    return rms, mx
+
+
+def _refined(gblib, kind, L, grids32, fp64_inverse=False):
+    import torch
+    s = torch.cuda.current_stream().cuda_stream
+    b = grids32.shape[0]
+    old = os.environ.get("FFTSO3_REFINE_FP64")
+    if fp64_inverse:
+        os.environ["FFTSO3_REFINE_FP64"] = "1"
+    try:
+        p = gblib.Plan(kind, L, b, "tc_bf16x3", "stable", gblib.FLAG_REFINE)
+    finally:
+        if fp64_inverse:
+            if old is None:
+                del os.environ["FFTSO3_REFINE_FP64"]
+            else:
+                os.environ["FFTSO3_REFINE_FP64"] = old
+    cplx = kind == gblib.SO3_COMPLEX
+    g = torch.from_numpy(np.ascontiguousarray(grids32).ravel()).cuda()
+    c = torch.empty(b * p.coeff_elems, dtype=torch.complex64 if cplx else torch.float32, device="cuda")
+    p.forward(g.data_ptr(), c.data_ptr(), s)
+    p.check()
+    out = c.cpu().numpy().astype(np.complex128 if cplx else np.float64).reshape(b, -1)
+    del p
+    return out
+
+
+@pytest.mark.parametrize("kind,L", [("complex", 15), ("complex", 31), ("real", 31), ("complex", 47), ("real", 20)])
+def test_refined_forward_matches_oracle(gblib, oracle, kind, L):
+    """Batch 9: two refinement chunks (8 + 1 functions), and both column tiles of the exact inverse."""
+    cplx = kind == "complex"
+    k = gblib.SO3_COMPLEX if cplx else gblib.SO3_REAL
+    N = 2 * (L + 1)
+    b = 9
+    grids, refs = [], []
+    for i in range(b):
+        F = so3_coeffs(L, seed=4000 + 17 * L + i, complex_=cplx, decay="pow")
+        if cplx:
+            g = oracle.so3_inverse_complex_grid(L, F).astype(np.complex64)
+            ref = oracle.so3_forward_complex(L, g.astype(np.complex128))
+        else:
+            g = oracle.so3_inverse_real_grid(L, F).astype(np.float32)
+            ref = oracle.so3_forward_real(L, g.astype(np.float64))
+        grids.append(g.reshape(N, N, N))
+        refs.append(ref)
+    out = _refined(gblib, k, L, np.stack(grids))
+    for i in range(b):
+        rms, mx = per_l_errors(out[i], refs[i], L)
+        assert rms <= 1e-7 and mx <= 1e-6, (i, rms, mx)
+
+
+def test_exact_and_fp64_refinement_agree(gblib, oracle):
+    """The tensor-core exact inverse and the FP64 inverse give the same refined coefficients (to the complex64
+    rounding of the output and the ~1e-9 of the exact inverse)."""
+    L = 31
+    N = 2 * (L + 1)
+    grids = []
+    for i in range(3):
+        F = so3_coeffs(L, seed=4500 + i, decay="pow")
+        grids.append(oracle.so3_inverse_complex_grid(L, F).astype(np.complex64).reshape(N, N, N))
+    grids = np.stack(grids)
+    a = _refined(gblib, gblib.SO3_COMPLEX, L, grids)
+    b = _refined(gblib, gblib.SO3_COMPLEX, L, grids, fp64_inverse=True)
+    for i in range(3):
+        rms, mx = per_l_errors(a[i], b[i], L)
+        assert rms <= 1e-7 and mx <= 1e-6, (i, rms, mx)
