@@ -149,41 +149,57 @@ def profiled_traffic(stage: str, l_max: int, batch: int):
 # --------------------------------------------------------------- CPU legs
 
 def cpu_sample(l_max: int, nslices: int | None = None, threads: int | None = None) -> dict:
-    """Oracle (restated reference algorithm, OpenMP) on beta slices 0..S-1 of
-    the forward and of the inverse at l_max; pairs/s extrapolated to all 2B slices."""
+    """Oracle (the reference algorithm restated, OpenMP over beta slices as the reference) on S beta slices
+    spread evenly over [0, pi) -- k = stride/2 + i stride -- of one l_max forward and one inverse; pairs/s
+    extrapolated to all 2B slices (every slice costs the same work)."""
     from oracle import oracle as O
 
     O.build()
     nth = threads or os.cpu_count() or 1
     O.set_num_threads(nth)
     N = 2 * (l_max + 1)
-    S = min(N, nslices or nth)
+    S = max(1, min(N, nslices or nth))
+    stride = N // S
+    k0 = stride // 2
     rng = np.random.default_rng(0)
     F = seeded_coeffs(l_max, 0)
     slab = (rng.standard_normal((S, N, N)) + 1j * rng.standard_normal((S, N, N)))
     t0 = time.perf_counter()
-    O.so3_forward_complex_slices(l_max, slab, 0, S)
+    O.so3_forward_complex_strided(l_max, slab, k0, stride)
     t1 = time.perf_counter()
-    O.so3_inverse_complex_slices(l_max, F, 0, S)
+    O.so3_inverse_complex_strided(l_max, F, k0, stride, S)
     t2 = time.perf_counter()
     per_pair = ((t1 - t0) + (t2 - t1)) * N / S
     return {"value": 1.0 / per_pair, "unit": UNIT, "cores": nth, "kind": "port",
-            "sample": f"beta slices 0..{S - 1} of {N} of one l_max={l_max} complex forward and inverse "
-                      f"(oracle restatement of fdcl_FFTSO3.cpp:659-763 / :498-531, OpenMP {nth} threads); "
-                      f"pairs/s extrapolated x{N}/{S}",
+            "sample": f"{S} of {N} beta slices (k = {k0} + {stride} i, spread over [0, pi)) of one l_max={l_max} "
+                      f"complex forward and inverse (oracle restatement of fdcl_FFTSO3.cpp:659-763 / :498-531, "
+                      f"OpenMP over slices, {nth} threads); pairs/s extrapolated x{N}/{S}",
             "seconds": t2 - t0}
+
+
+def cpu_baselines(l_max: int) -> dict:
+    """The CPU baseline at all host threads (the reported figure) and at one thread, as the reference's
+    example4 times its transforms (example/example4.cpp:30,58)."""
+    nth = os.cpu_count() or 1
+    full = cpu_sample(l_max, nslices=2 * nth, threads=nth)
+    one = cpu_sample(l_max, nslices=2, threads=1)
+    full.pop("seconds", None)
+    one.pop("seconds", None)
+    full["single_thread"] = {"value": one["value"], "cores": 1, "sample": one["sample"]}
+    return full
 
 
 def run_reference(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    nth = os.cpu_count() or 1
     for _ in range(args.warmup):
-        cpu_sample(args.l_max)
+        cpu_sample(args.l_max, nslices=nth)
     vals = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        vals.append(cpu_sample(args.l_max))
+        vals.append(cpu_sample(args.l_max, nslices=nth))
     wall = time.perf_counter() - t0
     v = float(np.mean([x["value"] for x in vals]))
     line = {
@@ -1063,8 +1079,7 @@ def main() -> None:
 
     cpu = None
     if not args.no_cpu:
-        cpu = cpu_sample(L)
-        cpu.pop("seconds", None)
+        cpu = cpu_baselines(L)
 
     if rank == 0:
         metric = METRIC if L == 255 else METRIC.replace("l_max=255", f"l_max={L}")

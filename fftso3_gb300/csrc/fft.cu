@@ -445,6 +445,103 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(const TIN* __restrict__ 
     }
 }
 
+// ---- double-float FFT along a strided axis of k-contiguous arrays (the refinement's grid synthesis)
+//
+// Line (o, k): element j at obase(o) + k + j S, obase(o) = (o / oinner) oouter + (o % oinner) oistride.  One CTA
+// transforms TK = 2048 / N consecutive k of one o (N = 64..512, a power of two) with 256 threads: TK lines of N
+// elements staged in shared memory (global accesses run k-fastest: TK consecutive elements per j), then radix-8
+// Stockham stages (a last radix-4 or 2 stage when log2 N is not a multiple of 3), each thread holding the 8
+// values of one butterfly in registers; stages run in place, a barrier between the reads and the writes.  Rows
+// are padded by one element per 8 (phys(i) = i + i / 8), so both the strided reads and the scattered writes of
+// a stage fill whole 16-byte bank groups.
+template <int N>
+__global__ void __launch_bounds__(256) fft_df32_k_kernel(dfc32* __restrict__ buf, long long S, long long oinner,
+                                                          long long oouter, long long oistride,
+                                                          const double2* __restrict__ twg)
+{
+    constexpr int TK = 2048 / N;     // lines per CTA
+    constexpr int TPL = N / 8;       // threads per line
+    constexpr int ROW = N + N / 8;   // padded row length
+    __shared__ dfc32 sm[TK * ROW];
+    __shared__ dfc32 w[N];
+    auto phys = [](int i) { return i + (i >> 3); };
+    const int tid = threadIdx.x;
+    const long long o = blockIdx.y;
+    const long long obase = (o / oinner) * oouter + (o % oinner) * oistride + (long long)blockIdx.x * TK;
+    for (int i = tid; i < N; i += 256) w[i] = dfc32{df32(twg[i].x), df32(twg[i].y)};
+#pragma unroll
+    for (int u = 0; u < N * TK / 256; ++u) {
+        const int e = tid + 256 * u, kk = e % TK, j = e / TK;
+        sm[kk * ROW + phys(j)] = buf[obase + (long long)j * S + kk];
+    }
+    __syncthreads();
+    const int kk = tid / TPL, t = tid % TPL;
+    dfc32* line = sm + kk * ROW;
+    int Ns = 1;
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {  // radix-8 stages while 8 Ns divides N
+        if (Ns * 8 > N) break;
+        const int kt = t % Ns;
+        dfc32 v[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) v[r] = line[phys(t + r * (N / 8))];
+        __syncthreads();
+        if (Ns > 1) {
+            const int e = kt * (N / (8 * Ns));
+#pragma unroll
+            for (int r = 1; r < 8; ++r) v[r] = cmul(v[r], w[r * e]);
+        }
+        dft_small<df32, 8>(v, w, N / 8);
+#pragma unroll
+        for (int r = 0; r < 8; ++r) line[phys((t - kt) * 8 + kt + r * Ns)] = v[r];
+        __syncthreads();
+        Ns *= 8;
+    }
+    if constexpr (N == 128 || N == 256) {  // one radix-2 or radix-4 stage: 8 / R butterflies per thread
+        constexpr int R = N == 256 ? 4 : 2;
+        constexpr int PER = 8 / R;
+        dfc32 v[PER][R];
+#pragma unroll
+        for (int b = 0; b < PER; ++b)
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[b][r] = line[phys(t + b * TPL + r * (N / R))];
+        __syncthreads();
+#pragma unroll
+        for (int b = 0; b < PER; ++b) {
+            const int j = t + b * TPL, kt = j % Ns, e = kt * (N / (R * Ns));
+#pragma unroll
+            for (int r = 1; r < R; ++r) v[b][r] = cmul(v[b][r], w[r * e]);
+            dft_small<df32, R>(v[b], w, N / R);
+#pragma unroll
+            for (int r = 0; r < R; ++r) line[phys((j - kt) * R + kt + r * Ns)] = v[b][r];
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int u = 0; u < N * TK / 256; ++u) {
+        const int e = tid + 256 * u, kk2 = e % TK, j = e / TK;
+        buf[obase + (long long)j * S + kk2] = sm[kk2 * ROW + phys(j)];
+    }
+}
+
+bool fft_df32_k_supported(int N) { return N == 64 || N == 128 || N == 256 || N == 512; }
+
+cudaError_t launch_fft_df32_k(void* buf, int N, long long S, long long nouter, long long oinner, long long oouter,
+                              long long oistride, const void* tw, cudaStream_t st)
+{
+    if (!fft_df32_k_supported(N) || nouter < 1 || nouter > 65535 || oinner < 1) return cudaErrorInvalidValue;
+    const dim3 grid((unsigned)(N / (2048 / N)), (unsigned)nouter);
+    dfc32* b = (dfc32*)buf;
+    const double2* t = (const double2*)tw;
+    switch (N) {
+        case 64: fft_df32_k_kernel<64><<<grid, 256, 0, st>>>(b, S, oinner, oouter, oistride, t); break;
+        case 128: fft_df32_k_kernel<128><<<grid, 256, 0, st>>>(b, S, oinner, oouter, oistride, t); break;
+        case 256: fft_df32_k_kernel<256><<<grid, 256, 0, st>>>(b, S, oinner, oouter, oistride, t); break;
+        default: fft_df32_k_kernel<512><<<grid, 256, 0, st>>>(b, S, oinner, oouter, oistride, t); break;
+    }
+    return cudaGetLastError();
+}
+
 void make_fft_factors(int N, FFTFactors& f)
 {
     f.N = N;

@@ -33,6 +33,13 @@ void make_fft_factors_prime_first(int N, FFTFactors& f);
 size_t fft_smem_bytes(int N, int lpb, bool fp64);
 cudaError_t launch_fft_lines(const FFTLaunch& L, cudaStream_t st);
 
+// Double-float (dfc32) FFT along a strided axis of arrays whose innermost index k (N values) is contiguous,
+// in place: line (o, k), o < nouter, has element j at obase(o) + k + j S, obase(o) = (o / oinner) oouter +
+// (o % oinner) oistride.  N = 64..512, powers of two (fft.cu).
+bool fft_df32_k_supported(int N);
+cudaError_t launch_fft_df32_k(void* buf, int N, long long S, long long nouter, long long oinner, long long oouter,
+                              long long oistride, const void* tw, cudaStream_t st);
+
 // Register-resident FP32 kernels for N = 64..1024, powers of two (fft_fast.cu).
 bool fft_fast_supported(int N);
 // nlines contiguous lines of N complex64: out[line][K] = FFT(in[line])[K] (in may equal out)

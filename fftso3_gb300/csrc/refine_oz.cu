@@ -806,7 +806,11 @@ int oz_inverse_resid(OZState* o, const void* F, bool f64, int nb, const void* fg
     T->end(st);
     // double-float FFT over q (lines (fn, p, k)), then over p (lines (fn, q, k)), in place
     T->begin(ST_REF_FFT, st);
-    {
+    if (fft_df32_k_supported(N)) {
+        // lines (fn, p, k) along q (stride N), then (fn, q, k) along p (stride N^2); k contiguous in both
+        OZK(launch_fft_df32_k(o->pen, N, N, (long long)nb * N, N, NN * N, NN, o->d_tw, st));
+        OZK(launch_fft_df32_k(o->pen, N, NN, (long long)nb * N, N, NN * N, N, o->d_tw, st));
+    } else {
         FFTLaunch Lq;
         Lq.in = o->pen;
         Lq.out = o->pen;

@@ -335,21 +335,31 @@ static void dft2_slice(int N, double *s, const double *tw)
  * replaced by the sampled grid f[k][j1][j2] (complex); the OpenMP structure is
  * the reference's: per-k local coefficients zeroed, accumulated, then merged
  * into F under a critical section. */
-static void so3_forward_complex_range(int l_max, const double *grid, int is_real, double *F, int k0, int k1);
+static void so3_forward_complex_range(int l_max, const double *grid, int is_real, double *F, int k0, int kstride,
+                                      int count);
 
 void orc_so3_forward_complex(int l_max, const double *grid, int is_real, double *F)
 {
-    so3_forward_complex_range(l_max, grid, is_real, F, 0, 2 * (l_max + 1));
+    so3_forward_complex_range(l_max, grid, is_real, F, 0, 1, 2 * (l_max + 1));
 }
 
 /* The slices k in [k0, k1) of the forward sum (bounded CPU timing samples);
  * grid holds only those slices, grid[(k - k0)][j1][j2]. */
 void orc_so3_forward_complex_slices(int l_max, const double *grid, double *F, int k0, int k1)
 {
-    so3_forward_complex_range(l_max, grid - 2L * k0 * (2 * (l_max + 1)) * (2 * (l_max + 1)), 0, F, k0, k1);
+    so3_forward_complex_range(l_max, grid, 0, F, k0, 1, k1 - k0);
 }
 
-static void so3_forward_complex_range(int l_max, const double *grid, int is_real, double *F, int k0, int k1)
+/* The slices k = k0 + i kstride, i < count, of the forward sum (CPU timing samples spread over
+ * beta); grid holds only those slices, grid[i][j1][j2]. */
+void orc_so3_forward_complex_strided(int l_max, const double *grid, double *F, int k0, int kstride, int count)
+{
+    so3_forward_complex_range(l_max, grid, 0, F, k0, kstride, count);
+}
+
+/* grid[i] is slice k = k0 + i kstride, i < count */
+static void so3_forward_complex_range(int l_max, const double *grid, int is_real, double *F, int k0, int kstride,
+                                      int count)
 {
     int B = l_max + 1, N = 2 * B;
     long C = so3_off(l_max + 1);
@@ -363,11 +373,12 @@ static void so3_forward_complex_range(int l_max, const double *grid, int is_real
         double *F_local = (double *)malloc(sizeof(double) * 2 * C);
         double *d = (double *)malloc(sizeof(double) * C);
         double *F_k = (double *)malloc(sizeof(double) * 2L * N * N);
-        int k;
+        int i;
 #pragma omp for schedule(static)
-        for (k = k0; k < k1; k++) {
+        for (i = 0; i < count; i++) {
+            const int k = k0 + i * kstride;
             double beta = orc_beta_k(B, k);
-            memcpy(F_k, grid + 2L * k * N * N, sizeof(double) * 2L * N * N);
+            memcpy(F_k, grid + 2L * i * N * N, sizeof(double) * 2L * N * N);
             dft2_slice(N, F_k, tw);
             orc_wigner_d(beta, l_max, d);
             memset(F_local, 0, sizeof(double) * 2 * C);
@@ -628,20 +639,27 @@ double orc_so3_inverse_real_point(int l_max, const double *F, double alpha, doub
  * every grid point, done separably per beta_k: Fmn(m,n) as the reference
  * forms it, then the alpha and gamma sums with the reference's exponentials
  * exp(-i m alpha_j1), exp(-i n gamma_j2).  O(B^4) instead of O(B^6). */
-static void so3_inverse_complex_range(int l_max, const double *F, double *grid, int k0, int k1);
+static void so3_inverse_complex_range(int l_max, const double *F, double *grid, int k0, int kstride, int count);
 
 void orc_so3_inverse_complex_grid(int l_max, const double *F, double *grid)
 {
-    so3_inverse_complex_range(l_max, F, grid, 0, 2 * (l_max + 1));
+    so3_inverse_complex_range(l_max, F, grid, 0, 1, 2 * (l_max + 1));
 }
 
 /* The slices k in [k0, k1) of the grid synthesis, written to grid[(k - k0)][j1][j2]. */
 void orc_so3_inverse_complex_slices(int l_max, const double *F, double *grid, int k0, int k1)
 {
-    so3_inverse_complex_range(l_max, F, grid - 2L * k0 * (2 * (l_max + 1)) * (2 * (l_max + 1)), k0, k1);
+    so3_inverse_complex_range(l_max, F, grid, k0, 1, k1 - k0);
 }
 
-static void so3_inverse_complex_range(int l_max, const double *F, double *grid, int k0, int k1)
+/* The slices k = k0 + i kstride, i < count, of the grid synthesis, written to grid[i][j1][j2]. */
+void orc_so3_inverse_complex_strided(int l_max, const double *F, double *grid, int k0, int kstride, int count)
+{
+    so3_inverse_complex_range(l_max, F, grid, k0, kstride, count);
+}
+
+/* grid[i] is slice k = k0 + i kstride, i < count */
+static void so3_inverse_complex_range(int l_max, const double *F, double *grid, int k0, int kstride, int count)
 {
     int B = l_max + 1, N = 2 * B, W = 2 * l_max + 1;
     double *ex = (double *)malloc(sizeof(double) * 2L * N * W);
@@ -657,9 +675,10 @@ static void so3_inverse_complex_range(int l_max, const double *F, double *grid, 
         double *d = (double *)malloc(sizeof(double) * so3_off(l_max + 1));
         double *Fmn = (double *)malloc(sizeof(double) * 2L * W * W);
         double *T = (double *)malloc(sizeof(double) * 2L * N * W);
-        int k;
+        int i;
 #pragma omp for schedule(static)
-        for (k = k0; k < k1; k++) {
+        for (i = 0; i < count; i++) {
+            const int k = k0 + i * kstride;
             orc_wigner_d(orc_beta_k(B, k), l_max, d);
             for (int m = -l_max; m <= l_max; m++)
                 for (int n = -l_max; n <= l_max; n++) {
@@ -696,7 +715,7 @@ static void so3_inverse_complex_range(int l_max, const double *F, double *grid, 
                         fr += ar * br - ai * bi;
                         fi += ar * bi + ai * br;
                     }
-                    long o = 2L * (((long)k * N + j1) * N + j2);
+                    long o = 2L * (((long)i * N + j1) * N + j2);
                     grid[o] = fr;
                     grid[o + 1] = fi;
                 }

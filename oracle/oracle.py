@@ -61,6 +61,8 @@ def lib():
             "orc_so3_inverse_complex_grid": (None, [i, _dp, _dp]),
             "orc_so3_forward_complex_slices": (None, [i, _dp, _dp, i, i]),
             "orc_so3_inverse_complex_slices": (None, [i, _dp, _dp, i, i]),
+            "orc_so3_forward_complex_strided": (None, [i, _dp, _dp, i, i, i]),
+            "orc_so3_inverse_complex_strided": (None, [i, _dp, _dp, i, i, i]),
             "orc_so3_inverse_real_grid": (None, [i, _dp, _dp]),
             "orc_so3_real_to_complex": (None, [i, _dp, _dp]),
             "orc_s2_forward_complex": (None, [i, _dp, i, _dp]),
@@ -217,6 +219,28 @@ def so3_inverse_complex_slices(l_max: int, F: np.ndarray, k0: int, k1: int) -> n
     F = np.ascontiguousarray(F, dtype=np.complex128)
     g = np.zeros((k1 - k0, N, N), dtype=np.complex128)
     lib().orc_so3_inverse_complex_slices(l_max, _p(F.view(np.float64)), _p(g.view(np.float64)), k0, k1)
+    return g
+
+
+def so3_forward_complex_strided(l_max: int, slab: np.ndarray, k0: int, kstride: int) -> np.ndarray:
+    """Contribution of the beta slices k0 + i kstride (slab[i], i < len(slab)) to the complex forward sum;
+    CPU timing samples spread over [0, pi)."""
+    N = 2 * (l_max + 1)
+    g = np.ascontiguousarray(slab, dtype=np.complex128)
+    assert g.ndim == 3 and g.shape[1:] == (N, N) and k0 + (g.shape[0] - 1) * kstride < N
+    F = np.zeros(so3_ncoeff(l_max), dtype=np.complex128)
+    lib().orc_so3_forward_complex_strided(l_max, _p(g.view(np.float64)), _p(F.view(np.float64)), k0, kstride,
+                                          g.shape[0])
+    return F
+
+
+def so3_inverse_complex_strided(l_max: int, F: np.ndarray, k0: int, kstride: int, count: int) -> np.ndarray:
+    """Grid synthesis of the beta slices k0 + i kstride, i < count: (count, N, N) complex."""
+    N = 2 * (l_max + 1)
+    assert k0 + (count - 1) * kstride < N
+    F = np.ascontiguousarray(F, dtype=np.complex128)
+    g = np.zeros((count, N, N), dtype=np.complex128)
+    lib().orc_so3_inverse_complex_strided(l_max, _p(F.view(np.float64)), _p(g.view(np.float64)), k0, kstride, count)
     return g
 
 
