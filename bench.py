@@ -1,24 +1,29 @@
 #!/usr/bin/env python
 """Benchmark: SO(3) forward+inverse transform pairs per second at l_max = 255.
 
-Workload (default): a batch of complex SO(3) functions at l_max = 255 (512^3
-Euler grid each, complex64 samples; synthetic seeded coefficients
-F ~ N(0,1)(l+1)^-1.5), transformed with the tensor-core split-BF16 path
-(FFTSO3_PREC_TC_BF16X3, stable Wigner-d recursion).  One step = inverse of the
-whole batch (coefficients -> grids) + forward of the whole batch
-(grids -> coefficients); value = functions / step time.  The library runs
-on one GPU (no sharding, no collectives): launched with more than one rank,
-rank 0 prints a line saying so and no GPU work is done.
+Headline (the first JSON line): a batch of 32 complex SO(3) functions at
+l_max = 255 (512^3 Euler grid each, complex64 samples; synthetic seeded
+coefficients F ~ N(0,1)(l+1)^-1.5), stable Wigner-d recursion.  One step =
+inverse of the whole batch on the tensor cores (split-BF16) + refined forward
+of the whole batch (split-BF16 forward, then one residual step
+F += forward(f - inverse(F)) whose inverse is exact on the tensor cores), the
+configuration that meets rel-err <= 1e-6 per degree against FP64; value =
+functions / step time.  Reported beside it: the plain split-BF16 step, the
+plain FP64 GPU path, the FP32 CUDA-core form, the accuracy against FP64, the
+end-to-end rate through the host-buffer C-ABI calls, the roofline of the
+dominant stage (CUDA-event stage timing inside the library) and of the whole
+step, and the CPU baseline: the oracle's restatement of the reference
+algorithm on beta slices spread over [0, pi), at all host threads and at one.
 
-Also reported: the plain FP64 GPU path on the same l_max (pairs/s), the
-accuracy of the tensor-core path against FP64, the end-to-end rate through the
-host-buffer C-ABI calls, the roofline of the dominant kernel (stage timing
-with CUDA events inside the library), and the CPU baseline: the oracle's
-restatement of the reference algorithm timed on the host cores on a bounded
-sample of beta slices.
+Then (--workload all, the default) one line per other configuration: the
+plain FP64 path at l_max = 127, 4096 real functions of uneven bandwidth, 256
+complex functions at l_max = 96, and 512 real S^2 signals at l_max = 511,
+each with its accuracy, roofline and CPU baseline.
 
---impl reference times only that CPU algorithm (all host threads) on the same
-workload and prints its own JSON line.
+The library runs on one GPU (no sharding, no collectives): launched with more
+than one rank, rank 0 prints a line saying so and no GPU work is done.
+--impl reference times only the CPU algorithm (all host threads) on the
+headline workload and prints its own JSON line.
 """
 from __future__ import annotations
 
@@ -228,7 +233,7 @@ def uneven_lmax(n: int, seed: int = 3) -> np.ndarray:
     return rng.integers(8, 65, size=n)
 
 
-def main_uneven(args) -> None:
+def uneven_line(args) -> dict:
     """The batching workload: n real SO(3) functions with l_max drawn uniformly
     from {8..64}, FP32 samples, coefficients N(0,1)/(2l+1); one fftso3_batch
     (tensor-core buckets, CUDA graph).  Compared with a per-function launch loop
@@ -268,7 +273,7 @@ def main_uneven(args) -> None:
     bt.check()
 
     # accuracy on a sample of functions against the FP64 plain path on the same FP32 samples
-    acc_rms, acc_idx = [], []
+    acc_rms, acc_max, acc_idx = [], [], []
     plans64 = {}
     bt.forward(grid.data_ptr(), coef_out.data_ptr(), sp)
     for i in np.linspace(0, n - 1, 8).astype(int):
@@ -281,6 +286,7 @@ def main_uneven(args) -> None:
         torch.cuda.synchronize()
         a = coef_out[c0:c0 + p.coeff_elems].double()
         acc_rms.append(float(torch.linalg.norm(a - ci) / torch.linalg.norm(ci)))
+        acc_max.append(per_l_errors(a.cpu().numpy(), ci.cpu().numpy(), L)[1])
         acc_idx.append(int(i))
     bt.check()
 
@@ -355,6 +361,50 @@ def main_uneven(args) -> None:
         fp64 = {"value": n * 1000.0 / ms64, "unit": UNIT, "ms_per_step": ms64,
                 "note": "per-function launch loop, FFTSO3_REAL FP64 plans (batch 1, one per l_max), float64 samples"}
         del g64, c64, go64, co64
+    # roofline of the dominant stage of the eager step: FFT stages against HBM (one complex64 read + write of the
+    # work grid per pass, both directions, summed over the buckets that use the stage), GEMMs against BF16
+    top, (top_ms, _) = max(st_all.items(), key=lambda kv: kv[1][0])
+    bsz = {}
+    for k in range(bt.buckets):
+        Lb, cnt = bt.bucket_info(k)
+        bsz[Lb] = cnt
+    if top.startswith("tc_gemm"):
+        fl = sum(8.0 * (Lb + 1) * ((Lb + 1) * (4 * (Lb + 1) ** 2 - 1) // 3) * c for Lb, c in bsz.items()
+                 if top in dict((L2, d) for _, L2, _, d in per_bucket).get(Lb, {}))
+        ach = fl / (top_ms / 1000.0) / 1e12
+        roof = {"bound": "tensor", "unit": "TFLOP/s", "achieved": ach, "peak": peaks["bf16_tflops_sustained"],
+                "frac": ach / peaks["bf16_tflops_sustained"], "algorithmic": "8 B C useful flops per function"}
+    else:
+        byts = sum(2 * 16.0 * (2 * (Lb + 1)) ** 3 * c for Lb, c in bsz.items()
+                   if top in dict((L2, d) for _, L2, _, d in per_bucket).get(Lb, {}))
+        ach = byts / (top_ms / 1000.0) / 1e9
+        roof = {"bound": "hbm", "unit": "GB/s", "achieved": ach, "peak": peaks["hbm_gbs"],
+                "frac": ach / peaks["hbm_gbs"],
+                "algorithmic": "one complex64 read + write of each bucket's work grid per pass, both directions"}
+    roof.update({"kernel": top, "ms_per_step": top_ms, "peak_source": peaks["source"], "traffic": None,
+                 "share_of_eager_step": top_ms / sum(v for v, _ in st_all.values())})
+    # CPU baseline: the oracle (the reference algorithm restated) on functions spread over the batch
+    cpu = None
+    if not args.no_cpu:
+        from oracle import oracle as O
+
+        O.build()
+        nth = os.cpu_count() or 1
+        O.set_num_threads(nth)
+        idx = np.linspace(0, n - 1, 8).astype(int)
+        t_sum = 0.0
+        for i in idx:
+            Li = int(lmax[i])
+            Fi = coef[bt.coeff_offset(i):bt.coeff_offset(i) + (Li + 1) * (4 * (Li + 1) ** 2 - 1) // 3].double().cpu().numpy()
+            t0 = time.perf_counter()
+            gi = O.so3_inverse_real_grid(Li, Fi)
+            O.so3_forward_real(Li, gi)
+            t_sum += time.perf_counter() - t0
+        cpu = {"value": len(idx) / t_sum, "unit": UNIT, "cores": nth, "kind": "port",
+               "sample": f"{len(idx)} functions spread over the batch (l_max {sorted(int(lmax[i]) for i in idx)}), "
+                         f"real inverse on the grid + real forward each (oracle restatement of "
+                         f"fdcl_FFTSO3.cpp:774-850 / :1141-1167, OpenMP over beta slices, {nth} threads); pairs/s "
+                         f"per function"}
     line = {
         "metric": UNEVEN_METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -368,13 +418,15 @@ def main_uneven(args) -> None:
                    "l2": "inputs larger than L2"},
         "io_gbs": io_bytes / (ms / 1000.0) / 1e9, "io_frac_of_hbm": io_bytes / (ms / 1000.0) / 1e9 / peaks["hbm_gbs"],
         "batch_create_s": t_create, "device_gb": bt.device_bytes / 1e9,
-        "accuracy": {"rel_rms_vs_fp64_max": max(acc_rms), "functions": acc_idx},
+        "accuracy": {"rel_rms_vs_fp64_max": max(acc_rms), "rel_max_per_l_vs_fp64_max": max(acc_max),
+                     "functions": acc_idx, "against": "FP64 GPU plans (FFTSO3_REAL) on the same FP32 samples"},
+        "roofline": roof, "cpu_baseline": cpu,
         "fp64_loop": fp64, "speedup_vs_fp64_loop": value / fp64["value"] if fp64 else None,
         "clocks": clocks, "gpu_launches": launches * args.steps,
         "stages_eager_sum_ms": stage_summary, "eager_timed_step_ms": eager_ms,
         "top_buckets": [{"l_max": L, "functions": c, "ms": t, "stages": d} for t, L, c, d in per_bucket[:6]],
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 # --------------------------------------------------------------- FP64 plain path
@@ -382,7 +434,7 @@ def main_uneven(args) -> None:
 FP64_METRIC = "SO(3) FP64 fwd+inv transforms/s at l_max={L}: plain FP64 GPU path (complex and real)"
 
 
-def main_fp64(args) -> None:
+def fp64_line(args) -> dict:
     """The plain FP64 GPU path (FFTSO3_PREC_FP64, reference recursion) on one function at
     l_max = 127 (256^3 grid), complex and real: transform pairs/s, HBM GB/s of the FFT passes
     and of the table generation (plan creation), FP64 rate of the beta-sum."""
@@ -455,13 +507,59 @@ def main_fp64(args) -> None:
                      "stages_ms": {k: v for k, (v, _) in st.items()}, "grid_elem_bytes": esz}
         del p, c, g, c2
         torch.cuda.empty_cache()
+    # roofline of the complex step's dominant stage: an FFT pass against HBM, or the contraction against FP64
+    peaks = measured_peaks()
+    cx = out["complex"]
+    top = max(cx["stages_ms"].items(), key=lambda kv: kv[1])[0]
+    if top in cx["fft"]:
+        gbs = cx["fft"][top]["gbs"]
+        roof = {"bound": "hbm", "unit": "GB/s", "kernel": f"fft_lines_kernel (FP64, {top})", "achieved": gbs,
+                "peak": peaks["hbm_gbs"], "frac": gbs / peaks["hbm_gbs"], "peak_source": peaks["source"],
+                "ms_per_launch": cx["fft"][top]["ms_per_launch"], "traffic": None,
+                "algorithmic": "one complex128 read + write of the grid per pass"}
+    else:
+        tf = cx["contraction"][top]["fp64_tflops"]
+        roof = {"bound": "fp64", "unit": "TFLOP/s", "kernel": top, "achieved": tf, "peak": FP64_NOMINAL_TFLOPS,
+                "frac": tf / FP64_NOMINAL_TFLOPS, "peak_source": "nominal FP64 (no measured FP64 peak)",
+                "ms_per_launch": cx["contraction"][top]["ms_per_launch"], "traffic": None,
+                "algorithmic": "8 B C flops per direction"}
+    # parity with the reference's algorithm: the oracle (CPU restatement) on one complex function
+    parity = None
+    if not args.no_accuracy:
+        from oracle import oracle as O
+
+        O.build()
+        O.set_num_threads(os.cpu_count() or 1)
+        rng = np.random.Generator(np.random.PCG64(7))
+        l = np.concatenate([np.full((2 * x + 1) ** 2, x) for x in range(B)])
+        F = (rng.standard_normal(C) + 1j * rng.standard_normal(C)) / (2 * l + 1)
+        g_or = O.so3_inverse_complex_grid(L, F)
+        F_or = O.so3_forward_complex(L, g_or)
+        p = _lib.Plan(_lib.SO3_COMPLEX, L, 1, "fp64", "reference")
+        c = torch.from_numpy(F).to(dev)
+        g = torch.empty(N ** 3, dtype=torch.complex128, device=dev)
+        p.inverse(c.data_ptr(), g.data_ptr(), sp)
+        gin = torch.from_numpy(np.ascontiguousarray(g_or).ravel()).to(dev)
+        c2 = torch.empty_like(c)
+        p.forward(gin.data_ptr(), c2.data_ptr(), sp)
+        torch.cuda.synchronize()
+        p.check()
+        gg = g.cpu().numpy().reshape(N, N, N)
+        rf, mf = per_l_errors(c2.cpu().numpy(), F_or, L)
+        parity = {"inverse_rel_rms": float(np.linalg.norm(gg - g_or) / np.linalg.norm(g_or)),
+                  "forward_rel_rms": rf, "forward_rel_max_per_l": mf,
+                  "against": "the oracle (reference algorithm restated in C, FP64, reference recursion) on one "
+                             "complex function, coefficients N(0,1)/(2l+1)"}
+        del p, c, g, gin, c2
+    cpu = cpu_baselines(L) if not args.no_cpu else None
     line = {"metric": FP64_METRIC.format(L=L), "value": out["complex"]["pairs_per_s"], "unit": UNIT, "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["complex"]["ms_per_pair"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": f"one SO(3) function, l_max={L} ({N}^3 grid), FP64, reference recursion; "
                                    "coefficients N(0,1)/(2l+1)"},
+            "roofline": roof, "accuracy": parity, "cpu_baseline": cpu,
             "complex": out["complex"], "real": out["real"]}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 # --------------------------------------------------------------- point evaluation
@@ -643,7 +741,7 @@ def main_fft(args) -> None:
 S2_METRIC = "S2 real fwd+inv transforms/s, {b} signals at l_max={L}: TC split-BF16 vs FP64"
 
 
-def main_s2(args) -> None:
+def s2_line(args) -> dict:
     """512 real S^2 signals at l_max = 511 (1024 x 1024 grids, FP32 samples,
     coefficients N(0,1)/(l+1)) through one FFTS2_real tensor-core plan."""
     import torch
@@ -753,6 +851,43 @@ def main_s2(args) -> None:
             t = stages[name][0] / stages[name][1] / 1000.0
             fft[name] = {"ms": t * 1000.0, "gbs": fft_bytes / t / 1e9, "frac_of_hbm": fft_bytes / t / 1e9 / peaks["hbm_gbs"]}
     value = b * 1000.0 / ms
+    # roofline of the dominant stage of one eager step
+    top, (top_ms, top_n) = max(stages.items(), key=lambda kv: kv[1][0])
+    if top in gemm:
+        roof = {"bound": "tensor", "unit": "TFLOP/s", "achieved": gemm[top]["tflops"],
+                "peak": peaks["bf16_tflops_sustained"], "frac": gemm[top]["frac_of_bf16"],
+                "algorithmic": "4 N B^2 useful flops per signal"}
+    elif top in fft:
+        roof = {"bound": "hbm", "unit": "GB/s", "achieved": fft[top]["gbs"], "peak": peaks["hbm_gbs"],
+                "frac": fft[top]["frac_of_hbm"], "algorithmic": "real samples (4 B) + complex pencils (8 B) per pass"}
+    else:
+        roof = {"bound": "hbm", "unit": "GB/s", "achieved": None, "peak": peaks["hbm_gbs"], "frac": None}
+    roof.update({"kernel": top, "ms_per_launch": top_ms / top_n, "peak_source": peaks["source"], "traffic": None,
+                 "share_of_eager_step": top_ms / sum(v for v, _ in stages.values())})
+    # per-degree error of the forward (rel_max = max_l max_m |a - b| / rms_m |b|)
+    a0 = coef_out[0].double().cpu().numpy()
+    b0 = F64.cpu().numpy()
+    mx = 0.0
+    for ll in range(B):
+        sl = slice(ll * ll, (ll + 1) * (ll + 1))
+        mx = max(mx, float(np.abs(a0[sl] - b0[sl]).max() / np.sqrt(np.mean(b0[sl] ** 2))))
+    acc["forward_rel_max_per_l"] = mx
+    # CPU baseline: the oracle on one signal (real inverse on the grid + real forward)
+    cpu = None
+    if not args.no_cpu:
+        from oracle import oracle as O
+
+        O.build()
+        nth = os.cpu_count() or 1
+        O.set_num_threads(nth)
+        Fs = coef[0].double().cpu().numpy()
+        t0 = time.perf_counter()
+        gs = O.s2_inverse_real_grid(L, Fs)
+        O.s2_forward_real(L, gs)
+        dt = time.perf_counter() - t0
+        cpu = {"value": 1.0 / dt, "unit": UNIT, "cores": nth, "kind": "port",
+               "sample": f"one signal at l_max={L}: real inverse on the grid + real forward (oracle restatement of "
+                         f"fdcl_FFTS2.cpp:424-436 / :500-512, OpenMP over theta, {nth} threads)"}
     line = {
         "metric": S2_METRIC.format(b=b, L=L), "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -761,14 +896,288 @@ def main_s2(args) -> None:
                                "N(0,1)/(l+1); FFTS2_real tensor-core plan", "signals": b, "l_max": L,
                    "l2": "inputs larger than L2 (2 GB of samples)"},
         "accuracy": acc, "fp64_path": fp64, "speedup_vs_fp64_path": value / fp64["value"],
-        "gemm": gemm, "fft": fft,
+        "roofline": roof, "cpu_baseline": cpu, "gemm": gemm, "fft": fft,
         "stages": {k: {"ms": v, "launches": c} for k, (v, c) in stages.items()},
         "gpu_launches": int(sum(c for _, c in stages.values())) * args.steps, "clocks": clocks,
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 # --------------------------------------------------------------- GPU arm
+
+def stage_roofline(name: str, tot_ms: float, cnt: int, L: int, b: int, chunk: int, peaks: dict):
+    """Achieved rate of one stage of an SO(3) complex tensor-core plan from its CUDA-event time, against the
+    measured peak: algorithmic bytes (HBM-bound stages) or useful flops (contractions) per timed record."""
+    B, N = L + 1, 2 * (L + 1)
+    C = B * (4 * B * B - 1) // 3
+    per = tot_ms / cnt / 1000.0
+    grid8 = 8.0 * b * N ** 3
+    flops = None
+    if name.startswith("tc_gemm"):
+        flops, alg = 8.0 * B * C * b, "8 B C useful flops per function per launch (6 split-BF16 products issued)"
+    elif name == "refine_inverse_contract":
+        flops, alg = 8.0 * B * C * chunk, "8 B C useful flops per function of the chunk (10 digit products issued)"
+    if flops is not None:
+        ach = flops / per / 1e12
+        return {"bound": "tensor", "unit": "TFLOP/s", "kernel": name, "achieved": ach,
+                "peak": peaks["bf16_tflops_sustained"], "frac": ach / peaks["bf16_tflops_sustained"],
+                "peak_source": peaks["source"] + " (sustained bf16)", "ms_per_launch": per * 1000.0,
+                "algorithmic": alg}
+    if name == "fft_2d":
+        byts, alg = 2 * grid8, "one complex64 read + write of every sample per launch (both FFT passes, L2 ring)"
+    elif name in ("fft_rows", "fft_cols", "tc_pack_fwd", "tc_pack_inv"):
+        byts, alg = 2 * grid8, "one complex64 read + write of every sample per pass"
+    elif name == "refine_inverse_fft":
+        byts, alg = 2 * 2 * 16.0 * chunk * N ** 3, "two double-float passes, 16 B read + written per sample each"
+    elif name == "basis_convert":
+        byts, alg = 2 * 8.0 * C * b, "one complex64 read + write of the coefficients"
+    else:
+        byts, alg = None, "mixed elementwise work"
+    ach = byts / per / 1e9 if byts else None
+    return {"bound": "hbm", "unit": "GB/s", "kernel": name, "achieved": ach, "peak": peaks["hbm_gbs"],
+            "frac": ach / peaks["hbm_gbs"] if ach else None, "peak_source": peaks["source"],
+            "ms_per_launch": per * 1000.0, "algorithmic": alg}
+
+
+def so3_tc_line(args, L: int, b: int, full: bool = True) -> dict:
+    """One SO(3) complex batch on the tensor cores: b functions at l_max = L, one step = inverse + forward of
+    the batch.  full (the headline): the forward carries the residual refinement (FFTSO3_FLAG_REFINE), so the
+    step meets rel-err <= 1e-6 under the per-degree metric; the end-to-end host-buffer rate, the plain
+    split-BF16 step and the FP32 CUDA-core form are reported beside it.  Otherwise (full = False) the plain
+    split-BF16 step with its accuracy against FP64, the FP64 path, roofline and CPU baseline."""
+    import torch
+
+    import fftso3_gb300 as fg
+    from fftso3_gb300 import _lib
+    from fftso3_gb300 import build as fbuild
+
+    fbuild.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    N = 2 * (L + 1)
+    B = L + 1
+    C = fg.so3_ncoeff(L)
+    peaks = measured_peaks()
+
+    def ev():
+        return torch.cuda.Event(enable_timing=True)
+
+    # ---- FP64 plain path: reference data for the accuracy checks (function 0) and its own rate
+    F0 = seeded_coeffs(L, 0)
+    fp64 = None
+    have_ref = not args.no_accuracy
+    g0_c64 = F0_fp64 = g0_ref = None
+    if have_ref:
+        p64 = _lib.Plan(_lib.SO3_COMPLEX, L, 1, "fp64", "stable")
+        c64 = torch.from_numpy(F0).to(dev)
+        g64 = torch.empty(N ** 3, dtype=torch.complex128, device=dev)
+        o64 = torch.empty_like(c64)
+        p64.inverse(c64.data_ptr(), g64.data_ptr(), sp)
+        p64.forward(g64.data_ptr(), o64.data_ptr(), sp)
+        torch.cuda.synchronize()
+        F0_fp64 = o64.cpu().numpy()  # FP64 forward of the FP64 synthesis
+        g0_c64 = g64.to(torch.complex64)
+        g0_ref = g64.cpu().numpy()
+        if not args.no_fp64:
+            reps = 2
+            e0, e1 = ev(), ev()
+            e0.record(stream)
+            for _ in range(reps):
+                p64.inverse(c64.data_ptr(), g64.data_ptr(), sp)
+                p64.forward(g64.data_ptr(), o64.data_ptr(), sp)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms64 = e0.elapsed_time(e1) / reps
+            fp64 = {"value": 1000.0 / ms64, "unit": UNIT, "ms_per_pair": ms64, "batch": 1,
+                    "note": "plain FP64 GPU path (FFTSO3_PREC_FP64, stable recursion), same l_max"}
+        del p64, g64, o64, c64
+        torch.cuda.empty_cache()
+
+    # ---- inputs: b seeded band-limited functions (function 0: the FP64 synthesis, rounded to complex64)
+    Fb = np.concatenate([seeded_coeffs(L, i) for i in range(b)]).astype(np.complex64)
+    coef = torch.from_numpy(Fb).to(dev)
+    grid = torch.empty(b * N ** 3, dtype=torch.complex64, device=dev)
+    coef_out = torch.empty_like(coef)
+    grid_out = torch.empty_like(grid)
+
+    def accuracy(plan):
+        """forward of function 0's complex64 grid and inverse of its coefficients, against FP64"""
+        coef_in = coef.clone()
+        coef_in[:C].copy_(torch.from_numpy(F0.astype(np.complex64)).to(dev))
+        plan.forward(grid.data_ptr(), coef_out.data_ptr(), sp)
+        plan.inverse(coef_in.data_ptr(), grid_out.data_ptr(), sp)
+        torch.cuda.synchronize()
+        plan.check()
+        fr, fm = per_l_errors(coef_out[:C].cpu().numpy().astype(np.complex128), F0_fp64, L)
+        gi = grid_out[:N ** 3].cpu().numpy().astype(np.complex128)
+        ir = float(np.linalg.norm(gi - g0_ref) / np.linalg.norm(g0_ref))
+        im = float(np.abs(gi - g0_ref).max() / np.sqrt(np.mean(np.abs(g0_ref) ** 2)))
+        del coef_in
+        return {"forward_rel_rms": fr, "forward_rel_max_per_l": fm, "inverse_rel_rms": ir, "inverse_rel_max": im}
+
+    def timed(plan, steps, warmup, clocks=False):
+        for _ in range(warmup):
+            plan.inverse(coef.data_ptr(), grid_out.data_ptr(), sp)
+            plan.forward(grid.data_ptr(), coef_out.data_ptr(), sp)
+        torch.cuda.synchronize()
+        plan.set_timing(True)
+        plan.stage_times(reset=True)
+        e0, e1 = ev(), ev()
+        clk = ClockSampler(0) if clocks else None
+        if clk:
+            clk.__enter__()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(steps):
+            plan.inverse(coef.data_ptr(), grid_out.data_ptr(), sp)
+            plan.forward(grid.data_ptr(), coef_out.data_ptr(), sp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if clk:
+            clk.__exit__(None, None, None)
+        t = e0.elapsed_time(e1) / steps
+        st = plan.stage_times(reset=True)
+        plan.set_timing(False)
+        plan.check()
+        return t, st, (clk.summary() if clk else None)
+
+    # ---- the measured plan: refined forward (headline) or plain split-BF16
+    flags = _lib.FLAG_AUTOTUNE | (_lib.FLAG_REFINE if full else 0)
+    plan = _lib.Plan(_lib.SO3_COMPLEX, L, b, "tc_bf16x3", "stable", flags)
+    chunk = min(b, 8)  # functions per refinement chunk (the library's choice at these sizes)
+    plan.inverse(coef.data_ptr(), grid.data_ptr(), sp)  # synthetic band-limited FP32 samples
+    if have_ref:
+        grid[:N ** 3].copy_(g0_c64)
+    torch.cuda.synchronize()
+    plan.check()
+    acc = accuracy(plan) if have_ref else {}
+    if have_ref:
+        acc["against"] = "FP64 GPU path (stable recursion) on the same function (function 0 of the batch)"
+        if full:  # the names of the refined forward's figures
+            acc["refined_forward_rel_rms"] = acc["forward_rel_rms"]
+            acc["refined_forward_rel_max_per_l"] = acc["forward_rel_max_per_l"]
+    ms, stages, clocks = timed(plan, args.steps, args.warmup, clocks=True)
+    value = b * 1000.0 / ms
+    nrec = int(sum(c for _, c in stages.values()))
+    # kernels in the timed region: one per timed record, plus the second kernel of the records that hold two
+    # (the double-float FFT's two passes; the coefficient gather with the Nyquist zeroing), one each per chunk
+    launches = nrec + 2 * int(stages.get("refine_inverse_fft", (0, 0))[1])
+    tot = sum(v for v, _ in stages.values())
+    stage_summary = {k: {"ms_per_launch": v / c, "launches": c, "share": v / tot} for k, (v, c) in stages.items()}
+    top, (top_ms, top_n) = max(stages.items(), key=lambda kv: kv[1][0])
+    roof = stage_roofline(top, top_ms, top_n, L, b, chunk, peaks)
+    roof["traffic"] = profiled_traffic(top, L, b)
+    roof["share_of_step"] = top_ms / tot
+
+    # ---- the step against its floors: HBM (algorithmic bytes of every stage) and tensor (issued MMA flops)
+    Kp = (N + 63) // 64 * 64
+    table_rows = sum((2 * m + 1) * (B - m) for m in range(B))
+    table_b = 3 * 2.0 * Kp * table_rows        # three BF16 planes, read once per split-BF16 GEMM launch
+    coef_b = 8.0 * b * C
+    grid_b = 8.0 * b * N ** 3
+    useful = 8.0 * B * C * b
+    tc_dir = 2 * grid_b + (grid_b + table_b + coef_b) + 2 * coef_b  # FFT + GEMM + permutation, one direction
+    step_bytes = 2 * tc_dir
+    tensor_flops = 2 * 6 * useful
+    if full:
+        nchunks = (b + chunk - 1) // chunk
+        oz_table = nchunks * 4 * 2.0 * Kp * table_rows   # digit planes, read once per chunk launch
+        step_bytes += (tc_dir                                     # forward of the residual
+                       + coef_b + 2 * 16.0 * b * C                 # gather: coefficients in, double-float runs out
+                       + oz_table + 16.0 * b * C + 2 * grid_b      # exact contraction: table, runs, pencils out
+                       + 4 * 2 * grid_b                            # double-float FFT: 2 passes, 16 B r + w
+                       + 2 * grid_b + 2 * grid_b                   # residual: grid + samples in, residual out
+                       + 3 * coef_b)                               # correction added
+        tensor_flops += 6 * useful + 10 * useful
+    hbm_floor_ms = step_bytes / (peaks["hbm_gbs"] * 1e9) * 1e3
+    tensor_floor_ms = tensor_flops / (peaks["bf16_tflops_sustained"] * 1e12) * 1e3
+    floor_ms = max(hbm_floor_ms, tensor_floor_ms)
+    step_roof = {"bound": "hbm" if hbm_floor_ms >= tensor_floor_ms else "tensor", "algorithmic_bytes": step_bytes,
+                 "hbm_floor_ms": hbm_floor_ms, "tensor_floor_ms": tensor_floor_ms, "ms_per_step": ms,
+                 "frac": floor_ms / ms, "peak_source": peaks["source"],
+                 "note": "split-BF16 directions: FFT 2 x grid bytes, GEMM pencils + BF16 table + coefficients, "
+                         "permutation 2 x coefficients" + ("; refinement: the residual's forward, the exact "
+                                                           "inverse (digit planes per chunk, double-float runs "
+                                                           "and pencils), its two double-float FFT passes, the "
+                                                           "residual and the correction" if full else "")}
+
+    # ---- end to end through the host-buffer C ABI (pinned host memory), the same plan and step count
+    e2e = None
+    if full and not args.no_e2e:
+        hg = torch.empty(b * N ** 3, dtype=torch.complex64, pin_memory=True)
+        hg.copy_(grid)
+        hc = torch.empty(b * C, dtype=torch.complex64, pin_memory=True)
+        hc.copy_(coef)
+        hco = torch.empty_like(hc, pin_memory=True)
+        # the inverse writes the grid the forward then reads (one pinned grid buffer)
+        plan.inverse_host(hc.data_ptr(), hg.data_ptr(), sp)
+        plan.forward_host(hg.data_ptr(), hco.data_ptr(), sp)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            plan.inverse_host(hc.data_ptr(), hg.data_ptr(), sp)
+            plan.forward_host(hg.data_ptr(), hco.data_ptr(), sp)
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / args.steps
+        e2e = {"value": b / dt, "unit": UNIT, "h2d_bytes_per_step": int(8 * b * C + 8 * b * N ** 3),
+               "d2h_bytes_per_step": int(8 * b * N ** 3 + 8 * b * C), "steps": args.steps}
+        del hg, hc, hco
+    plan.close()
+    del plan
+    torch.cuda.empty_cache()
+
+    # ---- beside the headline: the plain split-BF16 step (no refinement) and the FP32 CUDA-core form
+    plain = fp32 = None
+    if full:
+        pp = _lib.Plan(_lib.SO3_COMPLEX, L, b, "tc_bf16x3", "stable", _lib.FLAG_AUTOTUNE)
+        pacc = accuracy(pp) if have_ref else {}
+        pms, pst, _ = timed(pp, args.steps, min(args.warmup, 3))
+        ptop, (ptop_ms, ptop_n) = max(pst.items(), key=lambda kv: kv[1][0])
+        proof = stage_roofline(ptop, ptop_ms, ptop_n, L, b, chunk, peaks)
+        proof["traffic"] = profiled_traffic(ptop, L, b)
+        plain = {"value": b * 1000.0 / pms, "unit": UNIT, "ms_per_step": pms, "accuracy": pacc, "roofline": proof,
+                 "stages": {k: {"ms_per_launch": v / c, "launches": c} for k, (v, c) in pst.items()},
+                 "note": "split-BF16 forward and inverse without the residual step: its forward meets 1e-6 as "
+                         "rel_rms but not per degree (rel_max)"}
+        pp.close()
+        del pp
+        torch.cuda.empty_cache()
+        if not args.no_fp32:
+            p32 = _lib.Plan(_lib.SO3_COMPLEX, L, b, "fp32", "stable")
+            a32 = accuracy(p32) if have_ref else {}
+            ms32, _, _ = timed(p32, 1, 1)
+            fp32 = {"value": b * 1000.0 / ms32, "unit": UNIT, "ms_per_step": ms32, "accuracy": a32,
+                    "note": "FFTSO3_PREC_FP32: FP32 table and FMA accumulation on the CUDA cores, same batch"}
+            p32.close()
+            del p32
+            torch.cuda.empty_cache()
+
+    cpu = cpu_baselines(L) if not args.no_cpu else None
+    metric = METRIC if L == 255 else METRIC.replace("l_max=255", f"l_max={L}")
+    what = ("inverse (split-BF16) + refined forward (split-BF16, then one residual step with the inverse exact on "
+            "the tensor cores)" if full else "inverse + forward, split-BF16")
+    line = {
+        "metric": metric, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16x3 (split) / fp32 accumulate / fp32 FFT" +
+                                      ("; residual step: exact BF16 digit products, double-float FFT" if full else ""),
+        "data": "synthetic",
+        "config": {"workload": f"SO(3) complex, l_max={L}, batch={b} functions ({N}^3 complex64 grid each), stable "
+                               f"recursion; one step = {what}",
+                   "l_max": L, "batch": b, "precision": "tc_bf16x3" + (" + refine" if full else ""),
+                   "l2": f"inputs larger than L2 ({8.0 * b * N ** 3 / 1e9:.1f} GB of complex64 grids)"},
+        "e2e": e2e, "gpu_launches": launches, "roofline": roof, "step_roofline": step_roof,
+        "stages": stage_summary, "accuracy": acc, "fp64_path": fp64,
+        "speedup_vs_fp64_path": value / fp64["value"] if fp64 else None,
+        "clocks": clocks, "cpu_baseline": cpu,
+    }
+    if full:
+        line["unrefined_path"] = plain
+        line["fp32_cuda_core_path"] = fp32
+    return line
+
 
 def main() -> None:
     ap = argparse.ArgumentParser()
@@ -783,9 +1192,13 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp32", action="store_true", help="skip the FP32 CUDA-core beta-sum comparison")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64 reference (profiling runs)")
-    ap.add_argument("--workload", default="lmax255", choices=["lmax255", "uneven", "s2", "fp64", "fft", "points"],
-                    help="lmax255: the headline SO(3) batch at one l_max (--l-max/--batch); uneven: the "
-                         "mixed-bandwidth SO(3) batch; s2: the S^2 batch at l_max=511")
+    ap.add_argument("--workload", default="all",
+                    choices=["all", "lmax255", "uneven", "s2", "fp64", "lmax96", "fft", "points"],
+                    help="all (default): the headline line (SO(3) l_max=255 batch) first, then one line per other "
+                         "configuration (fp64, uneven, lmax96, s2); lmax255: the headline SO(3) batch at one l_max "
+                         "(--l-max/--batch) alone; uneven: the mixed-bandwidth SO(3) batch; s2: the S^2 batch at "
+                         "l_max=511; fp64: the plain FP64 path at l_max=127; lmax96: 256 complex SO(3) functions at "
+                         "l_max=96")
     ap.add_argument("--functions", type=int, default=4096, help="uneven workload: number of functions")
     ap.add_argument("--s2-l-max", type=int, default=511, help="s2 workload: l_max")
     ap.add_argument("--fp64-l-max", type=int, default=127, help="fp64 workload: l_max")
@@ -807,297 +1220,43 @@ def main() -> None:
                                              "or collectives; the headline is measured with --gpus 1"}),
                   flush=True)
         return
-    if args.workload == "uneven":
-        main_uneven(args)
-        return
-    if args.workload == "s2":
-        main_s2(args)
-        return
-    if args.workload == "fp64":
-        main_fp64(args)
-        return
     if args.workload == "fft":
         main_fft(args)
         return
     if args.workload == "points":
         main_points(args)
         return
+    run_workload(args)
 
+
+CONFIG_LINES = {
+    "fp64": lambda a: fp64_line(a),
+    "uneven": lambda a: uneven_line(a),
+    "lmax96": lambda a: so3_tc_line(a, 96, 256, full=False),
+    "s2": lambda a: s2_line(a),
+}
+
+
+def run_workload(args) -> None:
+    """The headline line first (the one the driver parses); with --workload all, then one line per other
+    configuration, each freeing its GPU memory before the next (a failure there prints an error line)."""
+    import gc
+
+    if args.workload not in ("all", "lmax255"):
+        print(json.dumps(CONFIG_LINES[args.workload](args)), flush=True)
+        return
+    print(json.dumps(so3_tc_line(args, args.l_max, args.batch, full=True)), flush=True)
+    if args.workload != "all":
+        return
     import torch
 
-    import fftso3_gb300 as fg
-    from fftso3_gb300 import _lib
-    from fftso3_gb300 import build as fbuild
-
-    fbuild.build()
-    rank = 0
-    local = 0
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    stream = torch.cuda.current_stream()
-    sp = stream.cuda_stream
-    L, b = args.l_max, args.batch
-    N = 2 * (L + 1)
-    C = fg.so3_ncoeff(L)
-
-    def barrier():
-        torch.cuda.synchronize()
-
-    # ---- FP64 plain path: reference data for the accuracy check + its own rate
-    F0 = seeded_coeffs(L, 1000 * rank)
-    fp64 = None
-    acc = {}
-    if args.no_accuracy:
-        args.no_fp64 = True
-    p64 = None if args.no_accuracy else _lib.Plan(_lib.SO3_COMPLEX, L, 1, "fp64", "stable")
-    c64 = torch.from_numpy(F0).to(dev)
-    g64 = torch.empty(N ** 3, dtype=torch.complex128, device=dev)
-    o64 = torch.empty_like(c64)
-    if p64 is not None:
-        p64.inverse(c64.data_ptr(), g64.data_ptr(), sp)
-        p64.forward(g64.data_ptr(), o64.data_ptr(), sp)
-    torch.cuda.synchronize()
-    F0_fp64 = o64.cpu().numpy()  # FP64 forward of the FP64 synthesis
-    g0_c64 = g64.to(torch.complex64)
-    g0_ref = g64.cpu().numpy()
-    if not args.no_fp64:
-        reps = 2
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(reps):
-            p64.inverse(c64.data_ptr(), g64.data_ptr(), sp)
-            p64.forward(g64.data_ptr(), o64.data_ptr(), sp)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / reps
-        fp64 = {"value": 1000.0 / ms, "unit": UNIT, "ms_per_pair": ms, "batch": 1,
-                "note": "plain FP64 GPU path (FFTSO3_PREC_FP64, stable recursion), same l_max"}
-    del p64, g64, o64, c64
-    torch.cuda.empty_cache()
-
-    # ---- tensor-core plan
-    plan = _lib.Plan(_lib.SO3_COMPLEX, L, b, "tc_bf16x3", "stable", _lib.FLAG_AUTOTUNE)
-    Fb = np.concatenate([seeded_coeffs(L, 1000 * rank + i) for i in range(b)]).astype(np.complex64)
-    coef = torch.from_numpy(Fb).to(dev)
-    grid = torch.empty(b * N ** 3, dtype=torch.complex64, device=dev)
-    plan.inverse(coef.data_ptr(), grid.data_ptr(), sp)  # synthetic band-limited inputs
-    if not args.no_accuracy:
-        grid[:N ** 3].copy_(g0_c64)                     # function 0: the FP64 synthesis
-    coef_out = torch.empty_like(coef)
-    grid_out = torch.empty_like(grid)
-    torch.cuda.synchronize()
-    plan.check()
-
-    # accuracy vs FP64 (function 0), before the timed region
-    coef0 = torch.from_numpy(F0.astype(np.complex64)).to(dev)
-    coef_in = coef.clone()
-    coef_in[:C].copy_(coef0)
-    if not args.no_accuracy:
-        plan.forward(grid.data_ptr(), coef_out.data_ptr(), sp)
-        plan.inverse(coef_in.data_ptr(), grid_out.data_ptr(), sp)
-        torch.cuda.synchronize()
-        plan.check()
-        fr, fm = per_l_errors(coef_out[:C].cpu().numpy().astype(np.complex128), F0_fp64, L)
-        gi = grid_out[:N ** 3].cpu().numpy().astype(np.complex128)
-        ir = float(np.linalg.norm(gi - g0_ref) / np.linalg.norm(g0_ref))
-        im = float(np.abs(gi - g0_ref).max() / np.sqrt(np.mean(np.abs(g0_ref) ** 2)))
-        acc = {"forward_rel_rms": fr, "forward_rel_max_per_l": fm, "inverse_rel_rms": ir,
-               "inverse_rel_max": im, "against": "FP64 GPU path (stable recursion) on the same function"}
-        # one residual refinement step F += forward(f - inverse(F)) (FFTSO3_FLAG_REFINE), same function
-        pr = _lib.Plan(_lib.SO3_COMPLEX, L, 1, "tc_bf16x3", "stable", _lib.FLAG_REFINE)
-        cr = torch.empty(C, dtype=torch.complex64, device=dev)
-        pr.forward(g0_c64.data_ptr(), cr.data_ptr(), sp)
-        e0r, e1r = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0r.record(stream)
-        pr.forward(g0_c64.data_ptr(), cr.data_ptr(), sp)
-        e1r.record(stream)
-        torch.cuda.synchronize()
-        pr.check()
-        rr, rm = per_l_errors(cr.cpu().numpy().astype(np.complex128), F0_fp64, L)
-        acc["refined_forward_rel_rms"] = rr
-        acc["refined_forward_rel_max_per_l"] = rm
-        acc["refined_forward_ms_batch1"] = e0r.elapsed_time(e1r)
-        del pr, cr
-    del coef_in, coef0
-
-    # ---- timed region: inputs resident in HBM (each grid 1 GB >> 129 MB L2)
-    for _ in range(args.warmup):
-        plan.inverse(coef.data_ptr(), grid_out.data_ptr(), sp)
-        plan.forward(grid.data_ptr(), coef_out.data_ptr(), sp)
-    barrier()
-    plan.set_timing(True)
-    plan.stage_times(reset=True)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
-        barrier()
-        e0.record(stream)
-        for _ in range(args.steps):
-            plan.inverse(coef.data_ptr(), grid_out.data_ptr(), sp)
-            plan.forward(grid.data_ptr(), coef_out.data_ptr(), sp)
-        e1.record(stream)
-        barrier()
-    ms = e0.elapsed_time(e1) / args.steps
-    stages = plan.stage_times(reset=True)
-    plan.set_timing(False)
-    plan.check()
-    clocks = clk.summary()
-    ms_max = ms
-    value = b * 1000.0 / ms_max
-    launches = int(sum(c for _, c in stages.values()))
-
-    # ---- roofline of the dominant kernel
-    peaks = measured_peaks()
-    B = L + 1
-    top = max(stages.items(), key=lambda kv: kv[1][0])
-    name, (tot_ms, cnt) = top
-    per_launch_s = tot_ms / cnt / 1000.0
-    useful_flops = 8.0 * B * C * b            # complex beta-sum flops per direction for the batch
-    grid_bytes = 8.0 * b * N ** 3             # one complex64 pass over the batch's grids
-    if name.startswith("tc_gemm"):
-        achieved = useful_flops / per_launch_s / 1e12
-        peak = peaks["bf16_tflops_sustained"]
-        roof = {"bound": "tensor", "unit": "TFLOP/s", "algorithmic": "8*B*C*batch useful flops per launch"}
-    else:
-        if name.startswith("fft") or name.startswith("tc_pack"):
-            byts = 2 * grid_bytes  # one complex64 read and write of the batch's grids (FFT pass / transpose)
-        else:
-            byts = grid_bytes
-        achieved = byts / per_launch_s / 1e9
-        peak = peaks["hbm_gbs"]
-        roof = {"bound": "hbm", "unit": "GB/s", "algorithmic": "bytes read + written per launch"}
-    roof.update({"kernel": name, "achieved": achieved, "peak": peak, "frac": achieved / peak,
-                 "peak_source": peaks["source"], "ms_per_launch": per_launch_s * 1000.0,
-                 "traffic": profiled_traffic(name, L, b)})
-    stage_summary = {k: {"ms_per_launch": v / c, "launches": c, "share": v / sum(x for x, _ in stages.values())}
-                     for k, (v, c) in stages.items()}
-    # ---- roofline of the whole step: the larger of its HBM floor (algorithmic bytes of every stage) and its
-    # tensor floor (the issued split-BF16 MMA flops), against the measured step time
-    Kp = (N + 63) // 64 * 64
-    table_rows = sum((2 * m + 1) * (B - m) for m in range(B))  # rows l of all symmetry groups
-    table_b = 3 * 2.0 * Kp * table_rows                        # three BF16 planes, read once per GEMM launch
-    coef_b = 8.0 * b * C                                        # complex64 coefficients of the batch
-    step_bytes = (2 * 2 * grid_bytes                            # FFT: two launches, one read + one write each
-                  + 2 * (grid_bytes + table_b + coef_b)         # GEMMs: pencils + table + coefficients
-                  + 2 * 2 * coef_b)                             # coefficient permutations
-    hbm_floor_ms = step_bytes / (peaks["hbm_gbs"] * 1e9) * 1e3
-    tensor_floor_ms = 2 * 6 * useful_flops / (peaks["bf16_tflops_sustained"] * 1e12) * 1e3
-    floor_ms = max(hbm_floor_ms, tensor_floor_ms)
-    step_roof = {"bound": "hbm" if hbm_floor_ms >= tensor_floor_ms else "tensor", "algorithmic_bytes": step_bytes,
-                 "hbm_floor_ms": hbm_floor_ms, "tensor_floor_ms": tensor_floor_ms, "ms_per_step": ms_max,
-                 "frac": floor_ms / ms_max, "peak_source": peaks["source"],
-                 "note": "FFT 4 x grid bytes, GEMMs 2 x (pencils + BF16 table planes + coefficients), permutations "
-                         "4 x coefficients; tensor floor = 6 issued BF16 products of the 8BC useful flops, both "
-                         "directions"}
-
-    # ---- end to end through the host-buffer C ABI (pinned host memory)
-    e2e = None
-    if not args.no_e2e:
-        hg = torch.empty(b * N ** 3, dtype=torch.complex64, pin_memory=True)
-        hg.copy_(grid)
-        hc = torch.empty(b * C, dtype=torch.complex64, pin_memory=True)
-        hc.copy_(coef)
-        hco = torch.empty_like(hc, pin_memory=True)
-        # the inverse writes the grid the forward then reads (one pinned grid buffer)
-        plan.inverse_host(hc.data_ptr(), hg.data_ptr(), sp)
-        plan.forward_host(hg.data_ptr(), hco.data_ptr(), sp)
-        barrier()
-        t0 = time.perf_counter()
-        ksteps = args.steps  # the same step count as the device-timed region
-        for _ in range(ksteps):
-            plan.inverse_host(hc.data_ptr(), hg.data_ptr(), sp)
-            plan.forward_host(hg.data_ptr(), hco.data_ptr(), sp)
-        barrier()
-        dt = (time.perf_counter() - t0) / ksteps
-        e2e = {"value": b / dt, "unit": UNIT, "h2d_bytes_per_step": int(8 * b * C + 8 * b * N ** 3),
-               "d2h_bytes_per_step": int(8 * b * N ** 3 + 8 * b * C), "steps": ksteps}
-        del hg, hc, hco
-
-    # ---- the FP32 form of the beta-sum (CUDA cores, FFTSO3_PREC_FP32) on the same batch
-    fp32 = None
-    plan.close()  # the tensor-core plan's tables and workspace make room for the FP32 plan
-    del plan, grid_out, coef_out
-    torch.cuda.empty_cache()
-    if not args.no_fp32:
-        p32 = _lib.Plan(_lib.SO3_COMPLEX, L, b, "fp32", "stable")
-        g32 = torch.empty_like(grid)
-        c32 = torch.empty_like(coef)
-        p32.inverse(coef.data_ptr(), g32.data_ptr(), sp)
-        p32.forward(grid.data_ptr(), c32.data_ptr(), sp)
-        torch.cuda.synchronize()
-        p32.check()
-        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        f0.record(stream)
-        p32.inverse(coef.data_ptr(), g32.data_ptr(), sp)
-        p32.forward(grid.data_ptr(), c32.data_ptr(), sp)
-        f1.record(stream)
-        torch.cuda.synchronize()
-        ms32 = f0.elapsed_time(f1)
-        fp32 = {"value": b * 1000.0 / ms32, "unit": UNIT, "ms_per_step": ms32,
-                "note": "FFTSO3_PREC_FP32: FP32 table and FMA accumulation on the CUDA cores, same batch"}
-        if not args.no_accuracy:
-            pa = _lib.Plan(_lib.SO3_COMPLEX, L, 1, "fp32", "stable")
-            ca = torch.empty(C, dtype=torch.complex64, device=dev)
-            pa.forward(g0_c64.data_ptr(), ca.data_ptr(), sp)
-            torch.cuda.synchronize()
-            fr32, fm32 = per_l_errors(ca.cpu().numpy().astype(np.complex128), F0_fp64, L)
-            fp32.update({"forward_rel_rms": fr32, "forward_rel_max_per_l": fm32})
-            del pa, ca
-        del p32, g32, c32
+    for name, fn in CONFIG_LINES.items():
+        gc.collect()
         torch.cuda.empty_cache()
-
-    # ---- the refined forward (FFTSO3_FLAG_REFINE: F += forward(f - inverse(F)), inverse and difference in FP64):
-    # inverse + refined forward of a few functions of the batch, pairs/s per function
-    refined = None
-    if not args.no_accuracy:
-        rb = min(b, 8)
-        pr = _lib.Plan(_lib.SO3_COMPLEX, L, rb, "tc_bf16x3", "stable", _lib.FLAG_REFINE)
-        gr = torch.empty(rb * N ** 3, dtype=torch.complex64, device=dev)
-        cr = torch.empty(rb * C, dtype=torch.complex64, device=dev)
-        pr.inverse(coef[:rb * C].data_ptr(), gr.data_ptr(), sp)
-        pr.forward(grid[:rb * N ** 3].data_ptr(), cr.data_ptr(), sp)
-        torch.cuda.synchronize()
-        pr.set_timing(True)
-        pr.stage_times(reset=True)
-        r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        r0.record(stream)
-        pr.inverse(coef[:rb * C].data_ptr(), gr.data_ptr(), sp)
-        pr.forward(grid[:rb * N ** 3].data_ptr(), cr.data_ptr(), sp)
-        r1.record(stream)
-        torch.cuda.synchronize()
-        pr.check()
-        rst = pr.stage_times(reset=True)
-        rms_ = r0.elapsed_time(r1)
-        refined = {"value": rb * 1000.0 / rms_, "unit": UNIT, "batch": rb, "ms_per_step": rms_,
-                   "forward_rel_rms": acc.get("refined_forward_rel_rms"),
-                   "forward_rel_max_per_l": acc.get("refined_forward_rel_max_per_l"),
-                   "stages_ms": {k: v for k, (v, _) in rst.items()},
-                   "note": "tensor-core inverse + refined forward (FFTSO3_FLAG_REFINE: the inverse of the first "
-                           "result exactly on the tensor cores (BF16 digit products summed without rounding) and "
-                           "f - inverse(F) in double-float, then the tensor-core forward of the residual)"}
-        del pr, gr, cr
-        torch.cuda.empty_cache()
-
-    cpu = None
-    if not args.no_cpu:
-        cpu = cpu_baselines(L)
-
-    if rank == 0:
-        metric = METRIC if L == 255 else METRIC.replace("l_max=255", f"l_max={L}")
-        line = {
-            "metric": metric, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "bf16x3 (split) / fp32 accumulate / fp32 FFT", "data": "synthetic",
-            "config": {"workload": f"SO(3) complex forward+inverse, l_max={L}, batch={b} functions per GPU "
-                                   f"({N}^3 complex64 grid each), TC split-BF16, stable recursion",
-                       "l_max": L, "batch_per_gpu": b, "precision": "tc_bf16x3",
-                       "l2": "inputs larger than L2 (1 GB grid per function)"},
-            "e2e": e2e, "gpu_launches": launches, "roofline": roof, "step_roofline": step_roof,
-            "stages": stage_summary,
-            "accuracy": acc, "refined_path": refined, "fp64_path": fp64, "fp32_cuda_core_path": fp32,
-            "speedup_vs_fp64_path": value / fp64["value"] if fp64 else None,
-            "clocks": clocks, "cpu_baseline": cpu,
-        }
-        print(json.dumps(line), flush=True)
+        try:
+            print(json.dumps(fn(args)), flush=True)
+        except Exception as e:  # report and go on: the headline is already out
+            print(json.dumps({"workload": name, "error": f"{type(e).__name__}: {e}"}), flush=True)
 
 
 if __name__ == "__main__":
