@@ -64,6 +64,8 @@ SIGNATURES = {
     "fftso3_inverse_host": (_i, [_vp, _vp, _vp, _vp]),
     "fftso3_inverse_points": (_i, [_vp, _vp, _i, _dp, _i, _vp, _vp]),
     "fftso3_wigner_d": (_i, [_d, _i, _i, _dp]),
+    "fftso3_derivative": (_i, [_vp, _vp, _i, _vp, _vp]),
+    "fftso3_clebsch_gordan": (_i, [_i, _i, _i, _vp]),
     "fftso3_forward_noalloc": (_i, [_i, _vp, _vp, _vp]),
     "fftso3_correlate_s2": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "fftso3_grid_argmax": (_i, [_vp, _vp, ctypes.POINTER(_ll), _dp, _vp]),
@@ -133,6 +135,17 @@ def grid_fft_check(workspace: int, stream: int = 0) -> None:
     check(lib().fftso3_grid_fft_check(workspace, stream))
 
 
+def clebsch_gordan(l1: int, l2: int, real: bool = False):
+    """The Clebsch-Gordan matrix of (l1, l2) computed on the GPU (fftso3_clebsch_gordan): (n, n) float64 for
+    the complex harmonics, complex128 for the real harmonics, n = (2 l1 + 1)(2 l2 + 1)."""
+    import numpy as np
+
+    n = (2 * int(l1) + 1) * (2 * int(l2) + 1)
+    out = np.empty((n, n), dtype=np.complex128 if real else np.float64, order="F")
+    check(lib().fftso3_clebsch_gordan(int(l1), int(l2), 1 if real else 0, out.ctypes.data))
+    return out
+
+
 class Plan:
     """Owns one ``fftso3_plan`` (tables and workspace on the current device)."""
 
@@ -180,6 +193,10 @@ class Plan:
     def inverse_points(self, coeff_ptr: int, index: int, pts, n: int, out_ptr: int, stream: int = 0) -> None:
         check(lib().fftso3_inverse_points(self._h, _vp(coeff_ptr), int(index), pts, int(n), _vp(out_ptr),
                                           _vp(stream)))
+
+    def derivative(self, coeff_ptr: int, axis: int, out_ptr: int, stream: int = 0) -> None:
+        """Coefficients of d/dt f(R exp(t e_axis)) for the batch (fftso3_derivative)."""
+        check(lib().fftso3_derivative(self._h, _vp(coeff_ptr), int(axis), _vp(out_ptr), _vp(stream)))
 
     def correlate_s2(self, F_ptr: int, G_ptr: int, grid_ptr: int, stream: int = 0) -> None:
         check(lib().fftso3_correlate_s2(self._h, _vp(F_ptr), _vp(G_ptr), _vp(grid_ptr), _vp(stream)))

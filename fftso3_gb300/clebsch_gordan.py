@@ -14,7 +14,9 @@ reference's phase).  The real-harmonic coefficients are
     c = conj(T^{l1} (x) T^{l2}) C ((+)_l T^l)^T,
 T = matrix2rsph (src/fdcl_Clebsch_Gordon.cpp:100-120, :179-209), so that
     U^{l1} (x) U^{l2} = c (+)_l U^l c^H.
-Host code: the tables are small and computed once per (l1, l2).
+compute() runs on the GPU (fftso3_clebsch_gordan: one thread per column of C, one
+per entry of c); compute_host() is the same recursion in numpy, kept as the CPU
+check of the tests.
 """
 from __future__ import annotations
 
@@ -56,6 +58,14 @@ class Clebsch_Gordon_complex:
         return self.C[self.row(l, m, l1, m1, l2, m2), self.col(l, m, l1, m1, l2, m2)]
 
     def compute(self, l1: int, l2: int) -> None:
+        """All coefficients of (l1, l2), on the GPU."""
+        from . import _lib
+
+        self.init(l1, l2)
+        self.C = _lib.clebsch_gordan(l1, l2, real=False)
+
+    def compute_host(self, l1: int, l2: int) -> None:
+        """The same coefficients with the recursion in numpy (the CPU check)."""
         self.init(l1, l2)
         for l in range(abs(l1 - l2), l1 + l2 + 1):
             for m in range(-l, l + 1):
@@ -106,7 +116,14 @@ class Clebsch_Gordon_real(Clebsch_Gordon_complex):
         return self.c[self.row(l, m, l1, m1, l2, m2), self.col(l, m, l1, m1, l2, m2)]
 
     def compute(self, l1: int, l2: int) -> None:
+        """All coefficients of (l1, l2), complex and real harmonics, on the GPU."""
+        from . import _lib
+
         super().compute(l1, l2)
+        self.c = _lib.clebsch_gordan(l1, l2, real=True)
+
+    def compute_host(self, l1: int, l2: int) -> None:
+        super().compute_host(l1, l2)
         T1, T2 = _rsph(l1), _rsph(l2)
         T12 = np.kron(T1, T2)
         n = self.C.shape[0]

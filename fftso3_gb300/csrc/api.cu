@@ -14,6 +14,7 @@
 #include "common.cuh"
 #include "contract.cuh"
 #include "fft.cuh"
+#include "operators.cuh"
 #include "refine_oz.cuh"
 #include "tables.cuh"
 #include "tc.cuh"
@@ -129,6 +130,7 @@ struct fftso3_plan {
     void* d_rfc = nullptr;         // complex FP64 coefficients of one chunk (real kinds)
     int rchunk = 0;
     OZState* oz = nullptr;         // SO(3), l_max <= 255: the refinement's inverse on the tensor cores, exactly
+    DerivEntry* d_deriv = nullptr; // rows of the derivative matrices u_1..u_3 (built on the first derivative call)
     long long bytes = 0;
     TCState* tc = nullptr;         // tensor-core contraction state
     StageTimer timer;              // optional per-stage CUDA-event timing
@@ -156,7 +158,7 @@ void plan_free(fftso3_plan* p)
 {
     void* ptrs[] = {p->d_tw, p->d_w, p->d_goff, p->d_table, p->d_lfact, p->d_work, p->d_fc, p->d_io_grid,
                     p->d_io_coeff, p->d_corr, p->d_amax, p->d_prec, p->d_pscratch, p->d_rw, p->d_rg, p->d_rc,
-                    p->d_rfc};
+                    p->d_rfc, p->d_deriv};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     if (p->tc) tc_destroy(p->tc);
@@ -828,6 +830,56 @@ int fftso3_inverse_points(fftso3_plan* plan, const void* coeffs, int index, cons
     } else if ((e = cudaMemcpy(out, d_out, sizeof(double2) * n, cudaMemcpyDeviceToHost)) != cudaSuccess) {
         return cuda_fail(e, "copy points");
     }
+    return FFTSO3_SUCCESS;
+}
+
+int fftso3_derivative(fftso3_plan* plan, const void* coeffs, int axis, void* coeffs_out, void* stream)
+{
+    int rc = check_plan(plan);
+    if (rc) return rc;
+    if (!plan->so3) return fail(FFTSO3_ERR_INVALID_ARG, "derivatives need an SO(3) plan");
+    if (axis < 1 || axis > 3) return fail(FFTSO3_ERR_INVALID_ARG, "axis must be 1, 2 or 3");
+    if (!coeffs || !coeffs_out) return fail(FFTSO3_ERR_INVALID_ARG, "NULL pointer argument");
+    if (coeffs == coeffs_out) return fail(FFTSO3_ERR_INVALID_ARG, "coeffs and coeffs_out must be different buffers");
+    const long long R = (long long)plan->B * plan->B;
+    if (!plan->d_deriv) {
+        std::vector<DerivEntry> t = derivative_table(plan->L, plan->real);
+        if (t.empty()) return fail(FFTSO3_ERR_CUDA, "internal: derivative table has a row with three nonzeros");
+        if ((rc = plan_alloc(plan, (void**)&plan->d_deriv, sizeof(DerivEntry) * t.size()))) return rc;
+        cudaError_t e = cudaMemcpy(plan->d_deriv, t.data(), sizeof(DerivEntry) * t.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaFree(plan->d_deriv);
+            plan->d_deriv = nullptr;
+            plan->bytes -= (long long)(sizeof(DerivEntry) * t.size());
+            return cuda_fail(e, "derivative table");
+        }
+    }
+    CK(launch_derivative(coeffs, coeffs_out, plan->d_deriv + (axis - 1) * R, plan->fp64, plan->real, plan->L,
+                         plan->batch, (cudaStream_t)stream));
+    return FFTSO3_SUCCESS;
+}
+
+int fftso3_clebsch_gordan(int l1, int l2, int real, void* out_host)
+{
+    if (l1 < 0 || l2 < 0) return fail(FFTSO3_ERR_INVALID_ARG, "l1 and l2 must be >= 0");
+    if (!out_host) return fail(FFTSO3_ERR_INVALID_ARG, "output pointer is NULL");
+    if (l1 > 1023 || l2 > 1023) return fail(FFTSO3_ERR_UNSUPPORTED, "l1, l2 above 1023 are not supported");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(FFTSO3_ERR_NO_DEVICE, "no CUDA device available");
+    const size_t n = (size_t)(2 * l1 + 1) * (2 * l2 + 1);
+    double* C = nullptr;
+    double2* cr = nullptr;
+    cudaError_t e = cudaMalloc(&C, sizeof(double) * n * n);
+    if (e == cudaSuccess && real) e = cudaMalloc(&cr, sizeof(double2) * n * n);
+    if (e == cudaSuccess) e = launch_clebsch_gordan(l1, l2, C, cr, 0);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess)
+        e = real ? cudaMemcpy(out_host, cr, sizeof(double2) * n * n, cudaMemcpyDeviceToHost)
+                 : cudaMemcpy(out_host, C, sizeof(double) * n * n, cudaMemcpyDeviceToHost);
+    if (C) cudaFree(C);
+    if (cr) cudaFree(cr);
+    if (e != cudaSuccess) return cuda_fail(e, "clebsch_gordan");
     return FFTSO3_SUCCESS;
 }
 

@@ -212,6 +212,22 @@ class _Transform:
         self.plan.inverse_points(c.data_ptr(), 0, pts.ctypes.data_as(_lib._dp), n, out.ctypes.data)
         return out
 
+    def derivative(self, F, axis: int):
+        """Coefficients of f_i(R) = d/dt f(R exp(t e_i)) at t = 0 (i = axis in 1..3), computed on the GPU
+        (fftso3_derivative): F^l (u_i^l)^T with u_i the matrices of deriv_wigner_D / deriv_real_harmonics.
+        SO(3) only."""
+        import torch
+
+        if not self._so3:
+            raise ValueError("derivatives are defined for SO(3) functions")
+        self.init(F.l_max)
+        c = torch.from_numpy(np.ascontiguousarray(F.M, dtype=self._coeff_dtype())).cuda()
+        out = torch.empty_like(c)
+        s = torch.cuda.current_stream().cuda_stream
+        self.plan.derivative(c.data_ptr(), int(axis), out.data_ptr(), s)
+        torch.cuda.synchronize()
+        return self._coeff_container(out.cpu().numpy())
+
     # -- device-resident batch API (torch CUDA tensors)
     def make_plan(self, batch: int) -> _lib.Plan:
         return _lib.Plan(self._kind, self.l_max, batch, self.precision, self.recursion,

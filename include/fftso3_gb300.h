@@ -185,6 +185,29 @@ int fftso3_grid_argmax(fftso3_plan* plan, const void* grid, long long* index_out
  * Replaces wigner_d(beta) (fdcl_FFTSO3.cpp:122-194). */
 int fftso3_wigner_d(double beta, int l_max, int recursion, double* d_out_host);
 
+/* Directional derivative of SO(3) functions: for each of the plan's `batch`
+ * coefficient vectors F (device, the plan's kind and element type), writes
+ * to coeffs_out (device, a different buffer) the coefficients of
+ *   f_i(R) = d/dt f(R exp(t e_i)) at t = 0,   i = axis in {1, 2, 3},
+ * i.e. F'^l = F^l (u_i^l)^T per degree, with u_i^l the matrices of
+ * deriv_wigner_D (fdcl_FFTSO3.cpp:417-453; complex kind) or
+ * deriv_real_harmonics (:1577-1645; real kind), which satisfy
+ * d/dt D^l(R exp(t e_i)) = D^l(R) u_i^l.  An inverse transform of the result
+ * gives the derivative on the whole grid.  The first call builds the plan's
+ * table of the matrices' nonzeros (at most two per row).  Asynchronous on
+ * `stream`.  SO(3) kinds only. */
+int fftso3_derivative(fftso3_plan* plan, const void* coeffs, int axis, void* coeffs_out, void* stream);
+
+/* Clebsch-Gordan coefficients for the pair (l1, l2), computed on the GPU:
+ * real = 0: the n x n matrix C of the complex harmonics (float64), real = 1:
+ * the matrix c of the real harmonics (complex128); n = (2 l1 + 1)(2 l2 + 1),
+ * column-major, row (l1 + m1)(2 l2 + 1) + l2 + m2, column
+ * l^2 - (l2 - l1)^2 + l + m, as Clebsch_Gordon_complex::compute and
+ * Clebsch_Gordon_real::compute (src/fdcl_Clebsch_Gordon.cpp:18-26, :41-98,
+ * :224-329).  out_host: n * n elements of host memory; the call allocates
+ * device scratch of that size and synchronises. */
+int fftso3_clebsch_gordan(int l1, int l2, int real, void* out_host);
+
 /* ---- batches of uneven bandwidth ----
  * One object for n_functions functions of one kind whose l_max differs per
  * function (l_max[i]).  It replaces the reference user's loop of

@@ -32,7 +32,7 @@ def _block(mats, lo, hi):
 @pytest.mark.parametrize("l1,l2", [(0, 0), (1, 1), (2, 1), (3, 5), (6, 4)])
 def test_complex_product_rule(oracle, l1, l2):
     cg = Clebsch_Gordon_complex()
-    cg.compute(l1, l2)
+    cg.compute_host(l1, l2)
     n = cg.C.shape[0]
     assert np.allclose(cg.C.T @ cg.C, np.eye(n), atol=1e-12)
     D = _D(oracle, l1 + l2, 0.7, 1.3, -0.4)
@@ -44,7 +44,7 @@ def test_complex_product_rule(oracle, l1, l2):
 @pytest.mark.parametrize("l1,l2", [(3, 5), (2, 2)])
 def test_real_product_rule(oracle, l1, l2):
     cg = Clebsch_Gordon_real()
-    cg.compute(l1, l2)
+    cg.compute_host(l1, l2)
     L = l1 + l2
     a, b, g = 2.1, 0.8, 1.7
     U = fg.FFTSO3_matrix_real(L, data=oracle.so3_real_harmonics(L, a, b, g))
@@ -56,7 +56,7 @@ def test_real_product_rule(oracle, l1, l2):
 
 def test_known_values():
     cg = Clebsch_Gordon_complex(1, 1)
-    cg.compute(1, 1)
+    cg.compute_host(1, 1)
     s2 = 1 / np.sqrt(2)
     assert np.isclose(cg(2, 2, 1, 1, 1, 1), 1.0)
     assert np.isclose(cg(2, 1, 1, 1, 1, 0), s2) and np.isclose(cg(2, 1, 1, 0, 1, 1), s2)
