@@ -135,8 +135,9 @@ def measured_peaks() -> dict:
 def profiled_traffic(stage: str, l_max: int, batch: int):
     """DRAM bytes per launch of `stage` from the committed ncu capture figures
     (profiles/traffic.json: stage, l_max, batch, bytes per launch), scaled to
-    this workload: by batch at the same l_max, and for the FFT stages (whose
-    traffic is one read and one write of every sample) by batch * N^3 across l_max."""
+    this workload: by batch (functions per launch) at the same l_max, and for
+    the FFT stages (whose traffic is one read and one write of every sample) by
+    batch * N^3 across l_max."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     if not os.path.exists(path):
         return None
@@ -146,7 +147,7 @@ def profiled_traffic(stage: str, l_max: int, batch: int):
         if L0 == l_max:
             return byts * batch / b0
     for L0, b0, byts in found:
-        if stage.startswith("fft"):
+        if "fft" in stage:
             return byts * batch / b0 * ((l_max + 1) / (L0 + 1)) ** 3
     return None
 
@@ -1068,7 +1069,7 @@ def so3_tc_line(args, L: int, b: int, full: bool = True) -> dict:
     stage_summary = {k: {"ms_per_launch": v / c, "launches": c, "share": v / tot} for k, (v, c) in stages.items()}
     top, (top_ms, top_n) = max(stages.items(), key=lambda kv: kv[1][0])
     roof = stage_roofline(top, top_ms, top_n, L, b, chunk, peaks)
-    roof["traffic"] = profiled_traffic(top, L, b)
+    roof["traffic"] = profiled_traffic(top, L, chunk if top.startswith("refine") else b)  # refinement: per chunk
     roof["share_of_step"] = top_ms / tot
 
     # ---- the step against its floors: HBM (algorithmic bytes of every stage) and tensor (issued MMA flops)
