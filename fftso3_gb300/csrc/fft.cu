@@ -451,24 +451,38 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(const TIN* __restrict__ 
 // transforms TK = 2048 / N consecutive k of one o (N = 64..512, a power of two) with 256 threads: TK lines of N
 // elements staged in shared memory (global accesses run k-fastest: TK consecutive elements per j), then radix-8
 // Stockham stages (a last radix-4 or 2 stage when log2 N is not a multiple of 3), each thread holding the 8
-// values of one butterfly in registers; stages run in place, a barrier between the reads and the writes.  Rows
-// are padded by one element per 8 (phys(i) = i + i / 8), so both the strided reads and the scattered writes of
-// a stage fill whole 16-byte bank groups.
+// values of one butterfly in registers; stages run in place, a barrier between the reads and the writes.
+// Shared-memory layout, so that every access of a warp fills whole 16-byte bank groups:
+//   rows padded by one element per 8 (phys(i) = i + i / 8): a stage's strided reads and scattered writes;
+//   row stride N + N / 8 + 1 elements (one extra 16-byte slot): the TK rows of the load / store phases;
+//   twiddles per stage as [r - 1][kt] (kt = butterfly index mod Ns): consecutive lanes, consecutive entries.
 template <int N>
-__global__ void __launch_bounds__(256) fft_df32_k_kernel(dfc32* __restrict__ buf, long long S, long long oinner,
-                                                          long long oouter, long long oistride,
-                                                          const double2* __restrict__ twg)
+__global__ void __launch_bounds__(256, 3) fft_df32_k_kernel(dfc32* __restrict__ buf, long long S, long long oinner,
+                                                             long long oouter, long long oistride,
+                                                             const double2* __restrict__ twg)
 {
-    constexpr int TK = 2048 / N;     // lines per CTA
-    constexpr int TPL = N / 8;       // threads per line
-    constexpr int ROW = N + N / 8;   // padded row length
+    constexpr int TK = 2048 / N;         // lines per CTA
+    constexpr int TPL = N / 8;           // threads per line
+    constexpr int ROW = N + N / 8 + 1;   // padded row length
     __shared__ dfc32 sm[TK * ROW];
-    __shared__ dfc32 w[N];
+    __shared__ dfc32 w[N];               // stage twiddle tables (at most N - 8 entries)
     auto phys = [](int i) { return i + (i >> 3); };
     const int tid = threadIdx.x;
     const long long o = blockIdx.y;
     const long long obase = (o / oinner) * oouter + (o % oinner) * oistride + (long long)blockIdx.x * TK;
-    for (int i = tid; i < N; i += 256) w[i] = dfc32{df32(twg[i].x), df32(twg[i].y)};
+    // stage tables: radix-8 stages with Ns = 8, 64 (when present) and the last radix-4 / 2 stage with Ns = 64
+    {
+        int off = 0;
+        for (int Ns = 8; Ns < N; Ns *= 8) {
+            const int R = Ns * 8 <= N ? 8 : N / Ns;
+            for (int i = tid; i < (R - 1) * Ns; i += 256) {
+                const int r = i / Ns + 1, kt = i % Ns;
+                const double2 v = twg[r * kt * (N / (R * Ns))];
+                w[off + i] = dfc32{df32(v.x), df32(v.y)};
+            }
+            off += (R - 1) * Ns;
+        }
+    }
 #pragma unroll
     for (int u = 0; u < N * TK / 256; ++u) {
         const int e = tid + 256 * u, kk = e % TK, j = e / TK;
@@ -477,7 +491,7 @@ __global__ void __launch_bounds__(256) fft_df32_k_kernel(dfc32* __restrict__ buf
     __syncthreads();
     const int kk = tid / TPL, t = tid % TPL;
     dfc32* line = sm + kk * ROW;
-    int Ns = 1;
+    int Ns = 1, toff = 0;
 #pragma unroll
     for (int s = 0; s < 3; ++s) {  // radix-8 stages while 8 Ns divides N
         if (Ns * 8 > N) break;
@@ -487,9 +501,9 @@ __global__ void __launch_bounds__(256) fft_df32_k_kernel(dfc32* __restrict__ buf
         for (int r = 0; r < 8; ++r) v[r] = line[phys(t + r * (N / 8))];
         __syncthreads();
         if (Ns > 1) {
-            const int e = kt * (N / (8 * Ns));
 #pragma unroll
-            for (int r = 1; r < 8; ++r) v[r] = cmul(v[r], w[r * e]);
+            for (int r = 1; r < 8; ++r) v[r] = cmul(v[r], w[toff + (r - 1) * Ns + kt]);
+            toff += 7 * Ns;
         }
         dft_small<df32, 8>(v, w, N / 8);
 #pragma unroll
@@ -508,9 +522,9 @@ __global__ void __launch_bounds__(256) fft_df32_k_kernel(dfc32* __restrict__ buf
         __syncthreads();
 #pragma unroll
         for (int b = 0; b < PER; ++b) {
-            const int j = t + b * TPL, kt = j % Ns, e = kt * (N / (R * Ns));
+            const int j = t + b * TPL, kt = j % Ns;
 #pragma unroll
-            for (int r = 1; r < R; ++r) v[b][r] = cmul(v[b][r], w[r * e]);
+            for (int r = 1; r < R; ++r) v[b][r] = cmul(v[b][r], w[toff + (r - 1) * Ns + kt]);
             dft_small<df32, R>(v[b], w, N / R);
 #pragma unroll
             for (int r = 0; r < R; ++r) line[phys((j - kt) * R + kt + r * Ns)] = v[b][r];
