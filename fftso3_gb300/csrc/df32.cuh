@@ -1,14 +1,19 @@
 // Double-FP32 ("double-float") arithmetic: a value is the unevaluated sum h + l
-// of two floats with |l| <= ulp(h) / 2, about 48 significant bits, computed on
-// the FP32 pipes.  On GB300 the FP64 units are a small fraction of the FP32
-// ones, so the refinement's FFT runs in this arithmetic instead of FP64.
+// of two floats, about 48 significant bits, computed on the FP32 pipes.  On
+// GB300 the FP64 units are a small fraction of the FP32 ones, so the
+// refinement's FFT runs in this arithmetic instead of FP64.
 //
 // The operations are the classical error-free transformations: two_sum
 // (Knuth), quick_two_sum (Dekker, for |a| >= |b|) and the FMA-based exact
-// product a*b = p + fma(a, b, -p).  Addition is the "sloppy" form (error
-// bounded relative to |a| + |b|, which is what an FFT's error analysis uses);
-// multiplication drops the l*l term.  Nothing here relies on -ffast-math
-// reassociation being off beyond nvcc's default (no fast-math flags are used).
+// product a*b = p + fma(a, b, -p).  The operators + and * are "lazy": the
+// rounding error of h is folded into l (a + b: h = fl(a.h + b.h),
+// l = err + a.l + b.l; a * b: h = fl(a.h b.h), l = err + a.h b.l + a.l b.h, the
+// l*l term dropped) but the pair is not renormalised after each operation, which
+// saves 3 of 11 and 3 of 7 instructions.  |l| then stays a small multiple of
+// ulp(h) over the short chains of an FFT butterfly network (one step of growth
+// per operation), so h + l keeps about 44 bits relative to the operands -- the
+// error an FFT's analysis is stated in.  df_two_sum / df_quick_two_sum give
+// normalised pairs where a caller needs them.  No fast-math flags are used.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -39,7 +44,7 @@ __device__ __forceinline__ df32 df_quick_two_sum(float a, float b)
 __device__ __forceinline__ df32 operator+(df32 a, df32 b)
 {
     const df32 s = df_two_sum(a.h, b.h);
-    return df_quick_two_sum(s.h, s.l + (a.l + b.l));
+    return df32(s.h, s.l + (a.l + b.l));
 }
 
 __device__ __forceinline__ df32 operator-(df32 a) { return df32(-a.h, -a.l); }
@@ -51,7 +56,7 @@ __device__ __forceinline__ df32 operator*(df32 a, df32 b)
     float e = fmaf(a.h, b.h, -p);
     e = fmaf(a.h, b.l, e);
     e = fmaf(a.l, b.h, e);
-    return df_quick_two_sum(p, e);
+    return df32(p, e);
 }
 
 __device__ __forceinline__ df32& operator+=(df32& a, df32 b) { return a = a + b; }
