@@ -1047,7 +1047,6 @@ def so3_tc_line(args, L: int, b: int, full: bool = True) -> dict:
     # ---- the measured plan: refined forward (headline) or plain split-BF16
     flags = _lib.FLAG_AUTOTUNE | (_lib.FLAG_REFINE if full else 0)
     plan = _lib.Plan(_lib.SO3_COMPLEX, L, b, "tc_bf16x3", "stable", flags)
-    chunk = min(b, 8)  # functions per refinement chunk (the library's choice at these sizes)
     plan.inverse(coef.data_ptr(), grid.data_ptr(), sp)  # synthetic band-limited FP32 samples
     if have_ref:
         grid[:N ** 3].copy_(g0_c64)
@@ -1061,6 +1060,10 @@ def so3_tc_line(args, L: int, b: int, full: bool = True) -> dict:
             acc["refined_forward_rel_max_per_l"] = acc["forward_rel_max_per_l"]
     ms, stages, clocks = timed(plan, args.steps, args.warmup, clocks=True)
     value = b * 1000.0 / ms
+    # functions per refinement chunk (the library sizes chunks to the free device memory): one timed record of
+    # the refinement FFT per chunk and step
+    nchunks = max(1, round(stages.get("refine_inverse_fft", (0, args.steps))[1] / args.steps))
+    chunk = -(-b // nchunks)
     nrec = int(sum(c for _, c in stages.values()))
     # kernels in the timed region: one per timed record, plus the second kernel of the records that hold two
     # (the double-float FFT's two passes; the coefficient gather with the Nyquist zeroing), one each per chunk
@@ -1083,7 +1086,6 @@ def so3_tc_line(args, L: int, b: int, full: bool = True) -> dict:
     step_bytes = 2 * tc_dir
     tensor_flops = 2 * 6 * useful
     if full:
-        nchunks = (b + chunk - 1) // chunk
         oz_table = nchunks * 4 * 2.0 * Kp * table_rows   # digit planes, read once per chunk launch
         step_bytes += (tc_dir                                     # forward of the residual
                        + coef_b + 2 * 16.0 * b * C                 # gather: coefficients in, double-float runs out
@@ -1168,6 +1170,7 @@ def so3_tc_line(args, L: int, b: int, full: bool = True) -> dict:
         "config": {"workload": f"SO(3) complex, l_max={L}, batch={b} functions ({N}^3 complex64 grid each), stable "
                                f"recursion; one step = {what}",
                    "l_max": L, "batch": b, "precision": "tc_bf16x3" + (" + refine" if full else ""),
+                   "refine_chunk": chunk if full else None,
                    "l2": f"inputs larger than L2 ({8.0 * b * N ** 3 / 1e9:.1f} GB of complex64 grids)"},
         "e2e": e2e, "gpu_launches": launches, "roofline": roof, "step_roofline": step_roof,
         "stages": stage_summary, "accuracy": acc, "fp64_path": fp64,

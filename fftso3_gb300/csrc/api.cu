@@ -509,11 +509,19 @@ int fftso3_plan_create(fftso3_plan** out, int kind, int l_max, int batch, int pr
         const char* ev_ref = getenv("FFTSO3_REFINE_FP64");
         const bool use_oz = (flags & FFTSO3_FLAG_REFINE) && p->so3 && oz_supported(L, N) && !(ev_ref && ev_ref[0] == '1');
         if (use_oz) {
-            // SO(3) refinement on the tensor cores: digit planes of the FP64 table, then the table is freed;
-            // chunks of up to 8 functions (one column tile), bounded to ~20 GB of double-float pencils
-            const size_t g16 = 16 * (size_t)p->grid_elems;
-            size_t nch = ((size_t)20 << 30) / g16;
-            nch = nch < 1 ? 1 : (nch > 8 ? 8 : nch);
+            // SO(3) refinement on the tensor cores: digit planes of the FP64 table, then the table is freed.
+            // Chunks of 16 functions (two column tiles, whose items share each table tile through L2, so the
+            // digit planes are read once per 16 functions) when the device has room for them with 16 GB to
+            // spare after the FP64 table is freed, else 8 (one column tile), else fewer
+            const size_t per_fn = 16 * ((size_t)p->grid_elems + (size_t)p->coeff_elems);  // pencils + runs
+            const size_t planes = 4 * 2 * (size_t)(p->table_elems / N) * (size_t)((N + 63) / 64 * 64);
+            const size_t tab64 = sizeof(double) * (size_t)p->table_elems;
+            size_t freeb = 0, totb = 0;
+            cudaMemGetInfo(&freeb, &totb);
+            const size_t spare = (size_t)16 << 30, slack = (size_t)2 << 30;
+            size_t nch = 16;
+            while (nch > 1 && (planes + nch * per_fn + slack > freeb || freeb + tab64 < planes + nch * per_fn + spare))
+                nch = nch > 8 ? 8 : nch - 1;
             p->rchunk = (int)(nch < (size_t)batch ? nch : (size_t)batch);
             std::string err;
             if ((rc = oz_create(&p->oz, p->d_table, goff, L, N, p->rchunk, p->d_tw, err))) {
@@ -666,6 +674,13 @@ int fftso3_forward_host(fftso3_plan* plan, const void* grid_host, void* coeffs_h
     // pinned buffers: read the samples / write the coefficients in place
     const void* gin = host_device_ptr(grid_host);
     void* cout = host_device_ptr(coeffs_host);
+    if (plan->tc && (plan->flags & FFTSO3_FLAG_REFINE)) {
+        // the refinement reads the samples twice (first forward, then the residual): copy them once into the
+        // residual buffer, which the residual then overwrites chunk by chunk, in place
+        void* stage = tc_resid_buffer(plan->tc);
+        CK(cudaMemcpyAsync(stage, grid_host, grid_bytes(plan), cudaMemcpyHostToDevice, st));
+        gin = stage;
+    }
     if ((!gin && (rc = ensure_io_grid(plan))) || (!cout && (rc = ensure_io_coeff(plan)))) return rc;
     if (!gin) {
         CK(cudaMemcpyAsync(plan->d_io_grid, grid_host, grid_bytes(plan), cudaMemcpyHostToDevice, st));

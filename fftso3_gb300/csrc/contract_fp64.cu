@@ -635,9 +635,8 @@ __global__ void widen_kernel(const float* __restrict__ in, double* __restrict__ 
 
 // r = f - g with f the FP32 samples the forward transformed and g the FP64
 // synthesis of its first result: the subtraction is done in FP64 (f is exact
-// there), only the small difference is rounded to FP32.
-__global__ void resid_fp64_kernel(const float* __restrict__ f, const double* __restrict__ g, float* __restrict__ r,
-                                  long long n)
+// there), only the small difference is rounded to FP32.  f may be r itself.
+__global__ void resid_fp64_kernel(const float* f, const double* __restrict__ g, float* r, long long n)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) r[i] = (float)((double)f[i] - g[i]);

@@ -549,10 +549,9 @@ __global__ void zero_nyquist_kernel(float4* __restrict__ H, int N, long long nb)
 
 // r[fn][k][j1][j2] = f - g with g[fn][j1][j2][k] the double-float grid: (f - g.h) - g.l in FP32 (f - g.h is
 // exact where g is close to f).  32 x 32 tiles of (k, j2) through shared memory; REAL: real samples and the real
-// part of g.
+// part of g.  f may be r itself (each element is read and then written by the same thread).
 template <bool REAL>
-__global__ void __launch_bounds__(256) resid_kernel(const float4* __restrict__ g, const void* __restrict__ fin,
-                                                    float* __restrict__ r, int N)
+__global__ void __launch_bounds__(256) resid_kernel(const float4* __restrict__ g, const void* fin, float* r, int N)
 {
     __shared__ float4 tile[32][33];
     const int k0 = blockIdx.x * 32, q0 = blockIdx.y * 32;

@@ -96,3 +96,39 @@ def test_exact_and_fp64_refinement_agree(gblib, oracle):
     for i in range(3):
         rms, mx = per_l_errors(a[i], b[i], L)
         assert rms <= 1e-7 and mx <= 1e-6, (i, rms, mx)
+
+
+@pytest.mark.parametrize("kind", ["complex", "real"])
+def test_refined_host_call_equals_device_call(gblib, oracle, kind):
+    """fftso3_forward_host on a refined plan (samples staged once into the residual buffer, which the residual
+    then overwrites in place) gives the same coefficients, bit for bit, as fftso3_forward on device buffers;
+    pageable and pinned host samples, batch 3, and the host samples are left unchanged."""
+    import torch
+    cplx = kind == "complex"
+    k = gblib.SO3_COMPLEX if cplx else gblib.SO3_REAL
+    L, b = 15, 3
+    N = 2 * (L + 1)
+    gs = []
+    for i in range(b):
+        F = so3_coeffs(L, seed=4700 + i, complex_=cplx, decay="pow")
+        g = oracle.so3_inverse_complex_grid(L, F) if cplx else oracle.so3_inverse_real_grid(L, F)
+        gs.append(g.astype(np.complex64 if cplx else np.float32).ravel())
+    host = np.ascontiguousarray(np.concatenate(gs))
+    keep = host.copy()
+    p = gblib.Plan(k, L, b, "tc_bf16x3", "stable", gblib.FLAG_REFINE)
+    s = torch.cuda.current_stream().cuda_stream
+    dt = torch.complex64 if cplx else torch.float32
+    dev = torch.from_numpy(host).cuda()
+    cd = torch.empty(b * p.coeff_elems, dtype=dt, device="cuda")
+    p.forward(dev.data_ptr(), cd.data_ptr(), s)
+    p.check()
+    want = cd.cpu().numpy()
+    out = np.empty_like(want)
+    p.forward_host(host.ctypes.data, out.ctypes.data, s)  # pageable
+    assert np.array_equal(out, want)
+    assert np.array_equal(host, keep)
+    pin = torch.from_numpy(host).pin_memory()
+    pout = torch.empty(want.size, dtype=dt).pin_memory()
+    p.forward_host(pin.data_ptr(), pout.data_ptr(), s)  # pinned
+    assert np.array_equal(pout.numpy(), want)
+    assert N ** 3 * b == host.size
