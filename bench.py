@@ -369,7 +369,21 @@ def uneven_line(args) -> dict:
     for k in range(bt.buckets):
         Lb, cnt = bt.bucket_info(k)
         bsz[Lb] = cnt
-    if top.startswith("tc_gemm"):
+    if top == "fft_slices":
+        # both passes of every beta slice in one launch per direction: the real grid read (or written) once and
+        # the complex64 pencils written (or read) once, 4 + 8 B per sample and direction
+        byts = sum(2 * 12.0 * (2 * (Lb + 1)) ** 3 * c for Lb, c in bsz.items())
+        ach = byts / (top_ms / 1000.0) / 1e9
+        roof = {"bound": "hbm", "unit": "GB/s", "achieved": ach, "peak": peaks["hbm_gbs"],
+                "frac": ach / peaks["hbm_gbs"],
+                "algorithmic": "real FP32 grid + complex64 pencils, once each per direction (12 B per sample)"}
+    elif top == "coeff_convert":
+        byts = sum(2 * 12.0 * ((Lb + 1) * (4 * (Lb + 1) ** 2 - 1) // 3) * c for Lb, c in bsz.items())
+        ach = byts / (top_ms / 1000.0) / 1e9
+        roof = {"bound": "hbm", "unit": "GB/s", "achieved": ach, "peak": peaks["hbm_gbs"],
+                "frac": ach / peaks["hbm_gbs"],
+                "algorithmic": "complex64 group-major + real FP32 packed coefficients, once each per direction"}
+    elif top.startswith("tc_gemm"):
         fl = sum(8.0 * (Lb + 1) * ((Lb + 1) * (4 * (Lb + 1) ** 2 - 1) // 3) * c for Lb, c in bsz.items()
                  if top in dict((L2, d) for _, L2, _, d in per_bucket).get(Lb, {}))
         ach = fl / (top_ms / 1000.0) / 1e12
@@ -412,10 +426,11 @@ def uneven_line(args) -> dict:
         "vs_baseline": None, "dtype": "bf16x3 (split) / fp32 accumulate / fp32 FFT; fp32 samples",
         "data": "synthetic",
         "config": {"workload": f"{n} real SO(3) functions, l_max uniform in 8..64 (seed 3), coefficients "
-                               "N(0,1)/(2l+1), FP32 samples; fftso3_batch, tensor-core buckets, CUDA graph, "
-                               "autotuned",
+                               "N(0,1)/(2l+1), FP32 samples; fftso3_batch, tensor-core buckets, CUDA graph",
                    "functions": n, "buckets": bt.buckets, "streams": bt.streams, "samples": int(G),
-                   "coefficients": int(Ctot), "autotune": "FFT launch shapes per N, bucket streams",
+                   "coefficients": int(Ctot),
+                   "form": ("three launches per direction over all buckets (slice FFT, fused GEMM, conversion)"
+                            if bt.graph_kernels(0) == 3 else "per-bucket phases around one fused GEMM launch"),
                    "l2": "inputs larger than L2"},
         "io_gbs": io_bytes / (ms / 1000.0) / 1e9, "io_frac_of_hbm": io_bytes / (ms / 1000.0) / 1e9 / peaks["hbm_gbs"],
         "batch_create_s": t_create, "device_gb": bt.device_bytes / 1e9,
@@ -425,8 +440,10 @@ def uneven_line(args) -> dict:
         "fp64_loop": fp64, "speedup_vs_fp64_loop": value / fp64["value"] if fp64 else None,
         "clocks": clocks, "gpu_launches": launches * args.steps,
         "stages_eager_sum_ms": stage_summary, "eager_timed_step_ms": eager_ms,
-        "top_buckets": [{"l_max": L, "functions": c, "ms": t, "stages": d} for t, L, c, d in per_bucket[:6]],
+        "graph_kernels": {"forward": bt.graph_kernels(0), "inverse": bt.graph_kernels(1)},
     }
+    if per_bucket and per_bucket[0][0] > 0:  # the per-bucket form: the costliest buckets
+        line["top_buckets"] = [{"l_max": L, "functions": c, "ms": t, "stages": d} for t, L, c, d in per_bucket[:6]]
     return line
 
 

@@ -75,6 +75,7 @@ SIGNATURES = {
     "fftso3_batch_coeff_offset": (_ll, [_vp, _i]),
     "fftso3_batch_bucket_count": (_i, [_vp]),
     "fftso3_batch_stream_count": (_i, [_vp]),
+    "fftso3_batch_graph_kernels": (_i, [_vp, _i]),
     "fftso3_batch_device_bytes": (_ll, [_vp]),
     "fftso3_batch_forward": (_i, [_vp, _vp, _vp, _vp]),
     "fftso3_batch_inverse": (_i, [_vp, _vp, _vp, _vp]),
@@ -282,6 +283,10 @@ class Batch:
     @property
     def device_bytes(self) -> int:
         return int(lib().fftso3_batch_device_bytes(self._h))
+
+    def graph_kernels(self, direction: int) -> int:
+        """Kernel nodes of the captured CUDA graph of direction 0 (forward) / 1 (inverse); -1 if none."""
+        return int(lib().fftso3_batch_graph_kernels(self._h, int(direction)))
 
     def forward(self, grid_ptr: int, coeff_ptr: int, stream: int = 0) -> None:
         check(lib().fftso3_batch_forward(self._h, _vp(grid_ptr), _vp(coeff_ptr), _vp(stream)))

@@ -20,18 +20,24 @@
 //    bucket's (group, row tile, column tile) items, longest first): forward =
 //    fork / per-bucket FFTs / join / fused GEMM / fork / per-bucket coefficient
 //    permutations / join, inverse the mirror image;
+//  * SO(3) tensor-core batches without refinement go further: each direction is
+//    three launches over all buckets (fused.cuh) -- one slice-FFT launch (every
+//    bucket's beta slices, a CTA per slice or per few slices), the fused GEMM,
+//    one coefficient-conversion launch -- on the caller's stream, no fork/join;
 //  * with FFTSO3_FLAG_GRAPH the whole fork / bucket launches / join sequence
 //    is captured once per (direction, input, output) into a CUDA graph and
 //    replayed with one cudaGraphLaunch afterwards, which removes the
 //    per-launch host cost of the several hundred small launches.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <numeric>
 #include <string>
 #include <vector>
 
 #include "../../include/fftso3_gb300.h"
 #include "common.cuh"
+#include "fused.cuh"
 #include "tc.cuh"
 
 using namespace fftso3;
@@ -76,13 +82,15 @@ struct fftso3_batch {
         cudaGraphExec_t exec = nullptr;
         const void* in = nullptr;
         void* out = nullptr;
+        int kernels = -1;                        // kernel nodes of the captured graph
     } graphs[2];
     long long bytes = 0;
     bool timing = false;                         // per-stage timing (eager launches, no graph)
     bool tuned = false;                          // stream count chosen (FFTSO3_FLAG_AUTOTUNE)
     int nstreams_used = 0;
     TCFused* fused = nullptr;                    // one GEMM launch over all buckets
-    StageTimer timer;                            // the fused GEMM's stage time
+    bool phases = false;                         // SO(3): three launches per direction over all buckets
+    StageTimer timer;                            // the fused launches' stage times
 };
 
 namespace {
@@ -219,6 +227,12 @@ int launch_all(fftso3_batch* b, int dir, const void* in, void* out, cudaStream_t
     };
     // timing mode runs the buckets one after another on the caller's stream (exact stage times)
     auto sof = [&](const fftso3_batch::Bucket& k) { return b->timing ? st : b->streams[k.stream]; };
+    if (b->phases) {
+        std::string err;
+        rc = dir == 0 ? tc_fused_forward(b->fused, in, out, st, &b->timer, err)
+                      : tc_fused_inverse(b->fused, in, out, st, &b->timer, err);
+        return rc ? bfail(rc, err) : FFTSO3_SUCCESS;
+    }
     if ((rc = fork_from(b, st))) return rc;
     if (!b->fused) {
         for (const auto& k : b->buckets) {
@@ -257,7 +271,7 @@ int run(fftso3_batch* b, int dir, const void* in, void* out, void* stream)
     if (rc) return rc;
     if (!in || !out) return bfail(FFTSO3_ERR_INVALID_ARG, "input/output pointer is NULL");
     cudaStream_t st = (cudaStream_t)stream;
-    if ((b->flags & FFTSO3_FLAG_AUTOTUNE) && !b->tuned && !b->timing)
+    if ((b->flags & FFTSO3_FLAG_AUTOTUNE) && !b->tuned && !b->timing && !b->phases)
         if ((rc = tune_streams(b, dir, in, out, st))) return rc;
     if (!(b->flags & FFTSO3_FLAG_GRAPH) || b->timing) return launch_all(b, dir, in, out, st);
 
@@ -278,6 +292,21 @@ int run(fftso3_batch* b, int dir, const void* in, void* out, void* stream)
             return rc;
         }
         if (e != cudaSuccess) return bcuda(e, "cudaStreamEndCapture");
+        {
+            size_t nn = 0;
+            g.kernels = -1;
+            if (cudaGraphGetNodes(graph, nullptr, &nn) == cudaSuccess) {
+                std::vector<cudaGraphNode_t> nodes(nn);
+                if (nn == 0 || cudaGraphGetNodes(graph, nodes.data(), &nn) == cudaSuccess) {
+                    int nk = 0;
+                    for (size_t i = 0; i < nn; ++i) {
+                        cudaGraphNodeType t;
+                        if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++nk;
+                    }
+                    g.kernels = nk;
+                }
+            }
+        }
         e = cudaGraphInstantiate(&g.exec, graph, 0);
         cudaGraphDestroy(graph);
         if (e != cudaSuccess) {
@@ -354,10 +383,24 @@ int fftso3_batch_create(fftso3_batch** out, int kind, const int* l_max, int n_fu
     b->goff[n_functions] = g;
     b->coff[n_functions] = c;
 
+    // SO(3) tensor-core batches without refinement run each direction as three launches over all buckets
+    // (slice FFT, GEMM, conversion) when one beta slice of the largest bandwidth fits a CTA's shared memory;
+    // their bucket plans then need no tuned FFT launch shapes.  FFTSO3_BATCH_PHASES=0 keeps the per-bucket
+    // phases around the fused GEMM.
+    bool want_phases = false;
+    if (precision == FFTSO3_PREC_TC_BF16X3 && !(flags & FFTSO3_FLAG_REFINE) && kind_is_so3(kind)) {
+        const char* ev = std::getenv("FFTSO3_BATCH_PHASES");
+        int maxsm = 0;
+        cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device);
+        want_phases = !(ev && ev[0] == '0') &&
+                      slice_fft_smem_bytes(2 * (b->buckets.back().L + 1), 1, real) <= (size_t)maxsm;
+    }
+    unsigned pflags = flags & (FFTSO3_FLAG_REFINE | FFTSO3_FLAG_AUTOTUNE);
+    if (want_phases) pflags &= ~FFTSO3_FLAG_AUTOTUNE;
+
     // one plan per bucket
     for (auto& k : b->buckets) {
-        int rc = fftso3_plan_create(&k.plan, kind, k.L, k.count, precision, recursion,
-                                    flags & (FFTSO3_FLAG_REFINE | FFTSO3_FLAG_AUTOTUNE));
+        int rc = fftso3_plan_create(&k.plan, kind, k.L, k.count, precision, recursion, pflags);
         if (rc) {
             k.plan = nullptr;
             std::string m = fftso3_last_error_string();
@@ -390,6 +433,21 @@ int fftso3_batch_create(fftso3_batch** out, int kind, const int* l_max, int n_fu
         for (auto& k : b->buckets) parts.push_back(plan_tc_state(k.plan));
         std::string err;
         int rc = tc_fused_create(&b->fused, parts, err);
+        if (!rc && want_phases) {
+            std::vector<long long> g0, c0;
+            for (auto& k : b->buckets) {
+                g0.push_back(k.g0);
+                c0.push_back(k.c0);
+            }
+            rc = tc_fused_phases(b->fused, g0, c0, err);
+            if (rc == FFTSO3_SUCCESS) {
+                b->phases = true;
+                b->tuned = true;
+                b->nstreams_used = 1;
+            } else if (rc == FFTSO3_ERR_UNSUPPORTED) {
+                rc = FFTSO3_SUCCESS;
+            }
+        }
         if (rc) {
             bail(rc);
             return bfail(rc, err);
@@ -427,6 +485,12 @@ long long fftso3_batch_coeff_offset(const fftso3_batch* b, int fn)
 int fftso3_batch_bucket_count(const fftso3_batch* b) { return b ? (int)b->buckets.size() : -1; }
 
 int fftso3_batch_stream_count(const fftso3_batch* b) { return b ? b->nstreams_used : -1; }
+
+int fftso3_batch_graph_kernels(const fftso3_batch* b, int direction)
+{
+    if (!b || direction < 0 || direction > 1) return -1;
+    return b->graphs[direction].exec ? b->graphs[direction].kernels : -1;
+}
 
 long long fftso3_batch_device_bytes(const fftso3_batch* b) { return b ? b->bytes : -1; }
 

@@ -47,6 +47,20 @@ __host__ __device__ __forceinline__ GroupPairs group_pairs(int m0, int n0) {
     return p;
 }
 
+// (m, n) -> (symmetry group g, pair p) consistent with group_pairs(): m0 = max(|m|, |n|), g = m0^2 + m0 + n0.
+__host__ __device__ __forceinline__ void pair_of(int m, int n, int& g, int& p) {
+    int m0, n0;
+    const int am = m < 0 ? -m : m, an = n < 0 ? -n : n;
+    if (am >= an) {
+        if (m >= 0) { m0 = m; n0 = n; p = 0; }
+        else { m0 = -m; n0 = -n; p = 1; }
+    } else {
+        if (n > 0) { m0 = n; n0 = m; p = 2; }
+        else { m0 = -n; n0 = -m; p = 3; }
+    }
+    g = m0 * m0 + m0 + n0;
+}
+
 // Records the message returned by fftso3_last_error_string() on this thread.
 void set_last_error(const std::string& msg);
 

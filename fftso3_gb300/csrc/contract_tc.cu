@@ -44,6 +44,7 @@
 #include "../../include/fftso3_gb300.h"
 #include "common.cuh"
 #include "contract.cuh"
+#include "fused.cuh"
 #include "tc.cuh"
 #include "tc_ptx.cuh"
 
@@ -849,21 +850,6 @@ __global__ void zero_nyquist_pencils_kernel(float2* __restrict__ H, int N, long 
     long long off = (which == 0) ? (((long long)B * N + a) * N + k) : ((a * N + B) * N + k);
     H[f * (long long)N * N * N + off] = make_float2(0.f, 0.f);
 }
-
-// (m, n) -> (symmetry group, pair) consistent with group_pairs().
-__device__ __forceinline__ void pair_of(int m, int n, int& g, int& p)
-{
-    int m0, n0;
-    if (abs(m) >= abs(n)) {
-        if (m >= 0) { m0 = m; n0 = n; p = 0; }
-        else { m0 = -m; n0 = -n; p = 1; }
-    } else {
-        if (n > 0) { m0 = n; n0 = m; p = 2; }
-        else { m0 = -n; n0 = -m; p = 3; }
-    }
-    g = m0 * m0 + m0 + n0;
-}
-
 
 // Tiled permutations between the group-major layout (contiguous in l for a
 // fixed (m, n)) and the packed layout (contiguous in m for a fixed (l, n)):
@@ -1904,11 +1890,19 @@ struct TCFused {
     int* d_err = nullptr;
     int nsm = 0;
     bool s2 = false;
+    // three-launch directions (SO(3) batches, tc_fused_phases): the bucket table of the slice FFT and the
+    // coefficient conversions
+    BucketSeg* d_bseg = nullptr;
+    int nbseg = 0;
+    long long nblk = 0, ncoef = 0;
+    size_t slice_smem = 0;
+    bool real = false;
 };
 
 void tc_fused_destroy(TCFused* f)
 {
     if (!f) return;
+    if (f->d_bseg) cudaFree(f->d_bseg);
     for (int d = 0; d < 2; ++d) {
         if (f->d_segs[d]) cudaFree(f->d_segs[d]);
         if (f->d_items[d]) cudaFree(f->d_items[d]);
@@ -2022,6 +2016,117 @@ int tc_fused_gemm(TCFused* f, bool fwd, cudaStream_t st, StageTimer* T, std::str
     else
         so3_tc_gemm_kernel<false, false, true><<<nctas, THREADS, SMEM_BYTES, st>>>(tm[0], tm[1], tm[2], a, f->d_segs[d]);
     TCK(cudaGetLastError());
+    T->end(st);
+    return FFTSO3_SUCCESS;
+}
+
+// The bucket table of the three-launch directions.  Buckets run longest slices first (descending N) in both
+// the slice FFT and the conversions; a CTA of the slice FFT takes as many slices of its bucket as the launch's
+// shared memory (sized for one slice of the largest N) holds, up to about the largest slice's sample count, so
+// small bandwidths get as much work per CTA as large ones.
+int tc_fused_phases(TCFused* f, const std::vector<long long>& g0, const std::vector<long long>& c0, std::string& err)
+{
+    const size_t n = f->parts.size();
+    if (f->s2 || g0.size() != n || c0.size() != n) {
+        err = "fused phases: SO(3) plans with one grid and one coefficient offset each";
+        return FFTSO3_ERR_UNSUPPORTED;
+    }
+    const bool real = f->parts[0]->real;
+    int Nmax = 0;
+    size_t smem = 0;
+    for (TCState* p : f->parts) {
+        if (p->real != real || p->refine || p->simt) {
+            err = "fused phases: tensor-core plans of one kind without refinement";
+            return FFTSO3_ERR_UNSUPPORTED;
+        }
+        Nmax = std::max(Nmax, p->N);
+        smem = std::max(smem, slice_fft_smem_bytes(p->N, 1, real));
+    }
+    int maxsm = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (smem > (size_t)maxsm) {
+        err = "fused phases: one beta slice of N = " + std::to_string(Nmax) + " exceeds the shared memory of a CTA";
+        return FFTSO3_ERR_UNSUPPORTED;
+    }
+    std::vector<int> ord(n);
+    for (size_t i = 0; i < n; ++i) ord[i] = (int)i;
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return f->parts[a]->N > f->parts[b]->N; });
+    std::vector<BucketSeg> segs;
+    long long blk = 0, coef = 0;
+    for (int i : ord) {
+        TCState* p = f->parts[i];
+        const int N = p->N;
+        BucketSeg s{};
+        s.L = p->L;
+        s.B = p->B;
+        s.N = N;
+        s.batch = p->batch;
+        s.G = slice_lines_per_group(N);
+        int spc = 1;
+        while (slice_fft_smem_bytes(N, spc + 1, real) <= smem && (long long)(spc + 1) * N * N <= (long long)Nmax * Nmax)
+            ++spc;
+        s.spc = spc;
+        s.fac = p->fac;
+        s.tw = reinterpret_cast<const double2*>(p->d_tw);
+        s.pencil = p->d_pencil;
+        s.fg = p->d_fg;
+        s.goff2 = p->d_goff2;
+        s.g0 = g0[i];
+        s.c0 = c0[i];
+        s.blk0 = blk;
+        s.coef0 = coef;
+        blk += ((long long)p->batch * N + spc - 1) / spc;
+        coef += (long long)p->batch * so3_off(p->B);
+        segs.push_back(s);
+    }
+    cudaError_t e;
+    if (f->d_bseg) cudaFree(f->d_bseg);
+    f->d_bseg = nullptr;
+    if ((e = cudaMalloc(&f->d_bseg, sizeof(BucketSeg) * segs.size())) != cudaSuccess ||
+        (e = cudaMemcpy(f->d_bseg, segs.data(), sizeof(BucketSeg) * segs.size(), cudaMemcpyHostToDevice)) !=
+            cudaSuccess) {
+        err = std::string("fused phases: ") + cudaGetErrorString(e);
+        return FFTSO3_ERR_CUDA;
+    }
+    f->nbseg = (int)segs.size();
+    f->nblk = blk;
+    f->ncoef = coef;
+    f->slice_smem = smem;
+    f->real = real;
+    return FFTSO3_SUCCESS;
+}
+
+int tc_fused_forward(TCFused* f, const void* grid, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err)
+{
+    if (!f->d_bseg) {
+        err = "internal: fused phases were not set up";
+        return FFTSO3_ERR_CUDA;
+    }
+    T->begin(ST_FFT_SLICES, st);
+    TCK(launch_slice_fft(f->d_bseg, f->nbseg, f->nblk, f->slice_smem, true, f->real, grid, nullptr, st));
+    T->end(st);
+    int rc = tc_fused_gemm(f, true, st, T, err);
+    if (rc) return rc;
+    T->begin(ST_CONVERT, st);
+    TCK(launch_fused_group_to_packed(f->d_bseg, f->nbseg, f->ncoef, f->real, coeffs, st));
+    T->end(st);
+    return FFTSO3_SUCCESS;
+}
+
+int tc_fused_inverse(TCFused* f, const void* coeffs, void* grid, cudaStream_t st, StageTimer* T, std::string& err)
+{
+    if (!f->d_bseg) {
+        err = "internal: fused phases were not set up";
+        return FFTSO3_ERR_CUDA;
+    }
+    T->begin(ST_CONVERT, st);
+    TCK(launch_fused_packed_to_group(f->d_bseg, f->nbseg, f->ncoef, f->real, coeffs, st));
+    T->end(st);
+    int rc = tc_fused_gemm(f, false, st, T, err);
+    if (rc) return rc;
+    T->begin(ST_FFT_SLICES, st);
+    TCK(launch_slice_fft(f->d_bseg, f->nbseg, f->nblk, f->slice_smem, false, f->real, nullptr, grid, st));
     T->end(st);
     return FFTSO3_SUCCESS;
 }

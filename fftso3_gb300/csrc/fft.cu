@@ -16,6 +16,7 @@
 #include "common.cuh"
 #include "df32.cuh"
 #include "fft.cuh"
+#include "fused.cuh"
 
 namespace fftso3 {
 
@@ -536,6 +537,252 @@ __global__ void __launch_bounds__(256, 3) fft_df32_k_kernel(dfc32* __restrict__ 
         const int e = tid + 256 * u, kk2 = e % TK, j = e / TK;
         buf[obase + (long long)j * S + kk2] = sm[kk2 * ROW + phys(j)];
     }
+}
+
+// ---- both FFT passes of the beta slices of an uneven batch, every bucket in one launch
+//
+// A CTA takes spc consecutive beta slices (N x N each, N = 2B) of one bucket and holds them in shared memory;
+// each pass moves groups of G lines into a line buffer, runs the same Stockham stages as fft_lines_kernel
+// (prime-first factors) between two line buffers and writes the lines back, so the grid slab is read (or
+// written) once and the pencils written (or read) once.  Real data keep only the columns q = 0..N/2 of the
+// Hermitian half-spectrum: the forward transforms two real rows per complex line (z = x_a + i x_b, separated
+// as in fft_lines_kernel) and N/2 + 1 columns, and writes each pencil (p, q), 0 < q < N/2, a second time as
+// its mirror (-p, -q) = conj; the inverse takes the Hermitian part H = (P(p, q) + conj P(-p, -q)) / 2 of the
+// pencils (the real part of the complex synthesis is the synthesis of H), transforms N/2 + 1 columns and then
+// two rows per complex line (z = Y_a + i Y_b, the real and imaginary parts of its transform are the rows).
+// Column lines are ordered slice-fastest, so the pencil accesses of neighbouring lines are consecutive k.
+__device__ float2* run_line_stages(float2* src, float2* dst, const float2* w, const float2* mat,
+                                   const FFTFactors& fac, int N, int nl, int LS)
+{
+    int Ns = 1;
+    const int ns = fac.n;
+    for (int s = 0; s < ns; ++s) {
+        const int R = fac.r[s];
+        switch (R) {
+            case 2: stockham_stage<float, 2>(src, dst, w, N, Ns, nl, LS); break;
+            case 3: stockham_stage<float, 3>(src, dst, w, N, Ns, nl, LS); break;
+            case 4: stockham_stage<float, 4>(src, dst, w, N, Ns, nl, LS); break;
+            case 5: stockham_stage<float, 5>(src, dst, w, N, Ns, nl, LS); break;
+            case 7: stockham_stage<float, 7>(src, dst, w, N, Ns, nl, LS); break;
+            case 8: stockham_stage<float, 8>(src, dst, w, N, Ns, nl, LS); break;
+            default:
+                if (Ns == 1) dft_prime_first<float>(src, dst, mat, N, R, nl, LS);
+                else stockham_generic<float>(src, dst, w, N, Ns, R, nl, LS);
+                break;
+        }
+        __syncthreads();
+        float2* t = src;
+        src = dst;
+        dst = t;
+        Ns *= R;
+    }
+    return src;
+}
+
+static int slice_prime_entries(const FFTFactors& f) { return f.r[0] > 8 ? prime_mat_entries(f.r[0]) : 0; }
+
+size_t slice_fft_smem_bytes(int N, int spc, bool real)
+{
+    FFTFactors f;
+    make_fft_factors_prime_first(N, f);
+    const size_t sst = (size_t)N * slice_row_stride(N, real) + 1;
+    const size_t G = (size_t)slice_lines_per_group(N);
+    return sizeof(float2) * (spc * sst + 2 * G * (N + 1) + N + slice_prime_entries(f));
+}
+
+template <bool FWD, bool REAL>
+__global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const BucketSeg* __restrict__ segs, int nseg,
+                                                                    const void* __restrict__ in,
+                                                                    void* __restrict__ out)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int sb;
+    const long long blk = blockIdx.x;
+    if (threadIdx.x == 0) {
+        int lo = 0, hi = nseg - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (segs[mid].blk0 <= blk) lo = mid;
+            else hi = mid - 1;
+        }
+        sb = lo;
+    }
+    __syncthreads();
+    const BucketSeg& S = segs[sb];
+    const int N = S.N, B = N / 2, LS = N + 1, G = S.G, spc = S.spc;
+    const int RS = slice_row_stride(N, REAL), NC = REAL ? B + 1 : N;
+    const int SSt = N * RS + 1;
+    const long long NN = (long long)N * N, NNN = NN * N;
+    const long long s0 = (blk - S.blk0) * spc;
+    const int ns = (int)min((long long)spc, (long long)S.batch * N - s0);
+    const int T = blockDim.x;
+    float2* X = reinterpret_cast<float2*>(smem_raw);
+    float2* A = X + (size_t)spc * SSt;
+    float2* Bf = A + G * LS;
+    float2* w = Bf + G * LS;
+    float2* mat = w + N;
+    const double2* tw = S.tw;
+    for (int i = threadIdx.x; i < N; i += T) w[i] = make_float2((float)tw[i].x, (float)tw[i].y);
+    if (S.fac.r[0] > 8) {
+        const int R = S.fac.r[0], P = (R - 1) / 2, P4 = (P + 3) / 4 * 4, Nr = N / R;
+        for (int i = threadIdx.x; i < P * P4; i += T) {
+            const int t = i / P4 + 1, q = i - (t - 1) * P4 + 1;
+            float c = 0.f, sn = 0.f;
+            if (q <= P) {
+                const double2 v = tw[((t * q) % R) * Nr];  // e^{-2 pi i t q / R}
+                c = (float)v.x;
+                sn = (float)(-v.y);
+            }
+            mat[i] = make_float2(c, sn);
+        }
+    }
+    const int NR = REAL ? B : N;  // row lines per slice
+    if (FWD) {
+        // rows: grid -> line buffer -> slice rows (real: the two half-spectra of each row pair)
+        const int nlr = ns * NR;
+        __syncthreads();
+        for (int l0 = 0; l0 < nlr; l0 += G) {
+            const int nl = min(G, nlr - l0), nle = (nl + 1) & ~1;
+            for (int e = threadIdx.x; e < nl * N; e += T) {
+                const int l = e / N, j = e - l * N, line = l0 + l;
+                const int s = line / NR, r = line - s * NR;
+                const long long base = S.g0 + (s0 + s) * NN;
+                if (REAL) {
+                    const float* g = reinterpret_cast<const float*>(in) + base + (long long)(2 * r) * N + j;
+                    A[l * LS + j] = make_float2(g[0], g[N]);
+                } else {
+                    A[l * LS + j] = reinterpret_cast<const float2*>(in)[base + (long long)r * N + j];
+                }
+            }
+            __syncthreads();
+            const float2* res = run_line_stages(A, Bf, w, mat, S.fac, N, nle, LS);
+            for (int e = threadIdx.x; e < nl * NC; e += T) {
+                const int l = e / NC, q = e - l * NC, line = l0 + l;
+                const int s = line / NR, r = line - s * NR;
+                float2* x = X + s * SSt;
+                if (REAL) {
+                    const float2 z = res[l * LS + q], zm = res[l * LS + (q == 0 ? 0 : N - q)];
+                    x[(2 * r) * RS + q] = make_float2(0.5f * (z.x + zm.x), 0.5f * (z.y - zm.y));
+                    x[(2 * r + 1) * RS + q] = make_float2(0.5f * (z.y + zm.y), -0.5f * (z.x - zm.x));
+                } else {
+                    x[r * RS + q] = res[l * LS + q];
+                }
+            }
+            __syncthreads();
+        }
+        // columns: slice -> line buffer -> pencils
+        const int nlc = ns * NC;
+        for (int l0 = 0; l0 < nlc; l0 += G) {
+            const int nl = min(G, nlc - l0), nle = (nl + 1) & ~1;
+            for (int e = threadIdx.x; e < nl * N; e += T) {
+                const int j = e / nl, l = e - j * nl, line = l0 + l;
+                const int q = line / ns, s = line - q * ns;
+                A[l * LS + j] = X[s * SSt + j * RS + q];
+            }
+            __syncthreads();
+            const float2* res = run_line_stages(A, Bf, w, mat, S.fac, N, nle, LS);
+            for (int e = threadIdx.x; e < nl * N; e += T) {
+                const int p = e / nl, l = e - p * nl, line = l0 + l;
+                const int q = line / ns, s = line - q * ns;
+                const long long sl = s0 + s, f = sl / N;
+                float2* P = S.pencil + f * NNN + (sl - f * N);
+                const float2 v = res[l * LS + p];
+                P[((long long)p * N + q) * N] = v;
+                if (REAL && q > 0 && q < B)
+                    P[((long long)(p == 0 ? 0 : N - p) * N + (N - q)) * N] = make_float2(v.x, -v.y);
+            }
+            __syncthreads();
+        }
+    } else {
+        // pencils -> slice (Nyquist bins zero; real: the Hermitian part)
+        for (int e = threadIdx.x; e < ns * N * NC; e += T) {
+            const int s = e % ns, pq = e / ns, q = pq % NC, p = pq / NC;
+            const long long sl = s0 + s, f = sl / N;
+            const float2* P = S.pencil + f * NNN + (sl - f * N);
+            float2 v = make_float2(0.f, 0.f);
+            if (p != B && q != B) {
+                v = P[((long long)p * N + q) * N];
+                if (REAL) {
+                    const float2 u = P[((long long)(p == 0 ? 0 : N - p) * N + (q == 0 ? 0 : N - q)) * N];
+                    v = make_float2(0.5f * (v.x + u.x), 0.5f * (v.y - u.y));
+                }
+            }
+            X[s * SSt + p * RS + q] = v;
+        }
+        __syncthreads();
+        // columns (along p), in place in the slice
+        const int nlc = ns * NC;
+        for (int l0 = 0; l0 < nlc; l0 += G) {
+            const int nl = min(G, nlc - l0), nle = (nl + 1) & ~1;
+            for (int e = threadIdx.x; e < nl * N; e += T) {
+                const int j = e / nl, l = e - j * nl, line = l0 + l;
+                const int q = line / ns, s = line - q * ns;
+                A[l * LS + j] = X[s * SSt + j * RS + q];
+            }
+            __syncthreads();
+            const float2* res = run_line_stages(A, Bf, w, mat, S.fac, N, nle, LS);
+            for (int e = threadIdx.x; e < nl * N; e += T) {
+                const int j = e / nl, l = e - j * nl, line = l0 + l;
+                const int q = line / ns, s = line - q * ns;
+                X[s * SSt + j * RS + q] = res[l * LS + j];
+            }
+            __syncthreads();
+        }
+        // rows: slice -> line buffer -> grid (real: two rows per complex line)
+        const int nlr = ns * NR;
+        for (int l0 = 0; l0 < nlr; l0 += G) {
+            const int nl = min(G, nlr - l0), nle = (nl + 1) & ~1;
+            for (int e = threadIdx.x; e < nl * N; e += T) {
+                const int l = e / N, j = e - l * N, line = l0 + l;
+                const int s = line / NR, r = line - s * NR;
+                const float2* x = X + s * SSt;
+                if (REAL) {
+                    float2 ya, yb;
+                    if (j <= B) {
+                        ya = x[(2 * r) * RS + j];
+                        yb = x[(2 * r + 1) * RS + j];
+                    } else {
+                        ya = x[(2 * r) * RS + N - j];
+                        yb = x[(2 * r + 1) * RS + N - j];
+                        ya.y = -ya.y;
+                        yb.y = -yb.y;
+                    }
+                    A[l * LS + j] = make_float2(ya.x - yb.y, ya.y + yb.x);
+                } else {
+                    A[l * LS + j] = x[r * RS + j];
+                }
+            }
+            __syncthreads();
+            const float2* res = run_line_stages(A, Bf, w, mat, S.fac, N, nle, LS);
+            for (int e = threadIdx.x; e < nl * N; e += T) {
+                const int l = e / N, j = e - l * N, line = l0 + l;
+                const int s = line / NR, r = line - s * NR;
+                const long long base = S.g0 + (s0 + s) * NN;
+                const float2 v = res[l * LS + j];
+                if (REAL) {
+                    float* g = reinterpret_cast<float*>(out) + base + (long long)(2 * r) * N + j;
+                    g[0] = v.x;
+                    g[N] = v.y;
+                } else {
+                    reinterpret_cast<float2*>(out)[base + (long long)r * N + j] = v;
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+cudaError_t launch_slice_fft(const BucketSeg* segs, int nseg, long long nblk, size_t smem, bool fwd, bool real,
+                             const void* in, void* out, cudaStream_t st)
+{
+    if (nblk <= 0) return cudaSuccess;
+    if (nblk > 0x7fffffffLL || nseg <= 0) return cudaErrorInvalidValue;
+    auto kern = fwd ? (real ? slice_fft_kernel<true, true> : slice_fft_kernel<true, false>)
+                    : (real ? slice_fft_kernel<false, true> : slice_fft_kernel<false, false>);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<(unsigned)nblk, SLICE_THREADS, smem, st>>>(segs, nseg, in, out);
+    return cudaGetLastError();
 }
 
 bool fft_df32_k_supported(int N) { return N == 64 || N == 128 || N == 256 || N == 512; }

@@ -1,0 +1,53 @@
+// Launches that span every l_max bucket of an uneven SO(3) tensor-core batch (fftso3_batch_*): with the fused
+// beta-sum GEMM (contract_tc.cu) a direction is three launches,
+//   forward: slice FFT (grid slabs -> pencils), GEMM, group-major -> packed coefficients (+ real basis);
+//   inverse: packed (+ real basis) -> scaled group-major, GEMM, slice FFT (pencils -> grid slabs).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "fft.cuh"
+
+namespace fftso3 {
+
+// One bucket: its sizes, FFT factors and twiddles, the bucket plan's pencils and group-major coefficients, the
+// element offsets of its slab in the caller's grid and coefficient buffers, and its first work index in each
+// fused launch.  A launch's segment table is ordered by its work index (blk0 and coef0 ascending).
+struct BucketSeg {
+    int L, B, N, batch;
+    int spc;                     // beta slices per CTA of the slice FFT
+    int G;                       // lines per Stockham group of the slice FFT (even)
+    FFTFactors fac;              // prime-first factors of N
+    const double2* tw;           // W[i] = e^{-2 pi i i / N}
+    float2* pencil;              // [fn][p][q][k]
+    float2* fg;                  // group-major coefficients [fn][so3_off(B)]
+    const long long* goff2;      // group-major offsets, B^2 + 1 entries
+    long long g0, c0;            // slab offsets (elements) in the caller's grids / coefficients
+    long long blk0;              // first CTA of the bucket in the slice FFT
+    long long coef0;             // first thread of the bucket in the coefficient conversions
+};
+
+constexpr int SLICE_THREADS = 256;
+constexpr int SLICE_LINE_ELEMS = 2048;  // elements of each of the two Stockham line buffers
+
+// Row stride of a slice in shared memory (complex: all N columns; real: columns 0..N/2 of the Hermitian
+// half-spectrum), odd so that column walks meet distinct banks, and the shared memory one CTA of the slice
+// FFT needs for spc slices of size N.
+__host__ __device__ inline int slice_row_stride(int N, bool real) { return real ? ((N / 2 + 1) | 1) : N + 1; }
+__host__ __device__ inline int slice_lines_per_group(int N) { return (SLICE_LINE_ELEMS / (N + 1)) & ~1; }
+size_t slice_fft_smem_bytes(int N, int spc, bool real);
+
+// Both FFT passes of the beta slices of every bucket in one launch (nblk CTAs, smem bytes of dynamic shared
+// memory each): fwd: grid slabs (complex64, or float32 when real) -> pencils; else pencils (Nyquist bins read
+// as zero; real: their Hermitian part) -> grid slabs (float32 when real).
+cudaError_t launch_slice_fft(const BucketSeg* segs, int nseg, long long nblk, size_t smem, bool fwd, bool real,
+                             const void* in, void* out, cudaStream_t st);
+
+// Coefficient conversions of every bucket in one launch (one thread per coefficient, ncoef in total):
+//   forward: group-major GEMM output -> packed coefficients (complex64, or the real basis in float32);
+//   inverse: packed coefficients (complex64 / real float32) -> group-major (2l + 1) sign F.
+cudaError_t launch_fused_group_to_packed(const BucketSeg* segs, int nseg, long long ncoef, bool real, void* out,
+                                         cudaStream_t st);
+cudaError_t launch_fused_packed_to_group(const BucketSeg* segs, int nseg, long long ncoef, bool real, const void* in,
+                                         cudaStream_t st);
+
+}  // namespace fftso3

@@ -41,6 +41,13 @@ int tc_fused_create(TCFused** out, const std::vector<TCState*>& parts, std::stri
 void tc_fused_destroy(TCFused* f);
 int tc_fused_gemm(TCFused* f, bool fwd, cudaStream_t st, StageTimer* T, std::string& err);
 int tc_fused_status(TCFused* f);
+// Three launches per direction over SO(3) plans of one kind without refinement (fused.cuh): slice FFT, GEMM,
+// conversion (forward) and the mirror image (inverse).  Plan i's functions sit at element offsets g0[i] / c0[i]
+// of the caller's grids / coefficients.  FFTSO3_ERR_UNSUPPORTED when one beta slice of the largest N does not
+// fit a CTA's shared memory (the per-plan phases then serve).
+int tc_fused_phases(TCFused* f, const std::vector<long long>& g0, const std::vector<long long>& c0, std::string& err);
+int tc_fused_forward(TCFused* f, const void* grid, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err);
+int tc_fused_inverse(TCFused* f, const void* coeffs, void* grid, cudaStream_t st, StageTimer* T, std::string& err);
 
 // Row-major 2-D BF16 tensor map (inner elements per row, outer rows; 128-byte swizzle, boxes of
 // box_inner x box_outer), resolved through the runtime's driver entry point.

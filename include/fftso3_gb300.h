@@ -214,9 +214,16 @@ int fftso3_clebsch_gordan(int l1, int l2, int real, void* out_host);
  * forward_transform / inverse_transform calls over functions
  * (fdcl_FFTSO3.cpp:654-763, :774-850, :1141-1167; fdcl_FFTS2.cpp:125-230,
  * :424-512), re-initialising the object whenever l_max changes (:500).
- * Functions are bucketed by l_max and every bucket runs as one batched plan;
- * the buckets run side by side on internal streams forked from and joined
- * into the caller's stream.
+ * Functions are bucketed by l_max and every bucket runs as one batched plan.
+ * Tensor-core SO(3) batches without refinement run each direction as three
+ * launches over all buckets on the caller's stream (forward: one launch of
+ * both FFT passes of every beta slice, one persistent beta-sum GEMM, one
+ * coefficient conversion; the inverse mirrors it) whenever one beta slice of
+ * the largest l_max fits a CTA's shared memory (l_max <= 77 complex, about
+ * <= 105 real); otherwise the buckets run side by side on internal streams forked
+ * from and joined into the caller's stream (tensor-core batches still share
+ * one GEMM launch).  FFTSO3_BATCH_PHASES=0 in the environment at creation
+ * selects the per-bucket form for every batch.
  * Layout: function i's grid starts fftso3_batch_grid_offset(b, i) elements
  * into `grids` and its coefficients fftso3_batch_coeff_offset(b, i) elements
  * into `coeffs` (elements of the kind's and precision's type, as for plans);
@@ -236,6 +243,9 @@ long long fftso3_batch_coeff_offset(const fftso3_batch* batch, int fn);
 int fftso3_batch_bucket_count(const fftso3_batch* batch);
 /* Internal streams the buckets are spread over (chosen by FFTSO3_FLAG_AUTOTUNE on the first call). */
 int fftso3_batch_stream_count(const fftso3_batch* batch);
+/* Kernel nodes of the CUDA graph captured for direction 0 (forward) or 1
+ * (inverse) with FFTSO3_FLAG_GRAPH; -1 before the first capture. */
+int fftso3_batch_graph_kernels(const fftso3_batch* batch, int direction);
 long long fftso3_batch_device_bytes(const fftso3_batch* batch);
 int fftso3_batch_forward(fftso3_batch* batch, const void* grids, void* coeffs, void* stream);
 int fftso3_batch_inverse(fftso3_batch* batch, const void* coeffs, void* grids, void* stream);

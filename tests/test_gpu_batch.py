@@ -4,6 +4,8 @@ Tolerances: the FP64 batch equals per-function FP64 plans bit for bit (same
 kernels, same arithmetic per function); tensor-core results are within
 1e-6 relative of the FP64 oracle, as for plans.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -143,14 +145,29 @@ def test_autotuned_plan_and_batch(gblib, oracle, torch_cuda):
         assert rel_err(co[b.coeff_offset(i):b.coeff_offset(i) + Fs[i].size], Fs[i]) < TOL
 
 
+def _per_bucket_batch(gblib, *args):
+    """A batch created with FFTSO3_BATCH_PHASES=0: per-bucket phases around the one fused GEMM launch."""
+    old = os.environ.get("FFTSO3_BATCH_PHASES")
+    os.environ["FFTSO3_BATCH_PHASES"] = "0"
+    try:
+        return gblib.Batch(*args)
+    finally:
+        if old is None:
+            del os.environ["FFTSO3_BATCH_PHASES"]
+        else:
+            os.environ["FFTSO3_BATCH_PHASES"] = old
+
+
 def test_fused_gemm_batch_equals_bucket_plans(gblib, torch_cuda):
-    """A tensor-core batch runs one GEMM launch over all buckets; every item is computed exactly as the
-    bucket's own plan computes it, so the results are bit-identical to one plan per l_max (complex SO(3))."""
+    """The per-bucket form (FFTSO3_BATCH_PHASES=0) runs one GEMM launch over all buckets; every item is computed
+    exactly as the bucket's own plan computes it, so the results are bit-identical to one plan per l_max
+    (complex SO(3))."""
     torch = torch_cuda
     s = torch.cuda.current_stream().cuda_stream
     lmax = [12, 20, 12, 31, 20, 12]
     kind = gblib.SO3_COMPLEX
-    b = gblib.Batch(kind, lmax, "tc_bf16x3", "reference", 0)
+    b = _per_bucket_batch(gblib, kind, lmax, "tc_bf16x3", "reference", 0)
+    assert b.streams >= 1
     Fs = [so3_coeffs(L, seed=1700 + i, decay="pow").astype(np.complex64) for i, L in enumerate(lmax)]
     cbuf = np.zeros(b.coeff_elems, dtype=np.complex64)
     for i in range(len(lmax)):
@@ -173,3 +190,76 @@ def test_fused_gemm_batch_equals_bucket_plans(gblib, torch_cuda):
         p.check()
         assert torch.equal(gp, g[g0:g0 + n_g])
         assert torch.equal(cp, c2[c0:c0 + n_c])
+
+
+@pytest.mark.parametrize("kind", ["complex", "real"])
+def test_three_launch_batch(gblib, oracle, torch_cuda, kind):
+    """SO(3) tensor-core batches run each direction as three launches over all buckets (slice FFT, fused GEMM,
+    coefficient conversion): the captured graphs hold three kernel nodes per direction, on one stream.  Results
+    within 1e-6 of the oracle, and within 1e-6 (relative) of one plan per l_max -- the slice FFT rounds
+    differently from the plans' FFTs.  l_max 60 (N = 122 = 2 * 61) takes the prime first stage; several slices
+    share a CTA for the small l_max."""
+    torch = torch_cuda
+    s = torch.cuda.current_stream().cuda_stream
+    cplx = kind == "complex"
+    k = gblib.SO3_COMPLEX if cplx else gblib.SO3_REAL
+    lmax = [8, 12, 8, 20, 15, 12, 31, 9, 8, 46, 60, 33, 60]
+    b = gblib.Batch(k, lmax, "tc_bf16x3", "reference", gblib.FLAG_GRAPH)
+    _layout_ok(b, lmax, k, gblib)
+    Fs = [so3_coeffs(L, seed=1900 + i, complex_=cplx) for i, L in enumerate(lmax)]
+    inv = oracle.so3_inverse_complex_grid if cplx else oracle.so3_inverse_real_grid
+    grids = [inv(L, F) for L, F in zip(lmax, Fs)]
+    npt, tt = (np.complex64, torch.complex64) if cplx else (np.float32, torch.float32)
+    gbuf = np.zeros(b.grid_elems, dtype=npt)
+    cbuf = np.zeros(b.coeff_elems, dtype=npt)
+    for i in range(len(lmax)):
+        gbuf[b.grid_offset(i):b.grid_offset(i) + grids[i].size] = grids[i].ravel()
+        cbuf[b.coeff_offset(i):b.coeff_offset(i) + Fs[i].size] = Fs[i]
+    g = torch.from_numpy(gbuf).cuda()
+    c = torch.from_numpy(cbuf).cuda()
+    cout = torch.zeros_like(c)
+    gout = torch.zeros_like(g)
+    for _ in range(2):  # capture, then replay
+        b.forward(g.data_ptr(), cout.data_ptr(), s)
+        b.inverse(c.data_ptr(), gout.data_ptr(), s)
+    b.check()
+    assert b.graph_kernels(0) == 3 and b.graph_kernels(1) == 3
+    assert b.streams == 1
+    wide = np.complex128 if cplx else np.float64
+    co = cout.cpu().numpy().astype(wide)
+    go = gout.cpu().numpy().astype(wide)
+    for i, L in enumerate(lmax):
+        F_i = co[b.coeff_offset(i):b.coeff_offset(i) + Fs[i].size]
+        g_i = go[b.grid_offset(i):b.grid_offset(i) + grids[i].size]
+        assert rel_err(F_i, Fs[i]) < TOL, (i, L)
+        assert rel_err(g_i, grids[i].ravel()) < TOL, (i, L)
+    for L in sorted(set(lmax)):
+        idx = [i for i in range(len(lmax)) if lmax[i] == L]
+        p = gblib.Plan(k, L, len(idx), "tc_bf16x3", "reference")
+        g0, c0 = b.grid_offset(idx[0]), b.coeff_offset(idx[0])
+        n_g, n_c = len(idx) * p.grid_elems, len(idx) * p.coeff_elems
+        gp = torch.empty(n_g, dtype=tt, device="cuda")
+        cp = torch.empty(n_c, dtype=tt, device="cuda")
+        p.inverse(c[c0:c0 + n_c].data_ptr(), gp.data_ptr(), s)
+        p.forward(g[g0:g0 + n_g].data_ptr(), cp.data_ptr(), s)
+        p.check()
+        assert rel_err(go[g0:g0 + n_g], gp.cpu().numpy().astype(wide)) < 1e-6, L
+        assert rel_err(co[c0:c0 + n_c], cp.cpu().numpy().astype(wide)) < 1e-6, L
+
+
+def test_three_launch_eager_timing(gblib, torch_cuda):
+    """With stage timing on, a three-launch batch runs eagerly and reports one slice-FFT, one GEMM and one
+    conversion launch per direction; the per-bucket form reports its per-bucket launches instead."""
+    torch = torch_cuda
+    s = torch.cuda.current_stream().cuda_stream
+    lmax = [8, 16, 8, 24]
+    b = gblib.Batch(gblib.SO3_REAL, lmax, "tc_bf16x3", "reference", gblib.FLAG_GRAPH)
+    g = torch.zeros(b.grid_elems, dtype=torch.float32, device="cuda")
+    c = torch.zeros(b.coeff_elems, dtype=torch.float32, device="cuda")
+    b.set_timing(True)
+    b.forward(g.data_ptr(), c.data_ptr(), s)
+    b.inverse(c.data_ptr(), g.data_ptr(), s)
+    b.check()
+    got = {name: int(n) for name, (ms, n) in b.stage_times(-1).items()}
+    assert got == {"fft_slices": 2, "tc_gemm_fwd": 1, "tc_gemm_inv": 1, "coeff_convert": 2}, got
+    assert b.graph_kernels(0) == -1
