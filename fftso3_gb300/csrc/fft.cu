@@ -457,10 +457,16 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(const TIN* __restrict__ 
 //   rows padded by one element per 8 (phys(i) = i + i / 8): a stage's strided reads and scattered writes;
 //   row stride N + N / 8 + 1 elements (one extra 16-byte slot): the TK rows of the load / store phases;
 //   twiddles per stage as [r - 1][kt] (kt = butterfly index mod Ns): consecutive lanes, consecutive entries.
-template <int N>
+// RESID (1 complex, 2 real samples): the transform along q of the refinement's grid synthesis, whose store phase
+// forms the residual instead of writing the lines back: r[fn][k][j1][j2] = (f - g.h) - g.l (FP32; real samples:
+// against the real part) at the same places of the samples f, o = (fn, j1) and the line index j = j2, so each of
+// the TK lines of a CTA is one contiguous row of the grid.  fin may be r (each element is read, then written, by
+// one thread).
+template <int N, int RESID>
 __global__ void __launch_bounds__(256, 3) fft_df32_k_kernel(dfc32* __restrict__ buf, long long S, long long oinner,
                                                              long long oouter, long long oistride,
-                                                             const double2* __restrict__ twg)
+                                                             const double2* __restrict__ twg, const void* fin,
+                                                             float* r)
 {
     constexpr int TK = 2048 / N;         // lines per CTA
     constexpr int TPL = N / 8;           // threads per line
@@ -532,10 +538,28 @@ __global__ void __launch_bounds__(256, 3) fft_df32_k_kernel(dfc32* __restrict__ 
         }
         __syncthreads();
     }
+    if constexpr (RESID == 0) {
 #pragma unroll
-    for (int u = 0; u < N * TK / 256; ++u) {
-        const int e = tid + 256 * u, kk2 = e % TK, j = e / TK;
-        buf[obase + (long long)j * S + kk2] = sm[kk2 * ROW + phys(j)];
+        for (int u = 0; u < N * TK / 256; ++u) {
+            const int e = tid + 256 * u, kk2 = e % TK, j = e / TK;
+            buf[obase + (long long)j * S + kk2] = sm[kk2 * ROW + phys(j)];
+        }
+    } else {
+        constexpr long long NN = (long long)N * N;
+        const long long rbase = (o / oinner) * NN * N + (o % oinner) * N + (long long)blockIdx.x * TK * NN;
+#pragma unroll
+        for (int u = 0; u < N * TK / 256; ++u) {
+            const int e = tid + 256 * u, kk2 = e / N, j = e % N;
+            const dfc32 v = sm[kk2 * ROW + phys(j)];
+            const long long i = rbase + kk2 * NN + j;
+            if constexpr (RESID == 2) {
+                r[i] = (reinterpret_cast<const float*>(fin)[i] - v.x.h) - v.x.l;
+            } else {
+                const float2 f = reinterpret_cast<const float2*>(fin)[i];
+                r[2 * i] = (f.x - v.x.h) - v.x.l;
+                r[2 * i + 1] = (f.y - v.y.h) - v.y.l;
+            }
+        }
     }
 }
 
@@ -795,11 +819,38 @@ cudaError_t launch_fft_df32_k(void* buf, int N, long long S, long long nouter, l
     dfc32* b = (dfc32*)buf;
     const double2* t = (const double2*)tw;
     switch (N) {
-        case 64: fft_df32_k_kernel<64><<<grid, 256, 0, st>>>(b, S, oinner, oouter, oistride, t); break;
-        case 128: fft_df32_k_kernel<128><<<grid, 256, 0, st>>>(b, S, oinner, oouter, oistride, t); break;
-        case 256: fft_df32_k_kernel<256><<<grid, 256, 0, st>>>(b, S, oinner, oouter, oistride, t); break;
-        default: fft_df32_k_kernel<512><<<grid, 256, 0, st>>>(b, S, oinner, oouter, oistride, t); break;
+        case 64: fft_df32_k_kernel<64, 0><<<grid, 256, 0, st>>>(b, S, oinner, oouter, oistride, t, nullptr, nullptr); break;
+        case 128: fft_df32_k_kernel<128, 0><<<grid, 256, 0, st>>>(b, S, oinner, oouter, oistride, t, nullptr, nullptr); break;
+        case 256: fft_df32_k_kernel<256, 0><<<grid, 256, 0, st>>>(b, S, oinner, oouter, oistride, t, nullptr, nullptr); break;
+        default: fft_df32_k_kernel<512, 0><<<grid, 256, 0, st>>>(b, S, oinner, oouter, oistride, t, nullptr, nullptr); break;
     }
+    return cudaGetLastError();
+}
+
+template <int RESID>
+static void df32_resid_launch(int N, dim3 grid, dfc32* b, long long NN, const double2* t, const void* fin, float* r,
+                              cudaStream_t st)
+{
+    const long long N3 = NN * N;
+    switch (N) {
+        case 64: fft_df32_k_kernel<64, RESID><<<grid, 256, 0, st>>>(b, N, N, N3, NN, t, fin, r); break;
+        case 128: fft_df32_k_kernel<128, RESID><<<grid, 256, 0, st>>>(b, N, N, N3, NN, t, fin, r); break;
+        case 256: fft_df32_k_kernel<256, RESID><<<grid, 256, 0, st>>>(b, N, N, N3, NN, t, fin, r); break;
+        default: fft_df32_k_kernel<512, RESID><<<grid, 256, 0, st>>>(b, N, N, N3, NN, t, fin, r); break;
+    }
+}
+
+cudaError_t launch_fft_df32_k_resid(const void* buf, int N, long long nb, const void* fin, bool real, float* r,
+                                    const void* tw, cudaStream_t st)
+{
+    if (!fft_df32_k_supported(N) || nb < 1 || nb * N > 65535) return cudaErrorInvalidValue;
+    const dim3 grid((unsigned)(N / (2048 / N)), (unsigned)(nb * N));
+    dfc32* b = (dfc32*)buf;
+    const long long NN = (long long)N * N;
+    if (real)
+        df32_resid_launch<2>(N, grid, b, NN, (const double2*)tw, fin, r, st);
+    else
+        df32_resid_launch<1>(N, grid, b, NN, (const double2*)tw, fin, r, st);
     return cudaGetLastError();
 }
 

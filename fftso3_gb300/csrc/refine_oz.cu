@@ -27,7 +27,9 @@
 //    i + j >= 4 and the digits below 2^-31), as double-float pencils.
 // A double-float FFT over (p, q) then gives the grid g, and the residual
 // r = f - g is formed against the FP32 samples in the same arithmetic (f is
-// exact there) and rounded to FP32 only as the small difference.
+// exact there) and rounded to FP32 only as the small difference -- for
+// N = 64..512 in the store phase of the FFT's second pass, whose lines are
+// rows of the grid, so g is never written out.
 //
 // Kernel layout (one CTA per SM, persistent over (group, 128 k, 8 functions) items):
 //   warp 0     TMA of the four table digit planes (MN-major operand, 128-byte swizzle);
@@ -803,12 +805,14 @@ int oz_inverse_resid(OZState* o, const void* F, bool f64, int nb, const void* fg
         OZK(cudaGetLastError());
     }
     T->end(st);
-    // double-float FFT over q (lines (fn, p, k)), then over p (lines (fn, q, k)), in place
+    // double-float FFT over p (lines (fn, q, k)), then over q (lines (fn, p, k)) with the residual against the
+    // FP32 samples formed in the second pass's store phase (its lines are rows of the grid [fn][k][j1][j2])
     T->begin(ST_REF_FFT, st);
     if (fft_df32_k_supported(N)) {
-        // lines (fn, p, k) along q (stride N), then (fn, q, k) along p (stride N^2); k contiguous in both
-        OZK(launch_fft_df32_k(o->pen, N, N, (long long)nb * N, N, NN * N, NN, o->d_tw, st));
         OZK(launch_fft_df32_k(o->pen, N, NN, (long long)nb * N, N, NN * N, N, o->d_tw, st));
+        OZK(launch_fft_df32_k_resid(o->pen, N, nb, fgrid, real, resid, o->d_tw, st));
+        T->end(st);
+        return FFTSO3_SUCCESS;
     } else {
         FFTLaunch Lq;
         Lq.in = o->pen;
