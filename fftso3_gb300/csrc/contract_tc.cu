@@ -1894,7 +1894,7 @@ struct TCFused {
     // coefficient conversions
     BucketSeg* d_bseg = nullptr;
     int nbseg = 0;
-    long long nblk = 0, ncoef = 0;
+    long long nblk = 0, ncblk = 0;
     size_t slice_smem = 0;
     bool real = false;
 };
@@ -2053,7 +2053,7 @@ int tc_fused_phases(TCFused* f, const std::vector<long long>& g0, const std::vec
     for (size_t i = 0; i < n; ++i) ord[i] = (int)i;
     std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return f->parts[a]->N > f->parts[b]->N; });
     std::vector<BucketSeg> segs;
-    long long blk = 0, coef = 0;
+    long long blk = 0, cblk = 0;
     for (int i : ord) {
         TCState* p = f->parts[i];
         const int N = p->N;
@@ -2064,20 +2064,20 @@ int tc_fused_phases(TCFused* f, const std::vector<long long>& g0, const std::vec
         s.batch = p->batch;
         s.G = slice_lines_per_group(N);
         int spc = 1;
-        while (slice_fft_smem_bytes(N, spc + 1, real) <= smem && (long long)(spc + 1) * N * N <= (long long)Nmax * Nmax)
+        while (spc < 256 && slice_fft_smem_bytes(N, spc + 1, real) <= smem &&
+               (long long)(spc + 1) * N * N <= (long long)Nmax * Nmax)
             ++spc;
         s.spc = spc;
         s.fac = p->fac;
         s.tw = reinterpret_cast<const double2*>(p->d_tw);
         s.pencil = p->d_pencil;
         s.fg = p->d_fg;
-        s.goff2 = p->d_goff2;
         s.g0 = g0[i];
         s.c0 = c0[i];
         s.blk0 = blk;
-        s.coef0 = coef;
+        s.cblk0 = cblk;
         blk += ((long long)p->batch * N + spc - 1) / spc;
-        coef += (long long)p->batch * so3_off(p->B);
+        cblk += ((long long)p->batch * so3_off(p->B) + CONVERT_THREADS - 1) / CONVERT_THREADS;
         segs.push_back(s);
     }
     cudaError_t e;
@@ -2091,7 +2091,7 @@ int tc_fused_phases(TCFused* f, const std::vector<long long>& g0, const std::vec
     }
     f->nbseg = (int)segs.size();
     f->nblk = blk;
-    f->ncoef = coef;
+    f->ncblk = cblk;
     f->slice_smem = smem;
     f->real = real;
     return FFTSO3_SUCCESS;
@@ -2109,7 +2109,7 @@ int tc_fused_forward(TCFused* f, const void* grid, void* coeffs, cudaStream_t st
     int rc = tc_fused_gemm(f, true, st, T, err);
     if (rc) return rc;
     T->begin(ST_CONVERT, st);
-    TCK(launch_fused_group_to_packed(f->d_bseg, f->nbseg, f->ncoef, f->real, coeffs, st));
+    TCK(launch_fused_group_to_packed(f->d_bseg, f->nbseg, f->ncblk, f->real, coeffs, st));
     T->end(st);
     return FFTSO3_SUCCESS;
 }
@@ -2121,7 +2121,7 @@ int tc_fused_inverse(TCFused* f, const void* coeffs, void* grid, cudaStream_t st
         return FFTSO3_ERR_CUDA;
     }
     T->begin(ST_CONVERT, st);
-    TCK(launch_fused_packed_to_group(f->d_bseg, f->nbseg, f->ncoef, f->real, coeffs, st));
+    TCK(launch_fused_packed_to_group(f->d_bseg, f->nbseg, f->ncblk, f->real, coeffs, st));
     T->end(st);
     int rc = tc_fused_gemm(f, false, st, T, err);
     if (rc) return rc;

@@ -605,15 +605,24 @@ __device__ float2* run_line_stages(float2* src, float2* dst, const float2* w, co
 
 static int slice_prime_entries(const FFTFactors& f) { return f.r[0] > 8 ? prime_mat_entries(f.r[0]) : 0; }
 
+// Per-line (or per-slice) tables of a CTA: two 64-bit global offsets and one shared-memory offset per entry.
+__host__ __device__ inline int slice_table_entries(int N, int spc)
+{
+    const int G = slice_lines_per_group(N);
+    return G > spc ? G : spc;
+}
+
 size_t slice_fft_smem_bytes(int N, int spc, bool real)
 {
     FFTFactors f;
     make_fft_factors_prime_first(N, f);
     const size_t sst = (size_t)N * slice_row_stride(N, real) + 1;
     const size_t G = (size_t)slice_lines_per_group(N);
-    return sizeof(float2) * (spc * sst + 2 * G * (N + 1) + N + slice_prime_entries(f));
+    const size_t tb = (size_t)slice_table_entries(N, spc);
+    return sizeof(float2) * (spc * sst + 2 * G * (N + 1) + N + slice_prime_entries(f)) + tb * (8 + 8 + 4);
 }
 
+// Every element walk below advances its indices by constant steps (one division per walk, none per element).
 template <bool FWD, bool REAL>
 __global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const BucketSeg* __restrict__ segs, int nseg,
                                                                     const void* __restrict__ in,
@@ -639,57 +648,94 @@ __global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const Bucke
     const long long NN = (long long)N * N, NNN = NN * N;
     const long long s0 = (blk - S.blk0) * spc;
     const int ns = (int)min((long long)spc, (long long)S.batch * N - s0);
-    const int T = blockDim.x;
+    constexpr int T = SLICE_THREADS;
+    const int tid = threadIdx.x;
+    const int R0 = S.fac.r[0];
+    const int nmat = R0 > 8 ? prime_mat_entries(R0) : 0;
     float2* X = reinterpret_cast<float2*>(smem_raw);
     float2* A = X + (size_t)spc * SSt;
     float2* Bf = A + G * LS;
     float2* w = Bf + G * LS;
     float2* mat = w + N;
+    const int TB = slice_table_entries(N, spc);
+    long long* lg = reinterpret_cast<long long*>(mat + nmat);  // per line: global offset
+    long long* lm = lg + TB;                                    // per line: mirrored pencil offset (real), or -1
+    int* lx = reinterpret_cast<int*>(lm + TB);                  // per line: offset in the slices
+    const float2* __restrict__ Pin = S.pencil;
+    float2* __restrict__ Pout = S.pencil;
     const double2* tw = S.tw;
-    for (int i = threadIdx.x; i < N; i += T) w[i] = make_float2((float)tw[i].x, (float)tw[i].y);
-    if (S.fac.r[0] > 8) {
-        const int R = S.fac.r[0], P = (R - 1) / 2, P4 = (P + 3) / 4 * 4, Nr = N / R;
-        for (int i = threadIdx.x; i < P * P4; i += T) {
+    for (int i = tid; i < N; i += T) w[i] = make_float2((float)tw[i].x, (float)tw[i].y);
+    if (R0 > 8) {
+        const int P = (R0 - 1) / 2, P4 = (P + 3) / 4 * 4, Nr = N / R0;
+        for (int i = tid; i < P * P4; i += T) {
             const int t = i / P4 + 1, q = i - (t - 1) * P4 + 1;
             float c = 0.f, sn = 0.f;
             if (q <= P) {
-                const double2 v = tw[((t * q) % R) * Nr];  // e^{-2 pi i t q / R}
+                const double2 v = tw[((t * q) % R0) * Nr];  // e^{-2 pi i t q / R}
                 c = (float)v.x;
                 sn = (float)(-v.y);
             }
             mat[i] = make_float2(c, sn);
         }
     }
-    const int NR = REAL ? B : N;  // row lines per slice
+    const int NR = REAL ? B : N;           // row lines per slice
+    const int rl = T / N, rj = T - rl * N;  // walk (l, j) over rows of N
+    const int cl = T / NC, cq = T - cl * NC;  // walk (l, q) over rows of NC
+    // row lines [l0, l0 + nl): global row offset and slice row offset
+    auto row_tables = [&](int l0, int nl) {
+        for (int i = tid; i < nl; i += T) {
+            const int line = l0 + i, s = line / NR, r = line - s * NR, rr = REAL ? 2 * r : r;
+            lg[i] = S.g0 + (s0 + s) * NN + (long long)rr * N;
+            lx[i] = s * SSt + rr * RS;
+        }
+    };
+    // column lines [l0, l0 + nl) (slice fastest): slice column offset, pencil offsets of (q) and (-q)
+    auto col_tables = [&](int l0, int nl) {
+        for (int i = tid; i < nl; i += T) {
+            const int line = l0 + i, q = line / ns, s = line - q * ns;
+            lx[i] = s * SSt + q;
+            const long long sl = s0 + s, f = sl / N, pb = f * NNN + (sl - f * N);
+            lg[i] = pb + (long long)q * N;
+            lm[i] = (REAL && q > 0 && q < B) ? pb + (long long)(N - q) * N : -1;
+        }
+    };
     if (FWD) {
         // rows: grid -> line buffer -> slice rows (real: the two half-spectra of each row pair)
         const int nlr = ns * NR;
-        __syncthreads();
         for (int l0 = 0; l0 < nlr; l0 += G) {
             const int nl = min(G, nlr - l0), nle = (nl + 1) & ~1;
-            for (int e = threadIdx.x; e < nl * N; e += T) {
-                const int l = e / N, j = e - l * N, line = l0 + l;
-                const int s = line / NR, r = line - s * NR;
-                const long long base = S.g0 + (s0 + s) * NN;
-                if (REAL) {
-                    const float* g = reinterpret_cast<const float*>(in) + base + (long long)(2 * r) * N + j;
-                    A[l * LS + j] = make_float2(g[0], g[N]);
-                } else {
-                    A[l * LS + j] = reinterpret_cast<const float2*>(in)[base + (long long)r * N + j];
+            row_tables(l0, nl);
+            __syncthreads();
+            {
+                int l = tid / N, j = tid - l * N;
+                for (int e = tid; e < nl * N; e += T) {
+                    if (REAL) {
+                        const float* g = reinterpret_cast<const float*>(in) + lg[l] + j;
+                        A[l * LS + j] = make_float2(g[0], g[N]);
+                    } else {
+                        A[l * LS + j] = reinterpret_cast<const float2*>(in)[lg[l] + j];
+                    }
+                    j += rj;
+                    l += rl;
+                    if (j >= N) { j -= N; ++l; }
                 }
             }
             __syncthreads();
             const float2* res = run_line_stages(A, Bf, w, mat, S.fac, N, nle, LS);
-            for (int e = threadIdx.x; e < nl * NC; e += T) {
-                const int l = e / NC, q = e - l * NC, line = l0 + l;
-                const int s = line / NR, r = line - s * NR;
-                float2* x = X + s * SSt;
-                if (REAL) {
-                    const float2 z = res[l * LS + q], zm = res[l * LS + (q == 0 ? 0 : N - q)];
-                    x[(2 * r) * RS + q] = make_float2(0.5f * (z.x + zm.x), 0.5f * (z.y - zm.y));
-                    x[(2 * r + 1) * RS + q] = make_float2(0.5f * (z.y + zm.y), -0.5f * (z.x - zm.x));
-                } else {
-                    x[r * RS + q] = res[l * LS + q];
+            {
+                int l = tid / NC, q = tid - l * NC;
+                for (int e = tid; e < nl * NC; e += T) {
+                    float2* x = X + lx[l];
+                    if (REAL) {
+                        const float2 z = res[l * LS + q], zm = res[l * LS + (q == 0 ? 0 : N - q)];
+                        x[q] = make_float2(0.5f * (z.x + zm.x), 0.5f * (z.y - zm.y));
+                        x[RS + q] = make_float2(0.5f * (z.y + zm.y), -0.5f * (z.x - zm.x));
+                    } else {
+                        x[q] = res[l * LS + q];
+                    }
+                    q += cq;
+                    l += cl;
+                    if (q >= NC) { q -= NC; ++l; }
                 }
             }
             __syncthreads();
@@ -698,57 +744,89 @@ __global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const Bucke
         const int nlc = ns * NC;
         for (int l0 = 0; l0 < nlc; l0 += G) {
             const int nl = min(G, nlc - l0), nle = (nl + 1) & ~1;
-            for (int e = threadIdx.x; e < nl * N; e += T) {
-                const int j = e / nl, l = e - j * nl, line = l0 + l;
-                const int q = line / ns, s = line - q * ns;
-                A[l * LS + j] = X[s * SSt + j * RS + q];
+            col_tables(l0, nl);
+            __syncthreads();
+            const int gj = T / nl, gl = T - gj * nl;  // walk (j, l), l fastest
+            {
+                int j = tid / nl, l = tid - j * nl;
+                for (int e = tid; e < nl * N; e += T) {
+                    A[l * LS + j] = X[lx[l] + j * RS];
+                    l += gl;
+                    j += gj;
+                    if (l >= nl) { l -= nl; ++j; }
+                }
             }
             __syncthreads();
             const float2* res = run_line_stages(A, Bf, w, mat, S.fac, N, nle, LS);
-            for (int e = threadIdx.x; e < nl * N; e += T) {
-                const int p = e / nl, l = e - p * nl, line = l0 + l;
-                const int q = line / ns, s = line - q * ns;
-                const long long sl = s0 + s, f = sl / N;
-                float2* P = S.pencil + f * NNN + (sl - f * N);
-                const float2 v = res[l * LS + p];
-                P[((long long)p * N + q) * N] = v;
-                if (REAL && q > 0 && q < B)
-                    P[((long long)(p == 0 ? 0 : N - p) * N + (N - q)) * N] = make_float2(v.x, -v.y);
+            {
+                int p = tid / nl, l = tid - p * nl;
+                for (int e = tid; e < nl * N; e += T) {
+                    const float2 v = res[l * LS + p];
+                    Pout[lg[l] + p * NN] = v;
+                    if (REAL && lm[l] >= 0) Pout[lm[l] + (p == 0 ? 0 : N - p) * NN] = make_float2(v.x, -v.y);
+                    l += gl;
+                    p += gj;
+                    if (l >= nl) { l -= nl; ++p; }
+                }
             }
             __syncthreads();
         }
     } else {
-        // pencils -> slice (Nyquist bins zero; real: the Hermitian part)
-        for (int e = threadIdx.x; e < ns * N * NC; e += T) {
-            const int s = e % ns, pq = e / ns, q = pq % NC, p = pq / NC;
-            const long long sl = s0 + s, f = sl / N;
-            const float2* P = S.pencil + f * NNN + (sl - f * N);
-            float2 v = make_float2(0.f, 0.f);
-            if (p != B && q != B) {
-                v = P[((long long)p * N + q) * N];
-                if (REAL) {
-                    const float2 u = P[((long long)(p == 0 ? 0 : N - p) * N + (q == 0 ? 0 : N - q)) * N];
-                    v = make_float2(0.5f * (v.x + u.x), 0.5f * (v.y - u.y));
+        // pencils -> slice (Nyquist bins zero; real: the Hermitian part), walk e = (p NC + q) ns + s
+        for (int i = tid; i < ns; i += T) {
+            const long long sl = s0 + i, f = sl / N;
+            lg[i] = f * NNN + (sl - f * N);
+        }
+        __syncthreads();
+        {
+            const int sinc = T % ns, pqinc = T / ns, qinc = pqinc % NC, pinc = pqinc / NC;
+            int s = tid % ns, q = (tid / ns) % NC, p = (tid / ns) / NC;
+            for (int e = tid; e < ns * N * NC; e += T) {
+                float2 v = make_float2(0.f, 0.f);
+                if (p != B && q != B) {
+                    v = Pin[lg[s] + ((long long)p * N + q) * N];
+                    if (REAL) {
+                        const float2 u = Pin[lg[s] + ((long long)(p == 0 ? 0 : N - p) * N + (q == 0 ? 0 : N - q)) * N];
+                        v = make_float2(0.5f * (v.x + u.x), 0.5f * (v.y - u.y));
+                    }
                 }
+                X[s * SSt + p * RS + q] = v;
+                s += sinc;
+                int c = 0;
+                if (s >= ns) { s -= ns; c = 1; }
+                q += qinc + c;
+                c = 0;
+                if (q >= NC) { q -= NC; c = 1; }
+                p += pinc + c;
             }
-            X[s * SSt + p * RS + q] = v;
         }
         __syncthreads();
         // columns (along p), in place in the slice
         const int nlc = ns * NC;
         for (int l0 = 0; l0 < nlc; l0 += G) {
             const int nl = min(G, nlc - l0), nle = (nl + 1) & ~1;
-            for (int e = threadIdx.x; e < nl * N; e += T) {
-                const int j = e / nl, l = e - j * nl, line = l0 + l;
-                const int q = line / ns, s = line - q * ns;
-                A[l * LS + j] = X[s * SSt + j * RS + q];
+            col_tables(l0, nl);
+            __syncthreads();
+            const int gj = T / nl, gl = T - gj * nl;
+            {
+                int j = tid / nl, l = tid - j * nl;
+                for (int e = tid; e < nl * N; e += T) {
+                    A[l * LS + j] = X[lx[l] + j * RS];
+                    l += gl;
+                    j += gj;
+                    if (l >= nl) { l -= nl; ++j; }
+                }
             }
             __syncthreads();
             const float2* res = run_line_stages(A, Bf, w, mat, S.fac, N, nle, LS);
-            for (int e = threadIdx.x; e < nl * N; e += T) {
-                const int j = e / nl, l = e - j * nl, line = l0 + l;
-                const int q = line / ns, s = line - q * ns;
-                X[s * SSt + j * RS + q] = res[l * LS + j];
+            {
+                int j = tid / nl, l = tid - j * nl;
+                for (int e = tid; e < nl * N; e += T) {
+                    X[lx[l] + j * RS] = res[l * LS + j];
+                    l += gl;
+                    j += gj;
+                    if (l >= nl) { l -= nl; ++j; }
+                }
             }
             __syncthreads();
         }
@@ -756,39 +834,48 @@ __global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const Bucke
         const int nlr = ns * NR;
         for (int l0 = 0; l0 < nlr; l0 += G) {
             const int nl = min(G, nlr - l0), nle = (nl + 1) & ~1;
-            for (int e = threadIdx.x; e < nl * N; e += T) {
-                const int l = e / N, j = e - l * N, line = l0 + l;
-                const int s = line / NR, r = line - s * NR;
-                const float2* x = X + s * SSt;
-                if (REAL) {
-                    float2 ya, yb;
-                    if (j <= B) {
-                        ya = x[(2 * r) * RS + j];
-                        yb = x[(2 * r + 1) * RS + j];
+            row_tables(l0, nl);
+            __syncthreads();
+            {
+                int l = tid / N, j = tid - l * N;
+                for (int e = tid; e < nl * N; e += T) {
+                    const float2* x = X + lx[l];
+                    if (REAL) {
+                        float2 ya, yb;
+                        if (j <= B) {
+                            ya = x[j];
+                            yb = x[RS + j];
+                        } else {
+                            ya = x[N - j];
+                            yb = x[RS + N - j];
+                            ya.y = -ya.y;
+                            yb.y = -yb.y;
+                        }
+                        A[l * LS + j] = make_float2(ya.x - yb.y, ya.y + yb.x);
                     } else {
-                        ya = x[(2 * r) * RS + N - j];
-                        yb = x[(2 * r + 1) * RS + N - j];
-                        ya.y = -ya.y;
-                        yb.y = -yb.y;
+                        A[l * LS + j] = x[j];
                     }
-                    A[l * LS + j] = make_float2(ya.x - yb.y, ya.y + yb.x);
-                } else {
-                    A[l * LS + j] = x[r * RS + j];
+                    j += rj;
+                    l += rl;
+                    if (j >= N) { j -= N; ++l; }
                 }
             }
             __syncthreads();
             const float2* res = run_line_stages(A, Bf, w, mat, S.fac, N, nle, LS);
-            for (int e = threadIdx.x; e < nl * N; e += T) {
-                const int l = e / N, j = e - l * N, line = l0 + l;
-                const int s = line / NR, r = line - s * NR;
-                const long long base = S.g0 + (s0 + s) * NN;
-                const float2 v = res[l * LS + j];
-                if (REAL) {
-                    float* g = reinterpret_cast<float*>(out) + base + (long long)(2 * r) * N + j;
-                    g[0] = v.x;
-                    g[N] = v.y;
-                } else {
-                    reinterpret_cast<float2*>(out)[base + (long long)r * N + j] = v;
+            {
+                int l = tid / N, j = tid - l * N;
+                for (int e = tid; e < nl * N; e += T) {
+                    const float2 v = res[l * LS + j];
+                    if (REAL) {
+                        float* g = reinterpret_cast<float*>(out) + lg[l] + j;
+                        g[0] = v.x;
+                        g[N] = v.y;
+                    } else {
+                        reinterpret_cast<float2*>(out)[lg[l] + j] = v;
+                    }
+                    j += rj;
+                    l += rl;
+                    if (j >= N) { j -= N; ++l; }
                 }
             }
             __syncthreads();

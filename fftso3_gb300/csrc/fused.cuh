@@ -11,7 +11,7 @@ namespace fftso3 {
 
 // One bucket: its sizes, FFT factors and twiddles, the bucket plan's pencils and group-major coefficients, the
 // element offsets of its slab in the caller's grid and coefficient buffers, and its first work index in each
-// fused launch.  A launch's segment table is ordered by its work index (blk0 and coef0 ascending).
+// fused launch.  A launch's segment table is ordered by its work index (blk0 and cblk0 ascending).
 struct BucketSeg {
     int L, B, N, batch;
     int spc;                     // beta slices per CTA of the slice FFT
@@ -20,10 +20,9 @@ struct BucketSeg {
     const double2* tw;           // W[i] = e^{-2 pi i i / N}
     float2* pencil;              // [fn][p][q][k]
     float2* fg;                  // group-major coefficients [fn][so3_off(B)]
-    const long long* goff2;      // group-major offsets, B^2 + 1 entries
     long long g0, c0;            // slab offsets (elements) in the caller's grids / coefficients
     long long blk0;              // first CTA of the bucket in the slice FFT
-    long long coef0;             // first thread of the bucket in the coefficient conversions
+    long long cblk0;             // first CTA of the bucket in the coefficient conversions
 };
 
 constexpr int SLICE_THREADS = 256;
@@ -42,12 +41,14 @@ size_t slice_fft_smem_bytes(int N, int spc, bool real);
 cudaError_t launch_slice_fft(const BucketSeg* segs, int nseg, long long nblk, size_t smem, bool fwd, bool real,
                              const void* in, void* out, cudaStream_t st);
 
-// Coefficient conversions of every bucket in one launch (one thread per coefficient, ncoef in total):
+// Coefficient conversions of every bucket in one launch (CONVERT_THREADS coefficients of one bucket per CTA,
+// nblk CTAs in total):
 //   forward: group-major GEMM output -> packed coefficients (complex64, or the real basis in float32);
 //   inverse: packed coefficients (complex64 / real float32) -> group-major (2l + 1) sign F.
-cudaError_t launch_fused_group_to_packed(const BucketSeg* segs, int nseg, long long ncoef, bool real, void* out,
+constexpr int CONVERT_THREADS = 256;
+cudaError_t launch_fused_group_to_packed(const BucketSeg* segs, int nseg, long long nblk, bool real, void* out,
                                          cudaStream_t st);
-cudaError_t launch_fused_packed_to_group(const BucketSeg* segs, int nseg, long long ncoef, bool real, const void* in,
+cudaError_t launch_fused_packed_to_group(const BucketSeg* segs, int nseg, long long nblk, bool real, const void* in,
                                          cudaStream_t st);
 
 }  // namespace fftso3

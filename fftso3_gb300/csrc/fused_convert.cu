@@ -8,7 +8,8 @@
 //            entries (l, +-m, +-n));
 //   inverse: group-major (2l + 1) sign F(l, m, n) of the pair at that place (real kinds: F = T^H F_r T from
 //            the four real entries (l, +-m, +-n)).
-// The gathers are scattered but stay inside one function's coefficients (a few MB at l_max = 64), which the
+// The group-major place of (l, m, n) and its inverse are closed-form (no table lookups), each CTA serves one
+// bucket, and the gathers stay inside one function's coefficients (a few MB at l_max = 64), which the
 // neighbouring threads of the launch read at the same time, so they are served by L2.
 #include "common.cuh"
 #include "fused.cuh"
@@ -18,15 +19,33 @@ namespace fftso3 {
 
 namespace {
 
-__device__ __forceinline__ int seg_of(const BucketSeg* __restrict__ segs, int nseg, long long t)
+// The group-major layout in closed form (the order the tensor-core plans build their offsets in, group by group
+// g = m0^2 + m0 + n0, pairs of group_pairs(), rows l = m0..L): the groups of one m0 >= 1 hold 8 m0 runs of
+// B - m0 rows -- n0 = -m0 (2 pairs), -m0 < n0 < m0 (4 pairs each), n0 = m0 (2 pairs) -- after the single run
+// of m0 = 0.
+__device__ __forceinline__ long long block_start(int m0, int B)
 {
-    int lo = 0, hi = nseg - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (segs[mid].coef0 <= t) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
+    if (m0 == 0) return 0;
+    const long long a = m0 - 1, b = m0;
+    return B + 8 * ((long long)B * (a * b / 2) - a * b * (2 * b - 1) / 6);
+}
+
+__device__ __forceinline__ int run_index(int m0, int n0, int pp)
+{
+    if (m0 == 0) return 0;
+    if (n0 == -m0) return pp;
+    if (n0 == m0) return 8 * m0 - 2 + pp;
+    return 2 + 4 * (n0 + m0 - 1) + pp;
+}
+
+// group-major offset of F(l, m, n) in a bucket of bandwidth B
+__device__ __forceinline__ long long gm_offset(int l, int m, int n, int B)
+{
+    int g, pp;
+    pair_of(m, n, g, pp);
+    const int am = m < 0 ? -m : m, an = n < 0 ? -n : n, m0 = am > an ? am : an;
+    const int n0 = g - m0 * m0 - m0;
+    return block_start(m0, B) + (long long)run_index(m0, n0, pp) * (B - m0) + (l - m0);
 }
 
 // largest l with so3_off(l) <= r
@@ -38,65 +57,86 @@ __device__ __forceinline__ int degree_of(long long r)
     return l;
 }
 
-template <bool REAL>
-__global__ void __launch_bounds__(256) fused_group_to_packed_kernel(const BucketSeg* __restrict__ segs, int nseg,
-                                                                    long long ncoef, void* __restrict__ out)
+// the CTA's bucket (thread 0 searches the table once)
+__device__ __forceinline__ const BucketSeg& cta_bucket(const BucketSeg* __restrict__ segs, int nseg, int* sb)
 {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ncoef) return;
-    const BucketSeg& S = segs[seg_of(segs, nseg, t)];
+    if (threadIdx.x == 0) {
+        const long long blk = blockIdx.x;
+        int lo = 0, hi = nseg - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (segs[mid].cblk0 <= blk) lo = mid;
+            else hi = mid - 1;
+        }
+        *sb = lo;
+    }
+    __syncthreads();
+    return segs[*sb];
+}
+
+template <bool REAL>
+__global__ void __launch_bounds__(CONVERT_THREADS) fused_group_to_packed_kernel(const BucketSeg* __restrict__ segs,
+                                                                                int nseg, void* __restrict__ out)
+{
+    __shared__ int sb;
+    const BucketSeg& S = cta_bucket(segs, nseg, &sb);
     const int B = S.B;
-    const long long C = so3_off(B), u = t - S.coef0, f = u / C, r = u - f * C;
+    const long long C = so3_off(B);
+    const long long u = (blockIdx.x - S.cblk0) * (long long)CONVERT_THREADS + threadIdx.x;
+    if (u >= (long long)S.batch * C) return;
+    const long long f = u / C, r = u - f * C;
     const int l = degree_of(r);
     const int W = 2 * l + 1, wi = (int)(r - so3_off(l));
     const int m = wi % W - l, n = wi / W - l;
     const float2* __restrict__ fg = S.fg + f * C;
-    const long long* __restrict__ goff2 = S.goff2;
-    auto val = [&](int mm, int nn) -> float2 {
-        int g, pp;
-        pair_of(mm, nn, g, pp);
-        const int am = mm < 0 ? -mm : mm, an = nn < 0 ? -nn : nn, m0 = am > an ? am : an;
-        return fg[goff2[g] + (long long)pp * (B - m0) + (l - m0)];
-    };
     if (!REAL) {
-        reinterpret_cast<float2*>(out)[S.c0 + u] = val(m, n);
+        reinterpret_cast<float2*>(out)[S.c0 + u] = fg[gm_offset(l, m, n, B)];
         return;
     }
     const int am[2] = {-m, m}, bn[2] = {-n, n};
     const int na = (m == 0) ? 1 : 2, nb = (n == 0) ? 1 : 2;
+    float2 v[2][2];
+    for (int ia = 0; ia < na; ++ia)
+        for (int ib = 0; ib < nb; ++ib) v[ia][ib] = fg[gm_offset(l, am[ia], bn[ib], B)];
     float acc = 0.f;
     for (int ia = 0; ia < na; ++ia)
         for (int ib = 0; ib < nb; ++ib) {
             const c2t<float> t1 = tmat_t<float>(m, am[ia]), t2 = conj_t(tmat_t<float>(n, bn[ib]));
-            const float2 v = val(am[ia], bn[ib]);
-            const c2t<float> c = cmul_t(cmul_t(t1, c2t<float>{v.x, v.y}), t2);
+            const c2t<float> c = cmul_t(cmul_t(t1, c2t<float>{v[ia][ib].x, v[ia][ib].y}), t2);
             acc += c.x;
         }
     reinterpret_cast<float*>(out)[S.c0 + u] = acc;
 }
 
 template <bool REAL>
-__global__ void __launch_bounds__(256) fused_packed_to_group_kernel(const BucketSeg* __restrict__ segs, int nseg,
-                                                                    long long ncoef, const void* __restrict__ in)
+__global__ void __launch_bounds__(CONVERT_THREADS) fused_packed_to_group_kernel(const BucketSeg* __restrict__ segs,
+                                                                                int nseg, const void* __restrict__ in)
 {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ncoef) return;
-    const BucketSeg& S = segs[seg_of(segs, nseg, t)];
+    __shared__ int sb;
+    const BucketSeg& S = cta_bucket(segs, nseg, &sb);
     const int B = S.B;
-    const long long C = so3_off(B), u = t - S.coef0, f = u / C, e = u - f * C;
-    const long long* __restrict__ go = S.goff2;
-    int lo = 0, hi = B * B - 1;
+    const long long C = so3_off(B);
+    const long long u = (blockIdx.x - S.cblk0) * (long long)CONVERT_THREADS + threadIdx.x;
+    if (u >= (long long)S.batch * C) return;
+    const long long f = u / C, e = u - f * C;
+    int lo = 0, hi = B - 1;  // m0: the block holding e
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        if (go[mid] <= e) lo = mid;
+        if (block_start(mid, B) <= e) lo = mid;
         else hi = mid - 1;
     }
-    int m0, n0;
-    group_mn(lo, m0, n0);
-    const int nl = B - m0;
-    const int off = (int)(e - go[lo]), pp = off / nl, l = m0 + off - pp * nl;
-    const GroupPairs P = group_pairs(m0, n0);
-    const int m = P.m[pp], n = P.n[pp];
+    const int m0 = lo, nl = B - m0;
+    const int rel = (int)(e - block_start(m0, B)), ri = rel / nl, l = m0 + rel - ri * nl;
+    int n0, pp;
+    if (m0 == 0) { n0 = 0; pp = 0; }
+    else if (ri < 2) { n0 = -m0; pp = ri; }
+    else if (ri >= 8 * m0 - 2) { n0 = m0; pp = ri - (8 * m0 - 2); }
+    else { n0 = -m0 + 1 + (ri - 2) / 4; pp = (ri - 2) & 3; }
+    // pair pp of group_pairs(m0, n0), without its table (which a dynamic index would put in local memory)
+    const int sgn = ((m0 + n0) & 1) ? -1 : 1;
+    const int m = pp == 0 ? m0 : pp == 1 ? -m0 : pp == 2 ? n0 : -n0;
+    const int n = pp == 0 ? n0 : pp == 1 ? -n0 : pp == 2 ? m0 : -m0;
+    const int psign = (pp == 1 || pp == 2) ? sgn : 1;
     float2 v;
     if (!REAL) {
         v = reinterpret_cast<const float2*>(in)[S.c0 + f * C + so3_idx(l, m, n)];
@@ -104,45 +144,45 @@ __global__ void __launch_bounds__(256) fused_packed_to_group_kernel(const Bucket
         const float* __restrict__ fr = reinterpret_cast<const float*>(in) + S.c0 + f * C;
         const int am[2] = {m, -m}, bn[2] = {n, -n};
         const int na = (m == 0) ? 1 : 2, nb = (n == 0) ? 1 : 2;
+        float x[2][2];
+        for (int ia = 0; ia < na; ++ia)
+            for (int ib = 0; ib < nb; ++ib) x[ia][ib] = fr[so3_idx(l, am[ia], bn[ib])];
         c2t<float> acc = {0.f, 0.f};
         for (int ia = 0; ia < na; ++ia)
             for (int ib = 0; ib < nb; ++ib) {
                 const c2t<float> c = cmul_t(conj_t(tmat_t<float>(am[ia], m)), tmat_t<float>(bn[ib], n));
-                const float x = fr[so3_idx(l, am[ia], bn[ib])];
-                acc.x += c.x * x;
-                acc.y += c.y * x;
+                acc.x += c.x * x[ia][ib];
+                acc.y += c.y * x[ia][ib];
             }
         v = make_float2(acc.x, acc.y);
     }
-    const float sc = (float)(2 * l + 1) * (float)P.sign[pp];
+    const float sc = (float)(2 * l + 1) * (float)psign;
     S.fg[f * C + e] = make_float2(sc * v.x, sc * v.y);
 }
 
-unsigned blocks_of(long long n) { return (unsigned)((n + 255) / 256); }
-
 }  // namespace
 
-cudaError_t launch_fused_group_to_packed(const BucketSeg* segs, int nseg, long long ncoef, bool real, void* out,
+cudaError_t launch_fused_group_to_packed(const BucketSeg* segs, int nseg, long long nblk, bool real, void* out,
                                          cudaStream_t st)
 {
-    if (ncoef <= 0) return cudaSuccess;
-    if ((ncoef + 255) / 256 > 0x7fffffffLL || nseg <= 0) return cudaErrorInvalidValue;
+    if (nblk <= 0) return cudaSuccess;
+    if (nblk > 0x7fffffffLL || nseg <= 0) return cudaErrorInvalidValue;
     if (real)
-        fused_group_to_packed_kernel<true><<<blocks_of(ncoef), 256, 0, st>>>(segs, nseg, ncoef, out);
+        fused_group_to_packed_kernel<true><<<(unsigned)nblk, CONVERT_THREADS, 0, st>>>(segs, nseg, out);
     else
-        fused_group_to_packed_kernel<false><<<blocks_of(ncoef), 256, 0, st>>>(segs, nseg, ncoef, out);
+        fused_group_to_packed_kernel<false><<<(unsigned)nblk, CONVERT_THREADS, 0, st>>>(segs, nseg, out);
     return cudaGetLastError();
 }
 
-cudaError_t launch_fused_packed_to_group(const BucketSeg* segs, int nseg, long long ncoef, bool real, const void* in,
+cudaError_t launch_fused_packed_to_group(const BucketSeg* segs, int nseg, long long nblk, bool real, const void* in,
                                          cudaStream_t st)
 {
-    if (ncoef <= 0) return cudaSuccess;
-    if ((ncoef + 255) / 256 > 0x7fffffffLL || nseg <= 0) return cudaErrorInvalidValue;
+    if (nblk <= 0) return cudaSuccess;
+    if (nblk > 0x7fffffffLL || nseg <= 0) return cudaErrorInvalidValue;
     if (real)
-        fused_packed_to_group_kernel<true><<<blocks_of(ncoef), 256, 0, st>>>(segs, nseg, ncoef, in);
+        fused_packed_to_group_kernel<true><<<(unsigned)nblk, CONVERT_THREADS, 0, st>>>(segs, nseg, in);
     else
-        fused_packed_to_group_kernel<false><<<blocks_of(ncoef), 256, 0, st>>>(segs, nseg, ncoef, in);
+        fused_packed_to_group_kernel<false><<<(unsigned)nblk, CONVERT_THREADS, 0, st>>>(segs, nseg, in);
     return cudaGetLastError();
 }
 
