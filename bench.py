@@ -5,10 +5,10 @@ Headline (the first JSON line): a batch of 32 complex SO(3) functions at
 l_max = 255 (512^3 Euler grid each, complex64 samples; synthetic seeded
 coefficients F ~ N(0,1)(l+1)^-1.5), stable Wigner-d recursion.  One step =
 inverse of the whole batch on the tensor cores (split-BF16) + refined forward
-of the whole batch (split-BF16 forward, then one residual step
-F += forward(f - inverse(F)) whose inverse is exact on the tensor cores), the
-configuration that meets rel-err <= 1e-6 per degree against FP64; value =
-functions / step time.  Reported beside it: the plain split-BF16 step, the
+of the whole batch (F0 = split-BF16 GEMM of the samples' double-float FFT,
+then one residual step F = F0 + GEMM(FFT(f) - N^2 H(F0)) formed in the pencil
+domain, H the exact tensor-core synthesis contraction), the configuration that
+meets rel-err <= 1e-6 per degree against FP64; value = functions / step time.  Reported beside it: the plain split-BF16 step, the
 plain FP64 GPU path, the FP32 CUDA-core form, the accuracy against FP64, the
 end-to-end rate through the host-buffer C-ABI calls, the roofline of the
 dominant stage (CUDA-event stage timing inside the library) and of the whole
@@ -933,7 +933,7 @@ def stage_roofline(name: str, tot_ms: float, cnt: int, L: int, b: int, chunk: in
     flops = None
     if name.startswith("tc_gemm"):
         flops, alg = 8.0 * B * C * b, "8 B C useful flops per function per launch (6 split-BF16 products issued)"
-    elif name == "refine_inverse_contract":
+    elif name == "refine_exact_contract":
         flops, alg = 8.0 * B * C * chunk, "8 B C useful flops per function of the chunk (10 digit products issued)"
     if flops is not None:
         ach = flops / per / 1e12
@@ -945,8 +945,10 @@ def stage_roofline(name: str, tot_ms: float, cnt: int, L: int, b: int, chunk: in
         byts, alg = 2 * grid8, "one complex64 read + write of every sample per launch (both FFT passes, L2 ring)"
     elif name in ("fft_rows", "fft_cols", "tc_pack_fwd", "tc_pack_inv"):
         byts, alg = 2 * grid8, "one complex64 read + write of every sample per pass"
-    elif name == "refine_inverse_fft":
-        byts, alg = 2 * 2 * 16.0 * chunk * N ** 3, "two double-float passes, 16 B read + written per sample each"
+    elif name == "refine_fft_df32":
+        byts, alg = (8.0 + 16 + 16 + 16) * chunk * N ** 3, ("double-float forward FFT of the samples: pass 1 reads "
+                                                          "8 B, writes 16 B; pass 2 reads 16 B, writes hi + lo "
+                                                          "8 + 8 B per sample")
     elif name == "basis_convert":
         byts, alg = 2 * 8.0 * C * b, "one complex64 read + write of the coefficients"
     else:
@@ -1079,12 +1081,12 @@ def so3_tc_line(args, L: int, b: int, full: bool = True) -> dict:
     value = b * 1000.0 / ms
     # functions per refinement chunk (the library sizes chunks to the free device memory): one timed record of
     # the refinement FFT per chunk and step
-    nchunks = max(1, round(stages.get("refine_inverse_fft", (0, args.steps))[1] / args.steps))
+    nchunks = max(1, round(stages.get("refine_fft_df32", (0, args.steps))[1] / args.steps))
     chunk = -(-b // nchunks)
     nrec = int(sum(c for _, c in stages.values()))
     # kernels in the timed region: one per timed record, plus the second kernel of the records that hold two
-    # (the double-float FFT's two passes; the coefficient gather with the Nyquist zeroing), one each per chunk
-    launches = nrec + 2 * int(stages.get("refine_inverse_fft", (0, 0))[1])
+    # (the double-float FFT's two passes, one record per chunk)
+    launches = nrec + int(stages.get("refine_fft_df32", (0, 0))[1])
     tot = sum(v for v, _ in stages.values())
     stage_summary = {k: {"ms_per_launch": v / c, "launches": c, "share": v / tot} for k, (v, c) in stages.items()}
     top, (top_ms, top_n) = max(stages.items(), key=lambda kv: kv[1][0])
@@ -1099,16 +1101,20 @@ def so3_tc_line(args, L: int, b: int, full: bool = True) -> dict:
     coef_b = 8.0 * b * C
     grid_b = 8.0 * b * N ** 3
     useful = 8.0 * B * C * b
-    tc_dir = 2 * grid_b + (grid_b + table_b + coef_b) + 2 * coef_b  # FFT + GEMM + permutation, one direction
+    gemm_dir = (grid_b + table_b + coef_b) + 2 * coef_b  # GEMM + permutation, one direction
+    tc_dir = 2 * grid_b + gemm_dir                         # with the FFT
     step_bytes = 2 * tc_dir
     tensor_flops = 2 * 6 * useful
     if full:
+        # the refined forward replaces the split-BF16 forward: double-float FFT of the samples, GEMM of its FP32
+        # part, exact synthesis contraction with the pencil-domain residual, GEMM of the residual, correction
         oz_table = nchunks * 4 * 2.0 * Kp * table_rows   # digit planes, read once per chunk launch
-        step_bytes += (tc_dir                                     # forward of the residual
+        step_bytes += (-tc_dir
+                       + 7 * grid_b                                # FFT: 8 B in, 16 + 16 B, hi + lo out
+                       + gemm_dir                                  # F0
                        + coef_b + 2 * 16.0 * b * C                 # gather: coefficients in, double-float runs out
-                       + oz_table + 16.0 * b * C + 2 * grid_b      # exact contraction: table, runs, pencils out
-                       + 4 * 2 * grid_b                            # double-float FFT: 2 passes, 16 B r + w
-                       + 2 * grid_b + 2 * grid_b                   # residual: grid + samples in, residual out
+                       + oz_table + 16.0 * b * C + 3 * grid_b      # contraction: table, runs, hi + lo in, r out
+                       + gemm_dir                                  # the residual's forward
                        + 3 * coef_b)                               # correction added
         tensor_flops += 6 * useful + 10 * useful
     hbm_floor_ms = step_bytes / (peaks["hbm_gbs"] * 1e9) * 1e3
@@ -1118,10 +1124,11 @@ def so3_tc_line(args, L: int, b: int, full: bool = True) -> dict:
                  "hbm_floor_ms": hbm_floor_ms, "tensor_floor_ms": tensor_floor_ms, "ms_per_step": ms,
                  "frac": floor_ms / ms, "peak_source": peaks["source"],
                  "note": "split-BF16 directions: FFT 2 x grid bytes, GEMM pencils + BF16 table + coefficients, "
-                         "permutation 2 x coefficients" + ("; refinement: the residual's forward, the exact "
-                                                           "inverse (digit planes per chunk, double-float runs "
-                                                           "and pencils), its two double-float FFT passes, the "
-                                                           "residual and the correction" if full else "")}
+                         "permutation 2 x coefficients" + ("; refined forward: double-float FFT of the samples "
+                                                           "(56 B per sample), two GEMMs + permutations, the "
+                                                           "exact synthesis contraction (digit planes per chunk, "
+                                                           "double-float runs, 24 B per sample of pencils) and "
+                                                           "the correction" if full else "")}
 
     # ---- end to end through the host-buffer C ABI (pinned host memory), the same plan and step count
     e2e = None
@@ -1176,13 +1183,14 @@ def so3_tc_line(args, L: int, b: int, full: bool = True) -> dict:
 
     cpu = cpu_baselines(L) if not args.no_cpu else None
     metric = METRIC if L == 255 else METRIC.replace("l_max=255", f"l_max={L}")
-    what = ("inverse (split-BF16) + refined forward (split-BF16, then one residual step with the inverse exact on "
-            "the tensor cores)" if full else "inverse + forward, split-BF16")
+    what = ("inverse (split-BF16) + refined forward (double-float FFT of the samples, split-BF16 GEMM, the residual "
+            "against the exact tensor-core synthesis formed in the pencil domain, split-BF16 GEMM of the residual)"
+            if full else "inverse + forward, split-BF16")
     line = {
         "metric": metric, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "bf16x3 (split) / fp32 accumulate / fp32 FFT" +
-                                      ("; residual step: exact BF16 digit products, double-float FFT" if full else ""),
+                                      ("; refined forward: double-float FFT, exact BF16 digit products" if full else ""),
         "data": "synthetic",
         "config": {"workload": f"SO(3) complex, l_max={L}, batch={b} functions ({N}^3 complex64 grid each), stable "
                                f"recursion; one step = {what}",

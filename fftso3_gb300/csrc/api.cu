@@ -299,10 +299,53 @@ int refine_forward(fftso3_plan* p, const void* grid, void* coeffs, cudaStream_t 
     return tc_refine_add(p->tc, resid, coeffs, st, &T, g_err);
 }
 
+// The spectral form of the refined forward (SO(3), exact inverse, N = 64..512): the samples' FFT in
+// double-float (pencils hi in the plan's pencil buffer, remainders lo in its residual buffer), F0 = the GEMM of
+// hi, then per chunk the residual in the pencil domain, r^ = (hi + lo) - N^2 H(F0) (H: the exact synthesis
+// contraction, whose FFT is N^2 H), written over hi, and F = F0 + the GEMM of r^.  Equal to the grid form
+// F0 + forward(f - inverse(F0)) -- the forward GEMM reads exactly these pencils -- without the FP32 FFTs of the
+// samples and of the residual and without the double-float FFT of the synthesis.
+int refine_forward_spectral(fftso3_plan* p, const void* grid, void* coeffs, cudaStream_t st)
+{
+    StageTimer& T = p->timer;
+    const long long C = p->coeff_elems, G = p->grid_elems;
+    float2* hi = tc_pencil_buffer(p->tc);
+    float2* lo = (float2*)tc_resid_buffer(p->tc);
+    const int per = p->real ? 1 : 2;  // floats per sample
+    for (int f0 = 0; f0 < p->batch; f0 += p->rchunk) {
+        const int nb = p->batch - f0 < p->rchunk ? p->batch - f0 : p->rchunk;
+        int rc = oz_forward_fft(p->oz, (const float*)grid + (long long)f0 * G * per, p->real, nb,
+                                hi + (long long)f0 * G, lo + (long long)f0 * G, st, &T, g_err);
+        if (rc) return rc;
+    }
+    int rc = tc_forward_pencils(p->tc, coeffs, st, &T, g_err);
+    if (rc) return rc;
+    for (int f0 = 0; f0 < p->batch; f0 += p->rchunk) {
+        const int nb = p->batch - f0 < p->rchunk ? p->batch - f0 : p->rchunk;
+        const void* Fc = (const float2*)coeffs + (long long)f0 * C;
+        if (p->real) {
+            STAGE(ST_REFINE, launch_widen((const float*)coeffs + (long long)f0 * C, (double*)p->d_rc,
+                                          (long long)nb * C, st));
+            STAGE(ST_BASIS, launch_so3_r2c(p->d_rc, p->d_rfc, true, p->L, nb, st));
+            Fc = p->d_rfc;
+        }
+        if ((rc = oz_resid_pencils(p->oz, Fc, p->real, nb, hi + (long long)f0 * G, lo + (long long)f0 * G, st, &T,
+                                   g_err)))
+            return rc;
+    }
+    return tc_refine_add_pencils(p->tc, coeffs, st, &T, g_err);
+}
+
+bool spectral_refine(const fftso3_plan* p)
+{
+    return p->tc && p->oz && (p->flags & FFTSO3_FLAG_REFINE) && oz_spectral(p->oz);
+}
+
 int run_forward(fftso3_plan* p, const void* grid, void* coeffs, cudaStream_t st)
 {
     const int N = p->N, L = p->L, b = p->batch;
     StageTimer& T = p->timer;
+    if (spectral_refine(p)) return refine_forward_spectral(p, grid, coeffs, st);
     if (p->tc) {
         int rc = tc_forward(p->tc, grid, coeffs, st, &T, g_err);
         if (rc || !(p->flags & FFTSO3_FLAG_REFINE)) return rc;
@@ -522,6 +565,10 @@ int fftso3_plan_create(fftso3_plan** out, int kind, int l_max, int batch, int pr
             size_t nch = 16;
             while (nch > 1 && (planes + nch * per_fn + slack > freeb || freeb + tab64 < planes + nch * per_fn + spare))
                 nch = nch > 8 ? 8 : nch - 1;
+            if (const char* ev = getenv("FFTSO3_REFINE_CHUNK")) {  // cap (1..16), e.g. to exercise several chunks
+                const int c = atoi(ev);
+                if (c >= 1 && (size_t)c < nch) nch = (size_t)c;
+            }
             p->rchunk = (int)(nch < (size_t)batch ? nch : (size_t)batch);
             std::string err;
             if ((rc = oz_create(&p->oz, p->d_table, goff, L, N, p->rchunk, p->d_tw, err))) {
@@ -675,9 +722,11 @@ int fftso3_forward_host(fftso3_plan* plan, const void* grid_host, void* coeffs_h
     const void* gin = host_device_ptr(grid_host);
     void* cout = host_device_ptr(coeffs_host);
     if (plan->tc && (plan->flags & FFTSO3_FLAG_REFINE)) {
-        // the refinement reads the samples twice (first forward, then the residual): copy them once into the
-        // residual buffer, which the residual then overwrites chunk by chunk, in place
-        void* stage = tc_resid_buffer(plan->tc);
+        // the refinement reads the samples twice: copy them once into the residual buffer (batch complex64 grids);
+        // the residual (grid form) or the FFT remainders (spectral form) then overwrite them chunk by chunk, each
+        // chunk's samples read before its outputs are written.  Real samples go to the buffer's upper half, so
+        // that a chunk's complex64 remainders never reach the samples of later chunks.
+        void* stage = (char*)tc_resid_buffer(plan->tc) + (plan->real ? grid_bytes(plan) : 0);
         CK(cudaMemcpyAsync(stage, grid_host, grid_bytes(plan), cudaMemcpyHostToDevice, st));
         gin = stage;
     }

@@ -1758,6 +1758,58 @@ int tc_forward(TCState* s, const void* grid, void* coeffs, cudaStream_t st, Stag
 
 void* tc_resid_buffer(TCState* s) { return s ? (void*)s->d_resid : nullptr; }
 
+float2* tc_pencil_buffer(TCState* s) { return s ? s->d_pencil : nullptr; }
+
+// forward from pencils already in d_pencil: GEMM, then the packed (and real-basis) coefficients
+static int forward_from_pencils(TCState* s, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err)
+{
+    T->begin(ST_GEMM_FWD, st);
+    int rc = launch_gemm(s, true, st, err);
+    if (rc) return rc;
+    T->end(st);
+    return tc_forward_finish(s, coeffs, st, T, err);
+}
+
+int tc_forward_pencils(TCState* s, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err)
+{
+    if (s->s2) {
+        err = "internal: pencil-domain forward is SO(3) only";
+        return FFTSO3_ERR_CUDA;
+    }
+    return forward_from_pencils(s, coeffs, st, T, err);
+}
+
+int tc_refine_add_pencils(TCState* s, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err)
+{
+    if (!s->refine || !s->d_coef2 || s->s2) {
+        err = "internal: refinement buffers were not allocated";
+        return FFTSO3_ERR_CUDA;
+    }
+    // the correction in the coefficients' own element type: complex in d_coef2, real kinds in d_fc
+    void* corr = s->real ? (void*)s->d_fc : (void*)s->d_coef2;
+    if (s->real) {
+        // tc_forward_finish writes the complex coefficients into d_fc first; route them through d_coef2
+        T->begin(ST_GEMM_FWD, st);
+        int rc = launch_gemm(s, true, st, err);
+        if (rc) return rc;
+        T->end(st);
+        T->begin(ST_BASIS, st);
+        group_to_packed_tiled<<<ptile_grid(s->L, s->batch), 256, 0, st>>>(s->d_fg, s->d_coef2, s->d_goff2, s->L,
+                                                                          coeffs_per_fn(s), s->batch);
+        TCK(cudaGetLastError());
+        TCK(launch_so3_c2r(s->d_coef2, s->d_fc, false, s->L, s->batch, st));
+        T->end(st);
+    } else {
+        int rc = forward_from_pencils(s, s->d_coef2, st, T, err);
+        if (rc) return rc;
+    }
+    const long long nc = (long long)s->batch * coeffs_per_fn(s);
+    T->begin(ST_REFINE, st);
+    TCK(launch_add_real((float*)coeffs, (const float*)corr, s->real ? nc : 2 * nc, st));
+    T->end(st);
+    return FFTSO3_SUCCESS;
+}
+
 int tc_refine_add(TCState* s, const void* resid, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err)
 {
     if (!s->refine || !s->d_coef2) {

@@ -457,16 +457,21 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(const TIN* __restrict__ 
 //   rows padded by one element per 8 (phys(i) = i + i / 8): a stage's strided reads and scattered writes;
 //   row stride N + N / 8 + 1 elements (one extra 16-byte slot): the TK rows of the load / store phases;
 //   twiddles per stage as [r - 1][kt] (kt = butterfly index mod Ns): consecutive lanes, consecutive entries.
-// RESID (1 complex, 2 real samples): the transform along q of the refinement's grid synthesis, whose store phase
-// forms the residual instead of writing the lines back: r[fn][k][j1][j2] = (f - g.h) - g.l (FP32; real samples:
-// against the real part) at the same places of the samples f, o = (fn, j1) and the line index j = j2, so each of
-// the TK lines of a CTA is one contiguous row of the grid.  fin may be r (each element is read, then written, by
-// one thread).
-template <int N, int RESID>
+// Grid-row forms, for lines o = (fn, j1) along j2 (S = N, oinner = N, oouter = N^3, oistride = N^2), whose TK
+// lines are TK rows of a grid [fn][k][j1][j2] (index rbase + kk N^2 + j):
+//   LOAD 1 / 2 (complex / real FP32 samples f): the lines are read from the grid rows instead of buf (the first
+//     pass of the double-float forward FFT; the store then writes buf [fn][j1][q][k]);
+//   STORE 1 / 2: the store forms the residual r = (f - g.h) - g.l (FP32; real samples: against the real part)
+//     at the samples' places instead of writing the lines back (fin may be r: each element is read, then
+//     written, by one thread).
+// STORE 3: the lines are written, renormalised, as two complex64 arrays at buf's index: hi (the FP32 rounding)
+// and lo (the remainder).
+template <int N, int LOAD, int STORE>
 __global__ void __launch_bounds__(256, 3) fft_df32_k_kernel(dfc32* __restrict__ buf, long long S, long long oinner,
                                                              long long oouter, long long oistride,
                                                              const double2* __restrict__ twg, const void* fin,
-                                                             float* r)
+                                                             float* r, float2* __restrict__ hi,
+                                                             float2* __restrict__ lo)
 {
     constexpr int TK = 2048 / N;         // lines per CTA
     constexpr int TPL = N / 8;           // threads per line
@@ -490,10 +495,28 @@ __global__ void __launch_bounds__(256, 3) fft_df32_k_kernel(dfc32* __restrict__ 
             off += (R - 1) * Ns;
         }
     }
+    constexpr long long NN = (long long)N * N;
+    const long long rbase = (o / oinner) * NN * N + (o % oinner) * N + (long long)blockIdx.x * TK * NN;
+    if constexpr (LOAD == 0) {
 #pragma unroll
-    for (int u = 0; u < N * TK / 256; ++u) {
-        const int e = tid + 256 * u, kk = e % TK, j = e / TK;
-        sm[kk * ROW + phys(j)] = buf[obase + (long long)j * S + kk];
+        for (int u = 0; u < N * TK / 256; ++u) {
+            const int e = tid + 256 * u, kk = e % TK, j = e / TK;
+            sm[kk * ROW + phys(j)] = buf[obase + (long long)j * S + kk];
+        }
+    } else {
+#pragma unroll
+        for (int u = 0; u < N * TK / 256; ++u) {
+            const int e = tid + 256 * u, kk2 = e / N, j = e % N;
+            const long long i = rbase + kk2 * NN + j;
+            dfc32 v;
+            if constexpr (LOAD == 2) {
+                v = dfc32{df32(reinterpret_cast<const float*>(fin)[i]), df32(0.f)};
+            } else {
+                const float2 x = reinterpret_cast<const float2*>(fin)[i];
+                v = dfc32{df32(x.x), df32(x.y)};
+            }
+            sm[kk2 * ROW + phys(j)] = v;
+        }
     }
     __syncthreads();
     const int kk = tid / TPL, t = tid % TPL;
@@ -538,21 +561,29 @@ __global__ void __launch_bounds__(256, 3) fft_df32_k_kernel(dfc32* __restrict__ 
         }
         __syncthreads();
     }
-    if constexpr (RESID == 0) {
+    if constexpr (STORE == 0) {
 #pragma unroll
         for (int u = 0; u < N * TK / 256; ++u) {
             const int e = tid + 256 * u, kk2 = e % TK, j = e / TK;
             buf[obase + (long long)j * S + kk2] = sm[kk2 * ROW + phys(j)];
         }
+    } else if constexpr (STORE == 3) {
+#pragma unroll
+        for (int u = 0; u < N * TK / 256; ++u) {
+            const int e = tid + 256 * u, kk2 = e % TK, j = e / TK;
+            const dfc32 v = sm[kk2 * ROW + phys(j)];
+            const df32 a = df_two_sum(v.x.h, v.x.l), b = df_two_sum(v.y.h, v.y.l);
+            const long long i = obase + (long long)j * S + kk2;
+            hi[i] = make_float2(a.h, b.h);
+            lo[i] = make_float2(a.l, b.l);
+        }
     } else {
-        constexpr long long NN = (long long)N * N;
-        const long long rbase = (o / oinner) * NN * N + (o % oinner) * N + (long long)blockIdx.x * TK * NN;
 #pragma unroll
         for (int u = 0; u < N * TK / 256; ++u) {
             const int e = tid + 256 * u, kk2 = e / N, j = e % N;
             const dfc32 v = sm[kk2 * ROW + phys(j)];
             const long long i = rbase + kk2 * NN + j;
-            if constexpr (RESID == 2) {
+            if constexpr (STORE == 2) {
                 r[i] = (reinterpret_cast<const float*>(fin)[i] - v.x.h) - v.x.l;
             } else {
                 const float2 f = reinterpret_cast<const float2*>(fin)[i];
@@ -898,6 +929,27 @@ cudaError_t launch_slice_fft(const BucketSeg* segs, int nseg, long long nblk, si
 
 bool fft_df32_k_supported(int N) { return N == 64 || N == 128 || N == 256 || N == 512; }
 
+template <int LOAD, int STORE>
+static void df32_k_launch(int N, dim3 grid, dfc32* b, long long S, long long oinner, long long oouter,
+                          long long oistride, const double2* t, const void* fin, float* r, float2* hi, float2* lo,
+                          cudaStream_t st)
+{
+    switch (N) {
+        case 64:
+            fft_df32_k_kernel<64, LOAD, STORE><<<grid, 256, 0, st>>>(b, S, oinner, oouter, oistride, t, fin, r, hi, lo);
+            break;
+        case 128:
+            fft_df32_k_kernel<128, LOAD, STORE><<<grid, 256, 0, st>>>(b, S, oinner, oouter, oistride, t, fin, r, hi, lo);
+            break;
+        case 256:
+            fft_df32_k_kernel<256, LOAD, STORE><<<grid, 256, 0, st>>>(b, S, oinner, oouter, oistride, t, fin, r, hi, lo);
+            break;
+        default:
+            fft_df32_k_kernel<512, LOAD, STORE><<<grid, 256, 0, st>>>(b, S, oinner, oouter, oistride, t, fin, r, hi, lo);
+            break;
+    }
+}
+
 cudaError_t launch_fft_df32_k(void* buf, int N, long long S, long long nouter, long long oinner, long long oouter,
                               long long oistride, const void* tw, cudaStream_t st)
 {
@@ -905,26 +957,8 @@ cudaError_t launch_fft_df32_k(void* buf, int N, long long S, long long nouter, l
     const dim3 grid((unsigned)(N / (2048 / N)), (unsigned)nouter);
     dfc32* b = (dfc32*)buf;
     const double2* t = (const double2*)tw;
-    switch (N) {
-        case 64: fft_df32_k_kernel<64, 0><<<grid, 256, 0, st>>>(b, S, oinner, oouter, oistride, t, nullptr, nullptr); break;
-        case 128: fft_df32_k_kernel<128, 0><<<grid, 256, 0, st>>>(b, S, oinner, oouter, oistride, t, nullptr, nullptr); break;
-        case 256: fft_df32_k_kernel<256, 0><<<grid, 256, 0, st>>>(b, S, oinner, oouter, oistride, t, nullptr, nullptr); break;
-        default: fft_df32_k_kernel<512, 0><<<grid, 256, 0, st>>>(b, S, oinner, oouter, oistride, t, nullptr, nullptr); break;
-    }
+    df32_k_launch<0, 0>(N, grid, b, S, oinner, oouter, oistride, t, nullptr, nullptr, nullptr, nullptr, st);
     return cudaGetLastError();
-}
-
-template <int RESID>
-static void df32_resid_launch(int N, dim3 grid, dfc32* b, long long NN, const double2* t, const void* fin, float* r,
-                              cudaStream_t st)
-{
-    const long long N3 = NN * N;
-    switch (N) {
-        case 64: fft_df32_k_kernel<64, RESID><<<grid, 256, 0, st>>>(b, N, N, N3, NN, t, fin, r); break;
-        case 128: fft_df32_k_kernel<128, RESID><<<grid, 256, 0, st>>>(b, N, N, N3, NN, t, fin, r); break;
-        case 256: fft_df32_k_kernel<256, RESID><<<grid, 256, 0, st>>>(b, N, N, N3, NN, t, fin, r); break;
-        default: fft_df32_k_kernel<512, RESID><<<grid, 256, 0, st>>>(b, N, N, N3, NN, t, fin, r); break;
-    }
 }
 
 cudaError_t launch_fft_df32_k_resid(const void* buf, int N, long long nb, const void* fin, bool real, float* r,
@@ -932,12 +966,32 @@ cudaError_t launch_fft_df32_k_resid(const void* buf, int N, long long nb, const 
 {
     if (!fft_df32_k_supported(N) || nb < 1 || nb * N > 65535) return cudaErrorInvalidValue;
     const dim3 grid((unsigned)(N / (2048 / N)), (unsigned)(nb * N));
-    dfc32* b = (dfc32*)buf;
     const long long NN = (long long)N * N;
+    const double2* t = (const double2*)tw;
     if (real)
-        df32_resid_launch<2>(N, grid, b, NN, (const double2*)tw, fin, r, st);
+        df32_k_launch<0, 2>(N, grid, (dfc32*)buf, N, N, NN * N, NN, t, fin, r, nullptr, nullptr, st);
     else
-        df32_resid_launch<1>(N, grid, b, NN, (const double2*)tw, fin, r, st);
+        df32_k_launch<0, 1>(N, grid, (dfc32*)buf, N, N, NN * N, NN, t, fin, r, nullptr, nullptr, st);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fft_df32_k_forward(void* buf, int N, long long nb, const void* f, bool real, float2* hi,
+                                      float2* lo, const void* tw, cudaStream_t st)
+{
+    if (!fft_df32_k_supported(N) || nb < 1 || nb * N > 65535) return cudaErrorInvalidValue;
+    const dim3 grid((unsigned)(N / (2048 / N)), (unsigned)(nb * N));
+    const long long NN = (long long)N * N;
+    const double2* t = (const double2*)tw;
+    dfc32* b = (dfc32*)buf;
+    // along j2, from the grid rows, into buf [fn][j1][q][k]
+    if (real)
+        df32_k_launch<2, 0>(N, grid, b, N, N, NN * N, NN, t, f, nullptr, nullptr, nullptr, st);
+    else
+        df32_k_launch<1, 0>(N, grid, b, N, N, NN * N, NN, t, f, nullptr, nullptr, nullptr, st);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    // along j1 (stride N^2), lines (fn, q), into the pencils [fn][p][q][k] as hi + lo
+    df32_k_launch<0, 3>(N, grid, b, NN, N, NN * N, N, t, nullptr, nullptr, hi, lo, st);
     return cudaGetLastError();
 }
 

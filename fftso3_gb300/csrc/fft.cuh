@@ -44,6 +44,11 @@ cudaError_t launch_fft_df32_k(void* buf, int N, long long S, long long nouter, l
 // the real part; fin may be r).  The lines along p must have been transformed before.
 cudaError_t launch_fft_df32_k_resid(const void* buf, int N, long long nb, const void* fin, bool real, float* r,
                                     const void* tw, cudaStream_t st);
+// Double-float forward FFT of nb sample grids f [fn][k][j1][j2] (complex64, or float32 when real) into the
+// k-contiguous pencils [fn][p][q][k], written renormalised as hi (complex64, the FP32 rounding) + lo (the
+// remainder); buf: nb double-float grids of work space.
+cudaError_t launch_fft_df32_k_forward(void* buf, int N, long long nb, const void* f, bool real, float2* hi,
+                                      float2* lo, const void* tw, cudaStream_t st);
 
 // Register-resident FP32 kernels for N = 64..1024, powers of two (fft_fast.cu).
 bool fft_fast_supported(int N);

@@ -94,6 +94,11 @@ struct Args {
     const signed char* ey;  // exponents [fn][group][pair]
     const signed char* et;  // exponents [group][k]
     float4* pout;           // double-float pencils [fn][p][q][k]
+    // spectral residual (rhi non-null): instead of H, write r = (rhi + rlo) - N^2 H at the forward pencil place
+    // (-m, -n) of each (m, n), into rhi (complex64 pencils [fn][p][q][k]; rlo the remainders); e2n = log2 N^2
+    float2* rhi;
+    const float2* rlo;
+    int e2n;
     int* err;
 };
 
@@ -364,11 +369,14 @@ __global__ void __launch_bounds__(THREADS, 1)
             item_mn(item, m0, n0);
             const GroupPairs P = group_pairs(m0, n0);
             const int k = item.y * BM + r;
+            const bool spectral = a.rhi != nullptr;
             long long poff[4];
 #pragma unroll
             for (int p = 0; p < 4; ++p) {
-                int pi = P.m[p] % N; if (pi < 0) pi += N;
-                int qi = P.n[p] % N; if (qi < 0) qi += N;
+                // synthesis: H(m, n) at (m, n) mod N; spectral residual: at the forward place (-m, -n) mod N
+                const int mm = spectral ? -P.m[p] : P.m[p], nn = spectral ? -P.n[p] : P.n[p];
+                int pi = mm % N; if (pi < 0) pi += N;
+                int qi = nn % N; if (qi < 0) qi += N;
                 poff[p] = ((long long)pi * N + qi) * N;
             }
             const int et = k < N ? (int)a.et[(long long)item.x * N + k] : 0;
@@ -389,7 +397,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                 for (int fq = 0; fq < 2; ++fq) {
                     const int f = item.z * FPT + cc * 2 + fq;
                     if (f >= a.batch || k >= N) continue;
-                    float4* Ho = a.pout + (long long)f * a.fstride + k;
+                    const long long fo = (long long)f * a.fstride + k;
                     const signed char* eyf = a.ey + ((long long)f * a.ngroups + item.x) * 4;
 #pragma unroll
                     for (int p = 0; p < 4; ++p) {
@@ -400,7 +408,17 @@ __global__ void __launch_bounds__(THREADS, 1)
                                                        __uint_as_float(v[2][cr]), __uint_as_float(v[3][cr]));
                         const df32 im = combine_levels(__uint_as_float(v[0][cr + 1]), __uint_as_float(v[1][cr + 1]),
                                                        __uint_as_float(v[2][cr + 1]), __uint_as_float(v[3][cr + 1]));
-                        Ho[poff[p]] = make_float4(ldexpf(re.h, E), ldexpf(re.l, E), ldexpf(im.h, E), ldexpf(im.l, E));
+                        if (spectral) {
+                            // N^2 H = FFT of the synthesised grid; hi - N^2 H.h is exact (close values)
+                            const int E2 = E + a.e2n;
+                            const long long i = fo + poff[p];
+                            const float2 h = a.rhi[i], l = a.rlo[i];
+                            a.rhi[i] = make_float2((h.x - ldexpf(re.h, E2)) + (l.x - ldexpf(re.l, E2)),
+                                                   (h.y - ldexpf(im.h, E2)) + (l.y - ldexpf(im.l, E2)));
+                        } else {
+                            a.pout[fo + poff[p]] =
+                                make_float4(ldexpf(re.h, E), ldexpf(re.l, E), ldexpf(im.h, E), ldexpf(im.l, E));
+                        }
                     }
                 }
             }
@@ -756,8 +774,10 @@ int oz_status(OZState* o)
         }                                                                      \
     } while (0)
 
-int oz_inverse_resid(OZState* o, const void* F, bool f64, int nb, const void* fgrid, bool real, float* resid,
-                     cudaStream_t st, StageTimer* T, std::string& err)
+// coefficients -> double-float group-major runs and their exponents, then the exact contraction: H into the
+// double-float pencils (rhi null), or the spectral residual into rhi
+static int oz_contract(OZState* o, const void* F, bool f64, int nb, float2* rhi, const float2* rlo, cudaStream_t st,
+                       StageTimer* T, std::string& err)
 {
     if (nb < 1 || nb > o->chunk) {
         err = "internal: refinement chunk larger than its buffers";
@@ -765,7 +785,6 @@ int oz_inverse_resid(OZState* o, const void* F, bool f64, int nb, const void* fg
     }
     const int N = o->N, L = o->L;
     const long long NN = (long long)N * N;
-    // coefficients -> double-float group-major runs and their exponents
     T->begin(ST_REFINE, st);
     {
         const long long warps = (long long)nb * o->ngroups;
@@ -777,12 +796,13 @@ int oz_inverse_resid(OZState* o, const void* F, bool f64, int nb, const void* fg
             gather_kernel<float2><<<blocks, 256, 0, st>>>((const float2*)F, o->C, o->Y, o->ey, o->goff2, L, o->ngroups,
                                                           nb);
         OZK(cudaGetLastError());
-        const long long tot = (long long)nb * 2 * NN;
-        zero_nyquist_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(o->pen, N, nb);
-        OZK(cudaGetLastError());
+        if (!rhi) {
+            const long long tot = (long long)nb * 2 * NN;
+            zero_nyquist_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(o->pen, N, nb);
+            OZK(cudaGetLastError());
+        }
     }
     T->end(st);
-    // the exact contraction
     T->begin(ST_REF_CONTRACT, st);
     {
         Args a;
@@ -799,12 +819,52 @@ int oz_inverse_resid(OZState* o, const void* F, bool f64, int nb, const void* fg
         a.ey = o->ey;
         a.et = o->et;
         a.pout = o->pen;
+        a.rhi = rhi;
+        a.rlo = rlo;
+        int e2n = 0;
+        while ((1LL << e2n) < NN) ++e2n;
+        a.e2n = e2n;
         a.err = o->err;
         const int nctas = o->nitems < o->nsm ? o->nitems : o->nsm;
         oz_inv_kernel<<<nctas, THREADS, SMEM_BYTES, st>>>(o->tm[0], o->tm[1], o->tm[2], o->tm[3], a);
         OZK(cudaGetLastError());
     }
     T->end(st);
+    return FFTSO3_SUCCESS;
+}
+
+bool oz_spectral(const OZState* o) { return o && fft_df32_k_supported(o->N); }
+
+int oz_forward_fft(OZState* o, const void* fgrid, bool real, int nb, float2* hi, float2* lo, cudaStream_t st,
+                   StageTimer* T, std::string& err)
+{
+    if (!oz_spectral(o) || nb < 1 || nb > o->chunk) {
+        err = "internal: double-float forward FFT needs N = 64..512 and nb <= chunk";
+        return FFTSO3_ERR_CUDA;
+    }
+    T->begin(ST_REF_FFT, st);
+    OZK(launch_fft_df32_k_forward(o->pen, o->N, nb, fgrid, real, hi, lo, o->d_tw, st));
+    T->end(st);
+    return FFTSO3_SUCCESS;
+}
+
+int oz_resid_pencils(OZState* o, const void* F, bool f64, int nb, float2* hi, const float2* lo, cudaStream_t st,
+                     StageTimer* T, std::string& err)
+{
+    if (!oz_spectral(o)) {
+        err = "internal: spectral residual needs N = 64..512";
+        return FFTSO3_ERR_CUDA;
+    }
+    return oz_contract(o, F, f64, nb, hi, lo, st, T, err);
+}
+
+int oz_inverse_resid(OZState* o, const void* F, bool f64, int nb, const void* fgrid, bool real, float* resid,
+                     cudaStream_t st, StageTimer* T, std::string& err)
+{
+    int rc = oz_contract(o, F, f64, nb, nullptr, nullptr, st, T, err);
+    if (rc) return rc;
+    const int N = o->N;
+    const long long NN = (long long)N * N;
     // double-float FFT over p (lines (fn, q, k)), then over q (lines (fn, p, k)) with the residual against the
     // FP32 samples formed in the second pass's store phase (its lines are rows of the grid [fn][k][j1][j2])
     T->begin(ST_REF_FFT, st);

@@ -26,4 +26,15 @@ int oz_status(OZState* o);
 int oz_inverse_resid(OZState* o, const void* F, bool f64, int nb, const void* fgrid, bool real, float* resid,
                      cudaStream_t st, StageTimer* T, std::string& err);
 
+// The spectral form of the residual step (N = 64..512): the forward's FFT in double-float and the residual in
+// the pencil domain, r^ = FFT(f) - N^2 H(F), which is what the forward GEMM consumes -- no FP32 FFT of f or of
+// the residual.  oz_forward_fft: nb <= chunk sample grids f (complex64, or float32 when real) -> pencils
+// [fn][p][q][k] as hi (complex64) + lo (remainder).  oz_resid_pencils: hi := (hi + lo) - N^2 H(F) at every
+// pencil place the forward GEMM reads, for nb <= chunk coefficient sets F (as oz_inverse_resid).
+bool oz_spectral(const OZState* o);
+int oz_forward_fft(OZState* o, const void* fgrid, bool real, int nb, float2* hi, float2* lo, cudaStream_t st,
+                   StageTimer* T, std::string& err);
+int oz_resid_pencils(OZState* o, const void* F, bool f64, int nb, float2* hi, const float2* lo, cudaStream_t st,
+                     StageTimer* T, std::string& err);
+
 }  // namespace fftso3

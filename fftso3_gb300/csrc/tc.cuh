@@ -24,6 +24,11 @@ int tc_inverse(TCState* s, const void* coeffs, void* grid, cudaStream_t st, Stag
 // plan's sample type), and coeffs += forward(resid) in the coefficients' element type.
 void* tc_resid_buffer(TCState* s);
 int tc_refine_add(TCState* s, const void* resid, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err);
+// Spectral refinement (SO(3)): the plan's pencil buffer (complex64 [fn][p][q][k], batch functions), the forward
+// from pencils already there (GEMM + coefficient permutation + real basis), and coeffs += forward(pencils).
+float2* tc_pencil_buffer(TCState* s);
+int tc_forward_pencils(TCState* s, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err);
+int tc_refine_add_pencils(TCState* s, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err);
 // Device error word of the tensor-core kernels (0 = no bounded wait timed out); synchronising read.
 int tc_status(TCState* s);
 

@@ -30,7 +30,7 @@ inline const char* stage_name(int s)
     static const char* names[ST_COUNT] = {"fft_rows", "fft_cols", "zero_nyquist", "fp64_fwd_contract",
                                           "fp64_inv_contract", "basis_convert", "tc_pack_fwd", "tc_gemm_fwd",
                                           "tc_pack_inv", "tc_gemm_inv", "tc_refine_elementwise", "fft_2d",
-                                          "refine_inverse_contract", "refine_inverse_fft", "fft_slices",
+                                          "refine_exact_contract", "refine_fft_df32", "fft_slices",
                                           "coeff_convert"};
     return (s >= 0 && s < ST_COUNT) ? names[s] : "";
 }

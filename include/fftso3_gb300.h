@@ -63,8 +63,12 @@ extern "C" {
 
 /* plan flags */
 #define FFTSO3_FLAG_REFINE 0x1u /* FP32-data forward: one residual step F += forward(f - inverse(F)); the
-                                   inverse of F and the difference f - inverse(F) are formed in FP64, so the
-                                   correction removes the first forward's FP32 FFT and contraction errors */
+                                   inverse of F and the difference f - inverse(F) are formed in FP64 or exactly
+                                   (SO(3), l_max <= 255: digit sums on the tensor cores; for N = 64..512 the
+                                   step runs in the pencil domain on a double-float FFT of the samples), so the
+                                   correction removes the first forward's FP32 FFT and contraction errors.
+                                   Environment at plan creation: FFTSO3_REFINE_FP64=1 keeps the FP64 inverse;
+                                   FFTSO3_REFINE_CHUNK=n caps the functions per refinement chunk */
 #define FFTSO3_FLAG_GRAPH 0x2u  /* batches: capture each direction into a CUDA graph, replay it */
 #define FFTSO3_FLAG_AUTOTUNE 0x4u /* tensor-core plans: time the launch shapes of the generic-N FFT passes on
                                      the plan's workspace at creation and keep the fastest (cached per N for

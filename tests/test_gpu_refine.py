@@ -2,8 +2,11 @@
 
 F += forward(f - inverse(F)): for SO(3) with l_max <= 255 the inverse runs on the
 tensor cores with exact digit sums (BF16 digit planes, FP32 TMEM accumulators that
-never round), then a double-float FFT and the residual against the FP32 samples;
-FFTSO3_REFINE_FP64=1 at plan creation selects the FP64 inverse instead.  Either
+never round).  For N = 64..512 (l_max 31, 63, 127, 255) the step is spectral: the
+samples' FFT in double-float, F0 from its FP32 part, and the residual
+FFT(f) - N^2 H(F0) in the pencil domain; otherwise a double-float FFT of the
+synthesis and the residual against the FP32 samples on the grid.
+FFTSO3_REFINE_FP64=1 at plan creation selects the FP64 inverse (grid form).  Either
 way the refined coefficients are the FP64 forward of the FP32 samples up to the
 complex64 rounding of the output.
 
@@ -32,21 +35,29 @@ def per_l_errors(a, b, l_max):
     return rms, mx
 
 
-def _refined(gblib, kind, L, grids32, fp64_inverse=False):
+def _with_env(env, make):
+    old = {k: os.environ.get(k) for k in env}
+    os.environ.update(env)
+    try:
+        return make()
+    finally:
+        for k, v in old.items():
+            if v is None:
+                del os.environ[k]
+            else:
+                os.environ[k] = v
+
+
+def _refined(gblib, kind, L, grids32, fp64_inverse=False, chunk=None):
     import torch
     s = torch.cuda.current_stream().cuda_stream
     b = grids32.shape[0]
-    old = os.environ.get("FFTSO3_REFINE_FP64")
+    env = {}
     if fp64_inverse:
-        os.environ["FFTSO3_REFINE_FP64"] = "1"
-    try:
-        p = gblib.Plan(kind, L, b, "tc_bf16x3", "stable", gblib.FLAG_REFINE)
-    finally:
-        if fp64_inverse:
-            if old is None:
-                del os.environ["FFTSO3_REFINE_FP64"]
-            else:
-                os.environ["FFTSO3_REFINE_FP64"] = old
+        env["FFTSO3_REFINE_FP64"] = "1"
+    if chunk:
+        env["FFTSO3_REFINE_CHUNK"] = str(chunk)
+    p = _with_env(env, lambda: gblib.Plan(kind, L, b, "tc_bf16x3", "stable", gblib.FLAG_REFINE))
     cplx = kind == gblib.SO3_COMPLEX
     g = torch.from_numpy(np.ascontiguousarray(grids32).ravel()).cuda()
     c = torch.empty(b * p.coeff_elems, dtype=torch.complex64 if cplx else torch.float32, device="cuda")
@@ -59,7 +70,7 @@ def _refined(gblib, kind, L, grids32, fp64_inverse=False):
 
 @pytest.mark.parametrize("kind,L", [("complex", 15), ("complex", 31), ("real", 31), ("complex", 47), ("real", 20)])
 def test_refined_forward_matches_oracle(gblib, oracle, kind, L):
-    """Batch 9: two refinement chunks (8 + 1 functions), and both column tiles of the exact inverse."""
+    """Batch 9 in refinement chunks of 4 (4 + 4 + 1 functions, FFTSO3_REFINE_CHUNK=4)."""
     cplx = kind == "complex"
     k = gblib.SO3_COMPLEX if cplx else gblib.SO3_REAL
     N = 2 * (L + 1)
@@ -75,7 +86,7 @@ def test_refined_forward_matches_oracle(gblib, oracle, kind, L):
             ref = oracle.so3_forward_real(L, g.astype(np.float64))
         grids.append(g.reshape(N, N, N))
         refs.append(ref)
-    out = _refined(gblib, k, L, np.stack(grids))
+    out = _refined(gblib, k, L, np.stack(grids), chunk=4)
     for i in range(b):
         rms, mx = per_l_errors(out[i], refs[i], L)
         assert rms <= 1e-7 and mx <= 1e-6, (i, rms, mx)
@@ -98,15 +109,17 @@ def test_exact_and_fp64_refinement_agree(gblib, oracle):
         assert rms <= 1e-7 and mx <= 1e-6, (i, rms, mx)
 
 
+@pytest.mark.parametrize("L", [15, 31])
 @pytest.mark.parametrize("kind", ["complex", "real"])
-def test_refined_host_call_equals_device_call(gblib, oracle, kind):
-    """fftso3_forward_host on a refined plan (samples staged once into the residual buffer, which the residual
-    then overwrites in place) gives the same coefficients, bit for bit, as fftso3_forward on device buffers;
-    pageable and pinned host samples, batch 3, and the host samples are left unchanged."""
+def test_refined_host_call_equals_device_call(gblib, oracle, kind, L):
+    """fftso3_forward_host on a refined plan (samples staged once into the residual buffer, which the residual --
+    grid form, l_max 15 -- or the FFT remainders -- spectral form, l_max 31 -- then overwrite chunk by chunk)
+    gives the same coefficients, bit for bit, as fftso3_forward on device buffers; pageable and pinned host
+    samples, batch 3, and the host samples are left unchanged."""
     import torch
     cplx = kind == "complex"
     k = gblib.SO3_COMPLEX if cplx else gblib.SO3_REAL
-    L, b = 15, 3
+    b = 3
     N = 2 * (L + 1)
     gs = []
     for i in range(b):
