@@ -1945,6 +1945,7 @@ struct TCFused {
     // three-launch directions (SO(3) batches, tc_fused_phases): the bucket table of the slice FFT and the
     // coefficient conversions
     BucketSeg* d_bseg = nullptr;
+    unsigned short* d_cseg = nullptr;  // segment of each conversion CTA
     int nbseg = 0;
     long long nblk = 0, ncblk = 0;
     size_t slice_smem = 0;
@@ -1955,6 +1956,7 @@ void tc_fused_destroy(TCFused* f)
 {
     if (!f) return;
     if (f->d_bseg) cudaFree(f->d_bseg);
+    if (f->d_cseg) cudaFree(f->d_cseg);
     for (int d = 0; d < 2; ++d) {
         if (f->d_segs[d]) cudaFree(f->d_segs[d]);
         if (f->d_items[d]) cudaFree(f->d_items[d]);
@@ -2132,12 +2134,26 @@ int tc_fused_phases(TCFused* f, const std::vector<long long>& g0, const std::vec
         cblk += ((long long)p->batch * so3_off(p->B) + CONVERT_THREADS - 1) / CONVERT_THREADS;
         segs.push_back(s);
     }
+    if (segs.size() > 65535 || Nmax > 512) {
+        err = "fused phases: at most 65535 buckets of l_max <= 255";
+        return FFTSO3_ERR_UNSUPPORTED;
+    }
+    std::vector<unsigned short> cseg((size_t)cblk);
+    for (size_t i = 0; i < segs.size(); ++i) {
+        const long long end = i + 1 < segs.size() ? segs[i + 1].cblk0 : cblk;
+        for (long long c = segs[i].cblk0; c < end; ++c) cseg[(size_t)c] = (unsigned short)i;
+    }
     cudaError_t e;
     if (f->d_bseg) cudaFree(f->d_bseg);
+    if (f->d_cseg) cudaFree(f->d_cseg);
     f->d_bseg = nullptr;
+    f->d_cseg = nullptr;
     if ((e = cudaMalloc(&f->d_bseg, sizeof(BucketSeg) * segs.size())) != cudaSuccess ||
         (e = cudaMemcpy(f->d_bseg, segs.data(), sizeof(BucketSeg) * segs.size(), cudaMemcpyHostToDevice)) !=
-            cudaSuccess) {
+            cudaSuccess ||
+        (e = cudaMalloc(&f->d_cseg, sizeof(unsigned short) * std::max<size_t>(cseg.size(), 1))) != cudaSuccess ||
+        (!cseg.empty() && (e = cudaMemcpy(f->d_cseg, cseg.data(), sizeof(unsigned short) * cseg.size(),
+                                          cudaMemcpyHostToDevice)) != cudaSuccess)) {
         err = std::string("fused phases: ") + cudaGetErrorString(e);
         return FFTSO3_ERR_CUDA;
     }
@@ -2161,7 +2177,7 @@ int tc_fused_forward(TCFused* f, const void* grid, void* coeffs, cudaStream_t st
     int rc = tc_fused_gemm(f, true, st, T, err);
     if (rc) return rc;
     T->begin(ST_CONVERT, st);
-    TCK(launch_fused_group_to_packed(f->d_bseg, f->nbseg, f->ncblk, f->real, coeffs, st));
+    TCK(launch_fused_group_to_packed(f->d_bseg, f->d_cseg, f->ncblk, f->real, coeffs, st));
     T->end(st);
     return FFTSO3_SUCCESS;
 }
@@ -2173,7 +2189,7 @@ int tc_fused_inverse(TCFused* f, const void* coeffs, void* grid, cudaStream_t st
         return FFTSO3_ERR_CUDA;
     }
     T->begin(ST_CONVERT, st);
-    TCK(launch_fused_packed_to_group(f->d_bseg, f->nbseg, f->ncblk, f->real, coeffs, st));
+    TCK(launch_fused_packed_to_group(f->d_bseg, f->d_cseg, f->ncblk, f->real, coeffs, st));
     T->end(st);
     int rc = tc_fused_gemm(f, false, st, T, err);
     if (rc) return rc;

@@ -45,6 +45,10 @@ template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
 // multiply by -i
 template <typename C> __device__ __forceinline__ C mul_mi(C a) { C r; r.x = a.y; r.y = -a.x; return r; }
 
+// Position of element i of a staged line: plain, or (PAD) one padding slot after every 8 elements, so that the
+// stride-R writes of a Stockham stage (and the other strided walks) spread over the shared-memory banks.
+template <bool PAD> __device__ __forceinline__ int lpos(int i) { return PAD ? i + (i >> 3) : i; }
+
 template <typename T, int R>
 __device__ __forceinline__ void dft_small(typename V2<T>::t* v, const typename V2<T>::t* w, int Nr)
 {
@@ -114,7 +118,7 @@ __device__ __forceinline__ void dft_small(typename V2<T>::t* v, const typename V
 // items b = threadIdx.x + i blockDim.x map to (line l, butterfly j) and the
 // twiddle class k = j mod Ns; they advance by constant steps (Nr is a
 // multiple of Ns, so k survives the wrap of j), so the loop does no division.
-template <typename T, int R>
+template <typename T, int R, bool PAD = false>
 __device__ __forceinline__ void stockham_stage(const typename V2<T>::t* __restrict__ src,
                                                typename V2<T>::t* __restrict__ dst,
                                                const typename V2<T>::t* __restrict__ w,
@@ -131,16 +135,17 @@ __device__ __forceinline__ void stockham_stage(const typename V2<T>::t* __restri
         const C* s = src + l * LS;
         C v[R];
 #pragma unroll
-        for (int t = 0; t < R; ++t) v[t] = s[j + t * Nr];
+        for (int t = 0; t < R; ++t) v[t] = s[lpos<PAD>(j + t * Nr)];
         if (Ns > 1) {
             int e = k * tstride;
 #pragma unroll
             for (int t = 1; t < R; ++t) v[t] = cmul(v[t], w[t * e]);
         }
         dft_small<T, R>(v, w, Nr);
-        C* d = dst + l * LS + (j - k) * R + k;
+        C* d = dst + l * LS;
+        const int o = (j - k) * R + k;
 #pragma unroll
-        for (int t = 0; t < R; ++t) d[t * Ns] = v[t];
+        for (int t = 0; t < R; ++t) d[lpos<PAD>(o + t * Ns)] = v[t];
         l += linc;
         j += jinc;
         k += kinc;
@@ -157,7 +162,7 @@ __device__ __forceinline__ void stockham_stage(const typename V2<T>::t* __restri
 // t (k tstride + q Nr) mod N, advances by one add and one conditional
 // subtract per term (no division in the inner loop).  Terms are summed in
 // ascending t, the plain DFT order.
-template <typename T>
+template <typename T, bool PAD = false>
 __device__ void stockham_generic(const typename V2<T>::t* __restrict__ src, typename V2<T>::t* __restrict__ dst,
                                  const typename V2<T>::t* __restrict__ w, int N, int Ns, int R, int lpb, int LS)
 {
@@ -175,7 +180,7 @@ __device__ void stockham_generic(const typename V2<T>::t* __restrict__ src, type
         const C* s = src + l * LS;
         C acc[GQ];
         int e[GQ], step[GQ];
-        const C x0 = s[j];
+        const C x0 = s[lpos<PAD>(j)];
 #pragma unroll
         for (int u = 0; u < GQ; ++u) {
             acc[u] = x0;
@@ -185,7 +190,7 @@ __device__ void stockham_generic(const typename V2<T>::t* __restrict__ src, type
             e[u] = st;
         }
         for (int t = 1; t < R; ++t) {
-            const C v = s[j + t * Nr];
+            const C v = s[lpos<PAD>(j + t * Nr)];
 #pragma unroll
             for (int u = 0; u < GQ; ++u) {
                 acc[u] = cadd(acc[u], cmul(v, w[e[u]]));
@@ -193,11 +198,12 @@ __device__ void stockham_generic(const typename V2<T>::t* __restrict__ src, type
                 e[u] = ne >= N ? ne - N : ne;
             }
         }
-        C* d = dst + l * LS + (j - k) * R + k;
+        C* d = dst + l * LS;
+        const int o = (j - k) * R + k;
 #pragma unroll
         for (int u = 0; u < GQ; ++u) {
             const int q = qb * GQ + u;
-            if (q < R) d[q * Ns] = acc[u];
+            if (q < R) d[lpos<PAD>(o + q * Ns)] = acc[u];
         }
     }
 }
@@ -213,16 +219,15 @@ __device__ void stockham_generic(const typename V2<T>::t* __restrict__ src, type
 // LPT lines (l and l + lpb/2 when lpb >= 2), so one matrix read feeds
 // 4 LPT FMAs; work items run (j, line) fastest, so the lanes of a warp share
 // one block of q and every matrix read is a broadcast.
-template <typename T, int LPT>
+template <typename T, int LPT, int GP = 4, bool PAD = false>
 __device__ void dft_prime_first_t(const typename V2<T>::t* __restrict__ src, typename V2<T>::t* __restrict__ dst,
                                   const typename V2<T>::t* __restrict__ mat, int N, int R, int lpb, int LS)
 {
     using C = typename V2<T>::t;
-    constexpr int GP = 4;
     const int Nr = N / R;
     const int P = (R - 1) / 2;
-    const int P4 = (P + GP - 1) / GP * GP;
-    const int nblk = P4 / GP;
+    const int MS = (P + 3) / 4 * 4;             // row stride of the matrix (as built: a multiple of 4)
+    const int nblk = (P + GP - 1) / GP;
     const int lgroups = lpb / LPT;               // line l and l + lgroups share each matrix read
     const int per_blk = Nr * lgroups;
     const int total = per_blk * nblk;
@@ -233,8 +238,8 @@ __device__ void dft_prime_first_t(const typename V2<T>::t* __restrict__ src, typ
         C x0[LPT], acc0[LPT], Cs[LPT][GP], Ss[LPT][GP];
 #pragma unroll
         for (int u = 0; u < LPT; ++u) {
-            s[u] = src + (l + u * lgroups) * LS + j;
-            x0[u] = s[u][0];
+            s[u] = src + (l + u * lgroups) * LS;
+            x0[u] = s[u][lpos<PAD>(j)];
             acc0[u] = x0[u];
 #pragma unroll
             for (int g = 0; g < GP; ++g) {
@@ -243,11 +248,11 @@ __device__ void dft_prime_first_t(const typename V2<T>::t* __restrict__ src, typ
             }
         }
         const C* m = mat + blk * GP;
-        for (int t = 1; t <= P; ++t, m += P4) {
+        for (int t = 1; t <= P; ++t, m += MS) {
             C a[LPT], bb[LPT];
 #pragma unroll
             for (int u = 0; u < LPT; ++u) {
-                const C xt = s[u][t * Nr], xr = s[u][(R - t) * Nr];
+                const C xt = s[u][lpos<PAD>(j + t * Nr)], xr = s[u][lpos<PAD>(j + (R - t) * Nr)];
                 a[u] = cadd(xt, xr);
                 bb[u] = csub(xt, xr);
                 acc0[u] = cadd(acc0[u], a[u]);
@@ -266,15 +271,16 @@ __device__ void dft_prime_first_t(const typename V2<T>::t* __restrict__ src, typ
         }
 #pragma unroll
         for (int u = 0; u < LPT; ++u) {
-            C* d = dst + (l + u * lgroups) * LS + j * R;
-            if (blk == 0) d[0] = acc0[u];
+            C* d = dst + (l + u * lgroups) * LS;
+            const int o = j * R;
+            if (blk == 0) d[lpos<PAD>(o)] = acc0[u];
 #pragma unroll
             for (int g = 0; g < GP; ++g) {
                 const int q = 1 + blk * GP + g;
                 if (q <= P) {
                     const C base = cadd(x0[u], Cs[u][g]);
-                    d[q] = V2<T>::mk(base.x + Ss[u][g].y, base.y - Ss[u][g].x);
-                    d[R - q] = V2<T>::mk(base.x - Ss[u][g].y, base.y + Ss[u][g].x);
+                    d[lpos<PAD>(o + q)] = V2<T>::mk(base.x + Ss[u][g].y, base.y - Ss[u][g].x);
+                    d[lpos<PAD>(o + R - q)] = V2<T>::mk(base.x - Ss[u][g].y, base.y + Ss[u][g].x);
                 }
             }
         }
@@ -614,15 +620,17 @@ __device__ float2* run_line_stages(float2* src, float2* dst, const float2* w, co
     for (int s = 0; s < ns; ++s) {
         const int R = fac.r[s];
         switch (R) {
-            case 2: stockham_stage<float, 2>(src, dst, w, N, Ns, nl, LS); break;
-            case 3: stockham_stage<float, 3>(src, dst, w, N, Ns, nl, LS); break;
-            case 4: stockham_stage<float, 4>(src, dst, w, N, Ns, nl, LS); break;
-            case 5: stockham_stage<float, 5>(src, dst, w, N, Ns, nl, LS); break;
-            case 7: stockham_stage<float, 7>(src, dst, w, N, Ns, nl, LS); break;
-            case 8: stockham_stage<float, 8>(src, dst, w, N, Ns, nl, LS); break;
+            case 2: stockham_stage<float, 2, true>(src, dst, w, N, Ns, nl, LS); break;
+            case 3: stockham_stage<float, 3, true>(src, dst, w, N, Ns, nl, LS); break;
+            case 4: stockham_stage<float, 4, true>(src, dst, w, N, Ns, nl, LS); break;
+            case 5: stockham_stage<float, 5, true>(src, dst, w, N, Ns, nl, LS); break;
+            case 7: stockham_stage<float, 7, true>(src, dst, w, N, Ns, nl, LS); break;
+            case 8: stockham_stage<float, 8, true>(src, dst, w, N, Ns, nl, LS); break;
             default:
-                if (Ns == 1) dft_prime_first<float>(src, dst, mat, N, R, nl, LS);
-                else stockham_generic<float>(src, dst, w, N, Ns, R, nl, LS);
+                // prime first stage: two outputs q per work item, so the few lines of a group still give
+                // every thread a (line pair, j, q block) item
+                if (Ns == 1) dft_prime_first_t<float, 2, 2, true>(src, dst, mat, N, R, nl, LS);
+                else stockham_generic<float, true>(src, dst, w, N, Ns, R, nl, LS);
                 break;
         }
         __syncthreads();
@@ -650,7 +658,7 @@ size_t slice_fft_smem_bytes(int N, int spc, bool real)
     const size_t sst = (size_t)N * slice_row_stride(N, real) + 1;
     const size_t G = (size_t)slice_lines_per_group(N);
     const size_t tb = (size_t)slice_table_entries(N, spc);
-    return sizeof(float2) * (spc * sst + 2 * G * (N + 1) + N + slice_prime_entries(f)) + tb * (8 + 8 + 4);
+    return sizeof(float2) * (spc * sst + 2 * G * slice_line_stride(N) + N + slice_prime_entries(f)) + tb * (8 + 8 + 4);
 }
 
 // Every element walk below advances its indices by constant steps (one division per walk, none per element).
@@ -673,7 +681,7 @@ __global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const Bucke
     }
     __syncthreads();
     const BucketSeg& S = segs[sb];
-    const int N = S.N, B = N / 2, LS = N + 1, G = S.G, spc = S.spc;
+    const int N = S.N, B = N / 2, LS = slice_line_stride(N), G = S.G, spc = S.spc;
     const int RS = slice_row_stride(N, REAL), NC = REAL ? B + 1 : N;
     const int SSt = N * RS + 1;
     const long long NN = (long long)N * N, NNN = NN * N;
@@ -739,12 +747,13 @@ __global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const Bucke
             __syncthreads();
             {
                 int l = tid / N, j = tid - l * N;
+#pragma unroll 4
                 for (int e = tid; e < nl * N; e += T) {
                     if (REAL) {
                         const float* g = reinterpret_cast<const float*>(in) + lg[l] + j;
-                        A[l * LS + j] = make_float2(g[0], g[N]);
+                        A[l * LS + lpos<true>(j)] = make_float2(g[0], g[N]);
                     } else {
-                        A[l * LS + j] = reinterpret_cast<const float2*>(in)[lg[l] + j];
+                        A[l * LS + lpos<true>(j)] = reinterpret_cast<const float2*>(in)[lg[l] + j];
                     }
                     j += rj;
                     l += rl;
@@ -758,11 +767,11 @@ __global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const Bucke
                 for (int e = tid; e < nl * NC; e += T) {
                     float2* x = X + lx[l];
                     if (REAL) {
-                        const float2 z = res[l * LS + q], zm = res[l * LS + (q == 0 ? 0 : N - q)];
+                        const float2 z = res[l * LS + lpos<true>(q)], zm = res[l * LS + lpos<true>(q == 0 ? 0 : N - q)];
                         x[q] = make_float2(0.5f * (z.x + zm.x), 0.5f * (z.y - zm.y));
                         x[RS + q] = make_float2(0.5f * (z.y + zm.y), -0.5f * (z.x - zm.x));
                     } else {
-                        x[q] = res[l * LS + q];
+                        x[q] = res[l * LS + lpos<true>(q)];
                     }
                     q += cq;
                     l += cl;
@@ -781,7 +790,7 @@ __global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const Bucke
             {
                 int j = tid / nl, l = tid - j * nl;
                 for (int e = tid; e < nl * N; e += T) {
-                    A[l * LS + j] = X[lx[l] + j * RS];
+                    A[l * LS + lpos<true>(j)] = X[lx[l] + j * RS];
                     l += gl;
                     j += gj;
                     if (l >= nl) { l -= nl; ++j; }
@@ -792,7 +801,7 @@ __global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const Bucke
             {
                 int p = tid / nl, l = tid - p * nl;
                 for (int e = tid; e < nl * N; e += T) {
-                    const float2 v = res[l * LS + p];
+                    const float2 v = res[l * LS + lpos<true>(p)];
                     Pout[lg[l] + p * NN] = v;
                     if (REAL && lm[l] >= 0) Pout[lm[l] + (p == 0 ? 0 : N - p) * NN] = make_float2(v.x, -v.y);
                     l += gl;
@@ -812,6 +821,7 @@ __global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const Bucke
         {
             const int sinc = T % ns, pqinc = T / ns, qinc = pqinc % NC, pinc = pqinc / NC;
             int s = tid % ns, q = (tid / ns) % NC, p = (tid / ns) / NC;
+#pragma unroll 4
             for (int e = tid; e < ns * N * NC; e += T) {
                 float2 v = make_float2(0.f, 0.f);
                 if (p != B && q != B) {
@@ -842,7 +852,7 @@ __global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const Bucke
             {
                 int j = tid / nl, l = tid - j * nl;
                 for (int e = tid; e < nl * N; e += T) {
-                    A[l * LS + j] = X[lx[l] + j * RS];
+                    A[l * LS + lpos<true>(j)] = X[lx[l] + j * RS];
                     l += gl;
                     j += gj;
                     if (l >= nl) { l -= nl; ++j; }
@@ -853,7 +863,7 @@ __global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const Bucke
             {
                 int j = tid / nl, l = tid - j * nl;
                 for (int e = tid; e < nl * N; e += T) {
-                    X[lx[l] + j * RS] = res[l * LS + j];
+                    X[lx[l] + j * RS] = res[l * LS + lpos<true>(j)];
                     l += gl;
                     j += gj;
                     if (l >= nl) { l -= nl; ++j; }
@@ -882,9 +892,9 @@ __global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const Bucke
                             ya.y = -ya.y;
                             yb.y = -yb.y;
                         }
-                        A[l * LS + j] = make_float2(ya.x - yb.y, ya.y + yb.x);
+                        A[l * LS + lpos<true>(j)] = make_float2(ya.x - yb.y, ya.y + yb.x);
                     } else {
-                        A[l * LS + j] = x[j];
+                        A[l * LS + lpos<true>(j)] = x[j];
                     }
                     j += rj;
                     l += rl;
@@ -896,7 +906,7 @@ __global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const Bucke
             {
                 int l = tid / N, j = tid - l * N;
                 for (int e = tid; e < nl * N; e += T) {
-                    const float2 v = res[l * LS + j];
+                    const float2 v = res[l * LS + lpos<true>(j)];
                     if (REAL) {
                         float* g = reinterpret_cast<float*>(out) + lg[l] + j;
                         g[0] = v.x;

@@ -32,7 +32,14 @@ constexpr int SLICE_LINE_ELEMS = 2048;  // elements of each of the two Stockham 
 // half-spectrum), odd so that column walks meet distinct banks, and the shared memory one CTA of the slice
 // FFT needs for spc slices of size N.
 __host__ __device__ inline int slice_row_stride(int N, bool real) { return real ? ((N / 2 + 1) | 1) : N + 1; }
-__host__ __device__ inline int slice_lines_per_group(int N) { return (SLICE_LINE_ELEMS / (N + 1)) & ~1; }
+// Stockham line buffers: lines of N elements padded by one slot per 8 (odd stride), groups of an even number
+// of lines within SLICE_LINE_ELEMS
+__host__ __device__ inline int slice_line_stride(int N) { return (N + (N >> 3) + 1) | 1; }
+__host__ __device__ inline int slice_lines_per_group(int N)
+{
+    const int g = (SLICE_LINE_ELEMS / slice_line_stride(N)) & ~1;
+    return g < 2 ? 2 : g;
+}
 size_t slice_fft_smem_bytes(int N, int spc, bool real);
 
 // Both FFT passes of the beta slices of every bucket in one launch (nblk CTAs, smem bytes of dynamic shared
@@ -42,13 +49,13 @@ cudaError_t launch_slice_fft(const BucketSeg* segs, int nseg, long long nblk, si
                              const void* in, void* out, cudaStream_t st);
 
 // Coefficient conversions of every bucket in one launch (CONVERT_THREADS coefficients of one bucket per CTA,
-// nblk CTAs in total):
+// nblk CTAs in total, CTA i serving bucket segs[cseg[i]]; l_max <= 255):
 //   forward: group-major GEMM output -> packed coefficients (complex64, or the real basis in float32);
 //   inverse: packed coefficients (complex64 / real float32) -> group-major (2l + 1) sign F.
 constexpr int CONVERT_THREADS = 256;
-cudaError_t launch_fused_group_to_packed(const BucketSeg* segs, int nseg, long long nblk, bool real, void* out,
-                                         cudaStream_t st);
-cudaError_t launch_fused_packed_to_group(const BucketSeg* segs, int nseg, long long nblk, bool real, const void* in,
-                                         cudaStream_t st);
+cudaError_t launch_fused_group_to_packed(const BucketSeg* segs, const unsigned short* cseg, long long nblk,
+                                         bool real, void* out, cudaStream_t st);
+cudaError_t launch_fused_packed_to_group(const BucketSeg* segs, const unsigned short* cseg, long long nblk,
+                                         bool real, const void* in, cudaStream_t st);
 
 }  // namespace fftso3

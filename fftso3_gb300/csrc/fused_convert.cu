@@ -23,11 +23,11 @@ namespace {
 // g = m0^2 + m0 + n0, pairs of group_pairs(), rows l = m0..L): the groups of one m0 >= 1 hold 8 m0 runs of
 // B - m0 rows -- n0 = -m0 (2 pairs), -m0 < n0 < m0 (4 pairs each), n0 = m0 (2 pairs) -- after the single run
 // of m0 = 0.
-__device__ __forceinline__ long long block_start(int m0, int B)
+__device__ __forceinline__ int block_start(int m0, int B)  // < 2^31 for B <= 256
 {
     if (m0 == 0) return 0;
-    const long long a = m0 - 1, b = m0;
-    return B + 8 * ((long long)B * (a * b / 2) - a * b * (2 * b - 1) / 6);
+    const int ab = (m0 - 1) * m0;
+    return B + 8 * (B * (ab / 2) - ab * (2 * m0 - 1) / 6);
 }
 
 __device__ __forceinline__ int run_index(int m0, int n0, int pp)
@@ -48,47 +48,32 @@ __device__ __forceinline__ long long gm_offset(int l, int m, int n, int B)
     return block_start(m0, B) + (long long)run_index(m0, n0, pp) * (B - m0) + (l - m0);
 }
 
-// largest l with so3_off(l) <= r
-__device__ __forceinline__ int degree_of(long long r)
+// largest l with l (4 l^2 - 1) / 3 <= r (the packed offset of degree l; < 2^31 for l <= 256)
+__device__ __forceinline__ int off32(int l) { return l * (4 * l * l - 1) / 3; }
+__device__ __forceinline__ int degree_of(int r)
 {
     int l = (int)cbrtf(0.75f * (float)r);
-    while (l > 0 && so3_off(l) > r) --l;
-    while (so3_off(l + 1) <= r) ++l;
+    while (l > 0 && off32(l) > r) --l;
+    while (off32(l + 1) <= r) ++l;
     return l;
 }
 
-// the CTA's bucket (thread 0 searches the table once)
-__device__ __forceinline__ const BucketSeg& cta_bucket(const BucketSeg* __restrict__ segs, int nseg, int* sb)
-{
-    if (threadIdx.x == 0) {
-        const long long blk = blockIdx.x;
-        int lo = 0, hi = nseg - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (segs[mid].cblk0 <= blk) lo = mid;
-            else hi = mid - 1;
-        }
-        *sb = lo;
-    }
-    __syncthreads();
-    return segs[*sb];
-}
 
 template <bool REAL>
 __global__ void __launch_bounds__(CONVERT_THREADS) fused_group_to_packed_kernel(const BucketSeg* __restrict__ segs,
-                                                                                int nseg, void* __restrict__ out)
+                                                                                const unsigned short* __restrict__ cseg,
+                                                                                void* __restrict__ out)
 {
-    __shared__ int sb;
-    const BucketSeg& S = cta_bucket(segs, nseg, &sb);
+    const BucketSeg& S = segs[cseg[blockIdx.x]];
     const int B = S.B;
-    const long long C = so3_off(B);
+    const int C = (int)so3_off(B);
     const long long u = (blockIdx.x - S.cblk0) * (long long)CONVERT_THREADS + threadIdx.x;
     if (u >= (long long)S.batch * C) return;
-    const long long f = u / C, r = u - f * C;
+    const int f = (int)(u / C), r = (int)(u - (long long)f * C);
     const int l = degree_of(r);
-    const int W = 2 * l + 1, wi = (int)(r - so3_off(l));
+    const int W = 2 * l + 1, wi = r - off32(l);
     const int m = wi % W - l, n = wi / W - l;
-    const float2* __restrict__ fg = S.fg + f * C;
+    const float2* __restrict__ fg = S.fg + (long long)f * C;
     if (!REAL) {
         reinterpret_cast<float2*>(out)[S.c0 + u] = fg[gm_offset(l, m, n, B)];
         return;
@@ -110,15 +95,15 @@ __global__ void __launch_bounds__(CONVERT_THREADS) fused_group_to_packed_kernel(
 
 template <bool REAL>
 __global__ void __launch_bounds__(CONVERT_THREADS) fused_packed_to_group_kernel(const BucketSeg* __restrict__ segs,
-                                                                                int nseg, const void* __restrict__ in)
+                                                                                const unsigned short* __restrict__ cseg,
+                                                                                const void* __restrict__ in)
 {
-    __shared__ int sb;
-    const BucketSeg& S = cta_bucket(segs, nseg, &sb);
+    const BucketSeg& S = segs[cseg[blockIdx.x]];
     const int B = S.B;
-    const long long C = so3_off(B);
+    const int C = (int)so3_off(B);
     const long long u = (blockIdx.x - S.cblk0) * (long long)CONVERT_THREADS + threadIdx.x;
     if (u >= (long long)S.batch * C) return;
-    const long long f = u / C, e = u - f * C;
+    const int f = (int)(u / C), e = (int)(u - (long long)f * C);
     int lo = 0, hi = B - 1;  // m0: the block holding e
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
@@ -126,7 +111,7 @@ __global__ void __launch_bounds__(CONVERT_THREADS) fused_packed_to_group_kernel(
         else hi = mid - 1;
     }
     const int m0 = lo, nl = B - m0;
-    const int rel = (int)(e - block_start(m0, B)), ri = rel / nl, l = m0 + rel - ri * nl;
+    const int rel = e - block_start(m0, B), ri = rel / nl, l = m0 + rel - ri * nl;
     int n0, pp;
     if (m0 == 0) { n0 = 0; pp = 0; }
     else if (ri < 2) { n0 = -m0; pp = ri; }
@@ -139,9 +124,9 @@ __global__ void __launch_bounds__(CONVERT_THREADS) fused_packed_to_group_kernel(
     const int psign = (pp == 1 || pp == 2) ? sgn : 1;
     float2 v;
     if (!REAL) {
-        v = reinterpret_cast<const float2*>(in)[S.c0 + f * C + so3_idx(l, m, n)];
+        v = reinterpret_cast<const float2*>(in)[S.c0 + (long long)f * C + so3_idx(l, m, n)];
     } else {
-        const float* __restrict__ fr = reinterpret_cast<const float*>(in) + S.c0 + f * C;
+        const float* __restrict__ fr = reinterpret_cast<const float*>(in) + S.c0 + (long long)f * C;
         const int am[2] = {m, -m}, bn[2] = {n, -n};
         const int na = (m == 0) ? 1 : 2, nb = (n == 0) ? 1 : 2;
         float x[2][2];
@@ -157,32 +142,32 @@ __global__ void __launch_bounds__(CONVERT_THREADS) fused_packed_to_group_kernel(
         v = make_float2(acc.x, acc.y);
     }
     const float sc = (float)(2 * l + 1) * (float)psign;
-    S.fg[f * C + e] = make_float2(sc * v.x, sc * v.y);
+    S.fg[(long long)f * C + e] = make_float2(sc * v.x, sc * v.y);
 }
 
 }  // namespace
 
-cudaError_t launch_fused_group_to_packed(const BucketSeg* segs, int nseg, long long nblk, bool real, void* out,
-                                         cudaStream_t st)
+cudaError_t launch_fused_group_to_packed(const BucketSeg* segs, const unsigned short* cseg, long long nblk,
+                                         bool real, void* out, cudaStream_t st)
 {
     if (nblk <= 0) return cudaSuccess;
-    if (nblk > 0x7fffffffLL || nseg <= 0) return cudaErrorInvalidValue;
+    if (nblk > 0x7fffffffLL) return cudaErrorInvalidValue;
     if (real)
-        fused_group_to_packed_kernel<true><<<(unsigned)nblk, CONVERT_THREADS, 0, st>>>(segs, nseg, out);
+        fused_group_to_packed_kernel<true><<<(unsigned)nblk, CONVERT_THREADS, 0, st>>>(segs, cseg, out);
     else
-        fused_group_to_packed_kernel<false><<<(unsigned)nblk, CONVERT_THREADS, 0, st>>>(segs, nseg, out);
+        fused_group_to_packed_kernel<false><<<(unsigned)nblk, CONVERT_THREADS, 0, st>>>(segs, cseg, out);
     return cudaGetLastError();
 }
 
-cudaError_t launch_fused_packed_to_group(const BucketSeg* segs, int nseg, long long nblk, bool real, const void* in,
-                                         cudaStream_t st)
+cudaError_t launch_fused_packed_to_group(const BucketSeg* segs, const unsigned short* cseg, long long nblk,
+                                         bool real, const void* in, cudaStream_t st)
 {
     if (nblk <= 0) return cudaSuccess;
-    if (nblk > 0x7fffffffLL || nseg <= 0) return cudaErrorInvalidValue;
+    if (nblk > 0x7fffffffLL) return cudaErrorInvalidValue;
     if (real)
-        fused_packed_to_group_kernel<true><<<(unsigned)nblk, CONVERT_THREADS, 0, st>>>(segs, nseg, in);
+        fused_packed_to_group_kernel<true><<<(unsigned)nblk, CONVERT_THREADS, 0, st>>>(segs, cseg, in);
     else
-        fused_packed_to_group_kernel<false><<<(unsigned)nblk, CONVERT_THREADS, 0, st>>>(segs, nseg, in);
+        fused_packed_to_group_kernel<false><<<(unsigned)nblk, CONVERT_THREADS, 0, st>>>(segs, cseg, in);
     return cudaGetLastError();
 }
 

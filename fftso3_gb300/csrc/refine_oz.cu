@@ -399,6 +399,18 @@ __global__ void __launch_bounds__(THREADS, 1)
                     if (f >= a.batch || k >= N) continue;
                     const long long fo = (long long)f * a.fstride + k;
                     const signed char* eyf = a.ey + ((long long)f * a.ngroups + item.x) * 4;
+                    // spectral residual: the function's four pair values, loads in flight together
+                    float2 sh[4], sl[4];
+                    if (spectral) {
+#pragma unroll
+                        for (int p = 0; p < 4; ++p) {
+                            sh[p] = sl[p] = make_float2(0.f, 0.f);
+                            if (p < P.np) {
+                                sh[p] = __ldcs(a.rhi + fo + poff[p]);
+                                sl[p] = __ldcs(a.rlo + fo + poff[p]);
+                            }
+                        }
+                    }
 #pragma unroll
                     for (int p = 0; p < 4; ++p) {
                         if (p >= P.np) break;
@@ -411,10 +423,10 @@ __global__ void __launch_bounds__(THREADS, 1)
                         if (spectral) {
                             // N^2 H = FFT of the synthesised grid; hi - N^2 H.h is exact (close values)
                             const int E2 = E + a.e2n;
-                            const long long i = fo + poff[p];
-                            const float2 h = a.rhi[i], l = a.rlo[i];
-                            a.rhi[i] = make_float2((h.x - ldexpf(re.h, E2)) + (l.x - ldexpf(re.l, E2)),
-                                                   (h.y - ldexpf(im.h, E2)) + (l.y - ldexpf(im.l, E2)));
+                            const float2 h = sh[p], l = sl[p];
+                            __stcs(a.rhi + fo + poff[p],
+                                   make_float2((h.x - ldexpf(re.h, E2)) + (l.x - ldexpf(re.l, E2)),
+                                               (h.y - ldexpf(im.h, E2)) + (l.y - ldexpf(im.l, E2))));
                         } else {
                             a.pout[fo + poff[p]] =
                                 make_float4(ldexpf(re.h, E), ldexpf(re.l, E), ldexpf(im.h, E), ldexpf(im.l, E));
