@@ -452,36 +452,32 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(const TIN* __restrict__ 
     }
 }
 
-// ---- double-float FFT along a strided axis of k-contiguous arrays (the refinement's grid synthesis)
+// ---- double-float FFT along a strided axis of k-contiguous arrays (the refinement's forward FFT)
 //
 // Line (o, k): element j at obase(o) + k + j S, obase(o) = (o / oinner) oouter + (o % oinner) oistride.  One CTA
-// transforms TK = 2048 / N consecutive k of one o (N = 64..512, a power of two) with 256 threads: TK lines of N
-// elements staged in shared memory (global accesses run k-fastest: TK consecutive elements per j), then radix-8
+// transforms TK = 2048 / N consecutive k of one o (N = 64..512, a power of two) with 256 threads: radix-8
 // Stockham stages (a last radix-4 or 2 stage when log2 N is not a multiple of 3), each thread holding the 8
-// values of one butterfly in registers; stages run in place, a barrier between the reads and the writes.
-// Shared-memory layout, so that every access of a warp fills whole 16-byte bank groups:
+// values of one butterfly in registers.  The first stage reads its butterflies straight from global memory and
+// the last one writes them straight back, with the threads of a warp on consecutive k (TK consecutive elements
+// per j); the stages in between exchange through shared memory with the threads of a line side by side.
+// Shared-memory layout, so that the accesses of a warp fill whole 16-byte bank groups:
 //   rows padded by one element per 8 (phys(i) = i + i / 8): a stage's strided reads and scattered writes;
-//   row stride N + N / 8 + 1 elements (one extra 16-byte slot): the TK rows of the load / store phases;
+//   row stride N + N / 8 + 1 elements (+ 2 at N = 512, four rows per CTA): the k-fastest first / last stages;
 //   twiddles per stage as [r - 1][kt] (kt = butterfly index mod Ns): consecutive lanes, consecutive entries.
-// Grid-row forms, for lines o = (fn, j1) along j2 (S = N, oinner = N, oouter = N^3, oistride = N^2), whose TK
-// lines are TK rows of a grid [fn][k][j1][j2] (index rbase + kk N^2 + j):
-//   LOAD 1 / 2 (complex / real FP32 samples f): the lines are read from the grid rows instead of buf (the first
-//     pass of the double-float forward FFT; the store then writes buf [fn][j1][q][k]);
-//   STORE 1 / 2: the store forms the residual r = (f - g.h) - g.l (FP32; real samples: against the real part)
-//     at the samples' places instead of writing the lines back (fin may be r: each element is read, then
-//     written, by one thread).
-// STORE 3: the lines are written, renormalised, as two complex64 arrays at buf's index: hi (the FP32 rounding)
-// and lo (the remainder).
+// LOAD 1 / 2: the first pass of the forward FFT of sample grids [fn][k][j1][j2] (complex64 / float32), lines
+// o = (fn, j1) along j2 (S = N, oinner = N, oouter = N^3, oistride = N^2): the TK lines are TK grid rows (index
+// rbase + kk N^2 + j), staged through shared memory with row-contiguous reads.
+// STORE 3: the lines are written renormalised as two complex64 arrays at buf's index: hi (the FP32 rounding) and
+// lo (the remainder).
 template <int N, int LOAD, int STORE>
 __global__ void __launch_bounds__(256, 3) fft_df32_k_kernel(dfc32* __restrict__ buf, long long S, long long oinner,
                                                              long long oouter, long long oistride,
                                                              const double2* __restrict__ twg, const void* fin,
-                                                             float* r, float2* __restrict__ hi,
-                                                             float2* __restrict__ lo)
+                                                             float2* __restrict__ hi, float2* __restrict__ lo)
 {
     constexpr int TK = 2048 / N;         // lines per CTA
     constexpr int TPL = N / 8;           // threads per line
-    constexpr int ROW = N + N / 8 + 1;   // padded row length
+    constexpr int ROW = N + N / 8 + (N == 512 ? 2 : 1);
     __shared__ dfc32 sm[TK * ROW];
     __shared__ dfc32 w[N];               // stage twiddle tables (at most N - 8 entries)
     auto phys = [](int i) { return i + (i >> 3); };
@@ -501,102 +497,88 @@ __global__ void __launch_bounds__(256, 3) fft_df32_k_kernel(dfc32* __restrict__ 
             off += (R - 1) * Ns;
         }
     }
-    constexpr long long NN = (long long)N * N;
-    const long long rbase = (o / oinner) * NN * N + (o % oinner) * N + (long long)blockIdx.x * TK * NN;
+    const int kq = tid % TK, tq = tid / TK;  // k-fastest thread of the first / last stage
+    const int kk = tid / TPL, t = tid % TPL;  // line-major thread of the middle stages
+    dfc32 v[8];
     if constexpr (LOAD == 0) {
 #pragma unroll
-        for (int u = 0; u < N * TK / 256; ++u) {
-            const int e = tid + 256 * u, kk = e % TK, j = e / TK;
-            sm[kk * ROW + phys(j)] = buf[obase + (long long)j * S + kk];
-        }
+        for (int r = 0; r < 8; ++r) v[r] = buf[obase + (long long)(tq + r * (N / 8)) * S + kq];
     } else {
+        constexpr long long NN = (long long)N * N;
+        const long long rbase = (o / oinner) * NN * N + (o % oinner) * N + (long long)blockIdx.x * TK * NN;
 #pragma unroll
         for (int u = 0; u < N * TK / 256; ++u) {
             const int e = tid + 256 * u, kk2 = e / N, j = e % N;
             const long long i = rbase + kk2 * NN + j;
-            dfc32 v;
+            dfc32 x;
             if constexpr (LOAD == 2) {
-                v = dfc32{df32(reinterpret_cast<const float*>(fin)[i]), df32(0.f)};
+                x = dfc32{df32(reinterpret_cast<const float*>(fin)[i]), df32(0.f)};
             } else {
-                const float2 x = reinterpret_cast<const float2*>(fin)[i];
-                v = dfc32{df32(x.x), df32(x.y)};
+                const float2 y = reinterpret_cast<const float2*>(fin)[i];
+                x = dfc32{df32(y.x), df32(y.y)};
             }
-            sm[kk2 * ROW + phys(j)] = v;
+            sm[kk2 * ROW + phys(j)] = x;
         }
-    }
-    __syncthreads();
-    const int kk = tid / TPL, t = tid % TPL;
-    dfc32* line = sm + kk * ROW;
-    int Ns = 1, toff = 0;
+        __syncthreads();
 #pragma unroll
-    for (int s = 0; s < 3; ++s) {  // radix-8 stages while 8 Ns divides N
-        if (Ns * 8 > N) break;
-        const int kt = t % Ns;
-        dfc32 v[8];
+        for (int r = 0; r < 8; ++r) v[r] = sm[kq * ROW + phys(tq + r * (N / 8))];
+        __syncthreads();
+    }
+    // stage 0 (Ns = 1)
+    dft_small<df32, 8>(v, w, N / 8);
+#pragma unroll
+    for (int r = 0; r < 8; ++r) sm[kq * ROW + phys(tq * 8 + r)] = v[r];
+    __syncthreads();
+    auto store = [&](int j, const dfc32& x) {  // element j of line kq, from the last stage's registers
+        const long long i = obase + (long long)j * S + kq;
+        if constexpr (STORE == 3) {
+            const df32 a = df_two_sum(x.x.h, x.x.l), b = df_two_sum(x.y.h, x.y.l);
+            hi[i] = make_float2(a.h, b.h);
+            lo[i] = make_float2(a.l, b.l);
+        } else {
+            buf[i] = x;
+        }
+    };
+    // stage 1 (Ns = 8): the last stage at N = 64
+    if constexpr (N == 64) {
+        const int kt = tq % 8;
+#pragma unroll
+        for (int r = 0; r < 8; ++r) v[r] = sm[kq * ROW + phys(tq + r * 8)];
+#pragma unroll
+        for (int r = 1; r < 8; ++r) v[r] = cmul(v[r], w[(r - 1) * 8 + kt]);
+        dft_small<df32, 8>(v, w, 8);
+#pragma unroll
+        for (int r = 0; r < 8; ++r) store(tq + r * 8, v[r]);  // (tq - kt) 8 + kt + 8 r with tq < 8
+        return;
+    } else {
+        dfc32* line = sm + kk * ROW;
+        const int kt = t % 8;
 #pragma unroll
         for (int r = 0; r < 8; ++r) v[r] = line[phys(t + r * (N / 8))];
         __syncthreads();
-        if (Ns > 1) {
 #pragma unroll
-            for (int r = 1; r < 8; ++r) v[r] = cmul(v[r], w[toff + (r - 1) * Ns + kt]);
-            toff += 7 * Ns;
-        }
+        for (int r = 1; r < 8; ++r) v[r] = cmul(v[r], w[(r - 1) * 8 + kt]);
         dft_small<df32, 8>(v, w, N / 8);
 #pragma unroll
-        for (int r = 0; r < 8; ++r) line[phys((t - kt) * 8 + kt + r * Ns)] = v[r];
-        __syncthreads();
-        Ns *= 8;
-    }
-    if constexpr (N == 128 || N == 256) {  // one radix-2 or radix-4 stage: 8 / R butterflies per thread
-        constexpr int R = N == 256 ? 4 : 2;
-        constexpr int PER = 8 / R;
-        dfc32 v[PER][R];
-#pragma unroll
-        for (int b = 0; b < PER; ++b)
-#pragma unroll
-            for (int r = 0; r < R; ++r) v[b][r] = line[phys(t + b * TPL + r * (N / R))];
-        __syncthreads();
-#pragma unroll
-        for (int b = 0; b < PER; ++b) {
-            const int j = t + b * TPL, kt = j % Ns;
-#pragma unroll
-            for (int r = 1; r < R; ++r) v[b][r] = cmul(v[b][r], w[toff + (r - 1) * Ns + kt]);
-            dft_small<df32, R>(v[b], w, N / R);
-#pragma unroll
-            for (int r = 0; r < R; ++r) line[phys((j - kt) * R + kt + r * Ns)] = v[b][r];
-        }
+        for (int r = 0; r < 8; ++r) line[phys((t - kt) * 8 + kt + r * 8)] = v[r];
         __syncthreads();
     }
-    if constexpr (STORE == 0) {
+    // last stage (Ns = 64): radix 8 (N = 512), 4 (256) or 2 (128); outputs j + 64 r of butterfly j < 64
+    constexpr int R = N == 512 ? 8 : N == 256 ? 4 : 2;
+    constexpr int PER = 8 / R;
+    constexpr int BPL = N / R;  // butterflies per line (= 64)
+    dfc32* lq = sm + kq * ROW;
 #pragma unroll
-        for (int u = 0; u < N * TK / 256; ++u) {
-            const int e = tid + 256 * u, kk2 = e % TK, j = e / TK;
-            buf[obase + (long long)j * S + kk2] = sm[kk2 * ROW + phys(j)];
-        }
-    } else if constexpr (STORE == 3) {
+    for (int b = 0; b < PER; ++b) {
+        const int j = tq + b * (256 / TK);  // butterfly of line kq
+        dfc32 x[R];
 #pragma unroll
-        for (int u = 0; u < N * TK / 256; ++u) {
-            const int e = tid + 256 * u, kk2 = e % TK, j = e / TK;
-            const dfc32 v = sm[kk2 * ROW + phys(j)];
-            const df32 a = df_two_sum(v.x.h, v.x.l), b = df_two_sum(v.y.h, v.y.l);
-            const long long i = obase + (long long)j * S + kk2;
-            hi[i] = make_float2(a.h, b.h);
-            lo[i] = make_float2(a.l, b.l);
-        }
-    } else {
+        for (int r = 0; r < R; ++r) x[r] = lq[phys(j + r * BPL)];
 #pragma unroll
-        for (int u = 0; u < N * TK / 256; ++u) {
-            const int e = tid + 256 * u, kk2 = e / N, j = e % N;
-            const dfc32 v = sm[kk2 * ROW + phys(j)];
-            const long long i = rbase + kk2 * NN + j;
-            if constexpr (STORE == 2) {
-                r[i] = (reinterpret_cast<const float*>(fin)[i] - v.x.h) - v.x.l;
-            } else {
-                const float2 f = reinterpret_cast<const float2*>(fin)[i];
-                r[2 * i] = (f.x - v.x.h) - v.x.l;
-                r[2 * i + 1] = (f.y - v.y.h) - v.y.l;
-            }
-        }
+        for (int r = 1; r < R; ++r) x[r] = cmul(x[r], w[56 + (r - 1) * 64 + j]);
+        dft_small<df32, R>(x, w, BPL);
+#pragma unroll
+        for (int r = 0; r < R; ++r) store(j + r * 64, x[r]);
     }
 }
 
@@ -941,21 +923,21 @@ bool fft_df32_k_supported(int N) { return N == 64 || N == 128 || N == 256 || N =
 
 template <int LOAD, int STORE>
 static void df32_k_launch(int N, dim3 grid, dfc32* b, long long S, long long oinner, long long oouter,
-                          long long oistride, const double2* t, const void* fin, float* r, float2* hi, float2* lo,
+                          long long oistride, const double2* t, const void* fin, float2* hi, float2* lo,
                           cudaStream_t st)
 {
     switch (N) {
         case 64:
-            fft_df32_k_kernel<64, LOAD, STORE><<<grid, 256, 0, st>>>(b, S, oinner, oouter, oistride, t, fin, r, hi, lo);
+            fft_df32_k_kernel<64, LOAD, STORE><<<grid, 256, 0, st>>>(b, S, oinner, oouter, oistride, t, fin, hi, lo);
             break;
         case 128:
-            fft_df32_k_kernel<128, LOAD, STORE><<<grid, 256, 0, st>>>(b, S, oinner, oouter, oistride, t, fin, r, hi, lo);
+            fft_df32_k_kernel<128, LOAD, STORE><<<grid, 256, 0, st>>>(b, S, oinner, oouter, oistride, t, fin, hi, lo);
             break;
         case 256:
-            fft_df32_k_kernel<256, LOAD, STORE><<<grid, 256, 0, st>>>(b, S, oinner, oouter, oistride, t, fin, r, hi, lo);
+            fft_df32_k_kernel<256, LOAD, STORE><<<grid, 256, 0, st>>>(b, S, oinner, oouter, oistride, t, fin, hi, lo);
             break;
         default:
-            fft_df32_k_kernel<512, LOAD, STORE><<<grid, 256, 0, st>>>(b, S, oinner, oouter, oistride, t, fin, r, hi, lo);
+            fft_df32_k_kernel<512, LOAD, STORE><<<grid, 256, 0, st>>>(b, S, oinner, oouter, oistride, t, fin, hi, lo);
             break;
     }
 }
@@ -965,23 +947,8 @@ cudaError_t launch_fft_df32_k(void* buf, int N, long long S, long long nouter, l
 {
     if (!fft_df32_k_supported(N) || nouter < 1 || nouter > 65535 || oinner < 1) return cudaErrorInvalidValue;
     const dim3 grid((unsigned)(N / (2048 / N)), (unsigned)nouter);
-    dfc32* b = (dfc32*)buf;
-    const double2* t = (const double2*)tw;
-    df32_k_launch<0, 0>(N, grid, b, S, oinner, oouter, oistride, t, nullptr, nullptr, nullptr, nullptr, st);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_fft_df32_k_resid(const void* buf, int N, long long nb, const void* fin, bool real, float* r,
-                                    const void* tw, cudaStream_t st)
-{
-    if (!fft_df32_k_supported(N) || nb < 1 || nb * N > 65535) return cudaErrorInvalidValue;
-    const dim3 grid((unsigned)(N / (2048 / N)), (unsigned)(nb * N));
-    const long long NN = (long long)N * N;
-    const double2* t = (const double2*)tw;
-    if (real)
-        df32_k_launch<0, 2>(N, grid, (dfc32*)buf, N, N, NN * N, NN, t, fin, r, nullptr, nullptr, st);
-    else
-        df32_k_launch<0, 1>(N, grid, (dfc32*)buf, N, N, NN * N, NN, t, fin, r, nullptr, nullptr, st);
+    df32_k_launch<0, 0>(N, grid, (dfc32*)buf, S, oinner, oouter, oistride, (const double2*)tw, nullptr, nullptr,
+                        nullptr, st);
     return cudaGetLastError();
 }
 
@@ -995,13 +962,13 @@ cudaError_t launch_fft_df32_k_forward(void* buf, int N, long long nb, const void
     dfc32* b = (dfc32*)buf;
     // along j2, from the grid rows, into buf [fn][j1][q][k]
     if (real)
-        df32_k_launch<2, 0>(N, grid, b, N, N, NN * N, NN, t, f, nullptr, nullptr, nullptr, st);
+        df32_k_launch<2, 0>(N, grid, b, N, N, NN * N, NN, t, f, nullptr, nullptr, st);
     else
-        df32_k_launch<1, 0>(N, grid, b, N, N, NN * N, NN, t, f, nullptr, nullptr, nullptr, st);
+        df32_k_launch<1, 0>(N, grid, b, N, N, NN * N, NN, t, f, nullptr, nullptr, st);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     // along j1 (stride N^2), lines (fn, q), into the pencils [fn][p][q][k] as hi + lo
-    df32_k_launch<0, 3>(N, grid, b, NN, N, NN * N, N, t, nullptr, nullptr, hi, lo, st);
+    df32_k_launch<0, 3>(N, grid, b, NN, N, NN * N, N, t, nullptr, hi, lo, st);
     return cudaGetLastError();
 }
 

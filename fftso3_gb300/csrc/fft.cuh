@@ -39,11 +39,6 @@ cudaError_t launch_fft_lines(const FFTLaunch& L, cudaStream_t st);
 bool fft_df32_k_supported(int N);
 cudaError_t launch_fft_df32_k(void* buf, int N, long long S, long long nouter, long long oinner, long long oouter,
                               long long oistride, const void* tw, cudaStream_t st);
-// The transform along q (stride N) of nb double-float pencil grids [fn][p][q][k] (N^3 each) that forms the
-// residual r[fn][k][j1][j2] = f - g in its store phase instead of writing g back (FP32; real samples: against
-// the real part; fin may be r).  The lines along p must have been transformed before.
-cudaError_t launch_fft_df32_k_resid(const void* buf, int N, long long nb, const void* fin, bool real, float* r,
-                                    const void* tw, cudaStream_t st);
 // Double-float forward FFT of nb sample grids f [fn][k][j1][j2] (complex64, or float32 when real) into the
 // k-contiguous pencils [fn][p][q][k], written renormalised as hi (complex64, the FP32 rounding) + lo (the
 // remainder); buf: nb double-float grids of work space.

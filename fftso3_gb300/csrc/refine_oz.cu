@@ -25,11 +25,14 @@
 //  * the epilogue combines the four levels in double-float and scales by 2^E,
 //    giving H to about 2^-30 of its largest term (the dropped products
 //    i + j >= 4 and the digits below 2^-31), as double-float pencils.
-// A double-float FFT over (p, q) then gives the grid g, and the residual
-// r = f - g is formed against the FP32 samples in the same arithmetic (f is
-// exact there) and rounded to FP32 only as the small difference -- for
-// N = 64..512 in the store phase of the FFT's second pass, whose lines are
-// rows of the grid, so g is never written out.
+// Grid form (N not a power of two from 64 to 512): a double-float FFT over
+// (p, q) then gives the grid g, and the residual r = f - g is formed against
+// the FP32 samples in the same arithmetic (f is exact there) and rounded to
+// FP32 only as the small difference.  Spectral form (N = 64..512): the
+// samples' FFT in double-float (pencils hi + lo), and the epilogue writes
+// r^ = (hi + lo) - N^2 H at the forward pencil place of each (m, n) instead
+// of H -- the FFT of the synthesised grid is N^2 H -- so neither g nor an
+// FFT of the residual is formed.
 //
 // Kernel layout (one CTA per SM, persistent over (group, 128 k, 8 functions) items):
 //   warp 0     TMA of the four table digit planes (MN-major operand, 128-byte swizzle);
@@ -107,6 +110,8 @@ __device__ __forceinline__ void item_mn(const int4& it, int& m0, int& n0)
     m0 = it.w >> 16;
     n0 = (it.w & 0xFFFF) - 32768;
 }
+
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
 // 2^e as a float for e in [-126, 127] (exact)
 __device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + e) << 23); }
@@ -380,6 +385,21 @@ __global__ void __launch_bounds__(THREADS, 1)
                 poff[p] = ((long long)pi * N + qi) * N;
             }
             const int et = k < N ? (int)a.et[(long long)item.x * N + k] : 0;
+            if (spectral && k < N) {
+                // the FFT values this item will read, requested into L2 while its MMAs run
+#pragma unroll 1
+                for (int fl = 0; fl < FPT; ++fl) {
+                    const int f = item.z * FPT + fl;
+                    if (f >= a.batch) break;
+                    const long long fo = (long long)f * a.fstride + k;
+#pragma unroll
+                    for (int p = 0; p < 4; ++p) {
+                        if (p >= P.np) break;
+                        prefetch_l2(a.rhi + fo + poff[p]);
+                        prefetch_l2(a.rlo + fo + poff[p]);
+                    }
+                }
+            }
             const int ab = t & 1;
             if (!mbar_wait(&accf[ab], (t >> 1) & 1, a.err, 25)) {
                 *abort_flag = 1;
@@ -877,15 +897,10 @@ int oz_inverse_resid(OZState* o, const void* F, bool f64, int nb, const void* fg
     if (rc) return rc;
     const int N = o->N;
     const long long NN = (long long)N * N;
-    // double-float FFT over p (lines (fn, q, k)), then over q (lines (fn, p, k)) with the residual against the
-    // FP32 samples formed in the second pass's store phase (its lines are rows of the grid [fn][k][j1][j2])
+    // double-float FFT over q (lines (fn, p, k)), then over p (lines (fn, q, k)) -- the grid form serves the
+    // sizes the spectral form does not (N not a power of two from 64 to 512)
     T->begin(ST_REF_FFT, st);
-    if (fft_df32_k_supported(N)) {
-        OZK(launch_fft_df32_k(o->pen, N, NN, (long long)nb * N, N, NN * N, N, o->d_tw, st));
-        OZK(launch_fft_df32_k_resid(o->pen, N, nb, fgrid, real, resid, o->d_tw, st));
-        T->end(st);
-        return FFTSO3_SUCCESS;
-    } else {
+    {
         FFTLaunch Lq;
         Lq.in = o->pen;
         Lq.out = o->pen;
