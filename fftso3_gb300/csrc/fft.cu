@@ -13,8 +13,6 @@
 // (the column pass) the global loads/stores run line-fastest so each warp
 // touches contiguous segments.  Twiddles come from an FP64 host table
 // W[i] = e^{-2 pi i i / N} staged in shared memory.
-#include <algorithm>
-
 #include "common.cuh"
 #include "df32.cuh"
 #include "fft.cuh"
@@ -648,19 +646,13 @@ size_t slice_fft_smem_bytes(int N, int spc, bool real)
 // Every element walk below advances its indices by constant steps (one division per walk, none per element).
 template <bool FWD, bool REAL>
 __global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const BucketSeg* __restrict__ segs, int nseg,
-                                                                    long long nblk, const void* __restrict__ in,
+                                                                    const void* __restrict__ in,
                                                                     void* __restrict__ out)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int sb;
-    constexpr int T = SLICE_THREADS;
-    const int tid = threadIdx.x;
-    // persistent: a contiguous range of work units (consecutive slices share the pencils' cache lines)
-    const long long per = (nblk + gridDim.x - 1) / gridDim.x;
-    const long long u0 = (long long)blockIdx.x * per, u1 = min(nblk, u0 + per);
-    int cur = -1;  // bucket whose twiddles are staged
-    for (long long blk = u0; blk < u1; ++blk) {
-    if (tid == 0) {
+    const long long blk = blockIdx.x;
+    if (threadIdx.x == 0) {
         int lo = 0, hi = nseg - 1;
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
@@ -670,15 +662,15 @@ __global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const Bucke
         sb = lo;
     }
     __syncthreads();
-    const int seg = sb;  // (thread 0 rewrites sb for the next unit once everyone has passed this unit's barriers)
-    const BucketSeg& S = segs[seg];
+    const BucketSeg& S = segs[sb];
     const int N = S.N, B = N / 2, LS = slice_line_stride(N), G = S.G, spc = S.spc;
     const int RS = slice_row_stride(N, REAL), NC = REAL ? B + 1 : N;
     const int SSt = N * RS + 1;
     const long long NN = (long long)N * N, NNN = NN * N;
-    const long long nsl = (long long)S.batch * N;
     const long long s0 = (blk - S.blk0) * spc;
-    const int ns = (int)min((long long)spc, nsl - s0);
+    const int ns = (int)min((long long)spc, (long long)S.batch * N - s0);
+    constexpr int T = SLICE_THREADS;
+    const int tid = threadIdx.x;
     const int R0 = S.fac.r[0];
     const int nmat = R0 > 8 ? prime_mat_entries(R0) : 0;
     float2* X = reinterpret_cast<float2*>(smem_raw);
@@ -692,30 +684,20 @@ __global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const Bucke
     int* lx = reinterpret_cast<int*>(lm + TB);                  // per line: offset in the slices
     const float2* __restrict__ Pin = S.pencil;
     float2* __restrict__ Pout = S.pencil;
-    if (seg != cur) {
-        cur = seg;
-        const double2* tw = S.tw;
-        for (int i = tid; i < N; i += T) w[i] = make_float2((float)tw[i].x, (float)tw[i].y);
-        if (R0 > 8) {
-            const int P = (R0 - 1) / 2, P4 = (P + 3) / 4 * 4, Nr = N / R0;
-            for (int i = tid; i < P * P4; i += T) {
-                const int t = i / P4 + 1, q = i - (t - 1) * P4 + 1;
-                float c = 0.f, sn = 0.f;
-                if (q <= P) {
-                    const double2 v = tw[((t * q) % R0) * Nr];  // e^{-2 pi i t q / R}
-                    c = (float)v.x;
-                    sn = (float)(-v.y);
-                }
-                mat[i] = make_float2(c, sn);
+    const double2* tw = S.tw;
+    for (int i = tid; i < N; i += T) w[i] = make_float2((float)tw[i].x, (float)tw[i].y);
+    if (R0 > 8) {
+        const int P = (R0 - 1) / 2, P4 = (P + 3) / 4 * 4, Nr = N / R0;
+        for (int i = tid; i < P * P4; i += T) {
+            const int t = i / P4 + 1, q = i - (t - 1) * P4 + 1;
+            float c = 0.f, sn = 0.f;
+            if (q <= P) {
+                const double2 v = tw[((t * q) % R0) * Nr];  // e^{-2 pi i t q / R}
+                c = (float)v.x;
+                sn = (float)(-v.y);
             }
+            mat[i] = make_float2(c, sn);
         }
-    }
-    if (FWD && blk + 1 < u1 && s0 + spc < nsl) {
-        // the next unit's grid rows (same bucket), requested into L2 while this one computes
-        const int nn = (int)min((long long)spc, nsl - s0 - spc);
-        const char* g = reinterpret_cast<const char*>(in) + (S.g0 + (s0 + spc) * NN) * (REAL ? 4 : 8);
-        const long long lines = ((long long)nn * NN * (REAL ? 4 : 8) + 127) / 128;
-        for (long long i = tid; i < lines; i += T) asm volatile("prefetch.global.L2 [%0];" ::"l"(g + 128 * i));
     }
     const int NR = REAL ? B : N;           // row lines per slice
     const int rl = T / N, rj = T - rl * N;  // walk (l, j) over rows of N
@@ -922,7 +904,6 @@ __global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const Bucke
             __syncthreads();
         }
     }
-    }  // work units
 }
 
 cudaError_t launch_slice_fft(const BucketSeg* segs, int nseg, long long nblk, size_t smem, bool fwd, bool real,
@@ -934,13 +915,7 @@ cudaError_t launch_slice_fft(const BucketSeg* segs, int nseg, long long nblk, si
                     : (real ? slice_fft_kernel<false, true> : slice_fft_kernel<false, false>);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    int dev = 0, nsm = 0, occ = 0;
-    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-    if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, SLICE_THREADS, smem)) != cudaSuccess)
-        return e;
-    const long long ctas = std::min<long long>(nblk, (long long)nsm * std::max(occ, 1));
-    kern<<<(unsigned)ctas, SLICE_THREADS, smem, st>>>(segs, nseg, nblk, in, out);
+    kern<<<(unsigned)nblk, SLICE_THREADS, smem, st>>>(segs, nseg, in, out);
     return cudaGetLastError();
 }
 

@@ -42,10 +42,9 @@ __host__ __device__ inline int slice_lines_per_group(int N)
 }
 size_t slice_fft_smem_bytes(int N, int spc, bool real);
 
-// Both FFT passes of the beta slices of every bucket in one launch: nblk work units (spc slices of one bucket
-// each, blk0 numbering), run by persistent CTAs (as many as are resident, each a contiguous range of units),
-// smem bytes of dynamic shared memory each: fwd: grid slabs (complex64, or float32 when real) -> pencils; else
-// pencils (Nyquist bins read as zero; real: their Hermitian part) -> grid slabs (float32 when real).
+// Both FFT passes of the beta slices of every bucket in one launch (nblk CTAs, smem bytes of dynamic shared
+// memory each): fwd: grid slabs (complex64, or float32 when real) -> pencils; else pencils (Nyquist bins read
+// as zero; real: their Hermitian part) -> grid slabs (float32 when real).
 cudaError_t launch_slice_fft(const BucketSeg* segs, int nseg, long long nblk, size_t smem, bool fwd, bool real,
                              const void* in, void* out, cudaStream_t st);
 
