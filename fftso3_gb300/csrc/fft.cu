@@ -602,17 +602,16 @@ __device__ float2* run_line_stages(float2* src, float2* dst, const float2* w, co
     for (int s = 0; s < ns; ++s) {
         const int R = fac.r[s];
         switch (R) {
-            case 2: stockham_stage<float, 2, true>(src, dst, w, N, Ns, nl, LS); break;
-            case 3: stockham_stage<float, 3, true>(src, dst, w, N, Ns, nl, LS); break;
-            case 4: stockham_stage<float, 4, true>(src, dst, w, N, Ns, nl, LS); break;
-            case 5: stockham_stage<float, 5, true>(src, dst, w, N, Ns, nl, LS); break;
-            case 7: stockham_stage<float, 7, true>(src, dst, w, N, Ns, nl, LS); break;
-            case 8: stockham_stage<float, 8, true>(src, dst, w, N, Ns, nl, LS); break;
+            case 2: stockham_stage<float, 2, SLICE_PAD>(src, dst, w, N, Ns, nl, LS); break;
+            case 3: stockham_stage<float, 3, SLICE_PAD>(src, dst, w, N, Ns, nl, LS); break;
+            case 4: stockham_stage<float, 4, SLICE_PAD>(src, dst, w, N, Ns, nl, LS); break;
+            case 5: stockham_stage<float, 5, SLICE_PAD>(src, dst, w, N, Ns, nl, LS); break;
+            case 7: stockham_stage<float, 7, SLICE_PAD>(src, dst, w, N, Ns, nl, LS); break;
+            case 8: stockham_stage<float, 8, SLICE_PAD>(src, dst, w, N, Ns, nl, LS); break;
             default:
-                // prime first stage: two outputs q per work item, so the few lines of a group still give
-                // every thread a (line pair, j, q block) item
-                if (Ns == 1) dft_prime_first_t<float, 2, 2, true>(src, dst, mat, N, R, nl, LS);
-                else stockham_generic<float, true>(src, dst, w, N, Ns, R, nl, LS);
+                // prime first stage: four outputs q per work item (two measured slower)
+                if (Ns == 1) dft_prime_first_t<float, 2, 4, SLICE_PAD>(src, dst, mat, N, R, nl, LS);
+                else stockham_generic<float, SLICE_PAD>(src, dst, w, N, Ns, R, nl, LS);
                 break;
         }
         __syncthreads();
@@ -733,9 +732,9 @@ __global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const Bucke
                 for (int e = tid; e < nl * N; e += T) {
                     if (REAL) {
                         const float* g = reinterpret_cast<const float*>(in) + lg[l] + j;
-                        A[l * LS + lpos<true>(j)] = make_float2(g[0], g[N]);
+                        A[l * LS + lpos<SLICE_PAD>(j)] = make_float2(g[0], g[N]);
                     } else {
-                        A[l * LS + lpos<true>(j)] = reinterpret_cast<const float2*>(in)[lg[l] + j];
+                        A[l * LS + lpos<SLICE_PAD>(j)] = reinterpret_cast<const float2*>(in)[lg[l] + j];
                     }
                     j += rj;
                     l += rl;
@@ -749,11 +748,11 @@ __global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const Bucke
                 for (int e = tid; e < nl * NC; e += T) {
                     float2* x = X + lx[l];
                     if (REAL) {
-                        const float2 z = res[l * LS + lpos<true>(q)], zm = res[l * LS + lpos<true>(q == 0 ? 0 : N - q)];
+                        const float2 z = res[l * LS + lpos<SLICE_PAD>(q)], zm = res[l * LS + lpos<SLICE_PAD>(q == 0 ? 0 : N - q)];
                         x[q] = make_float2(0.5f * (z.x + zm.x), 0.5f * (z.y - zm.y));
                         x[RS + q] = make_float2(0.5f * (z.y + zm.y), -0.5f * (z.x - zm.x));
                     } else {
-                        x[q] = res[l * LS + lpos<true>(q)];
+                        x[q] = res[l * LS + lpos<SLICE_PAD>(q)];
                     }
                     q += cq;
                     l += cl;
@@ -772,7 +771,7 @@ __global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const Bucke
             {
                 int j = tid / nl, l = tid - j * nl;
                 for (int e = tid; e < nl * N; e += T) {
-                    A[l * LS + lpos<true>(j)] = X[lx[l] + j * RS];
+                    A[l * LS + lpos<SLICE_PAD>(j)] = X[lx[l] + j * RS];
                     l += gl;
                     j += gj;
                     if (l >= nl) { l -= nl; ++j; }
@@ -783,7 +782,7 @@ __global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const Bucke
             {
                 int p = tid / nl, l = tid - p * nl;
                 for (int e = tid; e < nl * N; e += T) {
-                    const float2 v = res[l * LS + lpos<true>(p)];
+                    const float2 v = res[l * LS + lpos<SLICE_PAD>(p)];
                     Pout[lg[l] + p * NN] = v;
                     if (REAL && lm[l] >= 0) Pout[lm[l] + (p == 0 ? 0 : N - p) * NN] = make_float2(v.x, -v.y);
                     l += gl;
@@ -834,7 +833,7 @@ __global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const Bucke
             {
                 int j = tid / nl, l = tid - j * nl;
                 for (int e = tid; e < nl * N; e += T) {
-                    A[l * LS + lpos<true>(j)] = X[lx[l] + j * RS];
+                    A[l * LS + lpos<SLICE_PAD>(j)] = X[lx[l] + j * RS];
                     l += gl;
                     j += gj;
                     if (l >= nl) { l -= nl; ++j; }
@@ -845,7 +844,7 @@ __global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const Bucke
             {
                 int j = tid / nl, l = tid - j * nl;
                 for (int e = tid; e < nl * N; e += T) {
-                    X[lx[l] + j * RS] = res[l * LS + lpos<true>(j)];
+                    X[lx[l] + j * RS] = res[l * LS + lpos<SLICE_PAD>(j)];
                     l += gl;
                     j += gj;
                     if (l >= nl) { l -= nl; ++j; }
@@ -874,9 +873,9 @@ __global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const Bucke
                             ya.y = -ya.y;
                             yb.y = -yb.y;
                         }
-                        A[l * LS + lpos<true>(j)] = make_float2(ya.x - yb.y, ya.y + yb.x);
+                        A[l * LS + lpos<SLICE_PAD>(j)] = make_float2(ya.x - yb.y, ya.y + yb.x);
                     } else {
-                        A[l * LS + lpos<true>(j)] = x[j];
+                        A[l * LS + lpos<SLICE_PAD>(j)] = x[j];
                     }
                     j += rj;
                     l += rl;
@@ -888,7 +887,7 @@ __global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const Bucke
             {
                 int l = tid / N, j = tid - l * N;
                 for (int e = tid; e < nl * N; e += T) {
-                    const float2 v = res[l * LS + lpos<true>(j)];
+                    const float2 v = res[l * LS + lpos<SLICE_PAD>(j)];
                     if (REAL) {
                         float* g = reinterpret_cast<float*>(out) + lg[l] + j;
                         g[0] = v.x;

@@ -32,9 +32,10 @@ constexpr int SLICE_LINE_ELEMS = 2048;  // elements of each of the two Stockham 
 // half-spectrum), odd so that column walks meet distinct banks, and the shared memory one CTA of the slice
 // FFT needs for spc slices of size N.
 __host__ __device__ inline int slice_row_stride(int N, bool real) { return real ? ((N / 2 + 1) | 1) : N + 1; }
-// Stockham line buffers: lines of N elements padded by one slot per 8 (odd stride), groups of an even number
-// of lines within SLICE_LINE_ELEMS
-__host__ __device__ inline int slice_line_stride(int N) { return (N + (N >> 3) + 1) | 1; }
+// Stockham line buffers: lines of N elements (odd stride N + 1; SLICE_PAD: one padding slot per 8 elements,
+// measured slower), groups of an even number of lines within SLICE_LINE_ELEMS
+constexpr bool SLICE_PAD = false;
+__host__ __device__ inline int slice_line_stride(int N) { return SLICE_PAD ? (N + (N >> 3) + 1) | 1 : N + 1; }
 __host__ __device__ inline int slice_lines_per_group(int N)
 {
     const int g = (SLICE_LINE_ELEMS / slice_line_stride(N)) & ~1;

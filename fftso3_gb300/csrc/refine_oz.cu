@@ -385,18 +385,31 @@ __global__ void __launch_bounds__(THREADS, 1)
                 poff[p] = ((long long)pi * N + qi) * N;
             }
             const int et = k < N ? (int)a.et[(long long)item.x * N + k] : 0;
-            if (spectral && k < N) {
-                // the FFT values this item will read, requested into L2 while its MMAs run
-#pragma unroll 1
-                for (int fl = 0; fl < FPT; ++fl) {
-                    const int f = item.z * FPT + fl;
-                    if (f >= a.batch) break;
-                    const long long fo = (long long)f * a.fstride + k;
+            if (spectral) {
+                // the FFT values of the CTA's next item, requested into L2 an item ahead of their loads; the
+                // forward places (-m, -n) of the pairs (m0, n0), (-m0, -n0), (n0, m0), (-n0, -m0)
+                const int nit = it + (int)gridDim.x;
+                if (nit < a.nitems) {
+                    const int4 pit = a.items[nit];
+                    int pm0, pn0;
+                    item_mn(pit, pm0, pn0);
+                    const int np = pm0 == 0 ? 1 : (pn0 == pm0 || pn0 == -pm0) ? 2 : 4;
+                    const int pk = pit.y * BM + r;
+                    if (pk < N) {
 #pragma unroll
-                    for (int p = 0; p < 4; ++p) {
-                        if (p >= P.np) break;
-                        prefetch_l2(a.rhi + fo + poff[p]);
-                        prefetch_l2(a.rlo + fo + poff[p]);
+                        for (int p = 0; p < 4; ++p) {
+                            if (p >= np) break;
+                            const int mm = p == 0 ? -pm0 : p == 1 ? pm0 : p == 2 ? -pn0 : pn0;
+                            const int nn = p == 0 ? -pn0 : p == 1 ? pn0 : p == 2 ? -pm0 : pm0;
+                            const long long po = ((long long)((mm + N) % N) * N + (nn + N) % N) * N + pk;
+#pragma unroll 1
+                            for (int fl = 0; fl < FPT; ++fl) {
+                                const int f = pit.z * FPT + fl;
+                                if (f >= a.batch) break;
+                                prefetch_l2(a.rhi + (long long)f * a.fstride + po);
+                                prefetch_l2(a.rlo + (long long)f * a.fstride + po);
+                            }
+                        }
                     }
                 }
             }
