@@ -79,11 +79,7 @@ constexpr int STAGE_BYTES = STAGE_A + NS * BPLANE;
 constexpr int NPROD = 8;
 constexpr int NEPI = 4;
 constexpr int THREADS = 32 * (2 + NPROD + NEPI);
-// spectral residual: each epilogue thread stages its own FFT values (hi, lo of 2 functions x 4 pairs, one column
-// block) two blocks deep with cp.async
-constexpr int RING_ENTRIES = 2 * 4 * 2;  // [function of the block][pair][hi / lo]
-constexpr int RING_BYTES = 2 * RING_ENTRIES * BM * 8;
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 256 /*barriers*/ + RING_BYTES + 1024 /*alignment*/;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 256 /*barriers*/ + 1024 /*alignment*/;
 constexpr int ACC = NS * BN;            // TMEM columns of one accumulator buffer (levels 0..3)
 constexpr int TMEM_COLS = 2 * ACC;
 constexpr int EXP_MIN = -120, EXP_MAX = 120;
@@ -161,7 +157,6 @@ __global__ void __launch_bounds__(THREADS, 1)
     uint64_t* acce = accf + 2;
     uint32_t* tmem_slot = (uint32_t*)(acce + 2);
     volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
-    float2* ring = (float2*)(smem + STAGES * STAGE_BYTES + 256);  // [slot][entry][k row]
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     auto nsteps = [&](const int4& it) {
         int m0, n0;
@@ -372,69 +367,39 @@ __global__ void __launch_bounds__(THREADS, 1)
         const int quarter = warp & 3;
         const int r = quarter * 32 + lane;
         const int N = a.N;
-        const bool spectral = a.rhi != nullptr;
-        // spectral: the thread's own FFT values of a column block (item, cc): 8 (function, pair) places, hi and lo,
-        // copied with cp.async into ring slot s one block ahead of their use (each thread reads back only what it
-        // copied, so no barrier is needed; cp.async.wait_group orders them)
-        // forward places (-m, -n) mod N of the pairs (m0, n0), (-m0, -n0), (n0, m0), (-n0, -m0) of an item
-        auto places = [&](const int4& itm, int (&pos)[4]) -> int {
-            int pm0, pn0;
-            item_mn(itm, pm0, pn0);
-#pragma unroll
-            for (int p = 0; p < 4; ++p) {
-                const int mm = p == 0 ? -pm0 : p == 1 ? pm0 : p == 2 ? -pn0 : pn0;
-                const int nn = p == 0 ? -pn0 : p == 1 ? pn0 : p == 2 ? -pm0 : pm0;
-                pos[p] = ((mm + N) % N) * N + (nn + N) % N;
-            }
-            return pm0 == 0 ? 1 : (pn0 == pm0 || pn0 == -pm0) ? 2 : 4;
-        };
-        auto issue = [&](const int4& itm, const int (&pos)[4], int np, int cc, int slot) {
-            const int kk = itm.y * BM + r;
-            if (kk < N) {
-#pragma unroll
-                for (int fq = 0; fq < 2; ++fq) {
-                    const int f = itm.z * FPT + cc * 2 + fq;
-                    if (f >= a.batch) break;
-#pragma unroll
-                    for (int p = 0; p < 4; ++p) {
-                        if (p >= np) break;
-                        const long long g = (long long)f * a.fstride + (long long)pos[p] * N + kk;
-                        const int e = (fq * 4 + p) * 2;
-                        const uint32_t d = smem_u32(ring + ((slot * RING_ENTRIES + e) * BM + r));
-                        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(a.rhi + g) : "memory");
-                        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d + BM * 8), "l"(a.rlo + g)
-                                     : "memory");
-                    }
-                }
-            }
-            asm volatile("cp.async.commit_group;" ::: "memory");
-        };
-        int t = 0, gb = 0;  // items and column blocks done
-        if (spectral && (int)blockIdx.x < a.nitems) {
-            int pos0[4];
-            const int4 it0 = a.items[blockIdx.x];
-            const int np0 = places(it0, pos0);
-            issue(it0, pos0, np0, 0, 0);
-        }
+        int t = 0;
         for (int it = blockIdx.x; it < a.nitems && !*abort_flag; it += gridDim.x, ++t) {
             const int4 item = a.items[it];
             int m0, n0;
             item_mn(item, m0, n0);
             const GroupPairs P = group_pairs(m0, n0);
             const int k = item.y * BM + r;
-            // pencil places (p N + q): synthesis H(m, n) at (m, n) mod N; spectral residual at the forward place
-            // (-m, -n) mod N (places())
-            int pos[4];
-            const int npl = places(item, pos);
-            if (!spectral) {
+            const bool spectral = a.rhi != nullptr;
+            long long poff[4];
 #pragma unroll
-                for (int p = 0; p < 4; ++p) {
-                    int pi = P.m[p] % N; if (pi < 0) pi += N;
-                    int qi = P.n[p] % N; if (qi < 0) qi += N;
-                    pos[p] = pi * N + qi;
-                }
+            for (int p = 0; p < 4; ++p) {
+                // synthesis: H(m, n) at (m, n) mod N; spectral residual: at the forward place (-m, -n) mod N
+                const int mm = spectral ? -P.m[p] : P.m[p], nn = spectral ? -P.n[p] : P.n[p];
+                int pi = mm % N; if (pi < 0) pi += N;
+                int qi = nn % N; if (qi < 0) qi += N;
+                poff[p] = ((long long)pi * N + qi) * N;
             }
             const int et = k < N ? (int)a.et[(long long)item.x * N + k] : 0;
+            if (spectral && k < N) {
+                // the FFT values this item will read, requested into L2 while its MMAs run
+#pragma unroll 1
+                for (int fl = 0; fl < FPT; ++fl) {
+                    const int f = item.z * FPT + fl;
+                    if (f >= a.batch) break;
+                    const long long fo = (long long)f * a.fstride + k;
+#pragma unroll
+                    for (int p = 0; p < 4; ++p) {
+                        if (p >= P.np) break;
+                        prefetch_l2(a.rhi + fo + poff[p]);
+                        prefetch_l2(a.rlo + fo + poff[p]);
+                    }
+                }
+            }
             const int ab = t & 1;
             if (!mbar_wait(&accf[ab], (t >> 1) & 1, a.err, 25)) {
                 *abort_flag = 1;
@@ -443,33 +408,29 @@ __global__ void __launch_bounds__(THREADS, 1)
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t trow = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(ab * ACC);
 #pragma unroll 1
-            for (int cc = 0; cc < BN / 16; ++cc, ++gb) {  // 16 columns = 2 functions x 4 pairs x re/im
+            for (int cc = 0; cc < BN / 16; ++cc) {  // 16 columns = 2 functions x 4 pairs x re/im
                 uint32_t v[NS][16];
 #pragma unroll
                 for (int j = 0; j < NS; ++j) tmem_ld16_nowait(trow + (uint32_t)(j * BN + cc * 16), v[j]);
-                if (spectral) {
-                    // the next block's values into the other slot, then this block's own copies complete
-                    const int nit = it + (int)gridDim.x;
-                    if (cc + 1 < BN / 16) {
-                        issue(item, pos, npl, cc + 1, (gb + 1) & 1);
-                    } else if (nit < a.nitems) {
-                        int pn[4];
-                        const int4 itn = a.items[nit];
-                        const int npn = places(itn, pn);
-                        issue(itn, pn, npn, 0, (gb + 1) & 1);
-                    } else {
-                        asm volatile("cp.async.commit_group;" ::: "memory");
-                    }
-                    asm volatile("cp.async.wait_group 1;" ::: "memory");
-                }
                 tmem_wait_ld();
-                const float2* rs = ring + (gb & 1) * RING_ENTRIES * BM + r;
 #pragma unroll
                 for (int fq = 0; fq < 2; ++fq) {
                     const int f = item.z * FPT + cc * 2 + fq;
                     if (f >= a.batch || k >= N) continue;
                     const long long fo = (long long)f * a.fstride + k;
                     const signed char* eyf = a.ey + ((long long)f * a.ngroups + item.x) * 4;
+                    // spectral residual: the function's four pair values, loads in flight together
+                    float2 sh[4], sl[4];
+                    if (spectral) {
+#pragma unroll
+                        for (int p = 0; p < 4; ++p) {
+                            sh[p] = sl[p] = make_float2(0.f, 0.f);
+                            if (p < P.np) {
+                                sh[p] = __ldcs(a.rhi + fo + poff[p]);
+                                sl[p] = __ldcs(a.rlo + fo + poff[p]);
+                            }
+                        }
+                    }
 #pragma unroll
                     for (int p = 0; p < 4; ++p) {
                         if (p >= P.np) break;
@@ -482,12 +443,12 @@ __global__ void __launch_bounds__(THREADS, 1)
                         if (spectral) {
                             // N^2 H = FFT of the synthesised grid; hi - N^2 H.h is exact (close values)
                             const int E2 = E + a.e2n;
-                            const float2 h = rs[((fq * 4 + p) * 2) * BM], l = rs[((fq * 4 + p) * 2 + 1) * BM];
-                            __stcs(a.rhi + fo + (long long)pos[p] * N,
+                            const float2 h = sh[p], l = sl[p];
+                            __stcs(a.rhi + fo + poff[p],
                                    make_float2((h.x - ldexpf(re.h, E2)) + (l.x - ldexpf(re.l, E2)),
                                                (h.y - ldexpf(im.h, E2)) + (l.y - ldexpf(im.l, E2))));
                         } else {
-                            a.pout[fo + (long long)pos[p] * N] =
+                            a.pout[fo + poff[p]] =
                                 make_float4(ldexpf(re.h, E), ldexpf(re.l, E), ldexpf(im.h, E), ldexpf(im.l, E));
                         }
                     }
@@ -497,8 +458,6 @@ __global__ void __launch_bounds__(THREADS, 1)
             __syncwarp();
             if (lane == 0) mbar_arrive(&acce[ab]);
         }
-        // copies still in flight (an aborted run) complete before the CTA's shared memory is released
-        if (spectral) asm volatile("cp.async.wait_all;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
