@@ -134,6 +134,10 @@ struct fftso3_plan {
     long long bytes = 0;
     TCState* tc = nullptr;         // tensor-core contraction state
     StageTimer timer;              // optional per-stage CUDA-event timing
+    // host calls of the refined forward: the samples' copy runs on its own stream, piece by piece, ahead of the
+    // double-float FFT of each piece (created on first use)
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t copy_ev[3] = {nullptr, nullptr, nullptr};
 };
 
 namespace fftso3 {
@@ -163,6 +167,9 @@ void plan_free(fftso3_plan* p)
         if (q) cudaFree(q);
     if (p->tc) tc_destroy(p->tc);
     if (p->oz) oz_destroy(p->oz);
+    for (cudaEvent_t e : p->copy_ev)
+        if (e) cudaEventDestroy(e);
+    if (p->copy_stream) cudaStreamDestroy(p->copy_stream);
 }
 
 size_t cbytes(const fftso3_plan* p) { return p->fp64 ? 16 : 8; }  // complex element bytes
@@ -305,17 +312,38 @@ int refine_forward(fftso3_plan* p, const void* grid, void* coeffs, cudaStream_t 
 // contraction, whose FFT is N^2 H), written over hi, and F = F0 + the GEMM of r^.  Equal to the grid form
 // F0 + forward(f - inverse(F0)) -- the forward GEMM reads exactly these pencils -- without the FP32 FFTs of the
 // samples and of the residual and without the double-float FFT of the synthesis.
-int refine_forward_spectral(fftso3_plan* p, const void* grid, void* coeffs, cudaStream_t st)
+//
+// host (non-null): the samples are in host memory and `grid` is the plan's staging area for them; they are copied
+// there on the plan's copy stream in pieces of a few functions, each piece's FFT waiting only for its own copy,
+// so the copy of the next piece runs under the FFT of this one.
+int refine_forward_spectral(fftso3_plan* p, const void* grid, void* coeffs, cudaStream_t st, const void* host)
 {
     StageTimer& T = p->timer;
     const long long C = p->coeff_elems, G = p->grid_elems;
     float2* hi = tc_pencil_buffer(p->tc);
     float2* lo = (float2*)tc_resid_buffer(p->tc);
     const int per = p->real ? 1 : 2;  // floats per sample
-    for (int f0 = 0; f0 < p->batch; f0 += p->rchunk) {
-        const int nb = p->batch - f0 < p->rchunk ? p->batch - f0 : p->rchunk;
-        int rc = oz_forward_fft(p->oz, (const float*)grid + (long long)f0 * G * per, p->real, nb,
-                                hi + (long long)f0 * G, lo + (long long)f0 * G, st, &T, g_err);
+    const int piece = host ? (p->rchunk < 4 ? p->rchunk : 4) : p->rchunk;
+    if (host) {
+        if (!p->copy_stream) {
+            CK(cudaStreamCreateWithFlags(&p->copy_stream, cudaStreamNonBlocking));
+            for (cudaEvent_t& e : p->copy_ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        }
+        // the staging area is free once the caller's earlier work on st is done
+        CK(cudaEventRecord(p->copy_ev[2], st));
+        CK(cudaStreamWaitEvent(p->copy_stream, p->copy_ev[2], 0));
+    }
+    for (int f0 = 0, i = 0; f0 < p->batch; f0 += piece, ++i) {
+        const int nb = p->batch - f0 < piece ? p->batch - f0 : piece;
+        const float* g = (const float*)grid + (long long)f0 * G * per;
+        if (host) {
+            CK(cudaMemcpyAsync((void*)g, (const float*)host + (long long)f0 * G * per,
+                               sizeof(float) * (size_t)nb * G * per, cudaMemcpyHostToDevice, p->copy_stream));
+            CK(cudaEventRecord(p->copy_ev[i & 1], p->copy_stream));
+            CK(cudaStreamWaitEvent(st, p->copy_ev[i & 1], 0));
+        }
+        int rc = oz_forward_fft(p->oz, g, p->real, nb, hi + (long long)f0 * G, lo + (long long)f0 * G, st, &T,
+                                g_err);
         if (rc) return rc;
     }
     int rc = tc_forward_pencils(p->tc, coeffs, st, &T, g_err);
@@ -345,7 +373,7 @@ int run_forward(fftso3_plan* p, const void* grid, void* coeffs, cudaStream_t st)
 {
     const int N = p->N, L = p->L, b = p->batch;
     StageTimer& T = p->timer;
-    if (spectral_refine(p)) return refine_forward_spectral(p, grid, coeffs, st);
+    if (spectral_refine(p)) return refine_forward_spectral(p, grid, coeffs, st, nullptr);
     if (p->tc) {
         int rc = tc_forward(p->tc, grid, coeffs, st, &T, g_err);
         if (rc || !(p->flags & FFTSO3_FLAG_REFINE)) return rc;
@@ -725,10 +753,20 @@ int fftso3_forward_host(fftso3_plan* plan, const void* grid_host, void* coeffs_h
         // the refinement reads the samples twice: copy them once into the residual buffer (batch complex64 grids);
         // the residual (grid form) or the FFT remainders (spectral form) then overwrite them chunk by chunk, each
         // chunk's samples read before its outputs are written.  Real samples go to the buffer's upper half, so
-        // that a chunk's complex64 remainders never reach the samples of later chunks.
+        // that a chunk's complex64 remainders never reach the samples of later chunks.  The refined forward
+        // passes over the coefficients several times: it writes them to device memory and copies them out once.
         void* stage = (char*)tc_resid_buffer(plan->tc) + (plan->real ? grid_bytes(plan) : 0);
-        CK(cudaMemcpyAsync(stage, grid_host, grid_bytes(plan), cudaMemcpyHostToDevice, st));
-        gin = stage;
+        if ((rc = ensure_io_coeff(plan))) return rc;
+        if (spectral_refine(plan)) {
+            // the samples' copy pipelined under the double-float FFT, piece by piece
+            if ((rc = refine_forward_spectral(plan, stage, plan->d_io_coeff, st, grid_host))) return rc;
+        } else {
+            CK(cudaMemcpyAsync(stage, grid_host, grid_bytes(plan), cudaMemcpyHostToDevice, st));
+            if ((rc = run_forward(plan, stage, plan->d_io_coeff, st))) return rc;
+        }
+        CK(cudaMemcpyAsync(coeffs_host, plan->d_io_coeff, coeff_bytes(plan), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        return FFTSO3_SUCCESS;
     }
     if ((!gin && (rc = ensure_io_grid(plan))) || (!cout && (rc = ensure_io_coeff(plan)))) return rc;
     if (!gin) {

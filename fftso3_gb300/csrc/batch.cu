@@ -393,7 +393,7 @@ int fftso3_batch_create(fftso3_batch** out, int kind, const int* l_max, int n_fu
         int maxsm = 0;
         cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device);
         want_phases = !(ev && ev[0] == '0') &&
-                      slice_fft_smem_bytes(2 * (b->buckets.back().L + 1), 1, real) <= (size_t)maxsm;
+                      slice_fft_smem_bytes(2 * (b->buckets.back().L + 1), 1, real, false) <= (size_t)maxsm;
     }
     unsigned pflags = flags & (FFTSO3_FLAG_REFINE | FFTSO3_FLAG_AUTOTUNE);
     if (want_phases) pflags &= ~FFTSO3_FLAG_AUTOTUNE;

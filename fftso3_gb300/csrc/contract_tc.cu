@@ -1950,6 +1950,7 @@ struct TCFused {
     long long nblk = 0, ncblk = 0;
     size_t slice_smem = 0;
     bool real = false;
+    bool slice_wide = false;  // 512-thread slice FFT CTAs (FFTSO3_SLICE_WIDE=1)
 };
 
 void tc_fused_destroy(TCFused* f)
@@ -2086,6 +2087,8 @@ int tc_fused_phases(TCFused* f, const std::vector<long long>& g0, const std::vec
         return FFTSO3_ERR_UNSUPPORTED;
     }
     const bool real = f->parts[0]->real;
+    const char* ev_wide = getenv("FFTSO3_SLICE_WIDE");
+    const bool wide = ev_wide && ev_wide[0] == '1';
     int Nmax = 0;
     size_t smem = 0;
     for (TCState* p : f->parts) {
@@ -2094,7 +2097,7 @@ int tc_fused_phases(TCFused* f, const std::vector<long long>& g0, const std::vec
             return FFTSO3_ERR_UNSUPPORTED;
         }
         Nmax = std::max(Nmax, p->N);
-        smem = std::max(smem, slice_fft_smem_bytes(p->N, 1, real));
+        smem = std::max(smem, slice_fft_smem_bytes(p->N, 1, real, wide));
     }
     int maxsm = 0, dev = 0;
     cudaGetDevice(&dev);
@@ -2116,9 +2119,9 @@ int tc_fused_phases(TCFused* f, const std::vector<long long>& g0, const std::vec
         s.B = p->B;
         s.N = N;
         s.batch = p->batch;
-        s.G = slice_lines_per_group(N);
+        s.G = slice_lines_per_group(N, wide);
         int spc = 1;
-        while (spc < 256 && slice_fft_smem_bytes(N, spc + 1, real) <= smem &&
+        while (spc < 256 && slice_fft_smem_bytes(N, spc + 1, real, wide) <= smem &&
                (long long)(spc + 1) * N * N <= (long long)Nmax * Nmax)
             ++spc;
         s.spc = spc;
@@ -2162,6 +2165,7 @@ int tc_fused_phases(TCFused* f, const std::vector<long long>& g0, const std::vec
     f->ncblk = cblk;
     f->slice_smem = smem;
     f->real = real;
+    f->slice_wide = wide;
     return FFTSO3_SUCCESS;
 }
 
@@ -2172,7 +2176,7 @@ int tc_fused_forward(TCFused* f, const void* grid, void* coeffs, cudaStream_t st
         return FFTSO3_ERR_CUDA;
     }
     T->begin(ST_FFT_SLICES, st);
-    TCK(launch_slice_fft(f->d_bseg, f->nbseg, f->nblk, f->slice_smem, true, f->real, grid, nullptr, st));
+    TCK(launch_slice_fft(f->d_bseg, f->nbseg, f->nblk, f->slice_smem, true, f->real, f->slice_wide, grid, nullptr, st));
     T->end(st);
     int rc = tc_fused_gemm(f, true, st, T, err);
     if (rc) return rc;
@@ -2194,7 +2198,7 @@ int tc_fused_inverse(TCFused* f, const void* coeffs, void* grid, cudaStream_t st
     int rc = tc_fused_gemm(f, false, st, T, err);
     if (rc) return rc;
     T->begin(ST_FFT_SLICES, st);
-    TCK(launch_slice_fft(f->d_bseg, f->nbseg, f->nblk, f->slice_smem, false, f->real, nullptr, grid, st));
+    TCK(launch_slice_fft(f->d_bseg, f->nbseg, f->nblk, f->slice_smem, false, f->real, f->slice_wide, nullptr, grid, st));
     T->end(st);
     return FFTSO3_SUCCESS;
 }

@@ -626,25 +626,21 @@ __device__ float2* run_line_stages(float2* src, float2* dst, const float2* w, co
 static int slice_prime_entries(const FFTFactors& f) { return f.r[0] > 8 ? prime_mat_entries(f.r[0]) : 0; }
 
 // Per-line (or per-slice) tables of a CTA: two 64-bit global offsets and one shared-memory offset per entry.
-__host__ __device__ inline int slice_table_entries(int N, int spc)
-{
-    const int G = slice_lines_per_group(N);
-    return G > spc ? G : spc;
-}
+__host__ __device__ inline int slice_table_entries(int G, int spc) { return G > spc ? G : spc; }
 
-size_t slice_fft_smem_bytes(int N, int spc, bool real)
+size_t slice_fft_smem_bytes(int N, int spc, bool real, bool wide)
 {
     FFTFactors f;
     make_fft_factors_prime_first(N, f);
     const size_t sst = (size_t)N * slice_row_stride(N, real) + 1;
-    const size_t G = (size_t)slice_lines_per_group(N);
-    const size_t tb = (size_t)slice_table_entries(N, spc);
+    const size_t G = (size_t)slice_lines_per_group(N, wide);
+    const size_t tb = (size_t)slice_table_entries((int)G, spc);
     return sizeof(float2) * (spc * sst + 2 * G * slice_line_stride(N) + N + slice_prime_entries(f)) + tb * (8 + 8 + 4);
 }
 
 // Every element walk below advances its indices by constant steps (one division per walk, none per element).
-template <bool FWD, bool REAL>
-__global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const BucketSeg* __restrict__ segs, int nseg,
+template <bool FWD, bool REAL, int NT>
+__global__ void __launch_bounds__(NT, NT == 256 ? 2 : 1) slice_fft_kernel(const BucketSeg* __restrict__ segs, int nseg,
                                                                     const void* __restrict__ in,
                                                                     void* __restrict__ out)
 {
@@ -668,7 +664,7 @@ __global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const Bucke
     const long long NN = (long long)N * N, NNN = NN * N;
     const long long s0 = (blk - S.blk0) * spc;
     const int ns = (int)min((long long)spc, (long long)S.batch * N - s0);
-    constexpr int T = SLICE_THREADS;
+    constexpr int T = NT;
     const int tid = threadIdx.x;
     const int R0 = S.fac.r[0];
     const int nmat = R0 > 8 ? prime_mat_entries(R0) : 0;
@@ -677,7 +673,7 @@ __global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const Bucke
     float2* Bf = A + G * LS;
     float2* w = Bf + G * LS;
     float2* mat = w + N;
-    const int TB = slice_table_entries(N, spc);
+    const int TB = slice_table_entries(G, spc);
     long long* lg = reinterpret_cast<long long*>(mat + nmat);  // per line: global offset
     long long* lm = lg + TB;                                    // per line: mirrored pencil offset (real), or -1
     int* lx = reinterpret_cast<int*>(lm + TB);                  // per line: offset in the slices
@@ -905,17 +901,25 @@ __global__ void __launch_bounds__(SLICE_THREADS, 2) slice_fft_kernel(const Bucke
     }
 }
 
+template <int NT>
+static cudaError_t slice_launch(const BucketSeg* segs, int nseg, long long nblk, size_t smem, bool fwd, bool real,
+                                const void* in, void* out, cudaStream_t st)
+{
+    auto kern = fwd ? (real ? slice_fft_kernel<true, true, NT> : slice_fft_kernel<true, false, NT>)
+                    : (real ? slice_fft_kernel<false, true, NT> : slice_fft_kernel<false, false, NT>);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<(unsigned)nblk, NT, smem, st>>>(segs, nseg, in, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_slice_fft(const BucketSeg* segs, int nseg, long long nblk, size_t smem, bool fwd, bool real,
-                             const void* in, void* out, cudaStream_t st)
+                             bool wide, const void* in, void* out, cudaStream_t st)
 {
     if (nblk <= 0) return cudaSuccess;
     if (nblk > 0x7fffffffLL || nseg <= 0) return cudaErrorInvalidValue;
-    auto kern = fwd ? (real ? slice_fft_kernel<true, true> : slice_fft_kernel<true, false>)
-                    : (real ? slice_fft_kernel<false, true> : slice_fft_kernel<false, false>);
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    kern<<<(unsigned)nblk, SLICE_THREADS, smem, st>>>(segs, nseg, in, out);
-    return cudaGetLastError();
+    return wide ? slice_launch<512>(segs, nseg, nblk, smem, fwd, real, in, out, st)
+                : slice_launch<256>(segs, nseg, nblk, smem, fwd, real, in, out, st);
 }
 
 bool fft_df32_k_supported(int N) { return N == 64 || N == 128 || N == 256 || N == 512; }

@@ -25,29 +25,32 @@ struct BucketSeg {
     long long cblk0;             // first CTA of the bucket in the coefficient conversions
 };
 
-constexpr int SLICE_THREADS = 256;
-constexpr int SLICE_LINE_ELEMS = 2048;  // elements of each of the two Stockham line buffers
+// Two launch shapes: 256 threads per CTA with line buffers of 2048 elements (two CTAs per SM), or "wide":
+// 512 threads with 4096-element line buffers (one CTA per SM; twice the lines per Stockham group, so half the
+// barrier phases per slice and twice the work items of a prime-radix stage).
+__host__ __device__ inline int slice_threads(bool wide) { return wide ? 512 : 256; }
+__host__ __device__ inline int slice_line_elems(bool wide) { return wide ? 4096 : 2048; }
 
 // Row stride of a slice in shared memory (complex: all N columns; real: columns 0..N/2 of the Hermitian
 // half-spectrum), odd so that column walks meet distinct banks, and the shared memory one CTA of the slice
 // FFT needs for spc slices of size N.
 __host__ __device__ inline int slice_row_stride(int N, bool real) { return real ? ((N / 2 + 1) | 1) : N + 1; }
 // Stockham line buffers: lines of N elements (odd stride N + 1; SLICE_PAD: one padding slot per 8 elements,
-// measured slower), groups of an even number of lines within SLICE_LINE_ELEMS
+// measured slower), groups of an even number of lines within the launch shape's line elements
 constexpr bool SLICE_PAD = false;
 __host__ __device__ inline int slice_line_stride(int N) { return SLICE_PAD ? (N + (N >> 3) + 1) | 1 : N + 1; }
-__host__ __device__ inline int slice_lines_per_group(int N)
+__host__ __device__ inline int slice_lines_per_group(int N, bool wide)
 {
-    const int g = (SLICE_LINE_ELEMS / slice_line_stride(N)) & ~1;
+    const int g = (slice_line_elems(wide) / slice_line_stride(N)) & ~1;
     return g < 2 ? 2 : g;
 }
-size_t slice_fft_smem_bytes(int N, int spc, bool real);
+size_t slice_fft_smem_bytes(int N, int spc, bool real, bool wide);
 
 // Both FFT passes of the beta slices of every bucket in one launch (nblk CTAs, smem bytes of dynamic shared
 // memory each): fwd: grid slabs (complex64, or float32 when real) -> pencils; else pencils (Nyquist bins read
 // as zero; real: their Hermitian part) -> grid slabs (float32 when real).
 cudaError_t launch_slice_fft(const BucketSeg* segs, int nseg, long long nblk, size_t smem, bool fwd, bool real,
-                             const void* in, void* out, cudaStream_t st);
+                             bool wide, const void* in, void* out, cudaStream_t st);
 
 // Coefficient conversions of every bucket in one launch (CONVERT_THREADS coefficients of one bucket per CTA,
 // nblk CTAs in total, CTA i serving bucket segs[cseg[i]]; l_max <= 255):

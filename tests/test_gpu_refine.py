@@ -109,17 +109,17 @@ def test_exact_and_fp64_refinement_agree(gblib, oracle):
         assert rms <= 1e-7 and mx <= 1e-6, (i, rms, mx)
 
 
-@pytest.mark.parametrize("L", [15, 31])
+@pytest.mark.parametrize("L,b", [(15, 3), (31, 9)])
 @pytest.mark.parametrize("kind", ["complex", "real"])
-def test_refined_host_call_equals_device_call(gblib, oracle, kind, L):
+def test_refined_host_call_equals_device_call(gblib, oracle, kind, L, b):
     """fftso3_forward_host on a refined plan (samples staged once into the residual buffer, which the residual --
-    grid form, l_max 15 -- or the FFT remainders -- spectral form, l_max 31 -- then overwrite chunk by chunk)
-    gives the same coefficients, bit for bit, as fftso3_forward on device buffers; pageable and pinned host
-    samples, batch 3, and the host samples are left unchanged."""
+    grid form, l_max 15 -- or the FFT remainders -- spectral form, l_max 31, the samples copied in pieces of 4
+    functions under the FFT of the previous piece -- then overwrite chunk by chunk) gives the same coefficients,
+    bit for bit, as fftso3_forward on device buffers; pageable and pinned host samples, and the host samples are
+    left unchanged."""
     import torch
     cplx = kind == "complex"
     k = gblib.SO3_COMPLEX if cplx else gblib.SO3_REAL
-    b = 3
     N = 2 * (L + 1)
     gs = []
     for i in range(b):
