@@ -923,7 +923,7 @@ def s2_line(args) -> dict:
 
 # --------------------------------------------------------------- GPU arm
 
-def stage_roofline(name: str, tot_ms: float, cnt: int, L: int, b: int, chunk: int, peaks: dict):
+def stage_roofline(name: str, tot_ms: float, cnt: int, L: int, b: int, chunk: int, peaks: dict, piece: int = 0):
     """Achieved rate of one stage of an SO(3) complex tensor-core plan from its CUDA-event time, against the
     measured peak: algorithmic bytes (HBM-bound stages) or useful flops (contractions) per timed record."""
     B, N = L + 1, 2 * (L + 1)
@@ -946,7 +946,7 @@ def stage_roofline(name: str, tot_ms: float, cnt: int, L: int, b: int, chunk: in
     elif name in ("fft_rows", "fft_cols", "tc_pack_fwd", "tc_pack_inv"):
         byts, alg = 2 * grid8, "one complex64 read + write of every sample per pass"
     elif name == "refine_fft_df32":
-        byts, alg = (8.0 + 16 + 16 + 16) * chunk * N ** 3, ("double-float forward FFT of the samples: pass 1 reads "
+        byts, alg = (8.0 + 16 + 16 + 16) * (piece or chunk) * N ** 3, ("double-float forward FFT of the samples: pass 1 reads "
                                                           "8 B, writes 16 B; pass 2 reads 16 B, writes hi + lo "
                                                           "8 + 8 B per sample")
     elif name == "basis_convert":
@@ -1081,8 +1081,10 @@ def so3_tc_line(args, L: int, b: int, full: bool = True) -> dict:
     value = b * 1000.0 / ms
     # functions per refinement chunk (the library sizes chunks to the free device memory): one timed record of
     # the refinement FFT per chunk and step
-    nchunks = max(1, round(stages.get("refine_fft_df32", (0, args.steps))[1] / args.steps))
-    chunk = -(-b // nchunks)
+    nchunks = max(1, round(stages.get("refine_exact_contract", (0, args.steps))[1] / args.steps))
+    chunk = -(-b // nchunks)  # functions per exact-contraction launch
+    npieces = max(1, round(stages.get("refine_fft_df32", (0, args.steps))[1] / args.steps))
+    piece = -(-b // npieces)  # functions per double-float FFT record
     nrec = int(sum(c for _, c in stages.values()))
     # kernels in the timed region: one per timed record, plus the second kernel of the records that hold two
     # (the double-float FFT's two passes, one record per chunk)
@@ -1090,8 +1092,9 @@ def so3_tc_line(args, L: int, b: int, full: bool = True) -> dict:
     tot = sum(v for v, _ in stages.values())
     stage_summary = {k: {"ms_per_launch": v / c, "launches": c, "share": v / tot} for k, (v, c) in stages.items()}
     top, (top_ms, top_n) = max(stages.items(), key=lambda kv: kv[1][0])
-    roof = stage_roofline(top, top_ms, top_n, L, b, chunk, peaks)
-    roof["traffic"] = profiled_traffic(top, L, chunk if top.startswith("refine") else b)  # refinement: per chunk
+    roof = stage_roofline(top, top_ms, top_n, L, b, chunk, peaks, piece)
+    roof["traffic"] = profiled_traffic(top, L, (piece if top == "refine_fft_df32" else chunk)
+                                       if top.startswith("refine") else b)  # refinement: per launch record
     roof["share_of_step"] = top_ms / tot
 
     # ---- the step against its floors: HBM (algorithmic bytes of every stage) and tensor (issued MMA flops)
@@ -1195,7 +1198,7 @@ def so3_tc_line(args, L: int, b: int, full: bool = True) -> dict:
         "config": {"workload": f"SO(3) complex, l_max={L}, batch={b} functions ({N}^3 complex64 grid each), stable "
                                f"recursion; one step = {what}",
                    "l_max": L, "batch": b, "precision": "tc_bf16x3" + (" + refine" if full else ""),
-                   "refine_chunk": chunk if full else None,
+                   "refine_chunk": chunk if full else None, "refine_fft_piece": piece if full else None,
                    "l2": f"inputs larger than L2 ({8.0 * b * N ** 3 / 1e9:.1f} GB of complex64 grids)"},
         "e2e": e2e, "gpu_launches": launches, "roofline": roof, "step_roofline": step_roof,
         "stages": stage_summary, "accuracy": acc, "fp64_path": fp64,

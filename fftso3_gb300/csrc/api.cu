@@ -323,7 +323,8 @@ int refine_forward_spectral(fftso3_plan* p, const void* grid, void* coeffs, cuda
     float2* hi = tc_pencil_buffer(p->tc);
     float2* lo = (float2*)tc_resid_buffer(p->tc);
     const int per = p->real ? 1 : 2;  // floats per sample
-    const int piece = host ? (p->rchunk < 4 ? p->rchunk : 4) : p->rchunk;
+    const int fftn = oz_fft_functions(p->oz);
+    const int piece = host ? (fftn < 4 ? fftn : 4) : fftn;
     if (host) {
         if (!p->copy_stream) {
             CK(cudaStreamCreateWithFlags(&p->copy_stream, cudaStreamNonBlocking));
@@ -584,22 +585,31 @@ int fftso3_plan_create(fftso3_plan** out, int kind, int l_max, int batch, int pr
             // Chunks of 16 functions (two column tiles, whose items share each table tile through L2, so the
             // digit planes are read once per 16 functions) when the device has room for them with 16 GB to
             // spare after the FP64 table is freed, else 8 (one column tile), else fewer
-            const size_t per_fn = 16 * ((size_t)p->grid_elems + (size_t)p->coeff_elems);  // pencils + runs
+            // The spectral form (N = 64..512) needs the double-float pencils only as its FFT's work space
+            // (pen_fns = up to 8 functions at a time), so its contraction chunks grow to 32 functions (four column
+            // tiles sharing each table tile; the digit planes read once per 32 functions).
+            const bool spectral = fft_df32_k_supported(N);
+            const size_t pen_fn = 16 * (size_t)p->grid_elems, run_fn = 16 * (size_t)p->coeff_elems;
             const size_t planes = 4 * 2 * (size_t)(p->table_elems / N) * (size_t)((N + 63) / 64 * 64);
             const size_t tab64 = sizeof(double) * (size_t)p->table_elems;
             size_t freeb = 0, totb = 0;
             cudaMemGetInfo(&freeb, &totb);
             const size_t spare = (size_t)16 << 30, slack = (size_t)2 << 30;
-            size_t nch = 16;
-            while (nch > 1 && (planes + nch * per_fn + slack > freeb || freeb + tab64 < planes + nch * per_fn + spare))
-                nch = nch > 8 ? 8 : nch - 1;
+            auto need = [&](size_t nch) {
+                const size_t pens = spectral ? std::min<size_t>(nch, 8) : nch;
+                return planes + nch * run_fn + pens * pen_fn;
+            };
+            size_t nch = spectral ? 32 : 16;
+            while (nch > 1 && (need(nch) + slack > freeb || freeb + tab64 < need(nch) + spare))
+                nch = nch > 16 ? 16 : nch > 8 ? 8 : nch - 1;
             if (const char* ev = getenv("FFTSO3_REFINE_CHUNK")) {  // cap (1..16), e.g. to exercise several chunks
                 const int c = atoi(ev);
                 if (c >= 1 && (size_t)c < nch) nch = (size_t)c;
             }
             p->rchunk = (int)(nch < (size_t)batch ? nch : (size_t)batch);
+            const int pen_fns = spectral ? std::min(p->rchunk, 8) : p->rchunk;
             std::string err;
-            if ((rc = oz_create(&p->oz, p->d_table, goff, L, N, p->rchunk, p->d_tw, err))) {
+            if ((rc = oz_create(&p->oz, p->d_table, goff, L, N, p->rchunk, pen_fns, p->d_tw, err))) {
                 g_err = err;
                 return bail(rc);
             }

@@ -639,6 +639,7 @@ using namespace oz;
 
 struct OZState {
     int L = 0, N = 0, B = 0, ngroups = 0, chunk = 0, ntiles = 0, nsm = 0, Kp = 0;
+    int pen_fns = 0;  // functions the double-float pencil buffer holds
     long long total_rows = 0, C = 0;
     __nv_bfloat16* planes[NS] = {nullptr, nullptr, nullptr, nullptr};
     CUtensorMap tm[NS];
@@ -684,10 +685,10 @@ void oz_destroy(OZState* o)
 long long oz_device_bytes(const OZState* o) { return o ? o->bytes : 0; }
 
 int oz_create(OZState** out, const double* d_table, const std::vector<long long>& goff, int L, int N, int chunk,
-              const double* d_tw, std::string& err)
+              int pen_fns, const double* d_tw, std::string& err)
 {
     *out = nullptr;
-    if (!oz_supported(L, N) || chunk < 1) {
+    if (!oz_supported(L, N) || chunk < 1 || pen_fns < 1) {
         err = "internal: exact refinement inverse needs SO(3) l_max <= 255";
         return FFTSO3_ERR_UNSUPPORTED;
     }
@@ -697,6 +698,7 @@ int oz_create(OZState** out, const double* d_table, const std::vector<long long>
     o->N = N;
     o->ngroups = o->B * o->B;
     o->chunk = chunk;
+    o->pen_fns = pen_fns;
     o->ntiles = (chunk + FPT - 1) / FPT;
     o->Kp = (N + 63) / 64 * 64;
     o->C = so3_off(o->B);
@@ -777,7 +779,7 @@ int oz_create(OZState** out, const double* d_table, const std::vector<long long>
     const size_t grid = (size_t)N * N * N;
     if ((rc = oz_alloc(o, (void**)&o->Y, sizeof(float4) * (size_t)chunk * o->C, err))) return bail(rc);
     if ((rc = oz_alloc(o, (void**)&o->ey, (size_t)chunk * o->ngroups * 4, err))) return bail(rc);
-    if ((rc = oz_alloc(o, (void**)&o->pen, sizeof(float4) * (size_t)chunk * grid, err))) return bail(rc);
+    if ((rc = oz_alloc(o, (void**)&o->pen, sizeof(float4) * (size_t)pen_fns * grid, err))) return bail(rc);
     if ((rc = oz_alloc(o, (void**)&o->err, sizeof(int), err))) return bail(rc);
     cudaMemset(o->err, 0, sizeof(int));
     cudaError_t e = cudaFuncSetAttribute(oz_inv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
@@ -811,7 +813,7 @@ int oz_status(OZState* o)
 static int oz_contract(OZState* o, const void* F, bool f64, int nb, float2* rhi, const float2* rlo, cudaStream_t st,
                        StageTimer* T, std::string& err)
 {
-    if (nb < 1 || nb > o->chunk) {
+    if (nb < 1 || nb > o->chunk || (!rhi && nb > o->pen_fns)) {
         err = "internal: refinement chunk larger than its buffers";
         return FFTSO3_ERR_CUDA;
     }
@@ -867,11 +869,13 @@ static int oz_contract(OZState* o, const void* F, bool f64, int nb, float2* rhi,
 
 bool oz_spectral(const OZState* o) { return o && fft_df32_k_supported(o->N); }
 
+int oz_fft_functions(const OZState* o) { return o ? o->pen_fns : 0; }
+
 int oz_forward_fft(OZState* o, const void* fgrid, bool real, int nb, float2* hi, float2* lo, cudaStream_t st,
                    StageTimer* T, std::string& err)
 {
-    if (!oz_spectral(o) || nb < 1 || nb > o->chunk) {
-        err = "internal: double-float forward FFT needs N = 64..512 and nb <= chunk";
+    if (!oz_spectral(o) || nb < 1 || nb > o->pen_fns) {
+        err = "internal: double-float forward FFT needs N = 64..512 and nb <= its buffer's functions";
         return FFTSO3_ERR_CUDA;
     }
     T->begin(ST_REF_FFT, st);

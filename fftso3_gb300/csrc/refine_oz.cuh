@@ -14,9 +14,10 @@ struct OZState;
 // SO(3) with l_max <= 255 (at most 256 degrees per contraction keep the digit sums exact).
 bool oz_supported(int L, int N);
 // Builds the table's digit planes and exponents from the plan's FP64 Wigner-d table (goff: group offsets into
-// it) and buffers for `chunk` functions per call.
+// it), coefficient buffers for `chunk` functions per contraction and a double-float pencil buffer for pen_fns
+// functions (the grid form's synthesis needs pen_fns >= chunk; the spectral form's FFT runs pen_fns at a time).
 int oz_create(OZState** out, const double* d_table, const std::vector<long long>& goff, int L, int N, int chunk,
-              const double* d_tw, std::string& err);
+              int pen_fns, const double* d_tw, std::string& err);
 void oz_destroy(OZState* o);
 long long oz_device_bytes(const OZState* o);
 // Error word of the exact contraction kernel (a bounded wait that gave up); synchronising read.
@@ -32,6 +33,7 @@ int oz_inverse_resid(OZState* o, const void* F, bool f64, int nb, const void* fg
 // [fn][p][q][k] as hi (complex64) + lo (remainder).  oz_resid_pencils: hi := (hi + lo) - N^2 H(F) at every
 // pencil place the forward GEMM reads, for nb <= chunk coefficient sets F (as oz_inverse_resid).
 bool oz_spectral(const OZState* o);
+int oz_fft_functions(const OZState* o);
 int oz_forward_fft(OZState* o, const void* fgrid, bool real, int nb, float2* hi, float2* lo, cudaStream_t st,
                    StageTimer* T, std::string& err);
 int oz_resid_pencils(OZState* o, const void* F, bool f64, int nb, float2* hi, const float2* lo, cudaStream_t st,
