@@ -1087,6 +1087,7 @@ struct TCState {
     int n_items_fwd = 0, n_items_inv = 0;
     std::vector<int4> items_h[2];  // host copies (forward, inverse), for fused launches
     std::vector<int2> iaux_h[2];   // per item (goff2[g], grow0[g]), same order
+    std::vector<long long> h_goff2, h_grow0;  // host copies (the launch lists are rebuilt by the cluster tuner)
     int2* d_iaux_fwd = nullptr;
     int2* d_iaux_inv = nullptr;
     int nsm = 0;
@@ -1157,6 +1158,79 @@ void tc_destroy(TCState* s)
 long long tc_device_bytes(const TCState* s) { return s ? s->bytes : 0; }
 
 static int autotune_fft(TCState* s, std::string& err);
+static int autotune_cluster(TCState* s, std::string& err);
+static int launch_gemm(TCState* s, bool fwd, cudaStream_t st, std::string& err);
+static long long coeffs_per_fn(const TCState* s);
+static long long grid_per_fn(const TCState* s);
+
+// The tensor-core GEMM's launch lists for clusters of `csize` CTAs (a power of two <= column tiles): with
+// csize > 1, blocks of csize items (same group and row tile, consecutive column tiles; tiles past the batch
+// are empty) go to one cluster, which reads each table tile once for the block; csize = 1 takes the one-CTA
+// lists.  Replaces the device lists and sets s->csize.
+static int set_launch_lists(TCState* s, int csize, std::string& err)
+{
+    const int N = s->N;
+    std::vector<int4> itf, iti;
+    if (csize <= 1) {
+        itf = s->items_h[0];
+        iti = s->items_h[1];
+        csize = 1;
+    } else {
+        const int CLs = csize, ntb = (s->ntiles + CLs - 1) / CLs;
+        std::vector<std::vector<int4>> blocks;
+        for (int g = 0; g < s->ngroups; ++g) {
+            int m0 = g, n0 = 0;
+            if (!s->s2) group_mn(g, m0, n0);
+            const int nl = s->B - m0;
+            for (int mt = 0; mt * BM < nl; ++mt)
+                for (int b = 0; b < ntb; ++b)
+                    for (int r = 0; r < CLs; ++r) itf.push_back(make_int4(g, mt, b * CLs + r, item_w(m0, n0)));
+            for (int mt = 0; mt * BM < N; ++mt)
+                for (int b = 0; b < ntb; ++b) {
+                    std::vector<int4> blk;
+                    for (int r = 0; r < CLs; ++r) blk.push_back(make_int4(g, mt, b * CLs + r, item_w(m0, n0)));
+                    blocks.push_back(blk);
+                }
+        }
+        std::stable_sort(blocks.begin(), blocks.end(), [&](const std::vector<int4>& a, const std::vector<int4>& b) {
+            const int ma = a[0].w >> 16, mb = b[0].w >> 16;
+            return (s->B - ma + BK - 1) / BK > (s->B - mb + BK - 1) / BK;
+        });
+        for (const auto& blk : blocks) iti.insert(iti.end(), blk.begin(), blk.end());
+    }
+    std::vector<int2> auxf(itf.size()), auxi(iti.size());
+    for (size_t i = 0; i < itf.size(); ++i)
+        auxf[i] = make_int2((int)s->h_goff2[itf[i].x], (int)s->h_grow0[itf[i].x]);
+    for (size_t i = 0; i < iti.size(); ++i)
+        auxi[i] = make_int2((int)s->h_goff2[iti[i].x], (int)s->h_grow0[iti[i].x]);
+    // replace the device lists
+    auto drop = [&](void* p, size_t bytes) {
+        if (p) {
+            cudaFree(p);
+            s->bytes -= (long long)bytes;
+        }
+    };
+    drop(s->d_items_fwd, sizeof(int4) * (size_t)s->n_items_fwd);
+    drop(s->d_items_inv, sizeof(int4) * (size_t)s->n_items_inv);
+    drop(s->d_iaux_fwd, sizeof(int2) * (size_t)s->n_items_fwd);
+    drop(s->d_iaux_inv, sizeof(int2) * (size_t)s->n_items_inv);
+    s->d_items_fwd = s->d_items_inv = nullptr;
+    s->d_iaux_fwd = s->d_iaux_inv = nullptr;
+    s->n_items_fwd = s->n_items_inv = 0;
+    int rc;
+    if ((rc = tc_alloc(s, (void**)&s->d_items_fwd, sizeof(int4) * itf.size(), err))) return rc;
+    s->n_items_fwd = (int)itf.size();
+    if ((rc = tc_alloc(s, (void**)&s->d_iaux_fwd, sizeof(int2) * itf.size(), err))) return rc;
+    if ((rc = tc_alloc(s, (void**)&s->d_items_inv, sizeof(int4) * iti.size(), err))) return rc;
+    s->n_items_inv = (int)iti.size();
+    if ((rc = tc_alloc(s, (void**)&s->d_iaux_inv, sizeof(int2) * iti.size(), err))) return rc;
+    cudaMemcpy(s->d_items_fwd, itf.data(), sizeof(int4) * itf.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(s->d_items_inv, iti.data(), sizeof(int4) * iti.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(s->d_iaux_fwd, auxf.data(), sizeof(int2) * itf.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(s->d_iaux_inv, auxi.data(), sizeof(int2) * iti.size(), cudaMemcpyHostToDevice);
+    s->csize = csize;
+    return FFTSO3_SUCCESS;
+}
 
 int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64, const std::vector<long long>& goff,
               long long table_elems, const double* d_tw, const double* d_w, bool refine, bool real, bool s2,
@@ -1270,45 +1344,16 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
     });
     s->items_h[0] = itf;  // one-CTA order, for fused launches over several plans
     s->items_h[1] = iti;
-    // Launch lists.  With column tiles to share, clusters of C CTAs (C a power of two <= column tiles, at
-    // most FFTSO3_GEMM_CLUSTER, default 2) take blocks of C items (same group and row tile, consecutive
-    // column tiles; tiles past the batch are empty) and read each table tile once for the block.
+    // launch lists: clusters of C CTAs (C a power of two <= column tiles, at most FFTSO3_GEMM_CLUSTER, default
+    // 2) share each table tile; FFTSO3_FLAG_AUTOTUNE times C = 1, 2, 4 (below)
+    int csize0 = 1;
     {
         const char* ev = getenv("FFTSO3_GEMM_CLUSTER");
         int cmax = ev ? atoi(ev) : 2;
         cmax = cmax >= 4 ? 4 : cmax >= 2 ? 2 : 1;
-        int cl = 1;
         if (!simt)
-            while (cl * 2 <= cmax && cl * 2 <= s->ntiles) cl *= 2;
-        s->csize = cl;
+            while (csize0 * 2 <= cmax && csize0 * 2 <= s->ntiles) csize0 *= 2;
     }
-    if (s->csize > 1) {
-        const int CLs = s->csize, ntb = (s->ntiles + CLs - 1) / CLs;
-        std::vector<std::vector<int4>> blocks;
-        itf.clear();
-        for (int g = 0; g < s->ngroups; ++g) {
-            int m0 = g, n0 = 0;
-            if (!s2) group_mn(g, m0, n0);
-            const int nl = s->B - m0;
-            for (int mt = 0; mt * BM < nl; ++mt)
-                for (int b = 0; b < ntb; ++b)
-                    for (int r = 0; r < CLs; ++r) itf.push_back(make_int4(g, mt, b * CLs + r, item_w(m0, n0)));
-            for (int mt = 0; mt * BM < N; ++mt)
-                for (int b = 0; b < ntb; ++b) {
-                    std::vector<int4> blk;
-                    for (int r = 0; r < CLs; ++r) blk.push_back(make_int4(g, mt, b * CLs + r, item_w(m0, n0)));
-                    blocks.push_back(blk);
-                }
-        }
-        std::stable_sort(blocks.begin(), blocks.end(), [&](const std::vector<int4>& a, const std::vector<int4>& b) {
-            const int ma = a[0].w >> 16, mb = b[0].w >> 16;
-            return (s->B - ma + BK - 1) / BK > (s->B - mb + BK - 1) / BK;
-        });
-        iti.clear();
-        for (const auto& blk : blocks) iti.insert(iti.end(), blk.begin(), blk.end());
-    }
-    s->n_items_fwd = (int)itf.size();
-    s->n_items_inv = (int)iti.size();
     goff2[s->ngroups] = acc2;
     if (acc2 != C) {
         err = "internal: group-major layout does not cover the coefficients";
@@ -1325,23 +1370,15 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
             s->iaux_h[d][i] = make_int2((int)goff2[g], (int)grow0[g]);
         }
     }
-    std::vector<int2> auxf(itf.size()), auxi(iti.size());
-    for (size_t i = 0; i < itf.size(); ++i) auxf[i] = make_int2((int)goff2[itf[i].x], (int)grow0[itf[i].x]);
-    for (size_t i = 0; i < iti.size(); ++i) auxi[i] = make_int2((int)goff2[iti[i].x], (int)grow0[iti[i].x]);
+    s->h_goff2 = goff2;
+    s->h_grow0 = grow0;
     if ((rc = tc_alloc(s, (void**)&s->d_grow0, sizeof(long long) * grow0.size(), err))) return bail(rc);
     if ((rc = tc_alloc(s, (void**)&s->d_goff2, sizeof(long long) * goff2.size(), err))) return bail(rc);
     if ((rc = tc_alloc(s, (void**)&s->d_fg, sizeof(float2) * (size_t)batch * acc2, err))) return bail(rc);
     cudaMemcpy(s->d_goff2, goff2.data(), sizeof(long long) * goff2.size(), cudaMemcpyHostToDevice);
-    if ((rc = tc_alloc(s, (void**)&s->d_items_fwd, sizeof(int4) * itf.size(), err))) return bail(rc);
-    if ((rc = tc_alloc(s, (void**)&s->d_items_inv, sizeof(int4) * iti.size(), err))) return bail(rc);
-    if ((rc = tc_alloc(s, (void**)&s->d_iaux_fwd, sizeof(int2) * itf.size(), err))) return bail(rc);
-    if ((rc = tc_alloc(s, (void**)&s->d_iaux_inv, sizeof(int2) * iti.size(), err))) return bail(rc);
-    cudaMemcpy(s->d_iaux_fwd, auxf.data(), sizeof(int2) * itf.size(), cudaMemcpyHostToDevice);
-    cudaMemcpy(s->d_iaux_inv, auxi.data(), sizeof(int2) * iti.size(), cudaMemcpyHostToDevice);
+    if ((rc = set_launch_lists(s, csize0, err))) return bail(rc);
     if ((rc = tc_alloc(s, (void**)&s->d_err, sizeof(int), err))) return bail(rc);
     cudaMemcpy(s->d_grow0, grow0.data(), sizeof(long long) * grow0.size(), cudaMemcpyHostToDevice);
-    cudaMemcpy(s->d_items_fwd, itf.data(), sizeof(int4) * itf.size(), cudaMemcpyHostToDevice);
-    cudaMemcpy(s->d_items_inv, iti.data(), sizeof(int4) * iti.size(), cudaMemcpyHostToDevice);
     cudaMemset(s->d_err, 0, sizeof(int));
     for (int p = 0; p < 3 && !simt; ++p) {
         bool ok = tc_encode_bf16_2d(&s->tmA_fwd[p], s->d_tab[p], s->Kp, s->total_rows, 64, BM) &&
@@ -1365,6 +1402,8 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
     }
     if (autotune && !fft_fast_supported(N))
         if ((rc = autotune_fft(s, err))) return bail(rc);
+    if (autotune && !simt && s->ntiles > 1)
+        if ((rc = autotune_cluster(s, err))) return bail(rc);
     *out = s;
     return FFTSO3_SUCCESS;
 }
@@ -1488,6 +1527,75 @@ static int autotune_fft(TCState* s, std::string& err)
     cudaEventDestroy(e1);
     cudaStreamDestroy(st);
     return rc;
+}
+
+// FFTSO3_FLAG_AUTOTUNE: the GEMM's cluster size (1, 2 or 4 CTAs sharing each table tile, at most the column
+// tiles), timed on the plan's own buffers (one warm-up, then two forward and two inverse GEMMs each, CUDA
+// events; the buffers' contents do not matter to the timing and are overwritten by every call), cached per
+// (l_max, batch, family) for the process.
+static std::map<std::tuple<int, int, bool>, int> g_cluster_cache;
+
+static int autotune_cluster(TCState* s, std::string& err)
+{
+    const auto key = std::make_tuple(s->L, s->batch, s->s2);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mutex);
+        auto it = g_cluster_cache.find(key);
+        if (it != g_cluster_cache.end()) return it->second == s->csize ? FFTSO3_SUCCESS : set_launch_lists(s, it->second, err);
+    }
+    cudaStream_t st;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+        err = "autotune: cudaStreamCreate";
+        return FFTSO3_ERR_CUDA;
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaMemsetAsync(s->d_pencil, 0, sizeof(float2) * (size_t)s->batch * grid_per_fn(s), st);
+    cudaMemsetAsync(s->d_fg, 0, sizeof(float2) * (size_t)s->batch * coeffs_per_fn(s), st);
+    const int first = s->csize;
+    float best = 1e30f;
+    int bestc = first, rc = FFTSO3_SUCCESS;
+    for (int c = 1; c <= 4 && c <= s->ntiles && rc == FFTSO3_SUCCESS; c *= 2) {
+        if ((rc = set_launch_lists(s, c, err))) break;
+        if ((rc = launch_gemm(s, true, st, err)) || (rc = launch_gemm(s, false, st, err))) {
+            if (rc == FFTSO3_ERR_UNSUPPORTED) {  // no cluster of c CTAs fits: not a candidate
+                rc = FFTSO3_SUCCESS;
+                cudaGetLastError();
+                continue;
+            }
+            break;
+        }
+        cudaEventRecord(e0, st);
+        for (int r = 0; r < 2 && rc == FFTSO3_SUCCESS; ++r)
+            if ((rc = launch_gemm(s, true, st, err)) == FFTSO3_SUCCESS) rc = launch_gemm(s, false, st, err);
+        cudaEventRecord(e1, st);
+        if (rc) break;
+        if (cudaEventSynchronize(e1) != cudaSuccess) {
+            err = std::string("autotune: ") + cudaGetErrorString(cudaGetLastError());
+            rc = FFTSO3_ERR_CUDA;
+            break;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) {
+            best = ms;
+            bestc = c;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamDestroy(st);
+    if (rc) return rc;
+    if (tc_status(s) != 0) {
+        err = "autotune: the tensor-core GEMM gave up a bounded wait";
+        return FFTSO3_ERR_CUDA;
+    }
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mutex);
+        g_cluster_cache[key] = bestc;
+    }
+    return set_launch_lists(s, bestc, err);
 }
 
 #define TCK(call)                                                          \
