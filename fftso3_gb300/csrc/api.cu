@@ -347,6 +347,20 @@ int refine_forward_spectral(fftso3_plan* p, const void* grid, void* coeffs, cuda
                                 g_err);
         if (rc) return rc;
     }
+    if (!p->real) {
+        // complex: F0 stays group-major (the GEMM's layout, which the contraction reads as runs); one permutation
+        // of F0 + correction at the end
+        const float2* Fg = tc_group_buffer(p->tc);
+        int rc = tc_gemm_forward_group(p->tc, st, &T, g_err);
+        if (rc) return rc;
+        for (int f0 = 0; f0 < p->batch; f0 += p->rchunk) {
+            const int nb = p->batch - f0 < p->rchunk ? p->batch - f0 : p->rchunk;
+            if ((rc = oz_resid_pencils(p->oz, Fg + (long long)f0 * C, false, nb, hi + (long long)f0 * G,
+                                       lo + (long long)f0 * G, st, &T, g_err, true)))
+                return rc;
+        }
+        return tc_refine_finish_group(p->tc, coeffs, st, &T, g_err);
+    }
     int rc = tc_forward_pencils(p->tc, coeffs, st, &T, g_err);
     if (rc) return rc;
     for (int f0 = 0; f0 < p->batch; f0 += p->rchunk) {

@@ -1159,7 +1159,7 @@ long long tc_device_bytes(const TCState* s) { return s ? s->bytes : 0; }
 
 static int autotune_fft(TCState* s, std::string& err);
 static int autotune_cluster(TCState* s, std::string& err);
-static int launch_gemm(TCState* s, bool fwd, cudaStream_t st, std::string& err);
+static int launch_gemm(TCState* s, bool fwd, cudaStream_t st, std::string& err, float2* cout = nullptr);
 static long long coeffs_per_fn(const TCState* s);
 static long long grid_per_fn(const TCState* s);
 
@@ -1631,7 +1631,8 @@ static GemmArgs gemm_args(const TCState* s)
     return a;
 }
 
-static int launch_gemm(TCState* s, bool fwd, cudaStream_t st, std::string& err)
+// cout: the forward's group-major output (default: the plan's d_fg)
+static int launch_gemm(TCState* s, bool fwd, cudaStream_t st, std::string& err, float2* cout)
 {
     GemmArgs a = gemm_args(s);
     a.items = fwd ? s->d_items_fwd : s->d_items_inv;
@@ -1639,7 +1640,7 @@ static int launch_gemm(TCState* s, bool fwd, cudaStream_t st, std::string& err)
     a.nitems = fwd ? s->n_items_fwd : s->n_items_inv;
     if (fwd) {
         a.pin = s->d_pencil;
-        a.cout = s->d_fg;
+        a.cout = cout ? cout : s->d_fg;
     } else {
         a.cin = s->d_fg;
         a.pout = s->d_pencil;
@@ -1885,6 +1886,40 @@ int tc_forward_pencils(TCState* s, void* coeffs, cudaStream_t st, StageTimer* T,
         return FFTSO3_ERR_CUDA;
     }
     return forward_from_pencils(s, coeffs, st, T, err);
+}
+
+float2* tc_group_buffer(TCState* s) { return s ? s->d_fg : nullptr; }
+
+int tc_gemm_forward_group(TCState* s, cudaStream_t st, StageTimer* T, std::string& err)
+{
+    T->begin(ST_GEMM_FWD, st);
+    int rc = launch_gemm(s, true, st, err);
+    if (rc) return rc;
+    T->end(st);
+    return FFTSO3_SUCCESS;
+}
+
+int tc_refine_finish_group(TCState* s, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err)
+{
+    if (!s->refine || !s->d_coef2 || s->s2 || s->real) {
+        err = "internal: group-major refinement is for complex SO(3) refined plans";
+        return FFTSO3_ERR_CUDA;
+    }
+    // the correction's GEMM into d_coef2 (group-major), added to F0 in d_fg, then one permutation
+    T->begin(ST_GEMM_FWD, st);
+    int rc = launch_gemm(s, true, st, err, s->d_coef2);
+    if (rc) return rc;
+    T->end(st);
+    const long long nc = (long long)s->batch * coeffs_per_fn(s);
+    T->begin(ST_REFINE, st);
+    TCK(launch_add_real((float*)s->d_fg, (const float*)s->d_coef2, 2 * nc, st));
+    T->end(st);
+    T->begin(ST_BASIS, st);
+    group_to_packed_tiled<<<ptile_grid(s->L, s->batch), 256, 0, st>>>(s->d_fg, (float2*)coeffs, s->d_goff2, s->L,
+                                                                      coeffs_per_fn(s), s->batch);
+    TCK(cudaGetLastError());
+    T->end(st);
+    return FFTSO3_SUCCESS;
 }
 
 int tc_refine_add_pencils(TCState* s, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err)

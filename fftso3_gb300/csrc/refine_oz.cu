@@ -116,6 +116,10 @@ __device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefe
 // 2^e as a float for e in [-126, 127] (exact)
 __device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + e) << 23); }
 
+// x 2^e, as ldexpf but one multiplication while 2^e is a normal float (the product of x and an exact power of
+// two is the correctly rounded x 2^e, as ldexpf's)
+__device__ __forceinline__ float scale2(float x, int e) { return (e >= -126 && e <= 127) ? x * pow2f(e) : ldexpf(x, e); }
+
 // Digits of x = (h + l) sc (|x| <= 1): x 2^7 = s0 + s1 2^-8 + s2 2^-16 + s3 2^-24 + rest,
 // each |s_i| <= 128 an integer (exact in BF16); every step but the first is exact in FP32.
 __device__ __forceinline__ void digits4(float h, float l, float sc, float (&s)[NS])
@@ -445,11 +449,11 @@ __global__ void __launch_bounds__(THREADS, 1)
                             const int E2 = E + a.e2n;
                             const float2 h = sh[p], l = sl[p];
                             __stcs(a.rhi + fo + poff[p],
-                                   make_float2((h.x - ldexpf(re.h, E2)) + (l.x - ldexpf(re.l, E2)),
-                                               (h.y - ldexpf(im.h, E2)) + (l.y - ldexpf(im.l, E2))));
+                                   make_float2((h.x - scale2(re.h, E2)) + (l.x - scale2(re.l, E2)),
+                                               (h.y - scale2(im.h, E2)) + (l.y - scale2(im.l, E2))));
                         } else {
                             a.pout[fo + poff[p]] =
-                                make_float4(ldexpf(re.h, E), ldexpf(re.l, E), ldexpf(im.h, E), ldexpf(im.l, E));
+                                make_float4(scale2(re.h, E), scale2(re.l, E), scale2(im.h, E), scale2(im.l, E));
                         }
                     }
                 }
@@ -531,7 +535,8 @@ __global__ void table_digits_kernel(const double* __restrict__ table, const long
 // One warp per (function, group): the group's coefficient runs (2l+1) sign F(l, pair), l = m0..L, as
 // double-float (group-major, as the tensor-core path's layout; for FP32 input the product is exact:
 // h = fl(c v), l = fma(c, v, -h)) and one exponent per pair with max |value| < 2^E.
-template <typename CIN>
+// GROUP: F is already group-major (the forward GEMM's output), read as runs; else packed.
+template <typename CIN, bool GROUP = false>
 __global__ void gather_kernel(const CIN* __restrict__ F, long long cstride, float4* __restrict__ Y,
                               signed char* __restrict__ ey, const long long* __restrict__ goff2, int L, int ngroups,
                               int nb)
@@ -551,7 +556,7 @@ __global__ void gather_kernel(const CIN* __restrict__ F, long long cstride, floa
         if (p < P.np) {
             for (int li = lane; li < nl; li += 32) {
                 const int l = m0 + li;
-                const CIN v = Fb[so3_idx(l, P.m[p], P.n[p])];
+                const CIN v = GROUP ? Fb[goff2[g] + (long long)p * nl + li] : Fb[so3_idx(l, P.m[p], P.n[p])];
                 df32 re, im;
                 if constexpr (sizeof(v.x) == 8) {
                     re = df32((double)(2 * l + 1) * (double)v.x);
@@ -811,7 +816,7 @@ int oz_status(OZState* o)
 // coefficients -> double-float group-major runs and their exponents, then the exact contraction: H into the
 // double-float pencils (rhi null), or the spectral residual into rhi
 static int oz_contract(OZState* o, const void* F, bool f64, int nb, float2* rhi, const float2* rlo, cudaStream_t st,
-                       StageTimer* T, std::string& err)
+                       StageTimer* T, std::string& err, bool group = false)
 {
     if (nb < 1 || nb > o->chunk || (!rhi && nb > o->pen_fns)) {
         err = "internal: refinement chunk larger than its buffers";
@@ -826,6 +831,9 @@ static int oz_contract(OZState* o, const void* F, bool f64, int nb, float2* rhi,
         if (f64)
             gather_kernel<double2><<<blocks, 256, 0, st>>>((const double2*)F, o->C, o->Y, o->ey, o->goff2, L,
                                                            o->ngroups, nb);
+        else if (group)
+            gather_kernel<float2, true><<<blocks, 256, 0, st>>>((const float2*)F, o->C, o->Y, o->ey, o->goff2, L,
+                                                                o->ngroups, nb);
         else
             gather_kernel<float2><<<blocks, 256, 0, st>>>((const float2*)F, o->C, o->Y, o->ey, o->goff2, L, o->ngroups,
                                                           nb);
@@ -885,13 +893,13 @@ int oz_forward_fft(OZState* o, const void* fgrid, bool real, int nb, float2* hi,
 }
 
 int oz_resid_pencils(OZState* o, const void* F, bool f64, int nb, float2* hi, const float2* lo, cudaStream_t st,
-                     StageTimer* T, std::string& err)
+                     StageTimer* T, std::string& err, bool group_major)
 {
-    if (!oz_spectral(o)) {
-        err = "internal: spectral residual needs N = 64..512";
+    if (!oz_spectral(o) || (group_major && f64)) {
+        err = "internal: spectral residual needs N = 64..512 (group-major input: complex64)";
         return FFTSO3_ERR_CUDA;
     }
-    return oz_contract(o, F, f64, nb, hi, lo, st, T, err);
+    return oz_contract(o, F, f64, nb, hi, lo, st, T, err, group_major);
 }
 
 int oz_inverse_resid(OZState* o, const void* F, bool f64, int nb, const void* fgrid, bool real, float* resid,

@@ -36,7 +36,8 @@ bool oz_spectral(const OZState* o);
 int oz_fft_functions(const OZState* o);
 int oz_forward_fft(OZState* o, const void* fgrid, bool real, int nb, float2* hi, float2* lo, cudaStream_t st,
                    StageTimer* T, std::string& err);
+// group_major: F (complex64) is group-major, the forward GEMM's own output layout, instead of packed.
 int oz_resid_pencils(OZState* o, const void* F, bool f64, int nb, float2* hi, const float2* lo, cudaStream_t st,
-                     StageTimer* T, std::string& err);
+                     StageTimer* T, std::string& err, bool group_major = false);
 
 }  // namespace fftso3

@@ -29,6 +29,12 @@ int tc_refine_add(TCState* s, const void* resid, void* coeffs, cudaStream_t st, 
 float2* tc_pencil_buffer(TCState* s);
 int tc_forward_pencils(TCState* s, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err);
 int tc_refine_add_pencils(TCState* s, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err);
+// Complex SO(3) refined plans, group-major form: F0 = the forward GEMM of the pencils, left group-major in the
+// plan's group buffer (the exact contraction reads it there); then the correction's GEMM, F0 + correction, and one
+// permutation into the packed coefficients.
+float2* tc_group_buffer(TCState* s);
+int tc_gemm_forward_group(TCState* s, cudaStream_t st, StageTimer* T, std::string& err);
+int tc_refine_finish_group(TCState* s, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err);
 // Device error word of the tensor-core kernels (0 = no bounded wait timed out); synchronising read.
 int tc_status(TCState* s);
 
