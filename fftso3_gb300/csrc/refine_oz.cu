@@ -116,10 +116,6 @@ __device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefe
 // 2^e as a float for e in [-126, 127] (exact)
 __device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + e) << 23); }
 
-// x 2^e, as ldexpf but one multiplication while 2^e is a normal float (the product of x and an exact power of
-// two is the correctly rounded x 2^e, as ldexpf's)
-__device__ __forceinline__ float scale2(float x, int e) { return (e >= -126 && e <= 127) ? x * pow2f(e) : ldexpf(x, e); }
-
 // Digits of x = (h + l) sc (|x| <= 1): x 2^7 = s0 + s1 2^-8 + s2 2^-16 + s3 2^-24 + rest,
 // each |s_i| <= 128 an integer (exact in BF16); every step but the first is exact in FP32.
 __device__ __forceinline__ void digits4(float h, float l, float sc, float (&s)[NS])
@@ -449,11 +445,11 @@ __global__ void __launch_bounds__(THREADS, 1)
                             const int E2 = E + a.e2n;
                             const float2 h = sh[p], l = sl[p];
                             __stcs(a.rhi + fo + poff[p],
-                                   make_float2((h.x - scale2(re.h, E2)) + (l.x - scale2(re.l, E2)),
-                                               (h.y - scale2(im.h, E2)) + (l.y - scale2(im.l, E2))));
+                                   make_float2((h.x - ldexpf(re.h, E2)) + (l.x - ldexpf(re.l, E2)),
+                                               (h.y - ldexpf(im.h, E2)) + (l.y - ldexpf(im.l, E2))));
                         } else {
                             a.pout[fo + poff[p]] =
-                                make_float4(scale2(re.h, E), scale2(re.l, E), scale2(im.h, E), scale2(im.l, E));
+                                make_float4(ldexpf(re.h, E), ldexpf(re.l, E), ldexpf(im.h, E), ldexpf(im.l, E));
                         }
                     }
                 }
