@@ -233,6 +233,34 @@ def test_gemm_clusters_bitwise_equal_single_cta(gblib, torch_cuda, monkeypatch, 
     assert torch.equal(out[0][1], out[1][1])
 
 
+def test_gemm_cluster_autotune_bitwise_equal(gblib, torch_cuda):
+    """FFTSO3_FLAG_AUTOTUNE times GEMM clusters of 1, 2 and 4 CTAs on the plan's own buffers and keeps the fastest;
+    whichever it keeps, the results equal the untuned plan's bit for bit (64 functions at l_max = 63: four column
+    tiles, so all three cluster sizes are candidates), and a second tuned plan of the same shape reuses the
+    choice."""
+    torch = torch_cuda
+    L, b = 63, 64
+    N = 2 * (L + 1)
+    C = b * ((L + 1) * (4 * (L + 1) ** 2 - 1) // 3)
+    gen = torch.Generator(device="cuda").manual_seed(7)
+    grid = torch.randn(b * N ** 3, dtype=torch.complex64, device="cuda", generator=gen)
+    coef = torch.randn(C, dtype=torch.complex64, device="cuda", generator=gen)
+    s = torch.cuda.current_stream().cuda_stream
+    out = []
+    for flags in (0, gblib.FLAG_AUTOTUNE, gblib.FLAG_AUTOTUNE):
+        p = gblib.Plan(gblib.SO3_COMPLEX, L, b, "tc_bf16x3", "stable", flags)
+        g = torch.empty_like(grid)
+        co = torch.empty_like(coef)
+        p.inverse(coef.data_ptr(), g.data_ptr(), s)
+        p.forward(grid.data_ptr(), co.data_ptr(), s)
+        p.check()
+        out.append((g.cpu(), co.cpu()))
+        del p
+    for o in out[1:]:
+        assert torch.equal(out[0][0], o[0])
+        assert torch.equal(out[0][1], o[1])
+
+
 @pytest.mark.parametrize("kind", ["complex", "real"])
 def test_tc_round_trip_lmax255(gblib, torch_cuda, kind):
     """The headline size, l_max = 255 (512^3 grid, one-launch FFT at N = 512, clusters off at batch 1):
