@@ -248,7 +248,6 @@ __device__ void dft_prime_first_t(const typename V2<T>::t* __restrict__ src, typ
             }
         }
         const C* m = mat + blk * GP;
-#pragma unroll 2
         for (int t = 1; t <= P; ++t, m += MS) {
             C a[LPT], bb[LPT];
 #pragma unroll
