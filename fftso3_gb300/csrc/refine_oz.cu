@@ -316,18 +316,6 @@ __global__ void __launch_bounds__(THREADS, 1)
                     snxt = source(item2, a.iaux[it2]);
                     nk2 = nsteps(item2);
                 }
-                // the runs of the item after that, requested into L2 an item ahead of their loads (one 128-byte
-                // line per k-step and thread)
-                const int it3 = it2 + (int)gridDim.x;
-                if (it3 < a.nitems) {
-                    const int4 item3 = a.items[it3];
-                    const Src s3 = source(item3, a.iaux[it3]);
-                    if (s3.p) {
-                        const int nk3 = nsteps(item3);
-                        for (int i3 = 0; i3 < nk3; ++i3)
-                            if (i3 * BK + q8 * 8 < s3.lim) prefetch_l2(s3.p + i3 * BK + q8 * 8);
-                    }
-                }
             }
             float4 nxt[8];
             if (it2 < a.nitems) fetch(snxt, i2, nxt);
