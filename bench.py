@@ -933,7 +933,7 @@ def stage_roofline(name: str, tot_ms: float, cnt: int, L: int, b: int, chunk: in
     flops = None
     if name.startswith("tc_gemm"):
         flops, alg = 8.0 * B * C * b, "8 B C useful flops per function per launch (6 split-BF16 products issued)"
-    elif name == "refine_exact_contract":
+    elif name in ("refine_exact_contract", "exact_inverse_contract"):
         flops, alg = 8.0 * B * C * chunk, "8 B C useful flops per function of the chunk (10 digit products issued)"
     if flops is not None:
         ach = flops / per / 1e12
@@ -949,6 +949,10 @@ def stage_roofline(name: str, tot_ms: float, cnt: int, L: int, b: int, chunk: in
         byts, alg = (8.0 + 16 + 16 + 16) * (piece or chunk) * N ** 3, ("double-float forward FFT of the samples: pass 1 reads "
                                                           "8 B, writes 16 B; pass 2 reads 16 B, writes hi + lo "
                                                           "8 + 8 B per sample")
+    elif name == "exact_inverse_fft_df32":
+        byts, alg = (16.0 + 16 + 16 + 8) * (piece or chunk) * N ** 3, ("double-float FFT of the synthesis: pass 1 "
+                                                                    "reads and writes 16 B; pass 2 reads 16 B, "
+                                                                    "writes the complex64 grid (8 B) per sample")
     elif name == "basis_convert":
         byts, alg = 2 * 8.0 * C * b, "one complex64 read + write of the coefficients"
     else:
@@ -1063,8 +1067,8 @@ def so3_tc_line(args, L: int, b: int, full: bool = True) -> dict:
         plan.check()
         return t, st, (clk.summary() if clk else None)
 
-    # ---- the measured plan: refined forward (headline) or plain split-BF16
-    flags = _lib.FLAG_AUTOTUNE | (_lib.FLAG_REFINE if full else 0)
+    # ---- the measured plan: refined forward and exact inverse (headline) or plain split-BF16
+    flags = _lib.FLAG_AUTOTUNE | (_lib.FLAG_REFINE | _lib.FLAG_EXACT_INVERSE if full else 0)
     plan = _lib.Plan(_lib.SO3_COMPLEX, L, b, "tc_bf16x3", "stable", flags)
     plan.inverse(coef.data_ptr(), grid.data_ptr(), sp)  # synthetic band-limited FP32 samples
     if have_ref:
@@ -1085,16 +1089,20 @@ def so3_tc_line(args, L: int, b: int, full: bool = True) -> dict:
     chunk = -(-b // nchunks)  # functions per exact-contraction launch
     npieces = max(1, round(stages.get("refine_fft_df32", (0, args.steps))[1] / args.steps))
     piece = -(-b // npieces)  # functions per double-float FFT record
+    nichunks = max(1, round(stages.get("exact_inverse_contract", (0, args.steps))[1] / args.steps))
+    ichunk = -(-b // nichunks)  # functions per exact-inverse chunk (contraction and double-float FFT records)
     nrec = int(sum(c for _, c in stages.values()))
     # kernels in the timed region: one per timed record, plus the second kernel of the records that hold two
-    # (the double-float FFT's two passes, one record per chunk)
-    launches = nrec + int(stages.get("refine_fft_df32", (0, 0))[1])
+    # (the double-float FFTs' two passes; the gather and Nyquist zeroing before each exact-inverse contraction)
+    launches = nrec + int(stages.get("refine_fft_df32", (0, 0))[1]) + \
+        int(stages.get("exact_inverse_fft_df32", (0, 0))[1]) + int(stages.get("exact_inverse_contract", (0, 0))[1])
     tot = sum(v for v, _ in stages.values())
     stage_summary = {k: {"ms_per_launch": v / c, "launches": c, "share": v / tot} for k, (v, c) in stages.items()}
     top, (top_ms, top_n) = max(stages.items(), key=lambda kv: kv[1][0])
-    roof = stage_roofline(top, top_ms, top_n, L, b, chunk, peaks, piece)
-    roof["traffic"] = profiled_traffic(top, L, (piece if top == "refine_fft_df32" else chunk)
-                                       if top.startswith("refine") else b)  # refinement: per launch record
+    per_record = {"refine_fft_df32": piece, "refine_exact_contract": chunk, "exact_inverse_fft_df32": ichunk,
+                  "exact_inverse_contract": ichunk}
+    roof = stage_roofline(top, top_ms, top_n, L, b, per_record.get(top, chunk), peaks, per_record.get(top, 0))
+    roof["traffic"] = profiled_traffic(top, L, per_record.get(top, b))  # functions per launch record
     roof["share_of_step"] = top_ms / tot
 
     # ---- the step against its floors: HBM (algorithmic bytes of every stage) and tensor (issued MMA flops)
@@ -1120,6 +1128,14 @@ def so3_tc_line(args, L: int, b: int, full: bool = True) -> dict:
                        + gemm_dir                                  # the residual's forward
                        + 3 * coef_b)                               # correction added
         tensor_flops += 6 * useful + 10 * useful
+        # the exact inverse replaces the split-BF16 inverse: gather, exact synthesis contraction (digit planes per
+        # chunk, double-float runs in, double-float pencils out), double-float FFT rounded into the grid
+        step_bytes += (-tc_dir
+                       + coef_b + 2 * 16.0 * b * C                 # gather
+                       + nichunks * 4 * 2.0 * Kp * table_rows      # digit planes
+                       + 16.0 * b * C + 2 * grid_b                 # runs in, 16 B per pencil place out
+                       + 7 * grid_b)                               # FFT: 16 + 16 B, then 16 B in, 8 B out
+        tensor_flops += -6 * useful + 10 * useful
     hbm_floor_ms = step_bytes / (peaks["hbm_gbs"] * 1e9) * 1e3
     tensor_floor_ms = tensor_flops / (peaks["bf16_tflops_sustained"] * 1e12) * 1e3
     floor_ms = max(hbm_floor_ms, tensor_floor_ms)
@@ -1131,7 +1147,9 @@ def so3_tc_line(args, L: int, b: int, full: bool = True) -> dict:
                                                            "(56 B per sample), two GEMMs + permutations, the "
                                                            "exact synthesis contraction (digit planes per chunk, "
                                                            "double-float runs, 24 B per sample of pencils) and "
-                                                           "the correction" if full else "")}
+                                                           "the correction; exact inverse: the exact synthesis "
+                                                           "contraction (16 B per pencil place out) and the "
+                                                           "double-float FFT (56 B per sample)" if full else "")}
 
     # ---- end to end through the host-buffer C ABI (pinned host memory), the same plan and step count
     e2e = None
@@ -1158,9 +1176,20 @@ def so3_tc_line(args, L: int, b: int, full: bool = True) -> dict:
     del plan
     torch.cuda.empty_cache()
 
-    # ---- beside the headline: the plain split-BF16 step (no refinement) and the FP32 CUDA-core form
-    plain = fp32 = None
+    # ---- beside the headline: the refined forward with the split-BF16 inverse, the plain split-BF16 step (no
+    # refinement) and the FP32 CUDA-core form
+    plain = fp32 = fwdonly = None
     if full:
+        pf = _lib.Plan(_lib.SO3_COMPLEX, L, b, "tc_bf16x3", "stable", _lib.FLAG_AUTOTUNE | _lib.FLAG_REFINE)
+        facc = accuracy(pf) if have_ref else {}
+        fms, fst, _ = timed(pf, args.steps, min(args.warmup, 3))
+        fwdonly = {"value": b * 1000.0 / fms, "unit": UNIT, "ms_per_step": fms, "accuracy": facc,
+                   "stages": {k: {"ms_per_launch": v / c, "launches": c} for k, (v, c) in fst.items()},
+                   "note": "FFTSO3_FLAG_REFINE only: the refined forward meets 1e-6 per degree, the split-BF16 "
+                           "inverse's FP32 FFT leaves grid errors above 1e-6 of the rms (inverse_rel_max)"}
+        pf.close()
+        del pf
+        torch.cuda.empty_cache()
         pp = _lib.Plan(_lib.SO3_COMPLEX, L, b, "tc_bf16x3", "stable", _lib.FLAG_AUTOTUNE)
         pacc = accuracy(pp) if have_ref else {}
         pms, pst, _ = timed(pp, args.steps, min(args.warmup, 3))
@@ -1186,19 +1215,22 @@ def so3_tc_line(args, L: int, b: int, full: bool = True) -> dict:
 
     cpu = cpu_baselines(L) if not args.no_cpu else None
     metric = METRIC if L == 255 else METRIC.replace("l_max=255", f"l_max={L}")
-    what = ("inverse (split-BF16) + refined forward (double-float FFT of the samples, split-BF16 GEMM, the residual "
-            "against the exact tensor-core synthesis formed in the pencil domain, split-BF16 GEMM of the residual)"
+    what = ("exact inverse (exact tensor-core synthesis contraction, double-float FFT, one rounding to complex64) + "
+            "refined forward (double-float FFT of the samples, split-BF16 GEMM, the residual against the exact "
+            "tensor-core synthesis formed in the pencil domain, split-BF16 GEMM of the residual)"
             if full else "inverse + forward, split-BF16")
     line = {
         "metric": metric, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "bf16x3 (split) / fp32 accumulate / fp32 FFT" +
-                                      ("; refined forward: double-float FFT, exact BF16 digit products" if full else ""),
+                                      ("; refined forward and exact inverse: double-float FFTs, exact BF16 digit "
+                                       "products" if full else ""),
         "data": "synthetic",
         "config": {"workload": f"SO(3) complex, l_max={L}, batch={b} functions ({N}^3 complex64 grid each), stable "
                                f"recursion; one step = {what}",
-                   "l_max": L, "batch": b, "precision": "tc_bf16x3" + (" + refine" if full else ""),
+                   "l_max": L, "batch": b, "precision": "tc_bf16x3" + (" + refine + exact inverse" if full else ""),
                    "refine_chunk": chunk if full else None, "refine_fft_piece": piece if full else None,
+                   "exact_inverse_chunk": ichunk if full else None,
                    "l2": f"inputs larger than L2 ({8.0 * b * N ** 3 / 1e9:.1f} GB of complex64 grids)"},
         "e2e": e2e, "gpu_launches": launches, "roofline": roof, "step_roofline": step_roof,
         "stages": stage_summary, "accuracy": acc, "fp64_path": fp64,
@@ -1206,6 +1238,7 @@ def so3_tc_line(args, L: int, b: int, full: bool = True) -> dict:
         "clocks": clocks, "cpu_baseline": cpu,
     }
     if full:
+        line["refined_forward_plain_inverse_path"] = fwdonly
         line["unrefined_path"] = plain
         line["fp32_cuda_core_path"] = fp32
     return line

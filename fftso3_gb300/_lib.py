@@ -34,6 +34,7 @@ RECURSION_STABLE = 1
 FLAG_REFINE = 0x1
 FLAG_GRAPH = 0x2
 FLAG_AUTOTUNE = 0x4
+FLAG_EXACT_INVERSE = 0x8
 
 PRECISIONS = {"fp64": PREC_FP64, "tc_bf16x3": PREC_TC_BF16X3, "fp32": PREC_FP32}
 RECURSIONS = {"reference": RECURSION_REFERENCE, "stable": RECURSION_STABLE}

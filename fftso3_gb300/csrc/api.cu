@@ -411,8 +411,49 @@ int run_forward(fftso3_plan* p, const void* grid, void* coeffs, cudaStream_t st)
     return FFTSO3_SUCCESS;
 }
 
+// FFTSO3_FLAG_EXACT_INVERSE: the synthesis without FP32 rounding -- SO(3), l_max <= 255: exact digit sums on the
+// tensor cores and a double-float FFT, a contraction chunk of functions at a time, the double-float pencils in
+// the plan's pencil + residual buffers; otherwise the FP64 inverse in chunks of rchunk functions -- rounded once
+// into the FP32 grid.
+int exact_inverse(fftso3_plan* p, const void* coeffs, void* grid, cudaStream_t st)
+{
+    StageTimer& T = p->timer;
+    const long long C = p->coeff_elems, G = p->grid_elems;
+    const int per = p->real ? 1 : 2;  // floats per element
+    if (p->oz) {
+        void* pen = tc_exact_buffer(p->tc);
+        const int fftn = pen ? p->rchunk : oz_fft_functions(p->oz);
+        for (int f0 = 0; f0 < p->batch; f0 += fftn) {
+            const int nb = p->batch - f0 < fftn ? p->batch - f0 : fftn;
+            const void* Fc = (const float2*)coeffs + (long long)f0 * C;
+            if (p->real) {
+                STAGE(ST_BASIS, launch_widen((const float*)coeffs + (long long)f0 * C, (double*)p->d_rc,
+                                             (long long)nb * C, st));
+                STAGE(ST_BASIS, launch_so3_r2c(p->d_rc, p->d_rfc, true, p->L, nb, st));
+                Fc = p->d_rfc;
+            }
+            int rc = oz_inverse_exact(p->oz, Fc, p->real, nb, (float*)grid + (long long)f0 * G * per, p->real, st,
+                                      &T, g_err, pen);
+            if (rc) return rc;
+        }
+        return FFTSO3_SUCCESS;
+    }
+    for (int f0 = 0; f0 < p->batch; f0 += p->rchunk) {
+        const int nb = p->batch - f0 < p->rchunk ? p->batch - f0 : p->rchunk;
+        STAGE(ST_BASIS, launch_widen((const float*)coeffs + (long long)f0 * C * per, (double*)p->d_rc,
+                                     (long long)nb * C * per, st));
+        void* g64 = p->real ? p->d_rg : p->d_rw;
+        int rc = fp64_inverse(p, p->d_rc, g64, nb, p->d_rw, p->d_rfc, false, st);
+        if (rc) return rc;
+        STAGE(ST_BASIS, launch_narrow((const double*)g64, (float*)grid + (long long)f0 * G * per,
+                                      (long long)nb * G * per, st));
+    }
+    return FFTSO3_SUCCESS;
+}
+
 int run_inverse(fftso3_plan* p, const void* coeffs, void* grid, cudaStream_t st)
 {
+    if (p->tc && (p->flags & FFTSO3_FLAG_EXACT_INVERSE)) return exact_inverse(p, coeffs, grid, st);
     if (p->tc) return tc_inverse(p->tc, coeffs, grid, st, &p->timer, g_err);
     return fp64_inverse(p, coeffs, grid, p->batch, p->d_work, p->d_fc, false, st);
 }
@@ -473,7 +514,7 @@ int fftso3_plan_create(fftso3_plan** out, int kind, int l_max, int batch, int pr
         return fail(FFTSO3_ERR_INVALID_ARG, "unknown precision");
     if (recursion != FFTSO3_RECURSION_REFERENCE && recursion != FFTSO3_RECURSION_STABLE)
         return fail(FFTSO3_ERR_INVALID_ARG, "unknown recursion mode");
-    if ((flags & ~(FFTSO3_FLAG_REFINE | FFTSO3_FLAG_AUTOTUNE)) != 0)
+    if ((flags & ~(FFTSO3_FLAG_REFINE | FFTSO3_FLAG_AUTOTUNE | FFTSO3_FLAG_EXACT_INVERSE)) != 0)
         return fail(FFTSO3_ERR_INVALID_ARG, "unknown flag bits");
     if (is_so3(kind) && l_max > 511) return fail(FFTSO3_ERR_UNSUPPORTED, "SO(3) l_max above 511 is not supported");
     if (!is_so3(kind) && l_max > 2047) return fail(FFTSO3_ERR_UNSUPPORTED, "S^2 l_max above 2047 is not supported");
@@ -585,7 +626,8 @@ int fftso3_plan_create(fftso3_plan** out, int kind, int l_max, int batch, int pr
     } else {
         std::string err;
         rc = tc_create(&p->tc, p->L, p->N, batch, p->d_table, goff, p->table_elems, p->d_tw, p->d_w,
-                       (flags & FFTSO3_FLAG_REFINE) != 0, p->real, !p->so3, (flags & FFTSO3_FLAG_AUTOTUNE) != 0,
+                       (flags & (FFTSO3_FLAG_REFINE | FFTSO3_FLAG_EXACT_INVERSE)) != 0, p->real, !p->so3,
+                       (flags & FFTSO3_FLAG_AUTOTUNE) != 0,
                        precision == FFTSO3_PREC_FP32, err);
         if (rc) {
             g_err = err;
@@ -593,7 +635,8 @@ int fftso3_plan_create(fftso3_plan** out, int kind, int l_max, int batch, int pr
         }
         p->bytes += tc_device_bytes(p->tc);
         const char* ev_ref = getenv("FFTSO3_REFINE_FP64");
-        const bool use_oz = (flags & FFTSO3_FLAG_REFINE) && p->so3 && oz_supported(L, N) && !(ev_ref && ev_ref[0] == '1');
+        const unsigned exact_flags = FFTSO3_FLAG_REFINE | FFTSO3_FLAG_EXACT_INVERSE;
+        const bool use_oz = (flags & exact_flags) && p->so3 && oz_supported(L, N) && !(ev_ref && ev_ref[0] == '1');
         if (use_oz) {
             // SO(3) refinement on the tensor cores: digit planes of the FP64 table, then the table is freed.
             // Chunks of 16 functions (two column tiles, whose items share each table tile through L2, so the
@@ -636,9 +679,9 @@ int fftso3_plan_create(fftso3_plan** out, int kind, int l_max, int batch, int pr
             cudaFree(p->d_table);
             p->d_table = nullptr;
             p->bytes -= (long long)sizeof(double) * p->table_elems;
-        } else if (flags & FFTSO3_FLAG_REFINE) {
-            // the refinement's FP64 inverse keeps the FP64 table; its buffers hold one chunk of functions, the
-            // chunk sized to about 4 GB of FP64 work grid
+        } else if (flags & exact_flags) {
+            // the FP64 inverse of the refinement and of the exact inverse keeps the FP64 table; its buffers hold
+            // one chunk of functions, the chunk sized to about 4 GB of FP64 work grid
             const size_t g16 = 16 * (size_t)p->grid_elems;
             size_t nch = (size_t)4 << 30;
             nch = nch / g16 < 1 ? 1 : nch / g16;

@@ -36,6 +36,8 @@ cudaError_t launch_argmax(const void* x, bool fp64, long long n, int nb, int chu
 // residual refinement of the FP32-data plans: FP32 -> FP64 copy; r = f - g (FP64 difference rounded to FP32);
 // F += d.  n counts real elements (twice the complex count for interleaved complex data).
 cudaError_t launch_widen(const float* in, double* out, long long n, cudaStream_t st);
+// FP64 -> FP32 (rounded to nearest); n real elements
+cudaError_t launch_narrow(const double* in, float* out, long long n, cudaStream_t st);
 cudaError_t launch_resid_fp64(const float* f, const double* g, float* r, long long n, cudaStream_t st);
 cudaError_t launch_add_real(float* F, const float* d, long long n, cudaStream_t st);
 

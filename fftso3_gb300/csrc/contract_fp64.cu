@@ -655,6 +655,19 @@ cudaError_t launch_widen(const float* in, double* out, long long n, cudaStream_t
     return cudaGetLastError();
 }
 
+__global__ void narrow_kernel(const double* __restrict__ in, float* __restrict__ out, long long n)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (float)in[i];
+}
+
+cudaError_t launch_narrow(const double* in, float* out, long long n, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    narrow_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, out, n);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_resid_fp64(const float* f, const double* g, float* r, long long n, cudaStream_t st)
 {
     if (n <= 0) return cudaSuccess;

@@ -1076,7 +1076,7 @@ struct TCState {
     size_t ring_elems = 0;
     int* d_fctl = nullptr;        // fused FFT: tile counter and per-chunk completion counts
     float2* d_pencil = nullptr;   // pencils [fn][p][q][k]
-    float2* d_resid = nullptr;    // refinement: residual grid
+    float2* d_resid = nullptr;    // refinement: residual grid (right after d_pencil, in the same allocation)
     float2* d_coef2 = nullptr;    // refinement: correction coefficients
     float2* d_fc = nullptr;       // real kinds: complex coefficients [fn][C]
     long long* d_grow0 = nullptr;
@@ -1148,7 +1148,7 @@ void tc_destroy(TCState* s)
     if (!s) return;
     for (int p = 0; p < 3; ++p)
         if (s->d_tab[p]) cudaFree(s->d_tab[p]);
-    void* ptrs[] = {s->d_tab32, s->d_wf, s->d_work, s->d_ring, s->d_fctl, s->d_pencil, s->d_resid, s->d_coef2, s->d_fc, s->d_grow0, s->d_goff2, s->d_fg,
+    void* ptrs[] = {s->d_tab32, s->d_wf, s->d_work, s->d_ring, s->d_fctl, s->d_pencil, s->d_coef2, s->d_fc, s->d_grow0, s->d_goff2, s->d_fg,
                     s->d_items_fwd, s->d_items_inv, s->d_iaux_fwd, s->d_iaux_inv, s->d_err};
     for (void* q : ptrs)
         if (q) cudaFree(q);
@@ -1315,11 +1315,13 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
     } else if (!(s2 && fft_fast_supported(N))) {
         if ((rc = tc_alloc(s, (void**)&s->d_work, sizeof(float2) * gridel, err))) return bail(rc);
     }
-    if ((rc = tc_alloc(s, (void**)&s->d_pencil, sizeof(float2) * gridel, err))) return bail(rc);
+    // refinement: the residual buffer follows the pencils in one allocation, so that together they hold one
+    // 16-byte (double-float) element per pencil place for the exact inverse
+    if ((rc = tc_alloc(s, (void**)&s->d_pencil, sizeof(float2) * gridel * (refine ? 2 : 1), err))) return bail(rc);
     if (real)
         if ((rc = tc_alloc(s, (void**)&s->d_fc, sizeof(float2) * (size_t)batch * C, err))) return bail(rc);
     if (refine) {
-        if ((rc = tc_alloc(s, (void**)&s->d_resid, sizeof(float2) * gridel, err))) return bail(rc);
+        s->d_resid = s->d_pencil + gridel;
         if ((rc = tc_alloc(s, (void**)&s->d_coef2, sizeof(float2) * (size_t)batch * C, err))) return bail(rc);
     }
     // group rows and work items; the inverse list is ordered by decreasing cost
@@ -1868,6 +1870,8 @@ int tc_forward(TCState* s, const void* grid, void* coeffs, cudaStream_t st, Stag
 void* tc_resid_buffer(TCState* s) { return s ? (void*)s->d_resid : nullptr; }
 
 float2* tc_pencil_buffer(TCState* s) { return s ? s->d_pencil : nullptr; }
+
+void* tc_exact_buffer(TCState* s) { return s && s->d_resid ? (void*)s->d_pencil : nullptr; }
 
 // forward from pencils already in d_pencil: GEMM, then the packed (and real-basis) coefficients
 static int forward_from_pencils(TCState* s, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err)

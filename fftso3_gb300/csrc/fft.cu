@@ -33,6 +33,10 @@ template <> struct V2<float> {
     using t = float2;
     __device__ static inline float2 mk(float a, float b) { return make_float2(a, b); }
 };
+template <> struct V2<qf32> {
+    using t = qc32;
+    __device__ static inline qc32 mk(qf32 a, qf32 b) { return qc32{a, b}; }
+};
 
 template <typename C> __device__ __forceinline__ C cadd(C a, C b) { a.x += b.x; a.y += b.y; return a; }
 template <typename C> __device__ __forceinline__ C csub(C a, C b) { a.x -= b.x; a.y -= b.y; return a; }
@@ -112,6 +116,53 @@ __device__ __forceinline__ void dft_small(typename V2<T>::t* v, const typename V
 #pragma unroll
         for (int q = 0; q < R; ++q) v[q] = o[q];
     }
+}
+
+// The radix-8 DFT of dft_small in quantised double-float (df32.cuh): the W8 factors are products with the
+// double-float constant 1/sqrt(2), everything else exact sums of the high parts.
+__device__ __forceinline__ void dft8_q(qc32* v, float magic)
+{
+    const df32 h(0.70710678118654752440);
+    qc32 a[4], b[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) { a[t] = cadd(v[t], v[t + 4]); b[t] = csub(v[t], v[t + 4]); }
+    b[1] = qc32{q_mul(b[1].x + b[1].y, h, magic), q_mul(b[1].y - b[1].x, h, magic)};
+    b[2] = mul_mi(b[2]);
+    b[3] = qc32{q_mul(b[3].y - b[3].x, h, magic), -q_mul(b[3].x + b[3].y, h, magic)};
+    qc32 a0 = cadd(a[0], a[2]), a1 = csub(a[0], a[2]);
+    qc32 a2 = cadd(a[1], a[3]), a3 = mul_mi(csub(a[1], a[3]));
+    v[0] = cadd(a0, a2); v[4] = csub(a0, a2);
+    v[2] = cadd(a1, a3); v[6] = csub(a1, a3);
+    qc32 b0 = cadd(b[0], b[2]), b1 = csub(b[0], b[2]);
+    qc32 b2 = cadd(b[1], b[3]), b3 = mul_mi(csub(b[1], b[3]));
+    v[1] = cadd(b0, b2); v[5] = csub(b0, b2);
+    v[3] = cadd(b1, b3); v[7] = csub(b1, b3);
+}
+
+template <int R> __device__ __forceinline__ void dft_q(qc32* v, float magic)
+{
+    if constexpr (R == 8) dft8_q(v, magic);
+    else dft_small<qf32, R>(v, nullptr, 0);
+}
+
+// The quantum of a CTA's block of data (df32.cuh): m = this thread's largest |component|, red 8 floats of shared
+// memory; returns magic = 1.5 * 2^23 q with q = 2^(E - G), 2^E > the block's largest |component| and
+// G = 20 - log2 N: a pass of N points grows a component at most N sqrt(2)-fold, which keeps every value below
+// 2^(E + log2 N + 1/2) < 2^22 q (the range of the rounding to the quantum) with a bit to spare.
+template <int N> __device__ __forceinline__ float q_block_magic(float m, float* red)
+{
+    constexpr int G = 20 - (N == 512 ? 9 : N == 256 ? 8 : N == 128 ? 7 : 6);
+#pragma unroll
+    for (int s = 16; s; s >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, s));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    m = red[0];
+#pragma unroll
+    for (int i = 1; i < 8; ++i) m = fmaxf(m, red[i]);
+    const int eb = (__float_as_int(m) >> 23) & 0xff;  // biased exponent (0: zero or subnormal)
+    int e = eb - 126 - G + 23;                        // exponent of 2^23 q
+    e = e < -100 ? -100 : e > 120 ? 120 : e;
+    return 1.5f * __int_as_float((e + 127) << 23);
 }
 
 // One Stockham pass of radix R over the lpb lines in shared memory.  Thread
@@ -452,7 +503,13 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(const TIN* __restrict__ 
     }
 }
 
-// ---- double-float FFT along a strided axis of k-contiguous arrays (the refinement's forward FFT)
+// ---- double-float FFT along a strided axis of k-contiguous arrays (the refinement's forward FFT and the exact
+// inverse's synthesis FFT)
+//
+// Arithmetic: quantised double-float (df32.cuh), the quantum set per CTA from the largest component of its TK
+// lines, so the butterflies' sums need no two-sum; data in and out of the kernel are ordinary double-float pairs.
+// The high parts are renormalised after the first stages, so a pass keeps about 2^(-24 - G) of the CTA's
+// largest input per operation (G = 20 - log2 N, q_block_magic).
 //
 // Line (o, k): element j at obase(o) + k + j S, obase(o) = (o / oinner) oouter + (o % oinner) oistride.  One CTA
 // transforms TK = 2048 / N consecutive k of one o (N = 64..512, a power of two) with 256 threads: radix-8
@@ -469,6 +526,28 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(const TIN* __restrict__ 
 // rbase + kk N^2 + j), staged through shared memory with row-contiguous reads.
 // STORE 3: the lines are written renormalised as two complex64 arrays at buf's index: hi (the FP32 rounding) and
 // lo (the remainder).
+// STORE 4 / 5: the last pass of a synthesis, lines o = (fn, j1) along j2 (S = N, oinner = N, oouter = N^3,
+// oistride = N^2): the TK lines are written as TK grid rows [fn][k][j1][j2] (the mirror of LOAD 1 / 2) into hi,
+// rounded once to complex64 (4) or to the real part as float32 (5).  Each butterfly of the last stage reads and
+// writes the same places of its line, so the results go back into the line in shared memory and leave it as
+// row-contiguous writes after one barrier.
+// STORE 4 / 5: after the last stage, the TK lines (in shared memory, padded rows) as grid rows
+template <int N, int TK, int ROW, bool REAL_OUT>
+__device__ __forceinline__ void synth_rows_out(const qc32* sm, long long o, long long oinner, float2* out)
+{
+    constexpr long long NN = (long long)N * N;
+    __syncthreads();
+    const long long rbase = (o / oinner) * NN * N + (o % oinner) * N + (long long)blockIdx.x * TK * NN;
+#pragma unroll
+    for (int u = 0; u < N * TK / 256; ++u) {
+        const int e = threadIdx.x + 256 * u, kk2 = e / N, j = e % N;
+        const long long i = rbase + kk2 * NN + j;
+        const qc32 x = sm[kk2 * ROW + j + (j >> 3)];
+        if constexpr (REAL_OUT) reinterpret_cast<float*>(out)[i] = x.x.h + x.x.l;
+        else out[i] = make_float2(x.x.h + x.x.l, x.y.h + x.y.l);
+    }
+}
+
 template <int N, int LOAD, int STORE>
 __global__ void __launch_bounds__(256, 3) fft_df32_k_kernel(dfc32* __restrict__ buf, long long S, long long oinner,
                                                              long long oouter, long long oistride,
@@ -478,8 +557,9 @@ __global__ void __launch_bounds__(256, 3) fft_df32_k_kernel(dfc32* __restrict__ 
     constexpr int TK = 2048 / N;         // lines per CTA
     constexpr int TPL = N / 8;           // threads per line
     constexpr int ROW = N + N / 8 + (N == 512 ? 2 : 1);
-    __shared__ dfc32 sm[TK * ROW];
+    __shared__ qc32 sm[TK * ROW];
     __shared__ dfc32 w[N];               // stage twiddle tables (at most N - 8 entries)
+    __shared__ float red[8];
     auto phys = [](int i) { return i + (i >> 3); };
     const int tid = threadIdx.x;
     const long long o = blockIdx.y;
@@ -499,44 +579,58 @@ __global__ void __launch_bounds__(256, 3) fft_df32_k_kernel(dfc32* __restrict__ 
     }
     const int kq = tid % TK, tq = tid / TK;  // k-fastest thread of the first / last stage
     const int kk = tid / TPL, t = tid % TPL;  // line-major thread of the middle stages
-    dfc32 v[8];
+    // the CTA's block of TK lines: loaded as double-float, then put on the block's quantum
+    dfc32 d[8];
+    float mx = 0.f;
     if constexpr (LOAD == 0) {
 #pragma unroll
-        for (int r = 0; r < 8; ++r) v[r] = buf[obase + (long long)(tq + r * (N / 8)) * S + kq];
+        for (int r = 0; r < 8; ++r) {
+            d[r] = buf[obase + (long long)(tq + r * (N / 8)) * S + kq];
+            mx = fmaxf(mx, fmaxf(fabsf(d[r].x.h), fabsf(d[r].y.h)));
+        }
     } else {
         constexpr long long NN = (long long)N * N;
         const long long rbase = (o / oinner) * NN * N + (o % oinner) * N + (long long)blockIdx.x * TK * NN;
+        dfc32* st = reinterpret_cast<dfc32*>(sm);
 #pragma unroll
         for (int u = 0; u < N * TK / 256; ++u) {
             const int e = tid + 256 * u, kk2 = e / N, j = e % N;
             const long long i = rbase + kk2 * NN + j;
             dfc32 x;
             if constexpr (LOAD == 2) {
-                x = dfc32{df32(reinterpret_cast<const float*>(fin)[i]), df32(0.f)};
+                x = dfc32{df32(reinterpret_cast<const float*>(fin)[i], 0.f), df32(0.f, 0.f)};
             } else {
                 const float2 y = reinterpret_cast<const float2*>(fin)[i];
-                x = dfc32{df32(y.x), df32(y.y)};
+                x = dfc32{df32(y.x, 0.f), df32(y.y, 0.f)};
             }
-            sm[kk2 * ROW + phys(j)] = x;
+            mx = fmaxf(mx, fmaxf(fabsf(x.x.h), fabsf(x.y.h)));
+            st[kk2 * ROW + phys(j)] = x;
         }
         __syncthreads();
 #pragma unroll
-        for (int r = 0; r < 8; ++r) v[r] = sm[kq * ROW + phys(tq + r * (N / 8))];
-        __syncthreads();
+        for (int r = 0; r < 8; ++r) d[r] = st[kq * ROW + phys(tq + r * (N / 8))];
     }
-    // stage 0 (Ns = 1)
-    dft_small<df32, 8>(v, w, N / 8);
+    const float magic = q_block_magic<N>(mx, red);  // (its barrier also orders the staging reads above)
+    qc32 v[8];
 #pragma unroll
-    for (int r = 0; r < 8; ++r) sm[kq * ROW + phys(tq * 8 + r)] = v[r];
+    for (int r = 0; r < 8; ++r) v[r] = q_from(d[r], magic);
+    // stage 0 (Ns = 1)
+    dft8_q(v, magic);
+#pragma unroll
+    for (int r = 0; r < 8; ++r) sm[kq * ROW + phys(tq * 8 + r)] = q_renorm(v[r], magic);
     __syncthreads();
-    auto store = [&](int j, const dfc32& x) {  // element j of line kq, from the last stage's registers
+    auto store = [&](int j, const qc32& x) {  // element j of line kq, from the last stage's registers
+        if constexpr (STORE >= 4) {
+            sm[kq * ROW + phys(j)] = x;
+            return;
+        }
         const long long i = obase + (long long)j * S + kq;
         if constexpr (STORE == 3) {
             const df32 a = df_two_sum(x.x.h, x.x.l), b = df_two_sum(x.y.h, x.y.l);
             hi[i] = make_float2(a.h, b.h);
             lo[i] = make_float2(a.l, b.l);
         } else {
-            buf[i] = x;
+            buf[i] = dfc32{df32(x.x.h, x.x.l), df32(x.y.h, x.y.l)};
         }
     };
     // stage 1 (Ns = 8): the last stage at N = 64
@@ -545,41 +639,43 @@ __global__ void __launch_bounds__(256, 3) fft_df32_k_kernel(dfc32* __restrict__ 
 #pragma unroll
         for (int r = 0; r < 8; ++r) v[r] = sm[kq * ROW + phys(tq + r * 8)];
 #pragma unroll
-        for (int r = 1; r < 8; ++r) v[r] = cmul(v[r], w[(r - 1) * 8 + kt]);
-        dft_small<df32, 8>(v, w, 8);
+        for (int r = 1; r < 8; ++r) v[r] = q_cmul(v[r], w[(r - 1) * 8 + kt], magic);
+        dft8_q(v, magic);
 #pragma unroll
         for (int r = 0; r < 8; ++r) store(tq + r * 8, v[r]);  // (tq - kt) 8 + kt + 8 r with tq < 8
+        if constexpr (STORE >= 4) synth_rows_out<N, TK, ROW, STORE == 5>(sm, o, oinner, hi);
         return;
     } else {
-        dfc32* line = sm + kk * ROW;
+        qc32* line = sm + kk * ROW;
         const int kt = t % 8;
 #pragma unroll
         for (int r = 0; r < 8; ++r) v[r] = line[phys(t + r * (N / 8))];
         __syncthreads();
 #pragma unroll
-        for (int r = 1; r < 8; ++r) v[r] = cmul(v[r], w[(r - 1) * 8 + kt]);
-        dft_small<df32, 8>(v, w, N / 8);
+        for (int r = 1; r < 8; ++r) v[r] = q_cmul(v[r], w[(r - 1) * 8 + kt], magic);
+        dft8_q(v, magic);
 #pragma unroll
-        for (int r = 0; r < 8; ++r) line[phys((t - kt) * 8 + kt + r * 8)] = v[r];
+        for (int r = 0; r < 8; ++r) line[phys((t - kt) * 8 + kt + r * 8)] = q_renorm(v[r], magic);
         __syncthreads();
     }
     // last stage (Ns = 64): radix 8 (N = 512), 4 (256) or 2 (128); outputs j + 64 r of butterfly j < 64
     constexpr int R = N == 512 ? 8 : N == 256 ? 4 : 2;
     constexpr int PER = 8 / R;
     constexpr int BPL = N / R;  // butterflies per line (= 64)
-    dfc32* lq = sm + kq * ROW;
+    qc32* lq = sm + kq * ROW;
 #pragma unroll
     for (int b = 0; b < PER; ++b) {
         const int j = tq + b * (256 / TK);  // butterfly of line kq
-        dfc32 x[R];
+        qc32 x[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) x[r] = lq[phys(j + r * BPL)];
 #pragma unroll
-        for (int r = 1; r < R; ++r) x[r] = cmul(x[r], w[56 + (r - 1) * 64 + j]);
-        dft_small<df32, R>(x, w, BPL);
+        for (int r = 1; r < R; ++r) x[r] = q_cmul(x[r], w[56 + (r - 1) * 64 + j], magic);
+        dft_q<R>(x, magic);
 #pragma unroll
         for (int r = 0; r < R; ++r) store(j + r * 64, x[r]);
     }
+    if constexpr (STORE >= 4) synth_rows_out<N, TK, ROW, STORE == 5>(sm, o, oinner, hi);
 }
 
 // ---- both FFT passes of the beta slices of an uneven batch, every bucket in one launch
@@ -972,6 +1068,26 @@ cudaError_t launch_fft_df32_k_forward(void* buf, int N, long long nb, const void
     if (e != cudaSuccess) return e;
     // along j1 (stride N^2), lines (fn, q), into the pencils [fn][p][q][k] as hi + lo
     df32_k_launch<0, 3>(N, grid, b, NN, N, NN * N, N, t, nullptr, hi, lo, st);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fft_df32_k_synth(void* buf, int N, long long nb, void* out, bool real, const void* tw,
+                                    cudaStream_t st)
+{
+    if (!fft_df32_k_supported(N) || nb < 1 || nb * N > 65535) return cudaErrorInvalidValue;
+    const dim3 grid((unsigned)(N / (2048 / N)), (unsigned)(nb * N));
+    const long long NN = (long long)N * N;
+    const double2* t = (const double2*)tw;
+    dfc32* b = (dfc32*)buf;
+    // along p (stride N^2), lines (fn, q), in place
+    df32_k_launch<0, 0>(N, grid, b, NN, N, NN * N, N, t, nullptr, nullptr, nullptr, st);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    // along q, lines (fn, p), out as the grid rows [fn][k][j1][j2]
+    if (real)
+        df32_k_launch<0, 5>(N, grid, b, N, N, NN * N, NN, t, nullptr, (float2*)out, nullptr, st);
+    else
+        df32_k_launch<0, 4>(N, grid, b, N, N, NN * N, NN, t, nullptr, (float2*)out, nullptr, st);
     return cudaGetLastError();
 }
 

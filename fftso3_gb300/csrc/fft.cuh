@@ -44,6 +44,10 @@ cudaError_t launch_fft_df32_k(void* buf, int N, long long S, long long nouter, l
 // remainder); buf: nb double-float grids of work space.
 cudaError_t launch_fft_df32_k_forward(void* buf, int N, long long nb, const void* f, bool real, float2* hi,
                                       float2* lo, const void* tw, cudaStream_t st);
+// The double-float FFT of nb synthesis pencils buf [fn][p][q][k] (dfc32; overwritten) into the grids out
+// [fn][k][j1][j2], rounded once to complex64, or to the real part as float32 when real.
+cudaError_t launch_fft_df32_k_synth(void* buf, int N, long long nb, void* out, bool real, const void* tw,
+                                    cudaStream_t st);
 
 // Register-resident FP32 kernels for N = 64..1024, powers of two (fft_fast.cu).
 bool fft_fast_supported(int N);

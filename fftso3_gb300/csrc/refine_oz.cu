@@ -632,6 +632,34 @@ __global__ void __launch_bounds__(256) resid_kernel(const float4* __restrict__ g
     }
 }
 
+// The synthesis itself, rounded once: grid[fn][k][j1][j2] = the double-float g (complex64, or the real part as
+// float32 when REAL), transposed like resid_kernel.
+template <bool REAL>
+__global__ void __launch_bounds__(256) synth_out_kernel(const float4* __restrict__ g, void* out, int N)
+{
+    __shared__ float4 tile[32][33];
+    const int k0 = blockIdx.x * 32, q0 = blockIdx.y * 32;
+    const long long fj = blockIdx.z;  // fn N + j1
+    const long long f = fj / N, j1 = fj % N;
+    const long long NN = (long long)N * N;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int y = ty; y < 32; y += 8) {
+        const int q = q0 + y, k = k0 + tx;
+        if (q < N && k < N) tile[y][tx] = g[f * NN * N + (j1 * N + q) * N + k];
+    }
+    __syncthreads();
+    for (int y = ty; y < 32; y += 8) {
+        const int k = k0 + y, q = q0 + tx;
+        if (q >= N || k >= N) continue;
+        const float4 v = tile[tx][y];
+        const long long o = f * NN * N + (long long)k * NN + j1 * N + q;
+        if (REAL)
+            reinterpret_cast<float*>(out)[o] = v.x + v.y;
+        else
+            reinterpret_cast<float2*>(out)[o] = make_float2(v.x + v.y, v.z + v.w);
+    }
+}
+
 }  // namespace oz
 
 // --------------------------------------------------------------- host side
@@ -811,10 +839,13 @@ int oz_status(OZState* o)
 
 // coefficients -> double-float group-major runs and their exponents, then the exact contraction: H into the
 // double-float pencils (rhi null), or the spectral residual into rhi
+// pen: where the synthesis goes (rhi null): o->pen (pen_fns functions), or a caller's buffer of nb functions
 static int oz_contract(OZState* o, const void* F, bool f64, int nb, float2* rhi, const float2* rlo, cudaStream_t st,
-                       StageTimer* T, std::string& err, bool group = false)
+                       StageTimer* T, std::string& err, bool group = false, int stage = ST_REF_CONTRACT,
+                       float4* pen = nullptr)
 {
-    if (nb < 1 || nb > o->chunk || (!rhi && nb > o->pen_fns)) {
+    if (!pen) pen = o->pen;
+    if (nb < 1 || nb > o->chunk || (!rhi && pen == o->pen && nb > o->pen_fns)) {
         err = "internal: refinement chunk larger than its buffers";
         return FFTSO3_ERR_CUDA;
     }
@@ -836,12 +867,12 @@ static int oz_contract(OZState* o, const void* F, bool f64, int nb, float2* rhi,
         OZK(cudaGetLastError());
         if (!rhi) {
             const long long tot = (long long)nb * 2 * NN;
-            zero_nyquist_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(o->pen, N, nb);
+            zero_nyquist_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(pen, N, nb);
             OZK(cudaGetLastError());
         }
     }
     T->end(st);
-    T->begin(ST_REF_CONTRACT, st);
+    T->begin(stage, st);
     {
         Args a;
         a.items = o->items;
@@ -856,7 +887,7 @@ static int oz_contract(OZState* o, const void* F, bool f64, int nb, float2* rhi,
         a.Y = o->Y;
         a.ey = o->ey;
         a.et = o->et;
-        a.pout = o->pen;
+        a.pout = pen;
         a.rhi = rhi;
         a.rlo = rlo;
         int e2n = 0;
@@ -874,6 +905,8 @@ static int oz_contract(OZState* o, const void* F, bool f64, int nb, float2* rhi,
 bool oz_spectral(const OZState* o) { return o && fft_df32_k_supported(o->N); }
 
 int oz_fft_functions(const OZState* o) { return o ? o->pen_fns : 0; }
+
+int oz_chunk(const OZState* o) { return o ? o->chunk : 0; }
 
 int oz_forward_fft(OZState* o, const void* fgrid, bool real, int nb, float2* hi, float2* lo, cudaStream_t st,
                    StageTimer* T, std::string& err)
@@ -898,20 +931,16 @@ int oz_resid_pencils(OZState* o, const void* F, bool f64, int nb, float2* hi, co
     return oz_contract(o, F, f64, nb, hi, lo, st, T, err, group_major);
 }
 
-int oz_inverse_resid(OZState* o, const void* F, bool f64, int nb, const void* fgrid, bool real, float* resid,
-                     cudaStream_t st, StageTimer* T, std::string& err)
+// double-float FFT of the synthesis pencils in o->pen over q (lines (fn, p, k)), then over p (lines (fn, q, k)),
+// in place, by the generic line kernels (any N)
+static int synth_fft_lines(OZState* o, float4* pen, int nb, cudaStream_t st, std::string& err)
 {
-    int rc = oz_contract(o, F, f64, nb, nullptr, nullptr, st, T, err);
-    if (rc) return rc;
     const int N = o->N;
     const long long NN = (long long)N * N;
-    // double-float FFT over q (lines (fn, p, k)), then over p (lines (fn, q, k)) -- the grid form serves the
-    // sizes the spectral form does not (N not a power of two from 64 to 512)
-    T->begin(ST_REF_FFT, st);
     {
         FFTLaunch Lq;
-        Lq.in = o->pen;
-        Lq.out = o->pen;
+        Lq.in = pen;
+        Lq.out = pen;
         Lq.fac = o->fac;
         Lq.nlines = (long long)nb * NN;
         Lq.lpb = 8;
@@ -932,6 +961,18 @@ int oz_inverse_resid(OZState* o, const void* F, bool f64, int nb, const void* fg
         Lp.es = NN;
         OZK(launch_fft_lines(Lp, st));
     }
+    return FFTSO3_SUCCESS;
+}
+
+int oz_inverse_resid(OZState* o, const void* F, bool f64, int nb, const void* fgrid, bool real, float* resid,
+                     cudaStream_t st, StageTimer* T, std::string& err)
+{
+    int rc = oz_contract(o, F, f64, nb, nullptr, nullptr, st, T, err);
+    if (rc) return rc;
+    const int N = o->N;
+    // the grid form serves the sizes the spectral form does not (N not a power of two from 64 to 512)
+    T->begin(ST_REF_FFT, st);
+    if ((rc = synth_fft_lines(o, o->pen, nb, st, err))) return rc;
     T->end(st);
     // residual against the FP32 samples, transposed back to [fn][k][j1][j2]
     T->begin(ST_REFINE, st);
@@ -941,6 +982,29 @@ int oz_inverse_resid(OZState* o, const void* F, bool f64, int nb, const void* fg
             resid_kernel<true><<<grid, 256, 0, st>>>(o->pen, fgrid, resid, N);
         else
             resid_kernel<false><<<grid, 256, 0, st>>>(o->pen, fgrid, resid, N);
+        OZK(cudaGetLastError());
+    }
+    T->end(st);
+    return FFTSO3_SUCCESS;
+}
+
+int oz_inverse_exact(OZState* o, const void* F, bool f64, int nb, void* grid, bool real, cudaStream_t st,
+                     StageTimer* T, std::string& err, void* pen_buf)
+{
+    float4* pen = pen_buf ? (float4*)pen_buf : o->pen;
+    int rc = oz_contract(o, F, f64, nb, nullptr, nullptr, st, T, err, false, ST_INV_CONTRACT, pen);
+    if (rc) return rc;
+    const int N = o->N;
+    T->begin(ST_INV_FFT, st);
+    if (oz_spectral(o)) {
+        OZK(launch_fft_df32_k_synth(pen, N, nb, grid, real, o->d_tw, st));
+    } else {
+        if ((rc = synth_fft_lines(o, pen, nb, st, err))) return rc;
+        dim3 g((unsigned)((N + 31) / 32), (unsigned)((N + 31) / 32), (unsigned)((long long)nb * N));
+        if (real)
+            synth_out_kernel<true><<<g, 256, 0, st>>>(pen, grid, N);
+        else
+            synth_out_kernel<false><<<g, 256, 0, st>>>(pen, grid, N);
         OZK(cudaGetLastError());
     }
     T->end(st);

@@ -26,6 +26,14 @@ int oz_status(OZState* o);
 // f the FP32 samples (complex64, or float32 when real), r written like f.
 int oz_inverse_resid(OZState* o, const void* F, bool f64, int nb, const void* fgrid, bool real, float* resid,
                      cudaStream_t st, StageTimer* T, std::string& err);
+// The exact inverse (FFTSO3_FLAG_EXACT_INVERSE): for nb coefficient sets F (as oz_inverse_resid), the synthesis
+// with exact digit sums and a double-float FFT, rounded once into grid (complex64, or the real part as float32
+// when real).  The double-float synthesis pencils go to pen (nb <= chunk functions of 16-byte elements), or,
+// when pen is null, to the state's own buffer (nb <= oz_fft_functions()).
+int oz_inverse_exact(OZState* o, const void* F, bool f64, int nb, void* grid, bool real, cudaStream_t st,
+                     StageTimer* T, std::string& err, void* pen = nullptr);
+// Functions per contraction chunk.
+int oz_chunk(const OZState* o);
 
 // The spectral form of the residual step (N = 64..512): the forward's FFT in double-float and the residual in
 // the pencil domain, r^ = FFT(f) - N^2 H(F), which is what the forward GEMM consumes -- no FP32 FFT of f or of

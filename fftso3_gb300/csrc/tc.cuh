@@ -27,6 +27,9 @@ int tc_refine_add(TCState* s, const void* resid, void* coeffs, cudaStream_t st, 
 // Spectral refinement (SO(3)): the plan's pencil buffer (complex64 [fn][p][q][k], batch functions), the forward
 // from pencils already there (GEMM + coefficient permutation + real basis), and coeffs += forward(pencils).
 float2* tc_pencil_buffer(TCState* s);
+// Refinement plans: the pencil and residual buffers as one array of batch x (pencil places) 16-byte elements
+// (the exact inverse's double-float synthesis pencils); null otherwise.
+void* tc_exact_buffer(TCState* s);
 int tc_forward_pencils(TCState* s, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err);
 int tc_refine_add_pencils(TCState* s, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err);
 // Complex SO(3) refined plans, group-major form: F0 = the forward GEMM of the pencils, left group-major in the

@@ -22,6 +22,8 @@ enum Stage {
     ST_REF_FFT,
     ST_FFT_SLICES,
     ST_CONVERT,
+    ST_INV_CONTRACT,
+    ST_INV_FFT,
     ST_COUNT
 };
 
@@ -31,7 +33,7 @@ inline const char* stage_name(int s)
                                           "fp64_inv_contract", "basis_convert", "tc_pack_fwd", "tc_gemm_fwd",
                                           "tc_pack_inv", "tc_gemm_inv", "tc_refine_elementwise", "fft_2d",
                                           "refine_exact_contract", "refine_fft_df32", "fft_slices",
-                                          "coeff_convert"};
+                                          "coeff_convert", "exact_inverse_contract", "exact_inverse_fft_df32"};
     return (s >= 0 && s < ST_COUNT) ? names[s] : "";
 }
 

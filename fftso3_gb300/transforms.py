@@ -105,10 +105,11 @@ class _Transform:
     _so3 = True
 
     def __init__(self, l_max: int | None = None, *, precision: str = "fp64", recursion: str = "reference",
-                 refine: bool = False):
+                 refine: bool = False, exact_inverse: bool = False):
         self.precision = precision
         self.recursion = recursion
         self.refine = refine
+        self.exact_inverse = exact_inverse
         self.check_verbose = False
         self.l_max = -1
         self._plan = None
@@ -124,11 +125,14 @@ class _Transform:
             self.B = self.l_max + 1
             self._plan = None
 
+    def _flags(self) -> int:
+        return (_lib.FLAG_REFINE if self.refine else 0) | (_lib.FLAG_EXACT_INVERSE if self.exact_inverse else 0)
+
     @property
     def plan(self) -> _lib.Plan:
         if self._plan is None:
             self._plan = _lib.Plan(self._kind, self.l_max, 1, self.precision, self.recursion,
-                                   _lib.FLAG_REFINE if self.refine else 0)
+                                   self._flags())
         return self._plan
 
     @property
@@ -231,7 +235,7 @@ class _Transform:
     # -- device-resident batch API (torch CUDA tensors)
     def make_plan(self, batch: int) -> _lib.Plan:
         return _lib.Plan(self._kind, self.l_max, batch, self.precision, self.recursion,
-                         _lib.FLAG_REFINE if self.refine else 0)
+                         self._flags())
 
 
 class FFTSO3_complex(_Transform):

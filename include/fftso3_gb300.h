@@ -74,6 +74,12 @@ extern "C" {
                                      the plan's workspace at creation and keep the fastest (cached per N for
                                      the process); batches: also time 1/2/4/8 bucket streams on the first
                                      call of each direction */
+#define FFTSO3_FLAG_EXACT_INVERSE 0x8u /* FP32-data inverse synthesised without FP32 rounding and rounded once to
+                                          the output (complex64 / float32): SO(3) with l_max <= 255 by exact digit
+                                          sums on the tensor cores and a double-float FFT, otherwise in FP64, in
+                                          chunks of functions (the refinement's buffers, shared with
+                                          FFTSO3_FLAG_REFINE).  The grid values are the FP64 synthesis of the
+                                          coefficients up to that one rounding. */
 
 typedef struct fftso3_plan fftso3_plan;
 typedef struct fftso3_batch fftso3_batch;
