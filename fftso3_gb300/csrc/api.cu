@@ -115,6 +115,7 @@ struct fftso3_plan {
     void* d_work = nullptr;        // FFT workspace: batch * grid_elems complex
     void* d_fc = nullptr;          // complex coefficients of the real kinds
     void* d_io_grid = nullptr;     // staging for the *_host calls
+    void* d_io_ring = nullptr;     // exact inverse into host memory: two pieces of grids in flight to the host
     void* d_io_coeff = nullptr;
     void* d_corr = nullptr;        // correlation coefficients (fftso3_correlate_s2)
     void* d_amax = nullptr;        // arg-max scratch (fftso3_grid_argmax)
@@ -160,7 +161,7 @@ int plan_alloc(fftso3_plan* p, void** ptr, size_t bytes)
 
 void plan_free(fftso3_plan* p)
 {
-    void* ptrs[] = {p->d_tw, p->d_w, p->d_goff, p->d_table, p->d_lfact, p->d_work, p->d_fc, p->d_io_grid,
+    void* ptrs[] = {p->d_tw, p->d_w, p->d_goff, p->d_table, p->d_lfact, p->d_work, p->d_fc, p->d_io_grid, p->d_io_ring,
                     p->d_io_coeff, p->d_corr, p->d_amax, p->d_prec, p->d_pscratch, p->d_rw, p->d_rg, p->d_rc,
                     p->d_rfc, p->d_deriv};
     for (void* q : ptrs)
@@ -414,8 +415,9 @@ int run_forward(fftso3_plan* p, const void* grid, void* coeffs, cudaStream_t st)
 // FFTSO3_FLAG_EXACT_INVERSE: the synthesis without FP32 rounding -- SO(3), l_max <= 255: exact digit sums on the
 // tensor cores and a double-float FFT, a contraction chunk of functions at a time, the double-float pencils in
 // the plan's pencil + residual buffers; otherwise the FP64 inverse in chunks of rchunk functions -- rounded once
-// into the FP32 grid.
-int exact_inverse(fftso3_plan* p, const void* coeffs, void* grid, cudaStream_t st)
+// into the FP32 grid.  host (non-null): the grids go to host memory; grid is then device staging for them (unused
+// by the double-float FFT of N = 64..512, which streams pieces through a small device ring instead).
+int exact_inverse(fftso3_plan* p, const void* coeffs, void* grid, cudaStream_t st, void* host = nullptr)
 {
     StageTimer& T = p->timer;
     const long long C = p->coeff_elems, G = p->grid_elems;
@@ -423,6 +425,13 @@ int exact_inverse(fftso3_plan* p, const void* coeffs, void* grid, cudaStream_t s
     if (p->oz) {
         void* pen = tc_exact_buffer(p->tc);
         const int fftn = pen ? p->rchunk : oz_fft_functions(p->oz);
+        void* ring = nullptr;
+        if (host && oz_spectral(p->oz)) {
+            const size_t fn_bytes = (size_t)G * per * sizeof(float);
+            int rc = p->d_io_ring ? FFTSO3_SUCCESS : plan_alloc(p, &p->d_io_ring, 2 * (size_t)OZ_SYNTH_PIECE * fn_bytes);
+            if (rc) return rc;
+            ring = p->d_io_ring;
+        }
         for (int f0 = 0; f0 < p->batch; f0 += fftn) {
             const int nb = p->batch - f0 < fftn ? p->batch - f0 : fftn;
             const void* Fc = (const float2*)coeffs + (long long)f0 * C;
@@ -432,8 +441,9 @@ int exact_inverse(fftso3_plan* p, const void* coeffs, void* grid, cudaStream_t s
                 STAGE(ST_BASIS, launch_so3_r2c(p->d_rc, p->d_rfc, true, p->L, nb, st));
                 Fc = p->d_rfc;
             }
-            int rc = oz_inverse_exact(p->oz, Fc, p->real, nb, (float*)grid + (long long)f0 * G * per, p->real, st,
-                                      &T, g_err, pen);
+            const long long off = (long long)f0 * G * per;  // floats
+            int rc = oz_inverse_exact(p->oz, Fc, p->real, nb, ring ? nullptr : (float*)grid + off, p->real, st, &T,
+                                      g_err, pen, host ? (float*)host + off : nullptr, ring);
             if (rc) return rc;
         }
         return FFTSO3_SUCCESS;
@@ -448,6 +458,7 @@ int exact_inverse(fftso3_plan* p, const void* coeffs, void* grid, cudaStream_t s
         STAGE(ST_BASIS, launch_narrow((const double*)g64, (float*)grid + (long long)f0 * G * per,
                                       (long long)nb * G * per, st));
     }
+    if (host) CK(cudaMemcpyAsync(host, grid, (size_t)p->batch * G * per * sizeof(float), cudaMemcpyDeviceToHost, st));
     return FFTSO3_SUCCESS;
 }
 
@@ -852,13 +863,21 @@ int fftso3_inverse_host(fftso3_plan* plan, const void* coeffs_host, void* grid_h
     if (rc) return rc;
     if (!grid_host || !coeffs_host) return fail(FFTSO3_ERR_INVALID_ARG, "grid/coeffs pointer is NULL");
     cudaStream_t st = (cudaStream_t)stream;
-    const void* cin = host_device_ptr(coeffs_host);
-    void* gout = host_device_ptr(grid_host);
-    if ((!cin && (rc = ensure_io_coeff(plan))) || (!gout && (rc = ensure_io_grid(plan)))) return rc;
-    if (!cin) {
-        CK(cudaMemcpyAsync(plan->d_io_coeff, coeffs_host, coeff_bytes(plan), cudaMemcpyHostToDevice, st));
-        cin = plan->d_io_coeff;
+    // the coefficients always go to device memory in one copy (the inverse's first kernels gather them in an order
+    // that would cross the host link in small pieces)
+    if ((rc = ensure_io_coeff(plan))) return rc;
+    CK(cudaMemcpyAsync(plan->d_io_coeff, coeffs_host, coeff_bytes(plan), cudaMemcpyHostToDevice, st));
+    const void* cin = plan->d_io_coeff;
+    if (plan->tc && (plan->flags & FFTSO3_FLAG_EXACT_INVERSE)) {
+        // the exact inverse copies its grids out itself, piece by piece under its FFT where it can
+        if (!(plan->oz && oz_spectral(plan->oz)) && (rc = ensure_io_grid(plan))) return rc;
+        if ((rc = exact_inverse(plan, cin, plan->d_io_grid, st, grid_host))) return rc;
+        CK(cudaStreamSynchronize(st));
+        return FFTSO3_SUCCESS;
     }
+    // otherwise a grid in pinned host memory is written in place, by rows
+    void* gout = host_device_ptr(grid_host);
+    if (!gout && (rc = ensure_io_grid(plan))) return rc;
     if ((rc = run_inverse(plan, cin, gout ? gout : plan->d_io_grid, st))) return rc;
     if (!gout) CK(cudaMemcpyAsync(grid_host, plan->d_io_grid, grid_bytes(plan), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));

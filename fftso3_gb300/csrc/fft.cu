@@ -1071,24 +1071,31 @@ cudaError_t launch_fft_df32_k_forward(void* buf, int N, long long nb, const void
     return cudaGetLastError();
 }
 
-cudaError_t launch_fft_df32_k_synth(void* buf, int N, long long nb, void* out, bool real, const void* tw,
-                                    cudaStream_t st)
+cudaError_t launch_fft_df32_k_synth_pass(int pass, void* buf, int N, long long nb, void* out, bool real,
+                                         const void* tw, cudaStream_t st)
 {
-    if (!fft_df32_k_supported(N) || nb < 1 || nb * N > 65535) return cudaErrorInvalidValue;
+    if (!fft_df32_k_supported(N) || nb < 1 || nb * N > 65535 || (pass != 1 && pass != 2)) return cudaErrorInvalidValue;
     const dim3 grid((unsigned)(N / (2048 / N)), (unsigned)(nb * N));
     const long long NN = (long long)N * N;
     const double2* t = (const double2*)tw;
     dfc32* b = (dfc32*)buf;
-    // along p (stride N^2), lines (fn, q), in place
-    df32_k_launch<0, 0>(N, grid, b, NN, N, NN * N, N, t, nullptr, nullptr, nullptr, st);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    // along q, lines (fn, p), out as the grid rows [fn][k][j1][j2]
-    if (real)
+    if (pass == 1) {
+        // along p (stride N^2), lines (fn, q), in place
+        df32_k_launch<0, 0>(N, grid, b, NN, N, NN * N, N, t, nullptr, nullptr, nullptr, st);
+    } else if (real) {
+        // along q, lines (fn, p), out as the grid rows [fn][k][j1][j2]
         df32_k_launch<0, 5>(N, grid, b, N, N, NN * N, NN, t, nullptr, (float2*)out, nullptr, st);
-    else
+    } else {
         df32_k_launch<0, 4>(N, grid, b, N, N, NN * N, NN, t, nullptr, (float2*)out, nullptr, st);
+    }
     return cudaGetLastError();
+}
+
+cudaError_t launch_fft_df32_k_synth(void* buf, int N, long long nb, void* out, bool real, const void* tw,
+                                    cudaStream_t st)
+{
+    cudaError_t e = launch_fft_df32_k_synth_pass(1, buf, N, nb, out, real, tw, st);
+    return e != cudaSuccess ? e : launch_fft_df32_k_synth_pass(2, buf, N, nb, out, real, tw, st);
 }
 
 void make_fft_factors(int N, FFTFactors& f)

@@ -48,6 +48,9 @@ cudaError_t launch_fft_df32_k_forward(void* buf, int N, long long nb, const void
 // [fn][k][j1][j2], rounded once to complex64, or to the real part as float32 when real.
 cudaError_t launch_fft_df32_k_synth(void* buf, int N, long long nb, void* out, bool real, const void* tw,
                                     cudaStream_t st);
+// One of its two passes (1: along p, in place; 2: along q into out), for pipelining pieces of functions.
+cudaError_t launch_fft_df32_k_synth_pass(int pass, void* buf, int N, long long nb, void* out, bool real,
+                                         const void* tw, cudaStream_t st);
 
 // Register-resident FP32 kernels for N = 64..1024, powers of two (fft_fast.cu).
 bool fft_fast_supported(int N);

@@ -684,6 +684,9 @@ struct OZState {
     const double* d_tw = nullptr;
     int* err = nullptr;
     long long bytes = 0;
+    // exact inverse into host memory: the copy stream and its events (created on first use)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_ready[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr}, ev_join = nullptr;
 };
 
 bool oz_supported(int L, int N) { return L >= 0 && L <= 255 && N == 2 * (L + 1); }
@@ -708,6 +711,9 @@ void oz_destroy(OZState* o)
     void* ptrs[] = {o->et, o->ey, o->Y, o->pen, o->goff2, o->items, o->iaux, o->err};
     for (void* q : ptrs)
         if (q) cudaFree(q);
+    for (cudaEvent_t e : {o->ev_ready[0], o->ev_ready[1], o->ev_free[0], o->ev_free[1], o->ev_join})
+        if (e) cudaEventDestroy(e);
+    if (o->side) cudaStreamDestroy(o->side);
     delete o;
 }
 
@@ -989,14 +995,43 @@ int oz_inverse_resid(OZState* o, const void* F, bool f64, int nb, const void* fg
 }
 
 int oz_inverse_exact(OZState* o, const void* F, bool f64, int nb, void* grid, bool real, cudaStream_t st,
-                     StageTimer* T, std::string& err, void* pen_buf)
+                     StageTimer* T, std::string& err, void* pen_buf, void* host, void* ring)
 {
     float4* pen = pen_buf ? (float4*)pen_buf : o->pen;
     int rc = oz_contract(o, F, f64, nb, nullptr, nullptr, st, T, err, false, ST_INV_CONTRACT, pen);
     if (rc) return rc;
     const int N = o->N;
+    const long long G = (long long)N * N * N;
+    const size_t gbytes = (size_t)G * (real ? sizeof(float) : sizeof(float2));  // one function's grid
     T->begin(ST_INV_FFT, st);
-    if (oz_spectral(o)) {
+    if (oz_spectral(o) && host) {
+        // into host memory: both passes of each piece of OZ_SYNTH_PIECE functions on st into a slot of the
+        // two-slot device ring, then the slot's copy to the host on the copy stream, so the copies (the host link
+        // bounds them) run under the FFT of the next pieces; a slot is rewritten once its copy is done
+        if (!o->side) {
+            OZK(cudaStreamCreateWithFlags(&o->side, cudaStreamNonBlocking));
+            for (int i = 0; i < 2; ++i) {
+                OZK(cudaEventCreateWithFlags(&o->ev_ready[i], cudaEventDisableTiming));
+                OZK(cudaEventCreateWithFlags(&o->ev_free[i], cudaEventDisableTiming));
+            }
+            OZK(cudaEventCreateWithFlags(&o->ev_join, cudaEventDisableTiming));
+        }
+        for (int f0 = 0, i = 0; f0 < nb; f0 += OZ_SYNTH_PIECE, ++i) {
+            const int np = nb - f0 < OZ_SYNTH_PIECE ? nb - f0 : OZ_SYNTH_PIECE, sl = i & 1;
+            float4* pb = pen + (long long)f0 * G;
+            char* rb = (char*)ring + (size_t)sl * OZ_SYNTH_PIECE * gbytes;
+            OZK(launch_fft_df32_k_synth_pass(1, pb, N, np, rb, real, o->d_tw, st));
+            if (i >= 2) OZK(cudaStreamWaitEvent(st, o->ev_free[sl], 0));
+            OZK(launch_fft_df32_k_synth_pass(2, pb, N, np, rb, real, o->d_tw, st));
+            OZK(cudaEventRecord(o->ev_ready[sl], st));
+            OZK(cudaStreamWaitEvent(o->side, o->ev_ready[sl], 0));
+            OZK(cudaMemcpyAsync((char*)host + (size_t)f0 * gbytes, rb, (size_t)np * gbytes, cudaMemcpyDeviceToHost,
+                                o->side));
+            OZK(cudaEventRecord(o->ev_free[sl], o->side));
+        }
+        OZK(cudaEventRecord(o->ev_join, o->side));
+        OZK(cudaStreamWaitEvent(st, o->ev_join, 0));
+    } else if (oz_spectral(o)) {
         OZK(launch_fft_df32_k_synth(pen, N, nb, grid, real, o->d_tw, st));
     } else {
         if ((rc = synth_fft_lines(o, pen, nb, st, err))) return rc;
@@ -1006,6 +1041,7 @@ int oz_inverse_exact(OZState* o, const void* F, bool f64, int nb, void* grid, bo
         else
             synth_out_kernel<false><<<g, 256, 0, st>>>(pen, grid, N);
         OZK(cudaGetLastError());
+        if (host) OZK(cudaMemcpyAsync(host, grid, (size_t)nb * gbytes, cudaMemcpyDeviceToHost, st));
     }
     T->end(st);
     return FFTSO3_SUCCESS;

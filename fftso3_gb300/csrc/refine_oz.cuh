@@ -30,8 +30,13 @@ int oz_inverse_resid(OZState* o, const void* F, bool f64, int nb, const void* fg
 // with exact digit sums and a double-float FFT, rounded once into grid (complex64, or the real part as float32
 // when real).  The double-float synthesis pencils go to pen (nb <= chunk functions of 16-byte elements), or,
 // when pen is null, to the state's own buffer (nb <= oz_fft_functions()).
+// host (non-null): the grids go to host memory instead; grid is then the device staging for all nb grids
+// (the generic FFT) and ring a device buffer of 2 OZ_SYNTH_PIECE grids (N = 64..512), whose copies to the host
+// run under the FFT of the next pieces.
+constexpr int OZ_SYNTH_PIECE = 4;
 int oz_inverse_exact(OZState* o, const void* F, bool f64, int nb, void* grid, bool real, cudaStream_t st,
-                     StageTimer* T, std::string& err, void* pen = nullptr);
+                     StageTimer* T, std::string& err, void* pen = nullptr, void* host = nullptr,
+                     void* ring = nullptr);
 // Functions per contraction chunk.
 int oz_chunk(const OZState* o);
 

@@ -98,8 +98,12 @@ def test_exact_inverse_host_call_equals_device_call(gblib, oracle):
     want = g.cpu().numpy()
     host = np.ascontiguousarray(F.ravel())
     out = np.empty_like(want)
-    p.inverse_host(host.ctypes.data, out.ctypes.data, s)
+    p.inverse_host(host.ctypes.data, out.ctypes.data, s)  # pageable
     assert np.array_equal(out, want)
+    pin = torch.from_numpy(host).pin_memory()
+    pout = torch.empty(want.size, dtype=torch.complex64).pin_memory()
+    p.inverse_host(pin.data_ptr(), pout.data_ptr(), s)  # pinned: the grid written in place, piece by piece
+    assert np.array_equal(pout.numpy(), want)
 
 
 def test_exact_inverse_is_more_accurate_than_the_plain_inverse(gblib, oracle):
