@@ -1094,8 +1094,10 @@ def so3_tc_line(args, L: int, b: int, full: bool = True) -> dict:
     nrec = int(sum(c for _, c in stages.values()))
     # kernels in the timed region: one per timed record, plus the second kernel of the records that hold two
     # (the double-float FFTs' two passes; the gather and Nyquist zeroing before each exact-inverse contraction)
+    # (each contraction's gather record also holds its digit-image kernel, the exact inverse's its Nyquist zeroing)
     launches = nrec + int(stages.get("refine_fft_df32", (0, 0))[1]) + \
-        int(stages.get("exact_inverse_fft_df32", (0, 0))[1]) + int(stages.get("exact_inverse_contract", (0, 0))[1])
+        int(stages.get("exact_inverse_fft_df32", (0, 0))[1]) + 2 * int(stages.get("exact_inverse_contract", (0, 0))[1]) + \
+        int(stages.get("refine_exact_contract", (0, 0))[1])
     tot = sum(v for v, _ in stages.values())
     stage_summary = {k: {"ms_per_launch": v / c, "launches": c, "share": v / tot} for k, (v, c) in stages.items()}
     top, (top_ms, top_n) = max(stages.items(), key=lambda kv: kv[1][0])

@@ -663,9 +663,10 @@ int fftso3_plan_create(fftso3_plan** out, int kind, int l_max, int batch, int pr
             size_t freeb = 0, totb = 0;
             cudaMemGetInfo(&freeb, &totb);
             const size_t spare = (size_t)16 << 30, slack = (size_t)2 << 30;
+            const size_t img_tile = (size_t)oz_image_bytes_per_column_tile(L);
             auto need = [&](size_t nch) {
                 const size_t pens = spectral ? std::min<size_t>(nch, 8) : nch;
-                return planes + nch * run_fn + pens * pen_fn;
+                return planes + nch * run_fn + pens * pen_fn + (nch + 7) / 8 * img_tile;
             };
             size_t nch = spectral ? 32 : 16;
             while (nch > 1 && (need(nch) + slack > freeb || freeb + tab64 < need(nch) + spare))

@@ -75,10 +75,10 @@ constexpr int STAGES = 2;
 constexpr int APLANE = BM * BK * 2;     // 16 KB: 128 k x 64 l (two 64 x 64 boxes)
 constexpr int BPLANE = BN * BK * 2;     // 8 KB: 64 columns x 64 l
 constexpr int STAGE_A = NS * APLANE;
-constexpr int STAGE_BYTES = STAGE_A + NS * BPLANE;
-constexpr int NPROD = 8;
-constexpr int NEPI = 4;
-constexpr int THREADS = 32 * (2 + NPROD + NEPI);
+constexpr int STAGE_B = NS * BPLANE;    // 32 KB: one tile of the coefficients' digit image
+constexpr int STAGE_BYTES = STAGE_A + STAGE_B;
+constexpr int NEPI = 8;                 // epilogue warps: two per TMEM lane quarter, each half of the columns
+constexpr int THREADS = 32 * (2 + NEPI);
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 256 /*barriers*/ + 1024 /*alignment*/;
 constexpr int ACC = NS * BN;            // TMEM columns of one accumulator buffer (levels 0..3)
 constexpr int TMEM_COLS = 2 * ACC;
@@ -93,7 +93,9 @@ struct Args {
     int L, N, batch, ngroups;
     long long fstride;      // pencil elements per function (N^3)
     long long ystride;      // coefficients per function (C)
-    const float4* Y;        // double-float group-major coefficients [fn][goff2 + pair nl + l'] (re.h, re.l, im.h, im.l)
+    const unsigned char* bimg;  // the coefficients' digit image: [column tile][group tile gt0[g] + step] x STAGE_B
+    const int* gt0;             // first tile of each group in the image
+    long long nbt;              // tiles per column tile
     const signed char* ey;  // exponents [fn][group][pair]
     const signed char* et;  // exponents [group][k]
     float4* pout;           // double-float pencils [fn][p][q][k]
@@ -165,7 +167,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     };
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
-            mbar_init(&full[s], 1 + NPROD);
+            mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
         for (int b = 0; b < 2; ++b) {
@@ -201,13 +203,16 @@ __global__ void __launch_bounds__(THREADS, 1)
                         break;
                     }
                     unsigned char* st = smem + s * STAGE_BYTES;
-                    mbar_expect_tx(&full[s], STAGE_A);
+                    mbar_expect_tx(&full[s], STAGE_A + STAGE_B);
                     const int y = row0 + i * BK;
 #pragma unroll
                     for (int p = 0; p < NS; ++p)
 #pragma unroll
                         for (int h = 0; h < 2; ++h)
                             tma_load_2d(st + p * APLANE + h * (APLANE / 2), tm[p], item.y * BM + 64 * h, y, &full[s]);
+                    // the coefficients' four digit planes: one contiguous 32 KB tile, already in the swizzled layout
+                    const long long tile = (long long)item.z * a.nbt + a.gt0[item.x] + i;
+                    bulk_load(st + STAGE_A, a.bimg + tile * STAGE_B, STAGE_B, &full[s]);
                 }
             }
         }
@@ -264,107 +269,10 @@ __global__ void __launch_bounds__(THREADS, 1)
             }
             for (int u = (t >= 2 ? t - 2 : 0); u < t; ++u) mbar_wait(&accf[u & 1], (u >> 1) & 1, a.err, 26);
         }
-    } else if (warp < 2 + NPROD) {
-        // ---------------- coefficient producers (256 threads): thread = (column pair c, 16-byte chunk q8)
-        const int pt = threadIdx.x - 64;
-        const int c = pt >> 3, q8 = pt & 7;
-        const int fl = c >> 2, pp = c & 3;
-        const int Rre = 2 * c, Rim = Rre + 1;  // columns fl 8 + 2 pp (re), + 1 (im)
-        struct Src {
-            const float4* p;
-            int lim;
-            float sc;  // 2^-E of the column
-        };
-        auto source = [&](const int4& item, const int2& aux) -> Src {
-            int m0, n0;
-            item_mn(item, m0, n0);
-            const GroupPairs P = group_pairs(m0, n0);
-            const int f = item.z * FPT + fl;
-            Src r;
-            r.lim = a.L + 1 - m0;
-            r.p = nullptr;
-            r.sc = 0.f;
-            if (f >= a.batch || pp >= P.np) return r;
-            r.p = a.Y + (long long)f * a.ystride + aux.x + (long long)pp * r.lim;
-            r.sc = pow2f(-(int)a.ey[((long long)f * a.ngroups + item.x) * 4 + pp]);
-            return r;
-        };
-        auto fetch = [&](const Src& sr, int i, float4* v) {
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const int l = i * BK + q8 * 8 + j;
-                v[j] = (sr.p && l < sr.lim) ? __ldg(sr.p + l) : make_float4(0.f, 0.f, 0.f, 0.f);
-            }
-        };
-        int kc = 0, it = blockIdx.x, i = 0, nk_cur = 0;
-        float4 cur[8];
-        Src scur, snxt;
-        if (it < a.nitems) {
-            const int4 item0 = a.items[it];
-            scur = source(item0, a.iaux[it]);
-            nk_cur = nsteps(item0);
-            fetch(scur, 0, cur);
-        }
-        while (it < a.nitems && !*abort_flag) {
-            int it2 = it, i2 = i + 1, nk2 = nk_cur;
-            snxt = scur;
-            if (i2 == nk_cur) {
-                it2 += gridDim.x;
-                i2 = 0;
-                if (it2 < a.nitems) {
-                    const int4 item2 = a.items[it2];
-                    snxt = source(item2, a.iaux[it2]);
-                    nk2 = nsteps(item2);
-                }
-            }
-            float4 nxt[8];
-            if (it2 < a.nitems) fetch(snxt, i2, nxt);
-            const int s = kc % STAGES;
-            if (kc >= STAGES && !mbar_wait(&empty[s], ((kc / STAGES) - 1) & 1, a.err, 24)) {
-                *abort_flag = 1;
-                break;
-            }
-            const uint32_t bpl = smem_u32(smem + s * STAGE_BYTES + STAGE_A);
-            uint32_t wre[NS][4], wim[NS][4];
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                float dr0[NS], dr1[NS], di0[NS], di1[NS];
-                const float4 v0 = cur[2 * j], v1 = cur[2 * j + 1];
-                digits4(v0.x, v0.y, scur.sc, dr0);
-                digits4(v1.x, v1.y, scur.sc, dr1);
-                digits4(v0.z, v0.w, scur.sc, di0);
-                digits4(v1.z, v1.w, scur.sc, di1);
-#pragma unroll
-                for (int p = 0; p < NS; ++p) {
-                    wre[p][j] = pack_bf16(dr0[p], dr1[p]);
-                    wim[p][j] = pack_bf16(di0[p], di1[p]);
-                }
-            }
-            const uint32_t ore = (uint32_t)Rre * 128u + (uint32_t)((q8 ^ (Rre & 7)) * 16);
-            const uint32_t oim = (uint32_t)Rim * 128u + (uint32_t)((q8 ^ (Rim & 7)) * 16);
-#pragma unroll
-            for (int p = 0; p < NS; ++p) {
-                asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(bpl + p * BPLANE + ore), "r"(wre[p][0]),
-                             "r"(wre[p][1]), "r"(wre[p][2]), "r"(wre[p][3])
-                             : "memory");
-                asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(bpl + p * BPLANE + oim), "r"(wim[p][0]),
-                             "r"(wim[p][1]), "r"(wim[p][2]), "r"(wim[p][3])
-                             : "memory");
-            }
-            fence_proxy_async();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&full[s]);
-#pragma unroll
-            for (int j = 0; j < 8; ++j) cur[j] = nxt[j];
-            scur = snxt;
-            nk_cur = nk2;
-            it = it2;
-            i = i2;
-            ++kc;
-        }
     } else {
-        // ---------------- epilogue (4 warps, one TMEM lane quarter each; thread = one k row)
-        const int quarter = warp & 3;
+        // ---------------- epilogue (8 warps: two per TMEM lane quarter, each taking half of the columns; thread =
+        // one k row)
+        const int quarter = warp & 3, half = (warp - 2) >> 2;
         const int r = quarter * 32 + lane;
         const int N = a.N;
         int t = 0;
@@ -388,7 +296,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             if (spectral && k < N) {
                 // the FFT values this item will read, requested into L2 while its MMAs run
 #pragma unroll 1
-                for (int fl = 0; fl < FPT; ++fl) {
+                for (int fl = half * (FPT / 2); fl < (half + 1) * (FPT / 2); ++fl) {
                     const int f = item.z * FPT + fl;
                     if (f >= a.batch) break;
                     const long long fo = (long long)f * a.fstride + k;
@@ -408,7 +316,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t trow = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(ab * ACC);
 #pragma unroll 1
-            for (int cc = 0; cc < BN / 16; ++cc) {  // 16 columns = 2 functions x 4 pairs x re/im
+            for (int cc = half * (BN / 32); cc < (half + 1) * (BN / 32); ++cc) {  // 16 columns = 2 functions x 4 pairs x re/im
                 uint32_t v[NS][16];
 #pragma unroll
                 for (int j = 0; j < NS; ++j) tmem_ld16_nowait(trow + (uint32_t)(j * BN + cc * 16), v[j]);
@@ -632,6 +540,60 @@ __global__ void __launch_bounds__(256) resid_kernel(const float4* __restrict__ g
     }
 }
 
+// The coefficients' digit image: for column tile z (functions 8z .. 8z + 7) and group g, the B operand of each
+// of the group's K steps (BK degrees) as the contraction's shared-memory stage expects it -- four BF16 digit
+// planes of 64 columns (function fl, pair pp, re / im: column 8 fl + 2 pp + {0, 1}) x BK degrees, K-major, each
+// column's 128-byte row with its 16-byte chunks swizzled (chunk q at q ^ (row & 7)) -- so that one bulk copy
+// fills a stage.  Degrees past the group's run, missing pairs and functions past nb are zero.  One CTA per
+// (group, column tile), thread = (column pair c, chunk q8), as the digits were formed in shared memory before.
+__global__ void __launch_bounds__(256) digit_image_kernel(const float4* __restrict__ Y, const signed char* __restrict__ ey,
+                                                          const long long* __restrict__ goff2,
+                                                          const int* __restrict__ gt0, unsigned char* __restrict__ img,
+                                                          long long nbt, long long ystride, int L, int ngroups, int nb)
+{
+    const int g = blockIdx.x, z = blockIdx.y;
+    int m0, n0;
+    group_mn(g, m0, n0);
+    const GroupPairs P = group_pairs(m0, n0);
+    const int c = threadIdx.x >> 3, q8 = threadIdx.x & 7;
+    const int fl = c >> 2, pp = c & 3, f = z * FPT + fl;
+    const int lim = L + 1 - m0, nk = (lim + BK - 1) / BK;
+    const bool valid = f < nb && pp < P.np;
+    const float4* src = valid ? Y + (long long)f * ystride + goff2[g] + (long long)pp * lim : nullptr;
+    const float sc = valid ? pow2f(-(int)ey[((long long)f * ngroups + g) * 4 + pp]) : 0.f;
+    const int Rre = 2 * c, Rim = Rre + 1;
+    const uint32_t ore = (uint32_t)Rre * 128u + (uint32_t)((q8 ^ (Rre & 7)) * 16);
+    const uint32_t oim = (uint32_t)Rim * 128u + (uint32_t)((q8 ^ (Rim & 7)) * 16);
+    for (int i = 0; i < nk; ++i) {
+        float4 v[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int l = i * BK + q8 * 8 + j;
+            v[j] = (valid && l < lim) ? __ldg(src + l) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        uint32_t wre[NS][4], wim[NS][4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            float dr0[NS], dr1[NS], di0[NS], di1[NS];
+            digits4(v[2 * j].x, v[2 * j].y, sc, dr0);
+            digits4(v[2 * j + 1].x, v[2 * j + 1].y, sc, dr1);
+            digits4(v[2 * j].z, v[2 * j].w, sc, di0);
+            digits4(v[2 * j + 1].z, v[2 * j + 1].w, sc, di1);
+#pragma unroll
+            for (int p = 0; p < NS; ++p) {
+                wre[p][j] = pack_bf16(dr0[p], dr1[p]);
+                wim[p][j] = pack_bf16(di0[p], di1[p]);
+            }
+        }
+        unsigned char* tile = img + ((long long)z * nbt + gt0[g] + i) * STAGE_B;
+#pragma unroll
+        for (int p = 0; p < NS; ++p) {
+            *reinterpret_cast<uint4*>(tile + p * BPLANE + ore) = make_uint4(wre[p][0], wre[p][1], wre[p][2], wre[p][3]);
+            *reinterpret_cast<uint4*>(tile + p * BPLANE + oim) = make_uint4(wim[p][0], wim[p][1], wim[p][2], wim[p][3]);
+        }
+    }
+}
+
 // The synthesis itself, rounded once: grid[fn][k][j1][j2] = the double-float g (complex64, or the real part as
 // float32 when REAL), transposed like resid_kernel.
 template <bool REAL>
@@ -675,6 +637,9 @@ struct OZState {
     signed char* et = nullptr;  // [group][k]
     signed char* ey = nullptr;  // [chunk][group][pair]
     float4* Y = nullptr;        // [chunk][C] double-float group-major coefficients
+    unsigned char* bimg = nullptr;  // [column tile][tile] x STAGE_B: their digit image (digit_image_kernel)
+    int* gt0 = nullptr;             // first image tile of each group
+    long long nbt = 0;              // image tiles per column tile
     float4* pen = nullptr;      // [chunk][N^3] double-float pencils / grid
     long long* goff2 = nullptr;
     int4* items = nullptr;
@@ -708,7 +673,7 @@ void oz_destroy(OZState* o)
     if (!o) return;
     for (int p = 0; p < NS; ++p)
         if (o->planes[p]) cudaFree(o->planes[p]);
-    void* ptrs[] = {o->et, o->ey, o->Y, o->pen, o->goff2, o->items, o->iaux, o->err};
+    void* ptrs[] = {o->et, o->ey, o->Y, o->bimg, o->gt0, o->pen, o->goff2, o->items, o->iaux, o->err};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     for (cudaEvent_t e : {o->ev_ready[0], o->ev_ready[1], o->ev_free[0], o->ev_free[1], o->ev_join})
@@ -782,12 +747,15 @@ int oz_create(OZState** out, const double* d_table, const std::vector<long long>
         }
     // group-major offsets, work items (ordered by decreasing length), per-item (goff2, first row)
     std::vector<long long> goff2(o->ngroups + 1);
+    std::vector<int> gt0(o->ngroups);
     std::vector<int4> items;
     std::vector<int2> aux;
-    long long acc2 = 0;
+    long long acc2 = 0, acct = 0;
     for (int g = 0; g < o->ngroups; ++g) {
         int m0, n0;
         group_mn(g, m0, n0);
+        gt0[g] = (int)acct;
+        acct += (o->B - m0 + BK - 1) / BK;
         goff2[g] = acc2;
         acc2 += (long long)group_pairs(m0, n0).np * (o->B - m0);
         for (int nt = 0; nt < o->ntiles; ++nt)
@@ -804,6 +772,9 @@ int oz_create(OZState** out, const double* d_table, const std::vector<long long>
     for (size_t i = 0; i < items.size(); ++i)
         aux[i] = make_int2((int)goff2[items[i].x], (int)(goff[items[i].x] / N));
     o->nitems = (int)items.size();
+    o->nbt = acct;
+    if ((rc = oz_alloc(o, (void**)&o->gt0, sizeof(int) * gt0.size(), err))) return bail(rc);
+    cudaMemcpy(o->gt0, gt0.data(), sizeof(int) * gt0.size(), cudaMemcpyHostToDevice);
     if ((rc = oz_alloc(o, (void**)&o->goff2, sizeof(long long) * goff2.size(), err))) return bail(rc);
     if ((rc = oz_alloc(o, (void**)&o->items, sizeof(int4) * items.size(), err))) return bail(rc);
     if ((rc = oz_alloc(o, (void**)&o->iaux, sizeof(int2) * aux.size(), err))) return bail(rc);
@@ -814,6 +785,7 @@ int oz_create(OZState** out, const double* d_table, const std::vector<long long>
     const size_t grid = (size_t)N * N * N;
     if ((rc = oz_alloc(o, (void**)&o->Y, sizeof(float4) * (size_t)chunk * o->C, err))) return bail(rc);
     if ((rc = oz_alloc(o, (void**)&o->ey, (size_t)chunk * o->ngroups * 4, err))) return bail(rc);
+    if ((rc = oz_alloc(o, (void**)&o->bimg, (size_t)STAGE_B * o->ntiles * o->nbt, err))) return bail(rc);
     if ((rc = oz_alloc(o, (void**)&o->pen, sizeof(float4) * (size_t)pen_fns * grid, err))) return bail(rc);
     if ((rc = oz_alloc(o, (void**)&o->err, sizeof(int), err))) return bail(rc);
     cudaMemset(o->err, 0, sizeof(int));
@@ -871,6 +843,9 @@ static int oz_contract(OZState* o, const void* F, bool f64, int nb, float2* rhi,
             gather_kernel<float2><<<blocks, 256, 0, st>>>((const float2*)F, o->C, o->Y, o->ey, o->goff2, L, o->ngroups,
                                                           nb);
         OZK(cudaGetLastError());
+        digit_image_kernel<<<dim3((unsigned)o->ngroups, (unsigned)((nb + FPT - 1) / FPT)), 256, 0, st>>>(
+            o->Y, o->ey, o->goff2, o->gt0, o->bimg, o->nbt, o->C, L, o->ngroups, nb);
+        OZK(cudaGetLastError());
         if (!rhi) {
             const long long tot = (long long)nb * 2 * NN;
             zero_nyquist_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(pen, N, nb);
@@ -890,7 +865,9 @@ static int oz_contract(OZState* o, const void* F, bool f64, int nb, float2* rhi,
         a.ngroups = o->ngroups;
         a.fstride = NN * N;
         a.ystride = o->C;
-        a.Y = o->Y;
+        a.bimg = o->bimg;
+        a.gt0 = o->gt0;
+        a.nbt = o->nbt;
         a.ey = o->ey;
         a.et = o->et;
         a.pout = pen;
@@ -913,6 +890,13 @@ bool oz_spectral(const OZState* o) { return o && fft_df32_k_supported(o->N); }
 int oz_fft_functions(const OZState* o) { return o ? o->pen_fns : 0; }
 
 int oz_chunk(const OZState* o) { return o ? o->chunk : 0; }
+
+long long oz_image_bytes_per_column_tile(int L)
+{
+    long long t = 0;
+    for (int m0 = 0; m0 <= L; ++m0) t += (long long)(2 * m0 + 1) * ((L + 1 - m0 + BK - 1) / BK);
+    return t * STAGE_B;
+}
 
 int oz_forward_fft(OZState* o, const void* fgrid, bool real, int nb, float2* hi, float2* lo, cudaStream_t st,
                    StageTimer* T, std::string& err)

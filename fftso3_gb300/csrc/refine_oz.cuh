@@ -39,6 +39,8 @@ int oz_inverse_exact(OZState* o, const void* F, bool f64, int nb, void* grid, bo
                      void* ring = nullptr);
 // Functions per contraction chunk.
 int oz_chunk(const OZState* o);
+// Device bytes of the coefficients' digit image per column tile of 8 functions (the contraction's B operand).
+long long oz_image_bytes_per_column_tile(int L);
 
 // The spectral form of the residual step (N = 64..512): the forward's FFT in double-float and the residual in
 // the pencil domain, r^ = FFT(f) - N^2 H(F), which is what the forward GEMM consumes -- no FP32 FFT of f or of

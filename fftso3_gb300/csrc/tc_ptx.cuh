@@ -86,6 +86,16 @@ __device__ __forceinline__ void cluster_sync()
 }
 
 // L2 prefetch of the same box (no shared memory, no completion to wait for).
+// non-tensor bulk copy global -> shared memory, completing on an mbarrier (addresses 16-byte aligned, bytes a
+// multiple of 16)
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"((uint64_t)src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
 __device__ __forceinline__ void tma_prefetch_2d(const CUtensorMap* tm, int x, int y)
 {
     asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global.tile [%0, {%1, %2}];" ::"l"((uint64_t)tm), "r"(x), "r"(y)
