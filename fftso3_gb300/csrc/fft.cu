@@ -549,7 +549,7 @@ __device__ __forceinline__ void synth_rows_out(const qc32* sm, long long o, long
 }
 
 template <int N, int LOAD, int STORE>
-__global__ void __launch_bounds__(256, 3) fft_df32_k_kernel(dfc32* __restrict__ buf, long long S, long long oinner,
+__global__ void __launch_bounds__(256, 4) fft_df32_k_kernel(dfc32* __restrict__ buf, long long S, long long oinner,
                                                              long long oouter, long long oistride,
                                                              const double2* __restrict__ twg, const void* fin,
                                                              float2* __restrict__ hi, float2* __restrict__ lo)
