@@ -657,7 +657,7 @@ int fftso3_plan_create(fftso3_plan** out, int kind, int l_max, int batch, int pr
             // (pen_fns = up to 8 functions at a time), so its contraction chunks grow to 32 functions (four column
             // tiles sharing each table tile; the digit planes read once per 32 functions).
             const bool spectral = fft_df32_k_supported(N);
-            const size_t pen_fn = 16 * (size_t)p->grid_elems, run_fn = 16 * (size_t)p->coeff_elems;
+            const size_t pen_fn = 16 * (size_t)p->grid_elems;
             const size_t planes = 4 * 2 * (size_t)(p->table_elems / N) * (size_t)((N + 63) / 64 * 64);
             const size_t tab64 = sizeof(double) * (size_t)p->table_elems;
             size_t freeb = 0, totb = 0;
@@ -666,7 +666,7 @@ int fftso3_plan_create(fftso3_plan** out, int kind, int l_max, int batch, int pr
             const size_t img_tile = (size_t)oz_image_bytes_per_column_tile(L);
             auto need = [&](size_t nch) {
                 const size_t pens = spectral ? std::min<size_t>(nch, 8) : nch;
-                return planes + nch * run_fn + pens * pen_fn + (nch + 7) / 8 * img_tile;
+                return planes + pens * pen_fn + (nch + 7) / 8 * img_tile;
             };
             size_t nch = spectral ? 32 : 16;
             while (nch > 1 && (need(nch) + slack > freeb || freeb + tab64 < need(nch) + spare))

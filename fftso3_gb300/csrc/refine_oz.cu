@@ -92,7 +92,6 @@ struct Args {
     int nitems;
     int L, N, batch, ngroups;
     long long fstride;      // pencil elements per function (N^3)
-    long long ystride;      // coefficients per function (C)
     const unsigned char* bimg;  // the coefficients' digit image: [column tile][group tile gt0[g] + step] x STAGE_B
     const int* gt0;             // first tile of each group in the image
     long long nbt;              // tiles per column tile
@@ -436,62 +435,6 @@ __global__ void table_digits_kernel(const double* __restrict__ table, const long
 
 // ---- per-call kernels
 
-// One warp per (function, group): the group's coefficient runs (2l+1) sign F(l, pair), l = m0..L, as
-// double-float (group-major, as the tensor-core path's layout; for FP32 input the product is exact:
-// h = fl(c v), l = fma(c, v, -h)) and one exponent per pair with max |value| < 2^E.
-// GROUP: F is already group-major (the forward GEMM's output), read as runs; else packed.
-template <typename CIN, bool GROUP = false>
-__global__ void gather_kernel(const CIN* __restrict__ F, long long cstride, float4* __restrict__ Y,
-                              signed char* __restrict__ ey, const long long* __restrict__ goff2, int L, int ngroups,
-                              int nb)
-{
-    const long long w = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (w >= (long long)nb * ngroups) return;
-    const int lane = threadIdx.x & 31;
-    const int f = (int)(w / ngroups), g = (int)(w % ngroups);
-    int m0, n0;
-    group_mn(g, m0, n0);
-    const GroupPairs P = group_pairs(m0, n0);
-    const int nl = L + 1 - m0;
-    const CIN* Fb = F + (long long)f * cstride;
-    float4* Yb = Y + (long long)f * cstride + goff2[g];
-    for (int p = 0; p < 4; ++p) {
-        float mx = 0.f;
-        if (p < P.np) {
-            for (int li = lane; li < nl; li += 32) {
-                const int l = m0 + li;
-                const CIN v = GROUP ? Fb[goff2[g] + (long long)p * nl + li] : Fb[so3_idx(l, P.m[p], P.n[p])];
-                df32 re, im;
-                if constexpr (sizeof(v.x) == 8) {
-                    re = df32((double)(2 * l + 1) * (double)v.x);
-                    im = df32((double)(2 * l + 1) * (double)v.y);
-                } else {
-                    const float c = (float)(2 * l + 1);
-                    const float rh = c * (float)v.x, ih = c * (float)v.y;
-                    re = df32(rh, fmaf(c, (float)v.x, -rh));
-                    im = df32(ih, fmaf(c, (float)v.y, -ih));
-                }
-                if (P.sign[p] < 0) {
-                    re = -re;
-                    im = -im;
-                }
-                Yb[(long long)p * nl + li] = make_float4(re.h, re.l, im.h, im.l);
-                mx = fmaxf(mx, fmaxf(fabsf(re.h), fabsf(im.h)));
-            }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        if (lane == 0) {
-            int e = EXP_MIN;
-            if (mx > 0.f) {
-                frexpf(mx, &e);  // mx < 2^e; the low word adds at most half an ulp of mx
-                e = e < EXP_MIN ? EXP_MIN : (e > EXP_MAX ? EXP_MAX : e);
-            }
-            ey[((long long)f * ngroups + g) * 4 + p] = (signed char)e;
-        }
-    }
-}
-
 // the Nyquist pencils (p = B or q = B), which no (m, n) with |m|, |n| <= L maps to
 __global__ void zero_nyquist_kernel(float4* __restrict__ H, int N, long long nb)
 {
@@ -540,16 +483,44 @@ __global__ void __launch_bounds__(256) resid_kernel(const float4* __restrict__ g
     }
 }
 
+// The coefficient runs of the contraction: (2l+1) sign F(l, pair) for l = m0..L, as double-float (for FP32 input
+// the product is exact: h = fl(c v), l = fma(c, v, -h)).  F packed, or (GROUP) already group-major -- the forward
+// GEMM's output, runs at goff2[g] + pair nl + (l - m0).
+template <typename CIN, bool GROUP>
+__device__ __forceinline__ float4 run_value(const CIN* __restrict__ Fb, long long go, int l, int m0, int nl, int p,
+                                            int pm, int pn, int psign)
+{
+    const CIN v = GROUP ? Fb[go + (long long)p * nl + (l - m0)] : Fb[so3_idx(l, pm, pn)];
+    df32 re, im;
+    if constexpr (sizeof(v.x) == 8) {
+        re = df32((double)(2 * l + 1) * (double)v.x);
+        im = df32((double)(2 * l + 1) * (double)v.y);
+    } else {
+        const float c = (float)(2 * l + 1);
+        const float rh = c * (float)v.x, ih = c * (float)v.y;
+        re = df32(rh, fmaf(c, (float)v.x, -rh));
+        im = df32(ih, fmaf(c, (float)v.y, -ih));
+    }
+    if (psign < 0) {
+        re = -re;
+        im = -im;
+    }
+    return make_float4(re.h, re.l, im.h, im.l);
+}
+
 // The coefficients' digit image: for column tile z (functions 8z .. 8z + 7) and group g, the B operand of each
 // of the group's K steps (BK degrees) as the contraction's shared-memory stage expects it -- four BF16 digit
 // planes of 64 columns (function fl, pair pp, re / im: column 8 fl + 2 pp + {0, 1}) x BK degrees, K-major, each
 // column's 128-byte row with its 16-byte chunks swizzled (chunk q at q ^ (row & 7)) -- so that one bulk copy
 // fills a stage.  Degrees past the group's run, missing pairs and functions past nb are zero.  One CTA per
-// (group, column tile), thread = (column pair c, chunk q8), as the digits were formed in shared memory before.
-__global__ void __launch_bounds__(256) digit_image_kernel(const float4* __restrict__ Y, const signed char* __restrict__ ey,
+// (group, column tile), thread = (column pair c, chunk q8): a first sweep over the run finds the pair's exponent
+// E (max |value| < 2^E, written to ey), a second forms the digits of value 2^-E.
+template <typename CIN, bool GROUP>
+__global__ void __launch_bounds__(256) digit_image_kernel(const CIN* __restrict__ F, long long cstride,
+                                                          signed char* __restrict__ ey,
                                                           const long long* __restrict__ goff2,
                                                           const int* __restrict__ gt0, unsigned char* __restrict__ img,
-                                                          long long nbt, long long ystride, int L, int ngroups, int nb)
+                                                          long long nbt, int L, int ngroups, int nb)
 {
     const int g = blockIdx.x, z = blockIdx.y;
     int m0, n0;
@@ -559,8 +530,38 @@ __global__ void __launch_bounds__(256) digit_image_kernel(const float4* __restri
     const int fl = c >> 2, pp = c & 3, f = z * FPT + fl;
     const int lim = L + 1 - m0, nk = (lim + BK - 1) / BK;
     const bool valid = f < nb && pp < P.np;
-    const float4* src = valid ? Y + (long long)f * ystride + goff2[g] + (long long)pp * lim : nullptr;
-    const float sc = valid ? pow2f(-(int)ey[((long long)f * ngroups + g) * 4 + pp]) : 0.f;
+    const CIN* Fb = F + (long long)(valid ? f : 0) * cstride;
+    const long long go = goff2[g];
+    // the pair's (m, n) and sign, selected without a dynamic index into P (which would live in local memory)
+    int pm = P.m[0], pn = P.n[0], psign = P.sign[0];
+#pragma unroll
+    for (int q = 1; q < 4; ++q)
+        if (pp == q) {
+            pm = P.m[q];
+            pn = P.n[q];
+            psign = P.sign[q];
+        }
+    // exponent of the pair's run (the eight threads of a column pair are adjacent lanes)
+    float mx = 0.f;
+    if (valid)
+        for (int i = 0; i < nk; ++i)
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int li = i * BK + q8 * 8 + j;
+                if (li < lim) {
+                    const float4 y = run_value<CIN, GROUP>(Fb, go, m0 + li, m0, lim, pp, pm, pn, psign);
+                    mx = fmaxf(mx, fmaxf(fabsf(y.x), fabsf(y.z)));
+                }
+            }
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    int e = EXP_MIN;
+    if (mx > 0.f) {
+        frexpf(mx, &e);  // mx < 2^e; the low word adds at most half an ulp of mx
+        e = e < EXP_MIN ? EXP_MIN : (e > EXP_MAX ? EXP_MAX : e);
+    }
+    if (f < nb && q8 == 0) ey[((long long)f * ngroups + g) * 4 + pp] = (signed char)e;
+    const float sc = valid ? pow2f(-e) : 0.f;
     const int Rre = 2 * c, Rim = Rre + 1;
     const uint32_t ore = (uint32_t)Rre * 128u + (uint32_t)((q8 ^ (Rre & 7)) * 16);
     const uint32_t oim = (uint32_t)Rim * 128u + (uint32_t)((q8 ^ (Rim & 7)) * 16);
@@ -568,8 +569,9 @@ __global__ void __launch_bounds__(256) digit_image_kernel(const float4* __restri
         float4 v[8];
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-            const int l = i * BK + q8 * 8 + j;
-            v[j] = (valid && l < lim) ? __ldg(src + l) : make_float4(0.f, 0.f, 0.f, 0.f);
+            const int li = i * BK + q8 * 8 + j;
+            v[j] = (valid && li < lim) ? run_value<CIN, GROUP>(Fb, go, m0 + li, m0, lim, pp, pm, pn, psign)
+                                       : make_float4(0.f, 0.f, 0.f, 0.f);
         }
         uint32_t wre[NS][4], wim[NS][4];
 #pragma unroll
@@ -636,7 +638,6 @@ struct OZState {
     CUtensorMap tm[NS];
     signed char* et = nullptr;  // [group][k]
     signed char* ey = nullptr;  // [chunk][group][pair]
-    float4* Y = nullptr;        // [chunk][C] double-float group-major coefficients
     unsigned char* bimg = nullptr;  // [column tile][tile] x STAGE_B: their digit image (digit_image_kernel)
     int* gt0 = nullptr;             // first image tile of each group
     long long nbt = 0;              // image tiles per column tile
@@ -673,7 +674,7 @@ void oz_destroy(OZState* o)
     if (!o) return;
     for (int p = 0; p < NS; ++p)
         if (o->planes[p]) cudaFree(o->planes[p]);
-    void* ptrs[] = {o->et, o->ey, o->Y, o->bimg, o->gt0, o->pen, o->goff2, o->items, o->iaux, o->err};
+    void* ptrs[] = {o->et, o->ey, o->bimg, o->gt0, o->pen, o->goff2, o->items, o->iaux, o->err};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     for (cudaEvent_t e : {o->ev_ready[0], o->ev_ready[1], o->ev_free[0], o->ev_free[1], o->ev_join})
@@ -783,7 +784,6 @@ int oz_create(OZState** out, const double* d_table, const std::vector<long long>
     cudaMemcpy(o->iaux, aux.data(), sizeof(int2) * aux.size(), cudaMemcpyHostToDevice);
     // per-chunk buffers
     const size_t grid = (size_t)N * N * N;
-    if ((rc = oz_alloc(o, (void**)&o->Y, sizeof(float4) * (size_t)chunk * o->C, err))) return bail(rc);
     if ((rc = oz_alloc(o, (void**)&o->ey, (size_t)chunk * o->ngroups * 4, err))) return bail(rc);
     if ((rc = oz_alloc(o, (void**)&o->bimg, (size_t)STAGE_B * o->ntiles * o->nbt, err))) return bail(rc);
     if ((rc = oz_alloc(o, (void**)&o->pen, sizeof(float4) * (size_t)pen_fns * grid, err))) return bail(rc);
@@ -831,20 +831,16 @@ static int oz_contract(OZState* o, const void* F, bool f64, int nb, float2* rhi,
     const long long NN = (long long)N * N;
     T->begin(ST_REFINE, st);
     {
-        const long long warps = (long long)nb * o->ngroups;
-        const unsigned blocks = (unsigned)((warps + 7) / 8);
+        const dim3 grid((unsigned)o->ngroups, (unsigned)((nb + FPT - 1) / FPT));
         if (f64)
-            gather_kernel<double2><<<blocks, 256, 0, st>>>((const double2*)F, o->C, o->Y, o->ey, o->goff2, L,
-                                                           o->ngroups, nb);
+            digit_image_kernel<double2, false><<<grid, 256, 0, st>>>((const double2*)F, o->C, o->ey, o->goff2, o->gt0,
+                                                                     o->bimg, o->nbt, L, o->ngroups, nb);
         else if (group)
-            gather_kernel<float2, true><<<blocks, 256, 0, st>>>((const float2*)F, o->C, o->Y, o->ey, o->goff2, L,
-                                                                o->ngroups, nb);
+            digit_image_kernel<float2, true><<<grid, 256, 0, st>>>((const float2*)F, o->C, o->ey, o->goff2, o->gt0,
+                                                                   o->bimg, o->nbt, L, o->ngroups, nb);
         else
-            gather_kernel<float2><<<blocks, 256, 0, st>>>((const float2*)F, o->C, o->Y, o->ey, o->goff2, L, o->ngroups,
-                                                          nb);
-        OZK(cudaGetLastError());
-        digit_image_kernel<<<dim3((unsigned)o->ngroups, (unsigned)((nb + FPT - 1) / FPT)), 256, 0, st>>>(
-            o->Y, o->ey, o->goff2, o->gt0, o->bimg, o->nbt, o->C, L, o->ngroups, nb);
+            digit_image_kernel<float2, false><<<grid, 256, 0, st>>>((const float2*)F, o->C, o->ey, o->goff2, o->gt0,
+                                                                    o->bimg, o->nbt, L, o->ngroups, nb);
         OZK(cudaGetLastError());
         if (!rhi) {
             const long long tot = (long long)nb * 2 * NN;
@@ -864,7 +860,6 @@ static int oz_contract(OZState* o, const void* F, bool f64, int nb, float2* rhi,
         a.batch = nb;
         a.ngroups = o->ngroups;
         a.fstride = NN * N;
-        a.ystride = o->C;
         a.bimg = o->bimg;
         a.gt0 = o->gt0;
         a.nbt = o->nbt;
