@@ -924,9 +924,11 @@ __device__ __forceinline__ void ptile_index(PTileIdx& t, int L, int n, int l0, i
 // and reused, and two functions' tiles are in flight per iteration.
 constexpr int PFPC = 8;
 
+// Fg2 (optional): a second group-major array added to Fg on the way (the refinement's correction)
 __global__ void __launch_bounds__(256) group_to_packed_tiled(const float2* __restrict__ Fg, float2* __restrict__ F,
                                                              const long long* __restrict__ goff2, int L,
-                                                             long long cstride, int batch)
+                                                             long long cstride, int batch,
+                                                             const float2* __restrict__ Fg2 = nullptr)
 {
     __shared__ float2 tile[2][PT][PT + 1];  // [function & 1][m - mb][l - l0]
     __shared__ PTileIdx ix;
@@ -943,8 +945,18 @@ __global__ void __launch_bounds__(256) group_to_packed_tiled(const float2* __res
             const int mi = e / PT, li = e % PT, l = l0 + li;
             if (l < ix.gm0[mi] || l > L) continue;
             const long long o = ix.gbase[mi] + l;
-            tile[0][mi][li] = Fg[(long long)f * cstride + o];
-            if (nfn == 2) tile[1][mi][li] = Fg[(long long)(f + 1) * cstride + o];
+            float2 v0 = Fg[(long long)f * cstride + o], v1 = make_float2(0.f, 0.f);
+            if (nfn == 2) v1 = Fg[(long long)(f + 1) * cstride + o];
+            if (Fg2) {
+                const float2 d0 = Fg2[(long long)f * cstride + o];
+                v0 = make_float2(v0.x + d0.x, v0.y + d0.y);
+                if (nfn == 2) {
+                    const float2 d1 = Fg2[(long long)(f + 1) * cstride + o];
+                    v1 = make_float2(v1.x + d1.x, v1.y + d1.y);
+                }
+            }
+            tile[0][mi][li] = v0;
+            if (nfn == 2) tile[1][mi][li] = v1;
         }
         __syncthreads();
         // scatter: lanes run along m (contiguous in the packed layout)
@@ -1909,18 +1921,15 @@ int tc_refine_finish_group(TCState* s, void* coeffs, cudaStream_t st, StageTimer
         err = "internal: group-major refinement is for complex SO(3) refined plans";
         return FFTSO3_ERR_CUDA;
     }
-    // the correction's GEMM into d_coef2 (group-major), added to F0 in d_fg, then one permutation
+    // the correction's GEMM into d_coef2 (group-major), then one permutation that adds it to F0 (d_fg)
     T->begin(ST_GEMM_FWD, st);
     int rc = launch_gemm(s, true, st, err, s->d_coef2);
     if (rc) return rc;
     T->end(st);
-    const long long nc = (long long)s->batch * coeffs_per_fn(s);
-    T->begin(ST_REFINE, st);
-    TCK(launch_add_real((float*)s->d_fg, (const float*)s->d_coef2, 2 * nc, st));
-    T->end(st);
+    // F0 + the correction, added as the permutation reads them
     T->begin(ST_BASIS, st);
     group_to_packed_tiled<<<ptile_grid(s->L, s->batch), 256, 0, st>>>(s->d_fg, (float2*)coeffs, s->d_goff2, s->L,
-                                                                      coeffs_per_fn(s), s->batch);
+                                                                      coeffs_per_fn(s), s->batch, s->d_coef2);
     TCK(cudaGetLastError());
     T->end(st);
     return FFTSO3_SUCCESS;
