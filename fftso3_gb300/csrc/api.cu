@@ -858,15 +858,53 @@ int fftso3_forward_host(fftso3_plan* plan, const void* grid_host, void* coeffs_h
     return FFTSO3_SUCCESS;
 }
 
+// The exact inverse into host memory (SO(3), N = 64..512), pipelined in chunks of up to 8 functions (one column
+// tile of the exact contraction): each chunk's coefficients are copied in, contracted and transformed, and its
+// grids stream out through the device ring on the copy stream, so the copies out (the host link bounds the call)
+// start after the first chunk instead of after the whole batch.
+static int exact_inverse_host(fftso3_plan* p, const void* coeffs_host, void* grid_host, cudaStream_t st)
+{
+    StageTimer& T = p->timer;
+    const long long C = p->coeff_elems, G = p->grid_elems;
+    const int per = p->real ? 1 : 2;  // floats per element
+    const size_t fn_bytes = (size_t)G * per * sizeof(float), cf_bytes = (size_t)C * per * sizeof(float);
+    int rc = p->d_io_ring ? FFTSO3_SUCCESS : plan_alloc(p, &p->d_io_ring, 2 * (size_t)OZ_SYNTH_PIECE * fn_bytes);
+    if (rc) return rc;
+    void* pen = tc_exact_buffer(p->tc);
+    const int cf = std::min(p->rchunk, 8);
+    for (int f0 = 0; f0 < p->batch; f0 += cf) {
+        const int nb = p->batch - f0 < cf ? p->batch - f0 : cf;
+        float* cd = (float*)p->d_io_coeff + (long long)f0 * C * per;
+        CK(cudaMemcpyAsync(cd, (const char*)coeffs_host + (size_t)f0 * cf_bytes, (size_t)nb * cf_bytes,
+                           cudaMemcpyHostToDevice, st));
+        const void* Fc = cd;
+        if (p->real) {
+            T.begin(ST_BASIS, st);
+            CK(launch_widen(cd, (double*)p->d_rc, (long long)nb * C, st));
+            CK(launch_so3_r2c(p->d_rc, p->d_rfc, true, p->L, nb, st));
+            T.end(st);
+            Fc = p->d_rfc;
+        }
+        const bool last = f0 + nb >= p->batch;
+        if ((rc = oz_inverse_exact(p->oz, Fc, p->real, nb, nullptr, p->real, st, &T, g_err, pen,
+                                   (char*)grid_host + (size_t)f0 * fn_bytes, p->d_io_ring, last)))
+            return rc;
+    }
+    CK(cudaStreamSynchronize(st));
+    return FFTSO3_SUCCESS;
+}
+
 int fftso3_inverse_host(fftso3_plan* plan, const void* coeffs_host, void* grid_host, void* stream)
 {
     int rc = check_plan(plan);
     if (rc) return rc;
     if (!grid_host || !coeffs_host) return fail(FFTSO3_ERR_INVALID_ARG, "grid/coeffs pointer is NULL");
     cudaStream_t st = (cudaStream_t)stream;
-    // the coefficients always go to device memory in one copy (the inverse's first kernels gather them in an order
-    // that would cross the host link in small pieces)
+    // the coefficients always go to device memory in bulk copies (the inverse's first kernels gather them in an
+    // order that would cross the host link in small pieces)
     if ((rc = ensure_io_coeff(plan))) return rc;
+    if (plan->tc && (plan->flags & FFTSO3_FLAG_EXACT_INVERSE) && plan->oz && oz_spectral(plan->oz))
+        return exact_inverse_host(plan, coeffs_host, grid_host, st);
     CK(cudaMemcpyAsync(plan->d_io_coeff, coeffs_host, coeff_bytes(plan), cudaMemcpyHostToDevice, st));
     const void* cin = plan->d_io_coeff;
     if (plan->tc && (plan->flags & FFTSO3_FLAG_EXACT_INVERSE)) {

@@ -643,9 +643,13 @@ struct OZState {
     long long nbt = 0;              // image tiles per column tile
     float4* pen = nullptr;      // [chunk][N^3] double-float pencils / grid
     long long* goff2 = nullptr;
-    int4* items = nullptr;
+    int4* items = nullptr;      // work items of a full chunk (all column tiles)
     int2* iaux = nullptr;
     int nitems = 0;
+    // the same lists restricted to the first z column tiles (z = 1 .. ntiles - 1; order kept), for shorter chunks
+    std::vector<int4*> items_z;
+    std::vector<int2*> iaux_z;
+    std::vector<int> nitems_z;
     FFTFactors fac;
     const double* d_tw = nullptr;
     int* err = nullptr;
@@ -653,6 +657,7 @@ struct OZState {
     // exact inverse into host memory: the copy stream and its events (created on first use)
     cudaStream_t side = nullptr;
     cudaEvent_t ev_ready[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr}, ev_join = nullptr;
+    unsigned long long ring_seq = 0;  // pieces sent through the ring so far (its slot alternation)
 };
 
 bool oz_supported(int L, int N) { return L >= 0 && L <= 255 && N == 2 * (L + 1); }
@@ -676,6 +681,10 @@ void oz_destroy(OZState* o)
         if (o->planes[p]) cudaFree(o->planes[p]);
     void* ptrs[] = {o->et, o->ey, o->bimg, o->gt0, o->pen, o->goff2, o->items, o->iaux, o->err};
     for (void* q : ptrs)
+        if (q) cudaFree(q);
+    for (void* q : o->items_z)
+        if (q) cudaFree(q);
+    for (void* q : o->iaux_z)
         if (q) cudaFree(q);
     for (cudaEvent_t e : {o->ev_ready[0], o->ev_ready[1], o->ev_free[0], o->ev_free[1], o->ev_join})
         if (e) cudaEventDestroy(e);
@@ -782,6 +791,24 @@ int oz_create(OZState** out, const double* d_table, const std::vector<long long>
     cudaMemcpy(o->goff2, goff2.data(), sizeof(long long) * goff2.size(), cudaMemcpyHostToDevice);
     cudaMemcpy(o->items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice);
     cudaMemcpy(o->iaux, aux.data(), sizeof(int2) * aux.size(), cudaMemcpyHostToDevice);
+    for (int zt = 1; zt < o->ntiles; ++zt) {
+        std::vector<int4> iz;
+        std::vector<int2> az;
+        for (size_t i = 0; i < items.size(); ++i)
+            if (items[i].z < zt) {
+                iz.push_back(items[i]);
+                az.push_back(aux[i]);
+            }
+        int4* di = nullptr;
+        int2* da = nullptr;
+        if ((rc = oz_alloc(o, (void**)&di, sizeof(int4) * iz.size(), err))) return bail(rc);
+        o->items_z.push_back(di);
+        if ((rc = oz_alloc(o, (void**)&da, sizeof(int2) * az.size(), err))) return bail(rc);
+        o->iaux_z.push_back(da);
+        o->nitems_z.push_back((int)iz.size());
+        cudaMemcpy(di, iz.data(), sizeof(int4) * iz.size(), cudaMemcpyHostToDevice);
+        cudaMemcpy(da, az.data(), sizeof(int2) * az.size(), cudaMemcpyHostToDevice);
+    }
     // per-chunk buffers
     const size_t grid = (size_t)N * N * N;
     if ((rc = oz_alloc(o, (void**)&o->ey, (size_t)chunk * o->ngroups * 4, err))) return bail(rc);
@@ -852,9 +879,10 @@ static int oz_contract(OZState* o, const void* F, bool f64, int nb, float2* rhi,
     T->begin(stage, st);
     {
         Args a;
-        a.items = o->items;
-        a.iaux = o->iaux;
-        a.nitems = o->nitems;
+        const int zt = (nb + FPT - 1) / FPT;  // column tiles holding the chunk's functions
+        a.items = zt < o->ntiles ? o->items_z[zt - 1] : o->items;
+        a.iaux = zt < o->ntiles ? o->iaux_z[zt - 1] : o->iaux;
+        a.nitems = zt < o->ntiles ? o->nitems_z[zt - 1] : o->nitems;
         a.L = L;
         a.N = N;
         a.batch = nb;
@@ -885,6 +913,14 @@ bool oz_spectral(const OZState* o) { return o && fft_df32_k_supported(o->N); }
 int oz_fft_functions(const OZState* o) { return o ? o->pen_fns : 0; }
 
 int oz_chunk(const OZState* o) { return o ? o->chunk : 0; }
+
+int oz_host_join(OZState* o, cudaStream_t st)
+{
+    if (!o || !o->side) return FFTSO3_SUCCESS;
+    if (cudaEventRecord(o->ev_join, o->side) != cudaSuccess || cudaStreamWaitEvent(st, o->ev_join, 0) != cudaSuccess)
+        return FFTSO3_ERR_CUDA;
+    return FFTSO3_SUCCESS;
+}
 
 long long oz_image_bytes_per_column_tile(int L)
 {
@@ -974,7 +1010,7 @@ int oz_inverse_resid(OZState* o, const void* F, bool f64, int nb, const void* fg
 }
 
 int oz_inverse_exact(OZState* o, const void* F, bool f64, int nb, void* grid, bool real, cudaStream_t st,
-                     StageTimer* T, std::string& err, void* pen_buf, void* host, void* ring)
+                     StageTimer* T, std::string& err, void* pen_buf, void* host, void* ring, bool join)
 {
     float4* pen = pen_buf ? (float4*)pen_buf : o->pen;
     int rc = oz_contract(o, F, f64, nb, nullptr, nullptr, st, T, err, false, ST_INV_CONTRACT, pen);
@@ -995,12 +1031,13 @@ int oz_inverse_exact(OZState* o, const void* F, bool f64, int nb, void* grid, bo
             }
             OZK(cudaEventCreateWithFlags(&o->ev_join, cudaEventDisableTiming));
         }
-        for (int f0 = 0, i = 0; f0 < nb; f0 += OZ_SYNTH_PIECE, ++i) {
-            const int np = nb - f0 < OZ_SYNTH_PIECE ? nb - f0 : OZ_SYNTH_PIECE, sl = i & 1;
+        for (int f0 = 0; f0 < nb; f0 += OZ_SYNTH_PIECE) {
+            // the ring's slots alternate across calls; a slot's last copy (if any) must be done before it is rewritten
+            const int np = nb - f0 < OZ_SYNTH_PIECE ? nb - f0 : OZ_SYNTH_PIECE, sl = (int)(o->ring_seq++ & 1);
             float4* pb = pen + (long long)f0 * G;
             char* rb = (char*)ring + (size_t)sl * OZ_SYNTH_PIECE * gbytes;
             OZK(launch_fft_df32_k_synth_pass(1, pb, N, np, rb, real, o->d_tw, st));
-            if (i >= 2) OZK(cudaStreamWaitEvent(st, o->ev_free[sl], 0));
+            OZK(cudaStreamWaitEvent(st, o->ev_free[sl], 0));
             OZK(launch_fft_df32_k_synth_pass(2, pb, N, np, rb, real, o->d_tw, st));
             OZK(cudaEventRecord(o->ev_ready[sl], st));
             OZK(cudaStreamWaitEvent(o->side, o->ev_ready[sl], 0));
@@ -1008,8 +1045,10 @@ int oz_inverse_exact(OZState* o, const void* F, bool f64, int nb, void* grid, bo
                                 o->side));
             OZK(cudaEventRecord(o->ev_free[sl], o->side));
         }
-        OZK(cudaEventRecord(o->ev_join, o->side));
-        OZK(cudaStreamWaitEvent(st, o->ev_join, 0));
+        if (join) {
+            OZK(cudaEventRecord(o->ev_join, o->side));
+            OZK(cudaStreamWaitEvent(st, o->ev_join, 0));
+        }
     } else if (oz_spectral(o)) {
         OZK(launch_fft_df32_k_synth(pen, N, nb, grid, real, o->d_tw, st));
     } else {

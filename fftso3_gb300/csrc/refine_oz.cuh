@@ -34,9 +34,13 @@ int oz_inverse_resid(OZState* o, const void* F, bool f64, int nb, const void* fg
 // (the generic FFT) and ring a device buffer of 2 OZ_SYNTH_PIECE grids (N = 64..512), whose copies to the host
 // run under the FFT of the next pieces.
 constexpr int OZ_SYNTH_PIECE = 4;
+// join = false (host path): st does not wait for the last copies to the host (a later call's join, or the
+// caller's synchronisation of the copy stream through oz_host_join, covers them).
 int oz_inverse_exact(OZState* o, const void* F, bool f64, int nb, void* grid, bool real, cudaStream_t st,
                      StageTimer* T, std::string& err, void* pen = nullptr, void* host = nullptr,
-                     void* ring = nullptr);
+                     void* ring = nullptr, bool join = true);
+// st waits for every copy to the host issued so far.
+int oz_host_join(OZState* o, cudaStream_t st);
 // Functions per contraction chunk.
 int oz_chunk(const OZState* o);
 // Device bytes of the coefficients' digit image per column tile of 8 functions (the contraction's B operand).

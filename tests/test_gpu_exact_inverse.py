@@ -85,14 +85,21 @@ def test_exact_inverse_s2(gblib, oracle, kind):
         assert ok, (i, mx)
 
 
-def test_exact_inverse_host_call_equals_device_call(gblib, oracle):
+@pytest.mark.parametrize("kind,b", [("complex", 5), ("complex", 17), ("real", 17)])
+def test_exact_inverse_host_call_equals_device_call(gblib, oracle, kind, b):
+    """fftso3_inverse_host on an exact-inverse plan (l_max 31: chunks of 8 functions whose coefficients are copied
+    in and whose grids stream out through the two-slot device ring, across chunk boundaries) gives the device
+    call's grids bit for bit, into pageable and pinned host memory."""
     import torch
-    L, b = 31, 5
-    F = np.stack([so3_coeffs(L, seed=5300 + i, decay="pow") for i in range(b)]).astype(np.complex64)
-    p = gblib.Plan(gblib.SO3_COMPLEX, L, b, "tc_bf16x3", "stable", gblib.FLAG_EXACT_INVERSE | gblib.FLAG_REFINE)
+    L = 31
+    cplx = kind == "complex"
+    k = gblib.SO3_COMPLEX if cplx else gblib.SO3_REAL
+    F = np.stack([so3_coeffs(L, seed=5300 + i, complex_=cplx, decay="pow") for i in range(b)])
+    F = F.astype(np.complex64 if cplx else np.float32)
+    p = gblib.Plan(k, L, b, "tc_bf16x3", "stable", gblib.FLAG_EXACT_INVERSE | gblib.FLAG_REFINE)
     s = torch.cuda.current_stream().cuda_stream
     c = torch.from_numpy(F.ravel()).cuda()
-    g = torch.empty(b * p.grid_elems, dtype=torch.complex64, device="cuda")
+    g = torch.empty(b * p.grid_elems, dtype=torch.complex64 if cplx else torch.float32, device="cuda")
     p.inverse(c.data_ptr(), g.data_ptr(), s)
     p.check()
     want = g.cpu().numpy()
@@ -101,9 +108,11 @@ def test_exact_inverse_host_call_equals_device_call(gblib, oracle):
     p.inverse_host(host.ctypes.data, out.ctypes.data, s)  # pageable
     assert np.array_equal(out, want)
     pin = torch.from_numpy(host).pin_memory()
-    pout = torch.empty(want.size, dtype=torch.complex64).pin_memory()
-    p.inverse_host(pin.data_ptr(), pout.data_ptr(), s)  # pinned: the grid written in place, piece by piece
-    assert np.array_equal(pout.numpy(), want)
+    pout = torch.empty(want.size, dtype=g.dtype).pin_memory()
+    for _ in range(2):  # twice: the ring's slots continue from the previous call
+        pout.zero_()
+        p.inverse_host(pin.data_ptr(), pout.data_ptr(), s)
+        assert np.array_equal(pout.numpy(), want)
 
 
 def test_exact_inverse_is_more_accurate_than_the_plain_inverse(gblib, oracle):
