@@ -434,16 +434,22 @@ int exact_inverse(fftso3_plan* p, const void* coeffs, void* grid, cudaStream_t s
         }
         for (int f0 = 0; f0 < p->batch; f0 += fftn) {
             const int nb = p->batch - f0 < fftn ? p->batch - f0 : fftn;
-            const void* Fc = (const float2*)coeffs + (long long)f0 * C;
+            const void* Fc;
             if (p->real) {
                 STAGE(ST_BASIS, launch_widen((const float*)coeffs + (long long)f0 * C, (double*)p->d_rc,
                                              (long long)nb * C, st));
                 STAGE(ST_BASIS, launch_so3_r2c(p->d_rc, p->d_rfc, true, p->L, nb, st));
                 Fc = p->d_rfc;
+            } else {
+                // complex: permuted into group-major runs first, so the digit image reads contiguous runs
+                T.begin(ST_BASIS, st);
+                Fc = tc_group_from_packed(p->tc, coeffs, f0, nb, st);
+                T.end(st);
+                if (!Fc) return cuda_fail(cudaGetLastError(), "tc_group_from_packed");
             }
             const long long off = (long long)f0 * G * per;  // floats
             int rc = oz_inverse_exact(p->oz, Fc, p->real, nb, ring ? nullptr : (float*)grid + off, p->real, st, &T,
-                                      g_err, pen, host ? (float*)host + off : nullptr, ring);
+                                      g_err, pen, host ? (float*)host + off : nullptr, ring, true, !p->real);
             if (rc) return rc;
         }
         return FFTSO3_SUCCESS;
@@ -877,17 +883,20 @@ static int exact_inverse_host(fftso3_plan* p, const void* coeffs_host, void* gri
         float* cd = (float*)p->d_io_coeff + (long long)f0 * C * per;
         CK(cudaMemcpyAsync(cd, (const char*)coeffs_host + (size_t)f0 * cf_bytes, (size_t)nb * cf_bytes,
                            cudaMemcpyHostToDevice, st));
-        const void* Fc = cd;
+        const void* Fc;
+        T.begin(ST_BASIS, st);
         if (p->real) {
-            T.begin(ST_BASIS, st);
             CK(launch_widen(cd, (double*)p->d_rc, (long long)nb * C, st));
             CK(launch_so3_r2c(p->d_rc, p->d_rfc, true, p->L, nb, st));
-            T.end(st);
             Fc = p->d_rfc;
+        } else {
+            Fc = tc_group_from_packed(p->tc, p->d_io_coeff, f0, nb, st);
+            if (!Fc) return cuda_fail(cudaGetLastError(), "tc_group_from_packed");
         }
+        T.end(st);
         const bool last = f0 + nb >= p->batch;
         if ((rc = oz_inverse_exact(p->oz, Fc, p->real, nb, nullptr, p->real, st, &T, g_err, pen,
-                                   (char*)grid_host + (size_t)f0 * fn_bytes, p->d_io_ring, last)))
+                                   (char*)grid_host + (size_t)f0 * fn_bytes, p->d_io_ring, last, !p->real)))
             return rc;
     }
     CK(cudaStreamSynchronize(st));

@@ -974,9 +974,10 @@ __global__ void __launch_bounds__(256) group_to_packed_tiled(const float2* __res
 }
 
 // packed -> scaled group-major Y = (2l+1) sign F(l, pair)
+// raw: the values as they are (the exact contraction scales them itself), else (2l+1) sign F for the GEMM
 __global__ void __launch_bounds__(256) packed_to_group_tiled(const float2* __restrict__ F, float2* __restrict__ Y,
                                                              const long long* __restrict__ goff2, int L,
-                                                             long long cstride, int batch)
+                                                             long long cstride, int batch, bool raw = false)
 {
     __shared__ float2 tile[2][PT][PT + 1];  // [function & 1][m - mb][l - l0]
     __shared__ PTileIdx ix;
@@ -1001,7 +1002,7 @@ __global__ void __launch_bounds__(256) packed_to_group_tiled(const float2* __res
             const int e = threadIdx.x + u * 256;
             const int mi = e / PT, li = e % PT, l = l0 + li;
             if (l < ix.gm0[mi] || l > L) continue;
-            const float sc = (float)(2 * l + 1) * ix.gsign[mi];
+            const float sc = raw ? 1.f : (float)(2 * l + 1) * ix.gsign[mi];
             const long long o = ix.gbase[mi] + l;
             const float2 v0 = tile[0][mi][li];
             Y[(long long)f * cstride + o] = make_float2(sc * v0.x, sc * v0.y);
@@ -1884,6 +1885,15 @@ void* tc_resid_buffer(TCState* s) { return s ? (void*)s->d_resid : nullptr; }
 float2* tc_pencil_buffer(TCState* s) { return s ? s->d_pencil : nullptr; }
 
 void* tc_exact_buffer(TCState* s) { return s && s->d_resid ? (void*)s->d_pencil : nullptr; }
+
+const float2* tc_group_from_packed(TCState* s, const void* packed, int f0, int nb, cudaStream_t st)
+{
+    const long long C = coeffs_per_fn(s);
+    float2* out = s->d_fg + (long long)f0 * C;
+    packed_to_group_tiled<<<ptile_grid(s->L, nb), 256, 0, st>>>((const float2*)packed + (long long)f0 * C, out,
+                                                                 s->d_goff2, s->L, C, nb, true);
+    return cudaGetLastError() == cudaSuccess ? out : nullptr;
+}
 
 // forward from pencils already in d_pencil: GEMM, then the packed (and real-basis) coefficients
 static int forward_from_pencils(TCState* s, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err)

@@ -1010,10 +1010,15 @@ int oz_inverse_resid(OZState* o, const void* F, bool f64, int nb, const void* fg
 }
 
 int oz_inverse_exact(OZState* o, const void* F, bool f64, int nb, void* grid, bool real, cudaStream_t st,
-                     StageTimer* T, std::string& err, void* pen_buf, void* host, void* ring, bool join)
+                     StageTimer* T, std::string& err, void* pen_buf, void* host, void* ring, bool join,
+                     bool group_major)
 {
     float4* pen = pen_buf ? (float4*)pen_buf : o->pen;
-    int rc = oz_contract(o, F, f64, nb, nullptr, nullptr, st, T, err, false, ST_INV_CONTRACT, pen);
+    if (group_major && f64) {
+        err = "internal: group-major input of the exact inverse is complex64";
+        return FFTSO3_ERR_CUDA;
+    }
+    int rc = oz_contract(o, F, f64, nb, nullptr, nullptr, st, T, err, group_major, ST_INV_CONTRACT, pen);
     if (rc) return rc;
     const int N = o->N;
     const long long G = (long long)N * N * N;

@@ -35,10 +35,11 @@ int oz_inverse_resid(OZState* o, const void* F, bool f64, int nb, const void* fg
 // run under the FFT of the next pieces.
 constexpr int OZ_SYNTH_PIECE = 4;
 // join = false (host path): st does not wait for the last copies to the host (a later call's join, or the
-// caller's synchronisation of the copy stream through oz_host_join, covers them).
+// caller's synchronisation of the copy stream through oz_host_join, covers them).  group_major: F (complex64) is
+// in the tensor-core path's group-major order, unscaled (tc_group_from_packed), read as runs.
 int oz_inverse_exact(OZState* o, const void* F, bool f64, int nb, void* grid, bool real, cudaStream_t st,
                      StageTimer* T, std::string& err, void* pen = nullptr, void* host = nullptr,
-                     void* ring = nullptr, bool join = true);
+                     void* ring = nullptr, bool join = true, bool group_major = false);
 // st waits for every copy to the host issued so far.
 int oz_host_join(OZState* o, cudaStream_t st);
 // Functions per contraction chunk.

@@ -30,6 +30,10 @@ float2* tc_pencil_buffer(TCState* s);
 // Refinement plans: the pencil and residual buffers as one array of batch x (pencil places) 16-byte elements
 // (the exact inverse's double-float synthesis pencils); null otherwise.
 void* tc_exact_buffer(TCState* s);
+// Complex SO(3) plans: functions f0 .. f0 + nb - 1 of the packed complex64 coefficients, permuted unscaled into
+// the group-major buffer (the exact contraction's input order); returns their place there (null on a launch
+// error).
+const float2* tc_group_from_packed(TCState* s, const void* packed, int f0, int nb, cudaStream_t st);
 int tc_forward_pencils(TCState* s, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err);
 int tc_refine_add_pencils(TCState* s, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err);
 // Complex SO(3) refined plans, group-major form: F0 = the forward GEMM of the pencils, left group-major in the
