@@ -151,9 +151,13 @@ int fftso3_inverse(fftso3_plan* plan, const void* coeffs, void* grid, void* stre
 
 /* Host-buffer variants: transform host data and synchronise the stream
  * before returning (the reference's by-value call convention).  Host buffers
- * may be pageable or pinned: pageable buffers are staged through device
- * copies, pinned (page-locked) ones are read and written in place by the
- * kernels over the host link, without staging. */
+ * may be pageable or pinned (page-locked; faster).  The inverse copies the
+ * coefficients to the device in bulk; its grids are copied out (or, for plain
+ * plans and pinned buffers, written in place by the kernels over the host
+ * link).  Refined forwards copy the samples in pieces of a few functions under
+ * the FFT of the previous piece; exact inverses (SO(3), N = 64..512) run in
+ * chunks of 8 functions whose grids stream out through a small device ring
+ * on an internal copy stream while the next chunk is computed. */
 int fftso3_forward_host(fftso3_plan* plan, const void* grid_host, void* coeffs_host, void* stream);
 int fftso3_inverse_host(fftso3_plan* plan, const void* coeffs_host, void* grid_host, void* stream);
 
