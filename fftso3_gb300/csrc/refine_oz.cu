@@ -34,13 +34,16 @@
 // of H -- the FFT of the synthesised grid is N^2 H -- so neither g nor an
 // FFT of the residual is formed.
 //
+// The coefficients' digits are formed once per chunk (digit_image_kernel) as the shared-memory image of each
+// K step, so the kernel's B operand arrives by one bulk copy per stage.
 // Kernel layout (one CTA per SM, persistent over (group, 128 k, 8 functions) items):
-//   warp 0     TMA of the four table digit planes (MN-major operand, 128-byte swizzle);
+//   warp 0     TMA of the four table digit planes (MN-major operand, 128-byte swizzle) and bulk copy of the
+//              coefficients' 32 KB digit-image tile;
 //   warp 1     TMEM owner (512 columns: 2 buffers x 4 levels x 64) and MMA issuer:
 //              A_j x [B_0 .. B_{3-j}] as one MMA of N = (4 - j) 64 into levels j..3,
 //              so the 10 digit products take 4 instructions per 16 degrees;
-//   warps 2-9  coefficient producers: double-float Y -> four digit planes in shared memory;
-//   warps 10-13 epilogue: TMEM -> double-float H -> pencils [fn][p][q][k].
+//   warps 2-9  epilogue, two warps per TMEM lane quarter: TMEM -> double-float H -> pencils [fn][p][q][k]
+//              (or the spectral residual).
 // Every mbarrier wait is bounded (~1 s); on timeout the kernel records an error
 // code in the state's error word and unwinds, freeing its TMEM.
 #include <cuda.h>
@@ -227,7 +230,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                 const int nk = nsteps(item);
                 int m0, n0;
                 item_mn(item, m0, n0);
-                const int kvalid = a.L + 1 - m0;  // degrees; the producers zero the rest
+                const int kvalid = a.L + 1 - m0;  // degrees; the digit image is zero beyond
                 const int ab = t & 1;
                 if (t >= 2 && !mbar_wait(&acce[ab], ((t >> 1) - 1) & 1, a.err, 22)) {
                     *abort_flag = 1;
