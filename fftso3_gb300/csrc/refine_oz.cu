@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 
     if (warp == 0) {
         if (lane == 0) {
-            // ---------------- TMA producer of the table digit planes
+            // ---------------- TMA producer: the table digit planes and the coefficients' digit image
             const CUtensorMap* tm[NS] = {&t0, &t1, &t2, &t3};
             int kc = 0;
             for (int it = blockIdx.x; it < a.nitems && !*abort_flag; it += gridDim.x) {
