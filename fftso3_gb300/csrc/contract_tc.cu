@@ -101,6 +101,15 @@ __host__ __device__ constexpr uint32_t idesc_bf16(bool a_mn_major, int n = BN, i
 #define FFTSO3_MMA_N256 1
 #endif
 // hi + lo accumulator columns [c, c + 32): both loads in flight, one wait.
+__device__ __forceinline__ void tmem_ld32_one(uint32_t t, float* v)
+{
+    uint32_t a[32];
+    tmem_ld32_nowait(t, a);
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(a[i]);
+}
+
 __device__ __forceinline__ void tmem_ld32_sum(uint32_t thi, uint32_t tlo, float* v)
 {
     uint32_t a[32], b[32];
@@ -173,6 +182,21 @@ __device__ __forceinline__ void item_mn(const int4& it, int& m0, int& n0)
     n0 = (it.w & 0xFFFF) - 32768;
 }
 
+// One-term form: the BF16 rounding of 8 consecutive k values into row R of plane 0 only.
+__device__ __forceinline__ void store_chunk1(uint32_t bplanes, int R, int chunk, const float* x8)
+{
+    uint32_t w[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const __nv_bfloat162 v = __floats2bfloat162_rn(x8[2 * j], x8[2 * j + 1]);  // .x = low half
+        w[j] = *reinterpret_cast<const uint32_t*>(&v);
+    }
+    const uint32_t off = (uint32_t)R * 128u + (uint32_t)((chunk ^ (R & 7)) * 16);
+    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(bplanes + off), "r"(w[0]), "r"(w[1]), "r"(w[2]),
+                 "r"(w[3])
+                 : "memory");
+}
+
 // Store 8 consecutive k values (one 16-byte chunk) of row R of each BF16 plane.
 __device__ __forceinline__ void store_chunk(uint32_t bplanes, int R, int chunk, const float* x8)
 {
@@ -219,7 +243,9 @@ __device__ __forceinline__ GroupPairs s2_pairs(int m)
 // read once for all of them (each CTA issues its share of the tile's TMA boxes
 // with cluster multicast) and a stage is released when all C CTAs' MMAs are
 // done with it (multicast commits; empty barriers count C).
-template <bool FWD, bool S2, bool FUSED>
+// TERMS: BF16 terms per operand, 3 (split-BF16, six products) or 1 (one product: a refinement's correction,
+// whose input is small, needs no more)
+template <bool FWD, bool S2, bool FUSED, int TERMS = 3>
 __global__ void __launch_bounds__(THREADS, 1)
     so3_tc_gemm_kernel(const __grid_constant__ CUtensorMap tA0, const __grid_constant__ CUtensorMap tA1,
                        const __grid_constant__ CUtensorMap tA2, const __grid_constant__ GemmArgs args,
@@ -289,7 +315,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                     const int nk = nsteps(item, A);
                     if (i < nk) {
                         const long long row0 = args.iaux[it].y;
-                        for (int p = 0; p < 3; ++p) {
+                        for (int p = 0; p < TERMS; ++p) {
                             const CUtensorMap* tm = FUSED ? &segs[item.z >> 16].tm[p] : (p == 0 ? &tA0 : p == 1 ? &tA1 : &tA2);
                             if (FWD) {
                                 if (p % CL == (int)crank) tma_prefetch_2d(tm, i * BK, (int)(row0 + (long long)item.y * BM));
@@ -333,10 +359,11 @@ __global__ void __launch_bounds__(THREADS, 1)
                         break;
                     }
                     unsigned char* st = smem + s * STAGE_BYTES;
-                    mbar_expect_tx(&full[s], STAGE_A);  // the whole tile lands in every CTA of the cluster
+                    // the whole tile (its planes) lands in every CTA of the cluster
+                    mbar_expect_tx(&full[s], TERMS * PLANE_BYTES);
                     // the tile's boxes: plane p (forward), or plane p half h (inverse) = box j = 2 p + h;
                     // box j is issued by cluster rank j mod C
-                    for (int p = 0; p < 3; ++p) {
+                    for (int p = 0; p < TERMS; ++p) {
                         unsigned char* a = st + p * PLANE_BYTES;
                         if (FWD) {
                             if (p % CL != (int)crank) continue;
@@ -409,15 +436,15 @@ __global__ void __launch_bounds__(THREADS, 1)
                     for (int kk = 0; kk < BK / UK; ++kk) {
                         if (kk >= nkk) break;
 #pragma unroll
-                        for (int q = 0; q < 6; ++q) {
-                            if (FFTSO3_MMA_N256 && q == 1) continue;  // issued with q = 0
+                        for (int q = 0; q < (TERMS == 3 ? 6 : 1); ++q) {
+                            if (TERMS == 3 && FFTSO3_MMA_N256 && q == 1) continue;  // issued with q = 0
                             const uint32_t abase = st + pa[q] * PLANE_BYTES;
                             const uint32_t bbase = st + STAGE_A + pb[q] * PLANE_BYTES;
                             const uint64_t ad = FWD ? smem_desc(abase + kk * UK * 2, 16, 1024)
                                                     : smem_desc(abase + kk * UK * 128, PLANE_BYTES / 2, 1024);
                             const uint64_t bd = smem_desc(bbase + kk * UK * 2, 16, 1024);
                             const bool first = (i == 0) && kk == 0 && q <= 1;
-                            mma_bf16(q == 0 ? dhi : dlo, ad, bd, (FFTSO3_MMA_N256 && q == 0) ? id2 : id1,
+                            mma_bf16(q == 0 ? dhi : dlo, ad, bd, (TERMS == 3 && FFTSO3_MMA_N256 && q == 0) ? id2 : id1,
                                      first ? 0u : 1u);
                         }
                     }
@@ -561,8 +588,13 @@ __global__ void __launch_bounds__(THREADS, 1)
                     re[j] = v.x * wk;
                     im[j] = v.y * wk;
                 }
-                store_chunk(bpl, Rre, chunk, re);
-                store_chunk(bpl, Rim, chunk, im);
+                if constexpr (TERMS == 3) {
+                    store_chunk(bpl, Rre, chunk, re);
+                    store_chunk(bpl, Rim, chunk, im);
+                } else {
+                    store_chunk1(bpl, Rre, chunk, re);
+                    store_chunk1(bpl, Rim, chunk, im);
+                }
             }
             fence_proxy_async();
             __syncwarp();
@@ -623,7 +655,8 @@ __global__ void __launch_bounds__(THREADS, 1)
             const uint32_t trow = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(ab * 256);
             for (int chunk = 0; chunk < BN / 32; ++chunk) {
                 float v[32];
-                tmem_ld32_sum(trow + chunk * 32, trow + 128 + chunk * 32, v);
+                if constexpr (TERMS == 3) tmem_ld32_sum(trow + chunk * 32, trow + 128 + chunk * 32, v);
+                else tmem_ld32_one(trow + chunk * 32, v);
 #pragma unroll
                 for (int fq = 0; fq < 32 / (2 * PPF); ++fq) {
                     const int f = ctile(item) * FPTK + chunk * (32 / (2 * PPF)) + fq;
@@ -1172,7 +1205,8 @@ long long tc_device_bytes(const TCState* s) { return s ? s->bytes : 0; }
 
 static int autotune_fft(TCState* s, std::string& err);
 static int autotune_cluster(TCState* s, std::string& err);
-static int launch_gemm(TCState* s, bool fwd, cudaStream_t st, std::string& err, float2* cout = nullptr);
+static int launch_gemm(TCState* s, bool fwd, cudaStream_t st, std::string& err, float2* cout = nullptr,
+                       int terms = 3);
 static long long coeffs_per_fn(const TCState* s);
 static long long grid_per_fn(const TCState* s);
 
@@ -1404,12 +1438,13 @@ int tc_create(TCState** out, int L, int N, int batch, const double* d_table_fp64
         }
     }
     cudaError_t e = cudaSuccess;
-    const void* kernels[8] = {
+    const void* kernels[9] = {
         (const void*)so3_tc_gemm_kernel<true, false, false>, (const void*)so3_tc_gemm_kernel<false, false, false>,
         (const void*)so3_tc_gemm_kernel<true, true, false>,  (const void*)so3_tc_gemm_kernel<false, true, false>,
         (const void*)so3_tc_gemm_kernel<true, false, true>,  (const void*)so3_tc_gemm_kernel<false, false, true>,
-        (const void*)so3_tc_gemm_kernel<true, true, true>,   (const void*)so3_tc_gemm_kernel<false, true, true>};
-    for (int i = 0; i < 8 && e == cudaSuccess; ++i)
+        (const void*)so3_tc_gemm_kernel<true, true, true>,   (const void*)so3_tc_gemm_kernel<false, true, true>,
+        (const void*)so3_tc_gemm_kernel<true, false, false, 1>};
+    for (int i = 0; i < 9 && e == cudaSuccess; ++i)
         e = cudaFuncSetAttribute(kernels[i], cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     if (e != cudaSuccess) {
         err = std::string("tensor-core kernel attributes: ") + cudaGetErrorString(e);
@@ -1646,8 +1681,9 @@ static GemmArgs gemm_args(const TCState* s)
     return a;
 }
 
-// cout: the forward's group-major output (default: the plan's d_fg)
-static int launch_gemm(TCState* s, bool fwd, cudaStream_t st, std::string& err, float2* cout)
+// cout: the forward's group-major output (default: the plan's d_fg); terms: 1 selects the one-term kernel (SO(3)
+// forward only)
+static int launch_gemm(TCState* s, bool fwd, cudaStream_t st, std::string& err, float2* cout, int terms)
 {
     GemmArgs a = gemm_args(s);
     a.items = fwd ? s->d_items_fwd : s->d_items_inv;
@@ -1673,7 +1709,9 @@ static int launch_gemm(TCState* s, bool fwd, cudaStream_t st, std::string& err, 
         return FFTSO3_SUCCESS;
     }
     const CUtensorMap* tm = fwd ? s->tmA_fwd : s->tmA_inv;
-    auto kern = fwd ? (s->s2 ? so3_tc_gemm_kernel<true, true, false> : so3_tc_gemm_kernel<true, false, false>)
+    auto kern = fwd ? (s->s2 ? so3_tc_gemm_kernel<true, true, false>
+                             : (terms == 1 ? so3_tc_gemm_kernel<true, false, false, 1>
+                                           : so3_tc_gemm_kernel<true, false, false>))
                     : (s->s2 ? so3_tc_gemm_kernel<false, true, false> : so3_tc_gemm_kernel<false, false, false>);
     if (s->csize == 1) {
         const int nctas = a.nitems < s->nsm ? a.nitems : s->nsm;
@@ -1931,9 +1969,10 @@ int tc_refine_finish_group(TCState* s, void* coeffs, cudaStream_t st, StageTimer
         err = "internal: group-major refinement is for complex SO(3) refined plans";
         return FFTSO3_ERR_CUDA;
     }
-    // the correction's GEMM into d_coef2 (group-major), then one permutation that adds it to F0 (d_fg)
+    // the correction's GEMM into d_coef2 (group-major), then one permutation that adds it to F0 (d_fg).  One BF16
+    // term: the residual is ~5e-7 of the samples' spectrum, so the term's 2^-9 relative rounding leaves ~1e-9.
     T->begin(ST_GEMM_FWD, st);
-    int rc = launch_gemm(s, true, st, err, s->d_coef2);
+    int rc = launch_gemm(s, true, st, err, s->d_coef2, 1);
     if (rc) return rc;
     T->end(st);
     // F0 + the correction, added as the permutation reads them
