@@ -1933,11 +1933,13 @@ const float2* tc_group_from_packed(TCState* s, const void* packed, int f0, int n
     return cudaGetLastError() == cudaSuccess ? out : nullptr;
 }
 
-// forward from pencils already in d_pencil: GEMM, then the packed (and real-basis) coefficients
-static int forward_from_pencils(TCState* s, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err)
+// forward from pencils already in d_pencil: GEMM (terms: see launch_gemm), then the packed (and real-basis)
+// coefficients
+static int forward_from_pencils(TCState* s, void* coeffs, cudaStream_t st, StageTimer* T, std::string& err,
+                                int terms = 3)
 {
     T->begin(ST_GEMM_FWD, st);
-    int rc = launch_gemm(s, true, st, err);
+    int rc = launch_gemm(s, true, st, err, nullptr, terms);
     if (rc) return rc;
     T->end(st);
     return tc_forward_finish(s, coeffs, st, T, err);
@@ -1990,12 +1992,13 @@ int tc_refine_add_pencils(TCState* s, void* coeffs, cudaStream_t st, StageTimer*
         err = "internal: refinement buffers were not allocated";
         return FFTSO3_ERR_CUDA;
     }
-    // the correction in the coefficients' own element type: complex in d_coef2, real kinds in d_fc
+    // the correction in the coefficients' own element type: complex in d_coef2, real kinds in d_fc; its GEMM with
+    // one BF16 term (the residual is small: see tc_refine_finish_group)
     void* corr = s->real ? (void*)s->d_fc : (void*)s->d_coef2;
     if (s->real) {
         // tc_forward_finish writes the complex coefficients into d_fc first; route them through d_coef2
         T->begin(ST_GEMM_FWD, st);
-        int rc = launch_gemm(s, true, st, err);
+        int rc = launch_gemm(s, true, st, err, nullptr, 1);
         if (rc) return rc;
         T->end(st);
         T->begin(ST_BASIS, st);
@@ -2005,7 +2008,7 @@ int tc_refine_add_pencils(TCState* s, void* coeffs, cudaStream_t st, StageTimer*
         TCK(launch_so3_c2r(s->d_coef2, s->d_fc, false, s->L, s->batch, st));
         T->end(st);
     } else {
-        int rc = forward_from_pencils(s, s->d_coef2, st, T, err);
+        int rc = forward_from_pencils(s, s->d_coef2, st, T, err, 1);
         if (rc) return rc;
     }
     const long long nc = (long long)s->batch * coeffs_per_fn(s);
