@@ -1156,12 +1156,11 @@ def so3_tc_line(args, L: int, b: int, full: bool = True) -> dict:
     # ---- end to end through the host-buffer C ABI (pinned host memory), the same plan and step count
     e2e = None
     if full and not args.no_e2e:
-        # page-locked host buffers backed by huge pages (the library's host_empty): link-speed copies every call
-        hg = fg.host_empty(b * N ** 3, torch.complex64)
+        hg = torch.empty(b * N ** 3, dtype=torch.complex64, pin_memory=True)
         hg.copy_(grid)
-        hc = fg.host_empty(b * C, torch.complex64)
+        hc = torch.empty(b * C, dtype=torch.complex64, pin_memory=True)
         hc.copy_(coef)
-        hco = fg.host_empty(b * C, torch.complex64)
+        hco = torch.empty_like(hc, pin_memory=True)
         # the inverse writes the grid the forward then reads (one pinned grid buffer)
         plan.inverse_host(hc.data_ptr(), hg.data_ptr(), sp)
         plan.forward_host(hg.data_ptr(), hco.data_ptr(), sp)
@@ -1173,8 +1172,7 @@ def so3_tc_line(args, L: int, b: int, full: bool = True) -> dict:
         torch.cuda.synchronize()
         dt = (time.perf_counter() - t0) / args.steps
         e2e = {"value": b / dt, "unit": UNIT, "h2d_bytes_per_step": int(8 * b * C + 8 * b * N ** 3),
-               "d2h_bytes_per_step": int(8 * b * N ** 3 + 8 * b * C), "steps": args.steps,
-               "host_buffers": "page-locked, huge-page backed (fftso3_gb300.host_empty)"}
+               "d2h_bytes_per_step": int(8 * b * N ** 3 + 8 * b * C), "steps": args.steps}
         del hg, hc, hco
     plan.close()
     del plan

@@ -11,11 +11,10 @@ from .rotation import R_to_euler323, euler323_to_R, expm_SO3, hat
 from .transforms import FFTS2_complex, FFTS2_real, FFTSO3_complex, FFTSO3_real, alpha_j, beta_k, correlate_s2
 from ._lib import Batch, FFTSO3Error, Plan
 from .clebsch_gordan import Clebsch_Gordon_complex, Clebsch_Gordon_real
-from .hostmem import host_empty
 
 __all__ = [
     "FFTSO3_complex", "FFTSO3_real", "FFTS2_complex", "FFTS2_real",
     "FFTSO3_matrix_complex", "FFTSO3_matrix_real", "FFTS2_matrix_complex", "FFTS2_matrix_real",
     "so3_index", "so3_ncoeff", "so3_offset", "s2_index", "s2_ncoeff",
-    "R_to_euler323", "euler323_to_R", "expm_SO3", "hat", "alpha_j", "beta_k", "correlate_s2", "FFTSO3Error", "Plan", "Batch", "Clebsch_Gordon_complex", "Clebsch_Gordon_real", "host_empty",
+    "R_to_euler323", "euler323_to_R", "expm_SO3", "hat", "alpha_j", "beta_k", "correlate_s2", "FFTSO3Error", "Plan", "Batch", "Clebsch_Gordon_complex", "Clebsch_Gordon_real",
 ]

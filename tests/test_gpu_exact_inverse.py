@@ -134,30 +134,3 @@ def test_exact_inverse_is_more_accurate_than_the_plain_inverse(gblib, oracle):
     e_exact = np.abs(ge[0] - ref).max() / rms
     assert e_exact <= 2.0 ** -23 * np.abs(ref).max() / rms
     assert e_exact < e_plain
-
-
-def test_host_empty_buffers_in_host_calls(gblib, oracle):
-    """fftso3_gb300.host_empty: page-locked, 2 MB-aligned host tensors; the host-buffer calls on them give the
-    device calls' results bit for bit."""
-    import torch
-    import fftso3_gb300 as fg
-    L, b = 31, 5
-    F = np.stack([so3_coeffs(L, seed=5500 + i, decay="pow") for i in range(b)]).astype(np.complex64)
-    p = gblib.Plan(gblib.SO3_COMPLEX, L, b, "tc_bf16x3", "stable", gblib.FLAG_EXACT_INVERSE | gblib.FLAG_REFINE)
-    s = torch.cuda.current_stream().cuda_stream
-    c = torch.from_numpy(F.ravel()).cuda()
-    g = torch.empty(b * p.grid_elems, dtype=torch.complex64, device="cuda")
-    co = torch.empty_like(c)
-    p.inverse(c.data_ptr(), g.data_ptr(), s)
-    p.forward(g.data_ptr(), co.data_ptr(), s)
-    p.check()
-    hc = fg.host_empty(c.numel(), torch.complex64)
-    hg = fg.host_empty(g.numel(), torch.complex64)
-    hco = fg.host_empty(c.numel(), torch.complex64)
-    assert hg.is_pinned() and hg.data_ptr() % (2 << 20) == 0
-    hc.copy_(torch.from_numpy(F.ravel()))
-    p.inverse_host(hc.data_ptr(), hg.data_ptr(), s)
-    assert torch.equal(hg, g.cpu())
-    p.forward_host(hg.data_ptr(), hco.data_ptr(), s)
-    assert torch.equal(hco, co.cpu())
-    del hc, hg, hco  # registrations undone by the finalizers
